@@ -1,0 +1,191 @@
+/*
+ * seqan_gb300.h -- C-ABI of the GB300 batch pairwise-alignment engine.
+ *
+ * This is the drop-in boundary for SeqAn 2's batch alignment interface.  Every entry point
+ * takes plain pointers and sizes; residues are the reference alphabets' ordValue codes
+ * (Dna/Dna5: A=0 C=1 G=2 T=3 N=4; AminoAcid: the 27-letter order A B C D E F G H I J K L M
+ * N O P Q R S T U V W Y Z X *).  One call aligns a whole batch on one GPU.
+ *
+ * Reference interfaces each entry point replaces (paths relative to the SeqAn 2 tree):
+ *   gba_align_batch with GBA_OUT_SCORE, mode GBA_GLOBAL:
+ *       globalAlignmentScore(ExecutionPolicy<Parallel,Vectorial>, StringSet, StringSet,
+ *       Score, AlignConfig[, lower, upper])
+ *       align_parallel/parallel_align_interface.h:330-340 -> align/global_alignment_unbanded.h:739-821,
+ *       banded align/global_alignment_banded.h:558-652
+ *   ... mode GBA_LOCAL: localAlignmentScore(...) parallel_align_interface.h:357-365 ->
+ *       align/local_alignment_unbanded.h:554-572, banded align/local_alignment_banded.h:252
+ *   ... with GBA_OUT_SEGMENTS: globalAlignment / localAlignment over StringSet<Gaps>
+ *       parallel_align_interface.h:288-321 -> align/global_alignment_unbanded.h:831-888,
+ *       align/global_alignment_banded.h:658-700, align/local_alignment_unbanded.h:367-399;
+ *       segments are the reference's TraceSegment_ list (align/dp_trace_segment.h:60-100)
+ *       that _adaptTraceSegmentsTo turns into Gaps (align/dp_traceback_adaptor.h:57-117).
+ *   ... with GBA_OUT_CIGAR: getCigarString(cigar, gapsH, gapsV) bam_io/cigar.h:261-339.
+ *   gba_batch.h_shared = 1: the one-vs-many overload (String vs StringSet)
+ *       align/global_alignment_unbanded.h:766-821.
+ *
+ * Errors are status codes; nothing throws and nothing falls back to the CPU.
+ */
+#ifndef SEQAN_GB300_H_
+#define SEQAN_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBA_API __attribute__((visibility("default")))
+#else
+#define GBA_API
+#endif
+
+/* Status codes returned by every entry point. */
+enum {
+    GBA_OK = 0,
+    GBA_EINVAL = 1,        /* malformed arguments */
+    GBA_ENOMEM = 2,        /* device or pinned allocation failed */
+    GBA_EBUDGET = 3,       /* request exceeds the context's HBM budget */
+    GBA_ECUDA = 4,         /* a CUDA call failed; see gba_last_error */
+    GBA_ETIMEOUT = 5,      /* a bounded device wait or a host watchdog expired */
+    GBA_EUNSUPPORTED = 6,  /* parameter combination not supported */
+    GBA_ECAPACITY = 7      /* an output buffer supplied by the caller is too small */
+};
+
+/* Per-pair status flags (gba_result.pair_status). */
+enum {
+    GBA_PAIR_OK = 0,
+    GBA_PAIR_INVALID = 1,   /* empty sequence or band outside the matrix: score = numeric min */
+    GBA_PAIR_PROMOTED = 2   /* 16-bit cells were requested but the pair may leave the exact
+                               int16 range; it ran with 32-bit cells (exact result) */
+};
+
+enum { GBA_GLOBAL = 0, GBA_LOCAL = 1 };
+/* GBA_GAPS_AUTO picks affine iff gap_open != gap_extend, as the reference's
+ * interfaces do (align/global_alignment_unbanded.h:801-810). */
+enum { GBA_GAPS_AUTO = 0, GBA_GAPS_LINEAR = 1, GBA_GAPS_AFFINE = 2 };
+/* AlignConfig<TOP, LEFT, RIGHT, BOTTOM> (align/align_config.h:52-94). */
+enum { GBA_FREE_TOP = 1, GBA_FREE_LEFT = 2, GBA_FREE_RIGHT = 4, GBA_FREE_BOTTOM = 8 };
+/* Output selection bits. */
+enum { GBA_OUT_SCORE = 1, GBA_OUT_END = 2, GBA_OUT_SEGMENTS = 4, GBA_OUT_CIGAR = 8 };
+/* TraceSegment_ direction values (align/dp_profile.h:121-135). */
+enum { GBA_SEG_DIAGONAL = 1, GBA_SEG_HORIZONTAL = 2, GBA_SEG_VERTICAL = 4 };
+
+typedef struct gba_context gba_context;
+
+typedef struct {
+    int32_t device;            /* CUDA device ordinal */
+    int64_t hbm_budget_bytes;  /* 0 = no budget; otherwise batches needing more fail with GBA_EBUDGET */
+} gba_config;
+
+typedef struct {
+    int32_t mode;              /* GBA_GLOBAL / GBA_LOCAL */
+    int32_t gap_model;         /* GBA_GAPS_* */
+    int32_t free_ends;         /* GBA_FREE_* bits (global only; local treats all four as free) */
+    int32_t band_on;           /* 1: DPBandConfig<BandOn>(band_lower, band_upper) */
+    int32_t band_lower, band_upper;  /* diagonals, col - row convention (align/dp_band.h:111-161) */
+    int32_t match, mismatch;   /* Score<T, Simple> (score/score_simple.h:54-98) */
+    int32_t gap_open, gap_extend;  /* a gap of length k costs gap_open + (k-1) * gap_extend */
+    const int32_t *matrix;     /* optional alphabet_size^2 substitution table (row = H code),
+                                  e.g. the 27x27 Blosum62 of score/score_matrix_data.h */
+    int32_t alphabet_size;     /* codes must be < alphabet_size (<= 32) when matrix != NULL */
+    int32_t score_bits;        /* 16 or 32: the reference's TScoreValue width */
+    int32_t outputs;           /* GBA_OUT_* bits */
+    int32_t reserved[3];
+} gba_params;
+
+/* A batch: concatenated residue codes with n+1 offsets for each side. */
+typedef struct {
+    int64_t num_pairs;
+    const uint8_t *seq_h;
+    const int64_t *off_h;      /* num_pairs + 1 entries (2 when h_shared) */
+    const uint8_t *seq_v;
+    const int64_t *off_v;      /* num_pairs + 1 entries */
+    int32_t h_shared;          /* 1: every pair uses the single H sequence off_h[0]..off_h[1] */
+    int32_t reserved;
+} gba_batch;
+
+typedef struct {
+    uint32_t h_begin, v_begin, length, type;   /* TraceSegment_<unsigned, unsigned> */
+} gba_segment;
+
+/* Results.  Any pointer may be NULL when its output was not requested. */
+typedef struct {
+    int32_t *score;            /* [num_pairs] */
+    int32_t *end_h, *end_v;    /* [num_pairs] best cell (column, row) */
+    int32_t *begin_h, *begin_v;/* [num_pairs] alignment begin (GBA_OUT_SEGMENTS) */
+    int32_t *pair_status;      /* [num_pairs] GBA_PAIR_* */
+    /* Trace segments in the reference's order (traceback order, last segment = alignment
+     * begin).  Pair k owns segments[segment_offsets[k] .. segment_offsets[k+1]). */
+    gba_segment *segments;
+    int64_t segment_capacity;
+    int64_t *segment_offsets;  /* [num_pairs + 1] */
+    /* CIGAR as BAM-style uint32 (length << 4 | op), op index into "MIDNSHP=X"; the
+     * character string of getCigarString (bam_io/cigar.h:261-339), D runs >= 20 as N. */
+    uint32_t *cigar;
+    int64_t cigar_capacity;
+    int64_t *cigar_offsets;    /* [num_pairs + 1] */
+} gba_result;
+
+/* Context: device, stream, cached device buffers, HBM budget. */
+GBA_API int gba_create(gba_context **ctx, const gba_config *cfg);
+GBA_API int gba_destroy(gba_context *ctx);
+GBA_API const char *gba_status_string(int status);
+/* Copies the last error message of this context (CUDA error text etc.). */
+GBA_API int gba_last_error(gba_context *ctx, char *buf, size_t size);
+
+/* Aligns a batch held in HOST memory and writes host results; blocks until done.
+ * This is the call the reference-facing shim makes. */
+GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gba_batch *batch,
+                            gba_result *result);
+
+/* --- Device-resident path (inputs already in HBM) ------------------------------------ */
+
+typedef struct gba_plan gba_plan;
+
+/* Builds a launch plan from HOST offsets (lengths, binning, scratch sizes) and uploads it.
+ * The plan stays valid for any device batch with the same offsets. */
+GBA_API int gba_plan_create(gba_context *ctx, const gba_params *params, const gba_batch *host_batch,
+                            gba_plan **plan);
+GBA_API int gba_plan_destroy(gba_context *ctx, gba_plan *plan);
+/* Runs a plan on DEVICE inputs/outputs (pointers in dev_batch / dev_result are device
+ * pointers; segment/cigar outputs are written into the plan's device buffers and can be
+ * fetched with gba_plan_fetch).  Asynchronous on the context stream. */
+GBA_API int gba_plan_execute(gba_context *ctx, gba_plan *plan, const gba_batch *dev_batch,
+                             gba_result *dev_result);
+/* Copies a plan's segment/CIGAR outputs to host buffers (synchronous). */
+GBA_API int gba_plan_fetch(gba_context *ctx, gba_plan *plan, gba_result *host_result);
+
+/* --- Memory, stream and timing helpers (so hosts need no other CUDA binding) ---------- */
+GBA_API int gba_device_alloc(gba_context *ctx, void **ptr, size_t bytes);
+GBA_API int gba_device_free(gba_context *ctx, void *ptr);
+GBA_API int gba_host_alloc(gba_context *ctx, void **ptr, size_t bytes);   /* pinned */
+GBA_API int gba_host_free(gba_context *ctx, void *ptr);
+GBA_API int gba_copy_to_device(gba_context *ctx, void *dst, const void *src, size_t bytes);
+GBA_API int gba_copy_to_host(gba_context *ctx, void *dst, const void *src, size_t bytes);
+GBA_API int gba_synchronize(gba_context *ctx);
+/* CUDA events on the context stream: time between the two marks in milliseconds. */
+GBA_API int gba_timer_start(gba_context *ctx);
+GBA_API int gba_timer_stop(gba_context *ctx, float *ms);
+
+/* Statistics of the last batch: kernel time (CUDA events around the DP launch on the
+ * context stream), launches, cells. */
+typedef struct {
+    float dp_kernel_ms;        /* DP kernel(s) */
+    float traceback_kernel_ms; /* traceback + output kernels */
+    int32_t kernel_launches;   /* kernels this library launched for the batch */
+    int64_t cells;             /* algorithmic cells: sum m*n (in-band cells when banded) */
+    int64_t trace_bytes;       /* trace matrix bytes written */
+} gba_stats;
+GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
+
+/* Measures the device's 32-bit integer add/max rate (tera-ops per second) with a short
+ * kernel.  No counterpart in the reference: it is the roofline denominator that the
+ * benchmark reports the DP kernels against. */
+GBA_API int gba_measure_int_peak(gba_context *ctx, double *tops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

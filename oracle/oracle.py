@@ -1,0 +1,328 @@
+"""Test-only loaders for the oracle (C restatement) and the compiled reference.
+
+This module is TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg import it.  The engine (seqan_gb300/) never does.
+
+* ``liboracle``  -- oracle/seqan_oracle.c, the CPU restatement of SeqAn 2's DP, built with gcc
+  into oracle/_build/.  Builds on any host (x86 here, aarch64 on the GPU machine).
+* ``libseqan_ref`` -- SeqAn 2 itself, compiled from the reference's headers by
+  oracle/ref/Makefile into oracle/_ref/.  Only available where the reference tree exists; used
+  to pin the restatement and to generate tests/golden fixtures.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_LIB = os.path.join(HERE, "_ref", "libseqan_ref.so")
+ORACLE_LIB = os.path.join(BUILD, "libseqan_oracle.so")
+
+FREE_TOP, FREE_LEFT, FREE_RIGHT, FREE_BOTTOM = 1, 2, 4, 8
+SEG_DIAGONAL, SEG_HORIZONTAL, SEG_VERTICAL = 1, 2, 4
+
+
+class OrcParams(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("gap_model", C.c_int32), ("free_ends", C.c_int32),
+                ("band_on", C.c_int32), ("band_lower", C.c_int32), ("band_upper", C.c_int32),
+                ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
+                ("gap_extend", C.c_int32), ("matrix", C.POINTER(C.c_int32)),
+                ("alphabet_size", C.c_int32), ("score_bits", C.c_int32), ("traceback", C.c_int32)]
+
+
+class OrcResult(C.Structure):
+    _fields_ = [("score", C.c_int32), ("end_h", C.c_int32), ("end_v", C.c_int32),
+                ("begin_h", C.c_int32), ("begin_v", C.c_int32), ("n_segments", C.c_int32),
+                ("valid", C.c_int32)]
+
+
+class RefParams(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("free_ends", C.c_int32), ("band_on", C.c_int32),
+                ("band_lower", C.c_int32), ("band_upper", C.c_int32), ("match", C.c_int32),
+                ("mismatch", C.c_int32), ("gap_open", C.c_int32), ("gap_extend", C.c_int32),
+                ("alphabet", C.c_int32), ("blosum62", C.c_int32), ("score_bits", C.c_int32),
+                ("threads", C.c_int32)]
+
+
+class RefGapsOut(C.Structure):
+    _fields_ = [("score", C.c_int32), ("h_clip_begin", C.c_int32), ("h_clip_end", C.c_int32),
+                ("v_clip_begin", C.c_int32), ("v_clip_end", C.c_int32)]
+
+
+@dataclass
+class Problem:
+    """One alignment configuration, in the reference's terms."""
+    mode: str = "global"            # "global" | "local"
+    free_ends: int = 0              # AlignConfig<TOP,LEFT,RIGHT,BOTTOM> as FREE_* bits
+    band: tuple | None = None       # (lower, upper) or None
+    match: int = 2
+    mismatch: int = -3
+    gap_open: int = -5
+    gap_extend: int = -5
+    matrix: np.ndarray | None = None   # alphabet^2 int32 (row = H code)
+    score_bits: int = 32
+    alphabet: str = "dna"           # "dna" (Dna5 codes) | "aa" (AminoAcid codes)
+
+    @property
+    def affine(self) -> bool:
+        # The reference picks Gotoh iff open != extend (align/global_alignment_unbanded.h:801-810).
+        return self.gap_open != self.gap_extend
+
+
+def _compile_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "seqan_oracle.c")
+    if force or not os.path.exists(ORACLE_LIB) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = ORACLE_LIB + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-o", tmp, src])
+        os.replace(tmp, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+_orc = None
+_ref = None
+
+
+def liboracle():
+    global _orc
+    if _orc is None:
+        _orc = C.CDLL(_compile_oracle())
+        _orc.orc_align_batch.argtypes = [C.POINTER(OrcParams), C.c_int64, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_int32]
+        _orc.orc_align_batch.restype = C.c_int
+    return _orc
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def libref():
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(REF_LIB)
+        _ref.ref_batch_score.argtypes = [C.POINTER(RefParams), C.c_int64, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+        _ref.ref_batch_gaps.argtypes = [C.POINTER(RefParams), C.c_int64, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_int64]
+        _ref.ref_pair_segments.argtypes = [C.POINTER(RefParams), C.c_void_p, C.c_int32, C.c_void_p,
+                                           C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+        _ref.ref_has_shape.argtypes = [C.c_int32, C.POINTER(RefParams)]
+        _ref.ref_blosum62.argtypes = [C.c_void_p]
+        _ref.ref_encode.argtypes = [C.c_int32, C.c_char_p, C.c_int64, C.c_void_p]
+    return _ref
+
+
+def concat(seqs):
+    """List of uint8 arrays -> (codes, offsets[int64, n+1])."""
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    off = np.zeros(len(seqs) + 1, dtype=np.int64)
+    np.cumsum(lens, out=off[1:])
+    codes = np.concatenate([np.asarray(s, dtype=np.uint8) for s in seqs]) if len(seqs) and off[-1] else \
+        np.zeros(1, dtype=np.uint8)
+    return np.ascontiguousarray(codes), off
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _orc_params(pb: Problem, traceback: bool) -> OrcParams:
+    p = OrcParams()
+    p.mode = 1 if pb.mode == "local" else 0
+    p.gap_model = 1 if pb.affine else 0
+    p.free_ends = pb.free_ends
+    p.band_on = 1 if pb.band is not None else 0
+    p.band_lower, p.band_upper = (pb.band if pb.band is not None else (0, 0))
+    p.match, p.mismatch, p.gap_open, p.gap_extend = pb.match, pb.mismatch, pb.gap_open, pb.gap_extend
+    if pb.matrix is not None:
+        mat = np.ascontiguousarray(pb.matrix, dtype=np.int32)
+        p._mat_keepalive = mat
+        p.matrix = mat.ctypes.data_as(C.POINTER(C.c_int32))
+        p.alphabet_size = int(round(np.sqrt(mat.size)))
+    p.score_bits = pb.score_bits
+    p.traceback = 1 if traceback else 0
+    return p
+
+
+@dataclass
+class BatchResult:
+    score: np.ndarray
+    end_h: np.ndarray
+    end_v: np.ndarray
+    begin_h: np.ndarray | None = None
+    begin_v: np.ndarray | None = None
+    valid: np.ndarray | None = None
+    segments: list = field(default_factory=list)   # per pair: list of (h, v, len, type)
+
+
+def oracle_batch(pb: Problem, H, V, traceback: bool = False, threads: int = 0) -> BatchResult:
+    """Runs the C restatement on pairs (H[k], V[k])."""
+    lib = liboracle()
+    n = len(H)
+    sh, oh = concat(H)
+    sv, ov = concat(V)
+    params = _orc_params(pb, traceback)
+    out = (OrcResult * max(n, 1))()
+    segs = seg_off = None
+    if traceback:
+        caps = (oh[1:] - oh[:-1]) + (ov[1:] - ov[:-1]) + 4
+        seg_off = np.zeros(n + 1, dtype=np.int64)
+        np.cumsum(caps, out=seg_off[1:])
+        segs = np.zeros((int(seg_off[-1]) + 1, 4), dtype=np.uint32)
+    rc = lib.orc_align_batch(C.byref(params), n, _ptr(sh), _ptr(oh), _ptr(sv), _ptr(ov),
+                             C.cast(out, C.c_void_p), _ptr(segs), _ptr(seg_off), threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle returned {rc}")
+    arr = np.frombuffer(out, dtype=np.int32).reshape(-1, 7)[:n]
+    res = BatchResult(score=arr[:, 0].copy(), end_h=arr[:, 1].copy(), end_v=arr[:, 2].copy(),
+                      begin_h=arr[:, 3].copy(), begin_v=arr[:, 4].copy(), valid=arr[:, 6].copy())
+    if traceback:
+        for k in range(n):
+            cnt = arr[k, 5]
+            res.segments.append([tuple(int(x) for x in segs[seg_off[k] + i]) for i in range(max(cnt, 0))])
+    return res
+
+
+def _ref_params(pb: Problem, threads: int) -> RefParams:
+    p = RefParams()
+    p.mode = 1 if pb.mode == "local" else 0
+    p.free_ends = pb.free_ends
+    p.band_on = 1 if pb.band is not None else 0
+    p.band_lower, p.band_upper = (pb.band if pb.band is not None else (0, 0))
+    p.match, p.mismatch, p.gap_open, p.gap_extend = pb.match, pb.mismatch, pb.gap_open, pb.gap_extend
+    p.alphabet = 0 if pb.alphabet == "dna" else 1
+    p.blosum62 = 1 if pb.matrix is not None else 0
+    p.score_bits = pb.score_bits
+    p.threads = threads
+    return p
+
+
+def ref_has_shape(kind: int, pb: Problem) -> bool:
+    p = _ref_params(pb, 1)
+    return bool(libref().ref_has_shape(kind, C.byref(p)))
+
+
+def ref_batch_score(pb: Problem, H, V, threads: int = 1) -> np.ndarray:
+    lib = libref()
+    n = len(H)
+    sh, oh = concat(H)
+    sv, ov = concat(V)
+    out = np.zeros(max(n, 1), dtype=np.int32)
+    p = _ref_params(pb, threads)
+    rc = lib.ref_batch_score(C.byref(p), n, _ptr(sh), _ptr(oh), _ptr(sv), _ptr(ov), _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"reference call shape not instantiated (rc={rc}): {pb}")
+    return out[:n]
+
+
+def ref_batch_gaps(pb: Problem, H, V, threads: int = 1, cigar: bool = False):
+    """Returns (scores, clip[n,4] = hb,he,vb,ve, rows[list of (rowH, rowV)], cigars)."""
+    lib = libref()
+    n = len(H)
+    sh, oh = concat(H)
+    sv, ov = concat(V)
+    out = (RefGapsOut * max(n, 1))()
+    caps = 2 * ((oh[1:] - oh[:-1]) + (ov[1:] - ov[:-1])) + 4
+    row_off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(caps, out=row_off[1:])
+    rows = np.zeros(int(row_off[-1]) + 1, dtype=np.uint8)
+    cstride = int(caps.max() if n else 4) * 4 + 16
+    cig = np.zeros(n * cstride + 1, dtype=np.uint8) if cigar else None
+    p = _ref_params(pb, threads)
+    rc = lib.ref_batch_gaps(C.byref(p), n, _ptr(sh), _ptr(oh), _ptr(sv), _ptr(ov),
+                            C.cast(out, C.c_void_p), _ptr(rows), _ptr(row_off), _ptr(cig), cstride)
+    if rc != 0:
+        raise RuntimeError(f"reference call shape not instantiated (rc={rc}): {pb}")
+    arr = np.frombuffer(out, dtype=np.int32).reshape(-1, 5)[:n]
+    row_strs = []
+    for k in range(n):
+        raw = bytes(rows[row_off[k]:row_off[k + 1]]).split(b"\0", 1)[0].decode()
+        a, b = raw.split("\n")
+        row_strs.append((a, b))
+    cigars = None
+    if cigar:
+        cigars = [bytes(cig[k * cstride:(k + 1) * cstride]).split(b"\0", 1)[0].decode() for k in range(n)]
+    return arr[:, 0].copy(), arr[:, 1:5].copy(), row_strs, cigars
+
+
+def ref_pair_segments(pb: Problem, h, v):
+    lib = libref()
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    cap = len(h) + len(v) + 8
+    segs = np.zeros((cap, 4), dtype=np.uint32)
+    score = C.c_int32(0)
+    nseg = C.c_int32(0)
+    p = _ref_params(pb, 1)
+    rc = lib.ref_pair_segments(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), C.byref(score),
+                               _ptr(segs), cap, C.byref(nseg))
+    if rc != 0:
+        raise RuntimeError(f"reference call shape not instantiated (rc={rc}): {pb}")
+    return score.value, [tuple(int(x) for x in segs[i]) for i in range(nseg.value)]
+
+
+def ref_blosum62() -> np.ndarray:
+    out = np.zeros(27 * 27, dtype=np.int32)
+    libref().ref_blosum62(_ptr(out))
+    return out.reshape(27, 27)
+
+
+def ref_encode(alphabet: str, text: str) -> np.ndarray:
+    b = text.encode()
+    out = np.zeros(max(len(b), 1), dtype=np.uint8)
+    code = {"dna5": 0, "aa": 1, "dna": 2}[alphabet]
+    libref().ref_encode(code, b, len(b), _ptr(out))
+    return out[:len(b)]
+
+
+# ---------------------------------------------------------------------------------------------
+# Rendering helpers shared by the tests (segments -> gapped rows / CIGAR), following
+# _adaptTraceSegmentsTo (align/dp_traceback_adaptor.h:57-117) and getCigarString
+# (bam_io/cigar.h:261-339).
+# ---------------------------------------------------------------------------------------------
+
+def render_rows(segments, h_text: str, v_text: str):
+    """Gapped rows of the clipped alignment view, as operator<< on Gaps prints them."""
+    if not segments:
+        return "", ""
+    hb, vb = segments[-1][0], segments[-1][1]
+    rh, rv = [], []
+    ch, cv = hb, vb
+    for (_, _, ln, tp) in reversed(segments):
+        if tp == SEG_DIAGONAL:
+            rh.append(h_text[ch:ch + ln]); rv.append(v_text[cv:cv + ln]); ch += ln; cv += ln
+        elif tp == SEG_VERTICAL:
+            rh.append("-" * ln); rv.append(v_text[cv:cv + ln]); cv += ln
+        else:
+            rh.append(h_text[ch:ch + ln]); rv.append("-" * ln); ch += ln
+    return "".join(rh), "".join(rv)
+
+
+def segments_clip(segments):
+    """(h_begin, h_end, v_begin, v_end) as clippedBegin/EndPosition report them after
+    _adaptTraceSegmentsTo: the end is set to begin + the alignment's view length
+    (align/dp_traceback_adaptor.h:114-115), for both rows."""
+    if not segments:
+        return (0, 0, 0, 0)
+    hb, vb = segments[-1][0], segments[-1][1]
+    view = sum(s[2] for s in segments)
+    return (hb, hb + view, vb, vb + view)
+
+
+def cigar_string(segments) -> str:
+    ops = []
+    for (_, _, ln, tp) in reversed(segments):
+        op = "M" if tp == SEG_DIAGONAL else ("I" if tp == SEG_VERTICAL else "D")
+        if ops and ops[-1][0] == op:
+            ops[-1][1] += ln
+        else:
+            ops.append([op, ln])
+    return "".join(f"{n}{'N' if (o == 'D' and n >= 20) else o}" for o, n in ops)

@@ -1,0 +1,5 @@
+// Instantiation unit: a few reference call shapes, built in parallel (see ref_common.h).
+#include "../ref_common.h"
+
+SEQAN_REF_UNIT(k2_m0_b0_dna32_fe11, 2, run_segments, 0, 0, 1, 11, true, true, false, true, int32_t, Dna5, false)
+SEQAN_REF_UNIT(k2_m0_b0_dna32_fe12, 2, run_segments, 0, 0, 1, 12, false, false, true, true, int32_t, Dna5, false)

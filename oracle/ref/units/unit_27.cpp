@@ -1,0 +1,5 @@
+// Instantiation unit: a few reference call shapes, built in parallel (see ref_common.h).
+#include "../ref_common.h"
+
+SEQAN_REF_UNIT(k2_m0_b1_dna32_fe15, 2, run_segments, 0, 1, 1, 15, true, true, true, true, int32_t, Dna5, false)
+SEQAN_REF_UNIT(k2_m0_b1_dna32_fe6, 2, run_segments, 0, 1, 1, 6, false, true, true, false, int32_t, Dna5, false)

@@ -1,0 +1,430 @@
+/*
+ * seqan_oracle.c -- CPU restatement of SeqAn 2's pairwise DP.
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the checker the GPU engine is compared against and
+ * the CPU baseline timed beside it.  Nothing in seqan_gb300/ links or calls it.
+ *
+ * What is restated, with the reference lines each part follows (paths are relative to
+ * the SeqAn 2 source tree):
+ *   - column-major DP with one sparse score column and per-column diagonal/vertical
+ *     caches: align/dp_algorithm_impl.h:334-429 (_computeTrack) and :483-579
+ *     (unbanded _computeAlignmentImpl); banded columns :586-967.
+ *   - affine recurrences per recursion direction: align/dp_formula_affine.h:66-330;
+ *     linear: align/dp_formula_linear.h:62-258; Zero/Diagonal: align/dp_formula.h:249-309.
+ *   - tie rule of _maxScore with SingleTrace (left operand wins ties):
+ *     align/dp_formula.h:171-182.
+ *   - which cell uses which direction and which cells are tracked:
+ *     align/dp_meta_info.h:178-370.
+ *   - "infinity" = lowest()/2 of the cell type: align/dp_cell.h:126-146.
+ *   - best-cell scout with strict '>': align/dp_scout.h:166-180.
+ *   - start-cell trace correction: align/dp_algorithm_impl.h:1188-1205.
+ *   - traceback walk, initial direction and head/tail segments:
+ *     align/dp_traceback_impl.h:190-546; segment recording align/dp_trace_segment.h:318-337.
+ *   - invalid settings return numeric_limits<T>::min(): align/dp_algorithm_impl.h:183-256,
+ *     :1399-1400.
+ * With score_bits == 16 every sum is wrapped to int16, as the reference's int16 SIMD lanes
+ * do (simd/simd_base_seqan_impl_avx2.h add_epi16 semantics).
+ */
+#include "seqan_oracle.h"
+
+#include <limits.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+#define TV_NONE 0
+#define TV_DIAG 1
+#define TV_H 2
+#define TV_V 4
+#define TV_HO 8
+#define TV_VO 16
+#define TV_MFH 32
+#define TV_MFV 64
+
+enum { DIR_ZERO, DIR_ALL, DIR_HORIZONTAL, DIR_VERTICAL, DIR_UPPER, DIR_LOWER };
+
+typedef struct {
+    int bits16;
+    int inf;
+    int local;
+    int affine;
+    int ext, open;
+    int match, mismatch;
+    const int32_t *mat;
+    int asz;
+} ctx_t;
+
+static inline int wr(const ctx_t *c, long x)
+{
+    return c->bits16 ? (int)(int16_t)(uint16_t)(x & 0xffff) : (int)x;
+}
+
+static inline int sub_score(const ctx_t *c, uint8_t hv, uint8_t vv)
+{
+    if (c->mat) return c->mat[(int)hv * c->asz + (int)vv];
+    return hv == vv ? c->match : c->mismatch;
+}
+
+/* _maxScore with SingleTrace: the left operand wins ties (align/dp_formula.h:171-182). */
+#define MAXTL(target, tv, left, right, tl, tr) \
+    do { if ((left) < (right)) { (target) = (right); (tv) = (tr); } \
+         else { (target) = (left); (tv) = (tl); } } while (0)
+
+/* Per-column caches and the one sparse column (align/dp_matrix.h:137-147). */
+typedef struct {
+    int dS;          /* cacheDiag._score */
+    int vS, vF;      /* cacheVert._score, cacheVert._verticalScore */
+} caches_t;
+
+/* Computes one cell in place.  colS/colE hold the previous column's S/E at row i on entry
+ * (the sparse matrix cell) and this column's on exit.  Returns the trace value. */
+static inline int compute_cell(const ctx_t *c, int dir, int *colS, int *colE, caches_t *k,
+                               uint8_t hv, uint8_t vv, int *fOut)
+{
+    int tv = TV_NONE, t2, s, e, f;
+    int hS = *colS, hE = *colE;   /* previous horizontal cell (same row, previous column) */
+
+    switch (dir) {
+    case DIR_ZERO:
+        /* align/dp_formula.h:295-309: score 0; E of the cell and F of cacheVert stay. */
+        s = 0;
+        *colS = 0;
+        k->dS = 0;
+        k->vS = 0;
+        *fOut = k->vF;
+        return TV_NONE;
+    case DIR_ALL:
+        if (c->affine) {
+            int inter = wr(c, (long)k->dS + sub_score(c, hv, vv));
+            k->dS = hS;
+            MAXTL(e, tv, wr(c, (long)hE + c->ext), wr(c, (long)hS + c->open), TV_H, TV_HO);
+            MAXTL(f, t2, wr(c, (long)k->vF + c->ext), wr(c, (long)k->vS + c->open), TV_V, TV_VO);
+            tv |= t2;
+            {
+                int tmp2;
+                MAXTL(s, tmp2, f, e, TV_MFV, TV_MFH);
+                MAXTL(s, tv, inter, s, TV_DIAG | tv, tmp2 | tv);
+            }
+            k->vF = f;
+        } else {
+            int inter = wr(c, (long)k->dS + sub_score(c, hv, vv));
+            k->dS = hS;
+            MAXTL(s, tv, wr(c, (long)k->vS + c->ext), wr(c, (long)hS + c->ext),
+                  TV_V | TV_MFV, TV_H | TV_MFH);
+            MAXTL(s, tv, inter, s, TV_DIAG, tv);
+            e = hE;
+        }
+        break;
+    case DIR_HORIZONTAL:
+        if (c->affine) {
+            k->dS = hS;
+            MAXTL(e, tv, wr(c, (long)hE + c->ext), wr(c, (long)hS + c->open), TV_H, TV_HO);
+            tv |= TV_MFH;
+            k->vF = c->inf;
+            s = e;
+        } else {
+            k->dS = hS;
+            s = wr(c, (long)hS + c->ext);
+            tv = TV_H | TV_MFH;
+            e = hE;
+        }
+        break;
+    case DIR_VERTICAL:
+        if (c->affine) {
+            MAXTL(f, tv, wr(c, (long)k->vF + c->ext), wr(c, (long)k->vS + c->open), TV_V, TV_VO);
+            tv |= TV_MFV;
+            k->vF = f;
+            e = c->inf;
+            s = f;
+        } else {
+            s = wr(c, (long)k->vS + c->ext);
+            tv = TV_V | TV_MFV;
+            e = hE;
+        }
+        break;
+    case DIR_UPPER:
+        if (c->affine) {
+            int inter = wr(c, (long)k->dS + sub_score(c, hv, vv));
+            k->dS = hS;
+            MAXTL(e, tv, wr(c, (long)hE + c->ext), wr(c, (long)hS + c->open), TV_H, TV_HO);
+            k->vF = c->inf;
+            MAXTL(s, tv, inter, e, tv | TV_DIAG, tv | TV_MFH);
+        } else {
+            int inter = wr(c, (long)k->dS + sub_score(c, hv, vv));
+            k->dS = hS;
+            MAXTL(s, tv, inter, wr(c, (long)hS + c->ext), TV_DIAG, TV_H | TV_MFH);
+            e = hE;
+        }
+        break;
+    default: /* DIR_LOWER */
+        if (c->affine) {
+            MAXTL(f, tv, wr(c, (long)k->vF + c->ext), wr(c, (long)k->vS + c->open), TV_V, TV_VO);
+            k->vF = f;
+            e = c->inf;
+            MAXTL(s, tv, wr(c, (long)k->dS + sub_score(c, hv, vv)), f, tv | TV_DIAG, tv | TV_MFV);
+        } else {
+            MAXTL(s, tv, wr(c, (long)k->dS + sub_score(c, hv, vv)), wr(c, (long)k->vS + c->ext),
+                  TV_DIAG, TV_V | TV_MFV);
+            e = hE;
+        }
+        break;
+    }
+    if (c->local) {
+        /* align/dp_formula_affine.h:113-122: max(0, S) with 0 winning ties. */
+        int t3;
+        MAXTL(s, t3, 0, s, TV_NONE, tv);
+        tv = t3;
+    }
+    *colS = s;
+    *colE = e;
+    /* cacheVert follows the current cell, except in LowerDiagonal, which leaves it
+     * (align/dp_formula_affine.h:196-238, dp_formula_linear.h:154-186). */
+    if (dir != DIR_LOWER) k->vS = s;
+    *fOut = k->vF;
+    return tv;
+}
+
+typedef struct {
+    int s, e, f;
+    int col, row;
+} best_t;
+
+static inline void scout(best_t *b, int s, int e, int f, int col, int row)
+{
+    if (s > b->s) { b->s = s; b->e = e; b->f = f; b->col = col; b->row = row; }
+}
+
+/* ---------------------------------------------------------------------------------
+ * Traceback (align/dp_traceback_impl.h:190-546).
+ * ------------------------------------------------------------------------------- */
+
+typedef struct {
+    orc_segment *segs;
+    int cap, n, overflow;
+} segbuf_t;
+
+static void record(segbuf_t *sb, int hb, int vb, int len, int tv)
+{
+    int type;
+    if (len == 0) return;
+    if (tv & TV_DIAG) type = ORC_SEG_DIAGONAL;
+    else if (tv & TV_V) type = ORC_SEG_VERTICAL;
+    else if (tv & TV_H) type = ORC_SEG_HORIZONTAL;
+    else return;
+    if (sb->n >= sb->cap) { sb->overflow = 1; return; }
+    sb->segs[sb->n].h_begin = (uint32_t)hb;
+    sb->segs[sb->n].v_begin = (uint32_t)vb;
+    sb->segs[sb->n].length = (uint32_t)len;
+    sb->segs[sb->n].type = (uint32_t)type;
+    sb->n++;
+}
+
+/* Banded traceback bookkeeping of TracebackCoordinator_ (align/dp_traceback_impl.h:57-171)
+ * is not needed here because the trace matrix is stored dense in (column, row). */
+static void traceback(const ctx_t *c, const uint8_t *T, int n, int m, int col, int row,
+                      segbuf_t *sb, int global)
+{
+#define TAT(cc, rr) T[(size_t)(cc) * (size_t)(n + 1) + (size_t)(rr)]
+    int tv = TAT(col, row);
+    int last;
+    int frag = 0;
+
+    /* _retrieveInitialTraceDirection (:456-483); PreferGapsAtEnd_ is true for affine. */
+    if (c->affine) {
+        if (tv & TV_MFV) { tv &= (TV_V | TV_VO | TV_MFV); last = TV_V; }
+        else if (tv & TV_MFH) { tv &= (TV_H | TV_HO | TV_MFH); last = TV_H; }
+        else last = TV_DIAG;
+    } else {
+        if (tv & TV_DIAG) last = TV_DIAG;
+        else if (tv & (TV_V | TV_MFV)) last = TV_V;
+        else if (tv & (TV_H | TV_MFH)) last = TV_H;
+        else last = TV_NONE;
+    }
+
+    if (global) { /* TraceTail_ (:522-530) */
+        if (row != n) record(sb, m, row, n - row, TV_V);
+        if (col != m) record(sb, col, row, m - col, TV_H);
+    }
+
+    while (!(col <= 0 || row <= 0) && tv != TV_NONE) {
+        if (tv & TV_DIAG) {
+            if (!(last & TV_DIAG)) { record(sb, col, row, frag, last); last = TV_DIAG; frag = 0; }
+            --col; --row; tv = TAT(col, row); ++frag;
+        } else if ((tv & TV_MFV) && (tv & TV_V)) {
+            if (!(last & TV_V)) { record(sb, col, row, frag, last); last = TV_V; frag = 0; }
+            if (c->affine) {
+                while ((!(tv & TV_VO) || (tv & TV_V)) && row != 1) {
+                    --row; tv = TAT(col, row); ++frag;
+                }
+            }
+            --row; tv = TAT(col, row); ++frag;
+        } else if ((tv & TV_MFV) && (tv & TV_VO)) {
+            if (!(last & TV_V)) { record(sb, col, row, frag, last); last = TV_V; frag = 0; }
+            --row; tv = TAT(col, row); ++frag;
+        } else if ((tv & TV_MFH) && (tv & TV_H)) {
+            if (!(last & TV_H)) { record(sb, col, row, frag, last); last = TV_H; frag = 0; }
+            if (c->affine) {
+                while ((!(tv & TV_HO) || (tv & TV_H)) && col != 1) {
+                    --col; tv = TAT(col, row); ++frag;
+                }
+            }
+            --col; tv = TAT(col, row); ++frag;
+        } else if ((tv & TV_MFH) && (tv & TV_HO)) {
+            if (!(last & TV_H)) { record(sb, col, row, frag, last); last = TV_H; frag = 0; }
+            --col; tv = TAT(col, row); ++frag;
+        } else {
+            break;  /* NONE, or a value the reference asserts on */
+        }
+    }
+    record(sb, col, row, frag, last);
+    if (global) { /* TraceHead_ (:538-545) */
+        if (row != 0) record(sb, 0, 0, row, TV_V);
+        if (col != 0) record(sb, 0, 0, col, TV_H);
+    }
+#undef TAT
+}
+
+/* ---------------------------------------------------------------------------------
+ * Band validity (align/dp_algorithm_impl.h:193-234).
+ * ------------------------------------------------------------------------------- */
+static int band_valid(const orc_params *p, int m, int n, int fe)
+{
+    long lo = p->band_lower, up = p->band_upper;
+    if (!p->band_on) return 1;
+    if (up < -(long)n || lo > (long)m) return 0;
+    if (up < 0 && !(fe & ORC_FREE_LEFT)) return 0;
+    if (lo > 0 && !(fe & ORC_FREE_TOP)) return 0;
+    if (up + n < m && !(fe & ORC_FREE_BOTTOM)) return 0;
+    if (lo + n > m && !(fe & ORC_FREE_RIGHT)) return 0;
+    return 1;
+}
+
+/* ---------------------------------------------------------------------------------
+ * Unbanded DP (align/dp_algorithm_impl.h:483-579 with dp_meta_info.h:178-221).
+ * ------------------------------------------------------------------------------- */
+static void dp_unbanded(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
+                        int *colS, int *colE, uint8_t *T, best_t *b)
+{
+    int i, j;
+    for (i = 0; i <= n; ++i) { colS[i] = c->inf; colE[i] = c->inf; }
+    for (j = 0; j <= m; ++j) {
+        caches_t k;
+        int finalCol = (j == m);
+        k.dS = c->inf; k.vS = c->inf; k.vF = c->inf;
+        for (i = 0; i <= n; ++i) {
+            int dir, tv, f;
+            int tracked;
+            if (i == 0)
+                dir = (j == 0 || (fe & ORC_FREE_TOP)) ? DIR_ZERO : DIR_HORIZONTAL;
+            else if (j == 0)
+                dir = (fe & ORC_FREE_LEFT) ? DIR_ZERO : DIR_VERTICAL;
+            else
+                dir = DIR_ALL;
+            tv = compute_cell(c, dir, &colS[i], &colE[i], &k,
+                              j > 0 ? h[j - 1] : 0, i > 0 ? v[i - 1] : 0, &f);
+            if (T) T[(size_t)j * (size_t)(n + 1) + (size_t)i] = (uint8_t)tv;
+            if (c->local)
+                tracked = 1;
+            else if (i < n)
+                tracked = finalCol && (fe & ORC_FREE_RIGHT);
+            else
+                tracked = finalCol || (fe & ORC_FREE_BOTTOM);
+            if (tracked) scout(b, colS[i], colE[i], f, j, i);
+        }
+    }
+}
+
+int orc_align_pair(const orc_params *p,
+                   const uint8_t *h, int32_t m,
+                   const uint8_t *v, int32_t n,
+                   orc_result *out, orc_segment *segs, int32_t seg_cap)
+{
+    ctx_t c;
+    int fe;
+    int *colS, *colE;
+    uint8_t *T = NULL;
+    best_t b;
+
+    memset(out, 0, sizeof(*out));
+    c.bits16 = (p->score_bits == 16);
+    c.inf = c.bits16 ? -16384 : -(1 << 30);
+    c.local = (p->mode == ORC_LOCAL);
+    c.affine = (p->gap_model == ORC_AFFINE);
+    c.ext = p->gap_extend;
+    c.open = p->gap_open;
+    c.match = p->match;
+    c.mismatch = p->mismatch;
+    c.mat = p->matrix;
+    c.asz = p->alphabet_size;
+    fe = c.local ? (ORC_FREE_TOP | ORC_FREE_LEFT | ORC_FREE_RIGHT | ORC_FREE_BOTTOM) : p->free_ends;
+
+    if (m <= 0 || n <= 0 || !band_valid(p, m, n, fe)) {
+        out->score = c.bits16 ? -32768 : INT_MIN;
+        out->valid = 0;
+        out->n_segments = 0;
+        return 0;
+    }
+    if (p->band_on) {
+        /* Banded columns are restated in a later revision of this file. */
+        out->score = 0;
+        out->valid = -1;
+        return 1;
+    }
+    out->valid = 1;
+    colS = (int *)malloc(sizeof(int) * (size_t)(n + 1) * 2);
+    colE = colS + (n + 1);
+    if (p->traceback) T = (uint8_t *)malloc((size_t)(m + 1) * (size_t)(n + 1));
+    b.s = c.inf; b.e = c.inf; b.f = c.inf; b.col = 0; b.row = 0;
+
+    dp_unbanded(&c, fe, h, m, v, n, colS, colE, T, &b);
+
+    out->score = b.s;
+    out->end_h = b.col;
+    out->end_v = b.row;
+    if (T) {
+        segbuf_t sb;
+        uint8_t *cell = &T[(size_t)b.col * (size_t)(n + 1) + (size_t)b.row];
+        /* _correctTraceValue (align/dp_algorithm_impl.h:1188-1205), affine only. */
+        if (c.affine) {
+            if (b.f == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFV; }
+            else if (b.e == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFH; }
+        }
+        sb.segs = segs; sb.cap = segs ? seg_cap : 0; sb.n = 0; sb.overflow = 0;
+        traceback(&c, T, n, m, b.col, b.row, &sb, !c.local);
+        out->n_segments = sb.overflow ? -1 : sb.n;
+        if (sb.n > 0 && !sb.overflow) {
+            out->begin_h = (int32_t)segs[sb.n - 1].h_begin;
+            out->begin_v = (int32_t)segs[sb.n - 1].v_begin;
+        } else {
+            out->begin_h = 0;
+            out->begin_v = 0;
+        }
+        free(T);
+    }
+    free(colS);
+    return 0;
+}
+
+int orc_align_batch(const orc_params *p, int64_t n_pairs,
+                    const uint8_t *seq_h, const int64_t *off_h,
+                    const uint8_t *seq_v, const int64_t *off_v,
+                    orc_result *out, orc_segment *segs, const int64_t *seg_off,
+                    int32_t threads)
+{
+    int64_t k;
+    int rc = 0;
+    int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : rc) num_threads(nt)
+    for (k = 0; k < n_pairs; ++k) {
+        orc_segment *sp = NULL;
+        int32_t cap = 0;
+        if (p->traceback && segs && seg_off) {
+            sp = segs + seg_off[k];
+            cap = (int32_t)(seg_off[k + 1] - seg_off[k]);
+        }
+        rc |= orc_align_pair(p, seq_h + off_h[k], (int32_t)(off_h[k + 1] - off_h[k]),
+                             seq_v + off_v[k], (int32_t)(off_v[k + 1] - off_v[k]),
+                             &out[k], sp, cap);
+    }
+    return rc;
+}

@@ -1,0 +1,79 @@
+/*
+ * seqan_oracle.h -- CPU restatement of SeqAn 2's pairwise DP (test infrastructure only).
+ *
+ * This header and seqan_oracle.c are the CHECKER for the GPU engine.  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load the oracle.  The
+ * product path (seqan_gb300/) never links or calls it.
+ *
+ * Parity is pinned against the reference compiled from its own headers (oracle/ref/,
+ * built into oracle/_ref/) and against golden fixtures generated from it
+ * (tests/golden/).
+ */
+#ifndef SEQAN_ORACLE_H_
+#define SEQAN_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* AlignConfig<TOP, LEFT, RIGHT, BOTTOM> bits (align/align_config.h:52-94). */
+enum {
+    ORC_FREE_TOP = 1,     /* free first row    (DPFirstRow)    */
+    ORC_FREE_LEFT = 2,    /* free first column (DPFirstColumn) */
+    ORC_FREE_RIGHT = 4,   /* free last column  (DPLastColumn)  */
+    ORC_FREE_BOTTOM = 8   /* free last row     (DPLastRow)     */
+};
+
+enum { ORC_GLOBAL = 0, ORC_LOCAL = 1 };
+enum { ORC_LINEAR = 0, ORC_AFFINE = 1 };
+
+/* TraceSegment_ direction values (align/dp_profile.h:121-135). */
+enum { ORC_SEG_DIAGONAL = 1, ORC_SEG_HORIZONTAL = 2, ORC_SEG_VERTICAL = 4 };
+
+typedef struct {
+    int32_t mode;           /* ORC_GLOBAL / ORC_LOCAL */
+    int32_t gap_model;      /* ORC_LINEAR / ORC_AFFINE */
+    int32_t free_ends;      /* ORC_FREE_* bits, ignored for local (all free) */
+    int32_t band_on;        /* 0 / 1 */
+    int32_t band_lower;     /* lower diagonal, col - row convention */
+    int32_t band_upper;
+    int32_t match, mismatch, gap_open, gap_extend;
+    const int32_t *matrix;  /* alphabet_size^2 substitution table (row = H code) or NULL */
+    int32_t alphabet_size;
+    int32_t score_bits;     /* 16 or 32: cell width; 16 wraps like SeqAn's int16 SIMD lanes */
+    int32_t traceback;      /* 0 = score only, 1 = trace segments */
+} orc_params;
+
+typedef struct {
+    uint32_t h_begin, v_begin, length, type;  /* TraceSegment_<unsigned, unsigned> */
+} orc_segment;
+
+typedef struct {
+    int32_t score;
+    int32_t end_h, end_v;      /* coordinates of the best (traceback start) cell */
+    int32_t begin_h, begin_v;  /* alignment begin (first segment in alignment order) */
+    int32_t n_segments;        /* -1 if the segment buffer was too small */
+    int32_t valid;             /* 0 if _isValidDPSettings failed (score = numeric min) */
+} orc_result;
+
+/* One pair.  segs may be NULL when traceback == 0. */
+int orc_align_pair(const orc_params *p,
+                   const uint8_t *h, int32_t m,
+                   const uint8_t *v, int32_t n,
+                   orc_result *out, orc_segment *segs, int32_t seg_cap);
+
+/* A batch over concatenated code buffers (offsets have n_pairs + 1 entries).  Segments
+ * of pair k go to segs[seg_off[k] .. seg_off[k+1]) where the caller sized each slot as
+ * m + n + 4.  Runs with `threads` OpenMP threads (<= 0: all). */
+int orc_align_batch(const orc_params *p, int64_t n_pairs,
+                    const uint8_t *seq_h, const int64_t *off_h,
+                    const uint8_t *seq_v, const int64_t *off_v,
+                    orc_result *out, orc_segment *segs, const int64_t *seg_off,
+                    int32_t threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

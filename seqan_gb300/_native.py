@@ -1,0 +1,182 @@
+"""ctypes binding of the engine's C-ABI (include/seqan_gb300.h) and its in-tree build.
+
+The shared library is built in-tree into seqan_gb300/_lib/ by :func:`build` (nvcc for
+sm_103a).  Loading fails loudly when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_DIR = os.path.join(PKG, "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libseqan_gb300.so")
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC", "-shared"]
+
+# Status codes (include/seqan_gb300.h)
+GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY = range(8)
+GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED = 0, 1, 2
+GBA_GLOBAL, GBA_LOCAL = 0, 1
+GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE = 0, 1, 2
+GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
+GBA_OUT_SCORE, GBA_OUT_END, GBA_OUT_SEGMENTS, GBA_OUT_CIGAR = 1, 2, 4, 8
+GBA_SEG_DIAGONAL, GBA_SEG_HORIZONTAL, GBA_SEG_VERTICAL = 1, 2, 4
+
+# Every symbol include/seqan_gb300.h declares.
+EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", "gba_align_batch",
+            "gba_plan_create", "gba_plan_destroy", "gba_plan_execute", "gba_plan_fetch",
+            "gba_device_alloc", "gba_device_free", "gba_host_alloc", "gba_host_free",
+            "gba_copy_to_device", "gba_copy_to_host", "gba_synchronize", "gba_timer_start",
+            "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak"]
+
+
+class GbaConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("hbm_budget_bytes", C.c_int64)]
+
+
+class GbaParams(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("gap_model", C.c_int32), ("free_ends", C.c_int32),
+                ("band_on", C.c_int32), ("band_lower", C.c_int32), ("band_upper", C.c_int32),
+                ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
+                ("gap_extend", C.c_int32), ("matrix", C.c_void_p), ("alphabet_size", C.c_int32),
+                ("score_bits", C.c_int32), ("outputs", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class GbaBatch(C.Structure):
+    _fields_ = [("num_pairs", C.c_int64), ("seq_h", C.c_void_p), ("off_h", C.c_void_p),
+                ("seq_v", C.c_void_p), ("off_v", C.c_void_p), ("h_shared", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class GbaResult(C.Structure):
+    _fields_ = [("score", C.c_void_p), ("end_h", C.c_void_p), ("end_v", C.c_void_p),
+                ("begin_h", C.c_void_p), ("begin_v", C.c_void_p), ("pair_status", C.c_void_p),
+                ("segments", C.c_void_p), ("segment_capacity", C.c_int64),
+                ("segment_offsets", C.c_void_p), ("cigar", C.c_void_p),
+                ("cigar_capacity", C.c_int64), ("cigar_offsets", C.c_void_p)]
+
+
+class GbaStats(C.Structure):
+    _fields_ = [("dp_kernel_ms", C.c_float), ("traceback_kernel_ms", C.c_float),
+                ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64)]
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + \
+        [os.path.join(INCLUDE, "seqan_gb300.h")]
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compiles the engine for sm_103a into seqan_gb300/_lib/ (no-op when up to date)."""
+    srcs = _sources()
+    newest = max(os.path.getmtime(s) for s in srcs)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    os.makedirs(LIB_DIR, exist_ok=True)
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["nvcc", *NVCC_FLAGS, "-o", tmp, os.path.join(CSRC, "engine.cu")]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """Loads the engine library; raises if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"seqan_gb300 engine library missing ({LIB_PATH}); run "
+                                   "seqan_gb300._native.build() -- there is no CPU fallback")
+            L = C.CDLL(LIB_PATH)
+            vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+            L.gba_create.argtypes = [C.POINTER(vp), C.POINTER(GbaConfig)]
+            L.gba_destroy.argtypes = [vp]
+            L.gba_status_string.argtypes = [C.c_int]
+            L.gba_status_string.restype = C.c_char_p
+            L.gba_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+            L.gba_align_batch.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaBatch), C.POINTER(GbaResult)]
+            L.gba_plan_create.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaBatch), C.POINTER(vp)]
+            L.gba_plan_destroy.argtypes = [vp, vp]
+            L.gba_plan_execute.argtypes = [vp, vp, C.POINTER(GbaBatch), C.POINTER(GbaResult)]
+            L.gba_plan_fetch.argtypes = [vp, vp, C.POINTER(GbaResult)]
+            L.gba_device_alloc.argtypes = [vp, C.POINTER(vp), C.c_size_t]
+            L.gba_device_free.argtypes = [vp, vp]
+            L.gba_host_alloc.argtypes = [vp, C.POINTER(vp), C.c_size_t]
+            L.gba_host_free.argtypes = [vp, vp]
+            L.gba_copy_to_device.argtypes = [vp, vp, vp, C.c_size_t]
+            L.gba_copy_to_host.argtypes = [vp, vp, vp, C.c_size_t]
+            L.gba_synchronize.argtypes = [vp]
+            L.gba_timer_start.argtypes = [vp]
+            L.gba_timer_stop.argtypes = [vp, C.POINTER(C.c_float)]
+            L.gba_get_stats.argtypes = [vp, C.POINTER(GbaStats)]
+            L.gba_measure_int_peak.argtypes = [vp, C.POINTER(C.c_double)]
+            _lib = L
+    return _lib
+
+
+class GbaError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} [status {status}]")
+        self.status = status
+
+
+class Context:
+    """Owns a gba_context (device, stream, cached device buffers)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        L = lib()
+        self._h = C.c_void_p()
+        cfg = GbaConfig(device, hbm_budget_bytes)
+        rc = L.gba_create(C.byref(self._h), C.byref(cfg))
+        if rc != GBA_OK:
+            raise GbaError(rc, f"gba_create failed: {L.gba_status_string(rc).decode()}")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc: int, what: str):
+        if rc != GBA_OK:
+            buf = C.create_string_buffer(512)
+            lib().gba_last_error(self._h, buf, 512)
+            raise GbaError(rc, f"{what}: {lib().gba_status_string(rc).decode()}: {buf.value.decode()}")
+
+    def stats(self) -> GbaStats:
+        s = GbaStats()
+        self.check(lib().gba_get_stats(self._h, C.byref(s)), "gba_get_stats")
+        return s
+
+    def close(self):
+        if self._h:
+            lib().gba_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx

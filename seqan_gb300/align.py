@@ -1,0 +1,281 @@
+"""Host-side mirror of SeqAn 2's batch alignment interface over the GB300 engine.
+
+The functions keep the reference's names, argument order and meaning:
+
+* ``globalAlignmentScore(setH, setV, score, config=AlignConfig(), lower=None, upper=None)``
+  -- align_parallel/parallel_align_interface.h:330-340, align/global_alignment_unbanded.h:739-821,
+  banded align/global_alignment_banded.h:558-652.
+* ``localAlignmentScore(setH, setV, score, lower=None, upper=None)``
+  -- align/local_alignment_unbanded.h:554-572, align/local_alignment_banded.h:252.
+* ``globalAlignment(gapsH, gapsV, score, config, lower, upper)`` and ``localAlignment(...)``
+  over lists of :class:`Gaps` (overwritten in place, scores returned) --
+  align/global_alignment_unbanded.h:831-888, align/local_alignment_unbanded.h:367-399.
+* ``getCigarString(gapsRef, gapsRead)`` -- bam_io/cigar.h:261-339.
+
+An optional ``execution_policy`` first argument is accepted (and ignored: the whole batch runs
+on the GPU), as the reference's ``ExecutionPolicy<Parallel, Vectorial>`` overloads take one.
+Like the reference, invalid pairs (empty sequence, band outside the matrix) score
+``numeric_limits<T>::min()``.  Every call goes through the C-ABI; nothing runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from .alphabet import encode
+from .scoring import Blosum62, Score  # noqa: F401  (re-exported)
+
+
+@dataclass(frozen=True)
+class AlignConfig:
+    """AlignConfig<TOP, LEFT, RIGHT, BOTTOM> (align/align_config.h:52-94)."""
+    top: bool = False
+    left: bool = False
+    right: bool = False
+    bottom: bool = False
+
+    @property
+    def bits(self) -> int:
+        return (N.GBA_FREE_TOP if self.top else 0) | (N.GBA_FREE_LEFT if self.left else 0) | \
+            (N.GBA_FREE_RIGHT if self.right else 0) | (N.GBA_FREE_BOTTOM if self.bottom else 0)
+
+
+class ExecutionPolicy:
+    """Accepted for call-surface parity with ExecutionPolicy<Parallel, Vectorial>."""
+
+    def __init__(self, parallel: str = "Parallel", vectorial: str = "Vectorial", threads: int = 1):
+        self.parallel, self.vectorial, self.threads = parallel, vectorial, threads
+
+
+class Gaps:
+    """A gapped view of one sequence, filled by globalAlignment/localAlignment.
+
+    Holds the clipped begin/end (source positions) and the gapped row, like
+    Gaps<String<T>, ArrayGaps> after _adaptTraceSegmentsTo (align/dp_traceback_adaptor.h:57-117).
+    """
+
+    def __init__(self, source, alphabet: str = "dna5"):
+        self.text = source if isinstance(source, str) else None
+        self.codes = encode(source, alphabet)
+        self.alphabet = alphabet
+        self.clipped_begin = 0
+        self.clipped_end = len(self.codes)
+        self.gap_runs: list[tuple[int, int]] = []   # (view position, length)
+        self.segments = []                          # the pair's TraceSegment_ list
+
+    def __len__(self):
+        return self.clipped_end - self.clipped_begin + sum(l for _, l in self.gap_runs)
+
+    def row(self) -> str:
+        """The gapped row as operator<< prints it (clipped part, '-' for gaps)."""
+        txt = self.text if self.text is not None else _decode(self.codes, self.alphabet)
+        out = []
+        src = self.clipped_begin
+        view = 0
+        for pos, ln in self.gap_runs:
+            take = pos - view
+            out.append(txt[src:src + take]); src += take; view += take
+            out.append("-" * ln); view += ln
+        out.append(txt[src:self.clipped_end])
+        return "".join(out)
+
+    def __str__(self):
+        return self.row()
+
+
+def _decode(codes, alphabet):
+    from .alphabet import decode
+    return decode(codes, alphabet)
+
+
+def _split_policy(args):
+    if args and isinstance(args[0], ExecutionPolicy):
+        return args[1:]
+    return args
+
+
+def _as_codes(seqs, alphabet):
+    return [encode(s, alphabet) for s in seqs]
+
+
+def _concat(codes):
+    lens = np.fromiter((len(c) for c in codes), dtype=np.int64, count=len(codes))
+    off = np.zeros(len(codes) + 1, dtype=np.int64)
+    np.cumsum(lens, out=off[1:])
+    flat = np.concatenate(codes).astype(np.uint8, copy=False) if off[-1] else np.zeros(1, np.uint8)
+    return np.ascontiguousarray(flat), off
+
+
+def _vp(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def make_params(score, mode: int, config: AlignConfig | None, band, outputs: int) -> N.GbaParams:
+    p = N.GbaParams()
+    p.mode = mode
+    p.gap_model = N.GBA_GAPS_AUTO
+    p.free_ends = config.bits if (config is not None and mode == N.GBA_GLOBAL) else 0
+    if band is not None:
+        p.band_on, p.band_lower, p.band_upper = 1, int(band[0]), int(band[1])
+    p.match, p.mismatch = score.match, score.mismatch
+    p.gap_open, p.gap_extend = score.gap_open, score.gap_extend
+    if score.matrix is not None:
+        p.matrix = score.matrix.ctypes.data_as(C.c_void_p)
+        p.alphabet_size = score.matrix.shape[0]
+    p.score_bits = score.bits
+    p.outputs = outputs
+    return p
+
+
+@dataclass
+class BatchOutput:
+    score: np.ndarray
+    end_h: np.ndarray
+    end_v: np.ndarray
+    status: np.ndarray
+    begin_h: np.ndarray | None = None
+    begin_v: np.ndarray | None = None
+    segments: np.ndarray | None = None         # [total, 4] uint32
+    segment_offsets: np.ndarray | None = None  # [n+1]
+    cigar: np.ndarray | None = None            # [total] uint32 (len << 4 | op)
+    cigar_offsets: np.ndarray | None = None
+
+    def pair_segments(self, k):
+        s = self.segments[self.segment_offsets[k]:self.segment_offsets[k + 1]]
+        return [tuple(int(x) for x in row) for row in s]
+
+    def pair_cigar(self, k) -> str:
+        ops = "MIDNSHP=X"
+        c = self.cigar[self.cigar_offsets[k]:self.cigar_offsets[k + 1]]
+        return "".join(f"{int(x) >> 4}{ops[int(x) & 15]}" for x in c)
+
+
+def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None,
+                traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None) -> BatchOutput:
+    """Aligns lists of code arrays through gba_align_batch."""
+    ctx = ctx or N.default_context()
+    n = len(codes_v)
+    sh, oh = _concat(codes_h)
+    sv, ov = _concat(codes_v)
+    outputs = N.GBA_OUT_SCORE | N.GBA_OUT_END
+    if traceback:
+        outputs |= N.GBA_OUT_SEGMENTS
+    if cigar:
+        outputs |= N.GBA_OUT_CIGAR | N.GBA_OUT_SEGMENTS
+    params = make_params(score, mode, config, band, outputs)
+    b = N.GbaBatch(n, _vp(sh), _vp(oh), _vp(sv), _vp(ov), 1 if h_shared else 0, 0)
+    res = BatchOutput(score=np.zeros(n, np.int32), end_h=np.zeros(n, np.int32), end_v=np.zeros(n, np.int32),
+                      status=np.zeros(n, np.int32))
+    r = N.GbaResult()
+    r.score, r.end_h, r.end_v, r.pair_status = _vp(res.score), _vp(res.end_h), _vp(res.end_v), _vp(res.status)
+    if traceback or cigar:
+        lh = np.full(n, oh[1] - oh[0], np.int64) if h_shared else (oh[1:] - oh[:-1])
+        cap = int((lh + (ov[1:] - ov[:-1]) + 4).sum()) + 1
+        res.begin_h, res.begin_v = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        res.segments = np.zeros((cap, 4), np.uint32)
+        res.segment_offsets = np.zeros(n + 1, np.int64)
+        r.begin_h, r.begin_v = _vp(res.begin_h), _vp(res.begin_v)
+        r.segments, r.segment_capacity, r.segment_offsets = _vp(res.segments), cap, _vp(res.segment_offsets)
+        if cigar:
+            res.cigar = np.zeros(cap, np.uint32)
+            res.cigar_offsets = np.zeros(n + 1, np.int64)
+            r.cigar, r.cigar_capacity, r.cigar_offsets = _vp(res.cigar), cap, _vp(res.cigar_offsets)
+    ctx.check(N.lib().gba_align_batch(ctx.handle, C.byref(params), C.byref(b), C.byref(r)), "gba_align_batch")
+    return res
+
+
+def _band(args):
+    if len(args) >= 2 and args[0] is not None:
+        return (int(args[0]), int(args[1]))
+    return None
+
+
+def globalAlignmentScore(*args, alphabet: str = "dna5", **kw):
+    """globalAlignmentScore([policy,] setH, setV, score[, config][, lower, upper]) -> scores."""
+    args = _split_policy(args)
+    setH, setV, score = args[0], args[1], args[2]
+    rest = list(args[3:])
+    config = rest.pop(0) if rest and isinstance(rest[0], AlignConfig) else kw.get("config", AlignConfig())
+    band = _band(rest) or kw.get("band")
+    h_shared = not isinstance(setH, (list, tuple))
+    codes_h = [encode(setH, alphabet)] if h_shared else _as_codes(setH, alphabet)
+    out = align_codes(codes_h, _as_codes(setV, alphabet), score, N.GBA_GLOBAL, config, band, h_shared=h_shared)
+    return out.score.astype(score.dtype)
+
+
+def localAlignmentScore(*args, alphabet: str = "dna5", **kw):
+    """localAlignmentScore([policy,] setH, setV, score[, lower, upper]) -> scores."""
+    args = _split_policy(args)
+    setH, setV, score = args[0], args[1], args[2]
+    band = _band(list(args[3:])) or kw.get("band")
+    h_shared = not isinstance(setH, (list, tuple))
+    codes_h = [encode(setH, alphabet)] if h_shared else _as_codes(setH, alphabet)
+    out = align_codes(codes_h, _as_codes(setV, alphabet), score, N.GBA_LOCAL, None, band, h_shared=h_shared)
+    return out.score.astype(score.dtype)
+
+
+def _apply_segments(gH: Gaps, gV: Gaps, segs):
+    """_adaptTraceSegmentsTo (align/dp_traceback_adaptor.h:57-117)."""
+    gH.segments = gV.segments = segs
+    gH.gap_runs, gV.gap_runs = [], []
+    if not segs:
+        gH.clipped_begin = gH.clipped_end = gV.clipped_begin = gV.clipped_end = 0
+        return
+    hb, vb = segs[-1][0], segs[-1][1]
+    view = 0
+    ch, cv = hb, vb
+    for (_, _, ln, tp) in reversed(segs):
+        if tp == N.GBA_SEG_HORIZONTAL:
+            _add_run(gV.gap_runs, view, ln); ch += ln
+        elif tp == N.GBA_SEG_VERTICAL:
+            _add_run(gH.gap_runs, view, ln); cv += ln
+        else:
+            ch += ln; cv += ln
+        view += ln
+    gH.clipped_begin, gH.clipped_end = hb, ch
+    gV.clipped_begin, gV.clipped_end = vb, cv
+
+
+def _add_run(runs, pos, ln):
+    if runs and runs[-1][0] + runs[-1][1] == pos:
+        runs[-1] = (runs[-1][0], runs[-1][1] + ln)
+    else:
+        runs.append((pos, ln))
+
+
+def _align_gaps(mode, args, kw):
+    args = _split_policy(args)
+    gapsH, gapsV, score = args[0], args[1], args[2]
+    rest = list(args[3:])
+    config = rest.pop(0) if rest and isinstance(rest[0], AlignConfig) else kw.get("config", AlignConfig())
+    band = _band(rest) or kw.get("band")
+    out = align_codes([g.codes for g in gapsH], [g.codes for g in gapsV], score, mode,
+                      config if mode == N.GBA_GLOBAL else None, band, traceback=True)
+    for k, (gH, gV) in enumerate(zip(gapsH, gapsV)):
+        _apply_segments(gH, gV, out.pair_segments(k))
+    return out.score.astype(score.dtype)
+
+
+def globalAlignment(*args, **kw):
+    """globalAlignment([policy,] gapsH, gapsV, score[, config][, lower, upper]) -> scores."""
+    return _align_gaps(N.GBA_GLOBAL, args, kw)
+
+
+def localAlignment(*args, **kw):
+    """localAlignment([policy,] gapsH, gapsV, score[, lower, upper]) -> scores."""
+    return _align_gaps(N.GBA_LOCAL, args, kw)
+
+
+def getCigarString(gapsRef: Gaps, gapsRead: Gaps, spliced_gap_thresh: int = 20) -> str:
+    """CIGAR of an aligned pair (bam_io/cigar.h:261-339): M/I/D, D runs >= thresh as N."""
+    ops = []
+    for (_, _, ln, tp) in reversed(gapsRef.segments):
+        op = "M" if tp == N.GBA_SEG_DIAGONAL else ("I" if tp == N.GBA_SEG_VERTICAL else "D")
+        if ops and ops[-1][0] == op:
+            ops[-1][1] += ln
+        else:
+            ops.append([op, ln])
+    return "".join(f"{n}{'N' if (o == 'D' and n >= spliced_gap_thresh) else o}" for o, n in ops)

@@ -1,0 +1,101 @@
+// dp_common.cuh -- shared definitions of the GB300 alignment kernels.
+//
+// Trace values are the reference's TraceBitMap_ bits (align/dp_profile.h:121-135) so the
+// device traceback makes exactly the reference's decisions.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gba {
+
+constexpr uint8_t TV_NONE = 0;
+constexpr uint8_t TV_DIAG = 1;
+constexpr uint8_t TV_H = 2;
+constexpr uint8_t TV_V = 4;
+constexpr uint8_t TV_HO = 8;
+constexpr uint8_t TV_VO = 16;
+constexpr uint8_t TV_MFH = 32;
+constexpr uint8_t TV_MFV = 64;
+
+constexpr int FREE_TOP = 1, FREE_LEFT = 2, FREE_RIGHT = 4, FREE_BOTTOM = 8;
+
+// Rows per register strip of the one-pair-per-thread kernels.  16 trace bytes per strip
+// column make one 16-byte store.
+constexpr int STRIP_ROWS = 16;
+
+// Per-pair descriptor (device).  Offsets index the device code buffers.
+struct PairDesc {
+    int64_t h_off;
+    int64_t v_off;
+    int64_t trace_off;   // byte offset of this pair's trace matrix (16-byte aligned)
+    int32_t m;           // |H| (columns)
+    int32_t n;           // |V| (rows)
+    int32_t inf;         // DPCellDefaultInfinity of the cell width the pair runs with
+    int32_t pad;
+};
+
+// Arguments of the DP kernels, passed by value.
+struct DpArgs {
+    const uint8_t *seq_h;
+    const uint8_t *seq_v;
+    const PairDesc *pairs;
+    const int32_t *order;          // thread slot -> pair index (length-binned order)
+    const int64_t *warp_scratch;   // per warp: int2 offset of its interleaved boundary rows
+    int2 *scratch;
+    uint8_t *trace;
+    int32_t *score;
+    int32_t *end_h;
+    int32_t *end_v;
+    int32_t *best_e;               // E and F of the best cell (start-cell trace correction)
+    int32_t *best_f;
+    const int32_t *matrix;         // alphabet^2 table or nullptr
+    int64_t num_slots;
+    int32_t match, mismatch, gap_open, gap_extend;
+    int32_t free_ends;
+    int32_t alphabet;
+};
+
+struct TraceArgs {
+    const PairDesc *pairs;
+    const int32_t *order;
+    const uint8_t *trace;
+    const int32_t *score;
+    const int32_t *end_h;
+    const int32_t *end_v;
+    const int32_t *best_e;
+    const int32_t *best_f;
+    int32_t *begin_h;
+    int32_t *begin_v;
+    uint32_t *seg_slots;           // 4 words per segment, slot of pair k at seg_slot_off[k]
+    const int64_t *seg_slot_off;
+    int32_t *seg_count;
+    uint32_t *cigar_slots;
+    const int64_t *cigar_slot_off;
+    int32_t *cigar_count;
+    int64_t num_slots;
+    int32_t affine;
+    int32_t local;
+};
+
+__host__ __device__ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
+
+// Trace layout of one pair: row 0 as m+1 bytes (padded to 16), then rows 1..n in strips of
+// STRIP_ROWS rows; strip s stores column j's STRIP_ROWS bytes contiguously at
+// (s * (m + 1) + j) * STRIP_ROWS.
+__host__ __device__ inline int64_t trace_bytes(int m, int n)
+{
+    int64_t strips = (n + STRIP_ROWS - 1) / STRIP_ROWS;
+    return align16(m + 1) + strips * int64_t(m + 1) * STRIP_ROWS;
+}
+
+__device__ __forceinline__ uint8_t trace_at(const uint8_t *base, int m, int col, int row)
+{
+    if (row == 0) return base[col];
+    int r = row - 1;
+    int s = r / STRIP_ROWS;
+    int k = r - s * STRIP_ROWS;
+    return base[align16(m + 1) + (int64_t(s) * (m + 1) + col) * STRIP_ROWS + k];
+}
+
+}  // namespace gba

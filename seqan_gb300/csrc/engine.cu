@@ -1,0 +1,846 @@
+// engine.cu -- the C-ABI of the GB300 batch alignment engine (include/seqan_gb300.h).
+//
+// A call runs: validate -> plan (lengths, int16 range check, length-binned order, scratch
+// and trace offsets) -> upload -> DP kernel -> [traceback kernel -> compaction] -> download.
+// There is no CPU fallback: every alignment is computed by the kernels in this file.
+#include "../../include/seqan_gb300.h"
+
+#include "dp_common.cuh"
+#include "dp_kernels.cuh"
+#include "traceback_kernels.cuh"
+#include "int_peak.cuh"
+
+#include <cub/device/device_scan.cuh>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+using namespace gba;
+
+namespace {
+
+// ------------------------------------------------------------------------------------
+// Device buffer that only grows.
+// ------------------------------------------------------------------------------------
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes <= cap) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+    }
+    template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+}  // namespace
+
+struct gba_plan {
+    // host side
+    int64_t num_pairs = 0;
+    int64_t num_slots = 0;          // valid pairs
+    bool traceback = false;
+    bool cigar = false;
+    bool affine = false;
+    bool local = false;
+    bool matrix = false;
+    int32_t free_ends = 0;
+    gba_params params{};
+    std::vector<int32_t> matrix_host;
+    std::vector<int32_t> status;    // per pair GBA_PAIR_*
+    std::vector<int32_t> invalid_score;  // per invalid pair
+    int64_t cells = 0;
+    int64_t trace_total = 0;
+    int64_t seg_slots_total = 0;
+    int64_t cigar_slots_total = 0;
+    int64_t scratch_total = 0;      // int2 elements
+    int64_t seq_h_bytes = 0, seq_v_bytes = 0;
+    // device side
+    DevBuf pairs, order, warp_scratch, scratch, trace, best_e, best_f, matrix_dev;
+    DevBuf end_h, end_v, score_tmp, begin_h, begin_v;
+    DevBuf seg_slots, seg_slot_off, seg_count, seg_dense_off, seg_dense, seg_count64;
+    DevBuf cig_slots, cig_slot_off, cig_count, cig_dense_off, cig_dense, cig_count64;
+    DevBuf cub_tmp;
+    size_t cub_tmp_bytes = 0;
+    int64_t seg_dense_total = -1, cig_dense_total = -1;
+    bool owned = true;
+    void release()
+    {
+        DevBuf *all[] = {&pairs, &order, &warp_scratch, &scratch, &trace, &best_e, &best_f, &matrix_dev,
+                         &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots, &seg_slot_off,
+                         &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
+                         &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp};
+        for (DevBuf *b : all) b->release();
+    }
+    size_t device_bytes() const
+    {
+        const DevBuf *all[] = {&pairs, &order, &warp_scratch, &scratch, &trace, &best_e, &best_f,
+                               &matrix_dev, &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots,
+                               &seg_slot_off, &seg_count, &seg_dense_off, &seg_dense, &seg_count64,
+                               &cig_slots, &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense,
+                               &cig_count64, &cub_tmp};
+        size_t s = 0;
+        for (const DevBuf *b : all) s += b->cap;
+        return s;
+    }
+};
+
+struct gba_context {
+    int device = 0;
+    int64_t budget = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::string last_error;
+    gba_stats stats{};
+    bool stats_pending = false;     // events of the last run not read yet
+    gba_plan oneshot;               // buffers reused by gba_align_batch
+    DevBuf seq_h, seq_v;            // device copies of the inputs for gba_align_batch
+    DevBuf out_score, out_end_h, out_end_v;
+};
+
+namespace {
+
+int fail(gba_context *ctx, int code, const char *fmt, ...)
+{
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->last_error = buf;
+    }
+    return code;
+}
+
+#define GBA_CUDA(ctx, call)                                                                  \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            int code_ = (e_ == cudaErrorMemoryAllocation) ? GBA_ENOMEM : GBA_ECUDA;          \
+            return fail(ctx, code_, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),  \
+                        __FILE__, __LINE__);                                                 \
+        }                                                                                    \
+    } while (0)
+
+constexpr int kBlock = 128;
+
+bool is_affine(const gba_params &p)
+{
+    if (p.gap_model == GBA_GAPS_LINEAR) return false;
+    if (p.gap_model == GBA_GAPS_AFFINE) return true;
+    return p.gap_open != p.gap_extend;
+}
+
+int max_sub_abs(const gba_params &p, const std::vector<int32_t> &mat, int *max_pos)
+{
+    int mx = 0, mp = 0;
+    if (!mat.empty()) {
+        for (int32_t v : mat) {
+            mx = std::max(mx, std::abs(v));
+            mp = std::max(mp, int(v));
+        }
+    } else {
+        mx = std::max(std::abs(p.match), std::abs(p.mismatch));
+        mp = std::max(std::max(p.match, p.mismatch), 0);
+    }
+    *max_pos = mp;
+    return mx;
+}
+
+// True when every real cell value of an m x n problem stays inside the range where the
+// reference's wrapping int16 cells equal exact arithmetic: the best score is at most
+// max_pos * min(m, n) <= 32767, and no value falls to the int16 "infinity" of -16384
+// (align/dp_cell.h:143-146).  Scores are bounded below by the all-gap path.
+bool int16_exact(const gba_params &p, int max_pos, int64_t m, int64_t n, bool local)
+{
+    const int64_t open = std::abs(p.gap_open), ext = std::abs(p.gap_extend);
+    const int64_t upper = int64_t(max_pos) * std::min(m, n);
+    if (upper > 32767 - 64) return false;
+    if (local) return true;
+    const int64_t lower = -(3 * open + ext * (m + n + 2));
+    return lower > -16384 + 2 * (open + ext) + 64;
+}
+
+int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
+{
+    if (!p || !b) return fail(ctx, GBA_EINVAL, "null params or batch");
+    if (p->mode != GBA_GLOBAL && p->mode != GBA_LOCAL) return fail(ctx, GBA_EINVAL, "bad mode %d", p->mode);
+    if (p->gap_model < 0 || p->gap_model > 2) return fail(ctx, GBA_EINVAL, "bad gap model");
+    if (p->score_bits != 16 && p->score_bits != 32) return fail(ctx, GBA_EINVAL, "score_bits must be 16 or 32");
+    if (p->free_ends & ~15) return fail(ctx, GBA_EINVAL, "bad free_ends bits");
+    if (p->matrix && (p->alphabet_size <= 0 || p->alphabet_size > 32))
+        return fail(ctx, GBA_EINVAL, "alphabet_size must be in 1..32");
+    if (b->num_pairs < 0) return fail(ctx, GBA_EINVAL, "negative num_pairs");
+    if (b->num_pairs > 0 && (!b->off_h || !b->off_v || !b->seq_h || !b->seq_v))
+        return fail(ctx, GBA_EINVAL, "null sequence or offset pointer");
+    if (p->band_on) return fail(ctx, GBA_EUNSUPPORTED, "banded DP is not enabled in this build");
+    if ((p->outputs & GBA_OUT_CIGAR) && !(p->outputs & GBA_OUT_SEGMENTS))
+        return fail(ctx, GBA_EINVAL, "GBA_OUT_CIGAR requires GBA_OUT_SEGMENTS");
+    return GBA_OK;
+}
+
+// LSD radix sort of (key, index) by key descending; keys < 2^32.
+void sort_desc(std::vector<uint32_t> &keys, std::vector<int32_t> &idx)
+{
+    const size_t n = idx.size();
+    std::vector<uint32_t> k2(n);
+    std::vector<int32_t> i2(n);
+    for (int pass = 0; pass < 2; ++pass) {
+        const int shift = 16 * pass;
+        std::vector<size_t> cnt(65537, 0);
+        for (size_t i = 0; i < n; ++i) ++cnt[(0xffffu - ((keys[i] >> shift) & 0xffffu)) + 1];
+        for (size_t i = 1; i < cnt.size(); ++i) cnt[i] += cnt[i - 1];
+        for (size_t i = 0; i < n; ++i) {
+            size_t d = cnt[0xffffu - ((keys[i] >> shift) & 0xffffu)]++;
+            k2[d] = keys[i];
+            i2[d] = idx[i];
+        }
+        keys.swap(k2);
+        idx.swap(i2);
+    }
+}
+
+template <typename T>
+int upload(gba_context *ctx, DevBuf &buf, const std::vector<T> &v)
+{
+    GBA_CUDA(ctx, buf.ensure(v.size() * sizeof(T) + 16));
+    if (!v.empty())
+        GBA_CUDA(ctx, cudaMemcpyAsync(buf.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+    return GBA_OK;
+}
+
+// Builds a plan from host offsets.  `plan` buffers are (re)used.
+int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_plan *plan)
+{
+    int rc = validate(ctx, p, b);
+    if (rc) return rc;
+    const int64_t N = b->num_pairs;
+    plan->params = *p;
+    plan->num_pairs = N;
+    plan->affine = is_affine(*p);
+    plan->local = p->mode == GBA_LOCAL;
+    plan->free_ends = p->free_ends;
+    plan->traceback = (p->outputs & GBA_OUT_SEGMENTS) != 0;
+    plan->cigar = (p->outputs & GBA_OUT_CIGAR) != 0;
+    plan->matrix = p->matrix != nullptr;
+    plan->matrix_host.clear();
+    if (p->matrix) plan->matrix_host.assign(p->matrix, p->matrix + p->alphabet_size * p->alphabet_size);
+    int max_pos = 0;
+    max_sub_abs(*p, plan->matrix_host, &max_pos);
+
+    plan->status.assign(N, GBA_PAIR_OK);
+    std::vector<PairDesc> desc(std::max<int64_t>(N, 1));
+    std::vector<uint32_t> keys;
+    std::vector<int32_t> idx;
+    keys.reserve(N);
+    idx.reserve(N);
+    plan->cells = 0;
+    int64_t trace_off = 0;
+    const int64_t hs0 = b->h_shared ? b->off_h[0] : 0;
+    const int64_t hs1 = b->h_shared ? b->off_h[1] : 0;
+    plan->seq_h_bytes = N ? (b->h_shared ? b->off_h[1] : b->off_h[N]) : 0;
+    plan->seq_v_bytes = N ? b->off_v[N] : 0;
+    for (int64_t k = 0; k < N; ++k) {
+        const int64_t h0 = b->h_shared ? hs0 : b->off_h[k];
+        const int64_t h1 = b->h_shared ? hs1 : b->off_h[k + 1];
+        const int64_t v0 = b->off_v[k], v1 = b->off_v[k + 1];
+        if (h0 < 0 || v0 < 0 || h1 < h0 || v1 < v0)
+            return fail(ctx, GBA_EINVAL, "negative or decreasing offsets at pair %lld", (long long)k);
+        if (h1 - h0 > (1 << 30) || v1 - v0 > (1 << 30)) return fail(ctx, GBA_EINVAL, "sequence too long");
+        PairDesc &d = desc[k];
+        d.h_off = h0;
+        d.v_off = v0;
+        d.m = int32_t(h1 - h0);
+        d.n = int32_t(v1 - v0);
+        d.trace_off = 0;
+        d.pad = 0;
+        bool exact16 = p->score_bits == 16 && int16_exact(*p, max_pos, d.m, d.n, plan->local);
+        d.inf = exact16 ? -16384 : -(1 << 30);
+        if (p->score_bits == 16 && !exact16) plan->status[k] = GBA_PAIR_PROMOTED;
+        if (d.m == 0 || d.n == 0) {
+            plan->status[k] = GBA_PAIR_INVALID;
+            continue;
+        }
+        plan->cells += int64_t(d.m) * d.n;
+        if (plan->traceback) {
+            d.trace_off = trace_off;
+            trace_off += trace_bytes(d.m, d.n);
+        }
+        const int64_t strips = (d.n + STRIP_ROWS - 1) / STRIP_ROWS;
+        const int64_t cost = strips * (d.m + 1);
+        keys.push_back(uint32_t(std::min<int64_t>(cost, 0xffffffffLL)));
+        idx.push_back(int32_t(k));
+    }
+    plan->trace_total = trace_off;
+    sort_desc(keys, idx);
+    plan->num_slots = int64_t(idx.size());
+
+    // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
+    const int64_t warps = (plan->num_slots + 31) / 32;
+    std::vector<int64_t> wscr(std::max<int64_t>(warps, 1));
+    int64_t scr = 0;
+    for (int64_t w = 0; w < warps; ++w) {
+        int maxm = 0;
+        for (int64_t s = w * 32; s < std::min(plan->num_slots, (w + 1) * 32); ++s)
+            maxm = std::max(maxm, desc[idx[s]].m);
+        wscr[w] = scr;
+        scr += int64_t(maxm + 1) * 32;
+    }
+    plan->scratch_total = scr;
+
+    // Segment / CIGAR slots: at most m + n + 4 records per pair.
+    std::vector<int64_t> seg_off(N + 1, 0), cig_off;
+    if (plan->traceback) {
+        for (int64_t k = 0; k < N; ++k) {
+            const int64_t cap = plan->status[k] == GBA_PAIR_INVALID ? 0 : int64_t(desc[k].m) + desc[k].n + 4;
+            seg_off[k + 1] = seg_off[k] + cap;
+        }
+        plan->seg_slots_total = seg_off[N];
+        if (plan->cigar) {
+            cig_off = seg_off;
+            plan->cigar_slots_total = seg_off[N];
+        }
+    }
+
+    // HBM budget: everything this plan keeps on the device plus the input codes.
+    const int64_t need = int64_t(sizeof(PairDesc)) * N + 4 * N * 8 + scr * 8 + plan->trace_total +
+                         plan->seg_slots_total * 16 * 2 + plan->cigar_slots_total * 4 * 2 +
+                         plan->seq_h_bytes + plan->seq_v_bytes;
+    if (ctx->budget > 0 && need > ctx->budget)
+        return fail(ctx, GBA_EBUDGET, "batch needs %lld bytes of HBM, budget is %lld", (long long)need,
+                    (long long)ctx->budget);
+
+    if ((rc = upload(ctx, plan->pairs, desc))) return rc;
+    if ((rc = upload(ctx, plan->order, idx))) return rc;
+    if ((rc = upload(ctx, plan->warp_scratch, wscr))) return rc;
+    GBA_CUDA(ctx, plan->scratch.ensure(size_t(std::max<int64_t>(scr, 1)) * sizeof(int2)));
+    if (plan->matrix) {
+        if ((rc = upload(ctx, plan->matrix_dev, plan->matrix_host))) return rc;
+    }
+    GBA_CUDA(ctx, plan->end_h.ensure(size_t(N + 1) * 4));
+    GBA_CUDA(ctx, plan->end_v.ensure(size_t(N + 1) * 4));
+    GBA_CUDA(ctx, plan->score_tmp.ensure(size_t(N + 1) * 4));
+    if (plan->traceback) {
+        GBA_CUDA(ctx, plan->trace.ensure(size_t(std::max<int64_t>(plan->trace_total, 16))));
+        GBA_CUDA(ctx, plan->best_e.ensure(size_t(N + 1) * 4));
+        GBA_CUDA(ctx, plan->best_f.ensure(size_t(N + 1) * 4));
+        GBA_CUDA(ctx, plan->begin_h.ensure(size_t(N + 1) * 4));
+        GBA_CUDA(ctx, plan->begin_v.ensure(size_t(N + 1) * 4));
+        if ((rc = upload(ctx, plan->seg_slot_off, seg_off))) return rc;
+        GBA_CUDA(ctx, plan->seg_slots.ensure(size_t(std::max<int64_t>(plan->seg_slots_total, 1)) * 16));
+        GBA_CUDA(ctx, plan->seg_count.ensure(size_t(N + 1) * 4));
+        GBA_CUDA(ctx, plan->seg_count64.ensure(size_t(N + 1) * 8));
+        GBA_CUDA(ctx, plan->seg_dense_off.ensure(size_t(N + 1) * 8));
+        GBA_CUDA(ctx, plan->seg_dense.ensure(size_t(std::max<int64_t>(plan->seg_slots_total, 1)) * 16));
+        if (plan->cigar) {
+            if ((rc = upload(ctx, plan->cig_slot_off, cig_off))) return rc;
+            GBA_CUDA(ctx, plan->cig_slots.ensure(size_t(std::max<int64_t>(plan->cigar_slots_total, 1)) * 4));
+            GBA_CUDA(ctx, plan->cig_count.ensure(size_t(N + 1) * 4));
+            GBA_CUDA(ctx, plan->cig_count64.ensure(size_t(N + 1) * 8));
+            GBA_CUDA(ctx, plan->cig_dense_off.ensure(size_t(N + 1) * 8));
+            GBA_CUDA(ctx, plan->cig_dense.ensure(size_t(std::max<int64_t>(plan->cigar_slots_total, 1)) * 4));
+        }
+        size_t tmp = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tmp, (int64_t *)nullptr, (int64_t *)nullptr, int(N + 1));
+        plan->cub_tmp_bytes = tmp;
+        GBA_CUDA(ctx, plan->cub_tmp.ensure(tmp + 16));
+    }
+    plan->seg_dense_total = -1;
+    plan->cig_dense_total = -1;
+    return GBA_OK;
+}
+
+template <bool A, bool L, bool M, bool T>
+void launch_dp(const DpArgs &args, int grid, size_t smem, cudaStream_t s)
+{
+    k_dp_strip<A, L, M, T><<<grid, kBlock, smem, s>>>(args);
+}
+
+using DpLauncher = void (*)(const DpArgs &, int, size_t, cudaStream_t);
+
+DpLauncher pick_dp(bool a, bool l, bool m, bool t)
+{
+    static const DpLauncher table[16] = {
+        launch_dp<false, false, false, false>, launch_dp<false, false, false, true>,
+        launch_dp<false, false, true, false>,  launch_dp<false, false, true, true>,
+        launch_dp<false, true, false, false>,  launch_dp<false, true, false, true>,
+        launch_dp<false, true, true, false>,   launch_dp<false, true, true, true>,
+        launch_dp<true, false, false, false>,  launch_dp<true, false, false, true>,
+        launch_dp<true, false, true, false>,   launch_dp<true, false, true, true>,
+        launch_dp<true, true, false, false>,   launch_dp<true, true, false, true>,
+        launch_dp<true, true, true, false>,    launch_dp<true, true, true, true>};
+    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
+__global__ void k_widen(const int32_t *src, int64_t *dst, int64_t n)
+{
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+    if (i == n) dst[i] = 0;
+}
+
+// Invalid pairs: numeric_limits<T>::min() and an empty alignment
+// (align/dp_algorithm_impl.h:1399-1400).
+__global__ void k_fill_invalid(const PairDesc *pairs, int64_t n, int32_t minval, int32_t *score,
+                               int32_t *end_h, int32_t *end_v, int32_t *begin_h, int32_t *begin_v,
+                               int32_t *seg_count, int32_t *cig_count)
+{
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const PairDesc d = pairs[k];
+    if (d.m > 0 && d.n > 0) return;
+    score[k] = minval;
+    if (end_h) end_h[k] = 0;
+    if (end_v) end_v[k] = 0;
+    if (begin_h) begin_h[k] = 0;
+    if (begin_v) begin_v[k] = 0;
+    if (seg_count) seg_count[k] = 0;
+    if (cig_count) cig_count[k] = 0;
+}
+
+// Launches the kernels of a plan on device inputs.  Scores/end positions go to the given
+// device pointers; segments and CIGARs stay in the plan's device buffers.
+int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint8_t *dseq_v,
+             int32_t *dscore, int32_t *dend_h, int32_t *dend_v)
+{
+    const int64_t N = plan->num_pairs;
+    ctx->stats = gba_stats{};
+    ctx->stats.cells = plan->cells;
+    ctx->stats.trace_bytes = plan->trace_total;
+    if (N == 0) return GBA_OK;
+    int32_t *end_h = dend_h ? dend_h : plan->end_h.as<int32_t>();
+    int32_t *end_v = dend_v ? dend_v : plan->end_v.as<int32_t>();
+    const int32_t minval = plan->params.score_bits == 16 ? -32768 : INT32_MIN;
+    int launches = 0;
+
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    if (plan->num_slots > 0) {
+        DpArgs a{};
+        a.seq_h = dseq_h;
+        a.seq_v = dseq_v;
+        a.pairs = plan->pairs.as<PairDesc>();
+        a.order = plan->order.as<int32_t>();
+        a.warp_scratch = plan->warp_scratch.as<int64_t>();
+        a.scratch = plan->scratch.as<int2>();
+        a.trace = plan->traceback ? plan->trace.as<uint8_t>() : nullptr;
+        a.score = dscore;
+        a.end_h = end_h;
+        a.end_v = end_v;
+        a.best_e = plan->traceback ? plan->best_e.as<int32_t>() : nullptr;
+        a.best_f = plan->traceback ? plan->best_f.as<int32_t>() : nullptr;
+        a.matrix = plan->matrix ? plan->matrix_dev.as<int32_t>() : nullptr;
+        a.num_slots = plan->num_slots;
+        a.match = plan->params.match;
+        a.mismatch = plan->params.mismatch;
+        a.gap_open = plan->params.gap_open;
+        a.gap_extend = plan->params.gap_extend;
+        a.free_ends = plan->free_ends;
+        a.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
+        const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
+        const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
+        pick_dp(plan->affine, plan->local, plan->matrix, plan->traceback)(a, grid, smem, ctx->stream);
+        GBA_CUDA(ctx, cudaGetLastError());
+        ++launches;
+    }
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    {
+        const int grid = int((N + 255) / 256);
+        k_fill_invalid<<<grid, 256, 0, ctx->stream>>>(
+            plan->pairs.as<PairDesc>(), N, minval, dscore, end_h, end_v,
+            plan->traceback ? plan->begin_h.as<int32_t>() : nullptr,
+            plan->traceback ? plan->begin_v.as<int32_t>() : nullptr,
+            plan->traceback ? plan->seg_count.as<int32_t>() : nullptr,
+            plan->cigar ? plan->cig_count.as<int32_t>() : nullptr);
+        GBA_CUDA(ctx, cudaGetLastError());
+        ++launches;
+    }
+    if (plan->traceback) {
+        if (plan->num_slots > 0) {
+            TraceArgs t{};
+            t.pairs = plan->pairs.as<PairDesc>();
+            t.order = plan->order.as<int32_t>();
+            t.trace = plan->trace.as<uint8_t>();
+            t.score = dscore;
+            t.end_h = end_h;
+            t.end_v = end_v;
+            t.best_e = plan->best_e.as<int32_t>();
+            t.best_f = plan->best_f.as<int32_t>();
+            t.begin_h = plan->begin_h.as<int32_t>();
+            t.begin_v = plan->begin_v.as<int32_t>();
+            t.seg_slots = plan->seg_slots.as<uint32_t>();
+            t.seg_slot_off = plan->seg_slot_off.as<int64_t>();
+            t.seg_count = plan->seg_count.as<int32_t>();
+            t.cigar_slots = plan->cigar ? plan->cig_slots.as<uint32_t>() : nullptr;
+            t.cigar_slot_off = plan->cigar ? plan->cig_slot_off.as<int64_t>() : nullptr;
+            t.cigar_count = plan->cigar ? plan->cig_count.as<int32_t>() : nullptr;
+            t.num_slots = plan->num_slots;
+            t.affine = plan->affine;
+            t.local = plan->local;
+            const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
+            k_traceback<<<grid, kBlock, 0, ctx->stream>>>(t);
+            GBA_CUDA(ctx, cudaGetLastError());
+            ++launches;
+        }
+        // Dense packing: exclusive scan of the counts, then a copy per pair.
+        const int g1 = int((N + 1 + 255) / 256);
+        k_widen<<<g1, 256, 0, ctx->stream>>>(plan->seg_count.as<int32_t>(), plan->seg_count64.as<int64_t>(), N);
+        size_t tmp = plan->cub_tmp_bytes;
+        GBA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(plan->cub_tmp.ptr, tmp, plan->seg_count64.as<int64_t>(),
+                                                    plan->seg_dense_off.as<int64_t>(), int(N + 1), ctx->stream));
+        k_compact_u32<<<int((N + 7) / 8), 256, 0, ctx->stream>>>(
+            plan->seg_slots.as<uint32_t>(), plan->seg_slot_off.as<int64_t>(), plan->seg_count.as<int32_t>(),
+            plan->seg_dense_off.as<int64_t>(), plan->seg_dense.as<uint32_t>(), N, 4);
+        launches += 3;
+        if (plan->cigar) {
+            k_widen<<<g1, 256, 0, ctx->stream>>>(plan->cig_count.as<int32_t>(), plan->cig_count64.as<int64_t>(), N);
+            tmp = plan->cub_tmp_bytes;
+            GBA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(plan->cub_tmp.ptr, tmp, plan->cig_count64.as<int64_t>(),
+                                                        plan->cig_dense_off.as<int64_t>(), int(N + 1), ctx->stream));
+            k_compact_u32<<<int((N + 7) / 8), 256, 0, ctx->stream>>>(
+                plan->cig_slots.as<uint32_t>(), plan->cig_slot_off.as<int64_t>(), plan->cig_count.as<int32_t>(),
+                plan->cig_dense_off.as<int64_t>(), plan->cig_dense.as<uint32_t>(), N, 1);
+            launches += 3;
+        }
+        GBA_CUDA(ctx, cudaGetLastError());
+    }
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+    ctx->stats.kernel_launches = launches;
+    ctx->stats_pending = true;
+    plan->seg_dense_total = -1;
+    plan->cig_dense_total = -1;
+    return GBA_OK;
+}
+
+int finish_stats(gba_context *ctx)
+{
+    if (!ctx->stats_pending) return GBA_OK;
+    ctx->stats_pending = false;
+    GBA_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    float a = 0, b = 0;
+    GBA_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
+    GBA_CUDA(ctx, cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
+    ctx->stats.dp_kernel_ms = a;
+    ctx->stats.traceback_kernel_ms = b;
+    return GBA_OK;
+}
+
+// Copies segment/CIGAR outputs of a finished plan to host result buffers.
+int fetch_outputs(gba_context *ctx, gba_plan *plan, gba_result *r)
+{
+    const int64_t N = plan->num_pairs;
+    if (!plan->traceback || N == 0) {
+        if (plan->traceback && r->segment_offsets) r->segment_offsets[0] = 0;
+        if (plan->cigar && r->cigar_offsets) r->cigar_offsets[0] = 0;
+        return GBA_OK;
+    }
+    std::vector<int64_t> off(N + 1);
+    GBA_CUDA(ctx, cudaMemcpyAsync(off.data(), plan->seg_dense_off.ptr, (N + 1) * 8, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int64_t total = off[N];
+    if (r->segment_offsets) std::memcpy(r->segment_offsets, off.data(), (N + 1) * 8);
+    if (r->segments) {
+        if (total > r->segment_capacity)
+            return fail(ctx, GBA_ECAPACITY, "segment buffer holds %lld, need %lld", (long long)r->segment_capacity,
+                        (long long)total);
+        if (total > 0)
+            GBA_CUDA(ctx, cudaMemcpyAsync(r->segments, plan->seg_dense.ptr, total * 16, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+    }
+    if (r->begin_h)
+        GBA_CUDA(ctx, cudaMemcpyAsync(r->begin_h, plan->begin_h.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (r->begin_v)
+        GBA_CUDA(ctx, cudaMemcpyAsync(r->begin_v, plan->begin_v.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (plan->cigar) {
+        std::vector<int64_t> coff(N + 1);
+        GBA_CUDA(ctx, cudaMemcpyAsync(coff.data(), plan->cig_dense_off.ptr, (N + 1) * 8, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const int64_t ctotal = coff[N];
+        if (r->cigar_offsets) std::memcpy(r->cigar_offsets, coff.data(), (N + 1) * 8);
+        if (r->cigar) {
+            if (ctotal > r->cigar_capacity)
+                return fail(ctx, GBA_ECAPACITY, "cigar buffer holds %lld, need %lld", (long long)r->cigar_capacity,
+                            (long long)ctotal);
+            if (ctotal > 0)
+                GBA_CUDA(ctx, cudaMemcpyAsync(r->cigar, plan->cig_dense.ptr, ctotal * 4, cudaMemcpyDeviceToHost,
+                                              ctx->stream));
+        }
+    }
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GBA_OK;
+}
+
+}  // namespace
+
+// =======================================================================================
+// C-ABI
+// =======================================================================================
+extern "C" {
+
+GBA_API const char *gba_status_string(int s)
+{
+    switch (s) {
+    case GBA_OK: return "ok";
+    case GBA_EINVAL: return "invalid argument";
+    case GBA_ENOMEM: return "out of memory";
+    case GBA_EBUDGET: return "HBM budget exceeded";
+    case GBA_ECUDA: return "CUDA error";
+    case GBA_ETIMEOUT: return "timeout";
+    case GBA_EUNSUPPORTED: return "unsupported";
+    case GBA_ECAPACITY: return "output buffer too small";
+    default: return "unknown status";
+    }
+}
+
+GBA_API int gba_create(gba_context **out, const gba_config *cfg)
+{
+    if (!out) return GBA_EINVAL;
+    *out = nullptr;
+    std::unique_ptr<gba_context> ctx(new gba_context());
+    ctx->device = cfg ? cfg->device : 0;
+    ctx->budget = cfg ? cfg->hbm_budget_bytes : 0;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return GBA_ECUDA;
+    if (ctx->device < 0 || ctx->device >= ndev) return GBA_EINVAL;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GBA_ECUDA;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return GBA_ECUDA;
+    for (auto &ev : ctx->ev)
+        if (cudaEventCreate(&ev) != cudaSuccess) return GBA_ECUDA;
+    *out = ctx.release();
+    return GBA_OK;
+}
+
+GBA_API int gba_destroy(gba_context *ctx)
+{
+    if (!ctx) return GBA_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->oneshot.release();
+    ctx->seq_h.release();
+    ctx->seq_v.release();
+    ctx->out_score.release();
+    ctx->out_end_h.release();
+    ctx->out_end_v.release();
+    for (auto &ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GBA_OK;
+}
+
+GBA_API int gba_last_error(gba_context *ctx, char *buf, size_t size)
+{
+    if (!ctx || !buf || size == 0) return GBA_EINVAL;
+    std::snprintf(buf, size, "%s", ctx->last_error.c_str());
+    return GBA_OK;
+}
+
+GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gba_batch *batch,
+                            gba_result *result)
+{
+    if (!ctx || !result) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    gba_plan *plan = &ctx->oneshot;
+    int rc = build_plan(ctx, params, batch, plan);
+    if (rc) return rc;
+    const int64_t N = batch->num_pairs;
+    if (N == 0) {
+        if (plan->traceback && result->segment_offsets) result->segment_offsets[0] = 0;
+        if (plan->cigar && result->cigar_offsets) result->cigar_offsets[0] = 0;
+        return GBA_OK;
+    }
+    // Inputs: the concatenated codes as given.
+    GBA_CUDA(ctx, ctx->seq_h.ensure(size_t(plan->seq_h_bytes) + 16));
+    GBA_CUDA(ctx, ctx->seq_v.ensure(size_t(plan->seq_v_bytes) + 16));
+    if (plan->seq_h_bytes)
+        GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_h.ptr, batch->seq_h, plan->seq_h_bytes, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+    if (plan->seq_v_bytes)
+        GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_v.ptr, batch->seq_v, plan->seq_v_bytes, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+    GBA_CUDA(ctx, ctx->out_score.ensure(size_t(N) * 4));
+    rc = run_plan(ctx, plan, ctx->seq_h.as<uint8_t>(), ctx->seq_v.as<uint8_t>(), ctx->out_score.as<int32_t>(),
+                  nullptr, nullptr);
+    if (rc) return rc;
+    if (result->score)
+        GBA_CUDA(ctx, cudaMemcpyAsync(result->score, ctx->out_score.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (result->end_h)
+        GBA_CUDA(ctx, cudaMemcpyAsync(result->end_h, plan->end_h.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (result->end_v)
+        GBA_CUDA(ctx, cudaMemcpyAsync(result->end_v, plan->end_v.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    rc = fetch_outputs(ctx, plan, result);
+    if (rc) return rc;
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (result->pair_status) std::memcpy(result->pair_status, plan->status.data(), N * 4);
+    return finish_stats(ctx);
+}
+
+GBA_API int gba_plan_create(gba_context *ctx, const gba_params *params, const gba_batch *host_batch,
+                            gba_plan **out)
+{
+    if (!ctx || !out) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::unique_ptr<gba_plan> plan(new gba_plan());
+    int rc = build_plan(ctx, params, host_batch, plan.get());
+    if (rc) {
+        plan->release();
+        return rc;
+    }
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *out = plan.release();
+    return GBA_OK;
+}
+
+GBA_API int gba_plan_destroy(gba_context *ctx, gba_plan *plan)
+{
+    if (!plan) return GBA_OK;
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    plan->release();
+    delete plan;
+    return GBA_OK;
+}
+
+GBA_API int gba_plan_execute(gba_context *ctx, gba_plan *plan, const gba_batch *dev_batch, gba_result *dev_result)
+{
+    if (!ctx || !plan || !dev_batch || !dev_result) return GBA_EINVAL;
+    if (dev_batch->num_pairs != plan->num_pairs) return fail(ctx, GBA_EINVAL, "batch size differs from plan");
+    if (plan->num_pairs > 0 && !dev_result->score) return fail(ctx, GBA_EINVAL, "score output required");
+    return run_plan(ctx, plan, dev_batch->seq_h, dev_batch->seq_v, dev_result->score, dev_result->end_h,
+                    dev_result->end_v);
+}
+
+GBA_API int gba_plan_fetch(gba_context *ctx, gba_plan *plan, gba_result *host_result)
+{
+    if (!ctx || !plan || !host_result) return GBA_EINVAL;
+    int rc = fetch_outputs(ctx, plan, host_result);
+    if (rc) return rc;
+    if (host_result->pair_status && plan->num_pairs)
+        std::memcpy(host_result->pair_status, plan->status.data(), plan->num_pairs * 4);
+    return finish_stats(ctx);
+}
+
+GBA_API int gba_device_alloc(gba_context *ctx, void **ptr, size_t bytes)
+{
+    if (!ctx || !ptr) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    GBA_CUDA(ctx, cudaMalloc(ptr, std::max<size_t>(bytes, 16)));
+    return GBA_OK;
+}
+
+GBA_API int gba_device_free(gba_context *ctx, void *ptr)
+{
+    if (!ctx) return GBA_EINVAL;
+    if (ptr) GBA_CUDA(ctx, cudaFree(ptr));
+    return GBA_OK;
+}
+
+GBA_API int gba_host_alloc(gba_context *ctx, void **ptr, size_t bytes)
+{
+    if (!ctx || !ptr) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaMallocHost(ptr, std::max<size_t>(bytes, 16)));
+    return GBA_OK;
+}
+
+GBA_API int gba_host_free(gba_context *ctx, void *ptr)
+{
+    if (!ctx) return GBA_EINVAL;
+    if (ptr) GBA_CUDA(ctx, cudaFreeHost(ptr));
+    return GBA_OK;
+}
+
+GBA_API int gba_copy_to_device(gba_context *ctx, void *dst, const void *src, size_t bytes)
+{
+    if (!ctx) return GBA_EINVAL;
+    if (bytes) GBA_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return GBA_OK;
+}
+
+GBA_API int gba_copy_to_host(gba_context *ctx, void *dst, const void *src, size_t bytes)
+{
+    if (!ctx) return GBA_EINVAL;
+    if (bytes) GBA_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GBA_OK;
+}
+
+GBA_API int gba_synchronize(gba_context *ctx)
+{
+    if (!ctx) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GBA_OK;
+}
+
+GBA_API int gba_timer_start(gba_context *ctx)
+{
+    if (!ctx) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+    return GBA_OK;
+}
+
+GBA_API int gba_timer_stop(gba_context *ctx, float *ms)
+{
+    if (!ctx || !ms) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+    GBA_CUDA(ctx, cudaEventSynchronize(ctx->ev[5]));
+    GBA_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev[4], ctx->ev[5]));
+    return GBA_OK;
+}
+
+GBA_API int gba_measure_int_peak(gba_context *ctx, double *tops)
+{
+    if (!ctx || !tops) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    int sms = 0;
+    GBA_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    DevBuf out;
+    GBA_CUDA(ctx, out.ensure(64));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    k_int_peak<<<blocks, threads, 0, ctx->stream>>>(out.as<int32_t>(), iters, 5);  // warm-up
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[4], ctx->stream));
+    k_int_peak<<<blocks, threads, 0, ctx->stream>>>(out.as<int32_t>(), iters, 7);
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[5], ctx->stream));
+    GBA_CUDA(ctx, cudaEventSynchronize(ctx->ev[5]));
+    float ms = 0;
+    GBA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]));
+    out.release();
+    // 16 accumulators x 2 updates x (add + max) per iteration.
+    const double ops = double(blocks) * threads * iters * 16.0 * 2.0 * 2.0;
+    *tops = ops / (ms * 1e-3) / 1e12;
+    return GBA_OK;
+}
+
+GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
+{
+    if (!ctx || !stats) return GBA_EINVAL;
+    int rc = finish_stats(ctx);
+    if (rc) return rc;
+    *stats = ctx->stats;
+    return GBA_OK;
+}
+
+}  // extern "C"

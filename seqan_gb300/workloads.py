@@ -1,0 +1,130 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+There is no public dataset for this path; these generators stand in for it:
+
+* ``uniform_dna_pairs``   -- independent uniform ACGT pairs (the plain 1024 x 150 bp case).
+* ``mutated_dna_pairs``   -- reads of uniform length in [lo, hi]; the partner is the read with
+  per-position substitutions (to one of the 3 other bases) and single-base indels (50/50
+  insertion/deletion, inserted base uniform).
+* ``protein_pairs``       -- log-normal lengths (median 300, sigma 0.5, clipped to [50, 1000]),
+  residues i.i.d. from BACKGROUND_AA; a fraction of pairs is derived by substitution to a target
+  identity.
+* ``read_windows``        -- reads sampled from a random reference with substitutions and indels,
+  each paired with a reference window around its true origin.
+* ``serving_lengths``     -- the mixed length distribution of the serving workload.
+All generators use numpy's PCG64 with the given seed.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# Residue composition used for i.i.d. protein sequences over the 20 standard amino acids, as
+# AminoAcid codes (A=0 ... Y=23).  Stand-in for "standard background frequencies": the counts
+# are the residue composition of the protein FASTA files shipped with the reference's
+# T-Coffee app tests, counted by tests/golden/make_golden.py.
+AA20_CODES = np.array([0, 2, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 15, 16, 17, 18, 19, 21, 22, 23], dtype=np.uint8)
+BACKGROUND_AA_COUNTS = None  # filled from tests/golden/aa_background.json by load_background()
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def uniform_dna_pairs(n: int, length: int, seed: int = 1):
+    rng = _rng(seed)
+    H = rng.integers(0, 4, size=(n, length), dtype=np.uint8)
+    V = rng.integers(0, 4, size=(n, length), dtype=np.uint8)
+    return list(H), list(V)
+
+
+def mutate(rng, seq: np.ndarray, sub_rate: float, indel_rate: float, alphabet: int = 4) -> np.ndarray:
+    """Substitutions to a different symbol and single-symbol insertions/deletions."""
+    s = seq.copy()
+    L = len(s)
+    subs = rng.random(L) < sub_rate
+    if subs.any():
+        shift = rng.integers(1, alphabet, size=int(subs.sum()), dtype=np.uint8)
+        s[subs] = (s[subs] + shift) % alphabet
+    ev = rng.random(L) < indel_rate
+    if not ev.any():
+        return s
+    ins = rng.random(L) < 0.5
+    out = []
+    prev = 0
+    for pos in np.nonzero(ev)[0]:
+        out.append(s[prev:pos])
+        if ins[pos]:
+            out.append(rng.integers(0, alphabet, size=1, dtype=np.uint8))
+            out.append(s[pos:pos + 1])
+        prev = pos + 1
+    out.append(s[prev:])
+    return np.concatenate(out).astype(np.uint8)
+
+
+def mutated_dna_pairs(n: int, lo: int = 100, hi: int = 300, sub_rate: float = 0.05,
+                      indel_rate: float = 0.01, seed: int = 2):
+    rng = _rng(seed)
+    lens = rng.integers(lo, hi + 1, size=n)
+    H, V = [], []
+    for L in lens:
+        h = rng.integers(0, 4, size=int(L), dtype=np.uint8)
+        H.append(h)
+        V.append(mutate(rng, h, sub_rate, indel_rate))
+    return H, V
+
+
+def load_background():
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    path = os.path.join(os.path.dirname(here), "tests", "golden", "aa_background.json")
+    with open(path) as f:
+        d = json.load(f)
+    counts = np.array([d["counts"][c] for c in "ACDEFGHIKLMNPQRSTVWY"], dtype=np.float64)
+    return counts / counts.sum()
+
+
+def protein_pairs(n: int, median: int = 300, sigma: float = 0.5, lo: int = 50, hi: int = 1000,
+                  related: float = 0.3, identity: float = 0.4, seed: int = 3, background=None):
+    rng = _rng(seed)
+    p = load_background() if background is None else background
+
+    def draw_len():
+        return int(np.clip(np.round(np.exp(np.log(median) + sigma * rng.standard_normal())), lo, hi))
+
+    H, V = [], []
+    for _ in range(n):
+        h = AA20_CODES[rng.choice(20, size=draw_len(), p=p)]
+        if rng.random() < related:
+            v = h.copy()
+            subs = rng.random(len(v)) >= identity
+            v[subs] = AA20_CODES[rng.choice(20, size=int(subs.sum()), p=p)]
+        else:
+            v = AA20_CODES[rng.choice(20, size=draw_len(), p=p)]
+        H.append(h)
+        V.append(v)
+    return H, V
+
+
+def read_windows(n_reads: int, ref_len: int = 10_000_000, read_len: int = 150, flank: int = 10,
+                 sub_rate: float = 0.02, indel_rate: float = 0.002, seed: int = 4):
+    """Reads with their reference windows ref[o - flank, o + read_len + flank)."""
+    rng = _rng(seed)
+    ref = rng.integers(0, 4, size=ref_len, dtype=np.uint8)
+    origins = rng.integers(flank, ref_len - read_len - flank, size=n_reads)
+    win_len = read_len + 2 * flank
+    idx = (origins - flank)[:, None] + np.arange(win_len)[None, :]
+    windows = ref[idx]
+    reads = []
+    for k in range(n_reads):
+        r = ref[origins[k]:origins[k] + read_len]
+        reads.append(mutate(rng, r, sub_rate, indel_rate)[:read_len + 2])
+    return list(windows), reads
+
+
+def serving_lengths(n: int, seed: int = 5):
+    rng = _rng(seed)
+    u = rng.random(n)
+    lens = np.where(u < 0.90, rng.integers(100, 501, size=n),
+                    np.where(u < 0.99, rng.integers(1000, 5001, size=n), 10_000))
+    return lens

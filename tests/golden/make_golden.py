@@ -1,0 +1,165 @@
+"""Generates the golden fixtures in tests/golden/ from the compiled reference.
+
+Run where the reference tree exists (it builds oracle/_ref/ from its headers):
+    python tests/golden/make_golden.py
+Outputs (all small, committed):
+  reference_cases.json  seeded inputs with the reference's outputs: batch scores through
+                        ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
+                        CIGARs, and raw TraceSegment_ lists of the single-pair DP.
+  blosum62.json         the reference's 27x27 Blosum62 table (score/score_matrix_data.h).
+  alphabets.json        the reference's char -> ordValue maps for Dna5, Dna and AminoAcid.
+  aa_background.json    residue counts of the reference's T-Coffee test FASTA files, the
+                        stand-in for background amino-acid frequencies.
+"""
+from __future__ import annotations
+
+import collections
+import glob
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+REFERENCE = "/root/reference"
+
+from oracle import oracle as O  # noqa: E402
+
+DNA = "ACGTN"
+AA = "ABCDEFGHIJKLMNOPQRSTUVWYZX*"
+
+
+def text(codes, alphabet):
+    letters = AA if alphabet == "aa" else DNA
+    return "".join(letters[int(c)] for c in codes)
+
+
+def problem_dict(pb: O.Problem):
+    return {"mode": pb.mode, "free_ends": pb.free_ends, "band": list(pb.band) if pb.band else None,
+            "match": pb.match, "mismatch": pb.mismatch, "gap_open": pb.gap_open,
+            "gap_extend": pb.gap_extend, "blosum62": pb.matrix is not None,
+            "score_bits": pb.score_bits, "alphabet": pb.alphabet}
+
+
+def rand_pairs(rng, n, lo, hi, alphabet, related=0.5):
+    H, V = [], []
+    for _ in range(n):
+        if alphabet == "dna":
+            h = rng.integers(0, 4, rng.integers(lo, hi + 1)).astype(np.uint8)
+        else:
+            h = rng.choice(np.array([0, 2, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 15, 16, 17, 18, 19, 21, 22, 23],
+                                    dtype=np.uint8), rng.integers(lo, hi + 1))
+        if rng.random() < related:
+            v = h.copy()
+            sub = rng.random(len(v)) < 0.15
+            v[sub] = (v[sub] + 1) % (4 if alphabet == "dna" else 20)
+            if len(v) > 4 and rng.random() < 0.7:
+                a = rng.integers(0, len(v) - 2)
+                v = np.concatenate([v[:a], v[a + rng.integers(1, 3):]]) if rng.random() < 0.5 else \
+                    np.concatenate([v[:a], h[:rng.integers(1, 4)], v[a:]])
+        else:
+            lv = rng.integers(lo, hi + 1)
+            v = rng.integers(0, 4, lv).astype(np.uint8) if alphabet == "dna" else \
+                rng.integers(0, 20, lv).astype(np.uint8)
+        H.append(h.astype(np.uint8))
+        V.append(v.astype(np.uint8))
+    return H, V
+
+
+DNA_SCORES = [(2, -3, -5, -5), (2, -4, -6, -1), (4, -2, -10, -4), (2, -1, -1, -1)]  # match, mismatch, open, extend
+FREE_END_SETS = [0, 15, 9, 6]
+
+
+def main():
+    if not os.path.isdir(REFERENCE):
+        sys.exit("the reference tree is needed to generate fixtures")
+    if not O.ref_available():
+        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"-j{os.cpu_count()}"])
+    rng = np.random.Generator(np.random.PCG64(20261203))
+    cases = []
+    b62 = O.ref_blosum62()
+
+    def add(kind, pb, H, V):
+        alph = pb.alphabet
+        case = {"kind": kind, "problem": problem_dict(pb),
+                "H": [text(h, alph) for h in H], "V": [text(v, alph) for v in V]}
+        if kind == "score":
+            case["scores"] = [int(x) for x in O.ref_batch_score(pb, H, V, threads=2)]
+        elif kind == "gaps":
+            sc, clip, rows, cig = O.ref_batch_gaps(pb, H, V, threads=2, cigar=True)
+            case["scores"] = [int(x) for x in sc]
+            case["clip"] = [[int(x) for x in c] for c in clip]
+            case["rows"] = [list(r) for r in rows]
+            case["cigar"] = cig
+        else:
+            segs, scores = [], []
+            for h, v in zip(H, V):
+                s, sg = O.ref_pair_segments(pb, h, v)
+                scores.append(int(s))
+                segs.append([list(x) for x in sg])
+            case["scores"] = scores
+            case["segments"] = segs
+        cases.append(case)
+
+    # Batch scores (SIMD batch path).
+    for bits in (16, 32):
+        for (mt, mm, go, ge) in DNA_SCORES:
+            H, V = rand_pairs(rng, 48, 1, 70, "dna")
+            for fe in FREE_END_SETS:
+                add("score", O.Problem("global", fe, None, mt, mm, go, ge, None, bits, "dna"), H, V)
+            add("score", O.Problem("local", 0, None, mt, mm, go, ge, None, bits, "dna"), H, V)
+    for fe in FREE_END_SETS:
+        H, V = rand_pairs(rng, 32, 1, 90, "aa")
+        add("score", O.Problem("global", fe, None, 0, 0, -11, -1, b62, 16, "aa"), H, V)
+    H, V = rand_pairs(rng, 32, 1, 90, "aa")
+    add("score", O.Problem("local", 0, None, 0, 0, -11, -1, b62, 16, "aa"), H, V)
+    # Batch Gaps (SIMD batch path with traceback) + CIGAR.
+    for (mt, mm, go, ge) in DNA_SCORES[:3]:
+        H, V = rand_pairs(rng, 32, 1, 60, "dna")
+        for fe in FREE_END_SETS:
+            add("gaps", O.Problem("global", fe, None, mt, mm, go, ge, None, 16, "dna"), H, V)
+        add("gaps", O.Problem("local", 0, None, mt, mm, go, ge, None, 16, "dna"), H, V)
+        add("gaps", O.Problem("global", 0, None, mt, mm, go, ge, None, 32, "dna"), H, V)
+    for fe in FREE_END_SETS:
+        H, V = rand_pairs(rng, 24, 1, 80, "aa")
+        add("gaps", O.Problem("global", fe, None, 0, 0, -11, -1, b62, 16, "aa"), H, V)
+    H, V = rand_pairs(rng, 24, 1, 80, "aa")
+    add("gaps", O.Problem("local", 0, None, 0, 0, -11, -1, b62, 16, "aa"), H, V)
+    # Raw segment lists (single-pair DP), all 16 AlignConfigs.
+    for (mt, mm, go, ge) in DNA_SCORES:
+        H, V = rand_pairs(rng, 12, 1, 40, "dna")
+        for fe in range(16):
+            add("segments", O.Problem("global", fe, None, mt, mm, go, ge, None, 32, "dna"), H, V)
+        add("segments", O.Problem("local", 0, None, mt, mm, go, ge, None, 32, "dna"), H, V)
+
+    with open(os.path.join(HERE, "reference_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261203,
+                   "ref_simd_bytes": int(O.libref().ref_simd_bytes()), "cases": cases}, f, separators=(",", ":"))
+    with open(os.path.join(HERE, "blosum62.json"), "w") as f:
+        json.dump({"alphabet": AA, "matrix": b62.tolist()}, f)
+    printable = "".join(chr(i) for i in range(32, 127))
+    with open(os.path.join(HERE, "alphabets.json"), "w") as f:
+        json.dump({"chars": printable,
+                   "dna5": O.ref_encode("dna5", printable).tolist(),
+                   "dna": O.ref_encode("dna", printable).tolist(),
+                   "aa": O.ref_encode("aa", printable).tolist()}, f)
+    files = sorted(glob.glob(os.path.join(REFERENCE, "apps/seqan_tcoffee/tests/*.fa")) +
+                   glob.glob(os.path.join(REFERENCE, "apps/seqan_tcoffee/tests/*.fasta")))
+    cnt = collections.Counter()
+    for fn in files:
+        with open(fn) as fh:
+            for line in fh:
+                if not line.startswith(">"):
+                    cnt.update(c for c in line.strip().upper() if c in "ACDEFGHIKLMNPQRSTVWY")
+    with open(os.path.join(HERE, "aa_background.json"), "w") as f:
+        json.dump({"source": "apps/seqan_tcoffee/tests/*.fa, *.fasta of the reference tree",
+                   "files": len(files), "counts": {c: cnt[c] for c in "ACDEFGHIKLMNPQRSTVWY"}}, f)
+    print(f"{len(cases)} cases written")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+"""GPU parity: the engine (through the C-ABI) against the reference's fixtures and the oracle.
+
+Everything is integer arithmetic, so every comparison is exact: scores, best-cell positions,
+raw TraceSegment_ lists, begin positions and CIGARs."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SCORE_CASES = G.cases("score")
+GAPS_CASES = G.cases("gaps")
+SEG_CASES = G.cases("segments")
+
+
+def run_engine(p, H, V, traceback=False, cigar=False):
+    import seqan_gb300 as sg
+    score, mode, cfg, band = G.engine_args(p)
+    return sg.align_codes(H, V, score, mode=mode, config=cfg, band=band, traceback=traceback, cigar=cigar)
+
+
+@pytest.mark.parametrize("case", SCORE_CASES, ids=[G.case_id(c) for c in SCORE_CASES])
+def test_scores_match_reference_fixture(engine, case):
+    p = case["problem"]
+    H, V = G.codes(case["H"], p["alphabet"]), G.codes(case["V"], p["alphabet"])
+    out = run_engine(p, H, V)
+    assert out.score.tolist() == case["scores"]
+
+
+@pytest.mark.parametrize("case", GAPS_CASES, ids=[G.case_id(c) for c in GAPS_CASES])
+def test_gaps_and_cigar_match_reference_fixture(engine, case):
+    p = case["problem"]
+    H, V = G.codes(case["H"], p["alphabet"]), G.codes(case["V"], p["alphabet"])
+    out = run_engine(p, H, V, traceback=True, cigar=True)
+    assert out.score.tolist() == case["scores"]
+    for k in range(len(H)):
+        segs = out.pair_segments(k)
+        assert list(O.render_rows(segs, case["H"][k], case["V"][k])) == case["rows"][k], k
+        assert list(O.segments_clip(segs)) == case["clip"][k], k
+        assert out.pair_cigar(k) == case["cigar"][k], k
+
+
+@pytest.mark.parametrize("case", SEG_CASES, ids=[G.case_id(c) for c in SEG_CASES])
+def test_segments_match_reference_fixture(engine, case):
+    p = case["problem"]
+    H, V = G.codes(case["H"], p["alphabet"]), G.codes(case["V"], p["alphabet"])
+    out = run_engine(p, H, V, traceback=True)
+    assert out.score.tolist() == case["scores"]
+    for k in range(len(H)):
+        assert [list(s) for s in out.pair_segments(k)] == case["segments"][k], k
+
+
+def _random_pairs(seed, n, lo, hi, alpha=4):
+    rng = np.random.default_rng(seed)
+    H = [rng.integers(0, alpha, rng.integers(lo, hi + 1)).astype(np.uint8) for _ in range(n)]
+    V = []
+    for h in H:
+        if rng.random() < 0.5:
+            v = h.copy()
+            m = rng.random(len(v)) < 0.1
+            v[m] = (v[m] + 1) % alpha
+            V.append(v)
+        else:
+            V.append(rng.integers(0, alpha, rng.integers(lo, hi + 1)).astype(np.uint8))
+    return H, V
+
+
+SCHEMES = [(2, -3, -5, -5), (2, -4, -6, -1), (4, -2, -10, -4), (1, -1, -2, -2), (3, -2, -4, -4)]
+
+
+@pytest.mark.parametrize("fe", range(16))
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_all_free_end_configs_against_oracle(engine, fe, scheme):
+    import seqan_gb300 as sg
+    mt, mm, go, ge = scheme
+    H, V = _random_pairs(100 + fe, 150, 1, 90)
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    for bits, dtype in ((16, np.int16), (32, np.int32)):
+        out = sg.align_codes(H, V, sg.Score(mt, mm, ge, go, dtype=dtype), config=cfg, traceback=True, cigar=True)
+        ref = O.oracle_batch(O.Problem("global", fe, None, mt, mm, go, ge, None, bits), H, V, traceback=True)
+        assert np.array_equal(out.score, ref.score)
+        assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+        for k in range(len(H)):
+            assert out.pair_segments(k) == ref.segments[k], k
+            assert out.pair_cigar(k) == O.cigar_string(ref.segments[k]), k
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_local_against_oracle(engine, scheme):
+    import seqan_gb300 as sg
+    mt, mm, go, ge = scheme
+    H, V = _random_pairs(7, 300, 1, 160)
+    out = sg.align_codes(H, V, sg.Score(mt, mm, ge, go, dtype=np.int16), mode=1, traceback=True)
+    ref = O.oracle_batch(O.Problem("local", 0, None, mt, mm, go, ge, None, 16), H, V, traceback=True)
+    assert np.array_equal(out.score, ref.score)
+    assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+    for k in range(len(H)):
+        assert out.pair_segments(k) == ref.segments[k], k
+
+
+def test_blosum62_local_protein_against_oracle(engine):
+    import seqan_gb300 as sg
+    from seqan_gb300 import workloads as W
+    H, V = W.protein_pairs(60, median=200, seed=11)
+    sc = sg.Blosum62(-1, -11, dtype=np.int16)
+    out = sg.align_codes(H, V, sc, mode=1, traceback=True)
+    ref = O.oracle_batch(O.Problem("local", 0, None, 0, 0, -11, -1, sc.matrix, 16, "aa"), H, V, traceback=True)
+    assert np.array_equal(out.score, ref.score)
+    for k in range(len(H)):
+        assert out.pair_segments(k) == ref.segments[k], k
+
+
+def test_invalid_pairs_and_empty_batch(engine):
+    import seqan_gb300 as sg
+    e = np.zeros(0, np.uint8)
+    a = np.array([0, 1, 2, 3], np.uint8)
+    out = sg.align_codes([e, a, a], [a, e, a], sg.Score(2, -3, -5, dtype=np.int16), traceback=True, cigar=True)
+    assert out.score.tolist()[:2] == [-32768, -32768]
+    assert out.score[2] == 8
+    assert out.status.tolist()[:2] == [1, 1]
+    assert out.pair_segments(0) == [] and out.pair_cigar(1) == ""
+    out = sg.align_codes([], [], sg.Score(2, -3, -5))
+    assert len(out.score) == 0
+
+
+def test_int16_promotion_is_exact(engine):
+    """Pairs whose values can leave the exact int16 range run with 32-bit cells."""
+    import seqan_gb300 as sg
+    H, V = _random_pairs(5, 6, 3000, 5000)
+    out = sg.align_codes(H, V, sg.Score(2, -4, -1, -6, dtype=np.int16))
+    ref = O.oracle_batch(O.Problem("global", 0, None, 2, -4, -6, -1, None, 32), H, V)
+    assert np.array_equal(out.score, ref.score)
+    assert (out.status == 2).all()
+
+
+def test_one_vs_many(engine):
+    import seqan_gb300 as sg
+    H, V = _random_pairs(9, 50, 20, 80)
+    h = H[0]
+    got = sg.globalAlignmentScore("".join("ACGT"[c] for c in h), ["".join("ACGT"[c] for c in v) for v in V],
+                                  sg.Score(2, -3, -5))
+    ref = O.oracle_batch(O.Problem(), [h] * len(V), V)
+    assert got.tolist() == ref.score.tolist()
+
+
+def test_python_interface_gaps(engine):
+    """globalAlignment over Gaps fills rows like the reference's KAT (AlignConfig<>, NW)."""
+    import seqan_gb300 as sg
+    gH, gV = sg.Gaps("ATGT"), sg.Gaps("ATAGAT")
+    sc = sg.globalAlignment([gH], [gV], sg.Score(2, -1, -1))
+    assert int(sc[0]) == 6
+    assert (gH.row(), gV.row()) == ("AT-G-T", "ATAGAT")
