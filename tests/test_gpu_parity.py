@@ -126,13 +126,17 @@ def test_invalid_pairs_and_empty_batch(engine):
 
 
 def test_int16_promotion_is_exact(engine):
-    """Pairs whose values can leave the exact int16 range run with 32-bit cells."""
+    """Pairs whose values can leave the exact int16 range run with 32-bit cells; pairs inside it
+    keep 16-bit semantics.  Score(2,-4,-1,-6): 8,000+ bp pairs can fall below the int16
+    "infinity" (-16384), 300 bp pairs cannot."""
     import seqan_gb300 as sg
-    H, V = _random_pairs(5, 6, 3000, 5000)
+    Hl, Vl = _random_pairs(5, 3, 8000, 9000)
+    Hs, Vs = _random_pairs(6, 3, 200, 300)
+    H, V = Hl + Hs, Vl + Vs
     out = sg.align_codes(H, V, sg.Score(2, -4, -1, -6, dtype=np.int16))
     ref = O.oracle_batch(O.Problem("global", 0, None, 2, -4, -6, -1, None, 32), H, V)
     assert np.array_equal(out.score, ref.score)
-    assert (out.status == 2).all()
+    assert out.status.tolist() == [2, 2, 2, 0, 0, 0]
 
 
 def test_one_vs_many(engine):
