@@ -127,10 +127,10 @@ def test_invalid_pairs_and_empty_batch(engine):
 
 def test_int16_promotion_is_exact(engine):
     """Pairs whose values can leave the exact int16 range run with 32-bit cells; pairs inside it
-    keep 16-bit semantics.  Score(2,-4,-1,-6): 8,000+ bp pairs can fall below the int16
+    keep 16-bit semantics.  Score(2,-4,-1,-6): 9,000+ bp pairs can fall below the int16
     "infinity" (-16384), 300 bp pairs cannot."""
     import seqan_gb300 as sg
-    Hl, Vl = _random_pairs(5, 3, 8000, 9000)
+    Hl, Vl = _random_pairs(5, 3, 9000, 10000)
     Hs, Vs = _random_pairs(6, 3, 200, 300)
     H, V = Hl + Hs, Vl + Vs
     out = sg.align_codes(H, V, sg.Score(2, -4, -1, -6, dtype=np.int16))
