@@ -185,6 +185,38 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
  * benchmark reports the DP kernels against. */
 GBA_API int gba_measure_int_peak(gba_context *ctx, double *tops);
 
+/* --- Allocation-free scores ------------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory on the
+ * call path: hosts whose device memory all comes from their own pool (a database or plugin
+ * host that hands out buffers) and latency-bound request loops that keep cudaMalloc/cudaFree
+ * -- which can synchronize the device and take unbounded time -- out of their requests.
+ * The caller passes DEVICE pointers for inputs and outputs; the call needs no gba_context and
+ * makes no allocation of any kind.  The DP's scratch is a static device array of
+ * GBA_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit; one warp of
+ * lanes needs 32 * (max_h_len + 1) * 8 bytes of it, and a max_h_len that does not fit is
+ * refused with GBA_ECAPACITY.  Pairs longer than max_h_len are not computed and come back
+ * with score numeric_limits<T>::min() and GBA_PAIR_INVALID.  Scores and end positions only
+ * (no band, no traceback): the same values gba_align_batch returns.
+ * The first call on a device looks up the array's device address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race and must be
+ * serialized by the caller.  Asynchronous on `stream` (a cudaStream_t; NULL = legacy default
+ * stream). */
+#define GBA_NOALLOC_SCRATCH_BYTES (64u << 20)
+
+typedef struct {
+    int64_t num_pairs;
+    const uint8_t *seq_h;      /* device: concatenated H codes */
+    const int64_t *off_h;      /* device: num_pairs + 1 offsets */
+    const uint8_t *seq_v;      /* device */
+    const int64_t *off_v;      /* device */
+    int32_t max_h_len;         /* caller's bound on every |H| in the batch */
+    int32_t reserved;
+} gba_noalloc_batch;
+
+GBA_API int gba_align_score_noalloc(const gba_params *params, const gba_noalloc_batch *batch,
+                                    int32_t *score, int32_t *end_h, int32_t *end_v,
+                                    int32_t *pair_status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,13 +28,14 @@ GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE = 0, 1, 2
 GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
 GBA_OUT_SCORE, GBA_OUT_END, GBA_OUT_SEGMENTS, GBA_OUT_CIGAR = 1, 2, 4, 8
 GBA_SEG_DIAGONAL, GBA_SEG_HORIZONTAL, GBA_SEG_VERTICAL = 1, 2, 4
+GBA_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 # Every symbol include/seqan_gb300.h declares.
 EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", "gba_align_batch",
             "gba_plan_create", "gba_plan_destroy", "gba_plan_execute", "gba_plan_fetch",
             "gba_device_alloc", "gba_device_free", "gba_host_alloc", "gba_host_free",
             "gba_copy_to_device", "gba_copy_to_host", "gba_synchronize", "gba_timer_start",
-            "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak"]
+            "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc"]
 
 
 class GbaConfig(C.Structure):
@@ -63,6 +64,12 @@ class GbaResult(C.Structure):
                 ("cigar_capacity", C.c_int64), ("cigar_offsets", C.c_void_p)]
 
 
+class GbaNoAllocBatch(C.Structure):
+    _fields_ = [("num_pairs", C.c_int64), ("seq_h", C.c_void_p), ("off_h", C.c_void_p),
+                ("seq_v", C.c_void_p), ("off_v", C.c_void_p), ("max_h_len", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class GbaStats(C.Structure):
     _fields_ = [("dp_kernel_ms", C.c_float), ("traceback_kernel_ms", C.c_float),
                 ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64)]
@@ -81,7 +88,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB_PATH
     os.makedirs(LIB_DIR, exist_ok=True)
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    cmd = ["nvcc", *NVCC_FLAGS, "-o", tmp, os.path.join(CSRC, "engine.cu")]
+    units = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith(".cu")]
+    cmd = ["nvcc", *NVCC_FLAGS, "-o", tmp, *units]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)
@@ -124,6 +132,8 @@ def lib():
             L.gba_timer_stop.argtypes = [vp, C.POINTER(C.c_float)]
             L.gba_get_stats.argtypes = [vp, C.POINTER(GbaStats)]
             L.gba_measure_int_peak.argtypes = [vp, C.POINTER(C.c_double)]
+            L.gba_align_score_noalloc.argtypes = [C.POINTER(GbaParams), C.POINTER(GbaNoAllocBatch), vp, vp,
+                                                  vp, vp, vp]
             _lib = L
     return _lib
 
