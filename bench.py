@@ -180,6 +180,8 @@ def main():
     ap.add_argument("--workload", default="affine_dna_100k", choices=sorted(WORKLOADS))
     ap.add_argument("--ref-pairs", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16"],
+                    help="auto: packed 16-bit kernel (32-row strips) where eligible")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -232,7 +234,9 @@ def main():
     as_np(p_ov, ov.size, np.int64)[:] = ov
     p_score, p_eh, p_ev = pinned(npairs * 4), pinned(npairs * 4), pinned(npairs * 4)
 
-    params = sg.align.make_params(score, mode, None, None, N.GBA_OUT_SCORE | N.GBA_OUT_END)
+    flags = {"auto": 0, "general": N.GBA_FLAG_GENERAL_KERNEL, "packed16": N.GBA_FLAG_STRIP16}[args.kernel]
+    params = sg.align.make_params(score, mode, None, None, N.GBA_OUT_SCORE | N.GBA_OUT_END,
+                                  alphabet_size=4, flags=flags)
     host_batch = N.GbaBatch(npairs, p_sh, p_oh, p_sv, p_ov, 0, 0)
 
     # Device-resident inputs for `value`.
@@ -312,7 +316,8 @@ def main():
     achieved = ops / (dp_avg_ms * 1e-3) / 1e12
     roofline = {"bound": "int32", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
                 "frac": achieved / peak.value if peak.value else None, "traffic": None,
-                "kernel": "k_dp_strip", "ops_per_cell": OPS_PER_CELL[kind],
+                "kernel": "k_dp_strip (one pair per thread, int32)" if args.kernel == "general" else
+                          "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)", "ops_per_cell": OPS_PER_CELL[kind],
                 "dp_kernel_ms": dp_avg_ms,
                 "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"}
 
@@ -322,6 +327,7 @@ def main():
             "dtype": "int16" if score.bits == 16 else "int32", "data": "synthetic",
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "pairs": npairs,
                        "cells_per_step": cells, "l2": "flushed (256 MiB write) between timed steps",
+                       "kernel": args.kernel,
                        "parallelism": f"replicas x{world} (pairs are independent)"},
             "e2e": {"value": e2e_gcups, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * sum(e2e_s) / len(e2e_s)},

@@ -89,11 +89,21 @@ typedef struct {
     int32_t gap_open, gap_extend;  /* a gap of length k costs gap_open + (k-1) * gap_extend */
     const int32_t *matrix;     /* optional alphabet_size^2 substitution table (row = H code),
                                   e.g. the 27x27 Blosum62 of score/score_matrix_data.h */
-    int32_t alphabet_size;     /* codes must be < alphabet_size (<= 32) when matrix != NULL */
+    int32_t alphabet_size;     /* codes are < alphabet_size (<= 32 with a matrix); 0 = unknown */
     int32_t score_bits;        /* 16 or 32: the reference's TScoreValue width */
     int32_t outputs;           /* GBA_OUT_* bits */
-    int32_t reserved[3];
+    int32_t flags;             /* GBA_FLAG_* kernel selection (0 = automatic) */
+    int32_t reserved[2];
 } gba_params;
+
+/* Kernel selection flags (gba_params.flags); results are identical either way.
+ * With equality scoring the engine uses its packed two-pairs-per-thread 16-bit kernel when
+ * alphabet_size is between 1 and 8 (the caller's promise that every code is below it, as the
+ * reference's alphabet types guarantee) and the pair's values stay in the exact int16 range. */
+enum {
+    GBA_FLAG_GENERAL_KERNEL = 1,   /* force the one-pair-per-thread 32-bit kernel */
+    GBA_FLAG_STRIP16 = 2           /* packed kernel with 16-row strips instead of 32 */
+};
 
 /* A batch: concatenated residue codes with n+1 offsets for each side. */
 typedef struct {

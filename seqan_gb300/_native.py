@@ -29,6 +29,7 @@ GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
 GBA_OUT_SCORE, GBA_OUT_END, GBA_OUT_SEGMENTS, GBA_OUT_CIGAR = 1, 2, 4, 8
 GBA_SEG_DIAGONAL, GBA_SEG_HORIZONTAL, GBA_SEG_VERTICAL = 1, 2, 4
 GBA_NOALLOC_SCRATCH_BYTES = 64 << 20
+GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16 = 1, 2
 
 # Every symbol include/seqan_gb300.h declares.
 EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", "gba_align_batch",
@@ -47,7 +48,8 @@ class GbaParams(C.Structure):
                 ("band_on", C.c_int32), ("band_lower", C.c_int32), ("band_upper", C.c_int32),
                 ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
                 ("gap_extend", C.c_int32), ("matrix", C.c_void_p), ("alphabet_size", C.c_int32),
-                ("score_bits", C.c_int32), ("outputs", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("score_bits", C.c_int32), ("outputs", C.c_int32), ("flags", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class GbaBatch(C.Structure):

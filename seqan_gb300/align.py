@@ -113,7 +113,8 @@ def _vp(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
-def make_params(score, mode: int, config: AlignConfig | None, band, outputs: int) -> N.GbaParams:
+def make_params(score, mode: int, config: AlignConfig | None, band, outputs: int,
+                alphabet_size: int = 0, flags: int = 0) -> N.GbaParams:
     p = N.GbaParams()
     p.mode = mode
     p.gap_model = N.GBA_GAPS_AUTO
@@ -122,11 +123,13 @@ def make_params(score, mode: int, config: AlignConfig | None, band, outputs: int
         p.band_on, p.band_lower, p.band_upper = 1, int(band[0]), int(band[1])
     p.match, p.mismatch = score.match, score.mismatch
     p.gap_open, p.gap_extend = score.gap_open, score.gap_extend
+    p.alphabet_size = alphabet_size
     if score.matrix is not None:
         p.matrix = score.matrix.ctypes.data_as(C.c_void_p)
         p.alphabet_size = score.matrix.shape[0]
     p.score_bits = score.bits
     p.outputs = outputs
+    p.flags = flags
     return p
 
 
@@ -153,9 +156,16 @@ class BatchOutput:
         return "".join(f"{int(x) >> 4}{ops[int(x) & 15]}" for x in c)
 
 
+ALPHABET_SIZE = {"dna": 4, "dna5": 5, "aa": 27}
+
+
 def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None,
-                traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None) -> BatchOutput:
-    """Aligns lists of code arrays through gba_align_batch."""
+                traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None,
+                alphabet_size: int | None = None, flags: int = 0) -> BatchOutput:
+    """Aligns lists of code arrays through gba_align_batch.
+
+    alphabet_size bounds the codes (the reference's ValueSize of the alphabet); when None it is
+    taken from the codes themselves."""
     ctx = ctx or N.default_context()
     n = len(codes_v)
     sh, oh = _concat(codes_h)
@@ -165,7 +175,9 @@ def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=No
         outputs |= N.GBA_OUT_SEGMENTS
     if cigar:
         outputs |= N.GBA_OUT_CIGAR | N.GBA_OUT_SEGMENTS
-    params = make_params(score, mode, config, band, outputs)
+    if alphabet_size is None:
+        alphabet_size = int(max(sh.max(initial=0), sv.max(initial=0))) + 1 if n else 0
+    params = make_params(score, mode, config, band, outputs, alphabet_size, flags)
     b = N.GbaBatch(n, _vp(sh), _vp(oh), _vp(sv), _vp(ov), 1 if h_shared else 0, 0)
     res = BatchOutput(score=np.zeros(n, np.int32), end_h=np.zeros(n, np.int32), end_v=np.zeros(n, np.int32),
                       status=np.zeros(n, np.int32))
@@ -202,7 +214,8 @@ def globalAlignmentScore(*args, alphabet: str = "dna5", **kw):
     band = _band(rest) or kw.get("band")
     h_shared = not isinstance(setH, (list, tuple))
     codes_h = [encode(setH, alphabet)] if h_shared else _as_codes(setH, alphabet)
-    out = align_codes(codes_h, _as_codes(setV, alphabet), score, N.GBA_GLOBAL, config, band, h_shared=h_shared)
+    out = align_codes(codes_h, _as_codes(setV, alphabet), score, N.GBA_GLOBAL, config, band, h_shared=h_shared,
+                      alphabet_size=ALPHABET_SIZE[alphabet])
     return out.score.astype(score.dtype)
 
 
@@ -213,7 +226,8 @@ def localAlignmentScore(*args, alphabet: str = "dna5", **kw):
     band = _band(list(args[3:])) or kw.get("band")
     h_shared = not isinstance(setH, (list, tuple))
     codes_h = [encode(setH, alphabet)] if h_shared else _as_codes(setH, alphabet)
-    out = align_codes(codes_h, _as_codes(setV, alphabet), score, N.GBA_LOCAL, None, band, h_shared=h_shared)
+    out = align_codes(codes_h, _as_codes(setV, alphabet), score, N.GBA_LOCAL, None, band, h_shared=h_shared,
+                      alphabet_size=ALPHABET_SIZE[alphabet])
     return out.score.astype(score.dtype)
 
 

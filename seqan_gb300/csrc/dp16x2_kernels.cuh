@@ -1,0 +1,292 @@
+// dp16x2_kernels.cuh -- packed 16-bit DP: two pairs per thread, DPX max/add.
+//
+// For global alignments with equality scoring (Score<T, Simple>) whose every cell value
+// stays inside the exact int16 range (the same bound the engine uses to honour 16-bit
+// cells), each thread runs TWO pairs in the two 16-bit halves of 32-bit registers.  The
+// max/add steps are the sm_90+ DPX instructions __viaddmax_s16x2 (max(a + b, c)) and
+// __vimax3_s16x2, so one instruction advances two cells; the substitution score of both
+// halves comes from one PRMT lookup in a byte table.
+//
+// Scores and end positions are exactly those of the reference's DP: the recurrence values
+// are the same integers (align/dp_formula_affine.h:66-330, align/dp_formula_linear.h:62-258;
+// border cells align/dp_meta_info.h:178-221), and the tracked cells and the first-max rule
+// of the scout (align/dp_scout.h:166-180) are applied per half.
+//
+// Layout (all per warp, interleaved by lane so each warp access is 128 contiguous bytes):
+//   codes:    one 32-bit word per 4 columns of H and per 4 rows of V; byte k of a word holds
+//             the two pairs' residue codes (pair A in the low nibble, pair B in the high nibble)
+//   boundary: per column, the strip's bottom row (S2, F2) as one int2
+#pragma once
+
+#include "dp_common.cuh"
+
+namespace gba {
+
+// Slot = two pairs sharing one thread.
+struct Slot16 {
+    int32_t pa, pb;        // pair indices (pb = -1: no second pair)
+    int32_t m, n;          // max columns / rows over the two pairs
+};
+
+struct Dp16Args {
+    const uint8_t *seq_h;
+    const uint8_t *seq_v;
+    const PairDesc *pairs;
+    const Slot16 *slots;
+    const int64_t *warp_codes;    // per warp: word offset of its code region
+    const int32_t *warp_hwords;   // per warp: words of H codes per lane (the V codes follow)
+    uint32_t *codes;
+    const int64_t *warp_bnd;      // per warp: int2 offset of its boundary region
+    int2 *bnd;
+    int32_t *score, *end_h, *end_v;
+    int64_t num_slots;
+    int32_t match, mismatch, gap_open, gap_extend;
+    int32_t free_ends;
+};
+
+// ---- packing: residue codes of the two pairs -> interleaved nibble words -------------
+__global__ void __launch_bounds__(128) k_pack16(Dp16Args a)
+{
+    const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= a.num_slots) return;
+    const Slot16 sl = a.slots[s];
+    const int64_t w = s >> 5, lane = s & 31;
+    uint32_t *base = a.codes + a.warp_codes[w] + lane;
+    const int hw = a.warp_hwords[w];
+    const PairDesc A = a.pairs[sl.pa];
+    PairDesc B = A;
+    int mb = 0, nb = 0;
+    if (sl.pb >= 0) { B = a.pairs[sl.pb]; mb = B.m; nb = B.n; }
+    const uint8_t *ha = a.seq_h + A.h_off, *hb = a.seq_h + B.h_off;
+    const uint8_t *va = a.seq_v + A.v_off, *vb = a.seq_v + B.v_off;
+    for (int q = 0; q < hw; ++q) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = 4 * q + k;
+            const uint32_t ca = j < A.m ? (ha[j] & 7u) : 0u;
+            const uint32_t cb = j < mb ? (hb[j] & 7u) : 0u;
+            word |= (ca | (cb << 4)) << (8 * k);
+        }
+        base[int64_t(q) * 32] = word;
+    }
+    const int vw = (sl.n + 3) >> 2;
+    for (int q = 0; q < vw; ++q) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = 4 * q + k;
+            const uint32_t ca = i < A.n ? (va[i] & 7u) : 0u;
+            const uint32_t cb = i < nb ? (vb[i] & 7u) : 0u;
+            word |= (ca | (cb << 4)) << (8 * k);
+        }
+        base[int64_t(hw + q) * 32] = word;
+    }
+}
+
+__device__ __forceinline__ uint32_t pack2(int lo, int hi)
+{
+    return (uint32_t(lo) & 0xffffu) | (uint32_t(hi) << 16);
+}
+__device__ __forceinline__ int lo16(uint32_t x) { return int(int16_t(x & 0xffffu)); }
+__device__ __forceinline__ int hi16(uint32_t x) { return int(int16_t(x >> 16)); }
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
+{
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+    return d;
+}
+
+// Selector half for a row code v (3 bits): byte nibble v, then 8|v (sign replicate).
+__device__ __forceinline__ uint32_t vsel_of(uint32_t byte)
+{
+    const uint32_t a = byte & 7u, b = (byte >> 4) & 7u;
+    return a | ((a | 8u) << 4) | (b << 8) | ((b | 8u) << 12);
+}
+__device__ __forceinline__ uint32_t hsel_of(uint32_t byte)
+{
+    const uint32_t a = byte & 7u, b = (byte >> 4) & 7u;
+    return (a * 0x11u) | ((b * 0x11u) << 8);
+}
+
+struct Best2 {
+    int s[2], col[2], row[2];
+    __device__ __forceinline__ void init()
+    {
+        s[0] = s[1] = -16384; col[0] = col[1] = 0; row[0] = row[1] = 0;
+    }
+    __device__ __forceinline__ void offer(int h, int cs, int ccol, int crow)
+    {
+        if (cs >= s[h] && (cs > s[h] || ccol < col[h] || (ccol == col[h] && crow < row[h]))) {
+            s[h] = cs; col[h] = ccol; row[h] = crow;
+        }
+    }
+};
+
+// One pair-of-pairs per thread.  R rows per register strip.
+template <bool AFFINE, int R>
+__global__ void __launch_bounds__(128) k_dp16x2(Dp16Args a)
+{
+    const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= a.num_slots) return;
+    const Slot16 sl = a.slots[s];
+    const int64_t w = s >> 5, lane = s & 31;
+    const uint32_t *codes = a.codes + a.warp_codes[w] + lane;
+    const int hw = a.warp_hwords[w];
+    int2 *bnd = a.bnd + a.warp_bnd[w] + lane;
+
+    const PairDesc A = a.pairs[sl.pa];
+    const bool hasB = sl.pb >= 0;
+    int mB = 0, nB = 0;
+    if (hasB) { const PairDesc B = a.pairs[sl.pb]; mB = B.m; nB = B.n; }
+    const int mA = A.m, nA = A.n;
+    const int M = sl.m, N = sl.n;
+
+    const int fe = a.free_ends;
+    const bool fTop = fe & FREE_TOP, fLeft = fe & FREE_LEFT;
+    const bool fRight = fe & FREE_RIGHT, fBottom = fe & FREE_BOTTOM;
+    const int INF = -16384;
+    const uint32_t INF2 = pack2(INF, INF);
+    const uint32_t EXT2 = pack2(a.gap_extend, a.gap_extend);
+    const uint32_t OPEN2 = AFFINE ? pack2(a.gap_open, a.gap_open) : EXT2;
+    const uint32_t NEG2 = pack2(-32768, -32768);
+    // Byte table for PRMT: entry d = code_h XOR code_v, 0 -> match, 1..7 -> mismatch.
+    const uint32_t T0 = (uint32_t(a.match) & 0xffu) | ((uint32_t(a.mismatch) & 0xffu) * 0x01010100u);
+    const uint32_t T1 = (uint32_t(a.mismatch) & 0xffu) * 0x01010101u;
+
+    Best2 best;
+    best.init();
+    const int mh[2] = {mA, mB}, nh[2] = {nA, nB};
+    const int halves = hasB ? 2 : 1;
+
+    // ---- Row 0.  The boundary holds, per column, S of the row above the next strip and F of
+    // that strip's first row (already advanced: F(i, j) = max(F(i-1, j) + ext, S(i-1, j) + open)).
+    {
+        uint32_t s2 = 0, e2 = INF2;
+        bnd[0] = make_int2(0, int(AFFINE ? __viaddmax_s16x2(INF2, EXT2, __viaddmax_s16x2(s2, OPEN2, NEG2)) : INF2));
+        for (int j = 1; j <= M; ++j) {
+            if (!fTop) {
+                if (AFFINE) {
+                    e2 = __viaddmax_s16x2(e2, EXT2, __viaddmax_s16x2(s2, OPEN2, NEG2));
+                    s2 = e2;
+                } else {
+                    s2 = __viaddmax_s16x2(s2, EXT2, NEG2);
+                }
+            }
+            const uint32_t f1 = AFFINE ? __viaddmax_s16x2(INF2, EXT2, __viaddmax_s16x2(s2, OPEN2, NEG2)) : INF2;
+            bnd[int64_t(j) * 32] = make_int2(int(s2), int(f1));
+            if (fRight) {
+                if (j == mA) best.offer(0, lo16(s2), j, 0);
+                if (hasB && j == mB) best.offer(1, hi16(s2), j, 0);
+            }
+        }
+    }
+
+    // ---- Strips.
+    for (int i0 = 1; i0 <= N; i0 += R) {
+        uint32_t vs[R];
+#pragma unroll
+        for (int q = 0; q < R / 4; ++q) {
+            const int wq = (i0 - 1) / 4 + q;
+            const uint32_t word = (4 * wq < N) ? codes[int64_t(hw + wq) * 32] : 0u;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) vs[4 * q + k] = vsel_of(word >> (8 * k));
+        }
+        uint32_t Sp[R], Ep[R];
+        // Rows of each half that end inside this strip (for end-row tracking).
+        const int rA = nA - i0, rB = nB - i0;
+        const bool endA = rA >= 0 && rA < R, endB = hasB && rB >= 0 && rB < R;
+
+        // Column 0: Vertical (or Zero with a free first column); E enters column 1 as
+        // E(i, 1) = max(E(i, 0) + ext, S(i, 0) + open) with E(i, 0) = infinity.
+        uint32_t diagNext;
+        {
+            const int2 up = bnd[0];
+            uint32_t sUp = uint32_t(up.x), fUp = uint32_t(up.y);
+            diagNext = sUp;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                uint32_t s2;
+                if (fLeft) {
+                    s2 = 0;
+                } else if (AFFINE) {
+                    s2 = fUp;
+                } else {
+                    s2 = __viaddmax_s16x2(sUp, EXT2, NEG2);
+                }
+                if (AFFINE) {
+                    const uint32_t so = __viaddmax_s16x2(s2, OPEN2, NEG2);
+                    fUp = __viaddmax_s16x2(fUp, EXT2, so);
+                    Ep[r] = __viaddmax_s16x2(INF2, EXT2, so);
+                } else {
+                    Ep[r] = INF2;
+                }
+                Sp[r] = s2;
+                sUp = s2;
+                if (fBottom) {
+                    if (endA && r == rA) best.offer(0, lo16(s2), 0, nA);
+                    if (endB && r == rB) best.offer(1, hi16(s2), 0, nB);
+                }
+            }
+            bnd[0] = make_int2(int(sUp), int(fUp));
+        }
+
+        // Columns 1..M.
+        uint32_t hword = 0;
+        for (int j = 1; j <= M; ++j) {
+            if (((j - 1) & 3) == 0) hword = codes[int64_t((j - 1) >> 2) * 32];
+            const uint32_t hsel = hsel_of(hword >> (8 * ((j - 1) & 3)));
+            const int2 up = bnd[int64_t(j) * 32];
+            uint32_t sUp = uint32_t(up.x), fUp = uint32_t(up.y);
+            uint32_t diag = diagNext;
+            diagNext = sUp;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const uint32_t sub = prmt(T0, T1, hsel ^ vs[r]);
+                uint32_t s2;
+                if (AFFINE) {
+                    // S = max(diag + sub, E, F); then E(i, j+1), F(i+1, j) from S + open.
+                    s2 = __vimax3_s16x2(__viaddmax_s16x2(diag, sub, Ep[r]), fUp, fUp);
+                    const uint32_t so = __viaddmax_s16x2(s2, OPEN2, NEG2);
+                    Ep[r] = __viaddmax_s16x2(Ep[r], EXT2, so);
+                    fUp = __viaddmax_s16x2(fUp, EXT2, so);
+                } else {
+                    // S = max(diag + sub, max(up, left) + gap).
+                    s2 = __viaddmax_s16x2(diag, sub,
+                                          __viaddmax_s16x2(__vimax3_s16x2(sUp, Sp[r], Sp[r]), EXT2, NEG2));
+                }
+                diag = Sp[r];
+                Sp[r] = s2;
+                sUp = s2;
+            }
+            bnd[int64_t(j) * 32] = make_int2(int(sUp), int(fUp));
+            // Tracking: last column of each half, and its last row when the last row is free.
+            if (j == mA || (hasB && j == mB)) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int i = i0 + r;
+                    if (j == mA && i <= nA && (fRight || i == nA)) best.offer(0, lo16(Sp[r]), j, i);
+                    if (hasB && j == mB && i <= nB && (fRight || i == nB)) best.offer(1, hi16(Sp[r]), j, i);
+                }
+            }
+            if (fBottom && (endA || endB)) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (endA && r == rA && j < mA) best.offer(0, lo16(Sp[r]), j, nA);
+                    if (endB && r == rB && j < mB) best.offer(1, hi16(Sp[r]), j, nB);
+                }
+            }
+        }
+    }
+    for (int h = 0; h < halves; ++h) {
+        const int p = h == 0 ? sl.pa : sl.pb;
+        a.score[p] = best.s[h];
+        if (a.end_h) a.end_h[p] = best.col[h];
+        if (a.end_v) a.end_v[p] = best.row[h];
+    }
+    (void)mh;
+    (void)nh;
+}
+
+}  // namespace gba

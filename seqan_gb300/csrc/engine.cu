@@ -8,6 +8,7 @@
 #include "dp_common.cuh"
 #include "dp_kernels.cuh"
 #include "traceback_kernels.cuh"
+#include "dp16x2_kernels.cuh"
 #include "int_peak.cuh"
 
 #include <cub/device/device_scan.cuh>
@@ -80,6 +81,11 @@ struct gba_plan {
     DevBuf cig_slots, cig_slot_off, cig_count, cig_dense_off, cig_dense, cig_count64;
     DevBuf cub_tmp;
     size_t cub_tmp_bytes = 0;
+    // Packed two-pairs-per-thread path (dp16x2_kernels.cuh).
+    int64_t num16 = 0;              // slots (two pairs each)
+    int rows16 = 32;                // rows per register strip
+    int64_t codes_total = 0, bnd16_total = 0;
+    DevBuf slots16, warp_codes, warp_hwords, codes16, warp_bnd16, bnd16;
     int64_t seg_dense_total = -1, cig_dense_total = -1;
     bool owned = true;
     void release()
@@ -87,7 +93,8 @@ struct gba_plan {
         DevBuf *all[] = {&pairs, &order, &warp_scratch, &scratch, &trace, &best_e, &best_f, &matrix_dev,
                          &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots, &seg_slot_off,
                          &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
-                         &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp};
+                         &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
+                         &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16};
         for (DevBuf *b : all) b->release();
     }
     size_t device_bytes() const
@@ -96,7 +103,8 @@ struct gba_plan {
                                &matrix_dev, &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots,
                                &seg_slot_off, &seg_count, &seg_dense_off, &seg_dense, &seg_count64,
                                &cig_slots, &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense,
-                               &cig_count64, &cub_tmp};
+                               &cig_count64, &cub_tmp, &slots16, &warp_codes, &warp_hwords, &codes16,
+                               &warp_bnd16, &bnd16};
         size_t s = 0;
         for (const DevBuf *b : all) s += b->cap;
         return s;
@@ -249,6 +257,17 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     max_sub_abs(*p, plan->matrix_host, &max_pos);
 
     plan->status.assign(N, GBA_PAIR_OK);
+    // The packed 16-bit path: global score-only runs with equality scoring over an alphabet of
+    // at most 8 codes (the caller's alphabet_size), table entries that fit a byte, and gaps that
+    // keep int16 arithmetic exact (checked per pair below).
+    const bool packed_ok = !plan->local && !plan->traceback && !plan->matrix && !p->band_on &&
+                           !(p->flags & GBA_FLAG_GENERAL_KERNEL) && p->alphabet_size >= 1 &&
+                           p->alphabet_size <= 8 && p->match >= -128 && p->match <= 127 &&
+                           p->mismatch >= -128 && p->mismatch <= 127 && std::abs(p->gap_open) <= 1024 &&
+                           std::abs(p->gap_extend) <= 1024;
+    plan->rows16 = (p->flags & GBA_FLAG_STRIP16) ? 16 : 32;
+    std::vector<uint32_t> keys16;
+    std::vector<int32_t> idx16;
     std::vector<PairDesc> desc(std::max<int64_t>(N, 1));
     std::vector<uint32_t> keys;
     std::vector<int32_t> idx;
@@ -286,6 +305,12 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             d.trace_off = trace_off;
             trace_off += trace_bytes(d.m, d.n);
         }
+        if (packed_ok && int16_exact(*p, max_pos, d.m, d.n, false)) {
+            const int64_t strips = (d.n + plan->rows16 - 1) / plan->rows16;
+            keys16.push_back(uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL)));
+            idx16.push_back(int32_t(k));
+            continue;
+        }
         const int64_t strips = (d.n + STRIP_ROWS - 1) / STRIP_ROWS;
         const int64_t cost = strips * (d.m + 1);
         keys.push_back(uint32_t(std::min<int64_t>(cost, 0xffffffffLL)));
@@ -294,6 +319,43 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->trace_total = trace_off;
     sort_desc(keys, idx);
     plan->num_slots = int64_t(idx.size());
+
+    // Packed path: neighbours in the length-sorted order share a thread; per warp, the code
+    // words (4 residues per word, both pairs' codes per byte) and the boundary row are
+    // interleaved by lane.
+    sort_desc(keys16, idx16);
+    std::vector<Slot16> slots16((idx16.size() + 1) / 2);
+    for (size_t q = 0; q < slots16.size(); ++q) {
+        Slot16 &sl = slots16[q];
+        sl.pa = idx16[2 * q];
+        sl.pb = 2 * q + 1 < idx16.size() ? idx16[2 * q + 1] : -1;
+        sl.m = desc[sl.pa].m;
+        sl.n = desc[sl.pa].n;
+        if (sl.pb >= 0) {
+            sl.m = std::max(sl.m, desc[sl.pb].m);
+            sl.n = std::max(sl.n, desc[sl.pb].n);
+        }
+    }
+    plan->num16 = int64_t(slots16.size());
+    const int64_t warps16 = (plan->num16 + 31) / 32;
+    std::vector<int64_t> wcodes(std::max<int64_t>(warps16, 1)), wbnd(std::max<int64_t>(warps16, 1));
+    std::vector<int32_t> whw(std::max<int64_t>(warps16, 1));
+    int64_t ctot = 0, btot = 0;
+    for (int64_t w = 0; w < warps16; ++w) {
+        int maxm = 0, maxn = 0;
+        for (int64_t q = w * 32; q < std::min(plan->num16, (w + 1) * 32); ++q) {
+            maxm = std::max(maxm, slots16[q].m);
+            maxn = std::max(maxn, slots16[q].n);
+        }
+        const int hw = (maxm + 3) / 4, vw = (maxn + plan->rows16 - 1) / plan->rows16 * (plan->rows16 / 4);
+        wcodes[w] = ctot;
+        whw[w] = hw;
+        ctot += int64_t(hw + vw) * 32;
+        wbnd[w] = btot;
+        btot += int64_t(maxm + 1) * 32;
+    }
+    plan->codes_total = ctot;
+    plan->bnd16_total = btot;
 
     // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
     const int64_t warps = (plan->num_slots + 31) / 32;
@@ -324,6 +386,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
 
     // HBM budget: everything this plan keeps on the device plus the input codes.
     const int64_t need = int64_t(sizeof(PairDesc)) * N + 4 * N * 8 + scr * 8 + plan->trace_total +
+                         plan->codes_total * 4 + plan->bnd16_total * 8 + plan->num16 * int64_t(sizeof(Slot16)) +
                          plan->seg_slots_total * 16 * 2 + plan->cigar_slots_total * 4 * 2 +
                          plan->seq_h_bytes + plan->seq_v_bytes;
     if (ctx->budget > 0 && need > ctx->budget)
@@ -334,6 +397,14 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     if ((rc = upload(ctx, plan->order, idx))) return rc;
     if ((rc = upload(ctx, plan->warp_scratch, wscr))) return rc;
     GBA_CUDA(ctx, plan->scratch.ensure(size_t(std::max<int64_t>(scr, 1)) * sizeof(int2)));
+    if (plan->num16 > 0) {
+        if ((rc = upload(ctx, plan->slots16, slots16))) return rc;
+        if ((rc = upload(ctx, plan->warp_codes, wcodes))) return rc;
+        if ((rc = upload(ctx, plan->warp_hwords, whw))) return rc;
+        if ((rc = upload(ctx, plan->warp_bnd16, wbnd))) return rc;
+        GBA_CUDA(ctx, plan->codes16.ensure(size_t(std::max<int64_t>(ctot, 1)) * 4));
+        GBA_CUDA(ctx, plan->bnd16.ensure(size_t(std::max<int64_t>(btot, 1)) * sizeof(int2)));
+    }
     if (plan->matrix) {
         if ((rc = upload(ctx, plan->matrix_dev, plan->matrix_host))) return rc;
     }
@@ -434,6 +505,38 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
     int launches = 0;
 
     GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    if (plan->num16 > 0) {
+        Dp16Args a{};
+        a.seq_h = dseq_h;
+        a.seq_v = dseq_v;
+        a.pairs = plan->pairs.as<PairDesc>();
+        a.slots = plan->slots16.as<Slot16>();
+        a.warp_codes = plan->warp_codes.as<int64_t>();
+        a.warp_hwords = plan->warp_hwords.as<int32_t>();
+        a.codes = plan->codes16.as<uint32_t>();
+        a.warp_bnd = plan->warp_bnd16.as<int64_t>();
+        a.bnd = plan->bnd16.as<int2>();
+        a.score = dscore;
+        a.end_h = end_h;
+        a.end_v = end_v;
+        a.num_slots = plan->num16;
+        a.match = plan->params.match;
+        a.mismatch = plan->params.mismatch;
+        a.gap_open = plan->params.gap_open;
+        a.gap_extend = plan->params.gap_extend;
+        a.free_ends = plan->free_ends;
+        const int grid = int((plan->num16 + kBlock - 1) / kBlock);
+        k_pack16<<<grid, kBlock, 0, ctx->stream>>>(a);
+        if (plan->rows16 == 16) {
+            if (plan->affine) k_dp16x2<true, 16><<<grid, kBlock, 0, ctx->stream>>>(a);
+            else k_dp16x2<false, 16><<<grid, kBlock, 0, ctx->stream>>>(a);
+        } else {
+            if (plan->affine) k_dp16x2<true, 32><<<grid, kBlock, 0, ctx->stream>>>(a);
+            else k_dp16x2<false, 32><<<grid, kBlock, 0, ctx->stream>>>(a);
+        }
+        GBA_CUDA(ctx, cudaGetLastError());
+        launches += 2;
+    }
     if (plan->num_slots > 0) {
         DpArgs a{};
         a.seq_h = dseq_h;

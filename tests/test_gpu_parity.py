@@ -156,3 +156,25 @@ def test_python_interface_gaps(engine):
     sc = sg.globalAlignment([gH], [gV], sg.Score(2, -1, -1))
     assert int(sc[0]) == 6
     assert (gH.row(), gV.row()) == ("AT-G-T", "ATAGAT")
+
+
+@pytest.mark.parametrize("flags", [0, 2])          # packed kernel with 32-row and 16-row strips
+@pytest.mark.parametrize("fe", [0, 1, 2, 4, 8, 9, 6, 15, 5, 10])
+def test_packed_kernel_against_oracle(engine, flags, fe):
+    """The two-pairs-per-thread 16-bit kernel: uneven lengths in one slot, odd pair count,
+    Dna5 codes (N = 4), both gap models, every tracked-cell rule."""
+    import seqan_gb300 as sg
+    rng = np.random.default_rng(1000 + fe)
+    H = [rng.integers(0, 5, rng.integers(1, 260)).astype(np.uint8) for _ in range(333)]
+    V = [np.where(rng.random(len(h)) < 0.15, rng.integers(0, 5, len(h)), h).astype(np.uint8)
+         if rng.random() < 0.6 else rng.integers(0, 5, rng.integers(1, 260)).astype(np.uint8) for h in H]
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    for (mt, mm, go, ge) in [(2, -4, -6, -1), (2, -3, -5, -5), (5, -4, -10, -1)]:
+        for dtype, bits in ((np.int16, 16), (np.int32, 32)):
+            sc = sg.Score(mt, mm, ge, go, dtype=dtype)
+            out = sg.align_codes(H, V, sc, config=cfg, alphabet_size=5, flags=flags)
+            gen = sg.align_codes(H, V, sc, config=cfg, alphabet_size=5, flags=1)
+            ref = O.oracle_batch(O.Problem("global", fe, None, mt, mm, go, ge, None, bits), H, V)
+            assert np.array_equal(out.score, ref.score) and np.array_equal(gen.score, ref.score)
+            assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+            assert np.array_equal(out.status, gen.status)
