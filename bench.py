@@ -180,8 +180,10 @@ def main():
     ap.add_argument("--workload", default="affine_dna_100k", choices=sorted(WORKLOADS))
     ap.add_argument("--ref-pairs", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16"],
-                    help="auto: packed 16-bit kernel (32-row strips) where eligible")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-bucket comparison")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16", "plain"],
+                    help="auto: persistent packed 16-bit kernel (32-row strips), graph-replayed; "
+                         "plain: general kernel, one launch per length bucket")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -234,7 +236,8 @@ def main():
     as_np(p_ov, ov.size, np.int64)[:] = ov
     p_score, p_eh, p_ev = pinned(npairs * 4), pinned(npairs * 4), pinned(npairs * 4)
 
-    flags = {"auto": 0, "general": N.GBA_FLAG_GENERAL_KERNEL, "packed16": N.GBA_FLAG_STRIP16}[args.kernel]
+    flags = {"auto": N.GBA_FLAG_AUTOTUNE, "general": N.GBA_FLAG_GENERAL_KERNEL, "packed16": N.GBA_FLAG_STRIP16,
+             "plain": N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH}[args.kernel]
     params = sg.align.make_params(score, mode, None, None, N.GBA_OUT_SCORE | N.GBA_OUT_END,
                                   alphabet_size=4, flags=flags)
     host_batch = N.GbaBatch(npairs, p_sh, p_oh, p_sv, p_ov, 0, 0)
@@ -272,6 +275,7 @@ def main():
     sampler.start()
     step_ms, dp_ms, launches = [], [], 0
     ms = C.c_float()
+    tile = None
     for _ in range(args.steps):
         flush_l2()
         ctx.check(L.gba_timer_start(h), "timer")
@@ -281,6 +285,7 @@ def main():
         st = ctx.stats()
         dp_ms.append(st.dp_kernel_ms)
         launches += st.kernel_launches
+        tile = {"rows_per_strip": st.tile_rows, "min_blocks_per_sm": st.tile_min_blocks}
     ctx.check(L.gba_synchronize(h), "sync")
     barrier()
     clocks = sampler.stop()
@@ -291,6 +296,30 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = cells * world * args.steps / (total_ms * 1e-3) / 1e9
+
+    # The plain GPU form on the same device-resident batch: the general one-pair-per-thread
+    # kernel, one launch per 8-residue length bucket (comparison for the persistent form).
+    plain = None
+    if args.kernel == "auto" and not args.no_plain:
+        pparams = sg.align.make_params(score, mode, None, None, N.GBA_OUT_SCORE | N.GBA_OUT_END, alphabet_size=4,
+                                       flags=N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH)
+        pplan = C.c_void_p()
+        ctx.check(L.gba_plan_create(h, C.byref(pparams), C.byref(host_batch), C.byref(pplan)), "plain plan")
+        ctx.check(L.gba_plan_execute(h, pplan, C.byref(dev_batch), C.byref(dev_res)), "plain")
+        ctx.check(L.gba_synchronize(h), "sync")
+        pms = []
+        for _ in range(2):
+            flush_l2()
+            ctx.check(L.gba_timer_start(h), "timer")
+            ctx.check(L.gba_plan_execute(h, pplan, C.byref(dev_batch), C.byref(dev_res)), "plain")
+            ctx.check(L.gba_timer_stop(h, C.byref(ms)), "timer")
+            pms.append(ms.value)
+        plain_launches = ctx.stats().kernel_launches
+        L.gba_plan_destroy(h, pplan)
+        pg = cells / (sum(pms) / len(pms) * 1e-3) / 1e9
+        plain = {"value": pg, "unit": "GCUPS", "launches_per_step": plain_launches,
+                 "speedup_of_value": value / pg,
+                 "form": "general one-pair-per-thread kernel, one launch per 8-residue length bucket"}
 
     # End to end through the public C-ABI call with host buffers.
     host_res = N.GbaResult()
@@ -303,7 +332,9 @@ def main():
         t0 = time.perf_counter()
         ctx.check(L.gba_align_batch(h, C.byref(params), C.byref(host_batch), C.byref(host_res)), "e2e")
         e2e_s.append(time.perf_counter() - t0)
-    e2e_launches = ctx.stats().kernel_launches
+    est = ctx.stats()
+    e2e_launches = est.kernel_launches
+    e2e_breakdown = {"host_plan_ms": est.host_plan_ms, "dp_kernel_ms": est.dp_kernel_ms, "call_ms": est.call_ms}
     e2e_gcups = cells * world * len(e2e_s) / sum(e2e_s) / 1e9
     h2d = sh.nbytes + sv.nbytes
     d2h = 3 * npairs * 4
@@ -330,8 +361,12 @@ def main():
                        "kernel": args.kernel,
                        "parallelism": f"replicas x{world} (pairs are independent)"},
             "e2e": {"value": e2e_gcups, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": 1e3 * sum(e2e_s) / len(e2e_s)},
+                    "ms_per_step": 1e3 * sum(e2e_s) / len(e2e_s), "last_call": e2e_breakdown},
             "gpu_launches": launches, "roofline": roofline, "clocks": clocks}
+    if tile:
+        line["config"]["tiling"] = tile
+    if plain:
+        line["plain_gpu_form"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(H, V, score, kind)
     L.gba_plan_destroy(h, plan)

@@ -102,7 +102,12 @@ typedef struct {
  * reference's alphabet types guarantee) and the pair's values stay in the exact int16 range. */
 enum {
     GBA_FLAG_GENERAL_KERNEL = 1,   /* force the one-pair-per-thread 32-bit kernel */
-    GBA_FLAG_STRIP16 = 2           /* packed kernel with 16-row strips instead of 32 */
+    GBA_FLAG_STRIP16 = 2,          /* packed kernel with 16-row strips instead of 32 */
+    GBA_FLAG_PLAIN_BUCKETS = 4,    /* the plain GPU form: general kernel, one launch per
+                                      8-residue length bucket (comparison baseline) */
+    GBA_FLAG_NO_GRAPH = 8,         /* launch kernels directly instead of replaying a CUDA graph */
+    GBA_FLAG_AUTOTUNE = 16         /* time the packed kernel's tiling variants on the first run
+                                      of a plan and remember the fastest per batch shape */
 };
 
 /* A batch: concatenated residue codes with n+1 offsets for each side. */
@@ -187,6 +192,10 @@ typedef struct {
     int32_t kernel_launches;   /* kernels this library launched for the batch */
     int64_t cells;             /* algorithmic cells: sum m*n (in-band cells when banded) */
     int64_t trace_bytes;       /* trace matrix bytes written */
+    int32_t tile_rows;         /* packed kernel: rows per register strip (0 = not used) */
+    int32_t tile_min_blocks;   /* packed kernel: minimum resident blocks per SM */
+    float host_plan_ms;        /* gba_align_batch: host planning time */
+    float call_ms;             /* gba_align_batch: whole call, wall clock */
 } gba_stats;
 GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
 

@@ -29,7 +29,7 @@ GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
 GBA_OUT_SCORE, GBA_OUT_END, GBA_OUT_SEGMENTS, GBA_OUT_CIGAR = 1, 2, 4, 8
 GBA_SEG_DIAGONAL, GBA_SEG_HORIZONTAL, GBA_SEG_VERTICAL = 1, 2, 4
 GBA_NOALLOC_SCRATCH_BYTES = 64 << 20
-GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16 = 1, 2
+GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16, GBA_FLAG_PLAIN_BUCKETS, GBA_FLAG_NO_GRAPH, GBA_FLAG_AUTOTUNE = 1, 2, 4, 8, 16
 
 # Every symbol include/seqan_gb300.h declares.
 EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", "gba_align_batch",
@@ -74,7 +74,9 @@ class GbaNoAllocBatch(C.Structure):
 
 class GbaStats(C.Structure):
     _fields_ = [("dp_kernel_ms", C.c_float), ("traceback_kernel_ms", C.c_float),
-                ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64)]
+                ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64),
+                ("tile_rows", C.c_int32), ("tile_min_blocks", C.c_int32), ("host_plan_ms", C.c_float),
+                ("call_ms", C.c_float)]
 
 
 def _sources():

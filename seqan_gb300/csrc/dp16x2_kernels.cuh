@@ -42,24 +42,25 @@ struct Dp16Args {
     int64_t num_slots;
     int32_t match, mismatch, gap_open, gap_extend;
     int32_t free_ends;
+    int32_t num_tasks;            // warp-sized work items (32 consecutive slots each)
+    int32_t *task_counter;        // next work item; zeroed before each launch
 };
 
 // ---- packing: residue codes of the two pairs -> interleaved nibble words -------------
-__global__ void __launch_bounds__(128) k_pack16(Dp16Args a)
+// Each lane packs its own slot into its column of the warp's code region and is the only
+// reader of that column, so no synchronisation is needed.
+__device__ __forceinline__ void pack_slot(const Dp16Args &a, const Slot16 &sl, int64_t task, int lane)
 {
-    const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (s >= a.num_slots) return;
-    const Slot16 sl = a.slots[s];
-    const int64_t w = s >> 5, lane = s & 31;
-    uint32_t *base = a.codes + a.warp_codes[w] + lane;
-    const int hw = a.warp_hwords[w];
+    uint32_t *base = a.codes + a.warp_codes[task] + lane;
+    const int hw = a.warp_hwords[task];
     const PairDesc A = a.pairs[sl.pa];
     PairDesc B = A;
     int mb = 0, nb = 0;
     if (sl.pb >= 0) { B = a.pairs[sl.pb]; mb = B.m; nb = B.n; }
     const uint8_t *ha = a.seq_h + A.h_off, *hb = a.seq_h + B.h_off;
     const uint8_t *va = a.seq_v + A.v_off, *vb = a.seq_v + B.v_off;
-    for (int q = 0; q < hw; ++q) {
+    const int hq = (sl.m + 3) >> 2;
+    for (int q = 0; q < hq; ++q) {
         uint32_t word = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -124,14 +125,21 @@ struct Best2 {
     }
 };
 
-// One pair-of-pairs per thread.  R rows per register strip.
-template <bool AFFINE, int R>
-__global__ void __launch_bounds__(128) k_dp16x2(Dp16Args a)
+// Packs every slot's codes (one thread per slot, full occupancy) before the DP runs.
+__global__ void __launch_bounds__(128) k_pack16(Dp16Args a)
 {
     const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= a.num_slots) return;
+    pack_slot(a, a.slots[s], s >> 5, int(s & 31));
+}
+
+// One pair-of-pairs per thread.  R rows per register strip.
+template <bool AFFINE, int R>
+__device__ __forceinline__ void dp16x2_slot(const Dp16Args &a, int64_t w, int lane)
+{
+    const int64_t s = w * 32 + lane;
+    if (s >= a.num_slots) return;
     const Slot16 sl = a.slots[s];
-    const int64_t w = s >> 5, lane = s & 31;
     const uint32_t *codes = a.codes + a.warp_codes[w] + lane;
     const int hw = a.warp_hwords[w];
     int2 *bnd = a.bnd + a.warp_bnd[w] + lane;
@@ -232,13 +240,17 @@ __global__ void __launch_bounds__(128) k_dp16x2(Dp16Args a)
             bnd[0] = make_int2(int(sUp), int(fUp));
         }
 
-        // Columns 1..M.
-        uint32_t hword = 0;
+        // Columns 1..M.  The next column's boundary entry and code word are loaded one column
+        // ahead so their latency hides behind this column's R rows.
+        uint32_t hword = codes[0];
+        int2 up = bnd[32];
         for (int j = 1; j <= M; ++j) {
-            if (((j - 1) & 3) == 0) hword = codes[int64_t((j - 1) >> 2) * 32];
             const uint32_t hsel = hsel_of(hword >> (8 * ((j - 1) & 3)));
-            const int2 up = bnd[int64_t(j) * 32];
             uint32_t sUp = uint32_t(up.x), fUp = uint32_t(up.y);
+            if (j < M) {
+                up = bnd[int64_t(j + 1) * 32];
+                if ((j & 3) == 0) hword = codes[int64_t(j >> 2) * 32];
+            }
             uint32_t diag = diagNext;
             diagNext = sUp;
 #pragma unroll
@@ -287,6 +299,21 @@ __global__ void __launch_bounds__(128) k_dp16x2(Dp16Args a)
     }
     (void)mh;
     (void)nh;
+}
+
+// Persistent kernel: each warp takes the next work item (32 slots of the length-sorted order,
+// longest first) from an atomic counter until the queue is empty.
+template <bool AFFINE, int R, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_dp16x2(Dp16Args a)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(a.task_counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= a.num_tasks) break;
+        dp16x2_slot<AFFINE, R>(a, t, lane);
+    }
 }
 
 }  // namespace gba

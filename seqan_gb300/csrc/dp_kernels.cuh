@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(128) k_dp_strip(DpArgs a)
     const int64_t slot = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (slot >= a.num_slots) return;
     const int p = a.order[slot];
+    if (p < 0) return;   // padding slot (per-bucket launches start on a warp boundary)
     const PairDesc d = a.pairs[p];
     const int m = d.m, n = d.n;
     const int INF = d.inf;

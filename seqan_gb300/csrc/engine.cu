@@ -15,9 +15,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -85,7 +87,18 @@ struct gba_plan {
     int64_t num16 = 0;              // slots (two pairs each)
     int rows16 = 32;                // rows per register strip
     int64_t codes_total = 0, bnd16_total = 0;
-    DevBuf slots16, warp_codes, warp_hwords, codes16, warp_bnd16, bnd16;
+    DevBuf slots16, warp_codes, warp_hwords, codes16, warp_bnd16, bnd16, counter16;
+    int32_t tasks16 = 0;
+    int64_t grid16[8] = {};         // resident blocks of each packed-kernel variant
+    int variant16 = 0;              // chosen tiling variant
+    bool tune_pending = false;      // autotune at the first run
+    int64_t tune_key = 0;
+    int32_t launches = 0;           // kernels one run launches
+    // Plain per-bucket mode: general kernel launched once per length bucket.
+    std::vector<int64_t> bucket_start, bucket_count;
+    // Captured launch sequence (replayed while the device pointers stay the same).
+    cudaGraphExec_t graph = nullptr;
+    const void *graph_key[5] = {};
     int64_t seg_dense_total = -1, cig_dense_total = -1;
     bool owned = true;
     void release()
@@ -94,8 +107,15 @@ struct gba_plan {
                          &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots, &seg_slot_off,
                          &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
                          &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
-                         &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16};
+                         &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16};
         for (DevBuf *b : all) b->release();
+        drop_graph();
+    }
+    void drop_graph()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        for (auto &k : graph_key) k = nullptr;
     }
     size_t device_bytes() const
     {
@@ -104,7 +124,7 @@ struct gba_plan {
                                &seg_slot_off, &seg_count, &seg_dense_off, &seg_dense, &seg_count64,
                                &cig_slots, &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense,
                                &cig_count64, &cub_tmp, &slots16, &warp_codes, &warp_hwords, &codes16,
-                               &warp_bnd16, &bnd16};
+                               &warp_bnd16, &bnd16, &counter16};
         size_t s = 0;
         for (const DevBuf *b : all) s += b->cap;
         return s;
@@ -112,6 +132,7 @@ struct gba_plan {
 };
 
 struct gba_context {
+    std::map<int64_t, int> tuning;  // batch shape -> packed-kernel variant (autotuner results)
     int device = 0;
     int64_t budget = 0;
     cudaStream_t stream = nullptr;
@@ -237,6 +258,54 @@ int upload(gba_context *ctx, DevBuf &buf, const std::vector<T> &v)
     return GBA_OK;
 }
 
+// Tiling variants of the packed kernel: rows per register strip x minimum resident blocks per
+// SM (which caps registers per thread).  The autotuner times them on the real batch.
+struct Variant16 {
+    int rows, minb;
+};
+constexpr Variant16 kVariants16[] = {{32, 2}, {32, 3}, {24, 3}, {24, 4}, {16, 4}};
+constexpr int kNumVariants16 = int(sizeof(kVariants16) / sizeof(kVariants16[0]));
+
+const void *dp16_fn(int v, bool affine)
+{
+#define GBA_V16(R, B) (affine ? (const void *)k_dp16x2<true, R, B> : (const void *)k_dp16x2<false, R, B>)
+    switch (v) {
+    case 0: return GBA_V16(32, 2);
+    case 1: return GBA_V16(32, 3);
+    case 2: return GBA_V16(24, 3);
+    case 3: return GBA_V16(24, 4);
+    default: return GBA_V16(16, 4);
+    }
+#undef GBA_V16
+}
+
+void launch_dp16(int v, bool affine, int grid, const Dp16Args &a, cudaStream_t st)
+{
+#define GBA_L16(R, B)                                                         \
+    do {                                                                      \
+        if (affine) k_dp16x2<true, R, B><<<grid, kBlock, 0, st>>>(a);         \
+        else k_dp16x2<false, R, B><<<grid, kBlock, 0, st>>>(a);               \
+    } while (0)
+    switch (v) {
+    case 0: GBA_L16(32, 2); break;
+    case 1: GBA_L16(32, 3); break;
+    case 2: GBA_L16(24, 3); break;
+    case 3: GBA_L16(24, 4); break;
+    default: GBA_L16(16, 4); break;
+    }
+#undef GBA_L16
+}
+
+// Resident blocks of a persistent kernel on this device (all SMs x blocks per SM).
+int64_t persistent_grid(gba_context *ctx, const void *fn)
+{
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return int64_t(sms) * per_sm;
+}
+
 // Builds a plan from host offsets.  `plan` buffers are (re)used.
 int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_plan *plan)
 {
@@ -261,11 +330,12 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // at most 8 codes (the caller's alphabet_size), table entries that fit a byte, and gaps that
     // keep int16 arithmetic exact (checked per pair below).
     const bool packed_ok = !plan->local && !plan->traceback && !plan->matrix && !p->band_on &&
-                           !(p->flags & GBA_FLAG_GENERAL_KERNEL) && p->alphabet_size >= 1 &&
+                           !(p->flags & (GBA_FLAG_GENERAL_KERNEL | GBA_FLAG_PLAIN_BUCKETS)) &&
+                           p->alphabet_size >= 1 &&
                            p->alphabet_size <= 8 && p->match >= -128 && p->match <= 127 &&
                            p->mismatch >= -128 && p->mismatch <= 127 && std::abs(p->gap_open) <= 1024 &&
                            std::abs(p->gap_extend) <= 1024;
-    plan->rows16 = (p->flags & GBA_FLAG_STRIP16) ? 16 : 32;
+    plan->rows16 = 32;
     std::vector<uint32_t> keys16;
     std::vector<int32_t> idx16;
     std::vector<PairDesc> desc(std::max<int64_t>(N, 1));
@@ -317,7 +387,29 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         idx.push_back(int32_t(k));
     }
     plan->trace_total = trace_off;
-    sort_desc(keys, idx);
+    plan->bucket_start.clear();
+    plan->bucket_count.clear();
+    if (p->flags & GBA_FLAG_PLAIN_BUCKETS) {
+        // The plain GPU form: pairs grouped into 8-residue buckets of max(m, n), in input order
+        // inside a bucket, one launch per bucket.  Buckets start on a warp boundary (padding
+        // slots hold -1).
+        std::vector<std::vector<int32_t>> buckets;
+        for (int32_t k : idx) {
+            const int b = std::max(desc[k].m, desc[k].n) / 8;
+            if (b >= int(buckets.size())) buckets.resize(b + 1);
+            buckets[b].push_back(k);
+        }
+        idx.clear();
+        for (auto &bk : buckets) {
+            if (bk.empty()) continue;
+            plan->bucket_start.push_back(int64_t(idx.size()));
+            plan->bucket_count.push_back(int64_t(bk.size()));
+            idx.insert(idx.end(), bk.begin(), bk.end());
+            while (idx.size() % 32) idx.push_back(-1);
+        }
+    } else {
+        sort_desc(keys, idx);
+    }
     plan->num_slots = int64_t(idx.size());
 
     // Packed path: neighbours in the length-sorted order share a thread; per warp, the code
@@ -347,7 +439,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             maxm = std::max(maxm, slots16[q].m);
             maxn = std::max(maxn, slots16[q].n);
         }
-        const int hw = (maxm + 3) / 4, vw = (maxn + plan->rows16 - 1) / plan->rows16 * (plan->rows16 / 4);
+        const int hw = (maxm + 3) / 4, vw = (maxn + 3) / 4;
         wcodes[w] = ctot;
         whw[w] = hw;
         ctot += int64_t(hw + vw) * 32;
@@ -356,6 +448,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     }
     plan->codes_total = ctot;
     plan->bnd16_total = btot;
+    plan->tasks16 = int32_t(warps16);
 
     // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
     const int64_t warps = (plan->num_slots + 31) / 32;
@@ -364,7 +457,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     for (int64_t w = 0; w < warps; ++w) {
         int maxm = 0;
         for (int64_t s = w * 32; s < std::min(plan->num_slots, (w + 1) * 32); ++s)
-            maxm = std::max(maxm, desc[idx[s]].m);
+            if (idx[s] >= 0) maxm = std::max(maxm, desc[idx[s]].m);
         wscr[w] = scr;
         scr += int64_t(maxm + 1) * 32;
     }
@@ -404,7 +497,25 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         if ((rc = upload(ctx, plan->warp_bnd16, wbnd))) return rc;
         GBA_CUDA(ctx, plan->codes16.ensure(size_t(std::max<int64_t>(ctot, 1)) * 4));
         GBA_CUDA(ctx, plan->bnd16.ensure(size_t(std::max<int64_t>(btot, 1)) * sizeof(int2)));
+        GBA_CUDA(ctx, plan->counter16.ensure(16));
+        for (int v = 0; v < kNumVariants16; ++v) plan->grid16[v] = persistent_grid(ctx, dp16_fn(v, plan->affine));
+        // Variant: forced by flags, else the context's tuning table for this batch shape, else
+        // the default; GBA_FLAG_AUTOTUNE times all variants at the first run.
+        int64_t summ = 0, sumn = 0;
+        for (const Slot16 &sl : slots16) { summ += sl.m; sumn += sl.n; }
+        const int64_t mm = summ / plan->num16, mn = sumn / plan->num16;
+        plan->tune_key = (int64_t(plan->affine) << 40) | ((mm / 32) << 20) | (mn / 32);
+        plan->variant16 = 0;
+        plan->tune_pending = false;
+        if (p->flags & GBA_FLAG_STRIP16) {
+            plan->variant16 = kNumVariants16 - 1;
+        } else {
+            auto it = ctx->tuning.find(plan->tune_key);
+            if (it != ctx->tuning.end()) plan->variant16 = it->second;
+            else if (p->flags & GBA_FLAG_AUTOTUNE) plan->tune_pending = true;
+        }
     }
+    plan->drop_graph();
     if (plan->matrix) {
         if ((rc = upload(ctx, plan->matrix_dev, plan->matrix_host))) return rc;
     }
@@ -489,22 +600,20 @@ __global__ void k_fill_invalid(const PairDesc *pairs, int64_t n, int32_t minval,
     if (cig_count) cig_count[k] = 0;
 }
 
-// Launches the kernels of a plan on device inputs.  Scores/end positions go to the given
+// Enqueues the kernels of a plan on device inputs.  Scores/end positions go to the given
 // device pointers; segments and CIGARs stay in the plan's device buffers.
-int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint8_t *dseq_v,
-             int32_t *dscore, int32_t *dend_h, int32_t *dend_v)
+int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint8_t *dseq_v,
+                 int32_t *dscore, int32_t *dend_h, int32_t *dend_v, bool capturing)
 {
+    // Inside a capture the timing events must be graph nodes (external records).
+    const unsigned evflags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     const int64_t N = plan->num_pairs;
-    ctx->stats = gba_stats{};
-    ctx->stats.cells = plan->cells;
-    ctx->stats.trace_bytes = plan->trace_total;
-    if (N == 0) return GBA_OK;
     int32_t *end_h = dend_h ? dend_h : plan->end_h.as<int32_t>();
     int32_t *end_v = dend_v ? dend_v : plan->end_v.as<int32_t>();
     const int32_t minval = plan->params.score_bits == 16 ? -32768 : INT32_MIN;
     int launches = 0;
 
-    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    GBA_CUDA(ctx, cudaEventRecordWithFlags(ctx->ev[0], ctx->stream, evflags));
     if (plan->num16 > 0) {
         Dp16Args a{};
         a.seq_h = dseq_h;
@@ -525,17 +634,16 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         a.gap_open = plan->params.gap_open;
         a.gap_extend = plan->params.gap_extend;
         a.free_ends = plan->free_ends;
-        const int grid = int((plan->num16 + kBlock - 1) / kBlock);
-        k_pack16<<<grid, kBlock, 0, ctx->stream>>>(a);
-        if (plan->rows16 == 16) {
-            if (plan->affine) k_dp16x2<true, 16><<<grid, kBlock, 0, ctx->stream>>>(a);
-            else k_dp16x2<false, 16><<<grid, kBlock, 0, ctx->stream>>>(a);
-        } else {
-            if (plan->affine) k_dp16x2<true, 32><<<grid, kBlock, 0, ctx->stream>>>(a);
-            else k_dp16x2<false, 32><<<grid, kBlock, 0, ctx->stream>>>(a);
-        }
+        a.num_tasks = plan->tasks16;
+        a.task_counter = plan->counter16.as<int32_t>();
+        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter16.ptr, 0, sizeof(int32_t), ctx->stream));
+        const int grid = int(std::min<int64_t>(plan->grid16[plan->variant16],
+                                                (int64_t(plan->tasks16) * 32 + kBlock - 1) / kBlock));
+        k_pack16<<<int((plan->num16 + kBlock - 1) / kBlock), kBlock, 0, ctx->stream>>>(a);
+        launch_dp16(plan->variant16, plan->affine, grid, a, ctx->stream);
+        ++launches;
         GBA_CUDA(ctx, cudaGetLastError());
-        launches += 2;
+        launches += 1;
     }
     if (plan->num_slots > 0) {
         DpArgs a{};
@@ -559,13 +667,25 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         a.gap_extend = plan->params.gap_extend;
         a.free_ends = plan->free_ends;
         a.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
-        const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
         const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
-        pick_dp(plan->affine, plan->local, plan->matrix, plan->traceback)(a, grid, smem, ctx->stream);
+        DpLauncher launch = pick_dp(plan->affine, plan->local, plan->matrix, plan->traceback);
+        if (!plan->bucket_start.empty()) {
+            for (size_t b = 0; b < plan->bucket_start.size(); ++b) {
+                DpArgs ab = a;
+                ab.order = a.order + plan->bucket_start[b];
+                ab.warp_scratch = a.warp_scratch + plan->bucket_start[b] / 32;
+                ab.num_slots = plan->bucket_count[b];
+                launch(ab, int((ab.num_slots + kBlock - 1) / kBlock), smem, ctx->stream);
+                ++launches;
+            }
+            --launches;
+        } else {
+            launch(a, int((plan->num_slots + kBlock - 1) / kBlock), smem, ctx->stream);
+        }
         GBA_CUDA(ctx, cudaGetLastError());
         ++launches;
     }
-    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+    GBA_CUDA(ctx, cudaEventRecordWithFlags(ctx->ev[1], ctx->stream, evflags));
     {
         const int grid = int((N + 255) / 256);
         k_fill_invalid<<<grid, 256, 0, ctx->stream>>>(
@@ -626,11 +746,71 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         }
         GBA_CUDA(ctx, cudaGetLastError());
     }
-    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
-    ctx->stats.kernel_launches = launches;
-    ctx->stats_pending = true;
+    GBA_CUDA(ctx, cudaEventRecordWithFlags(ctx->ev[2], ctx->stream, evflags));
+    plan->launches = launches;
+    return GBA_OK;
+}
+
+// Runs a plan: the first run with a given set of device pointers captures the launch sequence
+// into a CUDA graph; later runs with the same pointers replay it with one graph launch.
+int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint8_t *dseq_v,
+             int32_t *dscore, int32_t *dend_h, int32_t *dend_v, bool allow_graph = true)
+{
+    ctx->stats = gba_stats{};
+    ctx->stats.cells = plan->cells;
+    ctx->stats.trace_bytes = plan->trace_total;
     plan->seg_dense_total = -1;
     plan->cig_dense_total = -1;
+    if (plan->num_pairs == 0) return GBA_OK;
+    if (plan->tune_pending) {
+        // Autotune: run every tiling variant once on this batch (each run computes the same
+        // results), keep the fastest for this context and batch shape.
+        float best_ms = 1e30f;
+        int best_v = 0;
+        for (int v = 0; v < kNumVariants16; ++v) {
+            plan->variant16 = v;
+            const int rc = enqueue_plan(ctx, plan, dseq_h, dseq_v, dscore, dend_h, dend_v, false);
+            if (rc) return rc;
+            GBA_CUDA(ctx, cudaEventSynchronize(ctx->ev[1]));
+            float ms = 0;
+            GBA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+            if (ms < best_ms) { best_ms = ms; best_v = v; }
+        }
+        plan->variant16 = best_v;
+        plan->tune_pending = false;
+        ctx->tuning[plan->tune_key] = best_v;
+        plan->drop_graph();
+    }
+    const void *key[5] = {dseq_h, dseq_v, dscore, dend_h, dend_v};
+    const bool use_graph = allow_graph && !(plan->params.flags & GBA_FLAG_NO_GRAPH);
+    if (use_graph && plan->graph && std::equal(key, key + 5, plan->graph_key)) {
+        GBA_CUDA(ctx, cudaGraphLaunch(plan->graph, ctx->stream));
+    } else if (use_graph) {
+        plan->drop_graph();
+        GBA_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_plan(ctx, plan, dseq_h, dseq_v, dscore, dend_h, dend_v, true);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (ec != cudaSuccess) return fail(ctx, GBA_ECUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return fail(ctx, GBA_ECUDA, "graph instantiate failed: %s", cudaGetErrorString(ei));
+        plan->graph = exec;
+        std::copy(key, key + 5, plan->graph_key);
+        GBA_CUDA(ctx, cudaGraphLaunch(plan->graph, ctx->stream));
+    } else {
+        const int rc = enqueue_plan(ctx, plan, dseq_h, dseq_v, dscore, dend_h, dend_v, false);
+        if (rc) return rc;
+    }
+    ctx->stats.kernel_launches = plan->launches;
+    ctx->stats.tile_rows = plan->num16 ? kVariants16[plan->variant16].rows : 0;
+    ctx->stats.tile_min_blocks = plan->num16 ? kVariants16[plan->variant16].minb : 0;
+    ctx->stats_pending = true;
     return GBA_OK;
 }
 
@@ -766,8 +946,10 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
     if (!ctx || !result) return GBA_EINVAL;
     GBA_CUDA(ctx, cudaSetDevice(ctx->device));
     gba_plan *plan = &ctx->oneshot;
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = build_plan(ctx, params, batch, plan);
     if (rc) return rc;
+    const float plan_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     const int64_t N = batch->num_pairs;
     if (N == 0) {
         if (plan->traceback && result->segment_offsets) result->segment_offsets[0] = 0;
@@ -784,8 +966,10 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
         GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_v.ptr, batch->seq_v, plan->seq_v_bytes, cudaMemcpyHostToDevice,
                                       ctx->stream));
     GBA_CUDA(ctx, ctx->out_score.ensure(size_t(N) * 4));
+    // A one-shot batch is planned anew on every call, so a captured graph would never be
+    // replayed: launch directly.
     rc = run_plan(ctx, plan, ctx->seq_h.as<uint8_t>(), ctx->seq_v.as<uint8_t>(), ctx->out_score.as<int32_t>(),
-                  nullptr, nullptr);
+                  nullptr, nullptr, false);
     if (rc) return rc;
     if (result->score)
         GBA_CUDA(ctx, cudaMemcpyAsync(result->score, ctx->out_score.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -797,7 +981,10 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
     if (rc) return rc;
     GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (result->pair_status) std::memcpy(result->pair_status, plan->status.data(), N * 4);
-    return finish_stats(ctx);
+    rc = finish_stats(ctx);
+    ctx->stats.host_plan_ms = plan_ms;
+    ctx->stats.call_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
 }
 
 GBA_API int gba_plan_create(gba_context *ctx, const gba_params *params, const gba_batch *host_batch,

@@ -178,3 +178,57 @@ def test_packed_kernel_against_oracle(engine, flags, fe):
             assert np.array_equal(out.score, ref.score) and np.array_equal(gen.score, ref.score)
             assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
             assert np.array_equal(out.status, gen.status)
+
+
+@pytest.mark.parametrize("flags", [4, 8, 1 | 8])
+def test_plain_buckets_and_direct_launch(engine, flags):
+    """The plain per-bucket form and direct (non-graph) launches give the same results."""
+    import seqan_gb300 as sg
+    H, V = _random_pairs(77, 500, 1, 300)
+    sc = sg.Score(2, -4, -1, -6, dtype=np.int16)
+    out = sg.align_codes(H, V, sc, alphabet_size=4, flags=flags)
+    ref = O.oracle_batch(O.Problem("global", 0, None, 2, -4, -6, -1, None, 16), H, V)
+    assert np.array_equal(out.score, ref.score)
+    assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+
+
+def test_device_resident_plan_replays_graph(engine):
+    """gba_plan_execute twice on the same device buffers (the second run replays the captured
+    graph) gives the oracle's scores both times."""
+    import ctypes as C
+    import seqan_gb300 as sg
+    from seqan_gb300 import _native as N
+    L, h = N.lib(), engine.handle
+    H, V = _random_pairs(78, 700, 50, 300)
+    sh, oh = sg.align._concat(H)
+    sv, ov = sg.align._concat(V)
+    n = len(H)
+    params = sg.align.make_params(sg.Score(2, -4, -1, -6, dtype=np.int16), 0, None, None,
+                                  N.GBA_OUT_SCORE | N.GBA_OUT_END, alphabet_size=4)
+    hb = N.GbaBatch(n, sh.ctypes.data, oh.ctypes.data, sv.ctypes.data, ov.ctypes.data, 0, 0)
+    ptrs = []
+
+    def dev(nbytes, src=None):
+        p = C.c_void_p()
+        engine.check(L.gba_device_alloc(h, C.byref(p), nbytes), "alloc")
+        if src is not None:
+            engine.check(L.gba_copy_to_device(h, p, src.ctypes.data, nbytes), "h2d")
+        ptrs.append(p)
+        return p
+
+    d_sh, d_sv = dev(sh.nbytes, sh), dev(sv.nbytes, sv)
+    d_sc, d_eh, d_ev = dev(4 * n), dev(4 * n), dev(4 * n)
+    plan = C.c_void_p()
+    engine.check(L.gba_plan_create(h, C.byref(params), C.byref(hb), C.byref(plan)), "plan")
+    db = N.GbaBatch(n, d_sh, None, d_sv, None, 0, 0)
+    dr = N.GbaResult()
+    dr.score, dr.end_h, dr.end_v = d_sc, d_eh, d_ev
+    ref = O.oracle_batch(O.Problem("global", 0, None, 2, -4, -6, -1, None, 16), H, V)
+    for _ in range(2):
+        engine.check(L.gba_plan_execute(h, plan, C.byref(db), C.byref(dr)), "execute")
+        got = np.zeros(n, np.int32)
+        engine.check(L.gba_copy_to_host(h, got.ctypes.data, d_sc, 4 * n), "d2h")
+        assert np.array_equal(got, ref.score)
+    L.gba_plan_destroy(h, plan)
+    for p in ptrs:
+        L.gba_device_free(h, p)
