@@ -300,6 +300,294 @@ static int band_valid(const orc_params *p, int m, int n, int fe)
 }
 
 /* ---------------------------------------------------------------------------------
+ * Banded DP (align/dp_algorithm_impl.h:586-967).  Cells are stored densely by (column, row);
+ * the reference's band-indexed storage only changes addressing.  A "track" computes rows
+ * [r0, r1] of one column like _computeTrack (:334-429): first cell, inner cells, last cell,
+ * with the recursion direction and tracking flag of each cell taken from DPMetaColumn_
+ * (align/dp_meta_info.h:178-370) for the column's type and location.
+ * ------------------------------------------------------------------------------- */
+enum { COL_INITIAL, COL_INNER, COL_FINAL };
+enum { LOC_FULL, LOC_TOP, LOC_MIDDLE, LOC_BOTTOM };
+
+typedef struct {
+    const ctx_t *c;
+    int fe, m, n;
+    const uint8_t *h, *v;
+    int *S, *E;          /* dense (m+1) x (n+1), column-major */
+    uint8_t *T;
+    best_t *b;
+    caches_t k;          /* caches of the current track */
+    int lastF;           /* cacheVert F after the last computed cell */
+    int upper;
+    int *Fslot;          /* F field of the band column's storage, one slot per diagonal */
+    int nslots;
+} band_t;
+
+#define BAT(bt, arr, col, row) (bt)->arr[(size_t)(col) * (size_t)((bt)->n + 1) + (size_t)(row)]
+
+static int first_dir(const band_t *bt, int type, int loc)
+{
+    if (type == COL_INITIAL) return DIR_ZERO;
+    if (loc == LOC_FULL || loc == LOC_TOP) return (bt->fe & ORC_FREE_TOP) ? DIR_ZERO : DIR_HORIZONTAL;
+    return DIR_UPPER;
+}
+static int inner_dir(const band_t *bt, int type)
+{
+    if (type == COL_INITIAL) return (bt->fe & ORC_FREE_LEFT) ? DIR_ZERO : DIR_VERTICAL;
+    return DIR_ALL;
+}
+static int last_dir(const band_t *bt, int type, int loc)
+{
+    if (type == COL_INITIAL) return (bt->fe & ORC_FREE_LEFT) ? DIR_ZERO : DIR_VERTICAL;
+    return (loc == LOC_TOP || loc == LOC_MIDDLE) ? DIR_LOWER : DIR_ALL;
+}
+/* Tracking flags of DPMetaColumn_ for first / inner / last cells. */
+static int track_flag(const band_t *bt, int type, int loc, int which /* 0 first 1 inner 2 last */)
+{
+    if (bt->c->local) return 1;
+    int lastColFree = (type == COL_FINAL) && (bt->fe & ORC_FREE_RIGHT);
+    if (which < 2) return lastColFree;
+    if (loc == LOC_FULL || loc == LOC_BOTTOM) return (type == COL_FINAL) || (bt->fe & ORC_FREE_BOTTOM);
+    return lastColFree;
+}
+
+static void band_cell(band_t *bt, int dir, int col, int row, int tracked)
+{
+    int f;
+    /* The horizontal neighbour (row, col-1): its S/E are read through the dense arrays. */
+    int sh = col > 0 ? BAT(bt, S, col - 1, row) : bt->c->inf;
+    int eh = col > 0 ? BAT(bt, E, col - 1, row) : bt->c->inf;
+    int tv = compute_cell(bt->c, dir, &sh, &eh, &bt->k,
+                          col > 0 ? bt->h[col - 1] : 0, row > 0 ? bt->v[row - 1] : 0, &f);
+    if (dir == DIR_ZERO) {
+        /* Zero leaves the cell's stored E as it was (never written: infinity). */
+        eh = BAT(bt, E, col, row);
+    }
+    BAT(bt, S, col, row) = sh;
+    BAT(bt, E, col, row) = eh;
+    if (bt->T) BAT(bt, T, col, row) = (uint8_t)tv;
+    bt->lastF = f;
+    if (tracked) {
+        /* _computeCell stores cacheVert's F into the tracked cell before scouting it
+         * (align/dp_algorithm_impl.h:303-311). */
+        int slot = bt->upper - col + row;
+        if (slot >= 0 && slot < bt->nslots) bt->Fslot[slot] = f;
+        scout(bt->b, sh, eh, f, col, row);
+    }
+}
+
+/* One track: rows r0..r1 of column col (r1 > r0). */
+static void band_track(band_t *bt, int col, int type, int loc, int r0, int r1)
+{
+    int i;
+    bt->k.dS = bt->c->inf; bt->k.vS = bt->c->inf; bt->k.vF = bt->c->inf;
+    /* _preInitCacheDiagonal: partial columns that start below row 0 read the diagonal
+     * neighbour of their first cell (dp_matrix_navigator_score_matrix.h:358-392). */
+    if (type != COL_INITIAL && (loc == LOC_MIDDLE || loc == LOC_BOTTOM) && r0 > 0 && col > 0)
+        bt->k.dS = BAT(bt, S, col - 1, r0 - 1);
+    band_cell(bt, first_dir(bt, type, loc), col, r0, track_flag(bt, type, loc, 0));
+    for (i = r0 + 1; i < r1; ++i) band_cell(bt, inner_dir(bt, type), col, i, track_flag(bt, type, loc, 1));
+    band_cell(bt, last_dir(bt, type, loc), col, r1, track_flag(bt, type, loc, 2));
+}
+
+/* Re-offers the last computed cell to the scout (the reference's extra _scoutBestScore calls
+ * at phase boundaries).  The scout copies the stored cell: its F is what the band column's
+ * slot holds (written only by tracked cells of that diagonal), unless the call site refreshes
+ * it from cacheVert first (set_f). */
+static void band_retrack_f(band_t *bt, int col, int row, int set_f)
+{
+    int slot = bt->upper - col + row;
+    int inside = slot >= 0 && slot < bt->nslots;
+    if (set_f && inside) bt->Fslot[slot] = bt->lastF;
+    scout(bt->b, BAT(bt, S, col, row), BAT(bt, E, col, row), inside ? bt->Fslot[slot] : bt->c->inf, col, row);
+}
+#define band_retrack(bt, col, row) band_retrack_f((bt), (col), (row), 0)
+
+static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
+                           int lower, int upper, int *S, int *E, uint8_t *T, best_t *b, int *Fslot)
+{
+    band_t bt;
+    int hb, hTop, hMid, hBot, hIt, vb, ve, tmp;
+    bt.c = c; bt.fe = fe; bt.m = m; bt.n = n; bt.h = h; bt.v = v; bt.S = S; bt.E = E; bt.T = T; bt.b = b;
+    bt.lastF = c->inf;
+    bt.upper = upper;
+    bt.Fslot = Fslot;
+    bt.nslots = upper - lower + 1;
+    {
+        size_t cells = (size_t)(m + 1) * (size_t)(n + 1), q;
+        for (q = 0; q < cells; ++q) { S[q] = c->inf; E[q] = c->inf; }
+    }
+#define MIN(a, b) ((a) < (b) ? (a) : (b))
+#define MAX(a, b) ((a) > (b) ? (a) : (b))
+    if (upper == lower) {
+        /* Band of one diagonal: _computeHammingDistance (:970-1110). */
+        int ih = MAX(0, MIN(m - 1, upper)), ihEnd = MIN(m - 1, upper + n);
+        int iv = MAX(0, MIN(n - 1, -lower)), ivEnd = MIN(n - 1, lower + m);
+        int col = ih + (upper >= 0 ? 0 : 0), row;
+        int tr;
+        /* The first cell of the diagonal gets direction Zero. */
+        col = upper >= 0 ? MIN(m, upper) : 0;
+        row = upper >= 0 ? 0 : MIN(n, -upper);
+        bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
+        band_cell(&bt, DIR_ZERO, col, row, 0);
+        if (upper < 0) {
+            if (upper == -n) { if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, col, row); return; }
+            if (c->local) band_retrack(&bt, col, row);
+        } else if (lower > 0) {
+            if (lower == m) { if (c->local || (fe & ORC_FREE_RIGHT)) band_retrack(&bt, col, row); return; }
+            if (c->local) band_retrack(&bt, col, row);
+        } else {
+            if (c->local) band_retrack(&bt, col, row);
+        }
+        tr = c->local;
+        while (ih != ihEnd && iv != ivEnd) {
+            int prev = BAT(&bt, S, col, row);
+            ++col; ++row;
+            {
+                int s = wr(c, (long)prev + sub_score(c, h[ih], v[iv]));
+                int t = TV_DIAG;
+                if (c->local) { if (s <= 0) { s = 0; t = TV_NONE; } }
+                BAT(&bt, S, col, row) = s;
+                if (T) BAT(&bt, T, col, row) = (uint8_t)t;
+            }
+            if (tr) scout(b, BAT(&bt, S, col, row), c->inf, c->inf, col, row);
+            ++ih; ++iv;
+        }
+        /* The reference computes one more diagonal cell here.  When the diagonal leaves the
+         * matrix through its bottom row with m < -2 * lower, its end iterators let that cell
+         * read past the end of V (undefined behaviour); the restatement stops at the matrix edge
+         * instead, so parity excludes that case. */
+        if (ih > m - 1 || iv > n - 1 || col + 1 > m || row + 1 > n) return;
+        {
+            int prev = BAT(&bt, S, col, row);
+            int s, t = TV_DIAG;
+            ++col; ++row;
+            s = wr(c, (long)prev + sub_score(c, h[ih], v[iv]));
+            if (c->local) { if (s <= 0) { s = 0; t = TV_NONE; } }
+            BAT(&bt, S, col, row) = s;
+            if (T) BAT(&bt, T, col, row) = (uint8_t)t;
+            if (ih == ihEnd) {
+                if (iv == ivEnd) scout(b, s, c->inf, c->inf, col, row);   /* final column, last cell: always */
+                if (c->local || (fe & ORC_FREE_BOTTOM)) scout(b, s, c->inf, c->inf, col, row);
+            } else {
+                if (c->local || (fe & ORC_FREE_RIGHT)) scout(b, s, c->inf, c->inf, col, row);
+            }
+        }
+        return;
+    }
+
+    /* Positions of seqVBegin / seqVEnd and of the H iterators (0-based character positions). */
+    vb = -MIN(0, 1 + upper);
+    ve = -MIN(0, MAX(-n, lower));
+    hb = MAX(0, MIN(m - 1, lower));
+    hTop = MIN(m - 1, MAX(0, upper));
+    hMid = MIN(m - 1, MAX(0, n + lower));
+    if (upper > n + lower) { tmp = hTop; hTop = hMid; hMid = tmp; }
+    hBot = MAX(0, MIN(m, upper + n) - 1);
+
+    /* Bands that start in the last column or end in the first one: the reference computes a
+     * single cell (direction Zero) and stops, even when the band holds a second cell.  Its
+     * traceback does not terminate on these shapes, so they take part in score parity only;
+     * the cell is placed at the band's first cell. */
+    if (hb == m - 1) {
+        int col = MAX(0, MIN(m, lower));
+        bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
+        band_cell(&bt, DIR_ZERO, col, 0, c->local);
+        if (c->local || (fe & ORC_FREE_RIGHT)) band_retrack(&bt, col, 0);
+        return;
+    }
+    if (hBot == 0) {
+        int row = MIN(n, -upper);
+        bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
+        band_cell(&bt, DIR_ZERO, 0, row, c->local);
+        if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, 0, row);
+        return;
+    }
+
+    if (upper < 0) {
+        ++vb;
+        band_track(&bt, 0, COL_INITIAL, lower > -n ? LOC_MIDDLE : LOC_BOTTOM, vb, ve);
+    } else if (lower >= 0) {
+        bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
+        band_cell(&bt, DIR_ZERO, hb, 0, c->local);
+        if (c->local) band_retrack(&bt, hb, 0);
+    } else {
+        band_track(&bt, 0, COL_INITIAL, lower <= -n ? LOC_FULL : LOC_TOP, vb, ve);
+    }
+
+    hIt = hb;
+    for (; hIt != hTop; ++hIt) {
+        ++ve;
+        band_track(&bt, hIt + 1, COL_INNER, LOC_TOP, vb, ve);
+    }
+    if (upper > n + lower) {
+        if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, hIt, ve);
+        for (; hIt != hMid; ++hIt) band_track(&bt, hIt + 1, COL_INNER, LOC_FULL, vb, ve);
+    } else {
+        for (; hIt != hMid; ++hIt) {
+            ++vb; ++ve;
+            band_track(&bt, hIt + 1, COL_INNER, LOC_MIDDLE, vb, ve);
+        }
+        if ((c->local || (fe & ORC_FREE_BOTTOM)) && lower + n < m) band_retrack(&bt, hIt, ve);
+    }
+    for (; hIt != hBot; ++hIt) {
+        ++vb;
+        band_track(&bt, hIt + 1, COL_INNER, LOC_BOTTOM, vb, ve);
+    }
+
+    /* Last band column. */
+    if (hIt < m - 1) {
+        /* The band ends before the final column: one cell (first cell of a bottom column). */
+        bt.k.dS = BAT(&bt, S, hIt, vb); bt.k.vS = c->inf; bt.k.vF = c->inf;
+        band_cell(&bt, DIR_UPPER, hIt + 1, vb + 1, c->local);
+        if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack_f(&bt, hIt + 1, vb + 1, 1);
+    } else if (hIt == m - 1) {
+        if (upper == m - n) {
+            bt.k.dS = BAT(&bt, S, hIt, vb); bt.k.vS = c->inf; bt.k.vF = c->inf;
+            band_cell(&bt, DIR_UPPER, m, vb + 1, c->local || (fe & ORC_FREE_RIGHT));
+            band_retrack_f(&bt, m, vb + 1, 1);
+        } else if (upper >= m) {
+            if (lower + n > m) {
+                ++ve;
+                band_track(&bt, m, COL_FINAL, LOC_TOP, vb, ve);
+            } else if (lower + n + 1 > m) {
+                ++ve;
+                band_track(&bt, m, COL_FINAL, LOC_TOP, vb, ve);
+                band_retrack_f(&bt, m, ve, 1);
+            } else {
+                band_track(&bt, m, COL_FINAL, LOC_FULL, vb, ve);
+            }
+        } else {
+            ++vb;
+            if (lower + n <= m) {
+                if (lower + n == m) {
+                    ++ve;
+                    band_track(&bt, m, COL_FINAL, LOC_MIDDLE, vb, ve);
+                    band_retrack_f(&bt, m, ve, 1);
+                } else {
+                    band_track(&bt, m, COL_FINAL, LOC_BOTTOM, vb, ve);
+                }
+            } else {
+                ++ve;
+                band_track(&bt, m, COL_FINAL, LOC_MIDDLE, vb, ve);
+            }
+        }
+    }
+#undef MIN
+#undef MAX
+}
+
+static void dp_banded(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
+                      int lower, int upper, int *S, int *E, uint8_t *T, best_t *b)
+{
+    int slots = upper - lower + 1, q;
+    int *Fslot = (int *)malloc(sizeof(int) * (size_t)(slots > 0 ? slots : 1));
+    for (q = 0; q < slots; ++q) Fslot[q] = c->inf;
+    dp_banded_impl(c, fe, h, m, v, n, lower, upper, S, E, T, b, Fslot);
+    free(Fslot);
+}
+
+/* ---------------------------------------------------------------------------------
  * Unbanded DP (align/dp_algorithm_impl.h:483-579 with dp_meta_info.h:178-221).
  * ------------------------------------------------------------------------------- */
 static void dp_unbanded(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
@@ -364,19 +652,20 @@ int orc_align_pair(const orc_params *p,
         out->n_segments = 0;
         return 0;
     }
-    if (p->band_on) {
-        /* Banded columns are restated in a later revision of this file. */
-        out->score = 0;
-        out->valid = -1;
-        return 1;
-    }
     out->valid = 1;
     colS = (int *)malloc(sizeof(int) * (size_t)(n + 1) * 2);
     colE = colS + (n + 1);
-    if (p->traceback) T = (uint8_t *)malloc((size_t)(m + 1) * (size_t)(n + 1));
+    if (p->traceback) T = (uint8_t *)calloc((size_t)(m + 1) * (size_t)(n + 1), 1);
     b.s = c.inf; b.e = c.inf; b.f = c.inf; b.col = 0; b.row = 0;
 
-    dp_unbanded(&c, fe, h, m, v, n, colS, colE, T, &b);
+    if (p->band_on) {
+        int *S = (int *)malloc(sizeof(int) * (size_t)(m + 1) * (size_t)(n + 1) * 2);
+        if (!T) T = NULL;
+        dp_banded(&c, fe, h, m, v, n, p->band_lower, p->band_upper, S, S + (size_t)(m + 1) * (size_t)(n + 1), T, &b);
+        free(S);
+    } else {
+        dp_unbanded(&c, fe, h, m, v, n, colS, colE, T, &b);
+    }
 
     out->score = b.s;
     out->end_h = b.col;

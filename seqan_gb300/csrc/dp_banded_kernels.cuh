@@ -1,0 +1,427 @@
+// dp_banded_kernels.cuh -- banded DP (DPBandConfig<BandOn>), one pair per thread.
+//
+// Follows the reference's banded column phases exactly (align/dp_algorithm_impl.h:586-967):
+// an initial column, columns attached to the top of the matrix, middle or full columns,
+// columns attached to the bottom, and the final column, each computed as a "track" of rows
+// [r0, r1] whose first, inner and last cells take the recursion direction and tracking flag
+// of DPMetaColumn_ (align/dp_meta_info.h:178-370); band width 1 runs the reference's
+// diagonal-only path (:970-1110).  The extra best-cell offers at phase boundaries are made
+// with the F value the reference's band storage holds for that cell (the column of the band is
+// stored one slot per diagonal, so a slot keeps the F of the last tracked cell on its
+// diagonal unless the call site refreshes it).
+//
+// Band state: per thread, slot k = upper - col + row (one per diagonal) of S, E and the stored
+// F, in per-thread arrays (local memory, L1-resident).  Trace: one byte per band slot per
+// column (the reference's TraceBitMap_ bits).
+#pragma once
+
+#include "dp_common.cuh"
+
+namespace gba {
+
+struct BandArgs {
+    const uint8_t *seq_h;
+    const uint8_t *seq_v;
+    const PairDesc *pairs;
+    const int32_t *order;
+    uint8_t *trace;                // per pair at PairDesc::trace_off: (m + 1) * W bytes
+    int32_t *score, *end_h, *end_v, *best_e, *best_f;
+    const int32_t *matrix;
+    int64_t num_slots;
+    int32_t match, mismatch, gap_open, gap_extend;
+    int32_t free_ends;
+    int32_t alphabet;
+    int32_t lower, upper;
+};
+
+enum { BCOL_INITIAL = 0, BCOL_INNER = 1, BCOL_FINAL = 2 };
+enum { BLOC_FULL = 0, BLOC_TOP = 1, BLOC_MIDDLE = 2, BLOC_BOTTOM = 3 };
+enum { BDIR_ZERO = 0, BDIR_ALL, BDIR_HORIZONTAL, BDIR_VERTICAL, BDIR_UPPER, BDIR_LOWER };
+
+template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX>
+struct BandedPair {
+    const BandArgs &a;
+    const int *smat;
+    const uint8_t *H, *V;
+    uint8_t *T;
+    int m, n, W, lower, upper, INF;
+    bool fTop, fLeft, fRight, fBottom;
+    int OPEN, EXT;
+    int S[WMAX], E[WMAX], Fs[WMAX];
+    // caches of the current track
+    int dS, vS, vF, lastF;
+    // scout (strict '>' in the reference's visiting order)
+    int bs, be, bf, bcol, brow;
+
+    __device__ BandedPair(const BandArgs &args, const int *sm) : a(args), smat(sm) {}
+
+    __device__ __forceinline__ int sub(int col, int row) const
+    {
+        const int hc = H[col - 1], vc = V[row - 1];
+        if (MATRIX) return smat[((hc & 31) << 5) | (vc & 31)];
+        return hc == vc ? a.match : a.mismatch;
+    }
+    __device__ __forceinline__ void scout(int s, int e, int f, int col, int row)
+    {
+        if (s > bs) { bs = s; be = e; bf = f; bcol = col; brow = row; }
+    }
+    __device__ __forceinline__ int slot(int col, int row) const { return upper - col + row; }
+    __device__ __forceinline__ bool in_slots(int k) const { return k >= 0 && k < W; }
+
+    // One cell; the horizontal neighbour (row, col - 1) is slot k + 1 of the previous column,
+    // which still holds it because slots are overwritten in increasing k within a column.
+    __device__ void cell(int dir, int col, int row, bool tracked)
+    {
+        const int k = slot(col, row);
+        const int hS = in_slots(k + 1) ? S[k + 1] : INF;
+        const int hE = in_slots(k + 1) ? E[k + 1] : INF;
+        const int eStored = in_slots(k) ? E[k] : INF;
+        int s, e = INF, f = vF, tv = TV_NONE;
+        switch (dir) {
+        case BDIR_ZERO:
+            s = 0;
+            e = eStored;       // stays as stored
+            dS = 0;
+            vS = 0;
+            f = vF;
+            break;
+        case BDIR_ALL: {
+            const int inter = dS + sub(col, row);
+            dS = hS;
+            if (AFFINE) {
+                int tE, tF, tm;
+                if (hE + EXT < hS + OPEN) { e = hS + OPEN; tE = TV_HO; } else { e = hE + EXT; tE = TV_H; }
+                if (vF + EXT < vS + OPEN) { f = vS + OPEN; tF = TV_VO; } else { f = vF + EXT; tF = TV_V; }
+                int g;
+                if (f < e) { g = e; tm = TV_MFH; } else { g = f; tm = TV_MFV; }
+                if (inter < g) { s = g; tv = tm | tE | tF; } else { s = inter; tv = TV_DIAG | tE | tF; }
+                vF = f;
+            } else {
+                const int gv = vS + EXT, gh = hS + EXT;
+                int g, tg;
+                if (gv < gh) { g = gh; tg = TV_H | TV_MFH; } else { g = gv; tg = TV_V | TV_MFV; }
+                if (inter < g) { s = g; tv = tg; } else { s = inter; tv = TV_DIAG; }
+                e = hE;
+            }
+            break;
+        }
+        case BDIR_HORIZONTAL:
+            dS = hS;
+            if (AFFINE) {
+                if (hE + EXT < hS + OPEN) { e = hS + OPEN; tv = TV_HO | TV_MFH; } else { e = hE + EXT; tv = TV_H | TV_MFH; }
+                vF = INF;
+                f = INF;
+                s = e;
+            } else {
+                s = hS + EXT;
+                tv = TV_H | TV_MFH;
+                e = hE;
+            }
+            break;
+        case BDIR_VERTICAL:
+            if (AFFINE) {
+                if (vF + EXT < vS + OPEN) { f = vS + OPEN; tv = TV_VO | TV_MFV; } else { f = vF + EXT; tv = TV_V | TV_MFV; }
+                vF = f;
+                e = INF;
+                s = f;
+            } else {
+                s = vS + EXT;
+                tv = TV_V | TV_MFV;
+                e = hE;
+            }
+            break;
+        case BDIR_UPPER: {
+            const int inter = dS + sub(col, row);
+            dS = hS;
+            if (AFFINE) {
+                int tE;
+                if (hE + EXT < hS + OPEN) { e = hS + OPEN; tE = TV_HO; } else { e = hE + EXT; tE = TV_H; }
+                vF = INF;
+                f = INF;
+                if (inter < e) { s = e; tv = tE | TV_MFH; } else { s = inter; tv = tE | TV_DIAG; }
+            } else {
+                const int gh = hS + EXT;
+                if (inter < gh) { s = gh; tv = TV_H | TV_MFH; } else { s = inter; tv = TV_DIAG; }
+                e = hE;
+            }
+            break;
+        }
+        default: {  // BDIR_LOWER
+            const int inter = dS + sub(col, row);
+            if (AFFINE) {
+                int tF;
+                if (vF + EXT < vS + OPEN) { f = vS + OPEN; tF = TV_VO; } else { f = vF + EXT; tF = TV_V; }
+                vF = f;
+                e = INF;
+                if (inter < f) { s = f; tv = tF | TV_MFV; } else { s = inter; tv = tF | TV_DIAG; }
+            } else {
+                const int gv = vS + EXT;
+                if (inter < gv) { s = gv; tv = TV_V | TV_MFV; } else { s = inter; tv = TV_DIAG; }
+                e = hE;
+            }
+            break;
+        }
+        }
+        if (LOCAL && dir != BDIR_ZERO) {
+            if (s <= 0) { s = 0; tv = TV_NONE; }
+        }
+        if (dir != BDIR_LOWER) vS = s;
+        lastF = f;
+        // Only the degenerate single-cell bands can produce a cell outside the band; it is
+        // scouted but not stored.
+        const bool inside = in_slots(k);
+        if (inside) {
+            S[k] = s;
+            E[k] = e;
+            if (TRACE) T[int64_t(col) * W + k] = uint8_t(tv);
+        }
+        if (tracked) {
+            if (inside) Fs[k] = f;
+            scout(s, e, f, col, row);
+        }
+    }
+
+    // The reference's extra best-cell offers at phase boundaries (see the file comment).
+    __device__ void retrack(int col, int row, bool set_f)
+    {
+        const int k = slot(col, row);
+        if (!in_slots(k)) {
+            // A degenerate single-cell band whose one cell lies outside the band: the cell
+            // just computed (direction Zero) is offered with its values.
+            scout(0, INF, INF, col, row);
+            return;
+        }
+        if (set_f) Fs[k] = lastF;
+        scout(S[k], E[k], Fs[k], col, row);
+    }
+
+    __device__ int first_dir(int type, int loc) const
+    {
+        if (type == BCOL_INITIAL) return BDIR_ZERO;
+        if (loc == BLOC_FULL || loc == BLOC_TOP) return fTop ? BDIR_ZERO : BDIR_HORIZONTAL;
+        return BDIR_UPPER;
+    }
+    __device__ int inner_dir(int type) const
+    {
+        if (type == BCOL_INITIAL) return fLeft ? BDIR_ZERO : BDIR_VERTICAL;
+        return BDIR_ALL;
+    }
+    __device__ int last_dir(int type, int loc) const
+    {
+        if (type == BCOL_INITIAL) return fLeft ? BDIR_ZERO : BDIR_VERTICAL;
+        return (loc == BLOC_TOP || loc == BLOC_MIDDLE) ? BDIR_LOWER : BDIR_ALL;
+    }
+    __device__ bool track_flag(int type, int loc, int which) const
+    {
+        if (LOCAL) return true;
+        const bool lastColFree = type == BCOL_FINAL && fRight;
+        if (which < 2) return lastColFree;
+        if (loc == BLOC_FULL || loc == BLOC_BOTTOM) return type == BCOL_FINAL || fBottom;
+        return lastColFree;
+    }
+
+    __device__ void track(int col, int type, int loc, int r0, int r1)
+    {
+        dS = INF; vS = INF; vF = INF;
+        if (type != BCOL_INITIAL && (loc == BLOC_MIDDLE || loc == BLOC_BOTTOM) && r0 > 0 && col > 0) {
+            const int kd = slot(col - 1, r0 - 1);
+            dS = in_slots(kd) ? S[kd] : INF;
+        }
+        cell(first_dir(type, loc), col, r0, track_flag(type, loc, 0));
+        for (int i = r0 + 1; i < r1; ++i) cell(inner_dir(type), col, i, track_flag(type, loc, 1));
+        cell(last_dir(type, loc), col, r1, track_flag(type, loc, 2));
+    }
+
+    __device__ void single(int dir, int col, int row, int diag_from_col, int diag_from_row, bool tracked)
+    {
+        dS = INF; vS = INF; vF = INF;
+        if (diag_from_col >= 0) {
+            const int kd = slot(diag_from_col, diag_from_row);
+            dS = in_slots(kd) ? S[kd] : INF;
+        }
+        cell(dir, col, row, tracked);
+    }
+
+    __device__ void run()
+    {
+        for (int k = 0; k < W; ++k) { S[k] = INF; E[k] = INF; Fs[k] = INF; }
+        bs = INF; be = INF; bf = INF; bcol = 0; brow = 0;
+        lastF = INF;
+        const int lo = lower, up = upper;
+        if (up == lo) {
+            // Band of one diagonal (align/dp_algorithm_impl.h:970-1110).
+            int ih = max(0, min(m - 1, up)), ihEnd = min(m - 1, up + n);
+            int iv = max(0, min(n - 1, -lo)), ivEnd = min(n - 1, lo + m);
+            int col = up >= 0 ? min(m, up) : 0;
+            int row = up >= 0 ? 0 : min(n, -up);
+            single(BDIR_ZERO, col, row, -1, 0, false);
+            if (up < 0) {
+                if (up == -n) { if (LOCAL || fBottom) retrack(col, row, false); return; }
+                if (LOCAL) retrack(col, row, false);
+            } else if (lo > 0) {
+                if (lo == m) { if (LOCAL || fRight) retrack(col, row, false); return; }
+                if (LOCAL) retrack(col, row, false);
+            } else {
+                if (LOCAL) retrack(col, row, false);
+            }
+            int prev = 0;
+            while (ih != ihEnd && iv != ivEnd) {
+                ++col; ++row;
+                int s = prev + (MATRIX ? smat[((H[ih] & 31) << 5) | (V[iv] & 31)] : (H[ih] == V[iv] ? a.match : a.mismatch));
+                int tv = TV_DIAG;
+                if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
+                if (TRACE) T[int64_t(col) * W] = uint8_t(tv);
+                if (LOCAL) scout(s, INF, INF, col, row);
+                prev = s;
+                ++ih; ++iv;
+            }
+            if (ih > m - 1 || iv > n - 1 || col + 1 > m || row + 1 > n) return;
+            ++col; ++row;
+            int s = prev + (MATRIX ? smat[((H[ih] & 31) << 5) | (V[iv] & 31)] : (H[ih] == V[iv] ? a.match : a.mismatch));
+            int tv = TV_DIAG;
+            if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
+            if (TRACE) T[int64_t(col) * W] = uint8_t(tv);
+            if (ih == ihEnd) {
+                if (iv == ivEnd) scout(s, INF, INF, col, row);
+                if (LOCAL || fBottom) scout(s, INF, INF, col, row);
+            } else {
+                if (LOCAL || fRight) scout(s, INF, INF, col, row);
+            }
+            return;
+        }
+
+        int vb = -min(0, 1 + up);
+        int ve = -min(0, max(-n, lo));
+        const int hb = max(0, min(m - 1, lo));
+        int hTop = min(m - 1, max(0, up));
+        int hMid = min(m - 1, max(0, n + lo));
+        if (up > n + lo) { const int t = hTop; hTop = hMid; hMid = t; }
+        const int hBot = max(0, min(m, up + n) - 1);
+
+        if (hb == m - 1) {
+            const int col = max(0, min(m, lo));
+            single(BDIR_ZERO, col, 0, -1, 0, LOCAL);
+            if (LOCAL || fRight) retrack(col, 0, false);
+            return;
+        }
+        if (hBot == 0) {
+            const int row = min(n, -up);
+            single(BDIR_ZERO, 0, row, -1, 0, LOCAL);
+            if (LOCAL || fBottom) retrack(0, row, false);
+            return;
+        }
+        if (up < 0) {
+            ++vb;
+            track(0, BCOL_INITIAL, lo > -n ? BLOC_MIDDLE : BLOC_BOTTOM, vb, ve);
+        } else if (lo >= 0) {
+            single(BDIR_ZERO, hb, 0, -1, 0, LOCAL);
+            if (LOCAL) retrack(hb, 0, false);
+        } else {
+            track(0, BCOL_INITIAL, lo <= -n ? BLOC_FULL : BLOC_TOP, vb, ve);
+        }
+        int hIt = hb;
+        for (; hIt != hTop; ++hIt) {
+            ++ve;
+            track(hIt + 1, BCOL_INNER, BLOC_TOP, vb, ve);
+        }
+        if (up > n + lo) {
+            if (LOCAL || fBottom) retrack(hIt, ve, false);
+            for (; hIt != hMid; ++hIt) track(hIt + 1, BCOL_INNER, BLOC_FULL, vb, ve);
+        } else {
+            for (; hIt != hMid; ++hIt) {
+                ++vb; ++ve;
+                track(hIt + 1, BCOL_INNER, BLOC_MIDDLE, vb, ve);
+            }
+            if ((LOCAL || fBottom) && lo + n < m) retrack(hIt, ve, false);
+        }
+        for (; hIt != hBot; ++hIt) {
+            ++vb;
+            track(hIt + 1, BCOL_INNER, BLOC_BOTTOM, vb, ve);
+        }
+        if (hIt < m - 1) {
+            single(BDIR_UPPER, hIt + 1, vb + 1, hIt, vb, LOCAL);
+            if (LOCAL || fBottom) retrack(hIt + 1, vb + 1, true);
+        } else if (hIt == m - 1) {
+            if (up == m - n) {
+                single(BDIR_UPPER, m, vb + 1, hIt, vb, LOCAL || fRight);
+                retrack(m, vb + 1, true);
+            } else if (up >= m) {
+                if (lo + n > m) {
+                    ++ve;
+                    track(m, BCOL_FINAL, BLOC_TOP, vb, ve);
+                } else if (lo + n + 1 > m) {
+                    ++ve;
+                    track(m, BCOL_FINAL, BLOC_TOP, vb, ve);
+                    retrack(m, ve, true);
+                } else {
+                    track(m, BCOL_FINAL, BLOC_FULL, vb, ve);
+                }
+            } else {
+                ++vb;
+                if (lo + n <= m) {
+                    if (lo + n == m) {
+                        ++ve;
+                        track(m, BCOL_FINAL, BLOC_MIDDLE, vb, ve);
+                        retrack(m, ve, true);
+                    } else {
+                        track(m, BCOL_FINAL, BLOC_BOTTOM, vb, ve);
+                    }
+                } else {
+                    ++ve;
+                    track(m, BCOL_FINAL, BLOC_MIDDLE, vb, ve);
+                }
+            }
+        }
+    }
+};
+
+template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX>
+__global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
+{
+    extern __shared__ int smat[];
+    if (MATRIX) {
+        for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+            const int r = i >> 5, c = i & 31;
+            smat[i] = (r < a.alphabet && c < a.alphabet) ? a.matrix[r * a.alphabet + c] : 0;
+        }
+        __syncthreads();
+    }
+    const int64_t slot = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (slot >= a.num_slots) return;
+    const int p = a.order[slot];
+    if (p < 0) return;
+    const PairDesc d = a.pairs[p];
+    BandedPair<AFFINE, LOCAL, MATRIX, TRACE, WMAX> bp(a, smat);
+    bp.m = d.m;
+    bp.n = d.n;
+    bp.W = a.upper - a.lower + 1;
+    bp.lower = a.lower;
+    bp.upper = a.upper;
+    bp.INF = d.inf;
+    bp.H = a.seq_h + d.h_off;
+    bp.V = a.seq_v + d.v_off;
+    bp.T = TRACE ? a.trace + d.trace_off : nullptr;
+    const int fe = LOCAL ? (FREE_TOP | FREE_LEFT | FREE_RIGHT | FREE_BOTTOM) : a.free_ends;
+    bp.fTop = fe & FREE_TOP;
+    bp.fLeft = fe & FREE_LEFT;
+    bp.fRight = fe & FREE_RIGHT;
+    bp.fBottom = fe & FREE_BOTTOM;
+    bp.OPEN = AFFINE ? a.gap_open : a.gap_extend;
+    bp.EXT = a.gap_extend;
+    bp.run();
+    a.score[p] = bp.bs;
+    if (a.end_h) a.end_h[p] = bp.bcol;
+    if (a.end_v) a.end_v[p] = bp.brow;
+    if (a.best_e) a.best_e[p] = bp.be;
+    if (a.best_f) a.best_f[p] = bp.bf;
+}
+
+// Trace byte of (col, row) in a banded trace matrix; cells outside the band read as NONE.
+__device__ __forceinline__ uint8_t trace_at_band(const uint8_t *base, int W, int upper, int col, int row)
+{
+    const int k = upper - col + row;
+    if (k < 0 || k >= W) return TV_NONE;
+    return base[int64_t(col) * W + k];
+}
+
+}  // namespace gba

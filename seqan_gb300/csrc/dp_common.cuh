@@ -32,7 +32,7 @@ struct PairDesc {
     int32_t m;           // |H| (columns)
     int32_t n;           // |V| (rows)
     int32_t inf;         // DPCellDefaultInfinity of the cell width the pair runs with
-    int32_t pad;
+    int32_t invalid;     // 1: empty sequence or band outside the matrix (score = numeric min)
 };
 
 // Arguments of the DP kernels, passed by value.
@@ -76,6 +76,8 @@ struct TraceArgs {
     int64_t num_slots;
     int32_t affine;
     int32_t local;
+    int32_t band_w;        // 0: strip layout; else banded layout with this many slots per column
+    int32_t band_upper;
 };
 
 __host__ __device__ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }

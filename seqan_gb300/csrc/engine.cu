@@ -9,6 +9,7 @@
 #include "dp_kernels.cuh"
 #include "traceback_kernels.cuh"
 #include "dp16x2_kernels.cuh"
+#include "dp_banded_kernels.cuh"
 #include "int_peak.cuh"
 
 #include <cub/device/device_scan.cuh>
@@ -171,6 +172,29 @@ int fail(gba_context *ctx, int code, const char *fmt, ...)
     } while (0)
 
 constexpr int kBlock = 128;
+constexpr int kMaxBandWidth = 512;   // band slots a thread keeps (local memory)
+
+// _checkBandProperties (align/dp_algorithm_impl.h:193-234): the band must meet the matrix and
+// may leave it only across sides whose end gaps are free.
+bool band_valid(const gba_params &p, int64_t m, int64_t n, int fe)
+{
+    const int64_t lo = p.band_lower, up = p.band_upper;
+    if (up < -n || lo > m) return false;
+    if (up < 0 && !(fe & GBA_FREE_LEFT)) return false;
+    if (lo > 0 && !(fe & GBA_FREE_TOP)) return false;
+    if (up + n < m && !(fe & GBA_FREE_BOTTOM)) return false;
+    if (lo + n > m && !(fe & GBA_FREE_RIGHT)) return false;
+    return true;
+}
+
+// In-band cells (i, j), 1 <= i <= n, 1 <= j <= m, lower <= j - i <= upper.
+int64_t band_cells(int64_t m, int64_t n, int64_t lo, int64_t up)
+{
+    int64_t c = 0;
+    for (int64_t dg = std::max(lo, 1 - n); dg <= std::min(up, m - 1); ++dg)
+        c += std::min(n, m - dg) - std::max<int64_t>(1, 1 - dg) + 1;
+    return c;
+}
 
 bool is_affine(const gba_params &p)
 {
@@ -221,7 +245,11 @@ int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
     if (b->num_pairs < 0) return fail(ctx, GBA_EINVAL, "negative num_pairs");
     if (b->num_pairs > 0 && (!b->off_h || !b->off_v || !b->seq_h || !b->seq_v))
         return fail(ctx, GBA_EINVAL, "null sequence or offset pointer");
-    if (p->band_on) return fail(ctx, GBA_EUNSUPPORTED, "banded DP is not enabled in this build");
+    if (p->band_on) {
+        if (p->band_lower > p->band_upper) return fail(ctx, GBA_EINVAL, "band_lower > band_upper");
+        if (int64_t(p->band_upper) - p->band_lower + 1 > kMaxBandWidth)
+            return fail(ctx, GBA_EUNSUPPORTED, "band wider than %d diagonals", kMaxBandWidth);
+    }
     if ((p->outputs & GBA_OUT_CIGAR) && !(p->outputs & GBA_OUT_SEGMENTS))
         return fail(ctx, GBA_EINVAL, "GBA_OUT_CIGAR requires GBA_OUT_SEGMENTS");
     return GBA_OK;
@@ -338,6 +366,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->rows16 = 32;
     std::vector<uint32_t> keys16;
     std::vector<int32_t> idx16;
+    std::map<uint64_t, int64_t> band_cell_cache;
     std::vector<PairDesc> desc(std::max<int64_t>(N, 1));
     std::vector<uint32_t> keys;
     std::vector<int32_t> idx;
@@ -362,18 +391,29 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         d.m = int32_t(h1 - h0);
         d.n = int32_t(v1 - v0);
         d.trace_off = 0;
-        d.pad = 0;
+        d.invalid = 0;
         bool exact16 = p->score_bits == 16 && int16_exact(*p, max_pos, d.m, d.n, plan->local);
         d.inf = exact16 ? -16384 : -(1 << 30);
         if (p->score_bits == 16 && !exact16) plan->status[k] = GBA_PAIR_PROMOTED;
-        if (d.m == 0 || d.n == 0) {
+        const int fe_all = plan->local ? 15 : p->free_ends;
+        if (d.m == 0 || d.n == 0 || (p->band_on && !band_valid(*p, d.m, d.n, fe_all))) {
             plan->status[k] = GBA_PAIR_INVALID;
+            d.invalid = 1;
             continue;
         }
-        plan->cells += int64_t(d.m) * d.n;
+        if (p->band_on) {
+            const uint64_t ck = (uint64_t(d.m) << 32) | uint32_t(d.n);
+            auto it = band_cell_cache.find(ck);
+            if (it == band_cell_cache.end())
+                it = band_cell_cache.emplace(ck, band_cells(d.m, d.n, p->band_lower, p->band_upper)).first;
+            plan->cells += it->second;
+        } else {
+            plan->cells += int64_t(d.m) * d.n;
+        }
         if (plan->traceback) {
             d.trace_off = trace_off;
-            trace_off += trace_bytes(d.m, d.n);
+            trace_off += p->band_on ? align16(int64_t(d.m + 1) * (p->band_upper - p->band_lower + 1))
+                                    : trace_bytes(d.m, d.n);
         }
         if (packed_ok && int16_exact(*p, max_pos, d.m, d.n, false)) {
             const int64_t strips = (d.n + plan->rows16 - 1) / plan->rows16;
@@ -560,6 +600,27 @@ void launch_dp(const DpArgs &args, int grid, size_t smem, cudaStream_t s)
 
 using DpLauncher = void (*)(const DpArgs &, int, size_t, cudaStream_t);
 
+template <bool A, bool L, bool M, bool T>
+void launch_banded(const BandArgs &args, int grid, size_t smem, cudaStream_t s)
+{
+    k_dp_banded<A, L, M, T, kMaxBandWidth><<<grid, kBlock, smem, s>>>(args);
+}
+using BandLauncher = void (*)(const BandArgs &, int, size_t, cudaStream_t);
+
+BandLauncher pick_banded(bool a, bool l, bool m, bool t)
+{
+    static const BandLauncher table[16] = {
+        launch_banded<false, false, false, false>, launch_banded<false, false, false, true>,
+        launch_banded<false, false, true, false>,  launch_banded<false, false, true, true>,
+        launch_banded<false, true, false, false>,  launch_banded<false, true, false, true>,
+        launch_banded<false, true, true, false>,   launch_banded<false, true, true, true>,
+        launch_banded<true, false, false, false>,  launch_banded<true, false, false, true>,
+        launch_banded<true, false, true, false>,   launch_banded<true, false, true, true>,
+        launch_banded<true, true, false, false>,   launch_banded<true, true, false, true>,
+        launch_banded<true, true, true, false>,    launch_banded<true, true, true, true>};
+    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
 DpLauncher pick_dp(bool a, bool l, bool m, bool t)
 {
     static const DpLauncher table[16] = {
@@ -589,8 +650,7 @@ __global__ void k_fill_invalid(const PairDesc *pairs, int64_t n, int32_t minval,
 {
     int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const PairDesc d = pairs[k];
-    if (d.m > 0 && d.n > 0) return;
+    if (!pairs[k].invalid) return;
     score[k] = minval;
     if (end_h) end_h[k] = 0;
     if (end_v) end_v[k] = 0;
@@ -645,7 +705,34 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         GBA_CUDA(ctx, cudaGetLastError());
         launches += 1;
     }
-    if (plan->num_slots > 0) {
+    if (plan->num_slots > 0 && plan->params.band_on) {
+        BandArgs b{};
+        b.seq_h = dseq_h;
+        b.seq_v = dseq_v;
+        b.pairs = plan->pairs.as<PairDesc>();
+        b.order = plan->order.as<int32_t>();
+        b.trace = plan->traceback ? plan->trace.as<uint8_t>() : nullptr;
+        b.score = dscore;
+        b.end_h = end_h;
+        b.end_v = end_v;
+        b.best_e = plan->traceback ? plan->best_e.as<int32_t>() : nullptr;
+        b.best_f = plan->traceback ? plan->best_f.as<int32_t>() : nullptr;
+        b.matrix = plan->matrix ? plan->matrix_dev.as<int32_t>() : nullptr;
+        b.num_slots = plan->num_slots;
+        b.match = plan->params.match;
+        b.mismatch = plan->params.mismatch;
+        b.gap_open = plan->params.gap_open;
+        b.gap_extend = plan->params.gap_extend;
+        b.free_ends = plan->free_ends;
+        b.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
+        b.lower = plan->params.band_lower;
+        b.upper = plan->params.band_upper;
+        const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
+        const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
+        pick_banded(plan->affine, plan->local, plan->matrix, plan->traceback)(b, grid, smem, ctx->stream);
+        GBA_CUDA(ctx, cudaGetLastError());
+        ++launches;
+    } else if (plan->num_slots > 0) {
         DpArgs a{};
         a.seq_h = dseq_h;
         a.seq_v = dseq_v;
@@ -719,6 +806,8 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
             t.num_slots = plan->num_slots;
             t.affine = plan->affine;
             t.local = plan->local;
+            t.band_w = plan->params.band_on ? plan->params.band_upper - plan->params.band_lower + 1 : 0;
+            t.band_upper = plan->params.band_upper;
             const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
             k_traceback<<<grid, kBlock, 0, ctx->stream>>>(t);
             GBA_CUDA(ctx, cudaGetLastError());

@@ -13,6 +13,7 @@
 #pragma once
 
 #include "dp_common.cuh"
+#include "dp_banded_kernels.cuh"
 
 namespace gba {
 
@@ -44,6 +45,7 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     const int64_t slot = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (slot >= a.num_slots) return;
     const int p = a.order[slot];
+    if (p < 0) return;   // padding slot
     const PairDesc d = a.pairs[p];
     const int m = d.m, n = d.n;
     const uint8_t *T = a.trace + d.trace_off;
@@ -56,7 +58,11 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     w.cap = int(a.seg_slot_off[p + 1] - a.seg_slot_off[p]);
     w.n = 0;
 
-    int tv = trace_at(T, m, col, row);
+    const int bw = a.band_w, bu = a.band_upper;
+    auto TAT = [&](int c, int r) -> int {
+        return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
+    };
+    int tv = TAT(col, row);
     if (affine) {
         const int s = a.score[p];
         if (a.best_f[p] == s) { tv &= ~TV_DIAG; tv |= TV_MFV; }
@@ -82,29 +88,29 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     while (!(col <= 0 || row <= 0) && tv != TV_NONE) {
         if (tv & TV_DIAG) {
             if (!(last & TV_DIAG)) { w.record(col, row, frag, last); last = TV_DIAG; frag = 0; }
-            --col; --row; tv = trace_at(T, m, col, row); ++frag;
+            --col; --row; tv = TAT(col, row); ++frag;
         } else if ((tv & TV_MFV) && (tv & TV_V)) {
             if (!(last & TV_V)) { w.record(col, row, frag, last); last = TV_V; frag = 0; }
             if (affine) {
                 while ((!(tv & TV_VO) || (tv & TV_V)) && row != 1) {
-                    --row; tv = trace_at(T, m, col, row); ++frag;
+                    --row; tv = TAT(col, row); ++frag;
                 }
             }
-            --row; tv = trace_at(T, m, col, row); ++frag;
+            --row; tv = TAT(col, row); ++frag;
         } else if ((tv & TV_MFV) && (tv & TV_VO)) {
             if (!(last & TV_V)) { w.record(col, row, frag, last); last = TV_V; frag = 0; }
-            --row; tv = trace_at(T, m, col, row); ++frag;
+            --row; tv = TAT(col, row); ++frag;
         } else if ((tv & TV_MFH) && (tv & TV_H)) {
             if (!(last & TV_H)) { w.record(col, row, frag, last); last = TV_H; frag = 0; }
             if (affine) {
                 while ((!(tv & TV_HO) || (tv & TV_H)) && col != 1) {
-                    --col; tv = trace_at(T, m, col, row); ++frag;
+                    --col; tv = TAT(col, row); ++frag;
                 }
             }
-            --col; tv = trace_at(T, m, col, row); ++frag;
+            --col; tv = TAT(col, row); ++frag;
         } else if ((tv & TV_MFH) && (tv & TV_HO)) {
             if (!(last & TV_H)) { w.record(col, row, frag, last); last = TV_H; frag = 0; }
-            --col; tv = trace_at(T, m, col, row); ++frag;
+            --col; tv = TAT(col, row); ++frag;
         } else {
             break;
         }

@@ -136,6 +136,61 @@ def main():
             add("segments", O.Problem("global", fe, None, mt, mm, go, ge, None, 32, "dna"), H, V)
         add("segments", O.Problem("local", 0, None, mt, mm, go, ge, None, 32, "dna"), H, V)
 
+    # Banded: random bands that meet the matrix.  Shapes the reference cannot run are left out:
+    # bands that start in the last column or end in the first one (its traceback does not
+    # terminate there) and one-diagonal bands whose diagonal leaves the matrix through the
+    # bottom row with m < -2 * lower (its diagonal-only path reads past the end of V).
+    def band_ok(m, n, lo, up):
+        hb = max(0, min(m - 1, lo))
+        hbot = max(0, min(m, up + n) - 1)
+        if hb == m - 1 or hbot == 0:
+            return False
+        if lo == up and max(0, min(n - 1, -lo)) > min(n - 1, lo + m):
+            return False
+        return True
+
+    def band_pairs(count, widths):
+        out = []
+        while len(out) < count:
+            H, V = rand_pairs(rng, 1, 2, 40, "dna")
+            m, n = len(H[0]), len(V[0])
+            lo = int(rng.integers(-n - 1, m + 1))
+            up = lo + int(rng.choice(widths)) - 1
+            if up < -n or lo > m or not band_ok(m, n, lo, up):
+                continue
+            out.append((H[0], V[0], lo, up))
+        return out
+
+    # The reference's SIMD batch traceback path with a band hangs or drops residues on several
+    # shapes, so banded tracebacks come from its scalar single-pair path ("segments"), and
+    # banded scores from single-pair batches.
+    for kind, bits_list, fes in (("score", (16, 32), (0, 9)), ("segments", (32,), (0, 9, 15, 6))):
+        for bits in bits_list:
+            for mode in ("global", "local"):
+                for fe in (fes if mode == "global" else (0,)):
+                    for (mt, mm, go, ge) in DNA_SCORES[:3]:
+                        added = 0
+                        while added < 6:
+                            (h, v, lo, up), = band_pairs(1, (1, 2, 3, 5, 8, 13, 33))
+                            pb = O.Problem(mode, fe, (lo, up), mt, mm, go, ge, None, bits, "dna")
+                            if not O.ref_has_shape({"score": 0, "gaps": 1, "segments": 2}[kind], pb):
+                                break
+                            # Tracebacks only for bands _checkBandProperties accepts: for the others
+                            # the reference leaves the Gaps rows inconsistent.
+                            if kind != "score" and not O.oracle_batch(pb, [h], [v]).valid[0]:
+                                continue
+                            add(kind, pb, [h], [v])
+                            added += 1
+
+    # Read-to-reference verification shape: 150 bp reads (substitutions only, so the batch has
+    # equal lengths -- the reference's SIMD batch path with a band only works then) against
+    # 170 bp windows, free reference overhang, band (-6, 26), affine (2,-4,-1,-6), with CIGARs.
+    from seqan_gb300 import workloads as W
+    wins, reads = W.read_windows(48, ref_len=100_000, sub_rate=0.03, indel_rate=0.0, seed=12)
+    reads = [r[:150] for r in reads]
+    add("gaps", O.Problem("global", 9, (-6, 26), 2, -4, -6, -1, None, 16, "dna"), wins, reads)
+    add("score", O.Problem("global", 9, (-6, 26), 2, -4, -6, -1, None, 16, "dna"), wins, reads)
+
     with open(os.path.join(HERE, "reference_cases.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261203,
                    "ref_simd_bytes": int(O.libref().ref_simd_bytes()), "cases": cases}, f, separators=(",", ":"))

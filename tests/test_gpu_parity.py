@@ -232,3 +232,51 @@ def test_device_resident_plan_replays_graph(engine):
     L.gba_plan_destroy(h, plan)
     for p in ptrs:
         L.gba_device_free(h, p)
+
+
+def _band_cases(seed, count):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        m, n = int(rng.integers(1, 45)), int(rng.integers(1, 45))
+        h = rng.integers(0, 4, m).astype(np.uint8)
+        v = h[:n].copy() if (n <= m and rng.random() < 0.5) else rng.integers(0, 4, n).astype(np.uint8)
+        lo = int(rng.integers(-n - 2, m + 2))
+        up = lo + int(rng.choice([1, 2, 3, 5, 8, 13, 33, 60])) - 1
+        out.append((h, v, lo, up))
+    return out
+
+
+@pytest.mark.parametrize("mode,fe", [("global", f) for f in (0, 1, 2, 4, 8, 9, 6, 15)] + [("local", 0)])
+@pytest.mark.parametrize("scheme", [(2, -3, -5, -5), (2, -4, -6, -1), (1, -1, -2, -1)])
+def test_banded_against_oracle(engine, mode, fe, scheme):
+    """Banded DP: every band phase (top, middle, full, bottom, final), one-diagonal bands and
+    the single-cell bands; scores, best cells, segment lists and CIGARs."""
+    import seqan_gb300 as sg
+    mt, mm, go, ge = scheme
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    md = 1 if mode == "local" else 0
+    for (h, v, lo, up) in _band_cases(hash((mode, fe, scheme)) % 1000, 60):
+        out = sg.align_codes([h], [v], sg.Score(mt, mm, ge, go, dtype=np.int32), mode=md, config=cfg,
+                             band=(lo, up), traceback=True, cigar=True)
+        ref = O.oracle_batch(O.Problem(mode, fe, (lo, up), mt, mm, go, ge, None, 32), [h], [v], traceback=True)
+        assert out.score[0] == ref.score[0], (lo, up, len(h), len(v))
+        if ref.valid[0]:
+            assert (out.end_h[0], out.end_v[0]) == (ref.end_h[0], ref.end_v[0]), (lo, up, len(h), len(v))
+            assert out.pair_segments(0) == ref.segments[0], (lo, up, len(h), len(v))
+            assert out.pair_cigar(0) == O.cigar_string(ref.segments[0])
+
+
+def test_banded_read_mapping_batch(engine):
+    """The read-to-reference verification shape: 150 bp reads with substitutions and indels
+    against 170 bp windows, band (-6, 26), free reference overhang, int16, CIGARs."""
+    import seqan_gb300 as sg
+    from seqan_gb300 import workloads as W
+    wins, reads = W.read_windows(2000, ref_len=1_000_000, seed=21)
+    sc = sg.Score(2, -4, -1, -6, dtype=np.int16)
+    out = sg.align_codes(wins, reads, sc, config=sg.AlignConfig(True, False, False, True), band=(-6, 26),
+                         traceback=True, cigar=True)
+    ref = O.oracle_batch(O.Problem("global", 9, (-6, 26), 2, -4, -6, -1, None, 16), wins, reads, traceback=True)
+    assert np.array_equal(out.score, ref.score)
+    for k in range(len(wins)):
+        assert out.pair_cigar(k) == O.cigar_string(ref.segments[k]), k
