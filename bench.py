@@ -36,24 +36,69 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # name: (description, generator kwargs)
-    "affine_dna_100k": "100000 pairs, uniform length in [100,300], partner 5% subs + 1% indels, "
+    "affine_dna_100k": "100000 pairs, read length uniform in [100,300], partner 5% subs + 1% indels, "
                        "Score(2,-4,-1,-6) int16, global, score + end position",
     "linear_dna_1024x150": "1024 pairs of uniform ACGT, both length 150, Score(2,-3,-5) int32, global, score",
+    "protein_local_tb_20k": "20000 protein pairs, log-normal lengths (median 300, sigma 0.5, [50,1000]), 30% "
+                            "related at 40% identity, Blosum62(-1,-11) int16, local, score + begin/end + "
+                            "trace segments (Gaps)",
+    "banded_reads_1m": "1000000 reads of 150 bp (2% subs, 0.2% indels) vs 170 bp windows of a 10 Mbp "
+                       "reference, AlignConfig<true,false,false,true>, band [-6,26], Score(2,-4,-1,-6) int16, "
+                       "score + CIGAR",
 }
+# Algorithmic integer ops per cell (add and max each count one): affine global 9
+# (E: 2 adds + 1 max, F: 2 + 1, S: 1 add + 2 max), affine local 10 (+ max with 0),
+# linear global 5, linear local 6.
 OPS_PER_CELL = {"affine_global": 9, "linear_global": 5, "affine_local": 10, "linear_local": 6}
 
 
-def make_workload(name: str, seed_offset: int = 0):
+class Spec:
+    def __init__(self, H, V, score, mode, kind, config=None, band=None, traceback=False, cigar=False,
+                 alphabet_size=4):
+        self.H, self.V, self.score, self.mode, self.kind = H, V, score, mode, kind
+        self.config, self.band, self.traceback, self.cigar = config, band, traceback, cigar
+        self.alphabet_size = alphabet_size
+
+
+def make_workload(name: str, seed_offset: int = 0) -> Spec:
     import seqan_gb300 as sg
     from seqan_gb300 import workloads as W
     if name == "affine_dna_100k":
         H, V = W.mutated_dna_pairs(100_000, 100, 300, 0.05, 0.01, seed=2 + seed_offset)
-        return H, V, sg.Score(2, -4, -1, -6, dtype=np.int16), 0, "affine_global"
+        return Spec(H, V, sg.Score(2, -4, -1, -6, dtype=np.int16), 0, "affine_global")
     if name == "linear_dna_1024x150":
         H, V = W.uniform_dna_pairs(1024, 150, seed=1 + seed_offset)
-        return H, V, sg.Score(2, -3, -5, dtype=np.int32), 0, "linear_global"
+        return Spec(H, V, sg.Score(2, -3, -5, dtype=np.int32), 0, "linear_global")
+    if name == "protein_local_tb_20k":
+        H, V = W.protein_pairs(20_000, seed=3 + seed_offset)
+        return Spec(H, V, sg.Blosum62(-1, -11, dtype=np.int16), 1, "affine_local", traceback=True,
+                    alphabet_size=27)
+    if name == "banded_reads_1m":
+        wins, reads = W.read_windows(1_000_000, seed=4 + seed_offset)
+        return Spec(wins, reads, sg.Score(2, -4, -1, -6, dtype=np.int16), 0, "affine_global",
+                    config=sg.AlignConfig(True, False, False, True), band=(-6, 26), traceback=True, cigar=True)
     raise SystemExit(f"unknown workload {name}")
+
+
+def oracle_problem(spec: Spec):
+    from oracle import oracle as O
+    fe = spec.config.bits if spec.config is not None else 0
+    return O.Problem("local" if spec.mode == 1 else "global", fe, spec.band, spec.score.match,
+                     spec.score.mismatch, spec.score.gap_open, spec.score.gap_extend, spec.score.matrix,
+                     spec.score.bits, "aa" if spec.alphabet_size > 5 else "dna")
+
+
+def algorithmic_cells(spec: Spec) -> int:
+    """m * n per pair; in-band cells (1 <= i <= n, 1 <= j <= m, lower <= j - i <= upper) when banded."""
+    lh = np.fromiter((len(h) for h in spec.H), dtype=np.int64, count=len(spec.H))
+    lv = np.fromiter((len(v) for v in spec.V), dtype=np.int64, count=len(spec.V))
+    if spec.band is None:
+        return int((lh * lv).sum())
+    lo, up = spec.band
+    total = 0
+    for dg in range(lo, up + 1):
+        total += np.clip(np.minimum(lv, lh - dg) - np.maximum(1, 1 - dg) + 1, 0, None).sum()
+    return int(total)
 
 
 class ClockSampler:
@@ -115,53 +160,55 @@ def concat(seqs):
     return np.concatenate(seqs).astype(np.uint8), off
 
 
-def cpu_baseline(H, V, score, kind: str, seconds_target: float = 10.0):
+def cpu_baseline(spec: Spec, seconds_target: float = 10.0):
     """Times the oracle (CPU restatement, all host threads) on a sample of the workload."""
     from oracle import oracle as O
-    pb = O.Problem("global", 0, None, score.match, score.mismatch, score.gap_open, score.gap_extend, None,
-                   score.bits)
+    pb = oracle_problem(spec)
     threads = os.cpu_count() or 1
+    H, V = spec.H, spec.V
     n = min(len(H), 2000)
     t0 = time.perf_counter()
-    O.oracle_batch(pb, H[:n], V[:n], threads=threads)
+    O.oracle_batch(pb, H[:n], V[:n], traceback=spec.traceback, threads=threads)
     dt = time.perf_counter() - t0
     # Grow the sample to about seconds_target of wall time, bounded by the workload.
     n = int(min(len(H), max(n, n * seconds_target / max(dt, 1e-3) / 3)))
     best = None
     for _ in range(2):
         t0 = time.perf_counter()
-        O.oracle_batch(pb, H[:n], V[:n], threads=threads)
+        O.oracle_batch(pb, H[:n], V[:n], traceback=spec.traceback, threads=threads)
         dt = time.perf_counter() - t0
         best = dt if best is None else min(best, dt)
-    cells = int(sum(len(h) * len(v) for h, v in zip(H[:n], V[:n])))
+    sub = Spec(H[:n], V[:n], spec.score, spec.mode, spec.kind, spec.config, spec.band)
+    cells = algorithmic_cells(sub)
     return {"value": cells / best / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
             "sample": f"first {n} pairs of the workload, oracle/seqan_oracle.c with OpenMP over {threads} "
-                      f"threads, best of 2", "cells": cells, "seconds": best}
+                      f"threads{' with traceback' if spec.traceback else ''}, best of 2",
+            "cells": cells, "seconds": best}
 
 
 def run_reference(args, rank):
     if rank != 0:
         return
-    H, V, score, _, _ = make_workload(args.workload)
+    spec = make_workload(args.workload)
     from oracle import oracle as O
-    pb = O.Problem("global", 0, None, score.match, score.mismatch, score.gap_open, score.gap_extend, None,
-                   score.bits)
+    pb = oracle_problem(spec)
     threads = os.cpu_count() or 1
-    n = min(len(H), args.ref_pairs)
-    cells = int(sum(len(h) * len(v) for h, v in zip(H[:n], V[:n])))
+    n = min(len(spec.H), args.ref_pairs)
+    H, V = spec.H[:n], spec.V[:n]
+    cells = algorithmic_cells(Spec(H, V, spec.score, spec.mode, spec.kind, spec.config, spec.band))
     for _ in range(args.warmup):
-        O.oracle_batch(pb, H[:n], V[:n], threads=threads)
+        O.oracle_batch(pb, H, V, traceback=spec.traceback, threads=threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.oracle_batch(pb, H[:n], V[:n], threads=threads)
+        O.oracle_batch(pb, H, V, traceback=spec.traceback, threads=threads)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     gcups = cells * len(times) / total / 1e9
     line = {"metric": "GCUPS, batched affine DNA align", "value": gcups, "unit": "GCUPS", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int16" if score.bits == 16 else "int32",
-            "data": "synthetic", "impl": "reference",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int16" if spec.score.bits == 16 else "int32", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "pairs_per_step": n, "description": WORKLOADS[args.workload]},
             "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": "port",
                              "sample": f"first {n} pairs of the workload per step; the reference's own SIMD "
@@ -208,11 +255,17 @@ def main():
     ctx = N.Context(local_rank)
     h = ctx.handle
 
-    H, V, score, mode, kind = make_workload(args.workload, seed_offset=rank)
+    spec = make_workload(args.workload, seed_offset=rank)
+    H, V, score, mode, kind = spec.H, spec.V, spec.score, spec.mode, spec.kind
     sh, oh = concat(H)
     sv, ov = concat(V)
     npairs = len(H)
-    cells = int(((oh[1:] - oh[:-1]) * (ov[1:] - ov[:-1])).sum())
+    cells = algorithmic_cells(spec)
+    outputs = N.GBA_OUT_SCORE | N.GBA_OUT_END
+    if spec.traceback:
+        outputs |= N.GBA_OUT_SEGMENTS
+    if spec.cigar:
+        outputs |= N.GBA_OUT_CIGAR
 
     def pinned(nbytes):
         p = C.c_void_p()
@@ -238,8 +291,8 @@ def main():
 
     flags = {"auto": N.GBA_FLAG_AUTOTUNE, "general": N.GBA_FLAG_GENERAL_KERNEL, "packed16": N.GBA_FLAG_STRIP16,
              "plain": N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH}[args.kernel]
-    params = sg.align.make_params(score, mode, None, None, N.GBA_OUT_SCORE | N.GBA_OUT_END,
-                                  alphabet_size=4, flags=flags)
+    params = sg.align.make_params(score, mode, spec.config, spec.band, outputs,
+                                  alphabet_size=spec.alphabet_size, flags=flags)
     host_batch = N.GbaBatch(npairs, p_sh, p_oh, p_sv, p_ov, 0, 0)
 
     # Device-resident inputs for `value`.
@@ -273,7 +326,7 @@ def main():
     barrier()
     ctx.check(L.gba_synchronize(h), "sync")
     sampler.start()
-    step_ms, dp_ms, launches = [], [], 0
+    step_ms, dp_ms, tb_ms, launches = [], [], [], 0
     ms = C.c_float()
     tile = None
     for _ in range(args.steps):
@@ -284,6 +337,7 @@ def main():
         step_ms.append(ms.value)
         st = ctx.stats()
         dp_ms.append(st.dp_kernel_ms)
+        tb_ms.append(st.traceback_kernel_ms)
         launches += st.kernel_launches
         tile = {"rows_per_strip": st.tile_rows, "min_blocks_per_sm": st.tile_min_blocks}
     ctx.check(L.gba_synchronize(h), "sync")
@@ -300,8 +354,9 @@ def main():
     # The plain GPU form on the same device-resident batch: the general one-pair-per-thread
     # kernel, one launch per 8-residue length bucket (comparison for the persistent form).
     plain = None
-    if args.kernel == "auto" and not args.no_plain:
-        pparams = sg.align.make_params(score, mode, None, None, N.GBA_OUT_SCORE | N.GBA_OUT_END, alphabet_size=4,
+    if args.kernel == "auto" and not args.no_plain and not spec.traceback and spec.band is None:
+        pparams = sg.align.make_params(score, mode, spec.config, None, N.GBA_OUT_SCORE | N.GBA_OUT_END,
+                                       alphabet_size=spec.alphabet_size,
                                        flags=N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH)
         pplan = C.c_void_p()
         ctx.check(L.gba_plan_create(h, C.byref(pparams), C.byref(host_batch), C.byref(pplan)), "plain plan")
@@ -324,6 +379,20 @@ def main():
     # End to end through the public C-ABI call with host buffers.
     host_res = N.GbaResult()
     host_res.score, host_res.end_h, host_res.end_v = p_score, p_eh, p_ev
+    seg_cap = int((oh[1:] - oh[:-1]).sum() + (ov[1:] - ov[:-1]).sum() + 4 * npairs) if spec.traceback else 0
+    extra_pinned = []
+    if spec.traceback:
+        p_seg = pinned(seg_cap * 16)
+        p_segoff = pinned((npairs + 1) * 8)
+        p_bh, p_bv = pinned(npairs * 4), pinned(npairs * 4)
+        extra_pinned += [p_seg, p_segoff, p_bh, p_bv]
+        host_res.segments, host_res.segment_capacity, host_res.segment_offsets = p_seg, seg_cap, p_segoff
+        host_res.begin_h, host_res.begin_v = p_bh, p_bv
+    if spec.cigar:
+        p_cig = pinned(seg_cap * 4)
+        p_cigoff = pinned((npairs + 1) * 8)
+        extra_pinned += [p_cig, p_cigoff]
+        host_res.cigar, host_res.cigar_capacity, host_res.cigar_offsets = p_cig, seg_cap, p_cigoff
     for _ in range(max(1, args.warmup)):
         ctx.check(L.gba_align_batch(h, C.byref(params), C.byref(host_batch), C.byref(host_res)), "e2e")
     e2e_s = []
@@ -336,13 +405,21 @@ def main():
     e2e_launches = est.kernel_launches
     e2e_breakdown = {"host_plan_ms": est.host_plan_ms, "dp_kernel_ms": est.dp_kernel_ms, "call_ms": est.call_ms}
     e2e_gcups = cells * world * len(e2e_s) / sum(e2e_s) / 1e9
-    h2d = sh.nbytes + sv.nbytes
+    h2d = sh.nbytes + sv.nbytes + oh.nbytes + ov.nbytes
     d2h = 3 * npairs * 4
+    if spec.traceback:
+        segoff = as_np(p_segoff, npairs + 1, np.int64)
+        d2h += int(segoff[-1]) * 16 + (npairs + 1) * 8 + 2 * npairs * 4
+    if spec.cigar:
+        cigoff = as_np(p_cigoff, npairs + 1, np.int64)
+        d2h += int(cigoff[-1]) * 4 + (npairs + 1) * 8
 
     # Roofline of the DP kernel: integer add/max ops against the measured integer rate.
     peak = C.c_double()
     ctx.check(L.gba_measure_int_peak(h, C.byref(peak)), "int peak")
     dp_avg_ms = sum(dp_ms) / len(dp_ms)
+    tb_avg_ms = sum(tb_ms) / len(tb_ms)
+    st_last = ctx.stats()
     ops = cells * OPS_PER_CELL[kind]
     achieved = ops / (dp_avg_ms * 1e-3) / 1e12
     roofline = {"bound": "int32", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
@@ -352,6 +429,14 @@ def main():
                 "dp_kernel_ms": dp_avg_ms,
                 "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"}
 
+    if spec.traceback:
+        roofline["trace_bytes_per_launch"] = int(st_last.trace_bytes)
+        roofline["trace_write_gbs"] = st_last.trace_bytes / (dp_avg_ms * 1e-3) / 1e9
+        roofline["traceback_and_output_ms"] = tb_avg_ms
+    if spec.band is not None:
+        roofline["kernel"] = "k_dp_banded (one pair per thread, band in per-thread slots)"
+    elif spec.mode == 1 or spec.traceback or args.kernel == "general":
+        roofline["kernel"] = "k_dp_strip (one pair per thread, int32)"
     line = {"metric": "GCUPS, batched affine DNA align", "value": value, "unit": "GCUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -368,11 +453,11 @@ def main():
     if plain:
         line["plain_gpu_form"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(H, V, score, kind)
+        line["cpu_baseline"] = cpu_baseline(spec)
     L.gba_plan_destroy(h, plan)
     for p in (d_sh, d_sv, d_score, d_eh, d_ev, d_flush):
         L.gba_device_free(h, p)
-    for p in (p_sh, p_sv, p_oh, p_ov, p_score, p_eh, p_ev, p_flush):
+    for p in [p_sh, p_sv, p_oh, p_ov, p_score, p_eh, p_ev, p_flush] + extra_pinned:
         L.gba_host_free(h, p)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -76,8 +76,9 @@ struct TraceArgs {
     int64_t num_slots;
     int32_t affine;
     int32_t local;
-    int32_t band_w;        // 0: strip layout; else banded layout with this many slots per column
+    int32_t band_w;        // banded layout: slots per column (0: not banded)
     int32_t band_upper;
+    int32_t warp_rows;     // warp layout: rows per lane strip (0: not the warp layout)
 };
 
 __host__ __device__ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }

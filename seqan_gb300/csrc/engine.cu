@@ -10,6 +10,7 @@
 #include "traceback_kernels.cuh"
 #include "dp16x2_kernels.cuh"
 #include "dp_banded_kernels.cuh"
+#include "dp_warp_kernels.cuh"
 #include "int_peak.cuh"
 
 #include <cub/device/device_scan.cuh>
@@ -90,6 +91,11 @@ struct gba_plan {
     int64_t codes_total = 0, bnd16_total = 0;
     DevBuf slots16, warp_codes, warp_hwords, codes16, warp_bnd16, bnd16, counter16;
     int32_t tasks16 = 0;
+    // Warp-per-pair path (dp_warp_kernels.cuh).
+    bool use_warp = false;
+    int warp_rows = 8;
+    int64_t grid_warp = 0;
+    DevBuf rowbuf, rowbuf_off, counter_warp;
     int64_t grid16[8] = {};         // resident blocks of each packed-kernel variant
     int variant16 = 0;              // chosen tiling variant
     bool tune_pending = false;      // autotune at the first run
@@ -108,7 +114,8 @@ struct gba_plan {
                          &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots, &seg_slot_off,
                          &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
                          &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
-                         &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16};
+                         &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16,
+                         &rowbuf, &rowbuf_off, &counter_warp};
         for (DevBuf *b : all) b->release();
         drop_graph();
     }
@@ -125,7 +132,7 @@ struct gba_plan {
                                &seg_slot_off, &seg_count, &seg_dense_off, &seg_dense, &seg_count64,
                                &cig_slots, &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense,
                                &cig_count64, &cub_tmp, &slots16, &warp_codes, &warp_hwords, &codes16,
-                               &warp_bnd16, &bnd16, &counter16};
+                               &warp_bnd16, &bnd16, &counter16, &rowbuf, &rowbuf_off, &counter_warp};
         size_t s = 0;
         for (const DevBuf *b : all) s += b->cap;
         return s;
@@ -334,6 +341,8 @@ int64_t persistent_grid(gba_context *ctx, const void *fn)
     return int64_t(sms) * per_sm;
 }
 
+const void *warp_fn(bool a, bool l, bool m, bool t);
+
 // Builds a plan from host offsets.  `plan` buffers are (re)used.
 int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_plan *plan)
 {
@@ -364,6 +373,10 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                            p->mismatch >= -128 && p->mismatch <= 127 && std::abs(p->gap_open) <= 1024 &&
                            std::abs(p->gap_extend) <= 1024;
     plan->rows16 = 32;
+    // Pairs that are neither banded nor on the packed path run one warp per pair, unless the
+    // one-pair-per-thread kernel is forced.
+    plan->use_warp = !p->band_on && !(p->flags & (GBA_FLAG_GENERAL_KERNEL | GBA_FLAG_PLAIN_BUCKETS));
+    plan->warp_rows = 8;
     std::vector<uint32_t> keys16;
     std::vector<int32_t> idx16;
     std::map<uint64_t, int64_t> band_cell_cache;
@@ -413,7 +426,8 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         if (plan->traceback) {
             d.trace_off = trace_off;
             trace_off += p->band_on ? align16(int64_t(d.m + 1) * (p->band_upper - p->band_lower + 1))
-                                    : trace_bytes(d.m, d.n);
+                         : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
+                                          : trace_bytes(d.m, d.n);
         }
         if (packed_ok && int16_exact(*p, max_pos, d.m, d.n, false)) {
             const int64_t strips = (d.n + plan->rows16 - 1) / plan->rows16;
@@ -490,8 +504,19 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->bnd16_total = btot;
     plan->tasks16 = int32_t(warps16);
 
+    // Warp path: one band-boundary row of m + 1 int2 per pair that spans more than one band.
+    std::vector<int64_t> rboff;
+    int64_t rbtot = 0;
+    if (plan->use_warp) {
+        rboff.assign(N + 1, 0);
+        for (int64_t k = 0; k < N; ++k) {
+            rboff[k] = rbtot;
+            if (!desc[k].invalid && desc[k].n > 32 * plan->warp_rows) rbtot += int64_t(desc[k].m) + 1;
+        }
+        rboff[N] = rbtot;
+    }
     // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
-    const int64_t warps = (plan->num_slots + 31) / 32;
+    const int64_t warps = plan->use_warp ? 0 : (plan->num_slots + 31) / 32;
     std::vector<int64_t> wscr(std::max<int64_t>(warps, 1));
     int64_t scr = 0;
     for (int64_t w = 0; w < warps; ++w) {
@@ -530,6 +555,12 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     if ((rc = upload(ctx, plan->order, idx))) return rc;
     if ((rc = upload(ctx, plan->warp_scratch, wscr))) return rc;
     GBA_CUDA(ctx, plan->scratch.ensure(size_t(std::max<int64_t>(scr, 1)) * sizeof(int2)));
+    if (plan->use_warp && plan->num_slots > 0) {
+        if ((rc = upload(ctx, plan->rowbuf_off, rboff))) return rc;
+        GBA_CUDA(ctx, plan->rowbuf.ensure(size_t(std::max<int64_t>(rbtot, 1)) * sizeof(int2)));
+        GBA_CUDA(ctx, plan->counter_warp.ensure(16));
+        plan->grid_warp = persistent_grid(ctx, warp_fn(plan->affine, plan->local, plan->matrix, plan->traceback));
+    }
     if (plan->num16 > 0) {
         if ((rc = upload(ctx, plan->slots16, slots16))) return rc;
         if ((rc = upload(ctx, plan->warp_codes, wcodes))) return rc;
@@ -606,6 +637,43 @@ void launch_banded(const BandArgs &args, int grid, size_t smem, cudaStream_t s)
     k_dp_banded<A, L, M, T, kMaxBandWidth><<<grid, kBlock, smem, s>>>(args);
 }
 using BandLauncher = void (*)(const BandArgs &, int, size_t, cudaStream_t);
+
+constexpr int kWarpRows = 8;
+template <bool A, bool L, bool M, bool T>
+void launch_warp(const WarpArgs &args, int grid, size_t smem, cudaStream_t s)
+{
+    k_dp_warp<A, L, M, T, kWarpRows><<<grid, kBlock, smem, s>>>(args);
+}
+using WarpLauncher = void (*)(const WarpArgs &, int, size_t, cudaStream_t);
+
+WarpLauncher pick_warp(bool a, bool l, bool m, bool t)
+{
+    static const WarpLauncher table[16] = {
+        launch_warp<false, false, false, false>, launch_warp<false, false, false, true>,
+        launch_warp<false, false, true, false>,  launch_warp<false, false, true, true>,
+        launch_warp<false, true, false, false>,  launch_warp<false, true, false, true>,
+        launch_warp<false, true, true, false>,   launch_warp<false, true, true, true>,
+        launch_warp<true, false, false, false>,  launch_warp<true, false, false, true>,
+        launch_warp<true, false, true, false>,   launch_warp<true, false, true, true>,
+        launch_warp<true, true, false, false>,   launch_warp<true, true, false, true>,
+        launch_warp<true, true, true, false>,    launch_warp<true, true, true, true>};
+    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
+const void *warp_fn(bool a, bool l, bool m, bool t)
+{
+#define GBA_WF(A, L, M, T) (const void *)k_dp_warp<A, L, M, T, kWarpRows>
+    const void *table[16] = {GBA_WF(false, false, false, false), GBA_WF(false, false, false, true),
+                             GBA_WF(false, false, true, false),  GBA_WF(false, false, true, true),
+                             GBA_WF(false, true, false, false),  GBA_WF(false, true, false, true),
+                             GBA_WF(false, true, true, false),   GBA_WF(false, true, true, true),
+                             GBA_WF(true, false, false, false),  GBA_WF(true, false, false, true),
+                             GBA_WF(true, false, true, false),   GBA_WF(true, false, true, true),
+                             GBA_WF(true, true, false, false),   GBA_WF(true, true, false, true),
+                             GBA_WF(true, true, true, false),    GBA_WF(true, true, true, true)};
+#undef GBA_WF
+    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
 
 BandLauncher pick_banded(bool a, bool l, bool m, bool t)
 {
@@ -732,6 +800,35 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         pick_banded(plan->affine, plan->local, plan->matrix, plan->traceback)(b, grid, smem, ctx->stream);
         GBA_CUDA(ctx, cudaGetLastError());
         ++launches;
+    } else if (plan->num_slots > 0 && plan->use_warp) {
+        WarpArgs w{};
+        w.seq_h = dseq_h;
+        w.seq_v = dseq_v;
+        w.pairs = plan->pairs.as<PairDesc>();
+        w.order = plan->order.as<int32_t>();
+        w.rowbuf = plan->rowbuf.as<int2>();
+        w.rowbuf_off = plan->rowbuf_off.as<int64_t>();
+        w.trace = plan->traceback ? plan->trace.as<uint8_t>() : nullptr;
+        w.score = dscore;
+        w.end_h = end_h;
+        w.end_v = end_v;
+        w.best_e = plan->traceback ? plan->best_e.as<int32_t>() : nullptr;
+        w.best_f = plan->traceback ? plan->best_f.as<int32_t>() : nullptr;
+        w.matrix = plan->matrix ? plan->matrix_dev.as<int32_t>() : nullptr;
+        w.task_counter = plan->counter_warp.as<int32_t>();
+        w.num_tasks = int32_t(plan->num_slots);
+        w.match = plan->params.match;
+        w.mismatch = plan->params.mismatch;
+        w.gap_open = plan->params.gap_open;
+        w.gap_extend = plan->params.gap_extend;
+        w.free_ends = plan->free_ends;
+        w.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
+        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter_warp.ptr, 0, sizeof(int32_t), ctx->stream));
+        const int grid = int(std::min<int64_t>(plan->grid_warp, (plan->num_slots * 32 + kBlock - 1) / kBlock));
+        const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
+        pick_warp(plan->affine, plan->local, plan->matrix, plan->traceback)(w, grid, smem, ctx->stream);
+        GBA_CUDA(ctx, cudaGetLastError());
+        ++launches;
     } else if (plan->num_slots > 0) {
         DpArgs a{};
         a.seq_h = dseq_h;
@@ -808,6 +905,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
             t.local = plan->local;
             t.band_w = plan->params.band_on ? plan->params.band_upper - plan->params.band_lower + 1 : 0;
             t.band_upper = plan->params.band_upper;
+            t.warp_rows = plan->use_warp ? plan->warp_rows : 0;
             const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
             k_traceback<<<grid, kBlock, 0, ctx->stream>>>(t);
             GBA_CUDA(ctx, cudaGetLastError());

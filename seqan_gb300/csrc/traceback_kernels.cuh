@@ -14,6 +14,7 @@
 
 #include "dp_common.cuh"
 #include "dp_banded_kernels.cuh"
+#include "dp_warp_kernels.cuh"
 
 namespace gba {
 
@@ -58,8 +59,9 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     w.cap = int(a.seg_slot_off[p + 1] - a.seg_slot_off[p]);
     w.n = 0;
 
-    const int bw = a.band_w, bu = a.band_upper;
+    const int bw = a.band_w, bu = a.band_upper, wr = a.warp_rows;
     auto TAT = [&](int c, int r) -> int {
+        if (wr) return int(trace_at_warp(T, m, wr, c, r));
         return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
     };
     int tv = TAT(col, row);

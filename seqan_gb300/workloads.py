@@ -108,18 +108,31 @@ def protein_pairs(n: int, median: int = 300, sigma: float = 0.5, lo: int = 50, h
 
 def read_windows(n_reads: int, ref_len: int = 10_000_000, read_len: int = 150, flank: int = 10,
                  sub_rate: float = 0.02, indel_rate: float = 0.002, seed: int = 4):
-    """Reads with their reference windows ref[o - flank, o + read_len + flank)."""
+    """Reads with their reference windows ref[o - flank, o + read_len + flank).
+
+    Substitutions are applied to all reads at once; the few reads that draw an indel are
+    rebuilt one by one."""
     rng = _rng(seed)
     ref = rng.integers(0, 4, size=ref_len, dtype=np.uint8)
     origins = rng.integers(flank, ref_len - read_len - flank, size=n_reads)
     win_len = read_len + 2 * flank
-    idx = (origins - flank)[:, None] + np.arange(win_len)[None, :]
-    windows = ref[idx]
-    reads = []
-    for k in range(n_reads):
-        r = ref[origins[k]:origins[k] + read_len]
-        reads.append(mutate(rng, r, sub_rate, indel_rate)[:read_len + 2])
-    return list(windows), reads
+    windows = ref[(origins - flank)[:, None] + np.arange(win_len)[None, :]]
+    reads = ref[origins[:, None] + np.arange(read_len)[None, :]].copy()
+    subs = rng.random(reads.shape) < sub_rate
+    reads[subs] = (reads[subs] + rng.integers(1, 4, size=int(subs.sum()), dtype=np.uint8)) % 4
+    indel = rng.random(reads.shape) < indel_rate
+    out = list(reads)
+    for k in np.nonzero(indel.any(axis=1))[0]:
+        r, pieces, prev = reads[k], [], 0
+        for pos in np.nonzero(indel[k])[0]:
+            pieces.append(r[prev:pos])
+            if rng.random() < 0.5:
+                pieces.append(rng.integers(0, 4, size=1, dtype=np.uint8))
+                pieces.append(r[pos:pos + 1])
+            prev = pos + 1
+        pieces.append(r[prev:])
+        out[k] = np.concatenate(pieces).astype(np.uint8)
+    return list(windows), out
 
 
 def serving_lengths(n: int, seed: int = 5):

@@ -280,3 +280,36 @@ def test_banded_read_mapping_batch(engine):
     assert np.array_equal(out.score, ref.score)
     for k in range(len(wins)):
         assert out.pair_cigar(k) == O.cigar_string(ref.segments[k]), k
+
+
+@pytest.mark.parametrize("mode,fe", [("global", 0), ("global", 9), ("global", 6), ("global", 15), ("local", 0)])
+def test_warp_kernel_multiband_traceback(engine, mode, fe):
+    """One warp per pair over several 256-row bands (lengths up to 1200), with tracebacks;
+    against the oracle and against the one-pair-per-thread kernel."""
+    import seqan_gb300 as sg
+    H, V = _random_pairs(300 + fe, 40, 1, 1200)
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    md = 1 if mode == "local" else 0
+    for (mt, mm, go, ge) in [(2, -4, -6, -1), (2, -3, -5, -5)]:
+        sc = sg.Score(mt, mm, ge, go, dtype=np.int32)
+        out = sg.align_codes(H, V, sc, mode=md, config=cfg, traceback=True, cigar=True)
+        gen = sg.align_codes(H, V, sc, mode=md, config=cfg, traceback=True, flags=1)
+        ref = O.oracle_batch(O.Problem(mode, fe, None, mt, mm, go, ge, None, 32), H, V, traceback=True)
+        assert np.array_equal(out.score, ref.score) and np.array_equal(gen.score, ref.score)
+        assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+        for k in range(len(H)):
+            assert out.pair_segments(k) == ref.segments[k], k
+            assert gen.pair_segments(k) == ref.segments[k], k
+            assert out.pair_cigar(k) == O.cigar_string(ref.segments[k]), k
+
+
+def test_warp_kernel_protein_local(engine):
+    import seqan_gb300 as sg
+    from seqan_gb300 import workloads as W
+    H, V = W.protein_pairs(150, seed=31)
+    sc = sg.Blosum62(-1, -11, dtype=np.int16)
+    out = sg.align_codes(H, V, sc, mode=1, traceback=True)
+    ref = O.oracle_batch(O.Problem("local", 0, None, 0, 0, -11, -1, sc.matrix, 16, "aa"), H, V, traceback=True)
+    assert np.array_equal(out.score, ref.score)
+    for k in range(len(H)):
+        assert out.pair_segments(k) == ref.segments[k], k
