@@ -228,6 +228,7 @@ def main():
     ap.add_argument("--ref-pairs", type=int, default=20000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-bucket comparison")
+    ap.add_argument("--pairs", type=int, default=0, help="use only the first N pairs (small profiling cases)")
     ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16", "plain"],
                     help="auto: persistent packed 16-bit kernel (32-row strips), graph-replayed; "
                          "plain: general kernel, one launch per length bucket")
@@ -256,6 +257,8 @@ def main():
     h = ctx.handle
 
     spec = make_workload(args.workload, seed_offset=rank)
+    if args.pairs:
+        spec.H, spec.V = spec.H[:args.pairs], spec.V[:args.pairs]
     H, V, score, mode, kind = spec.H, spec.V, spec.score, spec.mode, spec.kind
     sh, oh = concat(H)
     sv, ov = concat(V)
@@ -441,7 +444,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int16" if score.bits == 16 else "int32", "data": "synthetic",
-            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "pairs": npairs,
+            "config": {"workload": args.workload if not args.pairs else f"{args.workload} (first {npairs} pairs)",
+                       "description": WORKLOADS[args.workload], "pairs": npairs,
                        "cells_per_step": cells, "l2": "flushed (256 MiB write) between timed steps",
                        "kernel": args.kernel,
                        "parallelism": f"replicas x{world} (pairs are independent)"},

@@ -99,15 +99,19 @@ typedef struct {
 /* Kernel selection flags (gba_params.flags); results are identical either way.
  * With equality scoring the engine uses its packed two-pairs-per-thread 16-bit kernel when
  * alphabet_size is between 1 and 8 (the caller's promise that every code is below it, as the
- * reference's alphabet types guarantee) and the pair's values stay in the exact int16 range. */
+ * reference's alphabet types guarantee), the pair's values stay in the exact int16 range and
+ * the batch holds at least 32768 pairs; other unbanded pairs run one warp per pair, banded
+ * pairs one thread per pair. */
 enum {
     GBA_FLAG_GENERAL_KERNEL = 1,   /* force the one-pair-per-thread 32-bit kernel */
     GBA_FLAG_STRIP16 = 2,          /* packed kernel with 16-row strips instead of 32 */
     GBA_FLAG_PLAIN_BUCKETS = 4,    /* the plain GPU form: general kernel, one launch per
                                       8-residue length bucket (comparison baseline) */
     GBA_FLAG_NO_GRAPH = 8,         /* launch kernels directly instead of replaying a CUDA graph */
-    GBA_FLAG_AUTOTUNE = 16         /* time the packed kernel's tiling variants on the first run
+    GBA_FLAG_AUTOTUNE = 16,        /* time the packed kernel's tiling variants on the first run
                                       of a plan and remember the fastest per batch shape */
+    GBA_FLAG_PACKED = 32           /* use the packed kernel for eligible pairs even in batches
+                                      too small to fill the GPU with it */
 };
 
 /* A batch: concatenated residue codes with n+1 offsets for each side. */

@@ -180,6 +180,8 @@ int fail(gba_context *ctx, int code, const char *fmt, ...)
 
 constexpr int kBlock = 128;
 constexpr int kMaxBandWidth = 512;   // band slots a thread keeps (local memory)
+// Below this many pairs two-pairs-per-thread leaves most SMs idle; one warp per pair fills them.
+constexpr int64_t kPackedMinPairs = 32768;
 
 // _checkBandProperties (align/dp_algorithm_impl.h:193-234): the band must meet the matrix and
 // may leave it only across sides whose end gaps are free.
@@ -368,6 +370,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // keep int16 arithmetic exact (checked per pair below).
     const bool packed_ok = !plan->local && !plan->traceback && !plan->matrix && !p->band_on &&
                            !(p->flags & (GBA_FLAG_GENERAL_KERNEL | GBA_FLAG_PLAIN_BUCKETS)) &&
+                           (N >= kPackedMinPairs || (p->flags & (GBA_FLAG_STRIP16 | GBA_FLAG_PACKED))) &&
                            p->alphabet_size >= 1 &&
                            p->alphabet_size <= 8 && p->match >= -128 && p->match <= 127 &&
                            p->mismatch >= -128 && p->mismatch <= 127 && std::abs(p->gap_open) <= 1024 &&

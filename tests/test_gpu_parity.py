@@ -158,7 +158,7 @@ def test_python_interface_gaps(engine):
     assert (gH.row(), gV.row()) == ("AT-G-T", "ATAGAT")
 
 
-@pytest.mark.parametrize("flags", [0, 2])          # packed kernel with 32-row and 16-row strips
+@pytest.mark.parametrize("flags", [32, 2, 0])      # packed kernel (32-row, 16-row strips), warp kernel
 @pytest.mark.parametrize("fe", [0, 1, 2, 4, 8, 9, 6, 15, 5, 10])
 def test_packed_kernel_against_oracle(engine, flags, fe):
     """The two-pairs-per-thread 16-bit kernel: uneven lengths in one slot, odd pair count,
