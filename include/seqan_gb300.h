@@ -57,8 +57,9 @@ enum {
 enum {
     GBA_PAIR_OK = 0,
     GBA_PAIR_INVALID = 1,   /* empty sequence or band outside the matrix: score = numeric min */
-    GBA_PAIR_PROMOTED = 2   /* 16-bit cells were requested but the pair may leave the exact
+    GBA_PAIR_PROMOTED = 2,  /* 16-bit cells were requested but the pair may leave the exact
                                int16 range; it ran with 32-bit cells (exact result) */
+    GBA_PAIR_FAILED = 3     /* serving only: the request's batch failed (no result) */
 };
 
 enum { GBA_GLOBAL = 0, GBA_LOCAL = 1 };
@@ -207,6 +208,65 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
  * kernel.  No counterpart in the reference: it is the roofline denominator that the
  * benchmark reports the DP kernels against. */
 GBA_API int gba_measure_int_peak(gba_context *ctx, double *tops);
+
+/* --- Serving loop ---------------------------------------------------------------------
+ * No counterpart in the reference, which only has the blocking batch call.  A server owns a
+ * worker thread and `streams` batch slots, each with its own CUDA stream and device buffers
+ * that stay allocated between batches.  gba_server_submit queues one pair (its codes are
+ * copied); whenever a slot is free, the worker launches everything queued, in arrival order,
+ * up to max_batch_pairs pairs and as long as the device bytes of all batches in flight stay
+ * within hbm_budget_bytes, so requests that arrive while other batches run on the GPU are
+ * admitted as slots and memory free up, and their work overlaps on the device.  Finished
+ * batches are found by event query; gba_server_poll hands out their results.  Every request
+ * runs the same kernels as gba_align_batch: its result does not depend on which other
+ * requests share its batch.  All server calls are thread-safe. */
+typedef struct gba_server gba_server;
+
+typedef struct {
+    int32_t device;
+    int32_t streams;            /* batch slots in flight, 1..16 */
+    int64_t max_batch_pairs;    /* cap on the pairs of one launched batch (>= 1) */
+    int64_t hbm_budget_bytes;   /* admission bound on the device bytes of the batches in flight
+                                   (0 = none); a request that alone exceeds it is refused */
+} gba_server_config;
+
+typedef struct {
+    uint64_t tag;               /* the caller's tag from gba_server_submit */
+    int32_t score, end_h, end_v;
+    int32_t begin_h, begin_v;   /* with GBA_OUT_SEGMENTS */
+    int32_t status;             /* GBA_PAIR_* */
+    int32_t n_segments;         /* segments of this request in the poll's segment array */
+    int64_t segment_offset;     /* first of them */
+    double t_submit, t_done;    /* gba_clock_seconds() at submit / when its batch was found done */
+} gba_request_result;
+
+typedef struct {
+    int64_t submitted, completed, pending;  /* pending: queued, not launched yet */
+    int64_t batches;                        /* batches launched */
+    int64_t cells;                          /* DP cells of launched batches */
+    int64_t hbm_in_flight;                  /* device bytes of the batches in flight now */
+    int64_t hbm_in_flight_peak;             /* largest value hbm_in_flight took */
+} gba_server_stats;
+
+/* params: the scoring scheme and outputs of every request (no CIGAR); copied. */
+GBA_API int gba_server_create(gba_server **out, const gba_server_config *cfg, const gba_params *params);
+/* Queues pair (h[0..m), v[0..n)).  GBA_EBUDGET when the pair alone needs more device bytes
+ * than the budget. */
+GBA_API int gba_server_submit(gba_server *srv, uint64_t tag, const uint8_t *h, int64_t m, const uint8_t *v,
+                              int64_t n);
+/* Moves up to max_results finished requests into results (completion order) and their
+ * segments into segments[0..segment_capacity); *num_results / *num_segments say how many.
+ * Stops early at a request whose segments no longer fit (GBA_ECAPACITY if even the first one
+ * does not).  Does not wait. */
+GBA_API int gba_server_poll(gba_server *srv, gba_request_result *results, int64_t max_results,
+                            gba_segment *segments, int64_t segment_capacity, int64_t *num_results,
+                            int64_t *num_segments);
+GBA_API int gba_server_get_stats(gba_server *srv, gba_server_stats *stats);
+GBA_API int gba_server_last_error(gba_server *srv, char *buf, size_t size);
+/* Stops the worker after the batches in flight finish; unpolled results are dropped. */
+GBA_API int gba_server_destroy(gba_server *srv);
+/* Monotonic clock in seconds (the clock of t_submit / t_done). */
+GBA_API double gba_clock_seconds(void);
 
 /* --- Allocation-free scores ------------------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory on the

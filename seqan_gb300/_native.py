@@ -22,7 +22,7 @@ NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", 
 
 # Status codes (include/seqan_gb300.h)
 GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY = range(8)
-GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED = 0, 1, 2
+GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED, GBA_PAIR_FAILED = 0, 1, 2, 3
 GBA_GLOBAL, GBA_LOCAL = 0, 1
 GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE = 0, 1, 2
 GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
@@ -37,7 +37,9 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_plan_create", "gba_plan_destroy", "gba_plan_execute", "gba_plan_fetch",
             "gba_device_alloc", "gba_device_free", "gba_host_alloc", "gba_host_free",
             "gba_copy_to_device", "gba_copy_to_host", "gba_synchronize", "gba_timer_start",
-            "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc"]
+            "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc",
+            "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
+            "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds"]
 
 
 class GbaConfig(C.Structure):
@@ -78,6 +80,24 @@ class GbaStats(C.Structure):
                 ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64),
                 ("tile_rows", C.c_int32), ("tile_min_blocks", C.c_int32), ("host_plan_ms", C.c_float),
                 ("call_ms", C.c_float)]
+
+
+class GbaServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("streams", C.c_int32), ("max_batch_pairs", C.c_int64),
+                ("hbm_budget_bytes", C.c_int64)]
+
+
+class GbaRequestResult(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("score", C.c_int32), ("end_h", C.c_int32), ("end_v", C.c_int32),
+                ("begin_h", C.c_int32), ("begin_v", C.c_int32), ("status", C.c_int32),
+                ("n_segments", C.c_int32), ("segment_offset", C.c_int64), ("t_submit", C.c_double),
+                ("t_done", C.c_double)]
+
+
+class GbaServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("pending", C.c_int64),
+                ("batches", C.c_int64), ("cells", C.c_int64), ("hbm_in_flight", C.c_int64),
+                ("hbm_in_flight_peak", C.c_int64)]
 
 
 def _sources():
@@ -139,6 +159,15 @@ def lib():
             L.gba_measure_int_peak.argtypes = [vp, C.POINTER(C.c_double)]
             L.gba_align_score_noalloc.argtypes = [C.POINTER(GbaParams), C.POINTER(GbaNoAllocBatch), vp, vp,
                                                   vp, vp, vp]
+            L.gba_server_create.argtypes = [C.POINTER(vp), C.POINTER(GbaServerConfig), C.POINTER(GbaParams)]
+            L.gba_server_submit.argtypes = [vp, C.c_uint64, vp, i64, vp, i64]
+            L.gba_server_poll.argtypes = [vp, C.POINTER(GbaRequestResult), i64, vp, i64, C.POINTER(i64),
+                                          C.POINTER(i64)]
+            L.gba_server_get_stats.argtypes = [vp, C.POINTER(GbaServerStats)]
+            L.gba_server_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+            L.gba_server_destroy.argtypes = [vp]
+            L.gba_clock_seconds.argtypes = []
+            L.gba_clock_seconds.restype = C.c_double
             _lib = L
     return _lib
 

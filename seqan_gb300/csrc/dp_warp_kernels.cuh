@@ -1,18 +1,27 @@
-// dp_warp_kernels.cuh -- intra-pair parallel DP: one warp per pair (anti-diagonal wavefront).
+// dp_warp_kernels.cuh -- intra-pair parallel DP: bands of 32 * R rows, one warp per band.
 //
 // The 32 lanes of a warp own consecutive strips of R rows of V (a "band" of 32 * R rows).  At
 // step t lane l computes column t - l of its strip, so the lanes form an anti-diagonal front:
 // the bottom row of lane l - 1's strip for column j (its S and F) is handed to lane l by
 // __shfl_up_sync one step later, and the previous hand-off is the diagonal of lane l's first
-// row.  Matrices taller than one band pass the band's bottom row to the next band through a
-// per-pair row buffer in global memory.  Row 0 is computed by lane 0 of the first band as the
-// front passes.  Warps take pairs from a length-sorted queue (longest first).
+// row.  Row 0 is computed by lane 0 of band 0 as the front passes.
+//
+// The unit of work is one band of one pair.  Warps take (pair, band) tasks from a queue that
+// lists the pairs longest first and each pair's bands in order, so the bands of a long pair run
+// at the same time on different warps as a pipeline: band b reads band b - 1's bottom row
+// (S, F per column) from a two-slot row buffer in global memory, 32 columns at a time, once
+// band b - 1 has published that it has written them (a release/acquire counter per band).  Every
+// band a warp waits on was taken from the queue before its own band, by a warp that is running,
+// so the waits end; each wait still has an iteration limit after which the kernel records an
+// error and carries on.  Band b + 2 reuses band b's row slot: it writes column j only after
+// band b + 1 has produced column j, which band b + 1 does only after reading column j of band b.
 //
 // The per-cell code is the one-pair-per-thread strip kernel's (dp_kernels.cuh): recurrences,
 // tie rules, directions and tracked cells of the reference (align/dp_formula_affine.h:66-330,
 // align/dp_formula_linear.h:62-258, align/dp_meta_info.h:178-221).  Every lane keeps its own
 // best cell with the (column, row) order of the reference's column-major scout
-// (align/dp_scout.h:166-180) and the warp reduces the 32 candidates with the same order.
+// (align/dp_scout.h:166-180); the warp reduces the 32 candidates and the bands of a pair
+// combine theirs in band order with the same (total) order.
 //
 // Trace (optional): one byte per cell in step-major order -- for band b and step t the 32
 // lanes' R bytes are contiguous, so each step is one coalesced 32 * R byte store per warp.
@@ -22,13 +31,23 @@
 
 namespace gba {
 
+// Cross-band state of one band of a multi-band pair (zeroed before every run).
+struct BandState {
+    int progress;                  // columns of the band's bottom row written to the row buffer
+    int done;                      // 1 once s..row hold the best cell of bands 0..b
+    int s, e, f, col, row, pad;
+};
+
 struct WarpArgs {
     const uint8_t *seq_h;
     const uint8_t *seq_v;
     const PairDesc *pairs;
-    const int32_t *order;          // work item -> pair index (longest first)
-    int2 *rowbuf;                  // per pair at rowbuf_off[p]: (m + 1) int2 band boundary
+    const int2 *tasks;             // work item -> (pair, band); pairs longest first, bands in order
+    int2 *rowbuf;                  // per multi-band pair at rowbuf_off[p]: 2 x (m + 1) int2
     const int64_t *rowbuf_off;
+    BandState *bands;              // per multi-band pair at band_base[p]: one per band
+    const int64_t *band_base;
+    int32_t *error;                // set to 1 when a wait ran out
     uint8_t *trace;
     int32_t *score, *end_h, *end_v, *best_e, *best_f;
     const int32_t *matrix;
@@ -84,8 +103,38 @@ __device__ __forceinline__ void store_trace(uint8_t *dst, const uint32_t (&tw)[R
     }
 }
 
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Warp-wide wait until *p >= need, seen by every lane (each lane's own acquire orders its later
+// loads).  Gives up after about a second of polling, or at once when another wait already gave
+// up, recording the error.
+__device__ __forceinline__ void warp_wait_at_least(const int *p, int need, int32_t *error)
+{
+    for (int it = 0;; ++it) {
+        if (__all_sync(0xffffffffu, ld_acquire_gpu(p) >= need)) return;
+        if ((it & 1023) == 1023 && __any_sync(0xffffffffu, *(volatile int32_t *)error != 0)) return;
+        if (it > (1 << 22)) {
+            if ((threadIdx.x & 31) == 0) atomicExch(error, 1);
+            return;
+        }
+        __nanosleep(256);
+    }
+}
+
+constexpr int kRowChunk = 32;   // columns per row-buffer hand-off between bands
+
 template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int R>
-__device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
+__device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, int b, int lane)
 {
     const PairDesc d = a.pairs[p];
     const int m = d.m, n = d.n;
@@ -93,7 +142,6 @@ __device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
     const uint8_t *H = a.seq_h + d.h_off;
     const uint8_t *V = a.seq_v + d.v_off;
     uint8_t *T = TRACE ? a.trace + d.trace_off : nullptr;
-    int2 *rowbuf = a.rowbuf + a.rowbuf_off[p];
     const int fe = LOCAL ? (FREE_TOP | FREE_LEFT | FREE_RIGHT | FREE_BOTTOM) : a.free_ends;
     const bool fTop = fe & FREE_TOP, fLeft = fe & FREE_LEFT;
     const bool fRight = fe & FREE_RIGHT, fBottom = fe & FREE_BOTTOM;
@@ -104,9 +152,24 @@ __device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
     const int64_t row0Bytes = align16(m + 1);
 
     WarpBest best{INF, INF, INF, 0, 0};
-    if (LOCAL && lane == 0) best.offer(0, INF, INF, 0, 0);
+    if (LOCAL && lane == 0 && b == 0) best.offer(0, INF, INF, 0, 0);
+    // Row buffers: band b writes slot b & 1 and reads slot (b - 1) & 1.
+    int2 *rowOut = nullptr;
+    const int2 *rowIn = nullptr;
+    BandState *st = nullptr;
+    if (bands > 1) {
+        rowOut = a.rowbuf + a.rowbuf_off[p] + int64_t(b & 1) * (m + 1);
+        rowIn = a.rowbuf + a.rowbuf_off[p] + int64_t((b + 1) & 1) * (m + 1);
+        st = a.bands + a.band_base[p] + b;
+    }
+    int2 pre = make_int2(0, 0);   // lane k: entry c + k of the band above, for the next chunk c
+    auto fetch = [&](int c0) {
+        warp_wait_at_least(&st[-1].progress, min(c0 + kRowChunk, m + 1), a.error);
+        if (c0 + lane <= m) pre = __ldcg(rowIn + c0 + lane);
+    };
+    if (b > 0) fetch(0);
 
-    for (int b = 0; b < bands; ++b) {
+    {
         const int i0 = b * band_rows + lane * R + 1;      // first row of this lane's strip
         const bool active = i0 <= n;
         const bool lastStrip = i0 + R > n;                // the strip holds row n (or lies below it)
@@ -122,6 +185,13 @@ __device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
         uint8_t *Tband = TRACE ? T + row0Bytes + int64_t(b) * (m + 32) * 32 * R + int64_t(lane) * R : nullptr;
         for (int t = 0; t <= m + 31; ++t) {
             const int j = t - lane;
+            if (b > 0 && (t & (kRowChunk - 1)) == 0 && t <= m) {
+                // Stage chunk t of the band above, then prefetch chunk t + 32.
+                __syncwarp();
+                rb[lane] = pre;
+                __syncwarp();
+                if (t + kRowChunk <= m) fetch(t + kRowChunk);
+            }
             const int inS = __shfl_up_sync(0xffffffffu, outS, 1);
             const int inF = __shfl_up_sync(0xffffffffu, outF, 1);
             if (j < 0 || j > m) continue;
@@ -131,7 +201,7 @@ __device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
                 upS = inS;
                 upF = inF;
             } else if (b > 0) {
-                const int2 bb = rowbuf[j];
+                const int2 bb = rb[j & (kRowChunk - 1)];
                 upS = bb.x;
                 upF = bb.y;
             } else {
@@ -235,10 +305,11 @@ __device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
             if (TRACE) store_trace<R>(Tband + int64_t(t) * 32 * R, tw);
             outS = sUp;
             outF = fUp;
-            if (lane == 31 && b + 1 < bands) rowbuf[j] = make_int2(sUp, fUp);
+            if (lane == 31 && b + 1 < bands) {
+                rowOut[j] = make_int2(sUp, fUp);
+                if ((j & (kRowChunk - 1)) == kRowChunk - 1 || j == m) st_release_gpu(&st->progress, j + 1);
+            }
         }
-        // The next band's lane 0 reads what lane 31 stored.
-        __syncwarp();
     }
 
     // Warp reduction of the 32 best cells in the reference's column-major order.
@@ -250,6 +321,27 @@ __device__ void warp_pair(const WarpArgs &a, const int *smat, int p, int lane)
         const int oc = __shfl_down_sync(0xffffffffu, best.col, off);
         const int orr = __shfl_down_sync(0xffffffffu, best.row, off);
         if (lane + off < 32) best.offer(os, oe, of, oc, orr);
+    }
+    if (bands > 1) {
+        // Chain the bands' best cells in band order.
+        if (b > 0) {
+            warp_wait_at_least(&st[-1].done, 1, a.error);
+            if (lane == 0) {
+                const BandState *q = st - 1;
+                best.offer(__ldcg(&q->s), __ldcg(&q->e), __ldcg(&q->f), __ldcg(&q->col), __ldcg(&q->row));
+            }
+        }
+        if (b + 1 < bands) {
+            if (lane == 0) {
+                st->s = best.s;
+                st->e = best.e;
+                st->f = best.f;
+                st->col = best.col;
+                st->row = best.row;
+                st_release_gpu(&st->done, 1);
+            }
+            return;
+        }
     }
     if (lane == 0) {
         a.score[p] = best.s;
@@ -271,13 +363,18 @@ __global__ void __launch_bounds__(128) k_dp_warp(WarpArgs a)
         }
         __syncthreads();
     }
+    __shared__ int2 rbuf[4][kRowChunk];
+    static_assert(kRowChunk == 32, "one row-buffer entry per lane");
     const int lane = threadIdx.x & 31;
+    int2 *rb = rbuf[(threadIdx.x >> 5) & 3];
     for (;;) {
         int task = 0;
         if (lane == 0) task = atomicAdd(a.task_counter, 1);
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= a.num_tasks) break;
-        warp_pair<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, a.order[task], lane);
+        const int2 pb = a.tasks[task];
+        warp_band<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, rb, pb.x, pb.y, lane);
+        __syncwarp();
     }
 }
 

@@ -95,7 +95,10 @@ struct gba_plan {
     bool use_warp = false;
     int warp_rows = 8;
     int64_t grid_warp = 0;
-    DevBuf rowbuf, rowbuf_off, counter_warp;
+    DevBuf rowbuf, rowbuf_off, counter_warp, tasks_warp, band_base, band_state;
+    int64_t num_warp_tasks = 0;     // (pair, band) work items
+    int64_t num_band_states = 0;    // bands of pairs that span more than one band
+    int64_t num_tiled_tb = 0;       // leading slots whose traceback a whole warp walks
     int64_t grid16[8] = {};         // resident blocks of each packed-kernel variant
     int variant16 = 0;              // chosen tiling variant
     bool tune_pending = false;      // autotune at the first run
@@ -107,6 +110,7 @@ struct gba_plan {
     cudaGraphExec_t graph = nullptr;
     const void *graph_key[5] = {};
     int64_t seg_dense_total = -1, cig_dense_total = -1;
+    std::vector<int64_t> seg_off_host;   // per-pair segment slot offsets (num_pairs + 1)
     bool owned = true;
     void release()
     {
@@ -115,7 +119,7 @@ struct gba_plan {
                          &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
                          &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
                          &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16,
-                         &rowbuf, &rowbuf_off, &counter_warp};
+                         &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state};
         for (DevBuf *b : all) b->release();
         drop_graph();
     }
@@ -132,7 +136,8 @@ struct gba_plan {
                                &seg_slot_off, &seg_count, &seg_dense_off, &seg_dense, &seg_count64,
                                &cig_slots, &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense,
                                &cig_count64, &cub_tmp, &slots16, &warp_codes, &warp_hwords, &codes16,
-                               &warp_bnd16, &bnd16, &counter16, &rowbuf, &rowbuf_off, &counter_warp};
+                               &warp_bnd16, &bnd16, &counter16, &rowbuf, &rowbuf_off, &counter_warp,
+                               &tasks_warp, &band_base, &band_state};
         size_t s = 0;
         for (const DevBuf *b : all) s += b->cap;
         return s;
@@ -151,6 +156,8 @@ struct gba_context {
     gba_plan oneshot;               // buffers reused by gba_align_batch
     DevBuf seq_h, seq_v;            // device copies of the inputs for gba_align_batch
     DevBuf out_score, out_end_h, out_end_v;
+    DevBuf err_word;                // set by a kernel whose bounded wait ran out
+    bool check_err = false;         // the last run can set err_word
 };
 
 namespace {
@@ -468,6 +475,13 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         sort_desc(keys, idx);
     }
     plan->num_slots = int64_t(idx.size());
+    // Large pairs of the warp layout (a prefix of the cost-sorted order) get the warp-walked
+    // traceback; the key is strips of STRIP_ROWS rows x (m + 1) columns.
+    plan->num_tiled_tb = 0;
+    if (plan->use_warp && plan->traceback && !(p->flags & GBA_FLAG_PLAIN_BUCKETS))
+        while (plan->num_tiled_tb < int64_t(keys.size()) &&
+               keys[plan->num_tiled_tb] >= uint32_t(kTiledTraceCells / STRIP_ROWS))
+            ++plan->num_tiled_tb;
 
     // Packed path: neighbours in the length-sorted order share a thread; per warp, the code
     // words (4 residues per word, both pairs' codes per byte) and the boundary row are
@@ -507,17 +521,29 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->bnd16_total = btot;
     plan->tasks16 = int32_t(warps16);
 
-    // Warp path: one band-boundary row of m + 1 int2 per pair that spans more than one band.
-    std::vector<int64_t> rboff;
-    int64_t rbtot = 0;
+    // Warp path: (pair, band) tasks in the length-sorted pair order, each pair's bands in order.
+    // A pair of more than one band gets two row slots of m + 1 int2 and a BandState per band.
+    std::vector<int64_t> rboff, bbase;
+    std::vector<int2> wtasks;
+    int64_t rbtot = 0, nstates = 0;
     if (plan->use_warp) {
         rboff.assign(N + 1, 0);
-        for (int64_t k = 0; k < N; ++k) {
-            rboff[k] = rbtot;
-            if (!desc[k].invalid && desc[k].n > 32 * plan->warp_rows) rbtot += int64_t(desc[k].m) + 1;
+        bbase.assign(N + 1, 0);
+        const int band_rows = 32 * plan->warp_rows;
+        wtasks.reserve(idx.size());
+        for (int32_t k : idx) {
+            const int nb = (desc[k].n + band_rows - 1) / band_rows;
+            for (int bb = 0; bb < nb; ++bb) wtasks.push_back(make_int2(k, bb));
+            if (nb > 1) {
+                rboff[k] = rbtot;
+                rbtot += 2 * (int64_t(desc[k].m) + 1);
+                bbase[k] = nstates;
+                nstates += nb;
+            }
         }
-        rboff[N] = rbtot;
     }
+    plan->num_warp_tasks = int64_t(wtasks.size());
+    plan->num_band_states = nstates;
     // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
     const int64_t warps = plan->use_warp ? 0 : (plan->num_slots + 31) / 32;
     std::vector<int64_t> wscr(std::max<int64_t>(warps, 1));
@@ -539,6 +565,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             seg_off[k + 1] = seg_off[k] + cap;
         }
         plan->seg_slots_total = seg_off[N];
+        plan->seg_off_host = seg_off;
         if (plan->cigar) {
             cig_off = seg_off;
             plan->cigar_slots_total = seg_off[N];
@@ -549,7 +576,8 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     const int64_t need = int64_t(sizeof(PairDesc)) * N + 4 * N * 8 + scr * 8 + plan->trace_total +
                          plan->codes_total * 4 + plan->bnd16_total * 8 + plan->num16 * int64_t(sizeof(Slot16)) +
                          plan->seg_slots_total * 16 * 2 + plan->cigar_slots_total * 4 * 2 +
-                         plan->seq_h_bytes + plan->seq_v_bytes;
+                         plan->seq_h_bytes + plan->seq_v_bytes + rbtot * 8 + nstates * int64_t(sizeof(BandState)) +
+                         plan->num_warp_tasks * 8;
     if (ctx->budget > 0 && need > ctx->budget)
         return fail(ctx, GBA_EBUDGET, "batch needs %lld bytes of HBM, budget is %lld", (long long)need,
                     (long long)ctx->budget);
@@ -560,7 +588,11 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     GBA_CUDA(ctx, plan->scratch.ensure(size_t(std::max<int64_t>(scr, 1)) * sizeof(int2)));
     if (plan->use_warp && plan->num_slots > 0) {
         if ((rc = upload(ctx, plan->rowbuf_off, rboff))) return rc;
+        if ((rc = upload(ctx, plan->band_base, bbase))) return rc;
+        if ((rc = upload(ctx, plan->tasks_warp, wtasks))) return rc;
         GBA_CUDA(ctx, plan->rowbuf.ensure(size_t(std::max<int64_t>(rbtot, 1)) * sizeof(int2)));
+        GBA_CUDA(ctx, plan->band_state.ensure(size_t(std::max<int64_t>(nstates, 1)) * sizeof(BandState)));
+        GBA_CUDA(ctx, ctx->err_word.ensure(16));
         GBA_CUDA(ctx, plan->counter_warp.ensure(16));
         plan->grid_warp = persistent_grid(ctx, warp_fn(plan->affine, plan->local, plan->matrix, plan->traceback));
     }
@@ -808,9 +840,12 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         w.seq_h = dseq_h;
         w.seq_v = dseq_v;
         w.pairs = plan->pairs.as<PairDesc>();
-        w.order = plan->order.as<int32_t>();
+        w.tasks = plan->tasks_warp.as<int2>();
         w.rowbuf = plan->rowbuf.as<int2>();
         w.rowbuf_off = plan->rowbuf_off.as<int64_t>();
+        w.bands = plan->band_state.as<BandState>();
+        w.band_base = plan->band_base.as<int64_t>();
+        w.error = ctx->err_word.as<int32_t>();
         w.trace = plan->traceback ? plan->trace.as<uint8_t>() : nullptr;
         w.score = dscore;
         w.end_h = end_h;
@@ -819,7 +854,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         w.best_f = plan->traceback ? plan->best_f.as<int32_t>() : nullptr;
         w.matrix = plan->matrix ? plan->matrix_dev.as<int32_t>() : nullptr;
         w.task_counter = plan->counter_warp.as<int32_t>();
-        w.num_tasks = int32_t(plan->num_slots);
+        w.num_tasks = int32_t(plan->num_warp_tasks);
         w.match = plan->params.match;
         w.mismatch = plan->params.mismatch;
         w.gap_open = plan->params.gap_open;
@@ -827,7 +862,13 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         w.free_ends = plan->free_ends;
         w.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
         GBA_CUDA(ctx, cudaMemsetAsync(plan->counter_warp.ptr, 0, sizeof(int32_t), ctx->stream));
-        const int grid = int(std::min<int64_t>(plan->grid_warp, (plan->num_slots * 32 + kBlock - 1) / kBlock));
+        if (plan->num_band_states > 0) {
+            GBA_CUDA(ctx, cudaMemsetAsync(plan->band_state.ptr, 0, plan->num_band_states * sizeof(BandState),
+                                          ctx->stream));
+            GBA_CUDA(ctx, cudaMemsetAsync(ctx->err_word.ptr, 0, sizeof(int32_t), ctx->stream));
+        }
+        const int grid =
+            int(std::min<int64_t>(plan->grid_warp, (plan->num_warp_tasks * 32 + kBlock - 1) / kBlock));
         const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
         pick_warp(plan->affine, plan->local, plan->matrix, plan->traceback)(w, grid, smem, ctx->stream);
         GBA_CUDA(ctx, cudaGetLastError());
@@ -909,10 +950,21 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
             t.band_w = plan->params.band_on ? plan->params.band_upper - plan->params.band_lower + 1 : 0;
             t.band_upper = plan->params.band_upper;
             t.warp_rows = plan->use_warp ? plan->warp_rows : 0;
-            const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
-            k_traceback<<<grid, kBlock, 0, ctx->stream>>>(t);
+            const int64_t L = plan->num_tiled_tb;
+            if (L > 0) {
+                TraceArgs tl = t;
+                tl.num_slots = L;
+                k_traceback_tiled<kWarpRows><<<int((L + 1) / 2), 64, 0, ctx->stream>>>(tl);
+                ++launches;
+            }
+            if (plan->num_slots > L) {
+                TraceArgs ts = t;
+                ts.order = t.order + L;
+                ts.num_slots = plan->num_slots - L;
+                k_traceback<<<int((ts.num_slots + kBlock - 1) / kBlock), kBlock, 0, ctx->stream>>>(ts);
+                ++launches;
+            }
             GBA_CUDA(ctx, cudaGetLastError());
-            ++launches;
         }
         // Dense packing: exclusive scan of the counts, then a copy per pair.
         const int g1 = int((N + 1 + 255) / 256);
@@ -997,6 +1049,7 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         const int rc = enqueue_plan(ctx, plan, dseq_h, dseq_v, dscore, dend_h, dend_v, false);
         if (rc) return rc;
     }
+    ctx->check_err = plan->use_warp && plan->num_band_states > 0;
     ctx->stats.kernel_launches = plan->launches;
     ctx->stats.tile_rows = plan->num16 ? kVariants16[plan->variant16].rows : 0;
     ctx->stats.tile_min_blocks = plan->num16 ? kVariants16[plan->variant16].minb : 0;
@@ -1009,6 +1062,13 @@ int finish_stats(gba_context *ctx)
     if (!ctx->stats_pending) return GBA_OK;
     ctx->stats_pending = false;
     GBA_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
+    if (ctx->check_err) {
+        ctx->check_err = false;
+        int32_t e = 0;
+        GBA_CUDA(ctx, cudaMemcpyAsync(&e, ctx->err_word.ptr, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+        GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (e) return fail(ctx, GBA_ETIMEOUT, "a wait between the bands of a pair ran out");
+    }
     float a = 0, b = 0;
     GBA_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
     GBA_CUDA(ctx, cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
@@ -1116,6 +1176,7 @@ GBA_API int gba_destroy(gba_context *ctx)
     ctx->out_score.release();
     ctx->out_end_h.release();
     ctx->out_end_v.release();
+    ctx->err_word.release();
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1324,3 +1385,5 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 }
 
 }  // extern "C"
+
+#include "server.cuh"

@@ -6,7 +6,11 @@
 //   tail / head gap segments       align/dp_traceback_impl.h:522-545 (global only)
 //   walk order and gap walkers     align/dp_traceback_impl.h:190-450 (GapsLeft)
 //   segment recording              align/dp_trace_segment.h:318-337
-// and writes the segments in the reference's order (traceback order).  The CIGAR is the
+// and writes the segments in the reference's order (traceback order).  Pairs of the warp layout
+// with at least kTiledTraceCells cells are walked by a whole warp instead: every lane runs the
+// same walk, and the trace is read from a shared-memory tile of kTraceTileSteps steps of the
+// current band that the warp reloads together (coalesced) when the walk leaves it; lane 0
+// writes the outputs.  The CIGAR is the
 // run-length form of the same alignment columns that getCigarString iterates
 // (bam_io/cigar.h:261-339): DIAGONAL -> M, VERTICAL (gap in H) -> I, HORIZONTAL -> D, and a
 // D run of at least 20 becomes N.
@@ -22,6 +26,7 @@ struct SegWriter {
     uint32_t *out;
     int cap;
     int n;
+    bool leader;       // writes the records (all lanes of a warp walk keep the count)
     __device__ __forceinline__ void record(int hb, int vb, int len, int tv)
     {
         if (len == 0) return;
@@ -30,7 +35,7 @@ struct SegWriter {
         else if (tv & TV_V) type = TV_V;
         else if (tv & TV_H) type = TV_H;
         else return;
-        if (n < cap) {
+        if (leader && n < cap) {
             uint32_t *o = out + 4 * int64_t(n);
             o[0] = uint32_t(hb);
             o[1] = uint32_t(vb);
@@ -41,15 +46,13 @@ struct SegWriter {
     }
 };
 
-__global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
+// Walks pair p back from its best cell; TAT(col, row) reads one trace byte.  With leader false
+// the walk only counts (the other lanes of a warp walk).
+template <typename Cell>
+__device__ __forceinline__ void traceback_pair(const TraceArgs &a, int p, Cell &TAT, bool leader)
 {
-    const int64_t slot = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (slot >= a.num_slots) return;
-    const int p = a.order[slot];
-    if (p < 0) return;   // padding slot
     const PairDesc d = a.pairs[p];
     const int m = d.m, n = d.n;
-    const uint8_t *T = a.trace + d.trace_off;
     int col = a.end_h[p], row = a.end_v[p];
     const bool affine = a.affine != 0;
     const bool global = a.local == 0;
@@ -58,12 +61,8 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     w.out = a.seg_slots + 4 * a.seg_slot_off[p];
     w.cap = int(a.seg_slot_off[p + 1] - a.seg_slot_off[p]);
     w.n = 0;
+    w.leader = leader;
 
-    const int bw = a.band_w, bu = a.band_upper, wr = a.warp_rows;
-    auto TAT = [&](int c, int r) -> int {
-        if (wr) return int(trace_at_warp(T, m, wr, c, r));
-        return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
-    };
     int tv = TAT(col, row);
     if (affine) {
         const int s = a.score[p];
@@ -122,6 +121,7 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
         if (row != 0) w.record(0, 0, row, TV_V);
         if (col != 0) w.record(0, 0, col, TV_H);
     }
+    if (!leader) return;
     a.seg_count[p] = w.n;
     if (w.n > 0 && w.n <= w.cap) {
         const uint32_t *lastSeg = w.out + 4 * int64_t(w.n - 1);
@@ -162,6 +162,72 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     } else if (a.cigar_slots) {
         a.cigar_count[p] = 0;
     }
+}
+
+__global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
+{
+    const int64_t slot = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (slot >= a.num_slots) return;
+    const int p = a.order[slot];
+    if (p < 0) return;   // padding slot
+    const PairDesc d = a.pairs[p];
+    const int m = d.m;
+    const uint8_t *T = a.trace + d.trace_off;
+    const int bw = a.band_w, bu = a.band_upper, wr = a.warp_rows;
+    auto TAT = [&](int c, int r) -> int {
+        if (wr) return int(trace_at_warp(T, m, wr, c, r));
+        return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
+    };
+    traceback_pair(a, p, TAT, true);
+}
+
+constexpr int kTraceTileSteps = 64;             // steps of one band held in shared memory
+constexpr int64_t kTiledTraceCells = 1 << 20;   // pairs at least this large are walked by a warp
+
+// Trace reader of the warp layout (dp_warp_kernels.cuh) through a shared-memory tile: steps
+// [t0, t0 + kTraceTileSteps) of band tb, each step 32 * R bytes.  Called by all 32 lanes with
+// the same cell; a miss reloads the tile ending at the requested step (the walk only moves to
+// earlier steps).
+template <int R>
+struct TileCell {
+    const uint8_t *T;
+    int m;
+    uint4 *tile;
+    int tb, t0;
+    __device__ __forceinline__ int operator()(int col, int row)
+    {
+        if (row == 0) return T[col];
+        const int r0 = row - 1;
+        const int b = r0 / (32 * R);
+        const int within = r0 - b * 32 * R;
+        const int ln = within / R;
+        const int t = col + ln;
+        if (b != tb || t < t0 || t >= t0 + kTraceTileSteps) {
+            tb = b;
+            t0 = max(0, t - kTraceTileSteps + 1);
+            const int steps = min(kTraceTileSteps, m + 32 - t0);
+            const uint4 *src =
+                reinterpret_cast<const uint4 *>(T + align16(m + 1) + (int64_t(b) * (m + 32) + t0) * 32 * R);
+            const int lane = threadIdx.x & 31;
+            __syncwarp();
+            for (int q = lane; q < steps * 2 * R; q += 32) tile[q] = __ldcs(src + q);
+            __syncwarp();
+        }
+        return reinterpret_cast<const uint8_t *>(tile)[(t - t0) * 32 * R + within];
+    }
+};
+
+template <int R>
+__global__ void __launch_bounds__(64) k_traceback_tiled(TraceArgs a)
+{
+    __shared__ uint4 tiles[2][kTraceTileSteps * 2 * R];
+    const int64_t slot = int64_t(blockIdx.x) * 2 + (threadIdx.x >> 5);
+    if (slot >= a.num_slots) return;
+    const int p = a.order[slot];
+    if (p < 0) return;
+    const PairDesc d = a.pairs[p];
+    TileCell<R> cell{a.trace + d.trace_off, d.m, tiles[threadIdx.x >> 5], -1, 0};
+    traceback_pair(a, p, cell, (threadIdx.x & 31) == 0);
 }
 
 // Packs per-pair slot outputs densely: dst[off[k] ..] = src[slot_off[k] .. + count[k]].

@@ -313,3 +313,39 @@ def test_warp_kernel_protein_local(engine):
     assert np.array_equal(out.score, ref.score)
     for k in range(len(H)):
         assert out.pair_segments(k) == ref.segments[k], k
+
+
+def _long_mix(seed):
+    """A few long related pairs (1,000-6,000 bp and one 10,000 bp pair) mixed with short ones."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    H, V = [], []
+    for L in [10_000] + list(rng.integers(1000, 6001, 5)) + list(rng.integers(1, 400, 20)):
+        h = rng.integers(0, 4, int(L)).astype(np.uint8)
+        H.append(h)
+        V.append(W.mutate(rng, h, 0.05, 0.01))
+    order = rng.permutation(len(H))
+    return [H[i] for i in order], [V[i] for i in order]
+
+
+@pytest.mark.parametrize("mode,fe", [("global", 0), ("global", 9), ("global", 15), ("local", 0)])
+def test_long_pairs_pipelined_bands_and_warp_traceback(engine, mode, fe):
+    """Pairs of up to 40 bands, whose bands run on different warps and whose tracebacks are
+    walked by a warp through shared-memory tiles, mixed with short pairs; against the oracle."""
+    import seqan_gb300 as sg
+    H, V = _long_mix(700 + fe)
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    md = 1 if mode == "local" else 0
+    for (mt, mm, go, ge), bits in [((2, -4, -6, -1), 16), ((2, -3, -5, -5), 32)]:
+        sc = sg.Score(mt, mm, ge, go, dtype=np.int16 if bits == 16 else np.int32)
+        out = sg.align_codes(H, V, sc, mode=md, config=cfg, traceback=True, cigar=True)
+        # int16 scoring: pairs past the exact int16 range (the 10,000 bp one) are promoted to
+        # 32-bit cells, the others keep exact 16-bit values -- both equal 32-bit arithmetic.
+        ref = O.oracle_batch(O.Problem(mode, fe, None, mt, mm, go, ge, None, 32), H, V, traceback=True)
+        assert np.array_equal(out.score, ref.score)
+        assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+        for k in range(len(H)):
+            assert out.pair_segments(k) == ref.segments[k], k
+            assert out.pair_cigar(k) == O.cigar_string(ref.segments[k]), k
+        score_only = sg.align_codes(H, V, sc, mode=md, config=cfg)
+        assert np.array_equal(score_only.score, ref.score)
