@@ -13,7 +13,9 @@
 // band b - 1 has published that it has written them (a release/acquire counter per band).  Every
 // band a warp waits on was taken from the queue before its own band, by a warp that is running,
 // so the waits end; each wait still has an iteration limit after which the kernel records an
-// error and carries on.  Band b + 2 reuses band b's row slot: it writes column j only after
+// error and carries on.  A pipelined band idles for about 130 steps before its first column,
+// so when there is enough other work (many pairs) a narrow pair is instead one task (band -1)
+// whose warp runs its bands in order, with no waits.  Band b + 2 reuses band b's row slot: it writes column j only after
 // band b + 1 has produced column j, which band b + 1 does only after reading column j of band b.
 //
 // The per-cell code is the one-pair-per-thread strip kernel's (dp_kernels.cuh): recurrences,
@@ -88,6 +90,13 @@ struct WarpBest {
             s = cs; e = ce; f = cf; col = ccol; row = crow;
         }
     }
+    // For candidates visited in column-major order: a later cell wins only with a higher score.
+    __device__ __forceinline__ void offer_later(int cs, int ce, int cf, int ccol, int crow)
+    {
+        if (cs > s) {
+            s = cs; e = ce; f = cf; col = ccol; row = crow;
+        }
+    }
 };
 
 template <int R>
@@ -134,7 +143,8 @@ __device__ __forceinline__ void warp_wait_at_least(const int *p, int need, int32
 constexpr int kRowChunk = 32;   // columns per row-buffer hand-off between bands
 
 template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int R>
-__device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, int b, int lane)
+__device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, int b, int lane, bool seq,
+                          WarpBest &carry)
 {
     const PairDesc d = a.pairs[p];
     const int m = d.m, n = d.n;
@@ -164,7 +174,7 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
     }
     int2 pre = make_int2(0, 0);   // lane k: entry c + k of the band above, for the next chunk c
     auto fetch = [&](int c0) {
-        warp_wait_at_least(&st[-1].progress, min(c0 + kRowChunk, m + 1), a.error);
+        if (!seq) warp_wait_at_least(&st[-1].progress, min(c0 + kRowChunk, m + 1), a.error);
         if (c0 + lane <= m) pre = __ldcg(rowIn + c0 + lane);
     };
     if (b > 0) fetch(0);
@@ -184,6 +194,103 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
         int diagNext = INF;
         uint8_t *Tband = TRACE ? T + row0Bytes + int64_t(b) * (m + 32) * 32 * R + int64_t(lane) * R : nullptr;
         for (int t = 0; t <= m + 31; ++t) {
+            if (t == 32 && m - 1 >= 32) {
+                // Steady phase, steps 32 .. m - 1: every lane's column lies in [1, m - 1], so
+                // there is no column 0, no last column and no idle lane; lane 0's input is a
+                // select.  The recurrences run on max / add-max / 3-way max (the values equal the
+                // compare-and-select form of the other steps, ties included), and the trace bits
+                // come from comparisons off the dependency chain down the column.  Each lane
+                // meets its cells in column-major order.
+                const int rvalid = n - i0 + 1;             // rows of this strip inside the matrix
+                const int rowN = (rvalid >= 1 && rvalid <= R) ? rvalid - 1 : -1;   // row n, if here
+                const bool trackRowN = !LOCAL && fBottom && rowN >= 0;
+                int hnext = H[31 - lane];                  // H code of this lane's column at step 32
+                for (; t <= m - 1; ++t) {
+                    const int j = t - lane;
+                    if (b > 0 && (t & (kRowChunk - 1)) == 0) {
+                        __syncwarp();
+                        rb[lane] = pre;
+                        __syncwarp();
+                        if (t + kRowChunk <= m) fetch(t + kRowChunk);
+                    }
+                    const int inS = __shfl_up_sync(0xffffffffu, outS, 1);
+                    const int inF = __shfl_up_sync(0xffffffffu, outF, 1);
+                    const int hc = hnext;
+                    hnext = H[j];                          // column j + 1 at the next step
+                    int2 bb;
+                    if (b == 0) {
+                        // Row 0, column j (lane 0's; the other lanes' copies go unused).
+                        uint8_t tv0 = TV_NONE;
+                        if (!fTop) {
+                            if (AFFINE) {
+                                const int ex = e0 + EXT, op = s0 + OPEN;
+                                tv0 = ex < op ? (TV_HO | TV_MFH) : (TV_H | TV_MFH);
+                                e0 = max(ex, op);
+                                s0 = e0;
+                            } else {
+                                s0 = s0 + EXT;
+                                tv0 = TV_H | TV_MFH;
+                            }
+                        }
+                        if (TRACE && lane == 0) T[j] = tv0;
+                        bb = make_int2(s0, INF);
+                    } else {
+                        bb = rb[j & (kRowChunk - 1)];
+                    }
+                    int sUp = lane ? inS : bb.x;
+                    int fUp = lane ? inF : bb.y;
+                    int diag = diagNext;
+                    diagNext = sUp;
+                    const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
+                    uint32_t tw[R / 4];
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const int sub = MATRIX ? smat[hrow | (vc[r] & 31)] : (hc == vc[r] ? a.match : a.mismatch);
+                        const int inter = diag + sub;
+                        diag = Sp[r];
+                        int s, e = Ep[r], f = fUp;
+                        uint32_t tv = 0;
+                        if (AFFINE) {
+                            const int eExt = Ep[r] + EXT, eOpn = Sp[r] + OPEN;
+                            e = max(eExt, eOpn);
+                            const int fExt = fUp + EXT;
+                            f = __viaddmax_s32(sUp, OPEN, fExt);
+                            s = LOCAL ? __vimax3_s32_relu(inter, e, f) : __vimax3_s32(inter, e, f);
+                            if (TRACE) {
+                                tv = inter >= max(e, f) ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
+                                tv |= eExt < eOpn ? TV_HO : TV_H;
+                                tv |= fExt < sUp + OPEN ? TV_VO : TV_V;
+                            }
+                        } else {
+                            const int gv = sUp + EXT, gh = Sp[r] + EXT;
+                            s = LOCAL ? __vimax3_s32_relu(inter, gv, gh) : __vimax3_s32(inter, gv, gh);
+                            if (TRACE)
+                                tv = inter >= max(gv, gh) ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
+                        }
+                        if (TRACE && LOCAL && s == 0) tv = TV_NONE;
+                        Sp[r] = s;
+                        Ep[r] = e;
+                        sUp = s;
+                        fUp = f;
+                        if (TRACE) {
+                            if ((r & 3) == 0) tw[r >> 2] = 0;
+                            tw[r >> 2] |= tv << (8 * (r & 3));
+                        }
+                        if (LOCAL) {
+                            if (r < rvalid) best.offer_later(s, e, f, j, i0 + r);
+                        } else if (trackRowN && r == rowN) {
+                            best.offer_later(s, e, f, j, i0 + r);
+                        }
+                    }
+                    if (TRACE) store_trace<R>(Tband + int64_t(t) * 32 * R, tw);
+                    outS = sUp;
+                    outF = fUp;
+                    if (lane == 31 && b + 1 < bands) {
+                        rowOut[j] = make_int2(sUp, fUp);
+                        if (!seq && (j & (kRowChunk - 1)) == kRowChunk - 1) st_release_gpu(&st->progress, j + 1);
+                    }
+                }
+            }
             const int j = t - lane;
             if (b > 0 && (t & (kRowChunk - 1)) == 0 && t <= m) {
                 // Stage chunk t of the band above, then prefetch chunk t + 32.
@@ -307,7 +414,7 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
             outF = fUp;
             if (lane == 31 && b + 1 < bands) {
                 rowOut[j] = make_int2(sUp, fUp);
-                if ((j & (kRowChunk - 1)) == kRowChunk - 1 || j == m) st_release_gpu(&st->progress, j + 1);
+                if (!seq && ((j & (kRowChunk - 1)) == kRowChunk - 1 || j == m)) st_release_gpu(&st->progress, j + 1);
             }
         }
     }
@@ -322,7 +429,12 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
         const int orr = __shfl_down_sync(0xffffffffu, best.row, off);
         if (lane + off < 32) best.offer(os, oe, of, oc, orr);
     }
-    if (bands > 1) {
+    if (bands > 1 && seq) {
+        // One warp runs all bands of the pair in order: combine in registers.
+        if (lane == 0) carry.offer(best.s, best.e, best.f, best.col, best.row);
+        if (b + 1 < bands) return;
+        best = carry;
+    } else if (bands > 1) {
         // Chain the bands' best cells in band order.
         if (b > 0) {
             warp_wait_at_least(&st[-1].done, 1, a.error);
@@ -373,7 +485,19 @@ __global__ void __launch_bounds__(128) k_dp_warp(WarpArgs a)
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= a.num_tasks) break;
         const int2 pb = a.tasks[task];
-        warp_band<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, rb, pb.x, pb.y, lane);
+        WarpBest carry{0, 0, 0, 0, 0};
+        if (pb.y >= 0) {
+            warp_band<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, rb, pb.x, pb.y, lane, false, carry);
+        } else {
+            // Band -1: this warp runs every band of the pair in order (no waits between bands).
+            const PairDesc d = a.pairs[pb.x];
+            const int bands = (d.n + 32 * R - 1) / (32 * R);
+            carry = WarpBest{d.inf, d.inf, d.inf, 0, 0};
+            for (int b = 0; b < bands; ++b) {
+                warp_band<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, rb, pb.x, b, lane, true, carry);
+                __syncwarp();
+            }
+        }
         __syncwarp();
     }
 }

@@ -189,6 +189,9 @@ constexpr int kBlock = 128;
 constexpr int kMaxBandWidth = 512;   // band slots a thread keeps (local memory)
 // Below this many pairs two-pairs-per-thread leaves most SMs idle; one warp per pair fills them.
 constexpr int64_t kPackedMinPairs = 32768;
+// Pairs at least this wide pipeline their bands across warps even in large batches: the ~130
+// steps a pipelined band waits before its first column are then a small share of its work.
+constexpr int kPipelineMinCols = 1024;
 
 // _checkBandProperties (align/dp_algorithm_impl.h:193-234): the band must meet the matrix and
 // may leave it only across sides whose end gaps are free.
@@ -521,24 +524,34 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->bnd16_total = btot;
     plan->tasks16 = int32_t(warps16);
 
-    // Warp path: (pair, band) tasks in the length-sorted pair order, each pair's bands in order.
-    // A pair of more than one band gets two row slots of m + 1 int2 and a BandState per band.
+    // Warp path: tasks in the length-sorted pair order.  A pair's bands run as separate,
+    // pipelined tasks (pair, b) when the pair is wide or the batch too small to fill the GPU
+    // otherwise; else the pair is one task (pair, -1) whose warp runs its bands in order.  A
+    // pair of more than one band gets two row slots of m + 1 int2; a pipelined one also a
+    // BandState per band.
     std::vector<int64_t> rboff, bbase;
     std::vector<int2> wtasks;
     int64_t rbtot = 0, nstates = 0;
     if (plan->use_warp) {
+        plan->grid_warp = persistent_grid(ctx, warp_fn(plan->affine, plan->local, plan->matrix, plan->traceback));
+        const bool few_pairs = int64_t(idx.size()) < 2 * plan->grid_warp * (kBlock / 32);
         rboff.assign(N + 1, 0);
         bbase.assign(N + 1, 0);
         const int band_rows = 32 * plan->warp_rows;
         wtasks.reserve(idx.size());
         for (int32_t k : idx) {
             const int nb = (desc[k].n + band_rows - 1) / band_rows;
-            for (int bb = 0; bb < nb; ++bb) wtasks.push_back(make_int2(k, bb));
+            const bool pipe = nb > 1 && (few_pairs || desc[k].m >= kPipelineMinCols);
+            if (pipe) {
+                for (int bb = 0; bb < nb; ++bb) wtasks.push_back(make_int2(k, bb));
+                bbase[k] = nstates;
+                nstates += nb;
+            } else {
+                wtasks.push_back(make_int2(k, nb > 1 ? -1 : 0));
+            }
             if (nb > 1) {
                 rboff[k] = rbtot;
                 rbtot += 2 * (int64_t(desc[k].m) + 1);
-                bbase[k] = nstates;
-                nstates += nb;
             }
         }
     }
@@ -594,7 +607,6 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         GBA_CUDA(ctx, plan->band_state.ensure(size_t(std::max<int64_t>(nstates, 1)) * sizeof(BandState)));
         GBA_CUDA(ctx, ctx->err_word.ensure(16));
         GBA_CUDA(ctx, plan->counter_warp.ensure(16));
-        plan->grid_warp = persistent_grid(ctx, warp_fn(plan->affine, plan->local, plan->matrix, plan->traceback));
     }
     if (plan->num16 > 0) {
         if ((rc = upload(ctx, plan->slots16, slots16))) return rc;

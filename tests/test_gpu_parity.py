@@ -349,3 +349,29 @@ def test_long_pairs_pipelined_bands_and_warp_traceback(engine, mode, fe):
             assert out.pair_cigar(k) == O.cigar_string(ref.segments[k]), k
         score_only = sg.align_codes(H, V, sc, mode=md, config=cfg)
         assert np.array_equal(score_only.score, ref.score)
+
+
+@pytest.mark.parametrize("mode,fe", [("global", 0), ("global", 9), ("local", 0)])
+def test_many_narrow_multiband_pairs_run_bands_in_order(engine, mode, fe):
+    """20,000 pairs of 257-330 bp (two bands each): more pairs than twice the resident warps at
+    any occupancy, so each pair's warp runs its bands in order; against the oracle (scores and
+    ends of all pairs, segments of every 40th)."""
+    import seqan_gb300 as sg
+    rng = np.random.default_rng(900 + fe)
+    H = [rng.integers(0, 4, int(L)).astype(np.uint8) for L in rng.integers(257, 331, 20000)]
+    V = [h.copy() for h in H]
+    for v in V:
+        sub = rng.random(len(v)) < 0.08
+        v[sub] = (v[sub] + 1) % 4
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    md = 1 if mode == "local" else 0
+    sc = sg.Score(2, -4, -1, -6, dtype=np.int32)
+    out = sg.align_codes(H, V, sc, mode=md, config=cfg, traceback=True)
+    pb = O.Problem(mode, fe, None, 2, -4, -6, -1, None, 32)
+    ref = O.oracle_batch(pb, H, V)
+    assert np.array_equal(out.score, ref.score)
+    assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+    sub_idx = list(range(0, len(H), 40))
+    reft = O.oracle_batch(pb, [H[k] for k in sub_idx], [V[k] for k in sub_idx], traceback=True)
+    for i, k in enumerate(sub_idx):
+        assert out.pair_segments(k) == reft.segments[i], k
