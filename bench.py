@@ -52,6 +52,17 @@ WORKLOADS = {
 OPS_PER_CELL = {"affine_global": 9, "linear_global": 5, "affine_local": 10, "linear_local": 6}
 
 
+KERNEL_NAMES = [(2, "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)"),
+                (4, "k_dp_warp (one warp per 256-row band, anti-diagonal front)"),
+                (8, "k_dp_banded (one pair per thread, band in per-thread slots)"),
+                (1, "k_dp_strip (one pair per thread, int32)")]
+
+
+def kernel_label(bits: int) -> str:
+    """Names of the DP kernels a run launched (gba_stats.dp_kernels), the main one first."""
+    return " + ".join(name for bit, name in KERNEL_NAMES if bits & bit) or "none"
+
+
 class Spec:
     def __init__(self, H, V, score, mode, kind, config=None, band=None, traceback=False, cigar=False,
                  alphabet_size=4):
@@ -482,8 +493,7 @@ def main():
     achieved = ops / (dp_avg_ms * 1e-3) / 1e12
     roofline = {"bound": "int32", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
                 "frac": achieved / peak.value if peak.value else None, "traffic": None,
-                "kernel": "k_dp_strip (one pair per thread, int32)" if args.kernel == "general" else
-                          "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)", "ops_per_cell": OPS_PER_CELL[kind],
+                "kernel": kernel_label(st_last.dp_kernels), "ops_per_cell": OPS_PER_CELL[kind],
                 "dp_kernel_ms": dp_avg_ms,
                 "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"}
 
@@ -491,10 +501,6 @@ def main():
         roofline["trace_bytes_per_launch"] = int(st_last.trace_bytes)
         roofline["trace_write_gbs"] = st_last.trace_bytes / (dp_avg_ms * 1e-3) / 1e9
         roofline["traceback_and_output_ms"] = tb_avg_ms
-    if spec.band is not None:
-        roofline["kernel"] = "k_dp_banded (one pair per thread, band in per-thread slots)"
-    elif spec.mode == 1 or spec.traceback or args.kernel == "general":
-        roofline["kernel"] = "k_dp_strip (one pair per thread, int32)"
     line = {"metric": "GCUPS, batched affine DNA align", "value": value, "unit": "GCUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -201,7 +201,16 @@ typedef struct {
     int32_t tile_min_blocks;   /* packed kernel: minimum resident blocks per SM */
     float host_plan_ms;        /* gba_align_batch: host planning time */
     float call_ms;             /* gba_align_batch: whole call, wall clock */
+    int32_t dp_kernels;        /* GBA_KERNEL_* bits: the DP kernels the run launched */
 } gba_stats;
+
+/* DP kernels (gba_stats.dp_kernels). */
+enum {
+    GBA_KERNEL_STRIP = 1,      /* one pair per thread, 16-row register strips, int32 */
+    GBA_KERNEL_PACKED = 2,     /* two pairs per thread, int16x2 DPX */
+    GBA_KERNEL_WARP = 4,       /* bands of 256 rows, one warp per band, anti-diagonal front */
+    GBA_KERNEL_BANDED = 8      /* banded DP, one pair per thread */
+};
 GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
 
 /* Measures the device's 32-bit integer add/max rate (tera-ops per second) with a short

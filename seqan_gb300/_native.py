@@ -79,7 +79,7 @@ class GbaStats(C.Structure):
     _fields_ = [("dp_kernel_ms", C.c_float), ("traceback_kernel_ms", C.c_float),
                 ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64),
                 ("tile_rows", C.c_int32), ("tile_min_blocks", C.c_int32), ("host_plan_ms", C.c_float),
-                ("call_ms", C.c_float)]
+                ("call_ms", C.c_float), ("dp_kernels", C.c_int32)]
 
 
 class GbaServerConfig(C.Structure):

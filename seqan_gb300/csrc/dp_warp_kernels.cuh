@@ -99,6 +99,19 @@ struct WarpBest {
     }
 };
 
+// Maximum of a strip's R values with 3-way max instructions.
+template <int R>
+__device__ __forceinline__ int strip_max(const int (&v)[R])
+{
+    int m = v[0];
+    int r = 1;
+#pragma unroll
+    for (; r + 1 < R; r += 2) m = __vimax3_s32(m, v[r], v[r + 1]);
+#pragma unroll
+    for (; r < R; ++r) m = max(m, v[r]);
+    return m;
+}
+
 template <int R>
 __device__ __forceinline__ void store_trace(uint8_t *dst, const uint32_t (&tw)[R / 4])
 {
@@ -243,6 +256,7 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
                     diagNext = sUp;
                     const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
                     uint32_t tw[R / 4];
+                    int Fp[R];                             // F of each row (for the best cell)
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
                         const int sub = MATRIX ? smat[hrow | (vc[r] & 31)] : (hc == vc[r] ? a.match : a.mismatch);
@@ -257,30 +271,52 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
                             f = __viaddmax_s32(sUp, OPEN, fExt);
                             s = LOCAL ? __vimax3_s32_relu(inter, e, f) : __vimax3_s32(inter, e, f);
                             if (TRACE) {
-                                tv = inter >= max(e, f) ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
-                                tv |= eExt < eOpn ? TV_HO : TV_H;
-                                tv |= fExt < sUp + OPEN ? TV_VO : TV_V;
+                                // s == inter: the diagonal wins (ties included); e != eExt: the
+                                // gap opened (eExt < eOpn); f != fExt: likewise for F.  With the
+                                // local zero floor, s == 0 overrides everything below.
+                                tv = s == inter ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
+                                tv |= e != eExt ? TV_HO : TV_H;
+                                tv |= f != fExt ? TV_VO : TV_V;
                             }
                         } else {
                             const int gv = sUp + EXT, gh = Sp[r] + EXT;
                             s = LOCAL ? __vimax3_s32_relu(inter, gv, gh) : __vimax3_s32(inter, gv, gh);
                             if (TRACE)
-                                tv = inter >= max(gv, gh) ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
+                                tv = s == inter ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
                         }
                         if (TRACE && LOCAL && s == 0) tv = TV_NONE;
                         Sp[r] = s;
                         Ep[r] = e;
+                        Fp[r] = f;
                         sUp = s;
                         fUp = f;
                         if (TRACE) {
                             if ((r & 3) == 0) tw[r >> 2] = 0;
                             tw[r >> 2] |= tv << (8 * (r & 3));
                         }
-                        if (LOCAL) {
-                            if (r < rvalid) best.offer_later(s, e, f, j, i0 + r);
-                        } else if (trackRowN && r == rowN) {
-                            best.offer_later(s, e, f, j, i0 + r);
+                    }
+                    if (LOCAL) {
+                        // Column j's best row of this strip: the first row holding the strip's
+                        // maximum, taken only when it beats every earlier column.
+                        if (rvalid >= R) {
+                            const int mx = strip_max<R>(Sp);
+                            if (mx > best.s) {
+#pragma unroll
+                                for (int r = 0; r < R; ++r)
+                                    if (Sp[r] == mx) {
+                                        best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                                        break;
+                                    }
+                            }
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r < rvalid) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
                         }
+                    } else if (trackRowN) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == rowN) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
                     }
                     if (TRACE) store_trace<R>(Tband + int64_t(t) * 32 * R, tw);
                     outS = sUp;
@@ -465,7 +501,7 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
 }
 
 template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int R>
-__global__ void __launch_bounds__(128) k_dp_warp(WarpArgs a)
+__global__ void __launch_bounds__(128, 4) k_dp_warp(WarpArgs a)
 {
     extern __shared__ int smat[];
     if (MATRIX) {

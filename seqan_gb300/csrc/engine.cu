@@ -31,25 +31,37 @@ using namespace gba;
 namespace {
 
 // ------------------------------------------------------------------------------------
-// Device buffer that only grows.
+// Device buffer that only grows.  Bound to a stream, it is allocated and freed in stream
+// order (cudaMallocAsync / cudaFreeAsync): growing it does not synchronize the device, so
+// batches in flight on other streams keep running.  The buffer is idle whenever it grows.
 // ------------------------------------------------------------------------------------
 struct DevBuf {
     void *ptr = nullptr;
     size_t cap = 0;
+    cudaStream_t stream = nullptr;
+    bool async = false;
+    void bind(cudaStream_t s)
+    {
+        if (ptr && async != true) release();
+        stream = s;
+        async = true;
+    }
     cudaError_t ensure(size_t bytes)
     {
         if (bytes <= cap) return cudaSuccess;
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        cap = 0;
+        release();
         size_t want = std::max<size_t>(bytes, 256);
-        cudaError_t e = cudaMalloc(&ptr, want);
+        cudaError_t e = async ? cudaMallocAsync(&ptr, want, stream) : cudaMalloc(&ptr, want);
         if (e == cudaSuccess) cap = want;
+        else ptr = nullptr;
         return e;
     }
     void release()
     {
-        if (ptr) cudaFree(ptr);
+        if (ptr) {
+            if (async) cudaFreeAsync(ptr, stream);
+            else cudaFree(ptr);
+        }
         ptr = nullptr;
         cap = 0;
     }
@@ -122,6 +134,17 @@ struct gba_plan {
                          &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state};
         for (DevBuf *b : all) b->release();
         drop_graph();
+    }
+    void bind(cudaStream_t s)
+    {
+        DevBuf *all[] = {&pairs, &order, &warp_scratch, &scratch, &trace, &best_e, &best_f, &matrix_dev,
+                         &end_h, &end_v, &score_tmp, &begin_h, &begin_v, &seg_slots, &seg_slot_off,
+                         &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
+                         &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
+                         &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16,
+                         &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state};
+        for (DevBuf *b : all)
+            if (!b->async || b->stream != s) b->bind(s);
     }
     void drop_graph()
     {
@@ -361,6 +384,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     int rc = validate(ctx, p, b);
     if (rc) return rc;
     const int64_t N = b->num_pairs;
+    plan->bind(ctx->stream);
     plan->params = *p;
     plan->num_pairs = N;
     plan->affine = is_affine(*p);
@@ -1065,6 +1089,10 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
     ctx->stats.kernel_launches = plan->launches;
     ctx->stats.tile_rows = plan->num16 ? kVariants16[plan->variant16].rows : 0;
     ctx->stats.tile_min_blocks = plan->num16 ? kVariants16[plan->variant16].minb : 0;
+    ctx->stats.dp_kernels = (plan->num16 > 0 ? GBA_KERNEL_PACKED : 0) |
+                            (plan->num_slots > 0 ? (plan->params.band_on ? GBA_KERNEL_BANDED
+                                                    : plan->use_warp ? GBA_KERNEL_WARP : GBA_KERNEL_STRIP)
+                                                 : 0);
     ctx->stats_pending = true;
     return GBA_OK;
 }
@@ -1171,6 +1199,15 @@ GBA_API int gba_create(gba_context **out, const gba_config *cfg)
     if (ctx->device < 0 || ctx->device >= ndev) return GBA_EINVAL;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return GBA_ECUDA;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return GBA_ECUDA;
+    // Stream-ordered buffers: keep freed blocks in the device's pool for reuse instead of
+    // unmapping them at every synchronization (a setting of this process only).
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    for (DevBuf *b : {&ctx->seq_h, &ctx->seq_v, &ctx->out_score, &ctx->out_end_h, &ctx->out_end_v, &ctx->err_word})
+        b->bind(ctx->stream);
     for (auto &ev : ctx->ev)
         if (cudaEventCreate(&ev) != cudaSuccess) return GBA_ECUDA;
     *out = ctx.release();
@@ -1189,6 +1226,7 @@ GBA_API int gba_destroy(gba_context *ctx)
     ctx->out_end_h.release();
     ctx->out_end_v.release();
     ctx->err_word.release();
+    cudaStreamSynchronize(ctx->stream);   // the stream-ordered frees above
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1272,8 +1310,15 @@ GBA_API int gba_plan_destroy(gba_context *ctx, gba_plan *plan)
     if (ctx) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
+        plan->release();
+        cudaStreamSynchronize(ctx->stream);
+    } else {
+        // Without its context the plan's stream may be gone: free in order on the default stream.
+        cudaDeviceSynchronize();
+        plan->bind(nullptr);
+        plan->release();
+        cudaDeviceSynchronize();
     }
-    plan->release();
     delete plan;
     return GBA_OK;
 }

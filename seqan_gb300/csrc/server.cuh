@@ -331,6 +331,15 @@ GBA_API int gba_server_create(gba_server **out, const gba_server_config *cfg, co
             for (auto &x : s->slots) gba_destroy(x->ctx);
             return rc;
         }
+        for (DevBuf *db : {&sl->dseq_h, &sl->dseq_v, &sl->dscore}) db->bind(sl->ctx->stream);
+        // Pinned staging sized for a few thousand requests up front (growing it later can
+        // synchronize the device).
+        if (sl->seq_h.ensure(4u << 20) != cudaSuccess || sl->seq_v.ensure(4u << 20) != cudaSuccess ||
+            sl->out.ensure(1u << 20) != cudaSuccess || sl->segs.ensure(32u << 20) != cudaSuccess) {
+            gba_destroy(sl->ctx);
+            for (auto &x : s->slots) gba_destroy(x->ctx);
+            return GBA_ENOMEM;
+        }
         if (cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess) {
             gba_destroy(sl->ctx);
             for (auto &x : s->slots) gba_destroy(x->ctx);
