@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-shared"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-shared", "-lgomp"]
 
 # Status codes (include/seqan_gb300.h)
 GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY = range(8)

@@ -15,10 +15,12 @@
 
 #include <cub/device/device_scan.cuh>
 #include <cuda_runtime.h>
+#include <omp.h>
 
 #include <algorithm>
 #include <chrono>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -123,6 +125,11 @@ struct gba_plan {
     const void *graph_key[5] = {};
     int64_t seg_dense_total = -1, cig_dense_total = -1;
     std::vector<int64_t> seg_off_host;   // per-pair segment slot offsets (num_pairs + 1)
+    // Host-side planning arrays, reused by the next build of this plan.
+    std::vector<PairDesc> h_desc;
+    std::vector<uint32_t> h_keys16, h_keys, h_key;
+    std::vector<int32_t> h_idx16, h_idx;
+    std::vector<uint8_t> h_cls;
     bool owned = true;
     void release()
     {
@@ -297,10 +304,65 @@ int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
     return GBA_OK;
 }
 
-// LSD radix sort of (key, index) by key descending; keys < 2^32.
+int plan_threads(int64_t work);
+
+// Stable sort of (key, index) by key descending; keys < 2^32.  Small key ranges (the strip
+// costs of short pairs) take one counting pass, others two 16-bit LSD radix passes.
 void sort_desc(std::vector<uint32_t> &keys, std::vector<int32_t> &idx)
 {
     const size_t n = idx.size();
+    if (n == 0) return;
+    const uint32_t kmax = *std::max_element(keys.begin(), keys.end());
+    const int nth = kmax < 65536 ? plan_threads(int64_t(n)) : 1;
+    if (nth > 1) {
+        // Per-thread histograms of contiguous chunks; bucket-major, thread-minor offsets keep
+        // the sort stable.
+        const size_t K = size_t(kmax) + 1;
+        std::vector<uint32_t> hist(size_t(nth) * K, 0);
+        std::vector<uint32_t> k2(n);
+        std::vector<int32_t> i2(n);
+#pragma omp parallel num_threads(nth)
+        {
+            const int t = omp_get_thread_num();
+            const size_t a = n * t / nth, b = n * (t + 1) / nth;
+            uint32_t *h = hist.data() + size_t(t) * K;
+            for (size_t i = a; i < b; ++i) ++h[kmax - keys[i]];
+#pragma omp barrier
+#pragma omp single
+            {
+                uint32_t run = 0;
+                for (size_t q = 0; q < K; ++q)
+                    for (int u = 0; u < nth; ++u) {
+                        const uint32_t c = hist[size_t(u) * K + q];
+                        hist[size_t(u) * K + q] = run;
+                        run += c;
+                    }
+            }
+            for (size_t i = a; i < b; ++i) {
+                const size_t d = h[kmax - keys[i]]++;
+                k2[d] = keys[i];
+                i2[d] = idx[i];
+            }
+        }
+        keys.swap(k2);
+        idx.swap(i2);
+        return;
+    }
+    if (kmax < std::max<uint64_t>(65536, 4 * uint64_t(n))) {
+        std::vector<uint32_t> cnt(size_t(kmax) + 2, 0);
+        for (size_t i = 0; i < n; ++i) ++cnt[size_t(kmax - keys[i]) + 1];
+        for (size_t i = 1; i < cnt.size(); ++i) cnt[i] += cnt[i - 1];
+        std::vector<uint32_t> k2(n);
+        std::vector<int32_t> i2(n);
+        for (size_t i = 0; i < n; ++i) {
+            const size_t d = cnt[kmax - keys[i]]++;
+            k2[d] = keys[i];
+            i2[d] = idx[i];
+        }
+        keys.swap(k2);
+        idx.swap(i2);
+        return;
+    }
     std::vector<uint32_t> k2(n);
     std::vector<int32_t> i2(n);
     for (int pass = 0; pass < 2; ++pass) {
@@ -378,9 +440,41 @@ int64_t persistent_grid(gba_context *ctx, const void *fn)
 
 const void *warp_fn(bool a, bool l, bool m, bool t);
 
+// Host threads for a planning loop over `work` items: serial below 16,384 items.
+int plan_threads(int64_t work)
+{
+    if (work < 16384) return 1;
+    return int(std::max<int64_t>(1, std::min<int64_t>({int64_t(omp_get_max_threads()), 16, work / 8192})));
+}
+
+// Phase timer of build_plan: with GBA_PLAN_PROFILE set in the environment, each plan prints
+// its phases' host milliseconds to stderr (diagnostics only).
+struct PlanTimer {
+    bool on = std::getenv("GBA_PLAN_PROFILE") != nullptr;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now(), last = t0;
+    std::string line;
+    void mark(const char *what)
+    {
+        if (!on) return;
+        const auto now = std::chrono::steady_clock::now();
+        char buf[64];
+        std::snprintf(buf, sizeof(buf), " %s=%.3f", what, std::chrono::duration<double, std::milli>(now - last).count());
+        line += buf;
+        last = now;
+    }
+    ~PlanTimer()
+    {
+        if (on)
+            std::fprintf(stderr, "[gba plan] total=%.3f ms:%s\n",
+                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(),
+                         line.c_str());
+    }
+};
+
 // Builds a plan from host offsets.  `plan` buffers are (re)used.
 int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_plan *plan)
 {
+    PlanTimer timer;
     int rc = validate(ctx, p, b);
     if (rc) return rc;
     const int64_t N = b->num_pairs;
@@ -414,70 +508,129 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // one-pair-per-thread kernel is forced.
     plan->use_warp = !p->band_on && !(p->flags & (GBA_FLAG_GENERAL_KERNEL | GBA_FLAG_PLAIN_BUCKETS));
     plan->warp_rows = 8;
-    std::vector<uint32_t> keys16;
-    std::vector<int32_t> idx16;
-    std::map<uint64_t, int64_t> band_cell_cache;
-    std::vector<PairDesc> desc(std::max<int64_t>(N, 1));
-    std::vector<uint32_t> keys;
-    std::vector<int32_t> idx;
-    keys.reserve(N);
-    idx.reserve(N);
+    // Host arrays live in the plan and keep their capacity between builds (no zero fill).
+    auto &keys16 = plan->h_keys16;
+    auto &idx16 = plan->h_idx16;
+    auto &desc = plan->h_desc;
+    auto &keys = plan->h_keys;
+    auto &idx = plan->h_idx;
+    desc.resize(std::max<int64_t>(N, 1));
     plan->cells = 0;
     int64_t trace_off = 0;
     const int64_t hs0 = b->h_shared ? b->off_h[0] : 0;
     const int64_t hs1 = b->h_shared ? b->off_h[1] : 0;
     plan->seq_h_bytes = N ? (b->h_shared ? b->off_h[1] : b->off_h[N]) : 0;
     plan->seq_v_bytes = N ? b->off_v[N] : 0;
-    for (int64_t k = 0; k < N; ++k) {
-        const int64_t h0 = b->h_shared ? hs0 : b->off_h[k];
-        const int64_t h1 = b->h_shared ? hs1 : b->off_h[k + 1];
-        const int64_t v0 = b->off_v[k], v1 = b->off_v[k + 1];
-        if (h0 < 0 || v0 < 0 || h1 < h0 || v1 < v0)
-            return fail(ctx, GBA_EINVAL, "negative or decreasing offsets at pair %lld", (long long)k);
-        if (h1 - h0 > (1 << 30) || v1 - v0 > (1 << 30)) return fail(ctx, GBA_EINVAL, "sequence too long");
-        PairDesc &d = desc[k];
-        d.h_off = h0;
-        d.v_off = v0;
-        d.m = int32_t(h1 - h0);
-        d.n = int32_t(v1 - v0);
-        d.trace_off = 0;
-        d.invalid = 0;
-        bool exact16 = p->score_bits == 16 && int16_exact(*p, max_pos, d.m, d.n, plan->local);
-        d.inf = exact16 ? -16384 : -(1 << 30);
-        if (p->score_bits == 16 && !exact16) plan->status[k] = GBA_PAIR_PROMOTED;
-        const int fe_all = plan->local ? 15 : p->free_ends;
-        if (d.m == 0 || d.n == 0 || (p->band_on && !band_valid(*p, d.m, d.n, fe_all))) {
-            plan->status[k] = GBA_PAIR_INVALID;
-            d.invalid = 1;
-            continue;
+    // Per-pair pass, in parallel over contiguous chunks of pairs: descriptor, status, class
+    // (packed path / other / invalid), sort key and trace bytes.  Then each chunk appends its
+    // pairs to the class lists and assigns trace offsets at its prefix-summed position, so the
+    // lists are in input order exactly as a serial pass makes them.
+    const int nth = plan_threads(N);
+    auto &cls = plan->h_cls;
+    auto &key = plan->h_key;
+    cls.resize(N);
+    key.resize(N);
+    std::vector<int64_t> tbytes(plan->traceback ? N : 0);
+    std::vector<int64_t> c16(nth + 1, 0), cot(nth + 1, 0), ctr(nth + 1, 0);
+    int64_t first_bad = N, cells = 0;
+    const int fe_all = plan->local ? 15 : p->free_ends;
+#pragma omp parallel num_threads(nth) reduction(+ : cells) reduction(min : first_bad)
+    {
+        const int t = omp_get_thread_num();
+        const int64_t k0 = N * t / nth, k1 = N * (t + 1) / nth;
+        std::map<uint64_t, int64_t> band_cache;
+        int64_t n16 = 0, not16 = 0, tsum = 0;
+        for (int64_t k = k0; k < k1; ++k) {
+            const int64_t h0 = b->h_shared ? hs0 : b->off_h[k];
+            const int64_t h1 = b->h_shared ? hs1 : b->off_h[k + 1];
+            const int64_t v0 = b->off_v[k], v1 = b->off_v[k + 1];
+            PairDesc &d = desc[k];
+            cls[k] = 0;
+            if (h0 < 0 || v0 < 0 || h1 < h0 || v1 < v0 || h1 - h0 > (1 << 30) || v1 - v0 > (1 << 30)) {
+                first_bad = std::min(first_bad, k);
+                d.invalid = 1;
+                continue;
+            }
+            d.h_off = h0;
+            d.v_off = v0;
+            d.m = int32_t(h1 - h0);
+            d.n = int32_t(v1 - v0);
+            d.trace_off = 0;
+            d.invalid = 0;
+            const bool exact16 = p->score_bits == 16 && int16_exact(*p, max_pos, d.m, d.n, plan->local);
+            d.inf = exact16 ? -16384 : -(1 << 30);
+            plan->status[k] = (p->score_bits == 16 && !exact16) ? GBA_PAIR_PROMOTED : GBA_PAIR_OK;
+            if (d.m == 0 || d.n == 0 || (p->band_on && !band_valid(*p, d.m, d.n, fe_all))) {
+                plan->status[k] = GBA_PAIR_INVALID;
+                d.invalid = 1;
+                continue;
+            }
+            if (p->band_on) {
+                const uint64_t ck = (uint64_t(d.m) << 32) | uint32_t(d.n);
+                auto it = band_cache.find(ck);
+                if (it == band_cache.end())
+                    it = band_cache.emplace(ck, band_cells(d.m, d.n, p->band_lower, p->band_upper)).first;
+                cells += it->second;
+            } else {
+                cells += int64_t(d.m) * d.n;
+            }
+            if (plan->traceback) {
+                tbytes[k] = p->band_on ? align16(int64_t(d.m + 1) * (p->band_upper - p->band_lower + 1))
+                            : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
+                                             : trace_bytes(d.m, d.n);
+                tsum += tbytes[k];
+            }
+            // (packed_ok excludes local mode, so exact16 is the global-mode check here)
+            if (packed_ok && (p->score_bits == 16 ? exact16 : int16_exact(*p, max_pos, d.m, d.n, false))) {
+                const int64_t strips = (d.n + plan->rows16 - 1) / plan->rows16;
+                key[k] = uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL));
+                cls[k] = 1;
+                ++n16;
+            } else {
+                const int64_t strips = (d.n + STRIP_ROWS - 1) / STRIP_ROWS;
+                key[k] = uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL));
+                cls[k] = 2;
+                ++not16;
+            }
         }
-        if (p->band_on) {
-            const uint64_t ck = (uint64_t(d.m) << 32) | uint32_t(d.n);
-            auto it = band_cell_cache.find(ck);
-            if (it == band_cell_cache.end())
-                it = band_cell_cache.emplace(ck, band_cells(d.m, d.n, p->band_lower, p->band_upper)).first;
-            plan->cells += it->second;
-        } else {
-            plan->cells += int64_t(d.m) * d.n;
+        c16[t + 1] = n16;
+        cot[t + 1] = not16;
+        ctr[t + 1] = tsum;
+#pragma omp barrier
+#pragma omp single
+        for (int i = 0; i < nth; ++i) {
+            c16[i + 1] += c16[i];
+            cot[i + 1] += cot[i];
+            ctr[i + 1] += ctr[i];
         }
-        if (plan->traceback) {
-            d.trace_off = trace_off;
-            trace_off += p->band_on ? align16(int64_t(d.m + 1) * (p->band_upper - p->band_lower + 1))
-                         : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
-                                          : trace_bytes(d.m, d.n);
+#pragma omp single
+        {
+            keys16.resize(c16[nth]);
+            idx16.resize(c16[nth]);
+            keys.resize(cot[nth]);
+            idx.resize(cot[nth]);
         }
-        if (packed_ok && int16_exact(*p, max_pos, d.m, d.n, false)) {
-            const int64_t strips = (d.n + plan->rows16 - 1) / plan->rows16;
-            keys16.push_back(uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL)));
-            idx16.push_back(int32_t(k));
-            continue;
+        int64_t q16 = c16[t], qot = cot[t], toff = ctr[t];
+        for (int64_t k = k0; k < k1; ++k) {
+            if (cls[k] == 1) {
+                keys16[q16] = key[k];
+                idx16[q16++] = int32_t(k);
+            } else if (cls[k] == 2) {
+                keys[qot] = key[k];
+                idx[qot++] = int32_t(k);
+            }
+            if (plan->traceback && cls[k] != 0) {
+                desc[k].trace_off = toff;
+                toff += tbytes[k];
+            }
         }
-        const int64_t strips = (d.n + STRIP_ROWS - 1) / STRIP_ROWS;
-        const int64_t cost = strips * (d.m + 1);
-        keys.push_back(uint32_t(std::min<int64_t>(cost, 0xffffffffLL)));
-        idx.push_back(int32_t(k));
     }
+    if (first_bad < N)
+        return fail(ctx, GBA_EINVAL, "negative, decreasing or too long offsets at pair %lld", (long long)first_bad);
+    plan->cells = cells;
+    trace_off = ctr[nth];
     plan->trace_total = trace_off;
+    timer.mark("pairs");
     plan->bucket_start.clear();
     plan->bucket_count.clear();
     if (p->flags & GBA_FLAG_PLAIN_BUCKETS) {
@@ -514,7 +667,9 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // words (4 residues per word, both pairs' codes per byte) and the boundary row are
     // interleaved by lane.
     sort_desc(keys16, idx16);
+    timer.mark("sort");
     std::vector<Slot16> slots16((idx16.size() + 1) / 2);
+#pragma omp parallel for num_threads(plan_threads(int64_t(slots16.size()))) schedule(static)
     for (size_t q = 0; q < slots16.size(); ++q) {
         Slot16 &sl = slots16[q];
         sl.pa = idx16[2 * q];
@@ -530,19 +685,25 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     const int64_t warps16 = (plan->num16 + 31) / 32;
     std::vector<int64_t> wcodes(std::max<int64_t>(warps16, 1)), wbnd(std::max<int64_t>(warps16, 1));
     std::vector<int32_t> whw(std::max<int64_t>(warps16, 1));
-    int64_t ctot = 0, btot = 0;
+    std::vector<int32_t> wmaxm(std::max<int64_t>(warps16, 1)), wmaxn(std::max<int64_t>(warps16, 1));
+#pragma omp parallel for num_threads(plan_threads(warps16 * 32)) schedule(static)
     for (int64_t w = 0; w < warps16; ++w) {
         int maxm = 0, maxn = 0;
         for (int64_t q = w * 32; q < std::min(plan->num16, (w + 1) * 32); ++q) {
             maxm = std::max(maxm, slots16[q].m);
             maxn = std::max(maxn, slots16[q].n);
         }
-        const int hw = (maxm + 3) / 4, vw = (maxn + 3) / 4;
+        wmaxm[w] = maxm;
+        wmaxn[w] = maxn;
+    }
+    int64_t ctot = 0, btot = 0;
+    for (int64_t w = 0; w < warps16; ++w) {
+        const int hw = (wmaxm[w] + 3) / 4, vw = (wmaxn[w] + 3) / 4;
         wcodes[w] = ctot;
         whw[w] = hw;
         ctot += int64_t(hw + vw) * 32;
         wbnd[w] = btot;
-        btot += int64_t(maxm + 1) * 32;
+        btot += int64_t(wmaxm[w] + 1) * 32;
     }
     plan->codes_total = ctot;
     plan->bnd16_total = btot;
@@ -556,7 +717,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     std::vector<int64_t> rboff, bbase;
     std::vector<int2> wtasks;
     int64_t rbtot = 0, nstates = 0;
-    if (plan->use_warp) {
+    if (plan->use_warp && !idx.empty()) {
         plan->grid_warp = persistent_grid(ctx, warp_fn(plan->affine, plan->local, plan->matrix, plan->traceback));
         const bool few_pairs = int64_t(idx.size()) < 2 * plan->grid_warp * (kBlock / 32);
         rboff.assign(N + 1, 0);
@@ -582,7 +743,8 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->num_warp_tasks = int64_t(wtasks.size());
     plan->num_band_states = nstates;
     // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
-    const int64_t warps = plan->use_warp ? 0 : (plan->num_slots + 31) / 32;
+    // (only the one-pair-per-thread strip kernel uses these boundary rows)
+    const int64_t warps = (plan->use_warp || p->band_on) ? 0 : (plan->num_slots + 31) / 32;
     std::vector<int64_t> wscr(std::max<int64_t>(warps, 1));
     int64_t scr = 0;
     for (int64_t w = 0; w < warps; ++w) {
@@ -595,7 +757,9 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->scratch_total = scr;
 
     // Segment / CIGAR slots: at most m + n + 4 records per pair.
-    std::vector<int64_t> seg_off(N + 1, 0), cig_off;
+    std::vector<int64_t> seg_off(plan->traceback ? N + 1 : 0, 0), cig_off;
+    plan->seg_slots_total = 0;
+    plan->cigar_slots_total = 0;
     if (plan->traceback) {
         for (int64_t k = 0; k < N; ++k) {
             const int64_t cap = plan->status[k] == GBA_PAIR_INVALID ? 0 : int64_t(desc[k].m) + desc[k].n + 4;
@@ -619,6 +783,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         return fail(ctx, GBA_EBUDGET, "batch needs %lld bytes of HBM, budget is %lld", (long long)need,
                     (long long)ctx->budget);
 
+    timer.mark("layout");
     if ((rc = upload(ctx, plan->pairs, desc))) return rc;
     if ((rc = upload(ctx, plan->order, idx))) return rc;
     if ((rc = upload(ctx, plan->warp_scratch, wscr))) return rc;
@@ -691,6 +856,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     }
     plan->seg_dense_total = -1;
     plan->cig_dense_total = -1;
+    timer.mark("upload+alloc");
     return GBA_OK;
 }
 
@@ -1248,6 +1414,18 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
     GBA_CUDA(ctx, cudaSetDevice(ctx->device));
     gba_plan *plan = &ctx->oneshot;
     const auto t0 = std::chrono::steady_clock::now();
+    // Inputs: the concatenated codes as given.  Their copies are issued before planning so the
+    // transfer overlaps the host work.
+    if (batch && batch->num_pairs > 0 && batch->off_h && batch->off_v && batch->seq_h && batch->seq_v) {
+        const int64_t N0 = batch->num_pairs;
+        const int64_t hb = batch->h_shared ? batch->off_h[1] : batch->off_h[N0];
+        const int64_t vb = batch->off_v[N0];
+        if (hb < 0 || vb < 0) return fail(ctx, GBA_EINVAL, "negative sequence length");
+        GBA_CUDA(ctx, ctx->seq_h.ensure(size_t(hb) + 16));
+        GBA_CUDA(ctx, ctx->seq_v.ensure(size_t(vb) + 16));
+        if (hb) GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_h.ptr, batch->seq_h, hb, cudaMemcpyHostToDevice, ctx->stream));
+        if (vb) GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_v.ptr, batch->seq_v, vb, cudaMemcpyHostToDevice, ctx->stream));
+    }
     int rc = build_plan(ctx, params, batch, plan);
     if (rc) return rc;
     const float plan_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1257,15 +1435,6 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
         if (plan->cigar && result->cigar_offsets) result->cigar_offsets[0] = 0;
         return GBA_OK;
     }
-    // Inputs: the concatenated codes as given.
-    GBA_CUDA(ctx, ctx->seq_h.ensure(size_t(plan->seq_h_bytes) + 16));
-    GBA_CUDA(ctx, ctx->seq_v.ensure(size_t(plan->seq_v_bytes) + 16));
-    if (plan->seq_h_bytes)
-        GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_h.ptr, batch->seq_h, plan->seq_h_bytes, cudaMemcpyHostToDevice,
-                                      ctx->stream));
-    if (plan->seq_v_bytes)
-        GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_v.ptr, batch->seq_v, plan->seq_v_bytes, cudaMemcpyHostToDevice,
-                                      ctx->stream));
     GBA_CUDA(ctx, ctx->out_score.ensure(size_t(N) * 4));
     // A one-shot batch is planned anew on every call, so a captured graph would never be
     // replayed: launch directly.
