@@ -60,26 +60,41 @@ struct WarpArgs {
     int32_t alphabet;
 };
 
-// Trace bytes of one pair in the warp layout: row 0 (m + 1 bytes, padded), then for each band
-// (m + 32) steps x 32 lanes x R bytes.
-__host__ __device__ inline int64_t warp_trace_bytes(int m, int n, int R)
+// Bands are 32 lanes x R rows (R = 8: 256 rows), except that a pair's last band holding at most
+// half that many rows runs with R / 2 rows per lane: its idle rows would otherwise cost as much
+// as busy ones.  Rows per lane of the last band of an n-row pair:
+__host__ __device__ inline int warp_last_rows(int n, int R)
 {
-    const int64_t band_rows = 32 * R;
-    const int64_t bands = (n + band_rows - 1) / band_rows;
-    return align16(m + 1) + bands * int64_t(m + 32) * 32 * R;
+    const int rem = n - ((n - 1) / (32 * R)) * (32 * R);
+    return rem <= 16 * R ? R / 2 : R;
 }
 
-__device__ __forceinline__ uint8_t trace_at_warp(const uint8_t *base, int m, int R, int col, int row)
+// Trace bytes of one pair in the warp layout: row 0 (m + 1 bytes, padded), then for each band
+// (m + 32) steps x 32 lanes x (its rows per lane) bytes.
+__host__ __device__ inline int64_t warp_trace_bytes(int m, int n, int R)
+{
+    if (n <= 0) return align16(m + 1);
+    const int64_t bands = (n + 32 * R - 1) / (32 * R);
+    return align16(m + 1) + ((bands - 1) * R + warp_last_rows(n, R)) * int64_t(m + 32) * 32;
+}
+
+// Byte offset of band b's trace within the pair's trace, and its rows per lane.
+__host__ __device__ inline int64_t warp_band_trace_off(int m, int b, int R)
+{
+    return align16(m + 1) + int64_t(b) * (m + 32) * 32 * R;
+}
+
+__device__ __forceinline__ uint8_t trace_at_warp(const uint8_t *base, int m, int n, int R, int col, int row)
 {
     if (row == 0) return base[col];
     const int r0 = row - 1;
-    const int band_rows = 32 * R;
-    const int b = r0 / band_rows;
-    const int within = r0 - b * band_rows;
-    const int lane = within / R;
-    const int r = within - lane * R;
+    const int b = r0 / (32 * R);
+    const int Rb = (b == (n - 1) / (32 * R)) ? warp_last_rows(n, R) : R;
+    const int within = r0 - b * 32 * R;
+    const int lane = within / Rb;
+    const int r = within - lane * Rb;
     const int t = col + lane;
-    return base[align16(m + 1) + ((int64_t(b) * (m + 32) + t) * 32 + lane) * R + r];
+    return base[warp_band_trace_off(m, b, R) + (int64_t(t) * 32 + lane) * Rb + r];
 }
 
 struct WarpBest {
@@ -155,7 +170,8 @@ __device__ __forceinline__ void warp_wait_at_least(const int *p, int need, int32
 
 constexpr int kRowChunk = 32;   // columns per row-buffer hand-off between bands
 
-template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int R>
+// One band of pair p with R rows per lane; RF is the rows per lane of the pair's full bands.
+template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int RF, int R>
 __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, int b, int lane, bool seq,
                           WarpBest &carry)
 {
@@ -170,9 +186,8 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
     const bool fRight = fe & FREE_RIGHT, fBottom = fe & FREE_BOTTOM;
     const int OPEN = AFFINE ? a.gap_open : a.gap_extend;
     const int EXT = a.gap_extend;
-    const int band_rows = 32 * R;
+    const int band_rows = 32 * RF;
     const int bands = (n + band_rows - 1) / band_rows;
-    const int64_t row0Bytes = align16(m + 1);
 
     WarpBest best{INF, INF, INF, 0, 0};
     if (LOCAL && lane == 0 && b == 0) best.offer(0, INF, INF, 0, 0);
@@ -194,8 +209,9 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
 
     {
         const int i0 = b * band_rows + lane * R + 1;      // first row of this lane's strip
-        const bool active = i0 <= n;
-        const bool lastStrip = i0 + R > n;                // the strip holds row n (or lies below it)
+        const int rvalid = n - i0 + 1;                     // rows of this strip inside the matrix
+        const int rowN = (rvalid >= 1 && rvalid <= R) ? rvalid - 1 : -1;   // row n, if here
+        const bool trackRowN = !LOCAL && fBottom && rowN >= 0;
         uint8_t vc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) vc[r] = (i0 + r <= n) ? V[i0 + r - 1] : 0;
@@ -205,129 +221,19 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
         int s0 = 0, e0 = INF;            // row 0 (lane 0, band 0): S(0, j - 1), E(0, j - 1)
         int outS = INF, outF = INF;      // this lane's hand-off from the previous step
         int diagNext = INF;
-        uint8_t *Tband = TRACE ? T + row0Bytes + int64_t(b) * (m + 32) * 32 * R + int64_t(lane) * R : nullptr;
+        int hnext = H[0];
+        uint8_t *Tband = TRACE ? T + warp_band_trace_off(m, b, RF) + int64_t(lane) * R : nullptr;
+        // One loop body for every step.  Lane l holds column j = t - l; lanes with j outside
+        // [0, m] (the fill and drain of the front) compute values nothing reads: their trace
+        // bytes lie at steps the traceback never visits, their hand-off reaches only lanes that
+        // are idle too, and they offer no best cell.  Column 0 and column m take short branches.
+        // The recurrences run on max / add-max / 3-way max, which equal the reference's
+        // compare-and-select values, ties included; the trace bits come from comparisons of the
+        // chain's own values, off the dependency chain down the column.
         for (int t = 0; t <= m + 31; ++t) {
-            if (t == 32 && m - 1 >= 32) {
-                // Steady phase, steps 32 .. m - 1: every lane's column lies in [1, m - 1], so
-                // there is no column 0, no last column and no idle lane; lane 0's input is a
-                // select.  The recurrences run on max / add-max / 3-way max (the values equal the
-                // compare-and-select form of the other steps, ties included), and the trace bits
-                // come from comparisons off the dependency chain down the column.  Each lane
-                // meets its cells in column-major order.
-                const int rvalid = n - i0 + 1;             // rows of this strip inside the matrix
-                const int rowN = (rvalid >= 1 && rvalid <= R) ? rvalid - 1 : -1;   // row n, if here
-                const bool trackRowN = !LOCAL && fBottom && rowN >= 0;
-                int hnext = H[31 - lane];                  // H code of this lane's column at step 32
-                for (; t <= m - 1; ++t) {
-                    const int j = t - lane;
-                    if (b > 0 && (t & (kRowChunk - 1)) == 0) {
-                        __syncwarp();
-                        rb[lane] = pre;
-                        __syncwarp();
-                        if (t + kRowChunk <= m) fetch(t + kRowChunk);
-                    }
-                    const int inS = __shfl_up_sync(0xffffffffu, outS, 1);
-                    const int inF = __shfl_up_sync(0xffffffffu, outF, 1);
-                    const int hc = hnext;
-                    hnext = H[j];                          // column j + 1 at the next step
-                    int2 bb;
-                    if (b == 0) {
-                        // Row 0, column j (lane 0's; the other lanes' copies go unused).
-                        uint8_t tv0 = TV_NONE;
-                        if (!fTop) {
-                            if (AFFINE) {
-                                const int ex = e0 + EXT, op = s0 + OPEN;
-                                tv0 = ex < op ? (TV_HO | TV_MFH) : (TV_H | TV_MFH);
-                                e0 = max(ex, op);
-                                s0 = e0;
-                            } else {
-                                s0 = s0 + EXT;
-                                tv0 = TV_H | TV_MFH;
-                            }
-                        }
-                        if (TRACE && lane == 0) T[j] = tv0;
-                        bb = make_int2(s0, INF);
-                    } else {
-                        bb = rb[j & (kRowChunk - 1)];
-                    }
-                    int sUp = lane ? inS : bb.x;
-                    int fUp = lane ? inF : bb.y;
-                    int diag = diagNext;
-                    diagNext = sUp;
-                    const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
-                    uint32_t tw[R / 4];
-                    int Fp[R];                             // F of each row (for the best cell)
-#pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const int sub = MATRIX ? smat[hrow | (vc[r] & 31)] : (hc == vc[r] ? a.match : a.mismatch);
-                        const int inter = diag + sub;
-                        diag = Sp[r];
-                        int s, e = Ep[r], f = fUp;
-                        uint32_t tv = 0;
-                        if (AFFINE) {
-                            const int eExt = Ep[r] + EXT, eOpn = Sp[r] + OPEN;
-                            e = max(eExt, eOpn);
-                            const int fExt = fUp + EXT;
-                            f = __viaddmax_s32(sUp, OPEN, fExt);
-                            s = LOCAL ? __vimax3_s32_relu(inter, e, f) : __vimax3_s32(inter, e, f);
-                            if (TRACE) {
-                                // s == inter: the diagonal wins (ties included); e != eExt: the
-                                // gap opened (eExt < eOpn); f != fExt: likewise for F.  With the
-                                // local zero floor, s == 0 overrides everything below.
-                                tv = s == inter ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
-                                tv |= e != eExt ? TV_HO : TV_H;
-                                tv |= f != fExt ? TV_VO : TV_V;
-                            }
-                        } else {
-                            const int gv = sUp + EXT, gh = Sp[r] + EXT;
-                            s = LOCAL ? __vimax3_s32_relu(inter, gv, gh) : __vimax3_s32(inter, gv, gh);
-                            if (TRACE)
-                                tv = s == inter ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
-                        }
-                        if (TRACE && LOCAL && s == 0) tv = TV_NONE;
-                        Sp[r] = s;
-                        Ep[r] = e;
-                        Fp[r] = f;
-                        sUp = s;
-                        fUp = f;
-                        if (TRACE) {
-                            if ((r & 3) == 0) tw[r >> 2] = 0;
-                            tw[r >> 2] |= tv << (8 * (r & 3));
-                        }
-                    }
-                    if (LOCAL) {
-                        // Column j's best row of this strip: the first row holding the strip's
-                        // maximum, taken only when it beats every earlier column.
-                        if (rvalid >= R) {
-                            const int mx = strip_max<R>(Sp);
-                            if (mx > best.s) {
-#pragma unroll
-                                for (int r = 0; r < R; ++r)
-                                    if (Sp[r] == mx) {
-                                        best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
-                                        break;
-                                    }
-                            }
-                        } else {
-#pragma unroll
-                            for (int r = 0; r < R; ++r)
-                                if (r < rvalid) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
-                        }
-                    } else if (trackRowN) {
-#pragma unroll
-                        for (int r = 0; r < R; ++r)
-                            if (r == rowN) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
-                    }
-                    if (TRACE) store_trace<R>(Tband + int64_t(t) * 32 * R, tw);
-                    outS = sUp;
-                    outF = fUp;
-                    if (lane == 31 && b + 1 < bands) {
-                        rowOut[j] = make_int2(sUp, fUp);
-                        if (!seq && (j & (kRowChunk - 1)) == kRowChunk - 1) st_release_gpu(&st->progress, j + 1);
-                    }
-                }
-            }
             const int j = t - lane;
+            // Fill and drain steps (some lane outside [1, m - 1]); the same for the whole warp.
+            const bool edge = t < 32 || t >= m;
             if (b > 0 && (t & (kRowChunk - 1)) == 0 && t <= m) {
                 // Stage chunk t of the band above, then prefetch chunk t + 32.
                 __syncwarp();
@@ -337,42 +243,37 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
             }
             const int inS = __shfl_up_sync(0xffffffffu, outS, 1);
             const int inF = __shfl_up_sync(0xffffffffu, outF, 1);
-            if (j < 0 || j > m) continue;
-            // S and F of the row above this strip, column j.
-            int upS, upF;
-            if (lane > 0) {
-                upS = inS;
-                upF = inF;
-            } else if (b > 0) {
-                const int2 bb = rb[j & (kRowChunk - 1)];
-                upS = bb.x;
-                upF = bb.y;
-            } else {
-                // Row 0 cell (0, j): Zero at (0, 0) and with a free first row, else Horizontal.
+            const int hc = hnext;
+            hnext = H[edge ? min(max(j, 0), m - 1) : j];      // column j + 1 at the next step
+            // S and F of the row above this strip, column j (lane 0: row 0 or the band above).
+            int2 bb;
+            if (b == 0) {
+                // Row 0: Zero at (0, 0) and with a free first row, else Horizontal.  Lane 0's
+                // values; the other lanes' copies go unused.
                 uint8_t tv0 = TV_NONE;
-                if (j > 0 && !fTop) {
+                if (t >= 1 && !fTop) {
                     if (AFFINE) {
                         const int ex = e0 + EXT, op = s0 + OPEN;
-                        if (ex < op) { e0 = op; tv0 = TV_HO | TV_MFH; } else { e0 = ex; tv0 = TV_H | TV_MFH; }
+                        tv0 = ex < op ? (TV_HO | TV_MFH) : (TV_H | TV_MFH);
+                        e0 = max(ex, op);
                         s0 = e0;
                     } else {
                         s0 = s0 + EXT;
                         tv0 = TV_H | TV_MFH;
                     }
                 }
-                if (TRACE) T[j] = tv0;
-                if (j > 0 && (LOCAL || (j == m && fRight))) best.offer(s0, fTop ? INF : e0, INF, j, 0);
-                upS = s0;
-                upF = INF;
+                if (lane == 0 && t <= m) {
+                    if (TRACE) T[t] = tv0;
+                    if (!LOCAL && t == m && fRight && t > 0) best.offer_later(s0, fTop ? INF : e0, INF, t, 0);
+                }
+                bb = make_int2(s0, INF);
+            } else {
+                bb = rb[j & (kRowChunk - 1)];
             }
-            if (!active) {
-                outS = INF;
-                outF = INF;
-                continue;
-            }
+            int sUp = lane ? inS : bb.x;
+            int fUp = lane ? inF : bb.y;
             uint32_t tw[R / 4];
-            int sUp = upS, fUp = upF;
-            if (j == 0) {
+            if (edge && j == 0) {
                 // Column 0: Vertical, or Zero with a free first column.
                 diagNext = sUp;
 #pragma unroll
@@ -401,54 +302,84 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
                     if (i <= n && (LOCAL || (i == n && fBottom))) best.offer(s, INF, f, 0, i);
                 }
             } else {
-                const int hc = H[j - 1];
                 int diag = diagNext;
                 diagNext = sUp;
-                const bool trackCol = LOCAL || (j == m && fRight);
+                const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
+                int Fp[R];                                 // F of each row (for the best cell)
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    const int sub = MATRIX ? smat[((hc & 31) << 5) | (vc[r] & 31)] : (hc == vc[r] ? a.match : a.mismatch);
+                    const int sub = MATRIX ? smat[hrow | (vc[r] & 31)] : (hc == vc[r] ? a.match : a.mismatch);
                     const int inter = diag + sub;
                     diag = Sp[r];
                     int s, e = Ep[r], f = fUp;
-                    uint8_t tv;
+                    uint32_t tv = 0;
                     if (AFFINE) {
-                        uint8_t tvE, tvF, tm;
                         const int eExt = Ep[r] + EXT, eOpn = Sp[r] + OPEN;
-                        if (eExt < eOpn) { e = eOpn; tvE = TV_HO; } else { e = eExt; tvE = TV_H; }
-                        const int fExt = fUp + EXT, fOpn = sUp + OPEN;
-                        if (fExt < fOpn) { f = fOpn; tvF = TV_VO; } else { f = fExt; tvF = TV_V; }
-                        int g;
-                        if (f < e) { g = e; tm = TV_MFH; } else { g = f; tm = TV_MFV; }
-                        if (inter < g) { s = g; tv = tm | tvE | tvF; } else { s = inter; tv = TV_DIAG | tvE | tvF; }
+                        e = max(eExt, eOpn);
+                        const int fExt = fUp + EXT;
+                        f = __viaddmax_s32(sUp, OPEN, fExt);
+                        s = LOCAL ? __vimax3_s32_relu(inter, e, f) : __vimax3_s32(inter, e, f);
+                        if (TRACE) {
+                            // s == inter: the diagonal wins (ties included); e != eExt: the gap
+                            // opened (eExt < eOpn); f != fExt: likewise for F.  With the local
+                            // zero floor, s == 0 overrides everything below.
+                            tv = s == inter ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
+                            tv |= e != eExt ? TV_HO : TV_H;
+                            tv |= f != fExt ? TV_VO : TV_V;
+                        }
                     } else {
                         const int gv = sUp + EXT, gh = Sp[r] + EXT;
-                        int g;
-                        uint8_t tg;
-                        if (gv < gh) { g = gh; tg = TV_H | TV_MFH; } else { g = gv; tg = TV_V | TV_MFV; }
-                        if (inter < g) { s = g; tv = tg; } else { s = inter; tv = TV_DIAG; }
+                        s = LOCAL ? __vimax3_s32_relu(inter, gv, gh) : __vimax3_s32(inter, gv, gh);
+                        if (TRACE)
+                            tv = s == inter ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
                     }
-                    if (LOCAL) {
-                        if (s <= 0) { s = 0; tv = TV_NONE; }
-                    }
+                    if (TRACE && LOCAL && s == 0) tv = TV_NONE;
                     Sp[r] = s;
                     Ep[r] = e;
+                    Fp[r] = f;
                     sUp = s;
                     fUp = f;
                     if (TRACE) {
                         if ((r & 3) == 0) tw[r >> 2] = 0;
-                        tw[r >> 2] |= uint32_t(tv) << (8 * (r & 3));
+                        tw[r >> 2] |= tv << (8 * (r & 3));
                     }
-                    if (!lastStrip || i0 + r <= n) {
-                        if (trackCol || (lastStrip && i0 + r == n && (j == m || fBottom)))
-                            best.offer(s, e, f, j, i0 + r);
+                }
+                // Best cells of column j (1 <= j <= m) in column-major order.
+                if (!edge || (j >= 1 && j <= m)) {
+                    if (LOCAL) {
+                        // The first row holding the strip's maximum, taken only when it beats
+                        // every earlier column.
+                        if (rvalid >= R) {
+                            const int mx = strip_max<R>(Sp);
+                            if (mx > best.s) {
+#pragma unroll
+                                for (int r = 0; r < R; ++r)
+                                    if (Sp[r] == mx) {
+                                        best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                                        break;
+                                    }
+                            }
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r < rvalid) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                        }
+                    } else if (edge && j == m && (fRight || rowN >= 0)) {
+                        // Last column: every row with a free last column, else row n only.
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r < rvalid && (fRight || r == rowN)) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                    } else if (trackRowN) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == rowN) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
                     }
                 }
             }
             if (TRACE) store_trace<R>(Tband + int64_t(t) * 32 * R, tw);
             outS = sUp;
             outF = fUp;
-            if (lane == 31 && b + 1 < bands) {
+            if (lane == 31 && b + 1 < bands && (!edge || (j >= 0 && j <= m))) {
                 rowOut[j] = make_int2(sUp, fUp);
                 if (!seq && ((j & (kRowChunk - 1)) == kRowChunk - 1 || j == m)) st_release_gpu(&st->progress, j + 1);
             }
@@ -502,6 +433,7 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
 
 template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int R>
 __global__ void __launch_bounds__(128, 4) k_dp_warp(WarpArgs a)
+// R: rows per lane of full bands; a short last band runs with R / 2.
 {
     extern __shared__ int smat[];
     if (MATRIX) {
@@ -521,16 +453,22 @@ __global__ void __launch_bounds__(128, 4) k_dp_warp(WarpArgs a)
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= a.num_tasks) break;
         const int2 pb = a.tasks[task];
-        WarpBest carry{0, 0, 0, 0, 0};
+        const PairDesc d = a.pairs[pb.x];
+        const int bands = (d.n + 32 * R - 1) / (32 * R);
+        const bool halfLast = warp_last_rows(d.n, R) < R;
+        WarpBest carry{d.inf, d.inf, d.inf, 0, 0};
+        auto run = [&](int b, bool seq) {
+            if (halfLast && b == bands - 1)
+                warp_band<AFFINE, LOCAL, MATRIX, TRACE, R, R / 2>(a, smat, rb, pb.x, b, lane, seq, carry);
+            else
+                warp_band<AFFINE, LOCAL, MATRIX, TRACE, R, R>(a, smat, rb, pb.x, b, lane, seq, carry);
+        };
         if (pb.y >= 0) {
-            warp_band<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, rb, pb.x, pb.y, lane, false, carry);
+            run(pb.y, false);
         } else {
             // Band -1: this warp runs every band of the pair in order (no waits between bands).
-            const PairDesc d = a.pairs[pb.x];
-            const int bands = (d.n + 32 * R - 1) / (32 * R);
-            carry = WarpBest{d.inf, d.inf, d.inf, 0, 0};
             for (int b = 0; b < bands; ++b) {
-                warp_band<AFFINE, LOCAL, MATRIX, TRACE, R>(a, smat, rb, pb.x, b, lane, true, carry);
+                run(b, true);
                 __syncwarp();
             }
         }

@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     const uint8_t *T = a.trace + d.trace_off;
     const int bw = a.band_w, bu = a.band_upper, wr = a.warp_rows;
     auto TAT = [&](int c, int r) -> int {
-        if (wr) return int(trace_at_warp(T, m, wr, c, r));
+        if (wr) return int(trace_at_warp(T, m, d.n, wr, c, r));
         return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
     };
     traceback_pair(a, p, TAT, true);
@@ -185,13 +185,13 @@ constexpr int kTraceTileSteps = 64;             // steps of one band held in sha
 constexpr int64_t kTiledTraceCells = 1 << 20;   // pairs at least this large are walked by a warp
 
 // Trace reader of the warp layout (dp_warp_kernels.cuh) through a shared-memory tile: steps
-// [t0, t0 + kTraceTileSteps) of band tb, each step 32 * R bytes.  Called by all 32 lanes with
-// the same cell; a miss reloads the tile ending at the requested step (the walk only moves to
-// earlier steps).
+// [t0, t0 + kTraceTileSteps) of band tb, each step 32 * Rb bytes (Rb: the band's rows per lane,
+// R or, for a short last band, R / 2).  Called by all 32 lanes with the same cell; a miss
+// reloads the tile ending at the requested step (the walk only moves to earlier steps).
 template <int R>
 struct TileCell {
     const uint8_t *T;
-    int m;
+    int m, n;
     uint4 *tile;
     int tb, t0;
     __device__ __forceinline__ int operator()(int col, int row)
@@ -199,21 +199,21 @@ struct TileCell {
         if (row == 0) return T[col];
         const int r0 = row - 1;
         const int b = r0 / (32 * R);
+        const int Rb = (b == (n - 1) / (32 * R)) ? warp_last_rows(n, R) : R;
         const int within = r0 - b * 32 * R;
-        const int ln = within / R;
+        const int ln = within / Rb;
         const int t = col + ln;
         if (b != tb || t < t0 || t >= t0 + kTraceTileSteps) {
             tb = b;
             t0 = max(0, t - kTraceTileSteps + 1);
             const int steps = min(kTraceTileSteps, m + 32 - t0);
-            const uint4 *src =
-                reinterpret_cast<const uint4 *>(T + align16(m + 1) + (int64_t(b) * (m + 32) + t0) * 32 * R);
+            const uint4 *src = reinterpret_cast<const uint4 *>(T + warp_band_trace_off(m, b, R) + int64_t(t0) * 32 * Rb);
             const int lane = threadIdx.x & 31;
             __syncwarp();
-            for (int q = lane; q < steps * 2 * R; q += 32) tile[q] = __ldcs(src + q);
+            for (int q = lane; q < steps * 2 * Rb; q += 32) tile[q] = __ldcs(src + q);
             __syncwarp();
         }
-        return reinterpret_cast<const uint8_t *>(tile)[(t - t0) * 32 * R + within];
+        return reinterpret_cast<const uint8_t *>(tile)[(t - t0) * 32 * Rb + within];
     }
 };
 
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(64) k_traceback_tiled(TraceArgs a)
     const int p = a.order[slot];
     if (p < 0) return;
     const PairDesc d = a.pairs[p];
-    TileCell<R> cell{a.trace + d.trace_off, d.m, tiles[threadIdx.x >> 5], -1, 0};
+    TileCell<R> cell{a.trace + d.trace_off, d.m, d.n, tiles[threadIdx.x >> 5], -1, 0};
     traceback_pair(a, p, cell, (threadIdx.x & 31) == 0);
 }
 
