@@ -230,7 +230,133 @@ __device__ void warp_band(const WarpArgs &a, const int *smat, int2 *rb, int p, i
         // The recurrences run on max / add-max / 3-way max, which equal the reference's
         // compare-and-select values, ties included; the trace bits come from comparisons of the
         // chain's own values, off the dependency chain down the column.
+        // Full-height bands also get a lean copy of the cell code for the steady steps (all
+        // lanes in columns 1 .. m - 1: no edge tests, shorter per-step latency), except the
+        // matrix-scored traceback variant, whose code with that copy no longer fits the
+        // instruction cache next to the short band's (measured 5% slower).
+        constexpr bool kLeanSteady = R == RF && !(MATRIX && TRACE);
         for (int t = 0; t <= m + 31; ++t) {
+            if (kLeanSteady && t == 32 && m - 1 >= 32) {
+                // Steady phase, steps 32 .. m - 1: every lane's column lies in [1, m - 1], so
+                // there is no column 0, no last column and no idle lane; lane 0's input is a
+                // select.  The recurrences run on max / add-max / 3-way max (the values equal the
+                // compare-and-select form of the other steps, ties included), and the trace bits
+                // come from comparisons off the dependency chain down the column.  Each lane
+                // meets its cells in column-major order.
+                const int rvalid = n - i0 + 1;             // rows of this strip inside the matrix
+                const int rowN = (rvalid >= 1 && rvalid <= R) ? rvalid - 1 : -1;   // row n, if here
+                const bool trackRowN = !LOCAL && fBottom && rowN >= 0;
+                // hnext already holds H[31 - lane], this lane's column at step 32; the steady
+                // loop leaves in it the code the drain steps start from.
+                for (; t <= m - 1; ++t) {
+                    const int j = t - lane;
+                    if (b > 0 && (t & (kRowChunk - 1)) == 0) {
+                        __syncwarp();
+                        rb[lane] = pre;
+                        __syncwarp();
+                        if (t + kRowChunk <= m) fetch(t + kRowChunk);
+                    }
+                    const int inS = __shfl_up_sync(0xffffffffu, outS, 1);
+                    const int inF = __shfl_up_sync(0xffffffffu, outF, 1);
+                    const int hc = hnext;
+                    hnext = H[j];                          // column j + 1 at the next step
+                    int2 bb;
+                    if (b == 0) {
+                        // Row 0, column j (lane 0's; the other lanes' copies go unused).
+                        uint8_t tv0 = TV_NONE;
+                        if (!fTop) {
+                            if (AFFINE) {
+                                const int ex = e0 + EXT, op = s0 + OPEN;
+                                tv0 = ex < op ? (TV_HO | TV_MFH) : (TV_H | TV_MFH);
+                                e0 = max(ex, op);
+                                s0 = e0;
+                            } else {
+                                s0 = s0 + EXT;
+                                tv0 = TV_H | TV_MFH;
+                            }
+                        }
+                        if (TRACE && lane == 0) T[j] = tv0;
+                        bb = make_int2(s0, INF);
+                    } else {
+                        bb = rb[j & (kRowChunk - 1)];
+                    }
+                    int sUp = lane ? inS : bb.x;
+                    int fUp = lane ? inF : bb.y;
+                    int diag = diagNext;
+                    diagNext = sUp;
+                    const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
+                    uint32_t tw[R / 4];
+                    int Fp[R];                             // F of each row (for the best cell)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const int sub = MATRIX ? smat[hrow | (vc[r] & 31)] : (hc == vc[r] ? a.match : a.mismatch);
+                        const int inter = diag + sub;
+                        diag = Sp[r];
+                        int s, e = Ep[r], f = fUp;
+                        uint32_t tv = 0;
+                        if (AFFINE) {
+                            const int eExt = Ep[r] + EXT, eOpn = Sp[r] + OPEN;
+                            e = max(eExt, eOpn);
+                            const int fExt = fUp + EXT;
+                            f = __viaddmax_s32(sUp, OPEN, fExt);
+                            s = LOCAL ? __vimax3_s32_relu(inter, e, f) : __vimax3_s32(inter, e, f);
+                            if (TRACE) {
+                                // s == inter: the diagonal wins (ties included); e != eExt: the
+                                // gap opened (eExt < eOpn); f != fExt: likewise for F.  With the
+                                // local zero floor, s == 0 overrides everything below.
+                                tv = s == inter ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
+                                tv |= e != eExt ? TV_HO : TV_H;
+                                tv |= f != fExt ? TV_VO : TV_V;
+                            }
+                        } else {
+                            const int gv = sUp + EXT, gh = Sp[r] + EXT;
+                            s = LOCAL ? __vimax3_s32_relu(inter, gv, gh) : __vimax3_s32(inter, gv, gh);
+                            if (TRACE)
+                                tv = s == inter ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
+                        }
+                        if (TRACE && LOCAL && s == 0) tv = TV_NONE;
+                        Sp[r] = s;
+                        Ep[r] = e;
+                        Fp[r] = f;
+                        sUp = s;
+                        fUp = f;
+                        if (TRACE) {
+                            if ((r & 3) == 0) tw[r >> 2] = 0;
+                            tw[r >> 2] |= tv << (8 * (r & 3));
+                        }
+                    }
+                    if (LOCAL) {
+                        // Column j's best row of this strip: the first row holding the strip's
+                        // maximum, taken only when it beats every earlier column.
+                        if (rvalid >= R) {
+                            const int mx = strip_max<R>(Sp);
+                            if (mx > best.s) {
+#pragma unroll
+                                for (int r = 0; r < R; ++r)
+                                    if (Sp[r] == mx) {
+                                        best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                                        break;
+                                    }
+                            }
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (r < rvalid) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                        }
+                    } else if (trackRowN) {
+#pragma unroll
+                        for (int r = 0; r < R; ++r)
+                            if (r == rowN) best.offer_later(Sp[r], Ep[r], Fp[r], j, i0 + r);
+                    }
+                    if (TRACE) store_trace<R>(Tband + int64_t(t) * 32 * R, tw);
+                    outS = sUp;
+                    outF = fUp;
+                    if (lane == 31 && b + 1 < bands) {
+                        rowOut[j] = make_int2(sUp, fUp);
+                        if (!seq && (j & (kRowChunk - 1)) == kRowChunk - 1) st_release_gpu(&st->progress, j + 1);
+                    }
+                }
+            }
             const int j = t - lane;
             // Fill and drain steps (some lane outside [1, m - 1]); the same for the whole warp.
             const bool edge = t < 32 || t >= m;
