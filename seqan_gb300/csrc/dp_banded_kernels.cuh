@@ -11,8 +11,16 @@
 // diagonal unless the call site refreshes it).
 //
 // Band state: per thread, slot k = upper - col + row (one per diagonal) of S, E and the stored
-// F, in per-thread arrays (local memory, L1-resident).  Trace: one byte per band slot per
-// column (the reference's TraceBitMap_ bits).
+// F, in per-thread arrays (local memory).  Trace: one byte per band slot per column (the
+// reference's TraceBitMap_ bits), columns band_trace_stride(W) = W rounded up to 16 bytes
+// apart so a column can be written with 16-byte stores.
+//
+// Middle phase fast path: the columns whose track covers all W slots (first cell Upper, inner
+// cells All, last cell Lower, every cell tracked in local mode and none otherwise) are most of
+// a banded alignment.  For W <= kBandFastW they run with slots 0 .. W-2 in register arrays
+// (static indices), the last slot in scalars, a window of V codes packed four per register
+// and shifted one code per column, and the column's trace bytes packed into registers and
+// written with 16-byte stores; the per-cell rules are the generic cell()'s, ties included.
 #pragma once
 
 #include "dp_common.cuh"
@@ -34,6 +42,11 @@ struct BandArgs {
     int32_t lower, upper;
 };
 
+constexpr int kBandFastW = 40;   // widest band of the middle-phase fast path
+
+// Bytes between the trace columns of a band of W slots.
+__host__ __device__ inline int band_trace_stride(int W) { return (W + 15) & ~15; }
+
 enum { BCOL_INITIAL = 0, BCOL_INNER = 1, BCOL_FINAL = 2 };
 enum { BLOC_FULL = 0, BLOC_TOP = 1, BLOC_MIDDLE = 2, BLOC_BOTTOM = 3 };
 enum { BDIR_ZERO = 0, BDIR_ALL, BDIR_HORIZONTAL, BDIR_VERTICAL, BDIR_UPPER, BDIR_LOWER };
@@ -44,7 +57,7 @@ struct BandedPair {
     const int *smat;
     const uint8_t *H, *V;
     uint8_t *T;
-    int m, n, W, lower, upper, INF;
+    int m, n, W, Wt, lower, upper, INF;
     bool fTop, fLeft, fRight, fBottom;
     int OPEN, EXT;
     int S[WMAX], E[WMAX], Fs[WMAX];
@@ -173,7 +186,7 @@ struct BandedPair {
         if (inside) {
             S[k] = s;
             E[k] = e;
-            if (TRACE) T[int64_t(col) * W + k] = uint8_t(tv);
+            if (TRACE) T[int64_t(col) * Wt + k] = uint8_t(tv);
         }
         if (tracked) {
             if (inside) Fs[k] = f;
@@ -193,6 +206,158 @@ struct BandedPair {
         }
         if (set_f) Fs[k] = lastF;
         scout(S[k], E[k], Fs[k], col, row);
+    }
+
+    // Middle-phase columns hIt + 1 .. hMid with every track covering slots 0 .. W - 1 (first
+    // row in slot 0); advances hIt, vb and ve as the generic loop does.  Same per-cell rules as
+    // cell(): Upper for slot 0, All for slots 1 .. W - 2, Lower for slot W - 1.
+    __device__ void middle_fast(int &hIt, const int hMid, int &vb, int &ve)
+    {
+        constexpr int FW = kBandFastW;
+        constexpr int NW = FW / 4;                    // V window words (4 codes each)
+        constexpr int NT = ((FW + 15) / 16) * 4;      // trace words of one column
+        static_assert(FW % 4 == 0, "whole window words");
+        const int WL = W - 1;                         // register slots 0 .. W - 2
+        int Sr[FW], Er[FW];
+#pragma unroll
+        for (int k = 0; k < FW - 1; ++k)
+            if (k < WL) {
+                Sr[k] = S[k];
+                Er[k] = AFFINE ? E[k] : INF;
+            }
+        int sLast = S[WL], eLast = E[WL];
+        // V window of the next column: code k = V[first row - 1 + k] (0 past the end of V).
+        uint32_t vw[NW];
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            uint32_t w = 0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int idx = vb + 4 * q + c;
+                w |= uint32_t(idx < n ? V[idx] : 0) << (8 * c);
+            }
+            vw[q] = w;
+        }
+        for (; hIt != hMid; ++hIt) {
+            ++vb;
+            ++ve;
+            const int col = hIt + 1;
+            const int hc = H[col - 1];
+            const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
+            int dS = Sr[0];
+            int vS = INF, vF = INF;
+            uint32_t tw[NT];
+#pragma unroll
+            for (int q = 0; q < NT; ++q) tw[q] = 0;
+#pragma unroll
+            for (int k = 0; k < FW - 1; ++k) {
+                if (k >= WL) break;
+                const int vc = int((vw[k >> 2] >> (8 * (k & 3))) & 0xffu);
+                const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
+                const int inter = dS + sub;
+                const int hS = (k + 1 < WL) ? Sr[k + 1] : sLast;   // S(row, col - 1): slot k + 1
+                const int hE = (k + 1 < WL) ? Er[k + 1] : eLast;
+                dS = hS;
+                int s, e, f = INF;
+                uint32_t tv = 0;
+                if (k == 0) {
+                    // Upper: diagonal or horizontal.
+                    if (AFFINE) {
+                        const int eExt = hE + EXT, eOpn = hS + OPEN;
+                        e = max(eExt, eOpn);
+                        s = max(inter, e);
+                        tv = (eExt < eOpn ? TV_HO : TV_H) | (inter < e ? TV_MFH : TV_DIAG);
+                        vF = INF;
+                    } else {
+                        const int gh = hS + EXT;
+                        s = max(inter, gh);
+                        tv = inter < gh ? (TV_H | TV_MFH) : TV_DIAG;
+                        e = hE;
+                    }
+                } else {
+                    // All directions.
+                    if (AFFINE) {
+                        const int eExt = hE + EXT, eOpn = hS + OPEN;
+                        e = max(eExt, eOpn);
+                        const int fExt = vF + EXT, fOpn = vS + OPEN;
+                        f = max(fExt, fOpn);
+                        s = __vimax3_s32(inter, e, f);
+                        if (TRACE) {
+                            tv = (eExt < eOpn ? TV_HO : TV_H) | (fExt < fOpn ? TV_VO : TV_V);
+                            tv |= s == inter ? TV_DIAG : (f < e ? TV_MFH : TV_MFV);
+                        }
+                        vF = f;
+                    } else {
+                        const int gv = vS + EXT, gh = hS + EXT;
+                        s = __vimax3_s32(inter, gv, gh);
+                        if (TRACE) tv = s == inter ? TV_DIAG : (gv < gh ? (TV_H | TV_MFH) : (TV_V | TV_MFV));
+                        e = hE;
+                    }
+                }
+                if (LOCAL && s <= 0) {
+                    s = 0;
+                    tv = TV_NONE;
+                }
+                vS = s;
+                Sr[k] = s;
+                if (AFFINE) Er[k] = e;
+                if (TRACE) tw[k >> 2] |= tv << (8 * (k & 3));
+                if (LOCAL) {
+                    Fs[k] = f;
+                    scout(s, e, f, col, vb + k);
+                }
+            }
+            // Lower: diagonal or vertical (slot W - 1, row ve).
+            {
+                const int vc = V[ve - 1];
+                const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
+                const int inter = dS + sub;
+                int s, f = INF;
+                uint32_t tv;
+                if (AFFINE) {
+                    const int fExt = vF + EXT, fOpn = vS + OPEN;
+                    f = max(fExt, fOpn);
+                    s = max(inter, f);
+                    tv = (fExt < fOpn ? TV_VO : TV_V) | (inter < f ? TV_MFV : TV_DIAG);
+                } else {
+                    const int gv = vS + EXT;
+                    s = max(inter, gv);
+                    tv = inter < gv ? (TV_V | TV_MFV) : TV_DIAG;
+                }
+                if (LOCAL && s <= 0) {
+                    s = 0;
+                    tv = TV_NONE;
+                }
+                sLast = s;
+                eLast = INF;
+                lastF = f;
+                if (LOCAL) {
+                    Fs[WL] = f;
+                    scout(s, INF, f, col, ve);
+                }
+                if (TRACE) {
+                    uint8_t *Tc = T + int64_t(col) * Wt;
+#pragma unroll
+                    for (int q = 0; q < NT / 4; ++q)
+                        if (16 * q < W)
+                            reinterpret_cast<uint4 *>(Tc)[q] = make_uint4(tw[4 * q], tw[4 * q + 1], tw[4 * q + 2], tw[4 * q + 3]);
+                    Tc[WL] = uint8_t(tv);
+                }
+            }
+            // Shift the V window by one row: code k <- code k + 1, the new last code from V.
+#pragma unroll
+            for (int q = 0; q < NW - 1; ++q) vw[q] = __funnelshift_r(vw[q], vw[q + 1], 8);
+            const int idx = vb + FW - 1;
+            vw[NW - 1] = (vw[NW - 1] >> 8) | (uint32_t(idx < n ? V[idx] : 0) << 24);
+        }
+#pragma unroll
+        for (int k = 0; k < FW - 1; ++k)
+            if (k < WL) {
+                S[k] = Sr[k];
+                if (AFFINE) E[k] = Er[k];
+            }
+        S[WL] = sLast;
+        E[WL] = eLast;
     }
 
     __device__ int first_dir(int type, int loc) const
@@ -270,7 +435,7 @@ struct BandedPair {
                 int s = prev + (MATRIX ? smat[((H[ih] & 31) << 5) | (V[iv] & 31)] : (H[ih] == V[iv] ? a.match : a.mismatch));
                 int tv = TV_DIAG;
                 if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
-                if (TRACE) T[int64_t(col) * W] = uint8_t(tv);
+                if (TRACE) T[int64_t(col) * Wt] = uint8_t(tv);
                 if (LOCAL) scout(s, INF, INF, col, row);
                 prev = s;
                 ++ih; ++iv;
@@ -280,7 +445,7 @@ struct BandedPair {
             int s = prev + (MATRIX ? smat[((H[ih] & 31) << 5) | (V[iv] & 31)] : (H[ih] == V[iv] ? a.match : a.mismatch));
             int tv = TV_DIAG;
             if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
-            if (TRACE) T[int64_t(col) * W] = uint8_t(tv);
+            if (TRACE) T[int64_t(col) * Wt] = uint8_t(tv);
             if (ih == ihEnd) {
                 if (iv == ivEnd) scout(s, INF, INF, col, row);
                 if (LOCAL || fBottom) scout(s, INF, INF, col, row);
@@ -328,6 +493,8 @@ struct BandedPair {
             if (LOCAL || fBottom) retrack(hIt, ve, false);
             for (; hIt != hMid; ++hIt) track(hIt + 1, BCOL_INNER, BLOC_FULL, vb, ve);
         } else {
+            if (W >= 2 && W <= kBandFastW && hIt != hMid && ve - vb + 1 == W && upper - (hIt + 1) + (vb + 1) == 0)
+                middle_fast(hIt, hMid, vb, ve);
             for (; hIt != hMid; ++hIt) {
                 ++vb; ++ve;
                 track(hIt + 1, BCOL_INNER, BLOC_MIDDLE, vb, ve);
@@ -395,6 +562,7 @@ __global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
     bp.m = d.m;
     bp.n = d.n;
     bp.W = a.upper - a.lower + 1;
+    bp.Wt = band_trace_stride(bp.W);
     bp.lower = a.lower;
     bp.upper = a.upper;
     bp.INF = d.inf;
@@ -421,7 +589,7 @@ __device__ __forceinline__ uint8_t trace_at_band(const uint8_t *base, int W, int
 {
     const int k = upper - col + row;
     if (k < 0 || k >= W) return TV_NONE;
-    return base[int64_t(col) * W + k];
+    return base[int64_t(col) * band_trace_stride(W) + k];
 }
 
 }  // namespace gba

@@ -575,7 +575,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                 cells += int64_t(d.m) * d.n;
             }
             if (plan->traceback) {
-                tbytes[k] = p->band_on ? align16(int64_t(d.m + 1) * (p->band_upper - p->band_lower + 1))
+                tbytes[k] = p->band_on ? int64_t(d.m + 1) * band_trace_stride(p->band_upper - p->band_lower + 1)
                             : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
                                              : trace_bytes(d.m, d.n);
                 tsum += tbytes[k];
