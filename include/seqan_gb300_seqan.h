@@ -1,0 +1,359 @@
+// seqan_gb300_seqan.h -- SeqAn 2 call surface on the GB300 engine (header-only C++ binding).
+//
+// Include after <seqan/align.h> (and <seqan/align_parallel.h>) in code built against SeqAn 2
+// and link libseqan_gb300.so.  It adds a parallel policy tag `GB300` and overloads of the four
+// batch functions of align_parallel/parallel_align_interface.h:288-365 for
+// ExecutionPolicy<GB300, TVectorization>, with the reference's argument lists:
+//
+//   globalAlignmentScore(exec, setH, setV, score [, AlignConfig] [, lowerDiag, upperDiag])
+//   globalAlignmentScore(exec, seqH, setV, score [, AlignConfig])        (one vs many)
+//   localAlignmentScore (exec, setH, setV, score [, lowerDiag, upperDiag])
+//   globalAlignment     (exec, gapsSetH, gapsSetV, score [, AlignConfig] [, lowerDiag, upperDiag])
+//   localAlignment      (exec, gapsSetH, gapsSetV, score [, lowerDiag, upperDiag])
+//
+// so switching a call from ExecutionPolicy<Parallel, Vectorial> is a change of the policy
+// type only.  Sequences go to the engine as ordValue codes (the layout of
+// StringSet<..., Owner<ConcatDirect<>>>); Score<T, Simple> passes its four values and
+// Score<T, ScoreMatrix<...>> its table; T = int16_t selects 16-bit cells as the reference's
+// SIMD path does (pairs that could leave the exact int16 range run with 32-bit cells).  The
+// Gaps results are rebuilt by the reference's own _adaptTraceSegmentsTo
+// (align/dp_traceback_adaptor.h:57-117) from the engine's TraceSegment_ lists, so Gaps parity
+// is structural.  Errors throw std::runtime_error with the engine's message (the reference's
+// functions have no error channel).
+#ifndef SEQAN_GB300_SEQAN_H_
+#define SEQAN_GB300_SEQAN_H_
+
+#include <seqan/align.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "seqan_gb300.h"
+
+namespace seqan2 {
+
+struct GB300_;
+typedef Tag<GB300_> GB300;   // parallel policy: the GB300 batch engine
+
+namespace gb300_impl {
+
+// One engine context per process (device 0), created on first use.
+inline gba_context *context()
+{
+    static gba_context *ctx = [] {
+        gba_context *c = nullptr;
+        gba_config cfg{0, 0};
+        const int rc = gba_create(&c, &cfg);
+        if (rc != GBA_OK) throw std::runtime_error(std::string("gba_create: ") + gba_status_string(rc));
+        return c;
+    }();
+    return ctx;
+}
+
+inline void check(int rc, char const *what)
+{
+    if (rc == GBA_OK) return;
+    char buf[512] = {0};
+    gba_last_error(context(), buf, sizeof(buf));
+    throw std::runtime_error(std::string(what) + ": " + gba_status_string(rc) + ": " + buf);
+}
+
+// Concatenated ordValue codes and offsets of a set of sequences.
+struct Codes {
+    std::vector<uint8_t> seq;
+    std::vector<int64_t> off{0};
+    template <typename TSeq>
+    void add(TSeq const &s)
+    {
+        for (auto it = begin(s, Standard()); it != end(s, Standard()); ++it) seq.push_back(uint8_t(ordValue(*it)));
+        off.push_back(int64_t(seq.size()));
+    }
+};
+
+template <typename TSet>
+Codes flatten(TSet const &set)
+{
+    Codes c;
+    for (size_t k = 0; k < length(set); ++k) c.add(set[k]);
+    return c;
+}
+
+template <typename TGapsSet>
+Codes flatten_gaps(TGapsSet const &set)
+{
+    Codes c;
+    for (size_t k = 0; k < length(set); ++k) c.add(source(set[k]));
+    return c;
+}
+
+// Scoring scheme -> engine parameters.
+template <typename TValue, typename TAlphabet>
+void set_score(gba_params &p, std::vector<int32_t> &, Score<TValue, Simple> const &sc)
+{
+    p.match = scoreMatch(sc);
+    p.mismatch = scoreMismatch(sc);
+    p.gap_open = scoreGapOpen(sc);
+    p.gap_extend = scoreGapExtend(sc);
+    p.alphabet_size = int32_t(ValueSize<TAlphabet>::VALUE);
+}
+
+template <typename TValue, typename TAlphabet, typename TSeqValue, typename TSpec>
+void set_score(gba_params &p, std::vector<int32_t> &table, Score<TValue, ScoreMatrix<TSeqValue, TSpec>> const &sc)
+{
+    const int A = int(ValueSize<TAlphabet>::VALUE);
+    table.resize(size_t(A) * A);
+    for (int i = 0; i < A; ++i)
+        for (int j = 0; j < A; ++j) table[i * A + j] = int32_t(score(sc, TAlphabet(i), TAlphabet(j)));
+    p.matrix = table.data();
+    p.alphabet_size = A;
+    p.gap_open = scoreGapOpen(sc);
+    p.gap_extend = scoreGapExtend(sc);
+}
+
+template <typename TScoreValue>
+constexpr int score_bits()
+{
+    static_assert(sizeof(TScoreValue) == 2 || sizeof(TScoreValue) == 4,
+                  "the GB300 engine computes with 16- or 32-bit score values");
+    return sizeof(TScoreValue) == 2 ? 16 : 32;
+}
+
+template <bool TOP, bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+int free_ends(AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &)
+{
+    return (TOP ? GBA_FREE_TOP : 0) | (LEFT ? GBA_FREE_LEFT : 0) | (RIGHT ? GBA_FREE_RIGHT : 0) |
+           (BOTTOM ? GBA_FREE_BOTTOM : 0);
+}
+
+struct Band {
+    bool on = false;
+    int lower = 0, upper = 0;
+};
+
+// Runs one batch; returns the scores and, with `segments`, fills each pair's TraceSegment_ list.
+template <typename TScoreValue, typename TAlphabet, typename TScoreSpec>
+String<TScoreValue> run(Codes const &h, Codes const &v, bool h_shared, Score<TScoreValue, TScoreSpec> const &sc,
+                        int mode, int fe, Band band,
+                        std::vector<String<TraceSegment_<unsigned, unsigned>>> *segments)
+{
+    gba_params p{};
+    std::vector<int32_t> table;
+    set_score<TScoreValue, TAlphabet>(p, table, sc);
+    p.mode = mode;
+    p.gap_model = GBA_GAPS_AUTO;
+    p.free_ends = mode == GBA_GLOBAL ? fe : 0;
+    p.band_on = band.on;
+    p.band_lower = band.lower;
+    p.band_upper = band.upper;
+    p.score_bits = score_bits<TScoreValue>();
+    p.outputs = GBA_OUT_SCORE | GBA_OUT_END | (segments ? GBA_OUT_SEGMENTS : 0);
+    const int64_t n = int64_t(v.off.size()) - 1;
+    gba_batch b{};
+    b.num_pairs = n;
+    b.seq_h = h.seq.data();
+    b.off_h = h.off.data();
+    b.seq_v = v.seq.data();
+    b.off_v = v.off.data();
+    b.h_shared = h_shared ? 1 : 0;
+    std::vector<int32_t> score(size_t(n) + 1);
+    std::vector<gba_segment> segs;
+    std::vector<int64_t> seg_off(size_t(n) + 1);
+    gba_result r{};
+    r.score = score.data();
+    if (segments) {
+        // At most m + n + 4 segments per pair.
+        int64_t cap = 4 * n;
+        for (int64_t k = 0; k < n; ++k)
+            cap += (h_shared ? h.off[1] - h.off[0] : h.off[k + 1] - h.off[k]) + v.off[k + 1] - v.off[k];
+        segs.resize(size_t(cap) + 1);
+        r.segments = segs.data();
+        r.segment_capacity = cap;
+        r.segment_offsets = seg_off.data();
+    }
+    check(gba_align_batch(context(), &p, &b, &r), "gba_align_batch");
+    String<TScoreValue> out;
+    resize(out, size_t(n));
+    for (int64_t k = 0; k < n; ++k) out[k] = TScoreValue(score[k]);
+    if (segments) {
+        segments->resize(size_t(n));
+        for (int64_t k = 0; k < n; ++k) {
+            auto &dst = (*segments)[k];
+            clear(dst);
+            for (int64_t q = seg_off[k]; q < seg_off[k + 1]; ++q)
+                appendValue(dst, TraceSegment_<unsigned, unsigned>(segs[q].h_begin, segs[q].v_begin, segs[q].length,
+                                                                    uint8_t(segs[q].type)));
+        }
+    }
+    return out;
+}
+
+template <typename TSet>
+using AlphabetOf = typename Value<typename Value<TSet>::Type>::Type;
+
+template <typename TGapsSet>
+using GapsAlphabetOf = typename Value<typename Source<typename Value<TGapsSet>::Type>::Type>::Type;
+
+template <typename TScoreValue, typename TScoreSpec, typename TGapsSetH, typename TGapsSetV>
+String<TScoreValue> run_gaps(TGapsSetH &gapsH, TGapsSetV &gapsV, Score<TScoreValue, TScoreSpec> const &sc, int mode,
+                             int fe, Band band)
+{
+    if (length(gapsH) != length(gapsV)) throw std::runtime_error("gapsH and gapsV differ in length");
+    std::vector<String<TraceSegment_<unsigned, unsigned>>> segs;
+    String<TScoreValue> out = run<TScoreValue, GapsAlphabetOf<TGapsSetH>>(
+        flatten_gaps(gapsH), flatten_gaps(gapsV), false, sc, mode, fe, band, &segs);
+    for (size_t k = 0; k < length(gapsH); ++k) _adaptTraceSegmentsTo(gapsH[k], gapsV[k], segs[k]);
+    return out;
+}
+
+}  // namespace gb300_impl
+
+// ---- globalAlignmentScore ---------------------------------------------------------------
+
+template <typename TVec, typename TSetH, typename TSetV, typename TScoreValue, typename TScoreSpec, bool TOP,
+          bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+SEQAN_FUNC_ENABLE_IF(And<Is<ContainerConcept<typename Value<TSetH>::Type>>,
+                         Is<ContainerConcept<typename Value<TSetV>::Type>>>,
+                     String<TScoreValue>)
+globalAlignmentScore(ExecutionPolicy<GB300, TVec> const &, TSetH const &setH, TSetV const &setV,
+                     Score<TScoreValue, TScoreSpec> const &sc, AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac,
+                     int lowerDiag, int upperDiag)
+{
+    if (length(setH) != length(setV)) throw std::runtime_error("setH and setV differ in length");
+    return gb300_impl::run<TScoreValue, gb300_impl::AlphabetOf<TSetH>>(
+        gb300_impl::flatten(setH), gb300_impl::flatten(setV), false, sc, GBA_GLOBAL, gb300_impl::free_ends(ac),
+        gb300_impl::Band{true, lowerDiag, upperDiag}, nullptr);
+}
+
+template <typename TVec, typename TSetH, typename TSetV, typename TScoreValue, typename TScoreSpec, bool TOP,
+          bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+SEQAN_FUNC_ENABLE_IF(And<Is<ContainerConcept<typename Value<TSetH>::Type>>,
+                         Is<ContainerConcept<typename Value<TSetV>::Type>>>,
+                     String<TScoreValue>)
+globalAlignmentScore(ExecutionPolicy<GB300, TVec> const &, TSetH const &setH, TSetV const &setV,
+                     Score<TScoreValue, TScoreSpec> const &sc, AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac)
+{
+    if (length(setH) != length(setV)) throw std::runtime_error("setH and setV differ in length");
+    return gb300_impl::run<TScoreValue, gb300_impl::AlphabetOf<TSetH>>(
+        gb300_impl::flatten(setH), gb300_impl::flatten(setV), false, sc, GBA_GLOBAL, gb300_impl::free_ends(ac),
+        gb300_impl::Band{}, nullptr);
+}
+
+template <typename TVec, typename TSetH, typename TSetV, typename TScoreValue, typename TScoreSpec>
+SEQAN_FUNC_ENABLE_IF(And<Is<ContainerConcept<typename Value<TSetH>::Type>>,
+                         Is<ContainerConcept<typename Value<TSetV>::Type>>>,
+                     String<TScoreValue>)
+globalAlignmentScore(ExecutionPolicy<GB300, TVec> const &exec, TSetH const &setH, TSetV const &setV,
+                     Score<TScoreValue, TScoreSpec> const &sc, int lowerDiag, int upperDiag)
+{
+    return globalAlignmentScore(exec, setH, setV, sc, AlignConfig<>(), lowerDiag, upperDiag);
+}
+
+template <typename TVec, typename TSetH, typename TSetV, typename TScoreValue, typename TScoreSpec>
+SEQAN_FUNC_ENABLE_IF(And<Is<ContainerConcept<typename Value<TSetH>::Type>>,
+                         Is<ContainerConcept<typename Value<TSetV>::Type>>>,
+                     String<TScoreValue>)
+globalAlignmentScore(ExecutionPolicy<GB300, TVec> const &exec, TSetH const &setH, TSetV const &setV,
+                     Score<TScoreValue, TScoreSpec> const &sc)
+{
+    return globalAlignmentScore(exec, setH, setV, sc, AlignConfig<>());
+}
+
+// One vs many (align/global_alignment_unbanded.h:766-821).
+template <typename TVec, typename TString1, typename TString2, typename TSpec, typename TScoreValue,
+          typename TScoreSpec, bool TOP, bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+SEQAN_FUNC_DISABLE_IF(Is<ContainerConcept<typename Value<TString1>::Type>>, String<TScoreValue>)
+globalAlignmentScore(ExecutionPolicy<GB300, TVec> const &, TString1 const &seqH, StringSet<TString2, TSpec> const &setV,
+                     Score<TScoreValue, TScoreSpec> const &sc, AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac)
+{
+    gb300_impl::Codes h;
+    h.add(seqH);
+    return gb300_impl::run<TScoreValue, typename Value<TString1>::Type>(
+        h, gb300_impl::flatten(setV), true, sc, GBA_GLOBAL, gb300_impl::free_ends(ac), gb300_impl::Band{}, nullptr);
+}
+
+template <typename TVec, typename TString1, typename TString2, typename TSpec, typename TScoreValue,
+          typename TScoreSpec>
+SEQAN_FUNC_DISABLE_IF(Is<ContainerConcept<typename Value<TString1>::Type>>, String<TScoreValue>)
+globalAlignmentScore(ExecutionPolicy<GB300, TVec> const &exec, TString1 const &seqH,
+                     StringSet<TString2, TSpec> const &setV, Score<TScoreValue, TScoreSpec> const &sc)
+{
+    return globalAlignmentScore(exec, seqH, setV, sc, AlignConfig<>());
+}
+
+// ---- localAlignmentScore ----------------------------------------------------------------
+
+template <typename TVec, typename TSetH, typename TSetV, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> localAlignmentScore(ExecutionPolicy<GB300, TVec> const &, TSetH const &setH, TSetV const &setV,
+                                        Score<TScoreValue, TScoreSpec> const &sc, int lowerDiag, int upperDiag)
+{
+    if (length(setH) != length(setV)) throw std::runtime_error("setH and setV differ in length");
+    return gb300_impl::run<TScoreValue, gb300_impl::AlphabetOf<TSetH>>(
+        gb300_impl::flatten(setH), gb300_impl::flatten(setV), false, sc, GBA_LOCAL, 0,
+        gb300_impl::Band{true, lowerDiag, upperDiag}, nullptr);
+}
+
+template <typename TVec, typename TSetH, typename TSetV, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> localAlignmentScore(ExecutionPolicy<GB300, TVec> const &, TSetH const &setH, TSetV const &setV,
+                                        Score<TScoreValue, TScoreSpec> const &sc)
+{
+    if (length(setH) != length(setV)) throw std::runtime_error("setH and setV differ in length");
+    return gb300_impl::run<TScoreValue, gb300_impl::AlphabetOf<TSetH>>(
+        gb300_impl::flatten(setH), gb300_impl::flatten(setV), false, sc, GBA_LOCAL, 0, gb300_impl::Band{}, nullptr);
+}
+
+// ---- globalAlignment / localAlignment over StringSet<Gaps> -------------------------------
+
+template <typename TVec, typename TGapsSetH, typename TGapsSetV, typename TScoreValue, typename TScoreSpec, bool TOP,
+          bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &, TGapsSetH &gapsH, TGapsSetV &gapsV,
+                                    Score<TScoreValue, TScoreSpec> const &sc,
+                                    AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac, int lowerDiag,
+                                    int upperDiag)
+{
+    return gb300_impl::run_gaps(gapsH, gapsV, sc, GBA_GLOBAL, gb300_impl::free_ends(ac),
+                                gb300_impl::Band{true, lowerDiag, upperDiag});
+}
+
+template <typename TVec, typename TGapsSetH, typename TGapsSetV, typename TScoreValue, typename TScoreSpec, bool TOP,
+          bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &, TGapsSetH &gapsH, TGapsSetV &gapsV,
+                                    Score<TScoreValue, TScoreSpec> const &sc,
+                                    AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac)
+{
+    return gb300_impl::run_gaps(gapsH, gapsV, sc, GBA_GLOBAL, gb300_impl::free_ends(ac), gb300_impl::Band{});
+}
+
+template <typename TVec, typename TGapsSetH, typename TGapsSetV, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &exec, TGapsSetH &gapsH, TGapsSetV &gapsV,
+                                    Score<TScoreValue, TScoreSpec> const &sc, int lowerDiag, int upperDiag)
+{
+    return globalAlignment(exec, gapsH, gapsV, sc, AlignConfig<>(), lowerDiag, upperDiag);
+}
+
+template <typename TVec, typename TGapsSetH, typename TGapsSetV, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &exec, TGapsSetH &gapsH, TGapsSetV &gapsV,
+                                    Score<TScoreValue, TScoreSpec> const &sc)
+{
+    return globalAlignment(exec, gapsH, gapsV, sc, AlignConfig<>());
+}
+
+template <typename TVec, typename TGapsSetH, typename TGapsSetV, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> localAlignment(ExecutionPolicy<GB300, TVec> const &, TGapsSetH &gapsH, TGapsSetV &gapsV,
+                                   Score<TScoreValue, TScoreSpec> const &sc, int lowerDiag, int upperDiag)
+{
+    return gb300_impl::run_gaps(gapsH, gapsV, sc, GBA_LOCAL, 0, gb300_impl::Band{true, lowerDiag, upperDiag});
+}
+
+template <typename TVec, typename TGapsSetH, typename TGapsSetV, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> localAlignment(ExecutionPolicy<GB300, TVec> const &, TGapsSetH &gapsH, TGapsSetV &gapsV,
+                                   Score<TScoreValue, TScoreSpec> const &sc)
+{
+    return gb300_impl::run_gaps(gapsH, gapsV, sc, GBA_LOCAL, 0, gb300_impl::Band{});
+}
+
+}  // namespace seqan2
+
+#endif  // SEQAN_GB300_SEQAN_H_

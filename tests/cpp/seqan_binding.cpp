@@ -1,0 +1,57 @@
+// Instantiates every overload of include/seqan_gb300_seqan.h with the SeqAn 2 types a caller
+// uses (StringSet<Dna5String>, StringSet<Gaps<...>>, Score<int16_t|int, Simple>, Blosum62,
+// AlignConfig, bands).  Built by tests/test_cpp_binding.py against the reference's headers and
+// linked against libseqan_gb300.so; with a GPU it prints each result for comparison with the
+// same calls under ExecutionPolicy<Parallel, Vectorial>.
+#include <iostream>
+
+#include <seqan/align.h>
+#include <seqan/align_parallel.h>
+#include <seqan/score.h>
+
+#include "seqan_gb300_seqan.h"
+
+using namespace seqan2;
+
+int main()
+{
+    ExecutionPolicy<GB300, Vectorial> gpu;
+    StringSet<Dna5String> setH, setV;
+    appendValue(setH, "ACGTACGTTGACCA");
+    appendValue(setH, "GATTACA");
+    appendValue(setV, "ACGTTCGTTGCCA");
+    appendValue(setV, "GATCACAA");
+    Score<int16_t, Simple> sc16(2, -4, -1, -6);
+    Score<int, Simple> sc32(2, -3, -5, -5);
+
+    String<int16_t> a = globalAlignmentScore(gpu, setH, setV, sc16);
+    String<int16_t> b = globalAlignmentScore(gpu, setH, setV, sc16, AlignConfig<true, false, false, true>());
+    String<int> c = globalAlignmentScore(gpu, setH, setV, sc32, -3, 3);
+    String<int> d = globalAlignmentScore(gpu, setH, setV, sc32, AlignConfig<true, true, true, true>(), -3, 3);
+    String<int16_t> e = globalAlignmentScore(gpu, setH[0], setV, sc16);
+    String<int> f = localAlignmentScore(gpu, setH, setV, sc32);
+    String<int> g = localAlignmentScore(gpu, setH, setV, sc32, -2, 2);
+
+    StringSet<String<AminoAcid>> pH, pV;
+    appendValue(pH, "MKVLAAGIVGLLLA");
+    appendValue(pV, "MKVIAAGLVGLA");
+    Score<int16_t, ScoreMatrix<AminoAcid, ScoreSpecBlosum62>> blosum(-1, -11);
+    String<int16_t> h = localAlignmentScore(gpu, pH, pV, blosum);
+
+    typedef Gaps<Dna5String> TGaps;
+    StringSet<TGaps> gapsH, gapsV;
+    for (size_t k = 0; k < length(setH); ++k) {
+        appendValue(gapsH, TGaps(setH[k]));
+        appendValue(gapsV, TGaps(setV[k]));
+    }
+    String<int16_t> i = globalAlignment(gpu, gapsH, gapsV, sc16);
+    String<int16_t> j = globalAlignment(gpu, gapsH, gapsV, sc16, AlignConfig<false, true, true, false>());
+    String<int> k = globalAlignment(gpu, gapsH, gapsV, sc32, -4, 4);
+    String<int> l = localAlignment(gpu, gapsH, gapsV, sc32);
+    String<int> m = localAlignment(gpu, gapsH, gapsV, sc32, -4, 4);
+
+    std::cout << a[0] << ' ' << b[0] << ' ' << c[0] << ' ' << d[0] << ' ' << e[1] << ' ' << f[0] << ' ' << g[0] << ' '
+              << h[0] << ' ' << i[0] << ' ' << j[0] << ' ' << k[0] << ' ' << l[0] << ' ' << m[0] << '\n'
+              << gapsH[0] << '\n' << gapsV[0] << '\n';
+    return 0;
+}
