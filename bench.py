@@ -258,18 +258,19 @@ def run_serving(rate: float, duration: float, seed: int = 7, streams: int = 8):
                  max_batch_pairs=4096, hbm_budget_bytes=64 << 30)
     done = {}
     try:
+        # The arrival process runs in native code on its own thread (the call releases the
+        # GIL); this thread collects results meanwhile.
+        rc = []
         t0 = srv.clock()
-        for i in range(n):
-            while srv.clock() - t0 < arrivals[i]:
-                pass
-            srv.submit(i, H[i], V[i])
-            if i % 256 == 0:
-                for r in srv.poll():
-                    done[r.tag] = r
+        feeder = threading.Thread(target=lambda: rc.append(srv.submit_schedule(H, V, arrivals)))
+        feeder.start()
         while len(done) < n:
-            for r in srv.poll():
+            for r in srv.poll(segments=False):
                 done[r.tag] = r
+            if not feeder.is_alive() and rc and rc[0] != 0:
+                raise RuntimeError(f"submit_schedule failed with status {rc[0]}")
             time.sleep(0.0005)
+        feeder.join()
         t_end = max(r.t_done for r in done.values())
         st = srv.stats()
     finally:

@@ -271,6 +271,13 @@ GBA_API int gba_server_poll(gba_server *srv, gba_request_result *results, int64_
                             gba_segment *segments, int64_t segment_capacity, int64_t *num_results,
                             int64_t *num_segments);
 GBA_API int gba_server_get_stats(gba_server *srv, gba_server_stats *stats);
+/* Load replay (no counterpart in the reference): submits pair k of `requests` (host layout of
+ * gba_batch, h_shared allowed) with tag first_tag + k at at_seconds[k] after the call starts,
+ * waiting between submits on the calling thread; returns once all are submitted (the first
+ * failing submit's status otherwise).  For driving the server with a recorded or synthetic
+ * arrival process from native code. */
+GBA_API int gba_server_submit_schedule(gba_server *srv, const gba_batch *requests, const double *at_seconds,
+                                       uint64_t first_tag);
 GBA_API int gba_server_last_error(gba_server *srv, char *buf, size_t size);
 /* Stops the worker after the batches in flight finish; unpolled results are dropped. */
 GBA_API int gba_server_destroy(gba_server *srv);

@@ -39,7 +39,7 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_copy_to_device", "gba_copy_to_host", "gba_synchronize", "gba_timer_start",
             "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc",
             "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
-            "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds"]
+            "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule"]
 
 
 class GbaConfig(C.Structure):
@@ -164,6 +164,7 @@ def lib():
             L.gba_server_poll.argtypes = [vp, C.POINTER(GbaRequestResult), i64, vp, i64, C.POINTER(i64),
                                           C.POINTER(i64)]
             L.gba_server_get_stats.argtypes = [vp, C.POINTER(GbaServerStats)]
+            L.gba_server_submit_schedule.argtypes = [vp, C.POINTER(GbaBatch), vp, C.c_uint64]
             L.gba_server_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
             L.gba_server_destroy.argtypes = [vp]
             L.gba_clock_seconds.argtypes = []

@@ -379,6 +379,23 @@ GBA_API int gba_server_submit(gba_server *s, uint64_t tag, const uint8_t *h, int
     return GBA_OK;
 }
 
+GBA_API int gba_server_submit_schedule(gba_server *s, const gba_batch *req, const double *at, uint64_t first_tag)
+{
+    if (!s || !req || (req->num_pairs > 0 && (!at || !req->off_h || !req->off_v || !req->seq_h || !req->seq_v)))
+        return GBA_EINVAL;
+    const double t0 = clock_seconds();
+    for (int64_t k = 0; k < req->num_pairs; ++k) {
+        while (clock_seconds() - t0 < at[k]) {
+        }
+        const int64_t h0 = req->h_shared ? req->off_h[0] : req->off_h[k];
+        const int64_t h1 = req->h_shared ? req->off_h[1] : req->off_h[k + 1];
+        const int rc = gba_server_submit(s, first_tag + uint64_t(k), req->seq_h + h0, h1 - h0,
+                                         req->seq_v + req->off_v[k], req->off_v[k + 1] - req->off_v[k]);
+        if (rc) return rc;
+    }
+    return GBA_OK;
+}
+
 GBA_API int gba_server_poll(gba_server *s, gba_request_result *results, int64_t max_results, gba_segment *segments,
                             int64_t segment_capacity, int64_t *num_results, int64_t *num_segments)
 {

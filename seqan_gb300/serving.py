@@ -18,7 +18,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _native as N
-from .align import AlignConfig, make_params
+from .align import AlignConfig, _concat, make_params
 
 
 @dataclass
@@ -66,8 +66,21 @@ class Server:
         v = np.ascontiguousarray(v, dtype=np.uint8)
         return N.lib().gba_server_submit(self._h, tag, h.ctypes.data, len(h), v.ctypes.data, len(v))
 
-    def poll(self) -> list[RequestResult]:
-        """Finished requests (completion order); never waits."""
+    def submit_schedule(self, H, V, at_seconds, first_tag: int = 0) -> int:
+        """Submits pair k with tag first_tag + k at at_seconds[k] after the call starts, from
+        native code (no Python between submits); blocks until all are submitted.  Call it from
+        a thread to poll meanwhile: the call does not hold the GIL."""
+        sh, oh = _concat(H)
+        sv, ov = _concat(V)
+        at = np.ascontiguousarray(at_seconds, dtype=np.float64)
+        if len(at) != len(H) or len(H) != len(V):
+            raise ValueError("H, V and at_seconds differ in length")
+        b = N.GbaBatch(len(H), sh.ctypes.data, oh.ctypes.data, sv.ctypes.data, ov.ctypes.data, 0, 0)
+        return N.lib().gba_server_submit_schedule(self._h, C.byref(b), at.ctypes.data, first_tag)
+
+    def poll(self, segments: bool = True) -> list[RequestResult]:
+        """Finished requests (completion order); never waits.  segments=False skips building
+        the per-request segment lists."""
         L = N.lib()
         out = []
         while True:
@@ -83,7 +96,8 @@ class Server:
                 r = self._results[i]
                 segs = self._segs[r.segment_offset:r.segment_offset + r.n_segments]
                 out.append(RequestResult(r.tag, r.score, r.end_h, r.end_v, r.begin_h, r.begin_v, r.status,
-                                         r.t_submit, r.t_done, [tuple(int(x) for x in s) for s in segs]))
+                                         r.t_submit, r.t_done,
+                                         [tuple(int(x) for x in s) for s in segs] if segments else []))
             if nr.value < len(self._results):
                 return out
 

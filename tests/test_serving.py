@@ -114,3 +114,27 @@ def test_latency_timestamps_and_empty_pairs(engine):
     assert done[2].score == 8 and done[2].segments == [(0, 0, 4, 1)]
     for r in done.values():
         assert t0 <= r.t_submit <= r.t_done
+
+
+def test_native_submit_schedule(engine):
+    """A request trace replayed by gba_server_submit_schedule at its arrival times (native
+    thread) while Python polls; every result equals the oracle's and each was submitted no
+    earlier than its scheduled time."""
+    import threading
+    import seqan_gb300 as sg
+    from seqan_gb300.serving import Server
+    H, V = _pairs(9, np.random.default_rng(10).integers(50, 1500, 300))
+    at = np.sort(np.random.default_rng(11).uniform(0, 0.06, len(H)))
+    with Server(sg.Score(2, -4, -1, -6, dtype=np.int16), traceback=True, streams=4) as srv:
+        t0 = srv.clock()
+        rc = []
+        th = threading.Thread(target=lambda: rc.append(srv.submit_schedule(H, V, at, first_tag=5000)))
+        th.start()
+        done = _drain(srv, len(H))
+        th.join()
+    assert rc == [0]
+    ref = O.oracle_batch(O.Problem("global", 0, None, 2, -4, -6, -1, None, 32), H, V, traceback=True)
+    for k in range(len(H)):
+        r = done[5000 + k]
+        assert r.score == ref.score[k] and r.segments == ref.segments[k], k
+        assert r.t_submit >= t0 + at[k] - 1e-3
