@@ -111,8 +111,11 @@ enum {
     GBA_FLAG_NO_GRAPH = 8,         /* launch kernels directly instead of replaying a CUDA graph */
     GBA_FLAG_AUTOTUNE = 16,        /* time the packed kernel's tiling variants on the first run
                                       of a plan and remember the fastest per batch shape */
-    GBA_FLAG_PACKED = 32           /* use the packed kernel for eligible pairs even in batches
+    GBA_FLAG_PACKED = 32,          /* use the packed kernel for eligible pairs even in batches
                                       too small to fill the GPU with it */
+    GBA_FLAG_PACKED_SPLIT = 64,    /* packed kernel: every pair runs as a split slot (one pair per
+                                      thread, two strips at once) instead of only the longest */
+    GBA_FLAG_PACKED_NO_SPLIT = 128 /* packed kernel: no split slots (two pairs per thread only) */
 };
 
 /* A batch: concatenated residue codes with n+1 offsets for each side. */

@@ -118,6 +118,7 @@ struct gba_plan {
     bool tune_pending = false;      // autotune at the first run
     int64_t tune_key = 0;
     int32_t launches = 0;           // kernels one run launches
+    int err_slot = 0;               // word of the context's error buffer this plan's kernels use
     // Plain per-bucket mode: general kernel launched once per length bucket.
     std::vector<int64_t> bucket_start, bucket_count;
     // Captured launch sequence (replayed while the device pointers stay the same).
@@ -186,8 +187,10 @@ struct gba_context {
     gba_plan oneshot;               // buffers reused by gba_align_batch
     DevBuf seq_h, seq_v;            // device copies of the inputs for gba_align_batch
     DevBuf out_score, out_end_h, out_end_v;
-    DevBuf err_word;                // set by a kernel whose bounded wait ran out
-    bool check_err = false;         // the last run can set err_word
+    DevBuf err_word;                // one word per plan slot, set by a kernel whose bounded wait ran out
+    uint32_t check_err = 0;         // slots of err_word the runs since the last check can set
+    std::vector<std::unique_ptr<gba_plan>> chunk_plans;   // gba_align_batch chunks 1.. (0 = oneshot)
+    std::vector<cudaEvent_t> chunk_ev;                    // 3 per chunk
 };
 
 namespace {
@@ -219,6 +222,11 @@ constexpr int kBlock = 128;
 constexpr int kMaxBandWidth = 512;   // band slots a thread keeps (local memory)
 // Below this many pairs two-pairs-per-thread leaves most SMs idle; one warp per pair fills them.
 constexpr int64_t kPackedMinPairs = 32768;
+// gba_align_batch splits large score-only batches into up to kMaxChunks contiguous chunks of at
+// least kChunkPairs pairs: each chunk is planned on the host while the previous one runs.  A
+// chunk must still fill the GPU on its own (100,000 short pairs split in two ran 37% slower).
+constexpr int kMaxChunks = 8;
+constexpr int64_t kChunkPairs = 200000;
 // Pairs at least this wide pipeline their bands across warps even in large batches: the ~130
 // steps a pipelined band waits before its first column are then a small share of its work.
 constexpr int kPipelineMinCols = 1024;
@@ -668,12 +676,41 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // interleaved by lane.
     sort_desc(keys16, idx16);
     timer.mark("sort");
-    std::vector<Slot16> slots16((idx16.size() + 1) / 2);
+    // Split slots: a thread holds two pairs, so its time is set by its larger pair; pairs whose
+    // cells exceed the batch's average work per resident thread (the batch cannot finish before
+    // its longest thread) run one per thread as a split slot, two strips at once.  They are a
+    // prefix of the length-sorted order, rounded down to whole warps.
+    int64_t nsplit = 0;
+    if (!idx16.empty() && !(p->flags & GBA_FLAG_PACKED_NO_SPLIT)) {
+        if (p->flags & GBA_FLAG_PACKED_SPLIT) {
+            nsplit = int64_t(idx16.size());
+        } else {
+            const double resident = double(persistent_grid(ctx, dp16_fn(0, plan->affine))) * kBlock;
+            double total = 0;
+            for (int32_t k : idx16) total += double(desc[k].m) * desc[k].n;
+            const double per_thread = total / 2 / resident;
+            while (nsplit < int64_t(idx16.size()) && double(desc[idx16[nsplit]].m) * desc[idx16[nsplit]].n > per_thread)
+                ++nsplit;
+            nsplit -= nsplit % 32;
+        }
+    }
+    const int64_t rest16 = int64_t(idx16.size()) - nsplit;
+    std::vector<Slot16> slots16(size_t(nsplit + (rest16 + 1) / 2));
 #pragma omp parallel for num_threads(plan_threads(int64_t(slots16.size()))) schedule(static)
     for (size_t q = 0; q < slots16.size(); ++q) {
         Slot16 &sl = slots16[q];
-        sl.pa = idx16[2 * q];
-        sl.pb = 2 * q + 1 < idx16.size() ? idx16[2 * q + 1] : -1;
+        if (int64_t(q) < nsplit) {
+            sl.pa = idx16[q];
+            sl.pb = -1;
+            sl.m = desc[sl.pa].m + 1;   // steps: the high strip runs one column behind
+            sl.n = desc[sl.pa].n;
+            sl.split = 1;
+            continue;
+        }
+        const size_t u = size_t(nsplit) + 2 * (q - size_t(nsplit));
+        sl.pa = idx16[u];
+        sl.pb = u + 1 < idx16.size() ? idx16[u + 1] : -1;
+        sl.split = 0;
         sl.m = desc[sl.pa].m;
         sl.n = desc[sl.pa].n;
         if (sl.pb >= 0) {
@@ -794,7 +831,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         if ((rc = upload(ctx, plan->tasks_warp, wtasks))) return rc;
         GBA_CUDA(ctx, plan->rowbuf.ensure(size_t(std::max<int64_t>(rbtot, 1)) * sizeof(int2)));
         GBA_CUDA(ctx, plan->band_state.ensure(size_t(std::max<int64_t>(nstates, 1)) * sizeof(BandState)));
-        GBA_CUDA(ctx, ctx->err_word.ensure(16));
+        GBA_CUDA(ctx, ctx->err_word.ensure(kMaxChunks * sizeof(int32_t)));
         GBA_CUDA(ctx, plan->counter_warp.ensure(16));
     }
     if (plan->num16 > 0) {
@@ -1001,6 +1038,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         a.free_ends = plan->free_ends;
         a.num_tasks = plan->tasks16;
         a.task_counter = plan->counter16.as<int32_t>();
+        a.rows = kVariants16[plan->variant16].rows;
         GBA_CUDA(ctx, cudaMemsetAsync(plan->counter16.ptr, 0, sizeof(int32_t), ctx->stream));
         const int grid = int(std::min<int64_t>(plan->grid16[plan->variant16],
                                                 (int64_t(plan->tasks16) * 32 + kBlock - 1) / kBlock));
@@ -1047,7 +1085,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         w.rowbuf_off = plan->rowbuf_off.as<int64_t>();
         w.bands = plan->band_state.as<BandState>();
         w.band_base = plan->band_base.as<int64_t>();
-        w.error = ctx->err_word.as<int32_t>();
+        w.error = ctx->err_word.as<int32_t>() + plan->err_slot;
         w.trace = plan->traceback ? plan->trace.as<uint8_t>() : nullptr;
         w.score = dscore;
         w.end_h = end_h;
@@ -1067,7 +1105,8 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         if (plan->num_band_states > 0) {
             GBA_CUDA(ctx, cudaMemsetAsync(plan->band_state.ptr, 0, plan->num_band_states * sizeof(BandState),
                                           ctx->stream));
-            GBA_CUDA(ctx, cudaMemsetAsync(ctx->err_word.ptr, 0, sizeof(int32_t), ctx->stream));
+            GBA_CUDA(ctx, cudaMemsetAsync(ctx->err_word.as<int32_t>() + plan->err_slot, 0, sizeof(int32_t),
+                                          ctx->stream));
         }
         const int grid =
             int(std::min<int64_t>(plan->grid_warp, (plan->num_warp_tasks * 32 + kBlock - 1) / kBlock));
@@ -1251,7 +1290,7 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         const int rc = enqueue_plan(ctx, plan, dseq_h, dseq_v, dscore, dend_h, dend_v, false);
         if (rc) return rc;
     }
-    ctx->check_err = plan->use_warp && plan->num_band_states > 0;
+    if (plan->use_warp && plan->num_band_states > 0) ctx->check_err |= 1u << plan->err_slot;
     ctx->stats.kernel_launches = plan->launches;
     ctx->stats.tile_rows = plan->num16 ? kVariants16[plan->variant16].rows : 0;
     ctx->stats.tile_min_blocks = plan->num16 ? kVariants16[plan->variant16].minb : 0;
@@ -1263,18 +1302,26 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
     return GBA_OK;
 }
 
+// Reads the error words of the plan slots whose runs can set them.
+int check_wait_errors(gba_context *ctx)
+{
+    if (!ctx->check_err) return GBA_OK;
+    const uint32_t mask = ctx->check_err;
+    ctx->check_err = 0;
+    int32_t e[kMaxChunks] = {};
+    GBA_CUDA(ctx, cudaMemcpyAsync(e, ctx->err_word.ptr, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < kMaxChunks; ++i)
+        if ((mask >> i & 1u) && e[i]) return fail(ctx, GBA_ETIMEOUT, "a wait between the bands of a pair ran out");
+    return GBA_OK;
+}
+
 int finish_stats(gba_context *ctx)
 {
     if (!ctx->stats_pending) return GBA_OK;
     ctx->stats_pending = false;
     GBA_CUDA(ctx, cudaEventSynchronize(ctx->ev[2]));
-    if (ctx->check_err) {
-        ctx->check_err = false;
-        int32_t e = 0;
-        GBA_CUDA(ctx, cudaMemcpyAsync(&e, ctx->err_word.ptr, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
-        GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        if (e) return fail(ctx, GBA_ETIMEOUT, "a wait between the bands of a pair ran out");
-    }
+    if (int rc = check_wait_errors(ctx)) return rc;
     float a = 0, b = 0;
     GBA_CUDA(ctx, cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
     GBA_CUDA(ctx, cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
@@ -1332,6 +1379,83 @@ int fetch_outputs(gba_context *ctx, gba_plan *plan, gba_result *r)
 
 }  // namespace
 
+// Score-only batch of at least 2 * kChunkPairs pairs, in contiguous chunks: chunk c + 1 is
+// planned on the host while chunk c runs on the device (each chunk's pairs are length-sorted
+// within the chunk).  The input copies are already enqueued on ctx->stream.
+int align_batch_chunked(gba_context *ctx, const gba_params *params, const gba_batch *batch, gba_result *result,
+                        std::chrono::steady_clock::time_point t0)
+{
+    const int64_t N = batch->num_pairs;
+    const int K = int(std::min<int64_t>(kMaxChunks, N / kChunkPairs));
+    while (int(ctx->chunk_plans.size()) < K - 1) ctx->chunk_plans.emplace_back(new gba_plan());
+    while (int(ctx->chunk_ev.size()) < 3 * K) {
+        cudaEvent_t e = nullptr;
+        GBA_CUDA(ctx, cudaEventCreate(&e));
+        ctx->chunk_ev.push_back(e);
+    }
+    GBA_CUDA(ctx, ctx->out_score.ensure(size_t(N) * 4));
+    cudaEvent_t saved[3] = {ctx->ev[0], ctx->ev[1], ctx->ev[2]};
+    std::vector<int64_t> k0(K + 1);
+    for (int c = 0; c <= K; ++c) k0[c] = N * c / K;
+    gba_stats total{};
+    float plan_ms = 0;
+    int rc = GBA_OK;
+    for (int c = 0; c < K && rc == GBA_OK; ++c) {
+        gba_plan *plan = c == 0 ? &ctx->oneshot : ctx->chunk_plans[c - 1].get();
+        plan->err_slot = c;
+        gba_batch sub = *batch;
+        sub.num_pairs = k0[c + 1] - k0[c];
+        if (!batch->h_shared) sub.off_h = batch->off_h + k0[c];
+        sub.off_v = batch->off_v + k0[c];
+        const auto tp = std::chrono::steady_clock::now();
+        rc = build_plan(ctx, params, &sub, plan);
+        plan_ms += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - tp).count();
+        if (rc) break;
+        for (int i = 0; i < 3; ++i) ctx->ev[i] = ctx->chunk_ev[3 * c + i];
+        rc = run_plan(ctx, plan, ctx->seq_h.as<uint8_t>(), ctx->seq_v.as<uint8_t>(),
+                      ctx->out_score.as<int32_t>() + k0[c], nullptr, nullptr, false);
+        total.cells += plan->cells;
+        total.kernel_launches += plan->launches;
+        total.trace_bytes += plan->trace_total;
+        total.dp_kernels |= ctx->stats.dp_kernels;
+        total.tile_rows = ctx->stats.tile_rows;
+        total.tile_min_blocks = ctx->stats.tile_min_blocks;
+    }
+    for (int i = 0; i < 3; ++i) ctx->ev[i] = saved[i];
+    ctx->stats_pending = false;
+    if (rc) {
+        cudaStreamSynchronize(ctx->stream);
+        return rc;
+    }
+    if (result->score)
+        GBA_CUDA(ctx, cudaMemcpyAsync(result->score, ctx->out_score.ptr, N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    for (int c = 0; c < K; ++c) {
+        gba_plan *plan = c == 0 ? &ctx->oneshot : ctx->chunk_plans[c - 1].get();
+        const int64_t n = k0[c + 1] - k0[c];
+        if (result->end_h)
+            GBA_CUDA(ctx, cudaMemcpyAsync(result->end_h + k0[c], plan->end_h.ptr, n * 4, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+        if (result->end_v)
+            GBA_CUDA(ctx, cudaMemcpyAsync(result->end_v + k0[c], plan->end_v.ptr, n * 4, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+    }
+    GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < K; ++c) {
+        gba_plan *plan = c == 0 ? &ctx->oneshot : ctx->chunk_plans[c - 1].get();
+        if (result->pair_status) std::memcpy(result->pair_status + k0[c], plan->status.data(), (k0[c + 1] - k0[c]) * 4);
+        float a = 0, b = 0;
+        GBA_CUDA(ctx, cudaEventElapsedTime(&a, ctx->chunk_ev[3 * c], ctx->chunk_ev[3 * c + 1]));
+        GBA_CUDA(ctx, cudaEventElapsedTime(&b, ctx->chunk_ev[3 * c + 1], ctx->chunk_ev[3 * c + 2]));
+        total.dp_kernel_ms += a;
+        total.traceback_kernel_ms += b;
+    }
+    if ((rc = check_wait_errors(ctx))) return rc;
+    total.host_plan_ms = plan_ms;
+    total.call_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    ctx->stats = total;
+    return GBA_OK;
+}
+
 // =======================================================================================
 // C-ABI
 // =======================================================================================
@@ -1386,6 +1510,8 @@ GBA_API int gba_destroy(gba_context *ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     ctx->oneshot.release();
+    for (auto &cp : ctx->chunk_plans) cp->release();
+    for (cudaEvent_t e : ctx->chunk_ev) cudaEventDestroy(e);
     ctx->seq_h.release();
     ctx->seq_v.release();
     ctx->out_score.release();
@@ -1426,6 +1552,9 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
         if (hb) GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_h.ptr, batch->seq_h, hb, cudaMemcpyHostToDevice, ctx->stream));
         if (vb) GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_v.ptr, batch->seq_v, vb, cudaMemcpyHostToDevice, ctx->stream));
     }
+    if (params && batch && !(params->outputs & GBA_OUT_SEGMENTS) && batch->num_pairs >= 2 * kChunkPairs)
+        return align_batch_chunked(ctx, params, batch, result, t0);
+    plan->err_slot = 0;
     int rc = build_plan(ctx, params, batch, plan);
     if (rc) return rc;
     const float plan_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -162,8 +162,8 @@ int srv_launch(gba_server *s, SrvSlot &sl)
                   nullptr, false);
     if (rc) return rc;
     ctx->stats_pending = false;
-    sl.check_err = ctx->check_err;
-    ctx->check_err = false;
+    sl.check_err = ctx->check_err != 0;
+    ctx->check_err = 0;
     // Outputs: 6 int32 per pair (score, end_h, end_v, begin_h, begin_v, segment count), the
     // error word, then the per-pair segment slots.
     const bool tb = sl.plan.traceback;

@@ -158,11 +158,14 @@ def test_python_interface_gaps(engine):
     assert (gH.row(), gV.row()) == ("AT-G-T", "ATAGAT")
 
 
-@pytest.mark.parametrize("flags", [32, 2, 0])      # packed kernel (32-row, 16-row strips), warp kernel
+# packed kernel: 32-row strips (split slots for the 320 longest pairs, the rest two per thread),
+# 16-row strips, every pair split (32- and 16-row strips), no split slots; then the warp kernel
+@pytest.mark.parametrize("flags", [32, 2, 32 | 64, 2 | 64, 32 | 128, 0])
 @pytest.mark.parametrize("fe", [0, 1, 2, 4, 8, 9, 6, 15, 5, 10])
 def test_packed_kernel_against_oracle(engine, flags, fe):
-    """The two-pairs-per-thread 16-bit kernel: uneven lengths in one slot, odd pair count,
-    Dna5 codes (N = 4), both gap models, every tracked-cell rule."""
+    """The packed 16-bit kernel: two-pair slots (uneven lengths in one slot, odd pair count) and
+    split slots (one pair, two strips at once), Dna5 codes (N = 4), both gap models, every
+    tracked-cell rule."""
     import seqan_gb300 as sg
     rng = np.random.default_rng(1000 + fe)
     H = [rng.integers(0, 5, rng.integers(1, 260)).astype(np.uint8) for _ in range(333)]
@@ -375,3 +378,26 @@ def test_many_narrow_multiband_pairs_run_bands_in_order(engine, mode, fe):
     reft = O.oracle_batch(pb, [H[k] for k in sub_idx], [V[k] for k in sub_idx], traceback=True)
     for i, k in enumerate(sub_idx):
         assert out.pair_segments(k) == reft.segments[i], k
+
+
+@pytest.mark.parametrize("fe", [0, 9])
+def test_chunked_large_score_batch(engine, fe):
+    """450,000 pairs, score only: gba_align_batch plans and runs the batch as contiguous chunks
+    (each planned while the previous one runs); scores, ends and statuses against the oracle,
+    including a few pairs that need 32-bit cells."""
+    import seqan_gb300 as sg
+    rng = np.random.default_rng(1200 + fe)
+    H = [rng.integers(0, 4, int(L)).astype(np.uint8) for L in rng.integers(20, 41, 450000)]
+    V = [h.copy() for h in H]
+    for v in V[::3]:
+        sub = rng.random(len(v)) < 0.1
+        v[sub] = (v[sub] + 1) % 4
+    for k in (5, 230000, 449999):         # past the exact int16 range: promoted
+        H[k] = rng.integers(0, 4, 9500).astype(np.uint8)
+        V[k] = rng.integers(0, 4, 9400).astype(np.uint8)
+    cfg = sg.AlignConfig(bool(fe & 1), bool(fe & 2), bool(fe & 4), bool(fe & 8))
+    out = sg.align_codes(H, V, sg.Score(2, -4, -1, -6, dtype=np.int16), config=cfg, alphabet_size=4)
+    ref = O.oracle_batch(O.Problem("global", fe, None, 2, -4, -6, -1, None, 32), H, V)
+    assert np.array_equal(out.score, ref.score)
+    assert np.array_equal(out.end_h, ref.end_h) and np.array_equal(out.end_v, ref.end_v)
+    assert out.status[[5, 230000, 449999]].tolist() == [2, 2, 2] and (out.status == 2).sum() == 3
