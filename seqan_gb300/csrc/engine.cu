@@ -177,6 +177,7 @@ struct gba_plan {
 
 struct gba_context {
     std::map<int64_t, int> tuning;  // batch shape -> packed-kernel variant (autotuner results)
+    std::map<const void *, int64_t> grid_cache;   // kernel -> resident blocks on this device
     int device = 0;
     int64_t budget = 0;
     cudaStream_t stream = nullptr;
@@ -436,14 +437,19 @@ void launch_dp16(int v, bool affine, int grid, const Dp16Args &a, cudaStream_t s
 #undef GBA_L16
 }
 
-// Resident blocks of a persistent kernel on this device (all SMs x blocks per SM).
+// Resident blocks of a persistent kernel on this device (all SMs x blocks per SM); the
+// occupancy queries are cached per context (they do not change).
 int64_t persistent_grid(gba_context *ctx, const void *fn)
 {
+    auto it = ctx->grid_cache.find(fn);
+    if (it != ctx->grid_cache.end()) return it->second;
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    return int64_t(sms) * per_sm;
+    const int64_t g = int64_t(sms) * per_sm;
+    ctx->grid_cache.emplace(fn, g);
+    return g;
 }
 
 const void *warp_fn(bool a, bool l, bool m, bool t);
@@ -541,8 +547,9 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     std::vector<int64_t> tbytes(plan->traceback ? N : 0);
     std::vector<int64_t> c16(nth + 1, 0), cot(nth + 1, 0), ctr(nth + 1, 0);
     int64_t first_bad = N, cells = 0;
+    double cells16 = 0;   // cells of the packed-path pairs
     const int fe_all = plan->local ? 15 : p->free_ends;
-#pragma omp parallel num_threads(nth) reduction(+ : cells) reduction(min : first_bad)
+#pragma omp parallel num_threads(nth) reduction(+ : cells, cells16) reduction(min : first_bad)
     {
         const int t = omp_get_thread_num();
         const int64_t k0 = N * t / nth, k1 = N * (t + 1) / nth;
@@ -594,6 +601,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                 key[k] = uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL));
                 cls[k] = 1;
                 ++n16;
+                cells16 += double(d.m) * d.n;
             } else {
                 const int64_t strips = (d.n + STRIP_ROWS - 1) / STRIP_ROWS;
                 key[k] = uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL));
@@ -686,9 +694,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             nsplit = int64_t(idx16.size());
         } else {
             const double resident = double(persistent_grid(ctx, dp16_fn(0, plan->affine))) * kBlock;
-            double total = 0;
-            for (int32_t k : idx16) total += double(desc[k].m) * desc[k].n;
-            const double per_thread = total / 2 / resident;
+            const double per_thread = cells16 / 2 / resident;
             while (nsplit < int64_t(idx16.size()) && double(desc[idx16[nsplit]].m) * desc[idx16[nsplit]].n > per_thread)
                 ++nsplit;
             nsplit -= nsplit % 32;
