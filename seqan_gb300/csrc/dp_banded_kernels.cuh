@@ -238,11 +238,23 @@ struct BandedPair {
             }
             vw[q] = w;
         }
+        // Codes of the next column are loaded one column ahead (their latency hides behind a
+        // column of W cells): H, the last row's V code and the window's incoming V code.
+        int hcN = H[hIt];
+        int vLowN = V[ve];                               // V[ve + 1 - 1] of the first fast column
+        int vInN = (vb + FW < n) ? V[vb + FW] : 0;       // incoming window code after it
         for (; hIt != hMid; ++hIt) {
             ++vb;
             ++ve;
             const int col = hIt + 1;
-            const int hc = H[col - 1];
+            const int hc = hcN;
+            const int vLow = vLowN;
+            const int vIn = vInN;
+            if (col < hMid) {
+                hcN = H[col];
+                vLowN = ve < n ? V[ve] : 0;
+                vInN = (vb + FW < n) ? V[vb + FW] : 0;
+            }
             const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
             int dS = Sr[0];
             int vS = INF, vF = INF;
@@ -309,7 +321,7 @@ struct BandedPair {
             }
             // Lower: diagonal or vertical (slot W - 1, row ve).
             {
-                const int vc = V[ve - 1];
+                const int vc = vLow;
                 const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
                 const int inter = dS + sub;
                 int s, f = INF;
@@ -347,8 +359,7 @@ struct BandedPair {
             // Shift the V window by one row: code k <- code k + 1, the new last code from V.
 #pragma unroll
             for (int q = 0; q < NW - 1; ++q) vw[q] = __funnelshift_r(vw[q], vw[q + 1], 8);
-            const int idx = vb + FW - 1;
-            vw[NW - 1] = (vw[NW - 1] >> 8) | (uint32_t(idx < n ? V[idx] : 0) << 24);
+            vw[NW - 1] = (vw[NW - 1] >> 8) | (uint32_t(vIn) << 24);   // V[vb + FW - 1]
         }
 #pragma unroll
         for (int k = 0; k < FW - 1; ++k)
