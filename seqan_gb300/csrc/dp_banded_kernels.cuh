@@ -44,8 +44,17 @@ struct BandArgs {
 
 constexpr int kBandFastW = 40;   // widest band of the middle-phase fast path
 
-// Bytes between the trace columns of a band of W slots.
+// Bytes of a trace column of a band of W slots (W rounded up to 16).
 __host__ __device__ inline int band_trace_stride(int W) { return (W + 15) & ~15; }
+
+// Banded trace layout, interleaved by lane: the 32 pairs of a warp share one region, in which
+// 16-byte chunk q of column col of the pair in lane l lies at ((col * Wt / 16 + q) * 32 + l) * 16,
+// so a warp writes a chunk of its 32 columns with one 512-byte store.  A pair's trace_off points
+// at its lane's first chunk; relative to it, byte k of column col is at:
+__host__ __device__ inline int64_t band_trace_pos(int Wt, int col, int k)
+{
+    return (int64_t(col) * (Wt >> 4) + (k >> 4)) * 512 + (k & 15);
+}
 
 enum { BCOL_INITIAL = 0, BCOL_INNER = 1, BCOL_FINAL = 2 };
 enum { BLOC_FULL = 0, BLOC_TOP = 1, BLOC_MIDDLE = 2, BLOC_BOTTOM = 3 };
@@ -186,7 +195,7 @@ struct BandedPair {
         if (inside) {
             S[k] = s;
             E[k] = e;
-            if (TRACE) T[int64_t(col) * Wt + k] = uint8_t(tv);
+            if (TRACE) T[band_trace_pos(Wt, col, k)] = uint8_t(tv);
         }
         if (tracked) {
             if (inside) Fs[k] = f;
@@ -348,12 +357,12 @@ struct BandedPair {
                     scout(s, INF, f, col, ve);
                 }
                 if (TRACE) {
-                    uint8_t *Tc = T + int64_t(col) * Wt;
 #pragma unroll
                     for (int q = 0; q < NT / 4; ++q)
                         if (16 * q < W)
-                            reinterpret_cast<uint4 *>(Tc)[q] = make_uint4(tw[4 * q], tw[4 * q + 1], tw[4 * q + 2], tw[4 * q + 3]);
-                    Tc[WL] = uint8_t(tv);
+                            *reinterpret_cast<uint4 *>(T + band_trace_pos(Wt, col, 16 * q)) =
+                                make_uint4(tw[4 * q], tw[4 * q + 1], tw[4 * q + 2], tw[4 * q + 3]);
+                    T[band_trace_pos(Wt, col, WL)] = uint8_t(tv);
                 }
             }
             // Shift the V window by one row: code k <- code k + 1, the new last code from V.
@@ -446,7 +455,7 @@ struct BandedPair {
                 int s = prev + (MATRIX ? smat[((H[ih] & 31) << 5) | (V[iv] & 31)] : (H[ih] == V[iv] ? a.match : a.mismatch));
                 int tv = TV_DIAG;
                 if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
-                if (TRACE) T[int64_t(col) * Wt] = uint8_t(tv);
+                if (TRACE) T[band_trace_pos(Wt, col, 0)] = uint8_t(tv);
                 if (LOCAL) scout(s, INF, INF, col, row);
                 prev = s;
                 ++ih; ++iv;
@@ -456,7 +465,7 @@ struct BandedPair {
             int s = prev + (MATRIX ? smat[((H[ih] & 31) << 5) | (V[iv] & 31)] : (H[ih] == V[iv] ? a.match : a.mismatch));
             int tv = TV_DIAG;
             if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
-            if (TRACE) T[int64_t(col) * Wt] = uint8_t(tv);
+            if (TRACE) T[band_trace_pos(Wt, col, 0)] = uint8_t(tv);
             if (ih == ihEnd) {
                 if (iv == ivEnd) scout(s, INF, INF, col, row);
                 if (LOCAL || fBottom) scout(s, INF, INF, col, row);
@@ -600,7 +609,7 @@ __device__ __forceinline__ uint8_t trace_at_band(const uint8_t *base, int W, int
 {
     const int k = upper - col + row;
     if (k < 0 || k >= W) return TV_NONE;
-    return base[int64_t(col) * band_trace_stride(W) + k];
+    return base[band_trace_pos(band_trace_stride(W), col, k)];
 }
 
 }  // namespace gba

@@ -671,6 +671,26 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         sort_desc(keys, idx);
     }
     plan->num_slots = int64_t(idx.size());
+    // Banded traces are interleaved by lane within each warp of 32 slots (see band_trace_pos):
+    // a warp's region holds 32 x (its largest m + 1) columns of band_trace_stride(W) bytes.
+    if (p->band_on && plan->traceback && plan->num_slots > 0) {
+        const int Wt = band_trace_stride(p->band_upper - p->band_lower + 1);
+        const int64_t nw = (plan->num_slots + 31) / 32;
+        std::vector<int64_t> wsize(nw + 1, 0);
+#pragma omp parallel for num_threads(plan_threads(plan->num_slots)) schedule(static)
+        for (int64_t w = 0; w < nw; ++w) {
+            int maxm = -1;
+            for (int64_t s = 32 * w; s < std::min(plan->num_slots, 32 * w + 32); ++s)
+                if (idx[s] >= 0) maxm = std::max(maxm, desc[idx[s]].m);
+            wsize[w + 1] = maxm < 0 ? 0 : int64_t(maxm + 1) * Wt * 32;
+        }
+        for (int64_t w = 0; w < nw; ++w) wsize[w + 1] += wsize[w];
+#pragma omp parallel for num_threads(plan_threads(plan->num_slots)) schedule(static)
+        for (int64_t s = 0; s < plan->num_slots; ++s)
+            if (idx[s] >= 0) desc[idx[s]].trace_off = wsize[s / 32] + (s % 32) * 16;
+        trace_off = wsize[nw];
+        plan->trace_total = trace_off;
+    }
     // Large pairs of the warp layout (a prefix of the cost-sorted order) get the warp-walked
     // traceback; the key is strips of STRIP_ROWS rows x (m + 1) columns.
     plan->num_tiled_tb = 0;
