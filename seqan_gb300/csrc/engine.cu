@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -131,6 +132,7 @@ struct gba_plan {
     std::vector<uint32_t> h_keys16, h_keys, h_key;
     std::vector<int32_t> h_idx16, h_idx;
     std::vector<uint8_t> h_cls;
+    std::vector<Slot16> h_slots16;
     bool owned = true;
     void release()
     {
@@ -458,7 +460,7 @@ const void *warp_fn(bool a, bool l, bool m, bool t);
 int plan_threads(int64_t work)
 {
     if (work < 16384) return 1;
-    return int(std::max<int64_t>(1, std::min<int64_t>({int64_t(omp_get_max_threads()), 16, work / 8192})));
+    return int(std::max<int64_t>(1, std::min<int64_t>({int64_t(omp_get_max_threads()), 16, work / 4096})));
 }
 
 // Phase timer of build_plan: with GBA_PLAN_PROFILE set in the environment, each plan prints
@@ -539,6 +541,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // (packed path / other / invalid), sort key and trace bytes.  Then each chunk appends its
     // pairs to the class lists and assigns trace offsets at its prefix-summed position, so the
     // lists are in input order exactly as a serial pass makes them.
+    timer.mark("setup");
     const int nth = plan_threads(N);
     auto &cls = plan->h_cls;
     auto &key = plan->h_key;
@@ -714,14 +717,18 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             nsplit = int64_t(idx16.size());
         } else {
             const double resident = double(persistent_grid(ctx, dp16_fn(0, plan->affine))) * kBlock;
+            // keys16 (descending) are strips of rows16 rows x (m + 1) columns: about a slot's
+            // cells / rows16, so the split prefix ends at the first key below that threshold.
             const double per_thread = cells16 / 2 / resident;
-            while (nsplit < int64_t(idx16.size()) && double(desc[idx16[nsplit]].m) * desc[idx16[nsplit]].n > per_thread)
-                ++nsplit;
+            const uint32_t kthr = uint32_t(std::min<double>(per_thread / plan->rows16, 4e9));
+            nsplit = int64_t(std::upper_bound(keys16.begin(), keys16.end(), kthr, std::greater<uint32_t>()) -
+                             keys16.begin());
             nsplit -= nsplit % 32;
         }
     }
     const int64_t rest16 = int64_t(idx16.size()) - nsplit;
-    std::vector<Slot16> slots16(size_t(nsplit + (rest16 + 1) / 2));
+    auto &slots16 = plan->h_slots16;
+    slots16.resize(size_t(nsplit + (rest16 + 1) / 2));
 #pragma omp parallel for num_threads(plan_threads(int64_t(slots16.size()))) schedule(static)
     for (size_t q = 0; q < slots16.size(); ++q) {
         Slot16 &sl = slots16[q];
@@ -771,6 +778,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->codes_total = ctot;
     plan->bnd16_total = btot;
     plan->tasks16 = int32_t(warps16);
+    timer.mark("slots16");
 
     // Warp path: tasks in the length-sorted pair order.  A pair's bands run as separate,
     // pipelined tasks (pair, b) when the pair is wide or the batch too small to fill the GPU
@@ -819,6 +827,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     }
     plan->scratch_total = scr;
 
+    timer.mark("warp+strip");
     // Segment / CIGAR slots: at most m + n + 4 records per pair.
     std::vector<int64_t> seg_off(plan->traceback ? N + 1 : 0, 0), cig_off;
     plan->seg_slots_total = 0;
