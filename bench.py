@@ -58,6 +58,15 @@ KERNEL_NAMES = [(2, "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)"),
                 (1, "k_dp_strip (one pair per thread, int32)")]
 
 
+def measured_hbm_gbs():
+    """The measured HBM copy rate of this GPU pool (MEASURED_PEAKS.json at the repo root), or None."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def kernel_label(bits: int) -> str:
     """Names of the DP kernels a run launched (gba_stats.dp_kernels), the main one first."""
     return " + ".join(name for bit, name in KERNEL_NAMES if bits & bit) or "none"
@@ -501,6 +510,16 @@ def main():
     if spec.traceback:
         roofline["trace_bytes_per_launch"] = int(st_last.trace_bytes)
         roofline["trace_write_gbs"] = st_last.trace_bytes / (dp_avg_ms * 1e-3) / 1e9
+        # Traceback configs also count the algorithmic trace (0.5 byte per cell: a 2-bit source
+        # of S and one open/extend bit each for E and F) against the measured HBM copy rate;
+        # the bound is whichever fraction is larger.
+        hbm = measured_hbm_gbs()
+        if hbm:
+            tr_frac = 0.5 * cells / (dp_avg_ms * 1e-3) / 1e9 / hbm
+            roofline["trace_hbm"] = {"algorithmic_bytes_per_cell": 0.5, "achieved_gbs": 0.5 * cells / (dp_avg_ms * 1e-3) / 1e9,
+                                     "peak_gbs": hbm, "frac": tr_frac,
+                                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+            roofline["frac_traceback_max"] = max(roofline["frac"] or 0.0, tr_frac)
         roofline["traceback_and_output_ms"] = tb_avg_ms
     line = {"metric": "GCUPS, batched affine DNA align", "value": value, "unit": "GCUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,

@@ -10,6 +10,10 @@
 //   localAlignmentScore (exec, setH, setV, score [, lowerDiag, upperDiag])
 //   globalAlignment     (exec, gapsSetH, gapsSetV, score [, AlignConfig] [, lowerDiag, upperDiag])
 //   localAlignment      (exec, gapsSetH, gapsSetV, score [, lowerDiag, upperDiag])
+//   globalAlignment     (exec, alignSet, score [, AlignConfig] [, lowerDiag, upperDiag])
+//   localAlignment      (exec, alignSet, score [, lowerDiag, upperDiag])   (StringSet<Align>:
+//                        row 0 = H, row 1 = V; align/global_alignment_unbanded.h:894-952,
+//                        align/local_alignment_unbanded.h:405-439)
 //
 // so switching a call from ExecutionPolicy<Parallel, Vectorial> is a change of the policy
 // type only.  Sequences go to the engine as ordValue codes (the layout of
@@ -196,16 +200,40 @@ using AlphabetOf = typename Value<typename Value<TSet>::Type>::Type;
 template <typename TGapsSet>
 using GapsAlphabetOf = typename Value<typename Source<typename Value<TGapsSet>::Type>::Type>::Type;
 
+// Aligns pair k = (source(rowH(k)), source(rowV(k))) for k < count and rebuilds both Gaps rows.
+template <typename TScoreValue, typename TScoreSpec, typename TAlphabet, typename TRowH, typename TRowV>
+String<TScoreValue> run_rows(size_t count, TRowH rowH, TRowV rowV, Score<TScoreValue, TScoreSpec> const &sc, int mode,
+                             int fe, Band band)
+{
+    Codes h, v;
+    for (size_t k = 0; k < count; ++k) {
+        h.add(source(rowH(k)));
+        v.add(source(rowV(k)));
+    }
+    std::vector<String<TraceSegment_<unsigned, unsigned>>> segs;
+    String<TScoreValue> out = run<TScoreValue, TAlphabet>(h, v, false, sc, mode, fe, band, &segs);
+    for (size_t k = 0; k < count; ++k) _adaptTraceSegmentsTo(rowH(k), rowV(k), segs[k]);
+    return out;
+}
+
 template <typename TScoreValue, typename TScoreSpec, typename TGapsSetH, typename TGapsSetV>
 String<TScoreValue> run_gaps(TGapsSetH &gapsH, TGapsSetV &gapsV, Score<TScoreValue, TScoreSpec> const &sc, int mode,
                              int fe, Band band)
 {
     if (length(gapsH) != length(gapsV)) throw std::runtime_error("gapsH and gapsV differ in length");
-    std::vector<String<TraceSegment_<unsigned, unsigned>>> segs;
-    String<TScoreValue> out = run<TScoreValue, GapsAlphabetOf<TGapsSetH>>(
-        flatten_gaps(gapsH), flatten_gaps(gapsV), false, sc, mode, fe, band, &segs);
-    for (size_t k = 0; k < length(gapsH); ++k) _adaptTraceSegmentsTo(gapsH[k], gapsV[k], segs[k]);
-    return out;
+    return run_rows<TScoreValue, TScoreSpec, GapsAlphabetOf<TGapsSetH>>(
+        length(gapsH), [&](size_t k) -> decltype(gapsH[0]) & { return gapsH[k]; },
+        [&](size_t k) -> decltype(gapsV[0]) & { return gapsV[k]; }, sc, mode, fe, band);
+}
+
+// StringSet<Align>: row 0 is H, row 1 is V (align/global_alignment_unbanded.h:894-952).
+template <typename TScoreValue, typename TScoreSpec, typename TSeq, typename TAlignSpec, typename TSetSpec>
+String<TScoreValue> run_aligns(StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &set, Score<TScoreValue, TScoreSpec> const &sc,
+                               int mode, int fe, Band band)
+{
+    return run_rows<TScoreValue, TScoreSpec, typename Value<TSeq>::Type>(
+        length(set), [&](size_t k) -> decltype(row(set[0], 0)) & { return row(set[k], 0); },
+        [&](size_t k) -> decltype(row(set[0], 1)) & { return row(set[k], 1); }, sc, mode, fe, band);
 }
 
 }  // namespace gb300_impl
@@ -352,6 +380,58 @@ String<TScoreValue> localAlignment(ExecutionPolicy<GB300, TVec> const &, TGapsSe
                                    Score<TScoreValue, TScoreSpec> const &sc)
 {
     return gb300_impl::run_gaps(gapsH, gapsV, sc, GBA_LOCAL, 0, gb300_impl::Band{});
+}
+
+// ---- globalAlignment / localAlignment over StringSet<Align> ------------------------------
+
+template <typename TVec, typename TSeq, typename TAlignSpec, typename TSetSpec, typename TScoreValue, typename TScoreSpec,
+          bool TOP, bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &, StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &aligns,
+                                    Score<TScoreValue, TScoreSpec> const &sc,
+                                    AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac, int lowerDiag,
+                                    int upperDiag)
+{
+    return gb300_impl::run_aligns(aligns, sc, GBA_GLOBAL, gb300_impl::free_ends(ac),
+                                  gb300_impl::Band{true, lowerDiag, upperDiag});
+}
+
+template <typename TVec, typename TSeq, typename TAlignSpec, typename TSetSpec, typename TScoreValue, typename TScoreSpec,
+          bool TOP, bool LEFT, bool RIGHT, bool BOTTOM, typename TACSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &, StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &aligns,
+                                    Score<TScoreValue, TScoreSpec> const &sc,
+                                    AlignConfig<TOP, LEFT, RIGHT, BOTTOM, TACSpec> const &ac)
+{
+    return gb300_impl::run_aligns(aligns, sc, GBA_GLOBAL, gb300_impl::free_ends(ac), gb300_impl::Band{});
+}
+
+template <typename TVec, typename TSeq, typename TAlignSpec, typename TSetSpec, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &exec,
+                                    StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &aligns,
+                                    Score<TScoreValue, TScoreSpec> const &sc, int lowerDiag, int upperDiag)
+{
+    return globalAlignment(exec, aligns, sc, AlignConfig<>(), lowerDiag, upperDiag);
+}
+
+template <typename TVec, typename TSeq, typename TAlignSpec, typename TSetSpec, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> globalAlignment(ExecutionPolicy<GB300, TVec> const &exec,
+                                    StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &aligns,
+                                    Score<TScoreValue, TScoreSpec> const &sc)
+{
+    return globalAlignment(exec, aligns, sc, AlignConfig<>());
+}
+
+template <typename TVec, typename TSeq, typename TAlignSpec, typename TSetSpec, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> localAlignment(ExecutionPolicy<GB300, TVec> const &, StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &aligns,
+                                   Score<TScoreValue, TScoreSpec> const &sc, int lowerDiag, int upperDiag)
+{
+    return gb300_impl::run_aligns(aligns, sc, GBA_LOCAL, 0, gb300_impl::Band{true, lowerDiag, upperDiag});
+}
+
+template <typename TVec, typename TSeq, typename TAlignSpec, typename TSetSpec, typename TScoreValue, typename TScoreSpec>
+String<TScoreValue> localAlignment(ExecutionPolicy<GB300, TVec> const &, StringSet<Align<TSeq, TAlignSpec>, TSetSpec> &aligns,
+                                   Score<TScoreValue, TScoreSpec> const &sc)
+{
+    return gb300_impl::run_aligns(aligns, sc, GBA_LOCAL, 0, gb300_impl::Band{});
 }
 
 }  // namespace seqan2

@@ -50,8 +50,23 @@ int main()
     String<int> l = localAlignment(gpu, gapsH, gapsV, sc32);
     String<int> m = localAlignment(gpu, gapsH, gapsV, sc32, -4, 4);
 
+    typedef Align<Dna5String> TAlign;
+    StringSet<TAlign> aligns;
+    for (size_t q = 0; q < length(setH); ++q) {
+        TAlign al;
+        resize(rows(al), 2);
+        assignSource(row(al, 0), setH[q]);
+        assignSource(row(al, 1), setV[q]);
+        appendValue(aligns, al);
+    }
+    String<int16_t> n1 = globalAlignment(gpu, aligns, sc16);
+    String<int> n2 = globalAlignment(gpu, aligns, sc32, AlignConfig<true, false, false, true>(), -3, 5);
+    String<int> n3 = localAlignment(gpu, aligns, sc32);
+    String<int> n4 = localAlignment(gpu, aligns, sc32, -2, 2);
+
     std::cout << a[0] << ' ' << b[0] << ' ' << c[0] << ' ' << d[0] << ' ' << e[1] << ' ' << f[0] << ' ' << g[0] << ' '
-              << h[0] << ' ' << i[0] << ' ' << j[0] << ' ' << k[0] << ' ' << l[0] << ' ' << m[0] << '\n'
-              << gapsH[0] << '\n' << gapsV[0] << '\n';
+              << h[0] << ' ' << i[0] << ' ' << j[0] << ' ' << k[0] << ' ' << l[0] << ' ' << m[0] << ' ' << n1[0] << ' '
+              << n2[0] << ' ' << n3[0] << ' ' << n4[0] << '\n'
+              << gapsH[0] << '\n' << gapsV[0] << '\n' << aligns[0] << '\n';
     return 0;
 }
