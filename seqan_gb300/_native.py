@@ -32,6 +32,7 @@ GBA_NOALLOC_SCRATCH_BYTES = 64 << 20
 GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16, GBA_FLAG_PLAIN_BUCKETS, GBA_FLAG_NO_GRAPH, GBA_FLAG_AUTOTUNE = 1, 2, 4, 8, 16
 GBA_FLAG_PACKED = 32
 GBA_FLAG_PACKED_SPLIT, GBA_FLAG_PACKED_NO_SPLIT = 64, 128
+GBA_KERNEL_STRIP, GBA_KERNEL_PACKED, GBA_KERNEL_WARP, GBA_KERNEL_BANDED = 1, 2, 4, 8
 
 # Every symbol include/seqan_gb300.h declares.
 EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", "gba_align_batch",
