@@ -45,7 +45,14 @@ WORKLOADS = {
     "banded_reads_1m": "1000000 reads of 150 bp (2% subs, 0.2% indels) vs 170 bp windows of a 10 Mbp "
                        "reference, AlignConfig<true,false,false,true>, band [-6,26], Score(2,-4,-1,-6) int16, "
                        "score + CIGAR",
+    "xdrop_reads_1m": "1000000 seeds: 150 bp reads (3% subs, 0.3% indels) vs 250 bp windows of a 10 Mbp "
+                      "reference, one 19-mer seed per read on its true diagonal; extendSeed EXTEND_BOTH, "
+                      "GappedXDrop, Score<int,Simple>(1,-2,-2), scoreDropOff 20; seeds + extension scores",
 }
+SEED_WORKLOADS = {"xdrop_reads_1m"}
+# Integer ops of one x-drop cell: max(up, left) + gap, diagonal + score, the max of the two, the
+# drop-off compare and the anti-diagonal best (add and max each count one).
+XDROP_OPS_PER_CELL = 6
 # Algorithmic integer ops per cell (add and max each count one): affine global 9
 # (E: 2 adds + 1 max, F: 2 + 1, S: 1 add + 2 max), affine local 10 (+ max with 0),
 # linear global 5, linear local 6.
@@ -238,6 +245,206 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def make_seed_workload(name: str, seed_offset: int = 0):
+    from seqan_gb300 import workloads as W
+    if name == "xdrop_reads_1m":
+        wins, reads, seeds, _ = W.seed_windows(1_000_000, seed=6 + seed_offset)
+        return wins, reads, seeds
+    raise SystemExit(f"unknown seed workload {name}")
+
+
+def seed_problem():
+    from oracle import oracle as O
+    return O.SeedProblem(O.GAPPED_XDROP, O.EXTEND_BOTH, 1, -2, -2, 20)
+
+
+def seed_cpu_time(wins, reads, seeds, n, threads):
+    from oracle import oracle as O
+    arr = O.seeds_array(seeds[:n])
+    t0 = time.perf_counter()
+    O.oracle_extend_seeds(seed_problem(), wins[:n], reads[:n], arr, threads=threads)
+    return time.perf_counter() - t0
+
+
+def seed_cpu_baseline(wins, reads, seeds, seconds_target: float = 10.0):
+    """The oracle's seed extension (OpenMP over all host threads) on a sample of the seeds."""
+    threads = os.cpu_count() or 1
+    n = min(len(seeds), 20_000)
+    dt = seed_cpu_time(wins, reads, seeds, n, threads)
+    n = int(min(len(seeds), max(n, n * seconds_target / max(dt, 1e-3) / 3)))
+    best = min(seed_cpu_time(wins, reads, seeds, n, threads) for _ in range(2))
+    return {"value": n / best / 1e6, "unit": "Mseeds/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} seeds of the workload, orc_extend_seeds (oracle/seqan_oracle.c) with OpenMP "
+                      f"over {threads} threads, best of 2", "seeds": n, "seconds": best}
+
+
+def run_seed_reference(args):
+    wins, reads, seeds = make_seed_workload(args.workload)
+    threads = os.cpu_count() or 1
+    n = min(len(seeds), args.ref_pairs * 10)
+    for _ in range(args.warmup):
+        seed_cpu_time(wins, reads, seeds, n, threads)
+    times = [seed_cpu_time(wins, reads, seeds, n, threads) for _ in range(args.steps)]
+    rate = n * len(times) / sum(times) / 1e6
+    line = {"metric": "Mseeds/s, batched gapped x-drop seed extension", "value": rate, "unit": "Mseeds/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "seeds_per_step": n, "description": WORKLOADS[args.workload]},
+            "cpu_baseline": {"value": rate, "unit": "Mseeds/s", "cores": threads, "kind": "port",
+                             "sample": f"first {n} seeds of the workload per step; the reference's extendSeed "
+                                       "restated in oracle/seqan_oracle.c (pinned to the compiled reference), "
+                                       "OpenMP over the host threads"},
+            "e2e": {"value": rate, "unit": "Mseeds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_seed_bench(args, rank, world, local_rank, dist):
+    """Seed extension: value with seeds and sequences resident in HBM (gba_extend_seeds_device),
+    e2e through gba_extend_seeds with pinned host buffers."""
+    from seqan_gb300 import _native as N
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    h = ctx.handle
+    from oracle import oracle as O
+    wins, reads, seeds = make_seed_workload(args.workload, seed_offset=rank)
+    if args.pairs:
+        wins, reads, seeds = wins[:args.pairs], reads[:args.pairs], seeds[:args.pairs]
+    arr = O.seeds_array(seeds)
+    ns = len(arr)
+    sh, oh = concat(wins)
+    sv, ov = concat(reads)
+    max_v = int((ov[1:] - ov[:-1]).max())
+    sp = seed_problem()
+    params = N.GbaExtendParams(sp.method, sp.direction, sp.xdrop, sp.match, sp.mismatch, sp.gap, None, 0, 0)
+
+    def pinned(nbytes):
+        p = C.c_void_p()
+        ctx.check(L.gba_host_alloc(h, C.byref(p), nbytes), "gba_host_alloc")
+        return p
+
+    def device(nbytes):
+        p = C.c_void_p()
+        ctx.check(L.gba_device_alloc(h, C.byref(p), nbytes), "gba_device_alloc")
+        return p
+
+    def as_np(ptr, count, dtype):
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dtype))), shape=(count,))
+
+    host = {}
+    for name, a in (("sh", sh), ("oh", oh), ("sv", sv), ("ov", ov), ("seeds", arr)):
+        host[name] = pinned(a.nbytes)
+        as_np(host[name], a.size, a.dtype)[:] = a.reshape(-1)
+    host["io"] = pinned(arr.nbytes)
+    host["scores"] = pinned(ns * 8)
+    dev = {name: device(a.nbytes) for name, a in (("sh", sh), ("oh", oh), ("sv", sv), ("ov", ov), ("seeds0", arr),
+                                                    ("seeds", arr))}
+    dev["scores"] = device(ns * 8)
+    for name in ("sh", "oh", "sv", "ov"):
+        ctx.check(L.gba_copy_to_device(h, dev[name], host[name], {"sh": sh, "oh": oh, "sv": sv, "ov": ov}[name].nbytes),
+                  "copy")
+    ctx.check(L.gba_copy_to_device(h, dev["seeds0"], host["seeds"], arr.nbytes), "copy")
+    dbatch = N.GbaSeedBatch(len(wins), dev["sh"], dev["oh"], len(reads), dev["sv"], dev["ov"], ns, None, None, max_v)
+    hbatch = N.GbaSeedBatch(len(wins), host["sh"], host["oh"], len(reads), host["sv"], host["ov"], ns, None, None, 0)
+    flush_bytes = 256 << 20
+    d_flush, p_flush = device(flush_bytes), pinned(flush_bytes)
+
+    def reset_and_flush():
+        ctx.check(L.gba_copy_to_device(h, d_flush, p_flush, flush_bytes), "flush")
+        ctx.check(L.gba_copy_to_device(h, dev["seeds"], host["seeds"], arr.nbytes), "seeds")
+        ctx.check(L.gba_synchronize(h), "sync")
+
+    def run_device():
+        ctx.check(L.gba_extend_seeds_device(h, C.byref(params), C.byref(dbatch), dev["seeds"], dev["scores"]), "ext")
+
+    for _ in range(args.warmup):
+        reset_and_flush()
+        run_device()
+        ctx.check(L.gba_synchronize(h), "sync")
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    sampler.start()
+    step_ms = []
+    ms = C.c_float()
+    for _ in range(args.steps):
+        reset_and_flush()
+        ctx.check(L.gba_timer_start(h), "timer")
+        run_device()
+        ctx.check(L.gba_timer_stop(h, C.byref(ms)), "timer")
+        step_ms.append(ms.value)
+    ctx.check(L.gba_synchronize(h), "sync")
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    total_ms = sum(step_ms)
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ns * world * args.steps / (total_ms * 1e-3) / 1e6
+    # Parity spot check of the device run against the oracle (first 20,000 seeds).
+    out = np.zeros_like(arr)
+    ctx.check(L.gba_copy_to_host(h, out.ctypes.data, dev["seeds"], arr.nbytes), "d2h")
+    k = min(ns, 20_000)
+    ref, _ = O.oracle_extend_seeds(sp, wins[:k], reads[:k], arr[:k])
+    parity = bool(np.array_equal(out[:k], ref))
+
+    # e2e: the host-buffer C-ABI call, seeds copied in and back every step.
+    def run_host():
+        io = as_np(host["io"], arr.size, np.int64)
+        io[:] = arr.reshape(-1)
+        t0 = time.perf_counter()
+        ctx.check(L.gba_extend_seeds(h, C.byref(params), C.byref(hbatch), host["io"], host["scores"]), "e2e")
+        return time.perf_counter() - t0
+
+    for _ in range(max(1, args.warmup)):
+        run_host()
+    e2e_s = []
+    for _ in range(args.steps):
+        reset_and_flush()
+        e2e_s.append(run_host())
+    st = ctx.stats()
+    e2e = ns * world * len(e2e_s) / sum(e2e_s) / 1e6
+    peak = C.c_double()
+    ctx.check(L.gba_measure_int_peak(h, C.byref(peak)), "int peak")
+    kernel_ms = st.dp_kernel_ms
+    ops = st.cells * XDROP_OPS_PER_CELL
+    achieved = ops / (kernel_ms * 1e-3) / 1e12
+    line = {"metric": "Mseeds/s, batched gapped x-drop seed extension", "value": value, "unit": "Mseeds/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload if not args.pairs else f"{args.workload} (first {ns} seeds)",
+                       "description": WORKLOADS[args.workload], "seeds": ns, "cells_per_step": int(st.cells),
+                       "l2": "flushed (256 MiB write) between timed steps; seeds restored before each step",
+                       "parallelism": f"replicas x{world} (seeds are independent)",
+                       "shared_memory_ring": int(st.seed_ring), "fallback_seeds": int(st.seed_fallbacks)},
+            "e2e": {"value": e2e, "unit": "Mseeds/s", "h2d_bytes_per_step": int(sh.nbytes + sv.nbytes + oh.nbytes +
+                                                                               ov.nbytes + arr.nbytes),
+                    "d2h_bytes_per_step": int(arr.nbytes + ns * 8), "ms_per_step": 1e3 * sum(e2e_s) / len(e2e_s),
+                    "last_call": {"kernel_ms": kernel_ms, "call_ms": st.call_ms}},
+            "gpu_launches": args.steps * int(st.kernel_launches),
+            "roofline": {"bound": "int32", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "kernel": f"k_extend_gapped<{int(st.seed_ring)}> (persistent, one seed per thread, "
+                                   "anti-diagonal and residue rings in shared memory) + fallback levels + "
+                                   "k_apply_gapped",
+                         "ops_per_cell": XDROP_OPS_PER_CELL, "gcups": st.cells / (kernel_ms * 1e-3) / 1e9,
+                         "kernel_ms": kernel_ms,
+                         "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"},
+            "clocks": clocks, "parity_first_20000_vs_oracle": parity}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = seed_cpu_baseline(wins, reads, seeds)
+    for p in list(dev.values()) + [d_flush]:
+        L.gba_device_free(h, p)
+    for p in list(host.values()) + [p_flush]:
+        L.gba_host_free(h, p)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def serving_requests(n: int, seed: int):
     """Mixed-length affine DNA requests: 90% U[100,500], 9% U[1000,5000], 1% 10,000 bp; the
     partner has 5% substitutions and 1% indels."""
@@ -320,9 +527,18 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
-        run_reference(args, rank)
+        if args.workload in SEED_WORKLOADS:
+            if rank == 0:
+                run_seed_reference(args)
+        else:
+            run_reference(args, rank)
         if dist:
             dist.barrier()
+        return
+    if args.workload in SEED_WORKLOADS:
+        run_seed_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
         return
 
     import seqan_gb300 as sg

@@ -205,6 +205,9 @@ typedef struct {
     float host_plan_ms;        /* gba_align_batch: host planning time */
     float call_ms;             /* gba_align_batch: whole call, wall clock */
     int32_t dp_kernels;        /* GBA_KERNEL_* bits: the DP kernels the run launched */
+    int32_t seed_ring;         /* gba_extend_seeds, GappedXDrop: shared-memory ring slots per seed
+                                  (0: every seed ran on the global-memory fallback) */
+    int64_t seed_fallbacks;    /* gba_extend_seeds: seeds re-run on the fallback kernel */
 } gba_stats;
 
 /* DP kernels (gba_stats.dp_kernels). */
@@ -318,6 +321,69 @@ typedef struct {
 GBA_API int gba_align_score_noalloc(const gba_params *params, const gba_noalloc_batch *batch,
                                     int32_t *score, int32_t *end_h, int32_t *end_v,
                                     int32_t *pair_status, void *stream);
+
+/* --- Seed extension ---------------------------------------------------------------------
+ * extendSeed(seed, database, query, direction, MatchExtend) and
+ * extendSeed(seed, database, query, direction, scoringScheme, scoreDropOff,
+ *            UnGappedXDrop | GappedXDrop)
+ * (seeds/seeds_extension.h:181-218, 283-360, 780-835) over a batch of Seed<Simple> seeds, one
+ * call for the whole batch.  H is the database (horizontal) and V the query (vertical) side,
+ * as in the reference.  Each seed grows in place exactly as the reference's call grows it:
+ * begin/end positions in H and V and the lower/upper diagonals (H - V) its traces touched.
+ * Scores are Score<int, Simple>(match, mismatch, gap) or an alphabet_size^2 matrix
+ * (Score<int, ScoreMatrix<...>> with linear gap `gap`).  GappedXDrop requires gap < 0 (the
+ * reference asserts gap open == extend < 0) and every substitution score >= gap: below that the
+ * reference adds a substitution score to its `undefined` sentinel INT_MIN - gap and overflows
+ * int, so such schemes are refused with GBA_EUNSUPPORTED.  Gapped segments are limited to
+ * 2^29 residues (the reference computes 2 * max(rows, cols) in int). */
+enum { GBA_MATCH_EXTEND = 0, GBA_UNGAPPED_XDROP = 1, GBA_GAPPED_XDROP = 2 };
+/* ExtensionDirection (seeds/seeds_extension.h:123-129). */
+enum { GBA_EXTEND_NONE = 0, GBA_EXTEND_LEFT = 1, GBA_EXTEND_RIGHT = 2, GBA_EXTEND_BOTH = 3 };
+
+/* Seed<Simple, DefaultSeedConfig> (seeds/seeds_seed_simple.h:78-132): positions are size_t,
+ * diagonals signed, diagonal = H position - V position. */
+typedef struct {
+    int64_t begin_h, begin_v, end_h, end_v;
+    int64_t lower_diagonal, upper_diagonal;
+} gba_seed;
+
+typedef struct {
+    int32_t method;            /* GBA_MATCH_EXTEND / GBA_UNGAPPED_XDROP / GBA_GAPPED_XDROP */
+    int32_t direction;         /* GBA_EXTEND_* */
+    int32_t score_drop_off;    /* X of the x-drop methods; |X| < 2^30 */
+    int32_t match, mismatch;   /* Score<int, Simple> (ignored with a matrix) */
+    int32_t gap;               /* linear gap score */
+    const int32_t *matrix;     /* optional host alphabet_size^2 table, row = first argument of score() */
+    int32_t alphabet_size;     /* 1..32 with a matrix */
+    int32_t reserved;
+} gba_extend_params;
+
+/* Sequences and seeds.  Seed k lies on database seed_h[k] and query seed_v[k] (NULL: on
+ * database k / query k). */
+typedef struct {
+    int64_t num_h;
+    const uint8_t *seq_h;      /* concatenated database codes */
+    const int64_t *off_h;      /* num_h + 1 offsets */
+    int64_t num_v;
+    const uint8_t *seq_v;      /* concatenated query codes */
+    const int64_t *off_v;      /* num_v + 1 offsets */
+    int64_t num_seeds;
+    const int32_t *seed_h, *seed_v;
+    int64_t max_v_len;         /* gba_extend_seeds_device: a bound on every query length */
+} gba_seed_batch;
+
+/* Extends the seeds of a HOST batch in place (blocking).  scores: NULL or 2 per seed, the
+ * return values of the gapped left/right extensions (0 for an empty side, INT_MIN - gap when
+ * no cell stayed within the drop-off).  A seed outside its sequences fails the call with
+ * GBA_EINVAL, as does an empty UnGappedXDrop seed at the end of a sequence, whose left walk
+ * the reference starts past the end. */
+GBA_API int gba_extend_seeds(gba_context *ctx, const gba_extend_params *params, const gba_seed_batch *batch,
+                             gba_seed *seeds, int32_t *scores);
+/* The same on DEVICE pointers (batch arrays, seeds, scores; params->matrix stays a host
+ * pointer), asynchronous on the context stream; invalid seeds are left unchanged and reported
+ * by the next gba_synchronize as GBA_EINVAL. */
+GBA_API int gba_extend_seeds_device(gba_context *ctx, const gba_extend_params *params,
+                                    const gba_seed_batch *dev_batch, gba_seed *dev_seeds, int32_t *dev_scores);
 
 #ifdef __cplusplus
 }

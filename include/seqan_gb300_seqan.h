@@ -15,6 +15,16 @@
 //                        row 0 = H, row 1 = V; align/global_alignment_unbanded.h:894-952,
 //                        align/local_alignment_unbanded.h:405-439)
 //
+// and batch forms of extendSeed (seeds/seeds_extension.h:181-218, 283-360, 780-835), whose
+// reference form extends one Seed<Simple> per call:
+//
+//   extendSeed(exec, seeds, databases, queries, direction, MatchExtend())
+//   extendSeed(exec, seeds, databases, queries, direction, score, scoreDropOff,
+//              UnGappedXDrop() | GappedXDrop())
+//
+// seeds[k] lies on databases[k] / queries[k] (StringSets), or on the one database String and
+// queries[k];
+//
 // so switching a call from ExecutionPolicy<Parallel, Vectorial> is a change of the policy
 // type only.  Sequences go to the engine as ordValue codes (the layout of
 // StringSet<..., Owner<ConcatDirect<>>>); Score<T, Simple> passes its four values and
@@ -28,6 +38,7 @@
 #define SEQAN_GB300_SEQAN_H_
 
 #include <seqan/align.h>
+#include <seqan/seeds.h>
 
 #include <cstdint>
 #include <stdexcept>
@@ -432,6 +443,152 @@ String<TScoreValue> localAlignment(ExecutionPolicy<GB300, TVec> const &, StringS
                                    Score<TScoreValue, TScoreSpec> const &sc)
 {
     return gb300_impl::run_aligns(aligns, sc, GBA_LOCAL, 0, gb300_impl::Band{});
+}
+
+// ---- Seed extension ------------------------------------------------------------------------
+
+namespace gb300_impl {
+
+// The reference declares its tags as `typedef Tag<X_> const X`.
+template <typename T>
+struct is_gapped : std::is_same<T, typename std::remove_const<GappedXDrop>::type> {};
+template <typename T>
+struct is_xdrop_tag
+    : std::integral_constant<bool, is_gapped<T>::value ||
+                                       std::is_same<T, typename std::remove_const<UnGappedXDrop>::type>::value> {};
+
+template <typename TAlphabet, typename TScoreValue>
+void set_seed_score(gba_extend_params &p, std::vector<int32_t> &, Score<TScoreValue, Simple> const &sc)
+{
+    p.match = scoreMatch(sc);
+    p.mismatch = scoreMismatch(sc);
+    p.gap = scoreGapExtend(sc);
+    if (p.method == GBA_GAPPED_XDROP && scoreGapOpen(sc) != scoreGapExtend(sc))
+        throw std::runtime_error("GappedXDrop needs gap open == gap extend (seeds/seeds_extension.h:792-794)");
+}
+
+template <typename TAlphabet, typename TScoreValue, typename TSeqValue, typename TSpec>
+void set_seed_score(gba_extend_params &p, std::vector<int32_t> &table,
+                    Score<TScoreValue, ScoreMatrix<TSeqValue, TSpec>> const &sc)
+{
+    const int A = int(ValueSize<TAlphabet>::VALUE);
+    table.resize(size_t(A) * A);
+    for (int i = 0; i < A; ++i)
+        for (int j = 0; j < A; ++j) table[i * A + j] = int32_t(score(sc, TAlphabet(i), TAlphabet(j)));
+    p.matrix = table.data();
+    p.alphabet_size = A;
+    p.gap = scoreGapExtend(sc);
+    if (p.method == GBA_GAPPED_XDROP && scoreGapOpen(sc) != scoreGapExtend(sc))
+        throw std::runtime_error("GappedXDrop needs gap open == gap extend (seeds/seeds_extension.h:792-794)");
+}
+
+// Runs a batch; shared_db: every seed lies on databases[0].
+template <typename TConfig>
+void run_seeds(String<Seed<Simple, TConfig>> &seeds, Codes const &db, Codes const &qs, bool shared_db,
+               gba_extend_params const &p)
+{
+    const size_t n = length(seeds);
+    std::vector<gba_seed> es(n);
+    for (size_t k = 0; k < n; ++k) {
+        Seed<Simple, TConfig> const &s = seeds[k];
+        es[k] = gba_seed{int64_t(beginPositionH(s)), int64_t(beginPositionV(s)), int64_t(endPositionH(s)),
+                         int64_t(endPositionV(s)), int64_t(lowerDiagonal(s)), int64_t(upperDiagonal(s))};
+    }
+    std::vector<int32_t> ids_h(shared_db ? n : 0, 0);
+    gba_seed_batch b{};
+    b.num_h = int64_t(db.off.size()) - 1;
+    b.seq_h = db.seq.data();
+    b.off_h = db.off.data();
+    b.num_v = int64_t(qs.off.size()) - 1;
+    b.seq_v = qs.seq.data();
+    b.off_v = qs.off.data();
+    b.num_seeds = int64_t(n);
+    b.seed_h = shared_db ? ids_h.data() : nullptr;
+    check(gba_extend_seeds(context(), &p, &b, es.data(), nullptr), "gba_extend_seeds");
+    for (size_t k = 0; k < n; ++k) {
+        Seed<Simple, TConfig> &s = seeds[k];
+        setBeginPositionH(s, es[k].begin_h);
+        setBeginPositionV(s, es[k].begin_v);
+        setEndPositionH(s, es[k].end_h);
+        setEndPositionV(s, es[k].end_v);
+        setLowerDiagonal(s, es[k].lower_diagonal);
+        setUpperDiagonal(s, es[k].upper_diagonal);
+    }
+}
+
+template <typename TSeq>
+Codes flatten_one(TSeq const &s)
+{
+    Codes c;
+    c.add(s);
+    return c;
+}
+
+template <typename TAlphabet, typename TConfig, typename TScore>
+void extend_batch(String<Seed<Simple, TConfig>> &seeds, Codes const &db, Codes const &qs, bool shared_db,
+                  ExtensionDirection dir, int method, TScore const *sc, int dropOff)
+{
+    gba_extend_params p{};
+    p.method = method;
+    p.direction = int32_t(dir);
+    p.score_drop_off = dropOff;
+    std::vector<int32_t> table;
+    if (sc) set_seed_score<TAlphabet>(p, table, *sc);
+    run_seeds(seeds, db, qs, shared_db, p);
+}
+
+}  // namespace gb300_impl
+
+// Per-seed databases and queries (StringSets).
+template <typename TVec, typename TConfig, typename TDb, typename TDbSpec, typename TQ, typename TQSpec>
+void extendSeed(ExecutionPolicy<GB300, TVec> const &, String<Seed<Simple, TConfig>> &seeds,
+                StringSet<TDb, TDbSpec> const &databases, StringSet<TQ, TQSpec> const &queries,
+                ExtensionDirection direction, MatchExtend const &)
+{
+    typedef typename Value<TQ>::Type TAlphabet;
+    gb300_impl::extend_batch<TAlphabet>(seeds, gb300_impl::flatten(databases), gb300_impl::flatten(queries), false,
+                                        direction, GBA_MATCH_EXTEND, (Score<int, Simple> const *)nullptr, 0);
+}
+
+template <typename TVec, typename TConfig, typename TDb, typename TDbSpec, typename TQ, typename TQSpec,
+          typename TScoreValue, typename TScoreSpec, typename TXDropTag>
+void extendSeed(ExecutionPolicy<GB300, TVec> const &, String<Seed<Simple, TConfig>> &seeds,
+                StringSet<TDb, TDbSpec> const &databases, StringSet<TQ, TQSpec> const &queries,
+                ExtensionDirection direction, Score<TScoreValue, TScoreSpec> const &sc, TScoreValue scoreDropOff,
+                TXDropTag const &)
+{
+    static_assert(gb300_impl::is_xdrop_tag<TXDropTag>::value, "x-drop tag must be UnGappedXDrop or GappedXDrop");
+    typedef typename Value<TQ>::Type TAlphabet;
+    gb300_impl::extend_batch<TAlphabet>(seeds, gb300_impl::flatten(databases), gb300_impl::flatten(queries), false,
+                                        direction,
+                                        gb300_impl::is_gapped<TXDropTag>::value ? GBA_GAPPED_XDROP
+                                                                                    : GBA_UNGAPPED_XDROP,
+                                        &sc, int(scoreDropOff));
+}
+
+// One database shared by every seed; seeds[k] lies on queries[k].
+template <typename TVec, typename TConfig, typename TAlph, typename TDbSpec, typename TQ, typename TQSpec>
+void extendSeed(ExecutionPolicy<GB300, TVec> const &, String<Seed<Simple, TConfig>> &seeds,
+                String<TAlph, TDbSpec> const &database, StringSet<TQ, TQSpec> const &queries,
+                ExtensionDirection direction, MatchExtend const &)
+{
+    gb300_impl::extend_batch<TAlph>(seeds, gb300_impl::flatten_one(database), gb300_impl::flatten(queries), true,
+                                    direction, GBA_MATCH_EXTEND, (Score<int, Simple> const *)nullptr, 0);
+}
+
+template <typename TVec, typename TConfig, typename TAlph, typename TDbSpec, typename TQ, typename TQSpec,
+          typename TScoreValue, typename TScoreSpec, typename TXDropTag>
+void extendSeed(ExecutionPolicy<GB300, TVec> const &, String<Seed<Simple, TConfig>> &seeds,
+                String<TAlph, TDbSpec> const &database, StringSet<TQ, TQSpec> const &queries,
+                ExtensionDirection direction, Score<TScoreValue, TScoreSpec> const &sc, TScoreValue scoreDropOff,
+                TXDropTag const &)
+{
+    static_assert(gb300_impl::is_xdrop_tag<TXDropTag>::value, "x-drop tag must be UnGappedXDrop or GappedXDrop");
+    gb300_impl::extend_batch<TAlph>(seeds, gb300_impl::flatten_one(database), gb300_impl::flatten(queries), true,
+                                    direction,
+                                    gb300_impl::is_gapped<TXDropTag>::value ? GBA_GAPPED_XDROP
+                                                                                : GBA_UNGAPPED_XDROP,
+                                    &sc, int(scoreDropOff));
 }
 
 }  // namespace seqan2

@@ -49,6 +49,12 @@ class RefParams(C.Structure):
                 ("threads", C.c_int32)]
 
 
+class OrcXdropParams(C.Structure):
+    _fields_ = [("method", C.c_int32), ("direction", C.c_int32), ("match", C.c_int32),
+                ("mismatch", C.c_int32), ("gap", C.c_int32), ("xdrop", C.c_int32),
+                ("matrix", C.POINTER(C.c_int32)), ("alphabet_size", C.c_int32)]
+
+
 class RefGapsOut(C.Structure):
     _fields_ = [("score", C.c_int32), ("h_clip_begin", C.c_int32), ("h_clip_end", C.c_int32),
                 ("v_clip_begin", C.c_int32), ("v_clip_end", C.c_int32)]
@@ -96,6 +102,10 @@ def liboracle():
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_int32]
         _orc.orc_align_batch.restype = C.c_int
+        _orc.orc_extend_seeds.argtypes = [C.POINTER(OrcXdropParams), C.c_int64, C.c_void_p, C.c_void_p,
+                                          C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+        _orc.orc_extend_seeds.restype = C.c_int
     return _orc
 
 
@@ -117,6 +127,9 @@ def libref():
         _ref.ref_has_shape.argtypes = [C.c_int32, C.POINTER(RefParams)]
         _ref.ref_blosum62.argtypes = [C.c_void_p]
         _ref.ref_encode.argtypes = [C.c_int32, C.c_char_p, C.c_int64, C.c_void_p]
+        _ref.ref_extend_seeds.argtypes = [C.c_int32] * 8 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                             C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                                             C.c_void_p, C.c_int32]
     return _ref
 
 
@@ -288,6 +301,84 @@ def ref_encode(alphabet: str, text: str) -> np.ndarray:
 # _adaptTraceSegmentsTo (align/dp_traceback_adaptor.h:57-117) and getCigarString
 # (bam_io/cigar.h:261-339).
 # ---------------------------------------------------------------------------------------------
+
+# ---------------------------------------------------------------------------------------------
+# Seed extension: extendSeed(Seed<Simple>, database, query, direction, ...) over a batch
+# (seeds/seeds_extension.h).  Seeds are int64 arrays [n, 6] = beginH, beginV, endH, endV,
+# lowerDiagonal, upperDiagonal.
+# ---------------------------------------------------------------------------------------------
+
+EXTEND_LEFT, EXTEND_RIGHT, EXTEND_BOTH = 1, 2, 3
+MATCH_EXTEND, UNGAPPED_XDROP, GAPPED_XDROP = 0, 1, 2
+
+
+@dataclass
+class SeedProblem:
+    method: int = GAPPED_XDROP
+    direction: int = EXTEND_BOTH
+    match: int = 1
+    mismatch: int = -1
+    gap: int = -1
+    xdrop: int = 10
+    matrix: np.ndarray | None = None   # alphabet^2 int32, row = first argument of score()
+    alphabet: str = "dna"
+
+
+def seeds_array(seeds):
+    """[(beginH, beginV, length)] or [n, 6] -> int64 [n, 6] as Seed(beginH, beginV, length)
+    constructs it (seeds/seeds_seed_simple.h:98-104)."""
+    a = np.asarray(seeds, dtype=np.int64)
+    if a.ndim == 2 and a.shape[1] == 6:
+        return np.ascontiguousarray(a.copy())
+    a = a.reshape(-1, 3)
+    out = np.zeros((len(a), 6), dtype=np.int64)
+    out[:, 0], out[:, 1] = a[:, 0], a[:, 1]
+    out[:, 2], out[:, 3] = a[:, 0] + a[:, 2], a[:, 1] + a[:, 2]
+    out[:, 4] = out[:, 5] = a[:, 0] - a[:, 1]
+    return out
+
+
+def oracle_extend_seeds(sp: SeedProblem, H, V, seeds, pair_of_seed=None, threads: int = 0, seed_h=None,
+                        seed_v=None):
+    """C restatement over a batch; returns (seeds [n, 6], xscores [n, 2]).  Seed i lies on
+    H[seed_h[i]] and V[seed_v[i]]; pair_of_seed sets both."""
+    lib = liboracle()
+    sh, oh = concat(H)
+    sv, ov = concat(V)
+    s = seeds_array(seeds)
+    xs = np.zeros((max(len(s), 1), 2), dtype=np.int32)
+    p = OrcXdropParams(sp.method, sp.direction, sp.match, sp.mismatch, sp.gap, sp.xdrop, None, 0)
+    if sp.matrix is not None:
+        mat = np.ascontiguousarray(sp.matrix, dtype=np.int32)
+        p.matrix = mat.ctypes.data_as(C.POINTER(C.c_int32))
+        p.alphabet_size = int(round(np.sqrt(mat.size)))
+    if pair_of_seed is not None:
+        seed_h = seed_v = pair_of_seed
+    ih = None if seed_h is None else np.ascontiguousarray(seed_h, dtype=np.int32)
+    iv = None if seed_v is None else np.ascontiguousarray(seed_v, dtype=np.int32)
+    rc = lib.orc_extend_seeds(C.byref(p), len(H), _ptr(sh), _ptr(oh), len(V), _ptr(sv), _ptr(ov), len(s),
+                              _ptr(ih), _ptr(iv), _ptr(s), _ptr(xs), threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle returned {rc}")
+    return s, xs[:len(s)]
+
+
+def ref_extend_seeds(sp: SeedProblem, H, V, seeds, pair_of_seed=None, threads: int = 1):
+    """The reference's extendSeed over a batch; returns (seeds [n, 6], xscores [n, 2])."""
+    lib = libref()
+    sh, oh = concat(H)
+    sv, ov = concat(V)
+    s = seeds_array(seeds)
+    xs = np.zeros((max(len(s), 1), 2), dtype=np.int32)
+    pos = None if pair_of_seed is None else np.ascontiguousarray(pair_of_seed, dtype=np.int32)
+    rc = lib.ref_extend_seeds(sp.method, sp.direction, 0 if sp.alphabet == "dna" else 1,
+                              1 if sp.matrix is not None else 0, sp.match, sp.mismatch, sp.gap, sp.xdrop,
+                              len(H), _ptr(sh), _ptr(oh), _ptr(sv), _ptr(ov), len(s), _ptr(pos), _ptr(s),
+                              _ptr(xs), threads)
+    if rc != 0:
+        raise RuntimeError(f"reference returned {rc}")
+    return s, xs[:len(s)]
+
 
 def render_rows(segments, h_text: str, v_text: str):
     """Gapped rows of the clipped alignment view, as operator<< on Gaps prints them."""

@@ -717,3 +717,264 @@ int orc_align_batch(const orc_params *p, int64_t n_pairs,
     }
     return rc;
 }
+
+/* ===================================================================================== */
+/* Seed extension                                                                        */
+/* ===================================================================================== */
+
+static int xs_score(const orc_xdrop_params *p, int a, int b)
+{
+    if (p->matrix) return p->matrix[a * p->alphabet_size + b];
+    return a == b ? p->match : p->mismatch;
+}
+
+/* extendSeed [UnGappedXDrop] seeds/seeds_extension.h:283-360.  The left walk scores the pair
+ * at (posH, posV) while it tests (posH - 1, posV - 1) for a match, as the reference does. */
+/* extendSeed [MatchExtend] seeds/seeds_extension.h:181-218. */
+static void xs_match(const orc_xdrop_params *p, orc_seed *s, const uint8_t *db, uint64_t m, const uint8_t *q,
+                     uint64_t n)
+{
+    if (p->direction & ORC_EXTEND_LEFT) {
+        uint64_t posH = (uint64_t)s->begin_h, posV = (uint64_t)s->begin_v;
+        while (posH >= 1 && posV >= 1 && db[posH - 1] == q[posV - 1]) {
+            --posH;
+            --posV;
+        }
+        s->begin_h = (int64_t)posH;
+        s->begin_v = (int64_t)posV;
+    }
+    if (p->direction & ORC_EXTEND_RIGHT) {
+        uint64_t posH = (uint64_t)s->end_h, posV = (uint64_t)s->end_v;
+        while (posH < m && posV < n && db[posH] == q[posV]) {
+            ++posH;
+            ++posV;
+        }
+        s->end_h = (int64_t)posH;
+        s->end_v = (int64_t)posV;
+    }
+}
+
+static void xs_ungapped(const orc_xdrop_params *p, orc_seed *s, const uint8_t *db, uint64_t m, const uint8_t *q,
+                        uint64_t n)
+{
+    const int drop = -p->xdrop;
+    if (p->direction & ORC_EXTEND_LEFT) {
+        int tmp = 0;
+        uint64_t posH = (uint64_t)s->begin_h, posV = (uint64_t)s->begin_v, mism = 0;
+        while (posH >= 1 && posV >= 1 && tmp > drop) {
+            tmp += xs_score(p, db[posH], q[posV]);
+            if (db[posH - 1] == q[posV - 1]) {
+                mism = 0;
+                if (tmp > 0) tmp = 0;
+            } else {
+                mism += 1;
+            }
+            --posH;
+            --posV;
+        }
+        s->begin_h = (int64_t)(posH + mism);
+        s->begin_v = (int64_t)(posV + mism);
+    }
+    if (p->direction & ORC_EXTEND_RIGHT) {
+        int tmp = 0;
+        uint64_t posH = (uint64_t)s->end_h, posV = (uint64_t)s->end_v, mism = 0;
+        while (posH < m && posV < n && tmp > drop) {
+            tmp += xs_score(p, db[posH], q[posV]);
+            if (db[posH] == q[posV]) {
+                mism = 0;
+                if (tmp > 0) tmp = 0;
+            } else {
+                mism += 1;
+            }
+            ++posH;
+            ++posV;
+        }
+        s->end_h = (int64_t)(posH - mism);
+        s->end_v = (int64_t)(posV - mism);
+    }
+}
+
+/* _extendSeedGappedXDropOneDirection, seeds/seeds_extension.h:613-775, with _initAntiDiags
+ * (:457-481), _initAntiDiag3 (:498-520), _calcExtendedLowerDiag/UpperDiag (:522-545) and
+ * _updateExtendedSeed (:547-579).  qs/ds: the query (V) and database (H) segments; `left`
+ * reads them backwards from their ends.  Index arithmetic in size_t, diagonals signed, scores
+ * int, as in the reference. */
+static int xs_gapped_one(const orc_xdrop_params *p, orc_seed *s, const uint8_t *qs, uint64_t qlen,
+                         const uint8_t *ds, uint64_t dlen, int left)
+{
+    const uint64_t cols = qlen + 1, rows = dlen + 1;
+    if (rows == 1 || cols == 1) return 0;
+    const int len = 2 * (int)(cols > rows ? cols : rows);
+    const int minErr = INT_MIN / len;
+    const int gap = p->gap > minErr ? p->gap : minErr;
+    const int undefined = INT_MIN - gap;
+    const int xdrop = p->xdrop;
+    /* Score<int, Simple>: the mismatch score is raised to minErr too (:603-609). */
+    orc_xdrop_params sp = *p;
+    if (!p->matrix && sp.mismatch < minErr) sp.mismatch = minErr;
+    p = &sp;
+    /* anti-diagonal buffers: at most cols + 1 entries each */
+    int *buf = (int *)malloc(sizeof(int) * 3 * (size_t)(cols + 2));
+    int *ad1 = buf, *ad2 = buf + (cols + 2), *ad3 = buf + 2 * (cols + 2);
+    uint64_t len1 = 0, len2 = 1, len3 = 2;
+    ad2[0] = 0;
+    if (-gap > xdrop) {
+        ad3[0] = undefined;
+        ad3[1] = undefined;
+    } else {
+        ad3[0] = gap;
+        ad3[1] = gap;
+    }
+    uint64_t minCol = 1, maxCol = 2;
+    uint64_t off1 = 0, off2 = 0, off3 = 0;
+    uint64_t antiDiagNo = 1;
+    int best = 0;
+    int64_t lowerDiag = 0, upperDiag = 0;
+    while (minCol < maxCol) {
+        ++antiDiagNo;
+        int *t = ad1;
+        ad1 = ad2;
+        ad2 = ad3;
+        ad3 = t;
+        len1 = len2;
+        len2 = len3;
+        off1 = off2;
+        off2 = off3;
+        off3 = minCol - 1;
+        /* _initAntiDiag3 */
+        len3 = maxCol + 1 - off3;
+        ad3[0] = undefined;
+        ad3[maxCol - off3] = undefined;
+        if ((int)antiDiagNo * gap > best - xdrop) {
+            if (off3 == 0) ad3[0] = (int)(antiDiagNo * (uint64_t)(int64_t)gap);
+            if (antiDiagNo - maxCol == 0) ad3[maxCol - off3] = (int)(antiDiagNo * (uint64_t)(int64_t)gap);
+        }
+        int antiDiagBest = (int)(antiDiagNo * (uint64_t)(int64_t)gap);
+        for (uint64_t col = minCol; col < maxCol; ++col) {
+            const uint64_t i3 = col - off3, i2 = col - off2, i1 = col - off1;
+            uint64_t queryPos, dbPos;
+            if (!left) {
+                queryPos = col - 1;
+                dbPos = antiDiagNo - col - 1;
+            } else {
+                queryPos = cols - 1 - col;
+                dbPos = rows - 1 + col - antiDiagNo;
+            }
+            int tmp = (ad2[i2 - 1] > ad2[i2] ? ad2[i2 - 1] : ad2[i2]) + gap;
+            const int d = ad1[i1 - 1] + xs_score(p, qs[queryPos], ds[dbPos]);
+            tmp = tmp > d ? tmp : d;
+            if (tmp < best - xdrop) {
+                ad3[i3] = undefined;
+            } else {
+                ad3[i3] = tmp;
+                if (tmp > antiDiagBest) antiDiagBest = tmp;
+            }
+        }
+        if (antiDiagBest > best) best = antiDiagBest;
+        while (minCol - off3 < len3 && ad3[minCol - off3] == undefined && minCol - off2 - 1 < len2 &&
+               ad2[minCol - off2 - 1] == undefined)
+            ++minCol;
+        while (maxCol - off3 > 0 && ad3[maxCol - off3 - 1] == undefined && ad2[maxCol - off2 - 1] == undefined)
+            --maxCol;
+        ++maxCol;
+        {
+            const uint64_t minRow = antiDiagNo - minCol;
+            if ((int64_t)minCol - (int64_t)minRow < lowerDiag) lowerDiag = (int64_t)minCol - (int64_t)minRow;
+        }
+        {
+            const uint64_t mc = maxCol - 1;
+            const uint64_t maxRow = antiDiagNo + 1 - mc;
+            if ((int64_t)mc - 1 - (int64_t)maxRow > upperDiag) upperDiag = (int64_t)(mc - 1 - maxRow);
+        }
+        {
+            const int a = (int)minCol, b = (int)antiDiagNo + 2 - (int)rows;
+            minCol = (uint64_t)(a > b ? a : b);
+        }
+        if (maxCol > cols) maxCol = cols;
+    }
+    /* Position of the longest extension. */
+    uint64_t lcol = len3 + off3 - 2;
+    uint64_t lrow = antiDiagNo - lcol;
+    int lscore = ad3[lcol - off3];
+    if (lscore == undefined) {
+        if (ad2[len2 - 2] != undefined) {
+            lcol = len2 + off2 - 2;
+            lrow = antiDiagNo - 1 - lcol;
+            lscore = ad2[lcol - off2];
+        } else if (len2 > 2 && ad2[len2 - 3] != undefined) {
+            lcol = len2 + off2 - 3;
+            lrow = antiDiagNo - 1 - lcol;
+            lscore = ad2[lcol - off2];
+        }
+    }
+    if (lscore == undefined) {
+        for (uint64_t i = 0; i < len1; ++i) {
+            if (ad1[i] > lscore) {
+                lscore = ad1[i];
+                lcol = i + off1;
+                lrow = antiDiagNo - 2 - lcol;
+            }
+        }
+    }
+    free(buf);
+    if (lscore != undefined) {
+        if (left) {
+            const int64_t beginDiag = s->begin_h - s->begin_v;
+            if (s->lower_diag > beginDiag + lowerDiag) s->lower_diag = beginDiag + lowerDiag;
+            if (s->upper_diag < beginDiag + upperDiag) s->upper_diag = beginDiag + upperDiag;
+            s->begin_h = (int64_t)((uint64_t)s->begin_h - lrow);
+            s->begin_v = (int64_t)((uint64_t)s->begin_v - lcol);
+        } else {
+            const int64_t endDiag = s->end_h - s->end_v;
+            if (s->upper_diag < endDiag - lowerDiag) s->upper_diag = endDiag - lowerDiag;
+            if (s->lower_diag > endDiag - upperDiag) s->lower_diag = endDiag - upperDiag;
+            s->end_h = (int64_t)((uint64_t)s->end_h + lrow);
+            s->end_v = (int64_t)((uint64_t)s->end_v + lcol);
+        }
+    }
+    return lscore;
+}
+
+/* extendSeed [GappedXDrop] seeds/seeds_extension.h:780-835: left on the prefixes before the
+ * seed, right on the suffixes after it. */
+int orc_extend_seed(const orc_xdrop_params *p, orc_seed *seed, const uint8_t *db, int64_t m, const uint8_t *q,
+                    int64_t n, int32_t *xscore)
+{
+    if (!p || !seed) return -1;
+    if (xscore) xscore[0] = xscore[1] = 0;
+    if (p->method == ORC_MATCH_EXTEND) {
+        xs_match(p, seed, db, (uint64_t)m, q, (uint64_t)n);
+        return 0;
+    }
+    if (p->method == ORC_XDROP_UNGAPPED) {
+        xs_ungapped(p, seed, db, (uint64_t)m, q, (uint64_t)n);
+        return 0;
+    }
+    if (p->direction & ORC_EXTEND_LEFT) {
+        const int sc = xs_gapped_one(p, seed, q, (uint64_t)seed->begin_v, db, (uint64_t)seed->begin_h, 1);
+        if (xscore) xscore[0] = sc;
+    }
+    if (p->direction & ORC_EXTEND_RIGHT) {
+        const uint64_t eh = (uint64_t)seed->end_h, ev = (uint64_t)seed->end_v;
+        const int sc = xs_gapped_one(p, seed, q + ev, (uint64_t)n - ev, db + eh, (uint64_t)m - eh, 0);
+        if (xscore) xscore[1] = sc;
+    }
+    return 0;
+}
+
+int orc_extend_seeds(const orc_xdrop_params *p, int64_t n_h, const uint8_t *seq_h, const int64_t *off_h,
+                     int64_t n_v, const uint8_t *seq_v, const int64_t *off_v, int64_t n_seeds,
+                     const int32_t *seed_h, const int32_t *seed_v, orc_seed *seeds, int32_t *xscores,
+                     int32_t threads)
+{
+    if (!p || n_seeds < 0 || (n_seeds > 0 && !seeds)) return -1;
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+    for (int64_t i = 0; i < n_seeds; ++i) {
+        const int64_t kh = seed_h ? seed_h[i] : i, kv = seed_v ? seed_v[i] : i;
+        if (kh < 0 || kh >= n_h || kv < 0 || kv >= n_v) continue;
+        orc_extend_seed(p, &seeds[i], seq_h + off_h[kh], off_h[kh + 1] - off_h[kh], seq_v + off_v[kv],
+                        off_v[kv + 1] - off_v[kv], xscores ? xscores + 2 * i : NULL);
+    }
+    return 0;
+}

@@ -73,6 +73,43 @@ int orc_align_batch(const orc_params *p, int64_t n_pairs,
                     orc_result *out, orc_segment *segs, const int64_t *seg_off,
                     int32_t threads);
 
+/* ---- Seed extension (seeds/seeds_extension.h) ---------------------------------------
+ * Seed<Simple>: positions in H (the "database") and V (the "query"), diagonals = H - V.
+ * extendSeed(seed, database, query, direction, Score<int, Simple|ScoreMatrix>, scoreDropOff,
+ * UnGappedXDrop | GappedXDrop) restated for int scores (TScoreValue = int, positions size_t,
+ * diagonals signed).  The gapped form needs gap open == extend (linear) and, for defined
+ * behaviour of the reference's int arithmetic, every substitution score >= the gap score. */
+enum { ORC_EXTEND_LEFT = 1, ORC_EXTEND_RIGHT = 2, ORC_EXTEND_BOTH = 3 };
+enum { ORC_MATCH_EXTEND = 0, ORC_XDROP_UNGAPPED = 1, ORC_XDROP_GAPPED = 2 };
+
+typedef struct {
+    int64_t begin_h, begin_v, end_h, end_v;
+    int64_t lower_diag, upper_diag;
+} orc_seed;
+
+typedef struct {
+    int32_t method;            /* ORC_MATCH_EXTEND | ORC_XDROP_* */
+    int32_t direction;         /* ORC_EXTEND_* */
+    int32_t match, mismatch;   /* Score<int, Simple> (ignored with a matrix) */
+    int32_t gap;               /* linear gap score (open = extend) */
+    int32_t xdrop;             /* scoreDropOff */
+    const int32_t *matrix;     /* optional alphabet^2 table, row = first argument of score() */
+    int32_t alphabet_size;
+} orc_xdrop_params;
+
+/* Extends one seed in place; the scores of the gapped extensions (left, right; 0 when that side
+ * is empty, INT_MIN when nothing was defined) go to xscore[0..1] when non-NULL. */
+int orc_extend_seed(const orc_xdrop_params *p, orc_seed *seed, const uint8_t *db, int64_t m,
+                    const uint8_t *q, int64_t n, int32_t *xscore);
+
+/* A batch of seeds over databases H and queries V given as concatenated codes + offsets; seed i
+ * lies on H[seed_h[i]] and V[seed_v[i]] (NULL: index i).  xscores: NULL or 2 per seed.
+ * threads <= 0: all. */
+int orc_extend_seeds(const orc_xdrop_params *p, int64_t n_h, const uint8_t *seq_h, const int64_t *off_h,
+                     int64_t n_v, const uint8_t *seq_v, const int64_t *off_v, int64_t n_seeds,
+                     const int32_t *seed_h, const int32_t *seed_v, orc_seed *seeds, int32_t *xscores,
+                     int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

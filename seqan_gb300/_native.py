@@ -33,6 +33,8 @@ GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16, GBA_FLAG_PLAIN_BUCKETS, GBA_FLAG_NO_G
 GBA_FLAG_PACKED = 32
 GBA_FLAG_PACKED_SPLIT, GBA_FLAG_PACKED_NO_SPLIT = 64, 128
 GBA_KERNEL_STRIP, GBA_KERNEL_PACKED, GBA_KERNEL_WARP, GBA_KERNEL_BANDED = 1, 2, 4, 8
+GBA_MATCH_EXTEND, GBA_UNGAPPED_XDROP, GBA_GAPPED_XDROP = 0, 1, 2
+GBA_EXTEND_NONE, GBA_EXTEND_LEFT, GBA_EXTEND_RIGHT, GBA_EXTEND_BOTH = 0, 1, 2, 3
 
 # Every symbol include/seqan_gb300.h declares.
 EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", "gba_align_batch",
@@ -41,7 +43,8 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_copy_to_device", "gba_copy_to_host", "gba_synchronize", "gba_timer_start",
             "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc",
             "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
-            "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule"]
+            "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule",
+            "gba_extend_seeds", "gba_extend_seeds_device"]
 
 
 class GbaConfig(C.Structure):
@@ -81,7 +84,8 @@ class GbaStats(C.Structure):
     _fields_ = [("dp_kernel_ms", C.c_float), ("traceback_kernel_ms", C.c_float),
                 ("kernel_launches", C.c_int32), ("cells", C.c_int64), ("trace_bytes", C.c_int64),
                 ("tile_rows", C.c_int32), ("tile_min_blocks", C.c_int32), ("host_plan_ms", C.c_float),
-                ("call_ms", C.c_float), ("dp_kernels", C.c_int32)]
+                ("call_ms", C.c_float), ("dp_kernels", C.c_int32), ("seed_ring", C.c_int32),
+                ("seed_fallbacks", C.c_int64)]
 
 
 class GbaServerConfig(C.Structure):
@@ -100,6 +104,24 @@ class GbaServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("pending", C.c_int64),
                 ("batches", C.c_int64), ("cells", C.c_int64), ("hbm_in_flight", C.c_int64),
                 ("hbm_in_flight_peak", C.c_int64)]
+
+
+class GbaSeed(C.Structure):
+    _fields_ = [("begin_h", C.c_int64), ("begin_v", C.c_int64), ("end_h", C.c_int64), ("end_v", C.c_int64),
+                ("lower_diagonal", C.c_int64), ("upper_diagonal", C.c_int64)]
+
+
+class GbaExtendParams(C.Structure):
+    _fields_ = [("method", C.c_int32), ("direction", C.c_int32), ("score_drop_off", C.c_int32),
+                ("match", C.c_int32), ("mismatch", C.c_int32), ("gap", C.c_int32), ("matrix", C.c_void_p),
+                ("alphabet_size", C.c_int32), ("reserved", C.c_int32)]
+
+
+class GbaSeedBatch(C.Structure):
+    _fields_ = [("num_h", C.c_int64), ("seq_h", C.c_void_p), ("off_h", C.c_void_p),
+                ("num_v", C.c_int64), ("seq_v", C.c_void_p), ("off_v", C.c_void_p),
+                ("num_seeds", C.c_int64), ("seed_h", C.c_void_p), ("seed_v", C.c_void_p),
+                ("max_v_len", C.c_int64)]
 
 
 def _sources():
@@ -169,6 +191,8 @@ def lib():
             L.gba_server_submit_schedule.argtypes = [vp, C.POINTER(GbaBatch), vp, C.c_uint64]
             L.gba_server_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
             L.gba_server_destroy.argtypes = [vp]
+            L.gba_extend_seeds.argtypes = [vp, C.POINTER(GbaExtendParams), C.POINTER(GbaSeedBatch), vp, vp]
+            L.gba_extend_seeds_device.argtypes = [vp, C.POINTER(GbaExtendParams), C.POINTER(GbaSeedBatch), vp, vp]
             L.gba_clock_seconds.argtypes = []
             L.gba_clock_seconds.restype = C.c_double
             _lib = L

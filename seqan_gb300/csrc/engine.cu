@@ -11,6 +11,7 @@
 #include "dp16x2_kernels.cuh"
 #include "dp_banded_kernels.cuh"
 #include "dp_warp_kernels.cuh"
+#include "seed_kernels.cuh"
 #include "int_peak.cuh"
 
 #include <cub/device/device_scan.cuh>
@@ -194,6 +195,11 @@ struct gba_context {
     uint32_t check_err = 0;         // slots of err_word the runs since the last check can set
     std::vector<std::unique_ptr<gba_plan>> chunk_plans;   // gba_align_batch chunks 1.. (0 = oneshot)
     std::vector<cudaEvent_t> chunk_ev;                    // 3 per chunk
+    // seed extension: device copies of a host batch, the kernels' work words and scratch
+    DevBuf xs_seq_h, xs_seq_v, xs_off_h, xs_off_v, xs_ids, xs_seeds, xs_scores, xs_matrix, xs_work, xs_scratch,
+        xs_results;
+    bool xs_check = false;          // a device seed-extension run whose error word is unread
+    std::map<std::pair<const void *, size_t>, int64_t> xs_grid;   // (kernel, smem) -> resident blocks
 };
 
 namespace {
@@ -1719,11 +1725,13 @@ GBA_API int gba_copy_to_host(gba_context *ctx, void *dst, const void *src, size_
     return GBA_OK;
 }
 
+int seeds_check_error(gba_context *ctx);   // seeds_host.cuh
+
 GBA_API int gba_synchronize(gba_context *ctx)
 {
     if (!ctx) return GBA_EINVAL;
     GBA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return GBA_OK;
+    return seeds_check_error(ctx);
 }
 
 GBA_API int gba_timer_start(gba_context *ctx)
@@ -1777,3 +1785,4 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 }  // extern "C"
 
 #include "server.cuh"
+#include "seeds_host.cuh"

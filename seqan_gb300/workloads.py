@@ -12,6 +12,8 @@ There is no public dataset for this path; these generators stand in for it:
 * ``read_windows``        -- reads sampled from a random reference with substitutions and indels,
   each paired with a reference window around its true origin.
 * ``serving_lengths``     -- the mixed length distribution of the serving workload.
+* ``seed_windows``        -- read-mapping seeds: reads against reference windows with one exact
+  k-mer seed per read on the read's true diagonal (or the best-matching k-mer near it).
 All generators use numpy's PCG64 with the given seed.
 """
 from __future__ import annotations
@@ -133,6 +135,42 @@ def read_windows(n_reads: int, ref_len: int = 10_000_000, read_len: int = 150, f
         pieces.append(r[prev:])
         out[k] = np.concatenate(pieces).astype(np.uint8)
     return list(windows), out
+
+
+def seed_windows(n_reads: int, ref_len: int = 10_000_000, read_len: int = 150, flank: int = 50, k: int = 19,
+                 sub_rate: float = 0.03, indel_rate: float = 0.003, seed: int = 6, tries: int = 8):
+    """(windows, reads, seeds [(beginH, beginV, k)], pair_of_seed) for seed extension.
+
+    Each read comes from ref[o, o + read_len) (with substitutions and indels) and is paired with
+    the window ref[o - flank, o + read_len + flank).  Its seed is the first of `tries` random
+    read k-mers that occurs in the window on the true diagonal shifted by 0, -1 or +1 (indels
+    move it); a read without one gets the true-diagonal k-mer at its first tried start."""
+    wins, reads = read_windows(n_reads, ref_len, read_len, flank, sub_rate, indel_rate, seed)
+    rng = _rng(seed + 1)
+    n = len(reads)
+    W = np.stack(wins)
+    lens = np.array([len(r) for r in reads], dtype=np.int64)
+    R = np.full((n, int(lens.max()) + 2), 255, dtype=np.uint8)
+    for i, r in enumerate(reads):
+        R[i, :len(r)] = r
+    found = np.zeros(n, dtype=bool)
+    bh = np.zeros(n, dtype=np.int64)
+    bv = np.zeros(n, dtype=np.int64)
+    rows = np.arange(n)
+    span = np.arange(k)
+    for t in range(tries):
+        start = rng.integers(0, np.maximum(lens - k, 0) + 1)
+        if t == 0:
+            bv[:] = start
+            bh[:] = np.minimum(start + flank, W.shape[1] - k)
+        for shift in (0, -1, 1):
+            h0 = np.clip(start + flank + shift, 0, W.shape[1] - k)
+            eq = (R[rows[:, None], start[:, None] + span] == W[rows[:, None], h0[:, None] + span]).all(axis=1)
+            new = eq & ~found
+            bh[new], bv[new] = h0[new], start[new]
+            found |= new
+    seeds = np.stack([bh, bv, np.minimum(k, lens - bv)], axis=1)
+    return list(W), reads, seeds, np.arange(n, dtype=np.int32)
 
 
 def serving_lengths(n: int, seed: int = 5):

@@ -13,6 +13,32 @@
 
 using namespace seqan2;
 
+// Batch seed extension with the reference's seed and sequence types.
+static void seeds_demo(ExecutionPolicy<GB300, Vectorial> const &gpu)
+{
+    StringSet<DnaString> dbs, qs;
+    appendValue(dbs, "AACCCCTTTGGTGAAAAA");
+    appendValue(qs, "AAACCCTTTGGGTTTTT");
+    appendValue(dbs, "ttttcgatcgatgcttttt");
+    appendValue(qs, "aaaacgatcgatgc");
+    String<Seed<Simple>> seeds;
+    appendValue(seeds, Seed<Simple>(4, 4, 3));
+    appendValue(seeds, Seed<Simple>(4, 4, 9));
+    extendSeed(gpu, seeds, dbs, qs, EXTEND_BOTH, Score<int, Simple>(2, -1, -1), 1, GappedXDrop());
+    extendSeed(gpu, seeds, dbs, qs, EXTEND_BOTH, Score<int, Simple>(0, -1, -1), 2, UnGappedXDrop());
+    extendSeed(gpu, seeds, dbs, qs, EXTEND_LEFT, MatchExtend());
+    String<Seed<Simple>> onShared;
+    appendValue(onShared, Seed<Simple>(5, 5, 3));
+    StringSet<String<AminoAcid>> pq;
+    appendValue(pq, "CSNNHKMMMMAAGGW");
+    String<AminoAcid> pdb = "CSNNHKMMMMAAGGW";
+    Blosum62 b62(-9, -9);
+    extendSeed(gpu, onShared, pdb, pq, EXTEND_BOTH, b62, 1, GappedXDrop());
+    for (size_t k = 0; k < length(seeds); ++k)
+        std::cout << beginPositionH(seeds[k]) << " " << endPositionH(seeds[k]) << "\n";
+    std::cout << beginPositionH(onShared[0]) << " " << endPositionH(onShared[0]) << "\n";
+}
+
 int main()
 {
     ExecutionPolicy<GB300, Vectorial> gpu;
@@ -68,5 +94,6 @@ int main()
               << h[0] << ' ' << i[0] << ' ' << j[0] << ' ' << k[0] << ' ' << l[0] << ' ' << m[0] << ' ' << n1[0] << ' '
               << n2[0] << ' ' << n3[0] << ' ' << n4[0] << '\n'
               << gapsH[0] << '\n' << gapsV[0] << '\n' << aligns[0] << '\n';
+    seeds_demo(gpu);
     return 0;
 }

@@ -1,13 +1,15 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--only seeds]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
                         CIGARs, and raw TraceSegment_ lists of the single-pair DP.
   blosum62.json         the reference's 27x27 Blosum62 table (score/score_matrix_data.h).
   alphabets.json        the reference's char -> ordValue maps for Dna5, Dna and AminoAcid.
+  seed_cases.json       seeds extended by the reference's extendSeed (MatchExtend, UnGappedXDrop,
+                        GappedXDrop; seeds/seeds_extension.h) with the gapped extension scores.
   aa_background.json    residue counts of the reference's T-Coffee test FASTA files, the
                         stand-in for background amino-acid frequencies.
 """
@@ -79,9 +81,12 @@ def main():
         sys.exit("the reference tree is needed to generate fixtures")
     if not O.ref_available():
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"-j{os.cpu_count()}"])
+    b62 = O.ref_blosum62()
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "seeds":
+        write_seeds(b62)
+        return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
-    b62 = O.ref_blosum62()
 
     def add(kind, pb, H, V):
         alph = pb.alphabet
@@ -213,7 +218,102 @@ def main():
     with open(os.path.join(HERE, "aa_background.json"), "w") as f:
         json.dump({"source": "apps/seqan_tcoffee/tests/*.fa, *.fasta of the reference tree",
                    "files": len(files), "counts": {c: cnt[c] for c in "ACDEFGHIKLMNPQRSTVWY"}}, f)
-    print(f"{len(cases)} cases written")
+    print(f"{len(cases)} alignment cases written")
+    write_seeds(b62)
+
+
+def write_seeds(b62):
+    seeds = seed_cases(b62)
+    with open(os.path.join(HERE, "seed_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261204, "cases": seeds}, f,
+                  separators=(",", ":"))
+    print(f"{len(seeds)} seed cases written")
+
+
+def seed_cases(b62):
+    """Batches of seeds through the reference's extendSeed.  Gapped cases keep every substitution
+    score >= the gap score: below that the reference adds a score to its `undefined` sentinel
+    (INT_MIN - gap) and overflows int."""
+    rng = np.random.Generator(np.random.PCG64(20261204))
+    out = []
+
+    def related(n, A, sub, indel):
+        h = rng.integers(0, A, n).astype(np.uint8)
+        v = h.copy()
+        s = rng.random(n) < sub
+        v[s] = (v[s] + rng.integers(1, A, int(s.sum()))) % A
+        for _ in range(int(rng.poisson(indel * n))):
+            if len(v) < 4:
+                break
+            a = int(rng.integers(0, len(v) - 2))
+            v = np.delete(v, slice(a, a + int(rng.integers(1, 3)))) if rng.random() < 0.5 else \
+                np.insert(v, a, rng.integers(0, A, int(rng.integers(1, 3))).astype(np.uint8))
+        return h, v.astype(np.uint8)
+
+    def add(sp, H, V, seeds, pos):
+        alph = sp.alphabet
+        s, xs = O.ref_extend_seeds(sp, H, V, seeds, pos, threads=4)
+        out.append({"method": sp.method, "direction": sp.direction, "match": sp.match,
+                    "mismatch": sp.mismatch, "gap": sp.gap, "xdrop": sp.xdrop,
+                    "blosum62": sp.matrix is not None, "alphabet": alph,
+                    "H": [text(h, alph) for h in H], "V": [text(v, alph) for v in V],
+                    "pair_of_seed": None if pos is None else [int(x) for x in pos],
+                    "seeds": O.seeds_array(seeds).tolist(), "extended": s.tolist(),
+                    "xscores": xs.tolist() if sp.method == O.GAPPED_XDROP else None})
+
+    def batch(sp, count, lo, hi, A, seeds_per_pair=1):
+        H, V, seeds, pos = [], [], [], []
+        for k in range(count):
+            h, v = related(int(rng.integers(lo, hi + 1)), A, rng.uniform(0.0, 0.3), rng.uniform(0, 0.05))
+            if rng.random() < 0.2:
+                v = rng.integers(0, A, int(rng.integers(lo, hi + 1))).astype(np.uint8)
+            if A == 20:
+                h, v = AA_CODES[h], AA_CODES[v]
+            H.append(h)
+            V.append(v)
+            m, n = len(h), len(v)
+            for _ in range(seeds_per_pair):
+                L = int(rng.integers(0, min(m, n, 24) + 1))
+                bh = int(rng.integers(0, m - L + 1))
+                # mostly on the pair's own diagonal (a true seed), sometimes anywhere
+                bv = min(max(bh + int(rng.integers(-3, 4)), 0), n - L) if rng.random() < 0.7 else \
+                    int(rng.integers(0, n - L + 1))
+                if sp.method == O.UNGAPPED_XDROP and (sp.direction & 1) and bh > 0 and bv > 0 and \
+                        (bh >= m or bv >= n):
+                    continue   # the left walk scores database[beginH], past the end for such seeds
+                seeds.append((bh, bv, L))
+                pos.append(k)
+        add(sp, H, V, seeds, pos)
+
+    AA_CODES = np.array([0, 2, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 15, 16, 17, 18, 19, 21, 22, 23], dtype=np.uint8)
+    dna_scores = [(1, -1, -1), (2, -1, -1), (1, -2, -2), (2, -3, -5), (1, -5, -5), (1, -9, -9), (3, 0, -2)]
+    for method in (O.MATCH_EXTEND, O.UNGAPPED_XDROP, O.GAPPED_XDROP):
+        for direction in (O.EXTEND_LEFT, O.EXTEND_RIGHT, O.EXTEND_BOTH):
+            for (mt, mm, g) in dna_scores:
+                if method == O.GAPPED_XDROP and mm < g:
+                    continue
+                for xdrop in ((0, 1, 5, 20) if method else (0,)):
+                    batch(O.SeedProblem(method, direction, mt, mm, g, xdrop), 6, 1, 90, 4, 2)
+            if method:
+                for (g, xdrop) in ((-9, 1), (-9, 10), (-11, 25), (-4, 8)):
+                    batch(O.SeedProblem(method, direction, 0, 0, g, xdrop, b62, "aa"), 6, 1, 90, 20, 2)
+    # Read-mapping shape: 150 bp reads against 250 bp windows, 19-mer seeds on the true diagonal.
+    from seqan_gb300 import workloads as W
+    wins, reads, seeds, pos = W.seed_windows(40, seed=5)
+    for method in (O.UNGAPPED_XDROP, O.GAPPED_XDROP):
+        add(O.SeedProblem(method, O.EXTEND_BOTH, 1, -2, -2, 20), wins, reads, seeds, pos)
+    # Edges: seeds touching the sequence ends, empty seeds, one-letter sequences.
+    H = [np.array([0], np.uint8), np.array([1, 2, 3], np.uint8), np.array([2, 2, 2, 2], np.uint8),
+         np.zeros(0, np.uint8), np.array([3, 1], np.uint8)]
+    V = [np.array([0], np.uint8), np.array([1, 2, 3], np.uint8), np.array([2, 2], np.uint8),
+         np.array([1, 1], np.uint8), np.zeros(0, np.uint8)]
+    seeds = [(0, 0, 1), (0, 0, 0), (1, 1, 0), (3, 3, 0), (0, 0, 3), (2, 0, 2), (4, 2, 0), (0, 0, 0), (0, 1, 0),
+             (0, 0, 0), (2, 0, 0)]
+    pos = [0, 0, 1, 1, 1, 2, 2, 2, 3, 4, 4]
+    for direction in (O.EXTEND_LEFT, O.EXTEND_RIGHT, O.EXTEND_BOTH):
+        add(O.SeedProblem(O.GAPPED_XDROP, direction, 1, -1, -1, 3), H, V, seeds, pos)
+        add(O.SeedProblem(O.MATCH_EXTEND, direction), H, V, seeds, pos)
+    return out
 
 
 if __name__ == "__main__":
