@@ -32,7 +32,8 @@ class OrcParams(C.Structure):
                 ("band_on", C.c_int32), ("band_lower", C.c_int32), ("band_upper", C.c_int32),
                 ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
                 ("gap_extend", C.c_int32), ("matrix", C.POINTER(C.c_int32)),
-                ("alphabet_size", C.c_int32), ("score_bits", C.c_int32), ("traceback", C.c_int32)]
+                ("alphabet_size", C.c_int32), ("score_bits", C.c_int32), ("traceback", C.c_int32),
+                ("xdrop_on", C.c_int32), ("xdrop", C.c_int32)]
 
 
 class OrcResult(C.Structure):
@@ -73,6 +74,7 @@ class Problem:
     matrix: np.ndarray | None = None   # alphabet^2 int32 (row = H code)
     score_bits: int = 32
     alphabet: str = "dna"           # "dna" (Dna5 codes) | "aa" (AminoAcid codes)
+    xdrop: int | None = None        # mode "extend": the X-drop terminator's threshold
 
     @property
     def affine(self) -> bool:
@@ -149,7 +151,9 @@ def _ptr(a):
 
 def _orc_params(pb: Problem, traceback: bool) -> OrcParams:
     p = OrcParams()
-    p.mode = 1 if pb.mode == "local" else 0
+    p.mode = {"global": 0, "local": 1, "extend": 2}[pb.mode]
+    p.xdrop_on = 0 if pb.xdrop is None else 1
+    p.xdrop = 0 if pb.xdrop is None else int(pb.xdrop)
     p.gap_model = 1 if pb.affine else 0
     p.free_ends = pb.free_ends
     p.band_on = 1 if pb.band is not None else 0
@@ -378,6 +382,98 @@ def ref_extend_seeds(sp: SeedProblem, H, V, seeds, pair_of_seed=None, threads: i
     if rc != 0:
         raise RuntimeError(f"reference returned {rc}")
     return s, xs[:len(s)]
+
+
+# ---------------------------------------------------------------------------------------------
+# extendAlignment (align_extend/align_extend.h): an ungapped seed alignment hSeq[hb, he) /
+# vSeq[vb, ve) grown to the left on the reversed prefixes and to the right on the suffixes by the
+# AlignExtend DP (mode "extend", optional X-drop), then joined around the seed.
+# ---------------------------------------------------------------------------------------------
+
+@dataclass
+class ExtendResult:
+    score: int
+    row0: str
+    row1: str
+    h_begin: int
+    h_end: int
+    v_begin: int
+    v_end: int
+    left_score: int = 0
+    right_score: int = 0
+    left_segments: list = field(default_factory=list)    # prefix coordinates, traceback order
+    right_segments: list = field(default_factory=list)   # suffix coordinates, traceback order
+
+
+def _seg_end(seg):
+    hb, vb, ln, tp = seg
+    return (hb + (ln if tp in (SEG_DIAGONAL, SEG_HORIZONTAL) else 0),
+            vb + (ln if tp in (SEG_DIAGONAL, SEG_VERTICAL) else 0))
+
+
+def reverse_partial_trace(segments, len_h, len_v):
+    """_reversePartialTrace (align_extend/align_extend.h:91-109): begin = length - end, reversed."""
+    out = []
+    for seg in segments:
+        eh, ev = _seg_end(seg)
+        out.append((len_h - eh, len_v - ev, seg[2], seg[3]))
+    return out[::-1]
+
+
+def oracle_extend_alignment(pb: Problem, h, v, positions, direction, letters="ACGTN") -> ExtendResult:
+    """The reference's _extendAlignmentImpl (align_extend/align_extend.h:211-372) for an ungapped
+    seed, restated on the oracle's DP (pb.mode must be "extend")."""
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    hb, vb, he, ve = (int(x) for x in positions)
+    ext_left = bool(direction & EXTEND_LEFT) and hb > 0 and vb > 0
+    ext_right = bool(direction & EXTEND_RIGHT) and he < len(h) and ve < len(v)
+    sub = (lambda a, b: int(pb.matrix[a, b])) if pb.matrix is not None else \
+        (lambda a, b: pb.match if a == b else pb.mismatch)
+    center = sum(sub(int(h[hb + i]), int(v[vb + i])) for i in range(he - hb))
+    text = lambda codes: "".join(letters[int(c)] for c in codes)
+    left = ([], 0)
+    if ext_left:
+        r = oracle_batch(pb, [h[:hb][::-1].copy()], [v[:vb][::-1].copy()], traceback=True)
+        left = (reverse_partial_trace(r.segments[0], hb, vb), int(r.score[0]))
+    right = ([], 0)
+    if ext_right:
+        r = oracle_batch(pb, [h[he:].copy()], [v[ve:].copy()], traceback=True)
+        right = (r.segments[0], int(r.score[0]))
+    l0, l1 = render_rows(left[0], text(h[:hb]), text(v[:vb]))
+    r0, r1 = render_rows(right[0], text(h[he:]), text(v[ve:]))
+    lh = sum(s[2] for s in left[0] if s[3] in (SEG_DIAGONAL, SEG_HORIZONTAL))
+    lv = sum(s[2] for s in left[0] if s[3] in (SEG_DIAGONAL, SEG_VERTICAL))
+    rh = sum(s[2] for s in right[0] if s[3] in (SEG_DIAGONAL, SEG_HORIZONTAL))
+    rv = sum(s[2] for s in right[0] if s[3] in (SEG_DIAGONAL, SEG_VERTICAL))
+    return ExtendResult(left[1] + center + right[1], l0 + text(h[hb:he]) + r0, l1 + text(v[vb:ve]) + r1,
+                        hb - lh, he + rh, vb - lv, ve + rv, left[1], right[1], left[0], right[0])
+
+
+def ref_extend_alignment(pb: Problem, h, v, positions, direction) -> ExtendResult:
+    """The reference's extendAlignment on an ungapped seed (oracle/ref/units/align_extend.cpp)."""
+    lib = libref()
+    lib.ref_extend_alignment.argtypes = [C.c_int32] * 6 + [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                                            C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                                            C.c_void_p]
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    pos = np.array(positions, dtype=np.int64)
+    cap = 2 * (len(h) + len(v)) + 8
+    row0 = C.create_string_buffer(cap)
+    row1 = C.create_string_buffer(cap)
+    ends = np.zeros(4, dtype=np.int64)
+    score = C.c_int32(0)
+    rc = lib.ref_extend_alignment(0 if pb.alphabet == "dna" else 1, 1 if pb.matrix is not None else 0, pb.match,
+                                  pb.mismatch, pb.gap_open, pb.gap_extend, _ptr(h), len(h), _ptr(v), len(v),
+                                  _ptr(pos), int(direction), 0 if pb.xdrop is None else 1,
+                                  0 if pb.xdrop is None else int(pb.xdrop), C.byref(score), row0, row1, cap,
+                                  _ptr(ends))
+    if rc != 0:
+        raise RuntimeError(f"reference returned {rc}")
+    return ExtendResult(score.value, row0.value.decode(), row1.value.decode(), int(ends[0]), int(ends[1]),
+                        int(ends[2]), int(ends[3]))
 
 
 def render_rows(segments, h_text: str, v_text: str):

@@ -47,6 +47,7 @@ typedef struct {
     int bits16;
     int inf;
     int local;
+    int extend;     /* AlignExtend_: every cell tracked, no zero floor */
     int affine;
     int ext, open;
     int match, mismatch;
@@ -222,7 +223,7 @@ static void record(segbuf_t *sb, int hb, int vb, int len, int tv)
 /* Banded traceback bookkeeping of TracebackCoordinator_ (align/dp_traceback_impl.h:57-171)
  * is not needed here because the trace matrix is stored dense in (column, row). */
 static void traceback(const ctx_t *c, const uint8_t *T, int n, int m, int col, int row,
-                      segbuf_t *sb, int global)
+                      segbuf_t *sb, int tail, int head)
 {
 #define TAT(cc, rr) T[(size_t)(cc) * (size_t)(n + 1) + (size_t)(rr)]
     int tv = TAT(col, row);
@@ -241,7 +242,7 @@ static void traceback(const ctx_t *c, const uint8_t *T, int n, int m, int col, i
         else last = TV_NONE;
     }
 
-    if (global) { /* TraceTail_ (:522-530) */
+    if (tail) { /* TraceTail_ (:522-530) */
         if (row != n) record(sb, m, row, n - row, TV_V);
         if (col != m) record(sb, col, row, m - col, TV_H);
     }
@@ -277,7 +278,7 @@ static void traceback(const ctx_t *c, const uint8_t *T, int n, int m, int col, i
         }
     }
     record(sb, col, row, frag, last);
-    if (global) { /* TraceHead_ (:538-545) */
+    if (head) { /* TraceHead_ (:538-545) */
         if (row != 0) record(sb, 0, 0, row, TV_V);
         if (col != 0) record(sb, 0, 0, col, TV_H);
     }
@@ -590,10 +591,17 @@ static void dp_banded(const ctx_t *c, int fe, const uint8_t *h, int m, const uin
 /* ---------------------------------------------------------------------------------
  * Unbanded DP (align/dp_algorithm_impl.h:483-579 with dp_meta_info.h:178-221).
  * ------------------------------------------------------------------------------- */
+/* xdrop_on (ORC_EXTEND): the X-drop terminator of align_extend/dp_scout_xdrop.h:127-143 sets its
+ * flag at the last cell of a column when best - columnMax >= xdrop (columnMax: the column's
+ * maximum S; it is reset only when the flag is not set), and the column loop of
+ * _computeAlignmentImpl (align/dp_algorithm_impl.h:535-557) tests the flag after each inner
+ * column 1..m-1 only: a flag set in column 0 stops the DP after column 1, and the last column
+ * is computed whenever the loop runs out. */
 static void dp_unbanded(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
-                        int *colS, int *colE, uint8_t *T, best_t *b)
+                        int *colS, int *colE, uint8_t *T, best_t *b, int xdrop_on, int xdrop)
 {
     int i, j;
+    int terminated = 0, colmax = INT_MIN;
     for (i = 0; i <= n; ++i) { colS[i] = c->inf; colE[i] = c->inf; }
     for (j = 0; j <= m; ++j) {
         caches_t k;
@@ -611,13 +619,19 @@ static void dp_unbanded(const ctx_t *c, int fe, const uint8_t *h, int m, const u
             tv = compute_cell(c, dir, &colS[i], &colE[i], &k,
                               j > 0 ? h[j - 1] : 0, i > 0 ? v[i - 1] : 0, &f);
             if (T) T[(size_t)j * (size_t)(n + 1) + (size_t)i] = (uint8_t)tv;
-            if (c->local)
+            if (c->local || c->extend)
                 tracked = 1;
             else if (i < n)
                 tracked = finalCol && (fe & ORC_FREE_RIGHT);
             else
                 tracked = finalCol || (fe & ORC_FREE_BOTTOM);
             if (tracked) scout(b, colS[i], colE[i], f, j, i);
+            if (xdrop_on && colS[i] > colmax) colmax = colS[i];
+        }
+        if (xdrop_on) {
+            if (b->s - colmax >= xdrop) terminated = 1;
+            else colmax = INT_MIN;
+            if (terminated && j >= 1 && j < m) break;
         }
     }
 }
@@ -637,6 +651,7 @@ int orc_align_pair(const orc_params *p,
     c.bits16 = (p->score_bits == 16);
     c.inf = c.bits16 ? -16384 : -(1 << 30);
     c.local = (p->mode == ORC_LOCAL);
+    c.extend = (p->mode == ORC_EXTEND);
     c.affine = (p->gap_model == ORC_AFFINE);
     c.ext = p->gap_extend;
     c.open = p->gap_open;
@@ -644,7 +659,8 @@ int orc_align_pair(const orc_params *p,
     c.mismatch = p->mismatch;
     c.mat = p->matrix;
     c.asz = p->alphabet_size;
-    fe = c.local ? (ORC_FREE_TOP | ORC_FREE_LEFT | ORC_FREE_RIGHT | ORC_FREE_BOTTOM) : p->free_ends;
+    fe = c.local ? (ORC_FREE_TOP | ORC_FREE_LEFT | ORC_FREE_RIGHT | ORC_FREE_BOTTOM) : (c.extend ? 0 : p->free_ends);
+    if (c.extend && p->band_on) return -1;   /* the banded extension is not restated */
 
     if (m <= 0 || n <= 0 || !band_valid(p, m, n, fe)) {
         out->score = c.bits16 ? -32768 : INT_MIN;
@@ -664,7 +680,7 @@ int orc_align_pair(const orc_params *p,
         dp_banded(&c, fe, h, m, v, n, p->band_lower, p->band_upper, S, S + (size_t)(m + 1) * (size_t)(n + 1), T, &b);
         free(S);
     } else {
-        dp_unbanded(&c, fe, h, m, v, n, colS, colE, T, &b);
+        dp_unbanded(&c, fe, h, m, v, n, colS, colE, T, &b, c.extend && p->xdrop_on, p->xdrop);
     }
 
     out->score = b.s;
@@ -679,7 +695,7 @@ int orc_align_pair(const orc_params *p,
             else if (b.e == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFH; }
         }
         sb.segs = segs; sb.cap = segs ? seg_cap : 0; sb.n = 0; sb.overflow = 0;
-        traceback(&c, T, n, m, b.col, b.row, &sb, !c.local);
+        traceback(&c, T, n, m, b.col, b.row, &sb, !c.local && !c.extend, !c.local);
         out->n_segments = sb.overflow ? -1 : sb.n;
         if (sb.n > 0 && !sb.overflow) {
             out->begin_h = (int32_t)segs[sb.n - 1].h_begin;

@@ -26,14 +26,17 @@ enum {
     ORC_FREE_BOTTOM = 8   /* free last row     (DPLastRow)     */
 };
 
-enum { ORC_GLOBAL = 0, ORC_LOCAL = 1 };
+/* ORC_EXTEND: the DP of extendAlignment (align_extend/align_extend.h:115-206): AlignExtend_
+ * profile (align_extend/align_extend_base.h), i.e. a gap-initialised first row and column, every
+ * cell tracked without a zero floor, traceback to (0, 0) with no tail; unbanded. */
+enum { ORC_GLOBAL = 0, ORC_LOCAL = 1, ORC_EXTEND = 2 };
 enum { ORC_LINEAR = 0, ORC_AFFINE = 1 };
 
 /* TraceSegment_ direction values (align/dp_profile.h:121-135). */
 enum { ORC_SEG_DIAGONAL = 1, ORC_SEG_HORIZONTAL = 2, ORC_SEG_VERTICAL = 4 };
 
 typedef struct {
-    int32_t mode;           /* ORC_GLOBAL / ORC_LOCAL */
+    int32_t mode;           /* ORC_GLOBAL / ORC_LOCAL / ORC_EXTEND */
     int32_t gap_model;      /* ORC_LINEAR / ORC_AFFINE */
     int32_t free_ends;      /* ORC_FREE_* bits, ignored for local (all free) */
     int32_t band_on;        /* 0 / 1 */
@@ -44,6 +47,8 @@ typedef struct {
     int32_t alphabet_size;
     int32_t score_bits;     /* 16 or 32: cell width; 16 wraps like SeqAn's int16 SIMD lanes */
     int32_t traceback;      /* 0 = score only, 1 = trace segments */
+    int32_t xdrop_on;       /* ORC_EXTEND: the X-drop terminator (align_extend/dp_scout_xdrop.h) */
+    int32_t xdrop;
 } orc_params;
 
 typedef struct {

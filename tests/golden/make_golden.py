@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds]
+    python tests/golden/make_golden.py [--only seeds|extend]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -10,6 +10,8 @@ Outputs (all small, committed):
   alphabets.json        the reference's char -> ordValue maps for Dna5, Dna and AminoAcid.
   seed_cases.json       seeds extended by the reference's extendSeed (MatchExtend, UnGappedXDrop,
                         GappedXDrop; seeds/seeds_extension.h) with the gapped extension scores.
+  extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
+                        (align_extend/align_extend.h) with and without X-drop: score and rows.
   aa_background.json    residue counts of the reference's T-Coffee test FASTA files, the
                         stand-in for background amino-acid frequencies.
 """
@@ -82,8 +84,12 @@ def main():
     if not O.ref_available():
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"-j{os.cpu_count()}"])
     b62 = O.ref_blosum62()
-    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "seeds":
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "seeds":
         write_seeds(b62)
+        return
+    if only == "extend":
+        write_extend(b62)
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -220,6 +226,56 @@ def main():
                    "files": len(files), "counts": {c: cnt[c] for c in "ACDEFGHIKLMNPQRSTVWY"}}, f)
     print(f"{len(cases)} alignment cases written")
     write_seeds(b62)
+    write_extend(b62)
+
+
+def write_extend(b62):
+    """extendAlignment on ungapped seeds: random DNA and protein pairs (linear and affine gaps,
+    X-drop off and 0..30), plus read-mapping shapes (150 bp reads in 250 bp windows)."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(20261205))
+    cases = []
+
+    def add(pb, h, v, pos, d):
+        r = O.ref_extend_alignment(pb, h, v, pos, d)
+        cases.append({"alphabet": pb.alphabet, "blosum62": pb.matrix is not None, "match": pb.match,
+                      "mismatch": pb.mismatch, "gap_open": pb.gap_open, "gap_extend": pb.gap_extend,
+                      "xdrop": pb.xdrop, "H": text(h, pb.alphabet), "V": text(v, pb.alphabet),
+                      "positions": [int(x) for x in pos], "direction": int(d), "score": r.score,
+                      "row0": r.row0, "row1": r.row1, "ends": [r.h_begin, r.h_end, r.v_begin, r.v_end]})
+
+    for trial in range(600):
+        aa = trial % 4 == 3
+        A = 20 if aa else 4
+        L = int(rng.integers(2, 120))
+        h = rng.integers(0, A, L).astype(np.uint8)
+        v = W.mutate(rng, h, float(rng.uniform(0, 0.3)), float(rng.uniform(0, 0.08)), alphabet=A)
+        if trial % 5 == 0:
+            v = rng.integers(0, A, int(rng.integers(2, 120))).astype(np.uint8)
+        if aa:
+            h, v = W.AA20_CODES[h], W.AA20_CODES[v]
+        sl = int(rng.integers(1, min(len(h), len(v), 12) + 1))
+        hb = int(rng.integers(0, len(h) - sl + 1))
+        vb = min(max(hb + int(rng.integers(-3, 4)), 0), len(v) - sl)
+        xd = None if trial % 3 == 0 else int(rng.integers(0, 31))
+        if aa:
+            go = int(rng.choice([-11, -9, -4]))
+            pb = O.Problem("extend", 0, None, 0, 0, go, int(rng.choice([-1, go])), b62, 32, "aa", xd)
+        else:
+            go = int(rng.integers(-8, 0))
+            pb = O.Problem("extend", 0, None, int(rng.integers(1, 4)), int(rng.integers(-4, 0)), go,
+                           int(rng.choice([go, -1, -2])), None, 32, "dna", xd)
+        add(pb, h, v, (hb, vb, hb + sl, vb + sl), int(rng.integers(1, 4)))
+    wins, reads, seeds, _ = W.seed_windows(60, seed=15)
+    for k in range(60):
+        bh, bv, sl = (int(x) for x in seeds[k])
+        pb = O.Problem("extend", 0, None, 1, -2, -4 if k % 2 else -2, -1 if k % 2 else -2, None, 32, "dna",
+                       None if k % 3 == 0 else 20)
+        add(pb, wins[k], reads[k], (bh, bv, bh + sl, bv + sl), 3)
+    with open(os.path.join(HERE, "extend_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261205, "cases": cases}, f,
+                  separators=(",", ":"))
+    print(f"{len(cases)} extendAlignment cases written")
 
 
 def write_seeds(b62):
