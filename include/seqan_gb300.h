@@ -385,6 +385,44 @@ GBA_API int gba_extend_seeds(gba_context *ctx, const gba_extend_params *params, 
 GBA_API int gba_extend_seeds_device(gba_context *ctx, const gba_extend_params *params,
                                     const gba_seed_batch *dev_batch, gba_seed *dev_seeds, int32_t *dev_scores);
 
+/* --- Alignment extension ------------------------------------------------------------------
+ * extendAlignment(align, hSeq, vSeq, positions, direction, [xDrop,] scoreScheme)
+ * (align_extend/align_extend.h:211-372, 494-600), unbanded, over a batch.  For alignment k the
+ * aligned part spans hSeq[begin_h, end_h) / vSeq[begin_v, end_v) (positions from
+ * seeds[k]; the alignment itself is the caller's).  The left side runs the AlignExtend DP on the
+ * reversed prefixes when direction has LEFT and both begins are > 0, the right side on the
+ * suffixes when direction has RIGHT and both ends are inside their sequences: a gap-initialised
+ * first row and column, every cell tracked without a zero floor, traceback from the first
+ * maximum to the origin, and with xdrop_on the X-drop terminator of
+ * align_extend/dp_scout_xdrop.h (a column whose maximum lies xdrop or more below the best score
+ * ends the DP after the next inner-column check).  The reference's return value is
+ * left_score + the aligned part's score + right_score. */
+typedef struct {
+    int32_t direction;         /* GBA_EXTEND_LEFT / GBA_EXTEND_RIGHT / GBA_EXTEND_BOTH */
+    int32_t xdrop_on, xdrop;   /* the xDrop argument */
+    int32_t match, mismatch;   /* Score<int, Simple> (ignored with a matrix) */
+    int32_t gap_open, gap_extend;   /* Gotoh iff open != extend, as the reference picks */
+    const int32_t *matrix;     /* optional host alphabet_size^2 table (row = H residue) */
+    int32_t alphabet_size;     /* 1..32 with a matrix */
+    int32_t reserved;
+} gba_extend_align_params;
+
+typedef struct {
+    int32_t *left_score, *right_score;   /* [num_seeds]; 0 for a side that was not extended */
+    /* TraceSegment_ lists in traceback order (last segment = the side's alignment begin): the
+     * left side's in prefix coordinates (after the reference's _reversePartialTrace,
+     * align_extend/align_extend.h:91-109), the right side's in suffix coordinates.  Alignment
+     * k's left side owns segments[segment_offsets[2k] .. [2k+1]), its right side
+     * [segment_offsets[2k+1] .. [2k+2]). */
+    gba_segment *segments;
+    int64_t segment_capacity;
+    int64_t *segment_offsets;  /* [2 * num_seeds + 1] */
+} gba_extend_align_result;
+
+GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_params *params,
+                                  const gba_seed_batch *batch, const gba_seed *seeds,
+                                  gba_extend_align_result *result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,7 +44,7 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc",
             "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
             "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule",
-            "gba_extend_seeds", "gba_extend_seeds_device"]
+            "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments"]
 
 
 class GbaConfig(C.Structure):
@@ -124,6 +124,17 @@ class GbaSeedBatch(C.Structure):
                 ("max_v_len", C.c_int64)]
 
 
+class GbaExtendAlignParams(C.Structure):
+    _fields_ = [("direction", C.c_int32), ("xdrop_on", C.c_int32), ("xdrop", C.c_int32), ("match", C.c_int32),
+                ("mismatch", C.c_int32), ("gap_open", C.c_int32), ("gap_extend", C.c_int32),
+                ("matrix", C.c_void_p), ("alphabet_size", C.c_int32), ("reserved", C.c_int32)]
+
+
+class GbaExtendAlignResult(C.Structure):
+    _fields_ = [("left_score", C.c_void_p), ("right_score", C.c_void_p), ("segments", C.c_void_p),
+                ("segment_capacity", C.c_int64), ("segment_offsets", C.c_void_p)]
+
+
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + \
         [os.path.join(INCLUDE, "seqan_gb300.h")]
@@ -193,6 +204,8 @@ def lib():
             L.gba_server_destroy.argtypes = [vp]
             L.gba_extend_seeds.argtypes = [vp, C.POINTER(GbaExtendParams), C.POINTER(GbaSeedBatch), vp, vp]
             L.gba_extend_seeds_device.argtypes = [vp, C.POINTER(GbaExtendParams), C.POINTER(GbaSeedBatch), vp, vp]
+            L.gba_extend_alignments.argtypes = [vp, C.POINTER(GbaExtendAlignParams), C.POINTER(GbaSeedBatch), vp,
+                                                C.POINTER(GbaExtendAlignResult)]
             L.gba_clock_seconds.argtypes = []
             L.gba_clock_seconds.restype = C.c_double
             _lib = L

@@ -12,6 +12,7 @@
 #include "dp_banded_kernels.cuh"
 #include "dp_warp_kernels.cuh"
 #include "seed_kernels.cuh"
+#include "extend_kernels.cuh"
 #include "int_peak.cuh"
 
 #include <cub/device/device_scan.cuh>
@@ -200,6 +201,8 @@ struct gba_context {
         xs_results;
     bool xs_check = false;          // a device seed-extension run whose error word is unread
     std::map<std::pair<const void *, size_t>, int64_t> xs_grid;   // (kernel, smem) -> resident blocks
+    // alignment extension: tasks, per-task results, trace, segments, scratch
+    DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next;
 };
 
 namespace {
@@ -1786,3 +1789,4 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 
 #include "server.cuh"
 #include "seeds_host.cuh"
+#include "extend_host.cuh"
