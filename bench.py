@@ -50,6 +50,11 @@ WORKLOADS = {
                       "GappedXDrop, Score<int,Simple>(1,-2,-2), scoreDropOff 20; seeds + extension scores",
 }
 SEED_WORKLOADS = {"xdrop_reads_1m"}
+WORKLOADS["extend_reads_250k"] = ("250000 read alignments: 150 bp reads (3% subs, 0.3% indels) in 250 bp windows of a "
+                                  "10 Mbp reference, the aligned part a 19-mer seed on the true diagonal; "
+                                  "extendAlignment EXTEND_BOTH, xDrop 20, Score<int,Simple>(2,-4,-1,-6); scores + "
+                                  "trace segments of both sides")
+EXTEND_WORKLOADS = {"extend_reads_250k"}
 # Integer ops of one x-drop cell: max(up, left) + gap, diagonal + score, the max of the two, the
 # drop-off compare and the anti-diagonal best (add and max each count one).
 XDROP_OPS_PER_CELL = 6
@@ -445,6 +450,163 @@ def run_seed_bench(args, rank, world, local_rank, dist):
         print(json.dumps(line), flush=True)
 
 
+def extend_sides(wins, reads, seeds):
+    """The side tasks of extendAlignment: reversed prefixes (left) and suffixes (right)."""
+    H, V = [], []
+    for w, r, s in zip(wins, reads, seeds):
+        bh, bv, L = (int(x) for x in s)
+        if bh > 0 and bv > 0:
+            H.append(np.ascontiguousarray(w[:bh][::-1]))
+            V.append(np.ascontiguousarray(r[:bv][::-1]))
+        if bh + L < len(w) and bv + L < len(r):
+            H.append(np.ascontiguousarray(w[bh + L:]))
+            V.append(np.ascontiguousarray(r[bv + L:]))
+    return H, V
+
+
+def extend_cpu_time(H, V, threads):
+    from oracle import oracle as O
+    pb = O.Problem("extend", 0, None, 2, -4, -6, -1, None, 32, "dna", 20)
+    t0 = time.perf_counter()
+    O.oracle_batch(pb, H, V, traceback=True, threads=threads)
+    return time.perf_counter() - t0
+
+
+def run_extend_bench(args, rank, world, local_rank, dist):
+    import seqan_gb300 as sg
+    from seqan_gb300 import _native as N
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    h = ctx.handle
+    from seqan_gb300 import workloads as W
+    n_al = args.pairs or 250_000
+    wins, reads, seeds, _ = W.seed_windows(n_al, seed=16 + rank)
+    sh, oh = concat(wins)
+    sv, ov = concat(reads)
+    pos = np.zeros((n_al, 6), dtype=np.int64)
+    pos[:, 0], pos[:, 1] = seeds[:, 0], seeds[:, 1]
+    pos[:, 2], pos[:, 3] = seeds[:, 0] + seeds[:, 2], seeds[:, 1] + seeds[:, 2]
+
+    def pinned(a):
+        p = C.c_void_p()
+        ctx.check(L.gba_host_alloc(h, C.byref(p), max(a.nbytes, 1)), "gba_host_alloc")
+        C.memmove(p, a.ctypes.data, a.nbytes)
+        return p
+
+    p_sh, p_oh, p_sv, p_ov, p_pos = pinned(sh), pinned(oh), pinned(sv), pinned(ov), pinned(pos)
+    score = sg.Score(2, -4, -1, -6)
+    params = N.GbaExtendAlignParams(3, 1, 20, score.match, score.mismatch, score.gap_open, score.gap_extend,
+                                    None, 0, 0)
+    batch = N.GbaSeedBatch(n_al, p_sh, p_oh, n_al, p_sv, p_ov, n_al, None, None, 0)
+    cap = int(len(sh) + len(sv) + 8 * n_al)
+    segs = np.zeros((cap, 4), dtype=np.uint32)
+    offs = np.zeros(2 * n_al + 1, dtype=np.int64)
+    ls = np.zeros(n_al, dtype=np.int32)
+    rs = np.zeros(n_al, dtype=np.int32)
+    res = N.GbaExtendAlignResult(ls.ctypes.data, rs.ctypes.data, segs.ctypes.data, cap, offs.ctypes.data)
+
+    def call():
+        ctx.check(L.gba_extend_alignments(h, C.byref(params), C.byref(batch), p_pos, C.byref(res)), "extend")
+
+    for _ in range(args.warmup):
+        call()
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    sampler.start()
+    wall, kern, dpk = [], [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        wall.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        kern.append(st.dp_kernel_ms + st.traceback_kernel_ms)
+        dpk.append(st.dp_kernel_ms)
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    st = ctx.stats()
+    kernel_ms = sum(kern) / len(kern)
+    value = n_al * world / (kernel_ms * 1e-3) / 1e6
+    e2e = n_al * world * len(wall) / sum(wall) / 1e6
+    # parity spot check: the first 2,000 alignments against the oracle
+    from seqan_gb300 import align_extend as X
+    from oracle import oracle as O
+    pb = O.Problem("extend", 0, None, 2, -4, -6, -1, None, 32, "dna", 20)
+    parity = True
+    for k in range(min(n_al, 2000)):
+        ext = X.SideExtension(int(ls[k]), int(rs[k]),
+                              [tuple(int(x) for x in segs[q]) for q in range(offs[2 * k], offs[2 * k + 1])],
+                              [tuple(int(x) for x in segs[q]) for q in range(offs[2 * k + 1], offs[2 * k + 2])])
+        ref = O.oracle_extend_alignment(pb, wins[k], reads[k], pos[k, :4], 3)
+        if (ext.left_score, ext.right_score, ext.left_segments, ext.right_segments) != \
+                (ref.left_score, ref.right_score, ref.left_segments, ref.right_segments):
+            parity = False
+            break
+    peak = C.c_double()
+    ctx.check(L.gba_measure_int_peak(h, C.byref(peak)), "int peak")
+    dp_ms = sum(dpk) / len(dpk)
+    ops = 2 * st.cells * OPS_PER_CELL["affine_global"]     # score pass + trace pass over the same cells
+    achieved = ops / (dp_ms * 1e-3) / 1e12
+    line = {"metric": "M alignments/s, batched extendAlignment (X-drop)", "value": value, "unit": "M alignments/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "alignments": n_al,
+                       "cells_per_step": int(st.cells),
+                       "value_timing": "CUDA events around the score pass, trace pass and traceback inside "
+                                       "gba_extend_alignments (inputs in HBM)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "M alignments/s",
+                    "h2d_bytes_per_step": int(sh.nbytes + sv.nbytes + oh.nbytes + ov.nbytes + pos.nbytes),
+                    "d2h_bytes_per_step": int(offs[-1]) * 16 + int(offs.nbytes) + 2 * n_al * 4,
+                    "ms_per_step": 1e3 * sum(wall) / len(wall), "last_call_ms": st.call_ms},
+            "gpu_launches": args.steps * int(st.kernel_launches),
+            "roofline": {"bound": "int32", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "kernel": "k_extend_dp<affine> (score and trace passes) + k_extend_traceback",
+                         "ops_per_cell": OPS_PER_CELL["affine_global"], "dp_kernel_ms": dp_ms,
+                         "gcups_per_pass": st.cells / (dp_ms / 2 * 1e-3) / 1e9,
+                         "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"},
+            "clocks": clocks, "parity_first_2000_vs_oracle": parity}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        n = min(n_al, 50_000)
+        Hs, Vs = extend_sides(wins[:n], reads[:n], seeds[:n])
+        best = min(extend_cpu_time(Hs, Vs, threads) for _ in range(2))
+        line["cpu_baseline"] = {"value": n / best / 1e6, "unit": "M alignments/s", "cores": threads, "kind": "port",
+                                "sample": f"both sides of the first {n} alignments: the oracle's extension DP with "
+                                          f"X-drop and traceback (oracle/seqan_oracle.c), OpenMP over {threads} "
+                                          "threads, best of 2", "seconds": best}
+    for p in (p_sh, p_oh, p_sv, p_ov, p_pos):
+        L.gba_host_free(h, p)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_extend_reference(args):
+    from seqan_gb300 import workloads as W
+    n_al = min(args.pairs or 250_000, 50_000)
+    wins, reads, seeds, _ = W.seed_windows(n_al, seed=16)
+    Hs, Vs = extend_sides(wins, reads, seeds)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        extend_cpu_time(Hs, Vs, threads)
+    times = [extend_cpu_time(Hs, Vs, threads) for _ in range(args.steps)]
+    rate = n_al * len(times) / sum(times) / 1e6
+    print(json.dumps({"metric": "M alignments/s, batched extendAlignment (X-drop)", "value": rate,
+                      "unit": "M alignments/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload, "alignments_per_step": n_al,
+                                 "description": WORKLOADS[args.workload]},
+                      "cpu_baseline": {"value": rate, "unit": "M alignments/s", "cores": threads, "kind": "port",
+                                       "sample": f"both sides of {n_al} alignments per step, the oracle's extension "
+                                                 "DP with X-drop and traceback, OpenMP"},
+                      "e2e": {"value": rate, "unit": "M alignments/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
 def serving_requests(n: int, seed: int):
     """Mixed-length affine DNA requests: 90% U[100,500], 9% U[1000,5000], 1% 10,000 bp; the
     partner has 5% substitutions and 1% indels."""
@@ -527,7 +689,10 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
-        if args.workload in SEED_WORKLOADS:
+        if args.workload in EXTEND_WORKLOADS:
+            if rank == 0:
+                run_extend_reference(args)
+        elif args.workload in SEED_WORKLOADS:
             if rank == 0:
                 run_seed_reference(args)
         else:
@@ -537,6 +702,11 @@ def main():
         return
     if args.workload in SEED_WORKLOADS:
         run_seed_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in EXTEND_WORKLOADS:
+        run_extend_bench(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
         return

@@ -202,7 +202,7 @@ struct gba_context {
     bool xs_check = false;          // a device seed-extension run whose error word is unread
     std::map<std::pair<const void *, size_t>, int64_t> xs_grid;   // (kernel, smem) -> resident blocks
     // alignment extension: tasks, per-task results, trace, segments, scratch
-    DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next;
+    DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next, xa_packoff, xa_packed;
 };
 
 namespace {

@@ -33,37 +33,48 @@ int ext_check_params(gba_context *ctx, const gba_extend_align_params *p, std::ve
     return GBA_OK;
 }
 
-template <bool AFFINE, bool MATRIX, bool TRACE>
+template <bool AFFINE, bool MATRIX, bool TRACE, int W>
 int ext_launch_dp(gba_context *ctx, const ExtArgs &a)
 {
-    const void *fn = reinterpret_cast<const void *>(k_extend_dp<AFFINE, MATRIX, TRACE>);
+    const void *fn = reinterpret_cast<const void *>(k_extend_dp<AFFINE, MATRIX, TRACE, W>);
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, 0) != cudaSuccess || nb < 1) nb = 1;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const int64_t warps_needed = a.num_tasks;
-    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(int64_t(nb) * sms, (warps_needed + 3) / 4));
-    k_extend_dp<AFFINE, MATRIX, TRACE><<<unsigned(blocks), 128, 0, ctx->stream>>>(a);
+    const int64_t threads_needed = int64_t(a.num_tasks) * W;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(int64_t(nb) * sms, (threads_needed + 127) / 128));
+    k_extend_dp<AFFINE, MATRIX, TRACE, W><<<unsigned(blocks), 128, 0, ctx->stream>>>(a);
     GBA_CUDA(ctx, cudaGetLastError());
     return GBA_OK;
 }
 
-int ext_dp(gba_context *ctx, bool affine, bool matrix, bool trace, const ExtArgs &a)
+template <int W>
+int ext_dp_w(gba_context *ctx, bool affine, bool matrix, bool trace, const ExtArgs &a)
 {
     if (affine) {
-        if (matrix) return trace ? ext_launch_dp<true, true, true>(ctx, a) : ext_launch_dp<true, true, false>(ctx, a);
-        return trace ? ext_launch_dp<true, false, true>(ctx, a) : ext_launch_dp<true, false, false>(ctx, a);
+        if (matrix)
+            return trace ? ext_launch_dp<true, true, true, W>(ctx, a) : ext_launch_dp<true, true, false, W>(ctx, a);
+        return trace ? ext_launch_dp<true, false, true, W>(ctx, a) : ext_launch_dp<true, false, false, W>(ctx, a);
     }
-    if (matrix) return trace ? ext_launch_dp<false, true, true>(ctx, a) : ext_launch_dp<false, true, false>(ctx, a);
-    return trace ? ext_launch_dp<false, false, true>(ctx, a) : ext_launch_dp<false, false, false>(ctx, a);
+    if (matrix) return trace ? ext_launch_dp<false, true, true, W>(ctx, a) : ext_launch_dp<false, true, false, W>(ctx, a);
+    return trace ? ext_launch_dp<false, false, true, W>(ctx, a) : ext_launch_dp<false, false, false, W>(ctx, a);
 }
 
-// Resident warps of the DP kernels (an upper bound on the warps that need scratch).
-int64_t ext_max_warps(gba_context *ctx)
+// Lanes per task: 8 rows per lane, so a group of W lanes covers 8W rows per band; W follows the
+// batch's 90th-percentile task height (read halves of ~75 rows fill 8 or 16 lanes, not 32).
+int ext_dp(gba_context *ctx, int W, bool affine, bool matrix, bool trace, const ExtArgs &a)
+{
+    if (W == 8) return ext_dp_w<8>(ctx, affine, matrix, trace, a);
+    if (W == 16) return ext_dp_w<16>(ctx, affine, matrix, trace, a);
+    return ext_dp_w<32>(ctx, affine, matrix, trace, a);
+}
+
+// Resident groups of W lanes (an upper bound on the groups that need scratch).
+int64_t ext_max_groups(gba_context *ctx, int W)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    return int64_t(std::max(sms, 1)) * 16 * 4;   // 16 blocks of 4 warps per SM at most
+    return int64_t(std::max(sms, 1)) * 2048 / W;   // 2,048 resident threads per SM at most
 }
 
 }  // namespace
@@ -132,10 +143,19 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
         }
     }
     const int64_t nt = int64_t(tasks.size());
+    int W = 32;
+    if (nt > 0) {
+        std::vector<int32_t> heights(static_cast<size_t>(nt), 0);
+        for (int64_t t = 0; t < nt; ++t) heights[t] = tasks[t].n + 1;
+        const size_t q = size_t(nt) * 9 / 10;
+        std::nth_element(heights.begin(), heights.begin() + q, heights.end());
+        const int p90 = heights[q];
+        W = p90 <= 8 * 8 ? 8 : (p90 <= 8 * 16 ? 16 : 32);
+    }
     std::vector<ExtOut> outs(size_t(std::max<int64_t>(nt, 1)));
     std::vector<int32_t> counts;
     std::vector<ExtSegment> segs_host;
-    std::vector<int64_t> seg_off_host;
+    std::vector<int64_t> seg_off_host, packed_off;
     int launches = 0;
     float dp_ms = 0, tb_ms = 0;
     int64_t cells = 0;
@@ -162,15 +182,15 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
         a.asize = params->alphabet_size;
         a.xdrop_on = params->xdrop_on;
         a.xdrop = params->xdrop;
-        if (max_n + 1 > kExtBand) {
+        if (max_n + 1 > 8 * W) {
             a.scratch_stride = 2 * (max_n + 1);
-            GBA_CUDA(ctx, ctx->xa_scratch.ensure(size_t(ext_max_warps(ctx)) * size_t(a.scratch_stride) * 4));
+            GBA_CUDA(ctx, ctx->xa_scratch.ensure(size_t(ext_max_groups(ctx, W)) * size_t(a.scratch_stride) * 4));
             a.scratch = ctx->xa_scratch.as<int32_t>();
         }
         // score pass
         GBA_CUDA(ctx, cudaMemsetAsync(a.next, 0, 4, st));
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-        if (int rc = ext_dp(ctx, affine, matrix, false, a)) return rc;
+        if (int rc = ext_dp(ctx, W, affine, matrix, false, a)) return rc;
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
         ++launches;
         GBA_CUDA(ctx, cudaMemcpyAsync(outs.data(), a.out, size_t(nt) * sizeof(ExtOut), cudaMemcpyDeviceToHost, st));
@@ -216,7 +236,7 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
             at.trace = ctx->xa_trace.as<uint8_t>();
             GBA_CUDA(ctx, cudaMemsetAsync(a.next, 0, 4, st));
             GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-            if (int rc = ext_dp(ctx, affine, matrix, true, at)) return rc;
+            if (int rc = ext_dp(ctx, W, affine, matrix, true, at)) return rc;
             GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
             const unsigned grid = unsigned((c1 - c0 + 127) / 128);
             if (affine)
@@ -240,11 +260,28 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
             tb_ms += ms2;
             c0 = c1;
         }
+        // pack the used part of each slot, then copy only that back
         counts.resize(size_t(nt));
-        segs_host.resize(size_t(seg_off_host[nt]));
         GBA_CUDA(ctx, cudaMemcpyAsync(counts.data(), ctx->xa_segcnt.ptr, size_t(nt) * 4, cudaMemcpyDeviceToHost, st));
-        GBA_CUDA(ctx, cudaMemcpyAsync(segs_host.data(), ctx->xa_segs.ptr, segs_host.size() * sizeof(ExtSegment),
-                                      cudaMemcpyDeviceToHost, st));
+        GBA_CUDA(ctx, cudaStreamSynchronize(st));
+        packed_off.assign(size_t(nt) + 1, 0);
+        for (int64_t t = 0; t < nt; ++t) {
+            if (counts[t] < 0) return fail(ctx, GBA_ECUDA, "traceback slot overflow (internal)");
+            packed_off[t + 1] = packed_off[t] + counts[t];
+        }
+        GBA_CUDA(ctx, ctx->xa_packoff.ensure(size_t(nt + 1) * 8));
+        GBA_CUDA(ctx, ctx->xa_packed.ensure(size_t(std::max<int64_t>(packed_off[nt], 1)) * sizeof(ExtSegment)));
+        GBA_CUDA(ctx, cudaMemcpyAsync(ctx->xa_packoff.ptr, packed_off.data(), size_t(nt + 1) * 8,
+                                      cudaMemcpyHostToDevice, st));
+        k_extend_pack<<<unsigned((nt + 127) / 128), 128, 0, st>>>(
+            ctx->xa_segs.as<ExtSegment>(), ctx->xa_segoff.as<int64_t>(), ctx->xa_segcnt.as<int32_t>(),
+            ctx->xa_packoff.as<int64_t>(), ctx->xa_packed.as<ExtSegment>(), int(nt));
+        GBA_CUDA(ctx, cudaGetLastError());
+        ++launches;
+        segs_host.resize(size_t(packed_off[nt]));
+        if (packed_off[nt])
+            GBA_CUDA(ctx, cudaMemcpyAsync(segs_host.data(), ctx->xa_packed.ptr, segs_host.size() * sizeof(ExtSegment),
+                                          cudaMemcpyDeviceToHost, st));
         GBA_CUDA(ctx, cudaStreamSynchronize(st));
     }
     // Results: scores and segment lists; the left side's trace is mapped back from the reversed
@@ -257,8 +294,7 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
             if (t >= 0) {
                 score = outs[t].score;
                 const int32_t c = counts[t];
-                if (c < 0) return fail(ctx, GBA_ECUDA, "traceback slot overflow (internal)");
-                const ExtSegment *sg = segs_host.data() + seg_off_host[t];
+                const ExtSegment *sg = segs_host.data() + packed_off[t];
                 if (w + c > res->segment_capacity || (c && !res->segments))
                     return fail(ctx, GBA_ECAPACITY, "segment_capacity too small");
                 if (side == 1) {

@@ -3,8 +3,9 @@
 // column, every cell tracked, no zero floor -- with the optional X-drop terminator
 // (align_extend/dp_scout_xdrop.h), and its traceback to the origin.
 //
-// One warp per extension task (one side of one alignment), column-synchronous: lane L owns rows
-// 8L..8L+7 of each 256-row band, and a column is finished by all lanes before the next starts,
+// A group of W lanes (W = 8, 16 or 32; 32 / W groups per warp) per extension task (one side of
+// one alignment), column-synchronous: lane L of the group owns rows 8L..8L+7 of each 8W-row band,
+// and a column is finished by all lanes before the next starts,
 // so the column maximum (the X-drop rule) and the first maximum in column-major order (the
 // scout) are exact at every column and the DP stops exactly where the reference stops.  The
 // vertical gap chain of a column is a max-plus prefix scan: with X_i the best of the diagonal and
@@ -12,7 +13,9 @@
 //     affine:  F_{i+1} = max(F_i + max(ext, open), X_i + open),  S_i = max(X_i, F_i)
 //     linear:  S_i     = max(X_i, S_{i-1} + ext)
 // (max(F + ext, max(X, F) + open) = max(F + max(ext, open), X + open)), so each lane folds its
-// 8 rows, the warp scans the lane aggregates with five shuffles, and each lane replays its rows.
+// 8 rows, the group scans the lane aggregates with log2(W) shuffles, and each lane replays its
+// rows.  Groups of one warp run different tasks; their shuffles and ballots use the group's lanes
+// only, so a group that finishes a task fetches the next while the others continue.
 // Trace bits follow the reference's comparisons cell by cell (align/dp_formula_affine.h:66-125,
 // dp_formula_linear.h:62-106, the left operand winning ties).  Scores are int (the reference's
 // TScoreValue for Score<int, ...>); "infinity" is -2^30 (align/dp_cell.h:143-146).
@@ -24,7 +27,6 @@
 namespace gba {
 
 constexpr int kExtRows = 8;                    // rows per lane
-constexpr int kExtBand = 32 * kExtRows;        // rows per band
 constexpr int kExtInf = -(1 << 30);
 
 enum : uint8_t { XT_DIAG = 1, XT_H = 2, XT_V = 4, XT_HO = 8, XT_VO = 16, XT_MFH = 32, XT_MFV = 64 };
@@ -54,11 +56,15 @@ struct ExtArgs {
     int32_t asize;
     int32_t xdrop_on, xdrop;
     uint8_t *trace;
-    int32_t *scratch;          // per warp: 2 * (max n + 1) ints (bands after the first)
+    int32_t *scratch;          // per group: 2 * (max n + 1) ints (tasks with more than one band)
     int64_t scratch_stride;
 };
 
 __host__ __device__ inline int ext_trace_stride(int n) { return (n + 1 + 7) & ~7; }
+
+struct ExtSegment {
+    uint32_t h_begin, v_begin, length, type;
+};
 
 template <bool MATRIX>
 __device__ __forceinline__ int ext_sub(const ExtArgs &a, const int32_t *smat, int hc, int vc)
@@ -67,7 +73,7 @@ __device__ __forceinline__ int ext_sub(const ExtArgs &a, const int32_t *smat, in
     return hc == vc ? a.match : a.mismatch;
 }
 
-template <bool AFFINE, bool MATRIX, bool TRACE>
+template <bool AFFINE, bool MATRIX, bool TRACE, int W>
 __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
 {
     __shared__ int32_t smat[32 * 32];
@@ -75,10 +81,11 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
         for (int t = threadIdx.x; t < a.asize * a.asize; t += blockDim.x) smat[t] = a.matrix[t];
     }
     __syncthreads();
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int32_t *const scr = a.scratch ? a.scratch + (size_t)warp_global * a.scratch_stride : nullptr;
+    constexpr int kExtBand = W * kExtRows;             // rows per band
+    const int lane = threadIdx.x & (W - 1);            // lane within the group
+    const unsigned FULL = W == 32 ? 0xffffffffu : (((1u << W) - 1u) << ((threadIdx.x & 31) & ~(W - 1)));
+    const int group_global = (blockIdx.x * blockDim.x + threadIdx.x) / W;
+    int32_t *const scr = a.scratch ? a.scratch + (size_t)group_global * a.scratch_stride : nullptr;
     const int open = a.gap_open, ext = a.gap_extend;
     const int g = AFFINE ? max(ext, open) : ext;       // the vertical chain's per-row step
     const int g8 = kExtRows * g;
@@ -86,7 +93,7 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
     for (;;) {
         int t = 0;
         if (lane == 0) t = atomicAdd(a.next, 1);
-        t = __shfl_sync(FULL, t, 0);
+        t = __shfl_sync(FULL, t, 0, W);
         if (t >= a.num_tasks) break;
         const ExtTask tk = a.tasks[t];
         const int m = tk.m, n = tk.n;
@@ -128,9 +135,9 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
                     }
                 }
                 // previous column's S of the row above each of this lane's rows
-                int up = __shfl_up_sync(FULL, Sp[kExtRows - 1], 1);
+                int up = __shfl_up_sync(FULL, Sp[kExtRows - 1], 1, W);
                 if (lane == 0) up = bandDiag;
-                const int lastOld = __shfl_sync(FULL, Sp[kExtRows - 1], 31);
+                const int lastOld = __shfl_sync(FULL, Sp[kExtRows - 1], W - 1, W);
                 // X (best of diagonal and horizontal), E and their bits
                 int X[kExtRows], E[kExtRows];
                 uint8_t bits[kExtRows];
@@ -180,11 +187,11 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
                 int bnorm = agg - lane * g8;
                 int pre = bnorm;
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int q = __shfl_up_sync(FULL, pre, o);
+                for (int o = 1; o < W; o <<= 1) {
+                    const int q = __shfl_up_sync(FULL, pre, o, W);
                     if (lane >= o) pre = max(pre, q);
                 }
-                int excl = __shfl_up_sync(FULL, pre, 1);
+                int excl = __shfl_up_sync(FULL, pre, 1, W);
                 int in = bandF + lane * g8;               // what enters the band's first row, carried down
                 if (lane > 0) in = max(in, excl + (lane - 1) * g8);
                 // replay the lane's rows
@@ -207,8 +214,8 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
                     }
                 }
                 // the row above each row, final values of this column (for the trace bits)
-                int upF = __shfl_up_sync(FULL, F[kExtRows - 1], 1);
-                int upS = __shfl_up_sync(FULL, S[kExtRows - 1], 1);
+                int upF = __shfl_up_sync(FULL, F[kExtRows - 1], 1, W);
+                int upS = __shfl_up_sync(FULL, S[kExtRows - 1], 1, W);
                 if (lane == 0) {
                     upF = aboveF;
                     upS = aboveS;
@@ -263,13 +270,13 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
                 }
                 int wmax = lmax;
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(FULL, wmax, o));
-                const unsigned holders = __ballot_sync(FULL, lmax == wmax && lmax != INT_MIN);
+                for (int o = W / 2; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(FULL, wmax, o, W));
+                const unsigned holders = __ballot_sync(FULL, lmax == wmax && lmax != INT_MIN) & FULL;
                 if (holders) {
-                    const int src = __ffs(holders) - 1;
-                    const int brow = __shfl_sync(FULL, lrow, src);
-                    const int be = __shfl_sync(FULL, le, src);
-                    const int bf = __shfl_sync(FULL, lf, src);
+                    const int src = (__ffs(holders) - 1) & (W - 1);
+                    const int brow = __shfl_sync(FULL, lrow, src, W);
+                    const int be = __shfl_sync(FULL, le, src, W);
+                    const int bf = __shfl_sync(FULL, lf, src, W);
                     if (wmax > cbS) {       // earlier bands keep ties (smaller rows)
                         cbS = wmax;
                         cbR = brow;
@@ -282,12 +289,12 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
                 bandDiag = lastOld;
                 if (AFFINE) {
                     const int fNext = max(F[kExtRows - 1] + g, X[kExtRows - 1] + open);
-                    bandF = __shfl_sync(FULL, fNext, 31);
+                    bandF = __shfl_sync(FULL, fNext, W - 1, W);
                 } else {
-                    bandF = __shfl_sync(FULL, S[kExtRows - 1], 31);
+                    bandF = __shfl_sync(FULL, S[kExtRows - 1], W - 1, W);
                 }
-                aboveF = __shfl_sync(FULL, F[kExtRows - 1], 31);
-                aboveS = __shfl_sync(FULL, S[kExtRows - 1], 31);
+                aboveF = __shfl_sync(FULL, F[kExtRows - 1], W - 1, W);
+                aboveS = __shfl_sync(FULL, S[kExtRows - 1], W - 1, W);
 #pragma unroll
                 for (int r = 0; r < kExtRows; ++r) {
                     Sp[r] = S[r];
@@ -302,7 +309,7 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
                             scr[n + 1 + i] = E[r];
                         }
                     }
-                    __syncwarp();
+                    __syncwarp(FULL);
                 }
             }
             // the scout: first maximum in column-major order
@@ -333,18 +340,27 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
             o.pad[0] = o.pad[1] = 0;
             a.out[t] = o;
         }
-        __syncwarp();
+        __syncwarp(FULL);
     }
+}
+
+// Copies each task's segments from its traceback slot to the packed output (one thread per task).
+__global__ void __launch_bounds__(128) k_extend_pack(const ExtSegment *slots, const int64_t *slot_off,
+                                                     const int32_t *count, const int64_t *packed_off,
+                                                     ExtSegment *packed, int num_tasks)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= num_tasks) return;
+    const int c = count[t];
+    const ExtSegment *src = slots + slot_off[t];
+    ExtSegment *dst = packed + packed_off[t];
+    for (int q = 0; q < c; ++q) dst[q] = src[q];
 }
 
 // Traceback of one task from its best cell to the origin (align/dp_traceback_impl.h:190-546 with
 // the AlignExtend_ profile: TraceTail_ false, TraceHead_ true), one thread per task.  Segments in
 // traceback order (last = alignment begin) go to segs[seg_off[t] ...]; seg_count[t] gets their
 // number (-1 if the slot was too small).
-struct ExtSegment {
-    uint32_t h_begin, v_begin, length, type;
-};
-
 __device__ inline void ext_record(ExtSegment *s, int cap, int &cnt, int hb, int vb, int len, int tv)
 {
     if (len == 0) return;

@@ -87,6 +87,27 @@ def test_tall_queries_use_several_bands(engine):
         check_batch(pb, H, V, pos, O.EXTEND_BOTH)
 
 
+def test_narrow_groups_with_tall_minority(engine):
+    """70 bp reads (task heights <= 64: eight lanes per task) plus 5% reads of 300 bp whose sides
+    span several 64-row bands."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.default_rng(29)
+    H, V, pos = [], [], []
+    for k in range(1500):
+        L = 300 if k % 20 == 0 else 70
+        o = int(rng.integers(0, 40))
+        win = rng.integers(0, 4, L + 80).astype(np.uint8)
+        read = W.mutate(rng, win[o + 10:o + 10 + L], 0.04, 0.01)
+        sl = min(11, len(read) - 1)
+        s0 = int(rng.integers(0, len(read) - sl))
+        H.append(win)
+        V.append(read)
+        pos.append((o + 10 + s0, s0, o + 10 + s0 + sl, s0 + sl))
+    for xdrop in (None, 12):
+        pb = O.Problem("extend", 0, None, 2, -3, -5, -1, None, 32, "dna", xdrop)
+        check_batch(pb, H, V, pos, O.EXTEND_BOTH)
+
+
 def test_long_database_cut_short_by_xdrop(engine):
     """Reads seeded inside a 200 kbp database shared by all alignments: the extension over the
     database prefix / suffix stops where the X-drop terminator stops the reference."""
