@@ -553,7 +553,7 @@ def run_extend_bench(args, rank, world, local_rank, dist):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "alignments": n_al,
-                       "cells_per_step": int(st.cells),
+                       "cells_per_step": int(st.cells), "rows_per_band": int(st.tile_rows),
                        "value_timing": "CUDA events around the score pass, trace pass and traceback inside "
                                        "gba_extend_alignments (inputs in HBM)",
                        "parallelism": f"replicas x{world}"},

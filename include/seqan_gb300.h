@@ -200,7 +200,8 @@ typedef struct {
     int32_t kernel_launches;   /* kernels this library launched for the batch */
     int64_t cells;             /* algorithmic cells: sum m*n (in-band cells when banded) */
     int64_t trace_bytes;       /* trace matrix bytes written */
-    int32_t tile_rows;         /* packed kernel: rows per register strip (0 = not used) */
+    int32_t tile_rows;         /* packed kernel: rows per register strip (0 = not used);
+                                  gba_extend_alignments: rows per band (8 x lanes per task) */
     int32_t tile_min_blocks;   /* packed kernel: minimum resident blocks per SM */
     float host_plan_ms;        /* gba_align_batch: host planning time */
     float call_ms;             /* gba_align_batch: whole call, wall clock */

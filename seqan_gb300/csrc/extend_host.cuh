@@ -321,6 +321,7 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
     ctx->stats.traceback_kernel_ms = tb_ms;
     ctx->stats.kernel_launches = launches;
     ctx->stats.cells = cells;
+    ctx->stats.tile_rows = 8 * W;      // rows per band (lanes per task x 8)
     ctx->stats.call_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return GBA_OK;
 }

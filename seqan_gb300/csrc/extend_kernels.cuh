@@ -111,8 +111,10 @@ __global__ void __launch_bounds__(128) k_extend_dp(ExtArgs a)
         int bestS = kExtInf, bestC = 0, bestR = 0, bestE = kExtInf, bestF = kExtInf;
         bool flag = false;
         int lastCol = limit;
+        int hnext = limit >= 1 ? tk.h[tk.hstep] : 0;   // column residues are loaded one column ahead
         for (int j = 0; j <= limit; ++j) {
-            const int hc = j > 0 ? tk.h[tk.hstep * j] : 0;
+            const int hc = j > 0 ? hnext : 0;
+            if (j >= 1 && j < limit) hnext = tk.h[tk.hstep * (j + 1)];
             int bandF = kExtInf;        // affine: F of the band's first row; linear: S of the row above it
             int bandDiag = kExtInf;     // previous column's S of the row above the band
             int colMax = INT_MIN, cbS = INT_MIN, cbR = 0, cbE = 0, cbF = 0;
