@@ -424,6 +424,23 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
                                   const gba_seed_batch *batch, const gba_seed *seeds,
                                   gba_extend_align_result *result);
 
+/* --- Packed input ---------------------------------------------------------------------------
+ * String<TValue, Packed<>> (sequence/string_packed.h) as the engine's input, uploaded as is: the
+ * host string of a packed string is a 64-bit length word followed by data words, each holding
+ * N = 64 / BitsPerValue values with the first one in the most significant used bits.  The words
+ * cross to the device (4x fewer bytes than codes for Dna, 2.7x for Dna5) and are unpacked there. */
+typedef struct {
+    int64_t num;               /* packed strings */
+    const uint64_t *words;     /* the strings' host words back to back (an empty string has none) */
+    const int64_t *word_off;   /* num + 1 offsets into words */
+    int32_t bits_per_value;    /* BitsPerValue<TValue>: 2 Dna, 3 Dna5, 5 AminoAcid */
+    int32_t reserved;
+} gba_packed_set;
+
+/* gba_align_batch on packed sets: pair k is (h[k], v[k]), or (h[0], v[k]) with h_shared. */
+GBA_API int gba_align_packed(gba_context *ctx, const gba_params *params, const gba_packed_set *h,
+                             const gba_packed_set *v, int32_t h_shared, gba_result *result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,7 +44,7 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc",
             "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
             "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule",
-            "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments"]
+            "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments", "gba_align_packed"]
 
 
 class GbaConfig(C.Structure):
@@ -135,6 +135,11 @@ class GbaExtendAlignResult(C.Structure):
                 ("segment_capacity", C.c_int64), ("segment_offsets", C.c_void_p)]
 
 
+class GbaPackedSet(C.Structure):
+    _fields_ = [("num", C.c_int64), ("words", C.c_void_p), ("word_off", C.c_void_p),
+                ("bits_per_value", C.c_int32), ("reserved", C.c_int32)]
+
+
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + \
         [os.path.join(INCLUDE, "seqan_gb300.h")]
@@ -206,6 +211,8 @@ def lib():
             L.gba_extend_seeds_device.argtypes = [vp, C.POINTER(GbaExtendParams), C.POINTER(GbaSeedBatch), vp, vp]
             L.gba_extend_alignments.argtypes = [vp, C.POINTER(GbaExtendAlignParams), C.POINTER(GbaSeedBatch), vp,
                                                 C.POINTER(GbaExtendAlignResult)]
+            L.gba_align_packed.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaPackedSet),
+                                           C.POINTER(GbaPackedSet), C.c_int32, C.POINTER(GbaResult)]
             L.gba_clock_seconds.argtypes = []
             L.gba_clock_seconds.restype = C.c_double
             _lib = L

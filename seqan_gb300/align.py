@@ -161,11 +161,12 @@ ALPHABET_SIZE = {"dna": 4, "dna5": 5, "aa": 27}
 
 def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None,
                 traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None,
-                alphabet_size: int | None = None, flags: int = 0) -> BatchOutput:
+                alphabet_size: int | None = None, flags: int = 0, packed_bits: int | None = None) -> BatchOutput:
     """Aligns lists of code arrays through gba_align_batch.
 
     alphabet_size bounds the codes (the reference's ValueSize of the alphabet); when None it is
-    taken from the codes themselves."""
+    taken from the codes themselves.  packed_bits (2 Dna, 3 Dna5, 5 AminoAcid) sends the sequences
+    as String<TValue, Packed<>> host words through gba_align_packed instead."""
     ctx = ctx or N.default_context()
     n = len(codes_v)
     sh, oh = _concat(codes_h)
@@ -195,6 +196,15 @@ def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=No
             res.cigar = np.zeros(cap, np.uint32)
             res.cigar_offsets = np.zeros(n + 1, np.int64)
             r.cigar, r.cigar_capacity, r.cigar_offsets = _vp(res.cigar), cap, _vp(res.cigar_offsets)
+    if packed_bits:
+        from . import packed as P
+        hw, hoff = P.pack_set(codes_h[:1] if h_shared else codes_h, packed_bits)
+        vw, voff = P.pack_set(codes_v, packed_bits)
+        ph = N.GbaPackedSet(len(hoff) - 1, _vp(hw), _vp(hoff), packed_bits, 0)
+        pv = N.GbaPackedSet(len(voff) - 1, _vp(vw), _vp(voff), packed_bits, 0)
+        ctx.check(N.lib().gba_align_packed(ctx.handle, C.byref(params), C.byref(ph), C.byref(pv),
+                                           1 if h_shared else 0, C.byref(r)), "gba_align_packed")
+        return res
     ctx.check(N.lib().gba_align_batch(ctx.handle, C.byref(params), C.byref(b), C.byref(r)), "gba_align_batch")
     return res
 

@@ -203,6 +203,9 @@ struct gba_context {
     std::map<std::pair<const void *, size_t>, int64_t> xs_grid;   // (kernel, smem) -> resident blocks
     // alignment extension: tasks, per-task results, trace, segments, scratch
     DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next, xa_packoff, xa_packed;
+    // packed input: the codes are already in seq_h / seq_v (gba_align_packed unpacked them)
+    bool device_codes = false;
+    DevBuf pk_words, pk_off;
 };
 
 namespace {
@@ -312,7 +315,7 @@ int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
     if (p->matrix && (p->alphabet_size <= 0 || p->alphabet_size > 32))
         return fail(ctx, GBA_EINVAL, "alphabet_size must be in 1..32");
     if (b->num_pairs < 0) return fail(ctx, GBA_EINVAL, "negative num_pairs");
-    if (b->num_pairs > 0 && (!b->off_h || !b->off_v || !b->seq_h || !b->seq_v))
+    if (b->num_pairs > 0 && (!b->off_h || !b->off_v || ((!b->seq_h || !b->seq_v) && !ctx->device_codes)))
         return fail(ctx, GBA_EINVAL, "null sequence or offset pointer");
     if (p->band_on) {
         if (p->band_lower > p->band_upper) return fail(ctx, GBA_EINVAL, "band_lower > band_upper");
@@ -1586,7 +1589,8 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
     const auto t0 = std::chrono::steady_clock::now();
     // Inputs: the concatenated codes as given.  Their copies are issued before planning so the
     // transfer overlaps the host work.
-    if (batch && batch->num_pairs > 0 && batch->off_h && batch->off_v && batch->seq_h && batch->seq_v) {
+    if (!ctx->device_codes && batch && batch->num_pairs > 0 && batch->off_h && batch->off_v && batch->seq_h &&
+        batch->seq_v) {
         const int64_t N0 = batch->num_pairs;
         const int64_t hb = batch->h_shared ? batch->off_h[1] : batch->off_h[N0];
         const int64_t vb = batch->off_v[N0];
@@ -1790,3 +1794,4 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 #include "server.cuh"
 #include "seeds_host.cuh"
 #include "extend_host.cuh"
+#include "packed_host.cuh"

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend]
+    python tests/golden/make_golden.py [--only seeds|extend|packed]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -10,6 +10,8 @@ Outputs (all small, committed):
   alphabets.json        the reference's char -> ordValue maps for Dna5, Dna and AminoAcid.
   seed_cases.json       seeds extended by the reference's extendSeed (MatchExtend, UnGappedXDrop,
                         GappedXDrop; seeds/seeds_extension.h) with the gapped extension scores.
+  packed_cases.json     host words of String<Dna|Dna5|AminoAcid, Packed<>> built by the reference
+                        (the bits that hold no value, undefined there, masked to zero).
   extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
                         (align_extend/align_extend.h) with and without X-drop: score and rows.
   aa_background.json    residue counts of the reference's T-Coffee test FASTA files, the
@@ -90,6 +92,9 @@ def main():
         return
     if only == "extend":
         write_extend(b62)
+        return
+    if only == "packed":
+        write_packed()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -227,6 +232,31 @@ def main():
     print(f"{len(cases)} alignment cases written")
     write_seeds(b62)
     write_extend(b62)
+    write_packed()
+
+
+def write_packed():
+    import ctypes as C
+    from seqan_gb300 import packed as P
+    lib = O.libref()
+    lib.ref_pack_string.argtypes = [C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+    lib.ref_pack_string.restype = C.c_int64
+    rng = np.random.Generator(np.random.PCG64(20261206))
+    cases = []
+    for alph, name, A in ((2, "dna", 4), (0, "dna5", 5), (1, "aa", 27)):
+        bits = P.BITS[name]
+        for n in [0, 1, 2, P.values_per_word(bits) - 1, P.values_per_word(bits), P.values_per_word(bits) + 1] + \
+                [int(x) for x in rng.integers(3, 400, 20)]:
+            codes = rng.integers(0, A, n).astype(np.uint8)
+            out = np.zeros(n // P.values_per_word(bits) + 4, dtype=np.uint64)
+            nw = lib.ref_pack_string(alph, codes.ctypes.data, n, out.ctypes.data, len(out))
+            words = out[:nw] & P.used_mask(n, bits)
+            cases.append({"alphabet": name, "bits": bits, "codes": codes.tolist(),
+                          "words": [format(int(w), "016x") for w in words]})
+    with open(os.path.join(HERE, "packed_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261206, "cases": cases}, f,
+                  separators=(",", ":"))
+    print(f"{len(cases)} packed-string cases written")
 
 
 def write_extend(b62):
