@@ -205,7 +205,7 @@ struct gba_context {
     DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next, xa_packoff, xa_packed;
     // packed input: the codes are already in seq_h / seq_v (gba_align_packed unpacked them)
     bool device_codes = false;
-    DevBuf pk_words, pk_off;
+    DevBuf pk_words, pk_off_h, pk_off_v;
 };
 
 namespace {

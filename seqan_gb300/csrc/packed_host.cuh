@@ -39,36 +39,50 @@ int packed_offsets(gba_context *ctx, const gba_packed_set *s, std::vector<int64_
     if (s->bits_per_value != 2 && s->bits_per_value != 3 && s->bits_per_value != 5)
         return fail(ctx, GBA_EINVAL, "bits_per_value must be 2, 3 or 5");
     const int N = 64 / s->bits_per_value;
+    if (s->num > 0 && s->word_off[s->num] > s->word_off[0] && !s->words)
+        return fail(ctx, GBA_EINVAL, "null packed words");
     off.assign(size_t(s->num) + 1, 0);
+    // lengths from the length words (in parallel: one host word read per string), then the offsets
+    int64_t bad = -1;
+    const int threads = plan_threads(s->num * 4);
+#pragma omp parallel for num_threads(threads) schedule(static) reduction(max : bad)
     for (int64_t k = 0; k < s->num; ++k) {
         const int64_t nw = s->word_off[k + 1] - s->word_off[k];
-        if (nw < 0) return fail(ctx, GBA_EINVAL, "packed word offsets decrease at %lld", (long long)k);
         int64_t len = 0;
-        if (nw > 0) {
-            if (!s->words) return fail(ctx, GBA_EINVAL, "null packed words");
-            len = int64_t(s->words[s->word_off[k]]);
-            if (len < 0 || nw != 1 + (len + N - 1) / N)
-                return fail(ctx, GBA_EINVAL, "packed string %lld: %lld words do not hold length %lld", (long long)k,
-                            (long long)nw, (long long)len);
-        }
-        off[k + 1] = off[k] + len;
+        if (nw > 0) len = int64_t(s->words[s->word_off[k]]);
+        if (nw < 0 || len < 0 || (nw > 0 && nw != 1 + (len + N - 1) / N)) bad = std::max(bad, k);
+        off[k + 1] = len;
     }
+    if (bad >= 0) return fail(ctx, GBA_EINVAL, "packed string %lld: its words do not hold its length", (long long)bad);
+    for (int64_t k = 0; k < s->num; ++k) off[k + 1] += off[k];
+    return GBA_OK;
+}
+
+// Queues the words' copy and their unpacking on the context stream; nothing waits, so the copies
+// overlap the host's planning as gba_align_batch's own upload does.  (Pageable offsets are staged
+// by cudaMemcpyAsync before it returns.)
+int packed_copy_words(gba_context *ctx, const gba_packed_set *s, size_t words_at)
+{
+    const int64_t nw = s->num ? s->word_off[s->num] - s->word_off[0] : 0;
+    if (nw > 0)
+        GBA_CUDA(ctx, cudaMemcpyAsync(ctx->pk_words.as<char>() + words_at, s->words + s->word_off[0], size_t(nw) * 8,
+                                      cudaMemcpyHostToDevice, ctx->stream));
     return GBA_OK;
 }
 
 int packed_upload(gba_context *ctx, const gba_packed_set *s, const std::vector<int64_t> &off, DevBuf &codes,
-                  size_t words_at)
+                  DevBuf &offbuf, size_t words_at)
 {
     cudaStream_t st = ctx->stream;
     const int64_t nw = s->num ? s->word_off[s->num] - s->word_off[0] : 0;
     GBA_CUDA(ctx, codes.ensure(size_t(off.back()) + 16));
     if (nw == 0) return GBA_OK;
     char *wbase = ctx->pk_words.as<char>() + words_at;
-    GBA_CUDA(ctx, cudaMemcpyAsync(wbase, s->words + s->word_off[0], size_t(nw) * 8, cudaMemcpyHostToDevice, st));
     // word offsets rebased to the copied words, then residue offsets, in the offsets buffer
     std::vector<int64_t> wo(size_t(s->num) + 1);
     for (int64_t k = 0; k <= s->num; ++k) wo[k] = s->word_off[k] - s->word_off[0];
-    int64_t *dwo = ctx->pk_off.as<int64_t>();
+    GBA_CUDA(ctx, offbuf.ensure(size_t(2 * (s->num + 1)) * 8));
+    int64_t *dwo = offbuf.as<int64_t>();
     int64_t *dro = dwo + (s->num + 1);
     GBA_CUDA(ctx, cudaMemcpyAsync(dwo, wo.data(), wo.size() * 8, cudaMemcpyHostToDevice, st));
     GBA_CUDA(ctx, cudaMemcpyAsync(dro, off.data(), off.size() * 8, cudaMemcpyHostToDevice, st));
@@ -76,8 +90,6 @@ int packed_upload(gba_context *ctx, const gba_packed_set *s, const std::vector<i
     k_unpack_packed<<<grid, 128, 0, st>>>(reinterpret_cast<const uint64_t *>(wbase), dwo, dro, s->num,
                                           s->bits_per_value, codes.as<uint8_t>());
     GBA_CUDA(ctx, cudaGetLastError());
-    // the offsets buffer is reused by the next upload: keep the stream ordered
-    GBA_CUDA(ctx, cudaStreamSynchronize(st));
     return GBA_OK;
 }
 
@@ -90,17 +102,23 @@ GBA_API int gba_align_packed(gba_context *ctx, const gba_params *params, const g
 {
     if (!ctx || !params || !h || !v || !result) return GBA_EINVAL;
     GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (h->num < 0 || v->num < 0 || (h->num && !h->word_off) || (v->num && !v->word_off))
+        return fail(ctx, GBA_EINVAL, "bad packed set");
+    const int64_t hw = h->num ? h->word_off[h->num] - h->word_off[0] : 0;
+    const int64_t vw = v->num ? v->word_off[v->num] - v->word_off[0] : 0;
+    if (hw < 0 || vw < 0) return fail(ctx, GBA_EINVAL, "packed word offsets decrease");
+    if ((hw && !h->words) || (vw && !v->words)) return fail(ctx, GBA_EINVAL, "null packed words");
+    // the words' copies first: they run while the host reads the lengths
+    GBA_CUDA(ctx, ctx->pk_words.ensure(size_t(hw + vw) * 8 + 16));
+    if (int rc = packed_copy_words(ctx, h, 0)) return rc;
+    if (int rc = packed_copy_words(ctx, v, size_t(hw) * 8)) return rc;
     std::vector<int64_t> off_h, off_v;
     if (int rc = packed_offsets(ctx, h, off_h)) return rc;
     if (int rc = packed_offsets(ctx, v, off_v)) return rc;
     const int64_t N = v->num;
     if (h_shared ? h->num != 1 : h->num != N) return fail(ctx, GBA_EINVAL, "packed sets of different sizes");
-    const int64_t hw = h->num ? h->word_off[h->num] - h->word_off[0] : 0;
-    const int64_t vw = v->num ? v->word_off[v->num] - v->word_off[0] : 0;
-    GBA_CUDA(ctx, ctx->pk_words.ensure(size_t(hw + vw) * 8 + 16));
-    GBA_CUDA(ctx, ctx->pk_off.ensure(size_t(2 * (std::max(h->num, v->num) + 1)) * 8));
-    if (int rc = packed_upload(ctx, h, off_h, ctx->seq_h, 0)) return rc;
-    if (int rc = packed_upload(ctx, v, off_v, ctx->seq_v, size_t(hw) * 8)) return rc;
+    if (int rc = packed_upload(ctx, h, off_h, ctx->seq_h, ctx->pk_off_h, 0)) return rc;
+    if (int rc = packed_upload(ctx, v, off_v, ctx->seq_v, ctx->pk_off_v, size_t(hw) * 8)) return rc;
     gba_batch b{};
     b.num_pairs = N;
     b.seq_h = nullptr;
