@@ -441,6 +441,38 @@ typedef struct {
 GBA_API int gba_align_packed(gba_context *ctx, const gba_params *params, const gba_packed_set *h,
                              const gba_packed_set *v, int32_t h_shared, gba_result *result);
 
+/* --- SAM output -----------------------------------------------------------------------------
+ * The SAM lines of alignment records as the reference's SAM writer writes a BamAlignmentRecord
+ * (bam_io/write_sam.h:126-217: QNAME, FLAG, RNAME or '*', POS + 1, MAPQ, CIGAR or '*', RNEXT as
+ * '*', '=' or a name, PNEXT + 1, TLEN or '0', SEQ or '*', QUAL or '*'; no tags), formatted on the
+ * device.  Positions are 0-based with -1 for none, as in BamAlignmentRecord; the CIGAR is the
+ * BAM-packed form of gba_result.cigar; SEQ is residue codes turned into seq_letters[code]. */
+typedef struct {
+    int64_t num;                               /* records */
+    const char *qname;                         /* names back to back */
+    const int64_t *qname_off;                  /* num + 1 */
+    const uint16_t *flag;
+    const int32_t *ref_id, *pos;               /* rID, beginPos */
+    const uint8_t *mapq;
+    const uint32_t *cigar;                     /* length << 4 | op index into "MIDNSHP=X" */
+    const int64_t *cigar_off;                  /* num + 1 */
+    const int32_t *next_ref_id, *next_pos, *tlen;
+    const uint8_t *seq;                        /* residue codes */
+    const int64_t *seq_off;                    /* num + 1 */
+    const char *seq_letters;                   /* 32 letters, e.g. "ACGTN" padded */
+    const char *qual;                          /* qualities back to back, or NULL: every QUAL '*' */
+    const int64_t *qual_off;                   /* num + 1, or NULL */
+    const char *contig_names;                  /* the context's contig names back to back */
+    const int64_t *contig_off;                 /* num_contigs + 1 */
+    int64_t num_contigs;
+} gba_sam_records;
+
+/* Writes the lines to out and their offsets to line_off[0..num] (line k is out[line_off[k] ..
+ * line_off[k+1]), newline included); GBA_ECAPACITY (with line_off filled) if capacity is too
+ * small. */
+GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *records, char *out, int64_t capacity,
+                           int64_t *line_off);
+
 #ifdef __cplusplus
 }
 #endif

@@ -476,6 +476,62 @@ def ref_extend_alignment(pb: Problem, h, v, positions, direction) -> ExtendResul
                         int(ends[2]), int(ends[3]))
 
 
+# ---------------------------------------------------------------------------------------------
+# SAM lines (bam_io/write_sam.h:126-217) of BamAlignmentRecord fields given as plain lists.
+# ---------------------------------------------------------------------------------------------
+
+def write_sam(rec) -> str:
+    """Restates the reference's SAM record writer for rec (a seqan_gb300.sam.SamRecords)."""
+    lines = []
+    for k in range(len(rec.qname)):
+        rid, rn = int(rec.ref_id[k]), int(rec.next_ref_id[k])
+        cig = "".join(f"{int(c) >> 4}{'MIDNSHP=X'[int(c) & 15]}" for c in rec.cigar[k]) or "*"
+        seq = "".join(rec.letters[int(x)] for x in rec.seq[k]) or "*"
+        qual = (rec.qual[k] if rec.qual is not None else "") or "*"
+        tlen = int(rec.tlen[k])
+        lines.append("\t".join([rec.qname[k], str(int(rec.flag[k])), "*" if rid == -1 else rec.contigs[rid],
+                                 str(int(rec.pos[k]) + 1), str(int(rec.mapq[k])), cig,
+                                 "*" if rn == -1 else ("=" if rn == rid else rec.contigs[rn]),
+                                 str(int(rec.next_pos[k]) + 1), "0" if tlen == 0 else str(tlen), seq, qual]) + "\n")
+    return "".join(lines)
+
+
+def ref_write_sam(rec) -> str:
+    """The reference's SAM writer on the same records (oracle/ref/units/sam.cpp)."""
+    lib = libref()
+    lib.ref_write_sam.restype = C.c_int64
+    n = len(rec.qname)
+    enc = lambda parts: [p.encode() for p in parts]
+    qn = enc(rec.qname)
+    qoff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in qn], out=qoff[1:])
+    qname = b"".join(qn) or b"\0"
+    cig = np.concatenate([np.asarray(c, np.uint32) for c in rec.cigar] + [np.zeros(1, np.uint32)])
+    coff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(c) for c in rec.cigar], out=coff[1:])
+    seqs = enc(["".join(rec.letters[int(x)] for x in s) for s in rec.seq])
+    soff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in seqs], out=soff[1:])
+    quals = enc(rec.qual if rec.qual is not None else [""] * n)
+    quoff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in quals], out=quoff[1:])
+    cn = enc(rec.contigs)
+    cnoff = np.zeros(len(cn) + 1, np.int64)
+    np.cumsum([len(x) for x in cn], out=cnoff[1:])
+    arr = lambda a, t: np.ascontiguousarray(a, t)
+    flag, rid, pos = arr(rec.flag, np.uint16), arr(rec.ref_id, np.int32), arr(rec.pos, np.int32)
+    mapq, rn, pn, tl = arr(rec.mapq, np.uint8), arr(rec.next_ref_id, np.int32), arr(rec.next_pos, np.int32), \
+        arr(rec.tlen, np.int32)
+    cap = int(qoff[-1] + soff[-1] + quoff[-1] + 64 * n + 16 * int(coff[-1]) + 1024)
+    out = C.create_string_buffer(cap)
+    args = [C.c_int64(n), C.c_char_p(qname), _ptr(qoff), _ptr(flag), _ptr(rid), _ptr(pos), _ptr(mapq), _ptr(cig),
+            _ptr(coff), _ptr(rn), _ptr(pn), _ptr(tl), C.c_char_p(b"".join(seqs) or b"\0"), _ptr(soff),
+            C.c_char_p(b"".join(quals) or b"\0"), _ptr(quoff), C.c_int64(len(cn)), C.c_char_p(b"".join(cn) or b"\0"),
+            _ptr(cnoff), out, C.c_int64(cap)]
+    length = lib.ref_write_sam(*args)
+    return out.raw[:length].decode()
+
+
 def render_rows(segments, h_text: str, v_text: str):
     """Gapped rows of the clipped alignment view, as operator<< on Gaps prints them."""
     if not segments:

@@ -44,7 +44,8 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_timer_stop", "gba_get_stats", "gba_measure_int_peak", "gba_align_score_noalloc",
             "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
             "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule",
-            "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments", "gba_align_packed"]
+            "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments", "gba_align_packed",
+            "gba_format_sam"]
 
 
 class GbaConfig(C.Structure):
@@ -140,6 +141,15 @@ class GbaPackedSet(C.Structure):
                 ("bits_per_value", C.c_int32), ("reserved", C.c_int32)]
 
 
+class GbaSamRecords(C.Structure):
+    _fields_ = [("num", C.c_int64), ("qname", C.c_void_p), ("qname_off", C.c_void_p), ("flag", C.c_void_p),
+                ("ref_id", C.c_void_p), ("pos", C.c_void_p), ("mapq", C.c_void_p), ("cigar", C.c_void_p),
+                ("cigar_off", C.c_void_p), ("next_ref_id", C.c_void_p), ("next_pos", C.c_void_p),
+                ("tlen", C.c_void_p), ("seq", C.c_void_p), ("seq_off", C.c_void_p), ("seq_letters", C.c_void_p),
+                ("qual", C.c_void_p), ("qual_off", C.c_void_p), ("contig_names", C.c_void_p),
+                ("contig_off", C.c_void_p), ("num_contigs", C.c_int64)]
+
+
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + \
         [os.path.join(INCLUDE, "seqan_gb300.h")]
@@ -213,6 +223,7 @@ def lib():
                                                 C.POINTER(GbaExtendAlignResult)]
             L.gba_align_packed.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaPackedSet),
                                            C.POINTER(GbaPackedSet), C.c_int32, C.POINTER(GbaResult)]
+            L.gba_format_sam.argtypes = [vp, C.POINTER(GbaSamRecords), vp, i64, vp]
             L.gba_clock_seconds.argtypes = []
             L.gba_clock_seconds.restype = C.c_double
             _lib = L

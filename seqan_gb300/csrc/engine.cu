@@ -206,6 +206,7 @@ struct gba_context {
     // packed input: the codes are already in seq_h / seq_v (gba_align_packed unpacked them)
     bool device_codes = false;
     DevBuf pk_words, pk_off_h, pk_off_v;
+    DevBuf sam_in, sam_len, sam_tmp, sam_out;   // gba_format_sam
 };
 
 namespace {
@@ -1795,3 +1796,4 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 #include "seeds_host.cuh"
 #include "extend_host.cuh"
 #include "packed_host.cuh"
+#include "sam_host.cuh"

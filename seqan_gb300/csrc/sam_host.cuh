@@ -1,0 +1,272 @@
+// sam_host.cuh -- gba_format_sam: SAM lines of alignment records, formatted on the device as the
+// reference's SAM writer formats a BamAlignmentRecord (bam_io/write_sam.h:126-217); included at
+// the end of engine.cu.
+//
+// A length pass (one thread per record) sizes every line, a device scan places them, and a
+// write pass (one warp per record) writes each line: the numeric fields and CIGAR operations by one
+// lane, the name, sequence and qualities by all lanes.
+#pragma once
+
+namespace gba {
+
+struct SamArgs {
+    int64_t num;
+    const char *qname;
+    const int64_t *qname_off;
+    const uint16_t *flag;
+    const int32_t *ref_id, *pos, *next_ref_id, *next_pos, *tlen;
+    const uint8_t *mapq;
+    const uint32_t *cigar;
+    const int64_t *cigar_off;
+    const uint8_t *seq;
+    const int64_t *seq_off;
+    const char *letters;        // 32 letters for the residue codes
+    const char *qual;
+    const int64_t *qual_off;    // null: every qual is '*'
+    const char *cnames;
+    const int64_t *cname_off;
+    int64_t num_contigs;
+};
+
+__device__ __forceinline__ int dec_digits_u(uint64_t v)
+{
+    int d = 1;
+    while (v >= 10) {
+        v /= 10;
+        ++d;
+    }
+    return d;
+}
+
+__device__ __forceinline__ int dec_len(int64_t v) { return v < 0 ? 1 + dec_digits_u(uint64_t(-v)) : dec_digits_u(uint64_t(v)); }
+
+__device__ __forceinline__ char *dec_write(char *p, int64_t v)
+{
+    if (v < 0) {
+        *p++ = '-';
+        v = -v;
+    }
+    const int d = dec_digits_u(uint64_t(v));
+    for (int i = d - 1; i >= 0; --i) {
+        p[i] = char('0' + v % 10);
+        v /= 10;
+    }
+    return p + d;
+}
+
+__device__ __forceinline__ int64_t contig_len(const SamArgs &a, int32_t id)
+{
+    return (id < 0 || id >= a.num_contigs) ? 1 : a.cname_off[id + 1] - a.cname_off[id];
+}
+
+// Byte length of record k's line, in the writer's field order.
+__device__ int64_t sam_line_len(const SamArgs &a, int64_t k)
+{
+    int64_t n = a.qname_off[k + 1] - a.qname_off[k] + 1;
+    n += dec_len(a.flag[k]) + 1;
+    n += contig_len(a, a.ref_id[k]) + 1;
+    n += dec_len(int64_t(a.pos[k]) + 1) + 1;
+    n += dec_len(a.mapq[k]) + 1;
+    const int64_t c0 = a.cigar_off[k], c1 = a.cigar_off[k + 1];
+    if (c0 == c1) n += 1;
+    for (int64_t i = c0; i < c1; ++i) n += dec_len(a.cigar[i] >> 4) + 1;
+    n += 1;
+    const int32_t rn = a.next_ref_id[k];
+    n += (rn < 0 || rn == a.ref_id[k]) ? 1 : contig_len(a, rn);
+    n += 1;
+    n += dec_len(int64_t(a.next_pos[k]) + 1) + 1;
+    n += (a.tlen[k] == 0 ? 1 : dec_len(a.tlen[k])) + 1;
+    const int64_t sl = a.seq_off[k + 1] - a.seq_off[k];
+    n += (sl == 0 ? 1 : sl) + 1;
+    const int64_t ql = a.qual_off ? a.qual_off[k + 1] - a.qual_off[k] : 0;
+    n += (ql == 0 ? 1 : ql) + 1;
+    return n;
+}
+
+__global__ void __launch_bounds__(128) k_sam_lengths(SamArgs a, int64_t *len)
+{
+    const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < a.num) len[k] = sam_line_len(a, k);
+}
+
+__global__ void __launch_bounds__(128) k_sam_write(SamArgs a, const int64_t *line_off, char *out)
+{
+    const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= a.num) return;
+    char *p = out + line_off[k];
+    const unsigned FULL = 0xffffffffu;
+    // QNAME (all lanes)
+    const int64_t q0 = a.qname_off[k], ql = a.qname_off[k + 1] - q0;
+    for (int64_t i = lane; i < ql; i += 32) p[i] = a.qname[q0 + i];
+    p += ql;
+    // FLAG .. TLEN (lane 0), then the others learn where SEQ starts
+    int64_t seq_at = 0;
+    if (lane == 0) {
+        char *w = p;
+        *w++ = '\t';
+        w = dec_write(w, a.flag[k]);
+        *w++ = '\t';
+        const int32_t rid = a.ref_id[k];
+        if (rid < 0 || rid >= a.num_contigs) {
+            *w++ = '*';
+        } else {
+            for (int64_t i = a.cname_off[rid]; i < a.cname_off[rid + 1]; ++i) *w++ = a.cnames[i];
+        }
+        *w++ = '\t';
+        w = dec_write(w, int64_t(a.pos[k]) + 1);
+        *w++ = '\t';
+        w = dec_write(w, a.mapq[k]);
+        *w++ = '\t';
+        const int64_t c0 = a.cigar_off[k], c1 = a.cigar_off[k + 1];
+        if (c0 == c1) *w++ = '*';
+        for (int64_t i = c0; i < c1; ++i) {
+            w = dec_write(w, a.cigar[i] >> 4);
+            *w++ = "MIDNSHP=X"[a.cigar[i] & 15u];
+        }
+        *w++ = '\t';
+        const int32_t rn = a.next_ref_id[k];
+        if (rn < 0 || rn >= a.num_contigs) {
+            *w++ = '*';
+        } else if (rn == rid) {
+            *w++ = '=';
+        } else {
+            for (int64_t i = a.cname_off[rn]; i < a.cname_off[rn + 1]; ++i) *w++ = a.cnames[i];
+        }
+        *w++ = '\t';
+        w = dec_write(w, int64_t(a.next_pos[k]) + 1);
+        *w++ = '\t';
+        if (a.tlen[k] == 0) *w++ = '0';
+        else w = dec_write(w, a.tlen[k]);
+        *w++ = '\t';
+        seq_at = w - p;
+    }
+    seq_at = __shfl_sync(FULL, seq_at, 0);
+    p += seq_at;
+    // SEQ, QUAL (all lanes)
+    const int64_t s0 = a.seq_off[k], sl = a.seq_off[k + 1] - s0;
+    if (sl == 0) {
+        if (lane == 0) p[0] = '*';
+        p += 1;
+    } else {
+        for (int64_t i = lane; i < sl; i += 32) p[i] = a.letters[a.seq[s0 + i] & 31];
+        p += sl;
+    }
+    if (lane == 0) p[0] = '\t';
+    p += 1;
+    const int64_t u0 = a.qual_off ? a.qual_off[k] : 0, ul = a.qual_off ? a.qual_off[k + 1] - u0 : 0;
+    if (ul == 0) {
+        if (lane == 0) p[0] = '*';
+        p += 1;
+    } else {
+        for (int64_t i = lane; i < ul; i += 32) p[i] = a.qual[u0 + i];
+        p += ul;
+    }
+    if (lane == 0) p[0] = '\n';
+}
+
+}  // namespace gba
+
+extern "C" {
+
+GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out, int64_t capacity, int64_t *line_off)
+{
+    if (!ctx || !r || !line_off) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t n = r->num;
+    if (n < 0) return fail(ctx, GBA_EINVAL, "negative record count");
+    line_off[0] = 0;
+    if (n == 0) return GBA_OK;
+    if (!r->qname_off || !r->flag || !r->ref_id || !r->pos || !r->mapq || !r->cigar_off || !r->next_ref_id ||
+        !r->next_pos || !r->tlen || !r->seq_off || !r->seq_letters || (r->num_contigs > 0 && !r->contig_off))
+        return fail(ctx, GBA_EINVAL, "null record field");
+    // ids the writer can name (the reference indexes contigNames with them) and CIGAR operations
+    for (int64_t k = 0; k < n; ++k) {
+        if (r->ref_id[k] < -1 || r->ref_id[k] >= r->num_contigs || r->next_ref_id[k] < -1 ||
+            r->next_ref_id[k] >= r->num_contigs)
+            return fail(ctx, GBA_EINVAL, "record %lld: reference id outside the contigs", (long long)k);
+    }
+    if (r->cigar_off[n] > 0 && !r->cigar) return fail(ctx, GBA_EINVAL, "null cigar");
+    for (int64_t i = 0; i < r->cigar_off[n]; ++i)
+        if ((r->cigar[i] & 15u) > 8u) return fail(ctx, GBA_EINVAL, "CIGAR operation index above 8");
+    cudaStream_t st = ctx->stream;
+    // uploads: one buffer per field (the host arrays are the caller's)
+    struct Up {
+        const void *src;
+        size_t bytes;
+    };
+    const int64_t qn = r->qname_off[n], cn = r->cigar_off[n], sn = r->seq_off[n];
+    const int64_t un = r->qual_off ? r->qual_off[n] : 0;
+    const int64_t nc = r->num_contigs, cnb = nc ? r->contig_off[nc] : 0;
+    const Up ups[] = {{r->qname, size_t(qn)},           {r->qname_off, size_t(n + 1) * 8},
+                      {r->flag, size_t(n) * 2},         {r->ref_id, size_t(n) * 4},
+                      {r->pos, size_t(n) * 4},          {r->next_ref_id, size_t(n) * 4},
+                      {r->next_pos, size_t(n) * 4},     {r->tlen, size_t(n) * 4},
+                      {r->mapq, size_t(n)},             {r->cigar, size_t(cn) * 4},
+                      {r->cigar_off, size_t(n + 1) * 8}, {r->seq, size_t(sn)},
+                      {r->seq_off, size_t(n + 1) * 8},  {r->seq_letters, 32},
+                      {r->qual, size_t(un)},            {r->qual_off, r->qual_off ? size_t(n + 1) * 8 : 0},
+                      {r->contig_names, size_t(cnb)},   {r->contig_off, nc ? size_t(nc + 1) * 8 : 0}};
+    size_t total = 0;
+    size_t at[sizeof(ups) / sizeof(ups[0])];
+    for (size_t i = 0; i < sizeof(ups) / sizeof(ups[0]); ++i) {
+        at[i] = total;
+        total += (ups[i].bytes + 15) & ~size_t(15);
+    }
+    GBA_CUDA(ctx, ctx->sam_in.ensure(total + 16));
+    char *base = ctx->sam_in.as<char>();
+    for (size_t i = 0; i < sizeof(ups) / sizeof(ups[0]); ++i)
+        if (ups[i].bytes && ups[i].src)
+            GBA_CUDA(ctx, cudaMemcpyAsync(base + at[i], ups[i].src, ups[i].bytes, cudaMemcpyHostToDevice, st));
+    SamArgs a{};
+    a.num = n;
+    a.qname = base + at[0];
+    a.qname_off = reinterpret_cast<const int64_t *>(base + at[1]);
+    a.flag = reinterpret_cast<const uint16_t *>(base + at[2]);
+    a.ref_id = reinterpret_cast<const int32_t *>(base + at[3]);
+    a.pos = reinterpret_cast<const int32_t *>(base + at[4]);
+    a.next_ref_id = reinterpret_cast<const int32_t *>(base + at[5]);
+    a.next_pos = reinterpret_cast<const int32_t *>(base + at[6]);
+    a.tlen = reinterpret_cast<const int32_t *>(base + at[7]);
+    a.mapq = reinterpret_cast<const uint8_t *>(base + at[8]);
+    a.cigar = reinterpret_cast<const uint32_t *>(base + at[9]);
+    a.cigar_off = reinterpret_cast<const int64_t *>(base + at[10]);
+    a.seq = reinterpret_cast<const uint8_t *>(base + at[11]);
+    a.seq_off = reinterpret_cast<const int64_t *>(base + at[12]);
+    a.letters = base + at[13];
+    a.qual = base + at[14];
+    a.qual_off = r->qual_off ? reinterpret_cast<const int64_t *>(base + at[15]) : nullptr;
+    a.cnames = base + at[16];
+    a.cname_off = reinterpret_cast<const int64_t *>(base + at[17]);
+    a.num_contigs = nc;
+    // lengths, offsets (exclusive scan), text
+    GBA_CUDA(ctx, ctx->sam_len.ensure(size_t(n + 1) * 8 * 2));
+    int64_t *len = ctx->sam_len.as<int64_t>();
+    int64_t *off = len + (n + 1);
+    GBA_CUDA(ctx, cudaMemsetAsync(len + n, 0, 8, st));
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+    k_sam_lengths<<<unsigned((n + 127) / 128), 128, 0, st>>>(a, len);
+    GBA_CUDA(ctx, cudaGetLastError());
+    size_t tmp_bytes = 0;
+    GBA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, len, off, n + 1, st));
+    GBA_CUDA(ctx, ctx->sam_tmp.ensure(tmp_bytes + 16));
+    GBA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(ctx->sam_tmp.ptr, tmp_bytes, len, off, n + 1, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(line_off, off, size_t(n + 1) * 8, cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaStreamSynchronize(st));
+    const int64_t bytes = line_off[n];
+    if (bytes > capacity || !out) return fail(ctx, GBA_ECAPACITY, "SAM text needs %lld bytes", (long long)bytes);
+    GBA_CUDA(ctx, ctx->sam_out.ensure(size_t(bytes) + 16));
+    k_sam_write<<<unsigned((n * 32 + 127) / 128), 128, 0, st>>>(a, off, ctx->sam_out.as<char>());
+    GBA_CUDA(ctx, cudaGetLastError());
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(out, ctx->sam_out.ptr, size_t(bytes), cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaStreamSynchronize(st));
+    float ms = 0;
+    GBA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+    ctx->stats = gba_stats{};
+    ctx->stats.dp_kernel_ms = ms;
+    ctx->stats.kernel_launches = 4;
+    return GBA_OK;
+}
+
+}  // extern "C"

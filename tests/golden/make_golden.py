@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|packed]
+    python tests/golden/make_golden.py [--only seeds|extend|packed|sam]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -10,6 +10,7 @@ Outputs (all small, committed):
   alphabets.json        the reference's char -> ordValue maps for Dna5, Dna and AminoAcid.
   seed_cases.json       seeds extended by the reference's extendSeed (MatchExtend, UnGappedXDrop,
                         GappedXDrop; seeds/seeds_extension.h) with the gapped extension scores.
+  sam_cases.json        BamAlignmentRecord fields and the SAM text the reference's writer makes of them.
   packed_cases.json     host words of String<Dna|Dna5|AminoAcid, Packed<>> built by the reference
                         (the bits that hold no value, undefined there, masked to zero).
   extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
@@ -95,6 +96,9 @@ def main():
         return
     if only == "packed":
         write_packed()
+        return
+    if only == "sam":
+        write_sam_cases()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -233,6 +237,43 @@ def main():
     write_seeds(b62)
     write_extend(b62)
     write_packed()
+    write_sam_cases()
+
+
+def sam_records(rng, n):
+    from seqan_gb300 import sam as S
+    contigs = ["chr1", "chr2", "scaffold_17", "X"]
+    names, cig, seq, qual = [], [], [], []
+    for k in range(n):
+        names.append(f"read{k}" + ("" if k % 7 else "/1"))
+        ops = []
+        for _ in range(int(rng.integers(0, 6)) if k % 11 else 0):
+            ops.append((int(rng.integers(1, 300)) << 4) | int(rng.integers(0, 9)))
+        cig.append(ops)
+        L = 0 if k % 13 == 0 else int(rng.integers(1, 160))
+        seq.append(rng.integers(0, 5, L).astype(np.uint8))
+        qual.append("" if k % 5 == 0 else "".join(chr(33 + int(x)) for x in rng.integers(0, 42, L)))
+    rid = rng.integers(-1, len(contigs), n).astype(np.int32)
+    rn = np.where(rng.random(n) < 0.3, rid, rng.integers(-1, len(contigs), n)).astype(np.int32)
+    return S.SamRecords(names, rng.choice([0, 4, 16, 99, 147, 256, 2048, 65535], n).astype(np.uint16), rid,
+                        rng.integers(-1, 250_000_000, n).astype(np.int32), rng.choice([0, 1, 60, 255], n).astype(np.uint8),
+                        cig, rn, rng.integers(-1, 250_000_000, n).astype(np.int32),
+                        np.where(rng.random(n) < 0.3, 0, rng.integers(-800, 800, n)).astype(np.int32), seq, qual,
+                        contigs)
+
+
+def write_sam_cases():
+    rng = np.random.Generator(np.random.PCG64(20261207))
+    rec = sam_records(rng, 400)
+    text = O.ref_write_sam(rec)
+    with open(os.path.join(HERE, "sam_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261207, "contigs": rec.contigs,
+                   "qname": rec.qname, "flag": rec.flag.tolist(), "ref_id": rec.ref_id.tolist(),
+                   "pos": rec.pos.tolist(), "mapq": rec.mapq.tolist(), "cigar": [list(c) for c in rec.cigar],
+                   "next_ref_id": rec.next_ref_id.tolist(), "next_pos": rec.next_pos.tolist(),
+                   "tlen": rec.tlen.tolist(), "seq": [s.tolist() for s in rec.seq], "qual": rec.qual,
+                   "text": text}, f, separators=(",", ":"))
+    print(f"{len(rec.qname)} SAM records written")
 
 
 def write_packed():
