@@ -55,6 +55,142 @@ WORKLOADS["extend_reads_250k"] = ("250000 read alignments: 150 bp reads (3% subs
                                   "extendAlignment EXTEND_BOTH, xDrop 20, Score<int,Simple>(2,-4,-1,-6); scores + "
                                   "trace segments of both sides")
 EXTEND_WORKLOADS = {"extend_reads_250k"}
+WORKLOADS["sam_records_1m"] = ("1000000 SAM records of read alignments: names read<k>, flag 0/16, one contig, "
+                               "positions < 10^7, MAPQ 60, 1-3 CIGAR operations, 150 bp SEQ and QUAL; "
+                               "BamAlignmentRecord -> SAM text as the reference's writer")
+SAM_WORKLOADS = {"sam_records_1m"}
+
+
+def make_sam_records(n, seed=21):
+    from seqan_gb300 import sam as S
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = 150
+    seqs = list(rng.integers(0, 4, size=(n, L), dtype=np.uint8))
+    qual_chars = rng.integers(33, 75, size=(n, L), dtype=np.uint8)
+    quals = [bytes(q).decode() for q in qual_chars]
+    cig = []
+    for k in range(n):
+        if k % 3 == 0:
+            cig.append(np.array([(L << 4) | 0], np.uint32))
+        else:
+            a = int(rng.integers(20, 120))
+            cig.append(np.array([(a << 4) | 0, (1 << 4) | (1 + k % 2), ((L - a - (1 if k % 2 else 0)) << 4) | 0],
+                                np.uint32))
+    return S.SamRecords([f"read{k}" for k in range(n)], rng.choice([0, 16], n).astype(np.uint16),
+                        np.zeros(n, np.int32), rng.integers(0, 10_000_000, n).astype(np.int32),
+                        np.full(n, 60, np.uint8), cig, np.full(n, -1, np.int32), np.full(n, -1, np.int32),
+                        np.zeros(n, np.int32), seqs, quals, ["chrSim"])
+
+
+def run_sam_bench(args, rank, world, local_rank, dist):
+    from seqan_gb300 import _native as N
+    from oracle import oracle as O
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    h = ctx.handle
+    n = args.pairs or 1_000_000
+    rec = make_sam_records(n, seed=21 + rank)
+    a = O.sam_arrays(rec)
+    pinned_bufs = {}
+    for key, arr in a.items():
+        p = C.c_void_p()
+        ctx.check(L.gba_host_alloc(h, C.byref(p), max(arr.nbytes, 1)), "alloc")
+        C.memmove(p, arr.ctypes.data, arr.nbytes)
+        pinned_bufs[key] = p
+    P = pinned_bufs
+    r = N.GbaSamRecords(n, P["qname"], P["qoff"], P["flag"], P["rid"], P["pos"], P["mapq"], P["cigar"], P["coff"],
+                        P["rnext"], P["pnext"], P["tlen"], P["seq"], P["soff"], P["letters"], P["qual"], P["quoff"],
+                        P["cnames"], P["cnoff"], len(rec.contigs))
+    line_off = np.zeros(n + 1, np.int64)
+    rc = L.gba_format_sam(h, C.byref(r), None, 0, line_off.ctypes.data)
+    total = int(line_off[-1])
+    p_out = C.c_void_p()
+    ctx.check(L.gba_host_alloc(h, C.byref(p_out), total + 16), "alloc")
+
+    def call():
+        ctx.check(L.gba_format_sam(h, C.byref(r), p_out, total + 16, line_off.ctypes.data), "sam")
+
+    for _ in range(args.warmup):
+        call()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        wall.append(time.perf_counter() - t0)
+        kern.append(ctx.stats().dp_kernel_ms)
+    clocks = sampler.stop()
+    text = C.string_at(p_out, total).decode()
+    k = min(n, 20_000)
+    parity = text[:int(line_off[k])] == O.write_sam(type(rec)(rec.qname[:k], rec.flag[:k], rec.ref_id[:k], rec.pos[:k],
+                                                               rec.mapq[:k], rec.cigar[:k], rec.next_ref_id[:k],
+                                                               rec.next_pos[:k], rec.tlen[:k], rec.seq[:k],
+                                                               rec.qual[:k], rec.contigs))
+    kernel_ms = sum(kern) / len(kern)
+    value = n * world / (kernel_ms * 1e-3) / 1e6
+    e2e = n * world * len(wall) / sum(wall) / 1e6
+    hbm = measured_hbm_gbs()
+    in_bytes = sum(int(x.nbytes) for x in a.values())
+    line = {"metric": "M SAM records/s, device formatting", "value": value, "unit": "M records/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "records": n,
+                       "text_bytes": total, "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "M records/s", "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": total + 8 * (n + 1),
+                    "ms_per_step": 1e3 * sum(wall) / len(wall)},
+            "gpu_launches": args.steps * 4,
+            "roofline": {"bound": "hbm", "achieved": (in_bytes + total) / (kernel_ms * 1e-3) / 1e9,
+                         "peak": hbm, "unit": "GB/s",
+                         "frac": ((in_bytes + total) / (kernel_ms * 1e-3) / 1e9 / hbm) if hbm else None,
+                         "traffic": None, "kernel": "k_sam_lengths + CUB scan + k_sam_write",
+                         "algorithmic_bytes": "record fields read once + SAM text written once",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "clocks": clocks, "parity_first_20000_vs_oracle": parity}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            O.oracle_write_sam_c(rec, threads=threads, arrays=a)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        line["cpu_baseline"] = {"value": n / best / 1e6, "unit": "M records/s", "cores": threads, "kind": "port",
+                                "sample": f"all {n} records, orc_write_sam (oracle/seqan_oracle.c, the reference's "
+                                          f"SAM writer restated) with OpenMP over {threads} threads, best of 2",
+                                "seconds": best}
+    for p in list(pinned_bufs.values()) + [p_out]:
+        L.gba_host_free(h, p)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_sam_reference(args):
+    from oracle import oracle as O
+    n = min(args.pairs or 1_000_000, 1_000_000)
+    rec = make_sam_records(n)
+    a = O.sam_arrays(rec)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.oracle_write_sam_c(rec, threads=threads, arrays=a)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.oracle_write_sam_c(rec, threads=threads, arrays=a)
+        times.append(time.perf_counter() - t0)
+    rate = n * len(times) / sum(times) / 1e6
+    print(json.dumps({"metric": "M SAM records/s, device formatting", "value": rate, "unit": "M records/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload, "records_per_step": n,
+                                 "description": WORKLOADS[args.workload]},
+                      "cpu_baseline": {"value": rate, "unit": "M records/s", "cores": threads, "kind": "port",
+                                       "sample": f"{n} records per step, the reference's SAM writer restated in C "
+                                                 "(orc_write_sam), OpenMP"},
+                      "e2e": {"value": rate, "unit": "M records/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
 # Integer ops of one x-drop cell: max(up, left) + gap, diagonal + score, the max of the two, the
 # drop-off compare and the anti-diagonal best (add and max each count one).
 XDROP_OPS_PER_CELL = 6
@@ -689,7 +825,10 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
-        if args.workload in EXTEND_WORKLOADS:
+        if args.workload in SAM_WORKLOADS:
+            if rank == 0:
+                run_sam_reference(args)
+        elif args.workload in EXTEND_WORKLOADS:
             if rank == 0:
                 run_extend_reference(args)
         elif args.workload in SEED_WORKLOADS:
@@ -707,6 +846,11 @@ def main():
         return
     if args.workload in EXTEND_WORKLOADS:
         run_extend_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in SAM_WORKLOADS:
+        run_sam_bench(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
         return

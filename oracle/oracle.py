@@ -496,6 +496,51 @@ def write_sam(rec) -> str:
     return "".join(lines)
 
 
+def sam_arrays(rec):
+    """The records as the flat arrays of the C writers (engine and oracle)."""
+    n = len(rec.qname)
+    enc = [q.encode() for q in rec.qname]
+    qoff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in enc], out=qoff[1:])
+    cig = np.concatenate([np.asarray(c, np.uint32) for c in rec.cigar] + [np.zeros(1, np.uint32)])
+    coff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(c) for c in rec.cigar], out=coff[1:])
+    seq = np.concatenate([np.asarray(s, np.uint8) for s in rec.seq] + [np.zeros(1, np.uint8)])
+    soff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(s) for s in rec.seq], out=soff[1:])
+    qb = [q.encode() for q in (rec.qual if rec.qual is not None else [""] * n)]
+    quoff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in qb], out=quoff[1:])
+    cb = [c.encode() for c in rec.contigs]
+    cnoff = np.zeros(len(cb) + 1, np.int64)
+    np.cumsum([len(x) for x in cb], out=cnoff[1:])
+    letters = np.zeros(32, np.uint8)
+    letters[:len(rec.letters)] = np.frombuffer(rec.letters.encode(), np.uint8)
+    return dict(qname=np.frombuffer(b"".join(enc) + b"\0", np.uint8), qoff=qoff,
+                flag=np.ascontiguousarray(rec.flag, np.uint16), rid=np.ascontiguousarray(rec.ref_id, np.int32),
+                pos=np.ascontiguousarray(rec.pos, np.int32), mapq=np.ascontiguousarray(rec.mapq, np.uint8),
+                cigar=cig, coff=coff, rnext=np.ascontiguousarray(rec.next_ref_id, np.int32),
+                pnext=np.ascontiguousarray(rec.next_pos, np.int32), tlen=np.ascontiguousarray(rec.tlen, np.int32),
+                seq=seq, soff=soff, letters=letters, qual=np.frombuffer(b"".join(qb) + b"\0", np.uint8),
+                quoff=quoff, cnames=np.frombuffer(b"".join(cb) + b"\0", np.uint8), cnoff=cnoff)
+
+
+def oracle_write_sam_c(rec, threads: int = 0, arrays=None) -> str:
+    """The C restatement of the SAM writer (OpenMP), for timing the CPU path."""
+    lib = liboracle()
+    lib.orc_write_sam.restype = C.c_int64
+    a = arrays or sam_arrays(rec)
+    n = len(rec.qname)
+    args = [C.c_int64(n), _ptr(a["qname"]), _ptr(a["qoff"]), _ptr(a["flag"]), _ptr(a["rid"]), _ptr(a["pos"]),
+            _ptr(a["mapq"]), _ptr(a["cigar"]), _ptr(a["coff"]), _ptr(a["rnext"]), _ptr(a["pnext"]), _ptr(a["tlen"]),
+            _ptr(a["seq"]), _ptr(a["soff"]), _ptr(a["letters"]), _ptr(a["qual"]), _ptr(a["quoff"]),
+            C.c_int64(len(rec.contigs)), _ptr(a["cnames"]), _ptr(a["cnoff"])]
+    total = lib.orc_write_sam(*args, None, C.c_int64(0), C.c_int32(threads))
+    out = np.zeros(total + 1, np.uint8)
+    lib.orc_write_sam(*args, _ptr(out), C.c_int64(total + 1), C.c_int32(threads))
+    return bytes(out[:total]).decode()
+
+
 def ref_write_sam(rec) -> str:
     """The reference's SAM writer on the same records (oracle/ref/units/sam.cpp)."""
     lib = libref()

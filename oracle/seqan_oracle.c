@@ -994,3 +994,94 @@ int orc_extend_seeds(const orc_xdrop_params *p, int64_t n_h, const uint8_t *seq_
     }
     return 0;
 }
+
+/* ===================================================================================== */
+/* SAM output                                                                            */
+/* ===================================================================================== */
+
+static int sam_num(char *p, int64_t v)
+{
+    char tmp[24];
+    int n = 0, k = 0;
+    uint64_t u = v < 0 ? (uint64_t)(-v) : (uint64_t)v;
+    do { tmp[n++] = (char)('0' + u % 10); u /= 10; } while (u);
+    if (v < 0) { if (p) p[k] = '-'; ++k; }
+    while (n) { if (p) p[k] = tmp[n - 1]; ++k; --n; }
+    return k;
+}
+
+/* write(target, record, context, Sam()) of bam_io/write_sam.h:126-217 (no tags); p == NULL only
+ * counts. */
+static int64_t sam_line(char *p, int64_t k, const char *qname, const int64_t *qoff, const uint16_t *flag,
+                        const int32_t *rid, const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar,
+                        const int64_t *coff, const int32_t *rnext, const int32_t *pnext, const int32_t *tlen,
+                        const uint8_t *seq, const int64_t *soff, const char *letters, const char *qual,
+                        const int64_t *quoff, const char *cnames, const int64_t *cnoff)
+{
+    int64_t w = 0, i;
+#define PUT(c) do { if (p) p[w] = (c); ++w; } while (0)
+#define NUM(v) do { w += sam_num(p ? p + w : NULL, (int64_t)(v)); } while (0)
+    for (i = qoff[k]; i < qoff[k + 1]; ++i) PUT(qname[i]);
+    PUT('\t');
+    NUM(flag[k]);
+    PUT('\t');
+    if (rid[k] == -1) PUT('*');
+    else for (i = cnoff[rid[k]]; i < cnoff[rid[k] + 1]; ++i) PUT(cnames[i]);
+    PUT('\t');
+    NUM((int64_t)pos[k] + 1);
+    PUT('\t');
+    NUM(mapq[k]);
+    PUT('\t');
+    if (coff[k] == coff[k + 1]) PUT('*');
+    for (i = coff[k]; i < coff[k + 1]; ++i) { NUM(cigar[i] >> 4); PUT("MIDNSHP=X"[cigar[i] & 15u]); }
+    PUT('\t');
+    if (rnext[k] == -1) PUT('*');
+    else if (rnext[k] == rid[k]) PUT('=');
+    else for (i = cnoff[rnext[k]]; i < cnoff[rnext[k] + 1]; ++i) PUT(cnames[i]);
+    PUT('\t');
+    NUM((int64_t)pnext[k] + 1);
+    PUT('\t');
+    if (tlen[k] == 0) PUT('0');
+    else NUM(tlen[k]);
+    PUT('\t');
+    if (soff[k] == soff[k + 1]) PUT('*');
+    for (i = soff[k]; i < soff[k + 1]; ++i) PUT(letters[seq[i] & 31]);
+    PUT('\t');
+    if (!quoff || quoff[k] == quoff[k + 1]) PUT('*');
+    else for (i = quoff[k]; i < quoff[k + 1]; ++i) PUT(qual[i]);
+    PUT('\n');
+#undef PUT
+#undef NUM
+    return w;
+}
+
+int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const uint16_t *flag, const int32_t *rid,
+                      const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
+                      const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
+                      const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
+                      int64_t ncontigs, const char *cnames, const int64_t *cnoff, char *out, int64_t cap,
+                      int32_t threads)
+{
+    int64_t k, total;
+    int64_t *off;
+    (void)ncontigs;
+    if (n < 0) return -1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    off = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+    off[0] = 0;
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (k = 0; k < n; ++k)
+        off[k + 1] = sam_line(NULL, k, qname, qoff, flag, rid, pos, mapq, cigar, coff, rnext, pnext, tlen, seq,
+                              soff, letters, qual, quoff, cnames, cnoff);
+    for (k = 0; k < n; ++k) off[k + 1] += off[k];
+    total = off[n];
+    if (out && total <= cap) {
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (k = 0; k < n; ++k)
+            sam_line(out + off[k], k, qname, qoff, flag, rid, pos, mapq, cigar, coff, rnext, pnext, tlen, seq, soff,
+                     letters, qual, quoff, cnames, cnoff);
+    }
+    free(off);
+    return total;
+}
+

@@ -115,6 +115,16 @@ int orc_extend_seeds(const orc_xdrop_params *p, int64_t n_h, const uint8_t *seq_
                      const int32_t *seed_h, const int32_t *seed_v, orc_seed *seeds, int32_t *xscores,
                      int32_t threads);
 
+/* SAM lines of BamAlignmentRecord fields (bam_io/write_sam.h:126-217), no tags: record k's
+ * fields as in the engine's gba_sam_records.  Returns the text length (the text is written when
+ * it fits cap), or -1.  threads <= 0: all. */
+int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const uint16_t *flag, const int32_t *rid,
+                      const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
+                      const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
+                      const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
+                      int64_t ncontigs, const char *cnames, const int64_t *cnoff, char *out, int64_t cap,
+                      int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@ def fixture_records():
 def test_oracle_writer_matches_reference_fixture():
     rec, text = fixture_records()
     assert O.write_sam(rec) == text
+    assert O.oracle_write_sam_c(rec, threads=2) == text
     lines = text.splitlines()
     assert len(lines) == len(rec.qname)
     assert any("\t=\t" in ln for ln in lines) and any("\t*\t*\t" in ln for ln in lines)
