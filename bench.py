@@ -59,6 +59,148 @@ WORKLOADS["sam_records_1m"] = ("1000000 SAM records of read alignments: names re
                                "positions < 10^7, MAPQ 60, 1-3 CIGAR operations, 150 bp SEQ and QUAL; "
                                "BamAlignmentRecord -> SAM text as the reference's writer")
 SAM_WORKLOADS = {"sam_records_1m"}
+WORKLOADS["fasta_reads_2m"] = ("FASTA text of 2000000 reads of 150 bp (ids 'read<k> len=150', sequences in lines of 80 "
+                               "columns, 3% lower case, 0.1% N), about 345 MB; readRecord loop into Dna5 codes + "
+                               "record offsets")
+FASTA_WORKLOADS = {"fasta_reads_2m"}
+
+
+def fasta_reads_text(n, seed=3):
+    """FASTA text of n random 150 bp reads, each sequence wrapped into lines of 80 + 70 columns."""
+    rng = np.random.default_rng(seed)
+    codes = rng.integers(0, 4, (n, 150), dtype=np.uint8)
+    codes[rng.random((n, 150)) < 0.001] = 4
+    letters = np.frombuffer(b"ACGTN", np.uint8)[codes]
+    letters[rng.random((n, 150)) < 0.03] += 32
+    rows = np.empty((n, 152), np.uint8)
+    rows[:, :80] = letters[:, :80]
+    rows[:, 80] = 10
+    rows[:, 81:151] = letters[:, 80:]
+    rows[:, 151] = 10
+    heads = [b">read%d len=150\n" % k for k in range(n)]
+    hl = np.fromiter((len(h) for h in heads), np.int64, n)
+    out = np.empty(int(hl.sum()) + 152 * n, np.uint8)
+    starts = np.zeros(n, np.int64)
+    np.cumsum(hl[:-1] + 152, out=starts[1:])
+    hb = np.frombuffer(b"".join(heads), np.uint8)
+    hoff = np.zeros(n, np.int64)
+    np.cumsum(hl[:-1], out=hoff[1:])
+    idx = np.repeat(starts - hoff, hl) + np.arange(len(hb))
+    out[idx] = hb
+    ridx = (starts + hl)[:, None] + np.arange(152)[None, :]
+    out[ridx.ravel()] = rows.ravel()
+    return out.tobytes(), codes
+
+
+def run_fasta_bench(args, rank, world, local_rank, dist):
+    from seqan_gb300 import _native as N
+    from oracle import oracle as O
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    h = ctx.handle
+    n_reads = args.pairs or 2_000_000
+    text, codes = fasta_reads_text(n_reads, seed=3 + rank)
+    n = len(text)
+
+    def pinned(nbytes):
+        p = C.c_void_p()
+        ctx.check(L.gba_host_alloc(h, C.byref(p), max(nbytes, 16)), "alloc")
+        return p
+
+    p_text = pinned(n)
+    C.memmove(p_text, text, n)
+    cap = n_reads + 1
+    p_ib, p_ie, p_so, p_codes = pinned(8 * cap), pinned(8 * cap), pinned(8 * cap), pinned(n)
+    r = N.GbaSeqRecords(cap, n, p_ib, p_ie, p_so, None, p_codes, None, 0, 0, -1)
+
+    def call():
+        ctx.check(L.gba_read_fasta(h, p_text, n, 5, C.byref(r)), "gba_read_fasta")
+
+    for _ in range(args.warmup):
+        call()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        wall.append(time.perf_counter() - t0)
+        kern.append(ctx.stats().dp_kernel_ms)
+    clocks = sampler.stop()
+    got = np.ctypeslib.as_array(C.cast(p_codes, C.POINTER(C.c_uint8)), (r.residues,))
+    so = np.ctypeslib.as_array(C.cast(p_so, C.POINTER(C.c_int64)), (r.num + 1,))
+    parity = bool(r.num == n_reads and np.array_equal(got, codes.ravel()) and np.array_equal(
+        so, np.arange(n_reads + 1, dtype=np.int64) * 150))
+    k = min(n_reads, 20_000)
+    cut = text.index(b">read%d " % k) if k < n_reads else n
+    want = O.oracle_read_records(text[:cut], "fasta", "dna5")
+    ib = np.ctypeslib.as_array(C.cast(p_ib, C.POINTER(C.c_int64)), (k,))
+    ie = np.ctypeslib.as_array(C.cast(p_ie, C.POINTER(C.c_int64)), (k,))
+    parity = parity and all(text[ib[j]:ie[j]] == want[j][0] for j in range(k))
+    kernel_ms = sum(kern) / len(kern)
+    gb = n * world / 1e9
+    value = gb / (kernel_ms * 1e-3)
+    e2e = gb * len(wall) / sum(wall)
+    hbm = measured_hbm_gbs()
+    out_bytes = int(r.residues) + 24 * int(r.num)
+    achieved = (n + out_bytes) / (kernel_ms * 1e-3) / 1e9
+    line = {"metric": "GB/s of FASTA text read into records", "value": value, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "records": n_reads,
+                       "text_bytes": n, "residues": int(r.residues), "parallelism": f"replicas x{world}",
+                       "l2": "text larger than L2"},
+            "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": out_bytes,
+                    "ms_per_step": 1e3 * sum(wall) / len(wall)},
+            "gpu_launches": args.steps * 3,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm if hbm else None, "traffic": None,
+                         "kernel": "k_fasta_summary + k_fasta_scan_blocks + k_fasta_write",
+                         "algorithmic_bytes": "text read once + codes and 3 x 8 B per record written once",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "clocks": clocks, "parity_vs_generated_codes_and_oracle_ids": parity}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            O.oracle_read_records(text, "fasta", "dna5", raw=True)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        line["cpu_baseline"] = {"value": n / best / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                "sample": f"the whole {n} byte text, orc_read_records (oracle/seqan_oracle.c, the "
+                                          "reference's readRecord loop restated; sequential as the reference's "
+                                          "reader), best of 2",
+                                "seconds": best}
+    for p in (p_text, p_ib, p_ie, p_so, p_codes):
+        L.gba_host_free(h, p)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_fasta_reference(args):
+    from oracle import oracle as O
+    n_reads = args.pairs or 2_000_000
+    text, _ = fasta_reads_text(n_reads)
+    for _ in range(args.warmup):
+        O.oracle_read_records(text, "fasta", "dna5", raw=True)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.oracle_read_records(text, "fasta", "dna5", raw=True)
+        times.append(time.perf_counter() - t0)
+    rate = len(text) * len(times) / sum(times) / 1e9
+    print(json.dumps({"metric": "GB/s of FASTA text read into records", "value": rate, "unit": "GB/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload, "text_bytes": len(text),
+                                 "description": WORKLOADS[args.workload]},
+                      "cpu_baseline": {"value": rate, "unit": "GB/s", "cores": 1, "kind": "port",
+                                       "sample": "the whole text per step, the reference's readRecord loop restated "
+                                                 "in C (orc_read_records), sequential as the reference's reader"},
+                      "e2e": {"value": rate, "unit": "GB/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
 
 
 def make_sam_records(n, seed=21):
@@ -825,7 +967,10 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
-        if args.workload in SAM_WORKLOADS:
+        if args.workload in FASTA_WORKLOADS:
+            if rank == 0:
+                run_fasta_reference(args)
+        elif args.workload in SAM_WORKLOADS:
             if rank == 0:
                 run_sam_reference(args)
         elif args.workload in EXTEND_WORKLOADS:
@@ -846,6 +991,11 @@ def main():
         return
     if args.workload in EXTEND_WORKLOADS:
         run_extend_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in FASTA_WORKLOADS:
+        run_fasta_bench(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
         return

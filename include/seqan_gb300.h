@@ -50,7 +50,8 @@ enum {
     GBA_ECUDA = 4,         /* a CUDA call failed; see gba_last_error */
     GBA_ETIMEOUT = 5,      /* a bounded device wait or a host watchdog expired */
     GBA_EUNSUPPORTED = 6,  /* parameter combination not supported */
-    GBA_ECAPACITY = 7      /* an output buffer supplied by the caller is too small */
+    GBA_ECAPACITY = 7,     /* an output buffer supplied by the caller is too small */
+    GBA_EPARSE = 8         /* input text is not in the format (ParseError / UnexpectedEnd) */
 };
 
 /* Per-pair status flags (gba_result.pair_status). */
@@ -472,6 +473,37 @@ typedef struct {
  * small. */
 GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *records, char *out, int64_t capacity,
                            int64_t *line_off);
+
+/* --- FASTA / FASTQ input -------------------------------------------------------------------
+ * Every record of a FASTA or FASTQ text, as the loop
+ *     while (!atEnd(iter)) readRecord(id, seq, qual, iter, Fasta | Fastq);
+ * reads them (seq_io/fasta_fastq.h:265-283 FASTA, :354-392 FASTQ) with seq a String<Dna>,
+ * String<Dna5> or String<AminoAcid> (alphabet 4, 5, 27) and qual a CharString, into the layout
+ * gba_align_batch takes: record k's residue codes are codes[seq_off[k], seq_off[k+1]), its id is
+ * text[id_begin[k], id_end[k]) and its FASTQ qualities quals[seq_off[k], qual_end[k]) (FASTA:
+ * qual_end[k] = seq_off[k]).  Whitespace inside a sequence is skipped; any other character
+ * outside the alphabet (IsInAlphabet, stream/tokenization.h:51-63) is GBA_EPARSE with
+ * error_offset at it, as the reference's ParseError; a non-empty text without a record start is
+ * GBA_EPARSE with error_offset = length (UnexpectedEnd).  When a capacity is too small the call
+ * returns GBA_ECAPACITY with num and residues set.  gba_read_fasta parses on the device;
+ * gba_read_fastq parses on the host (ctx may be NULL). */
+typedef struct {
+    int64_t record_capacity;   /* entries of id_begin / id_end / qual_end (>= num) and seq_off (>= num + 1) */
+    int64_t residue_capacity;  /* bytes of codes (and quals) */
+    int64_t *id_begin, *id_end;
+    int64_t *seq_off;
+    int64_t *qual_end;         /* may be NULL */
+    uint8_t *codes;
+    char *quals;               /* FASTQ qualities; may be NULL */
+    int64_t num;               /* out: records */
+    int64_t residues;          /* out: residues of all records */
+    int64_t error_offset;      /* out: text offset of a GBA_EPARSE, else -1 */
+} gba_seq_records;
+
+GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t length, int32_t alphabet,
+                           gba_seq_records *records);
+GBA_API int gba_read_fastq(gba_context *ctx, const char *text, int64_t length, int32_t alphabet,
+                           gba_seq_records *records);
 
 #ifdef __cplusplus
 }

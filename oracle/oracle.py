@@ -614,3 +614,82 @@ def cigar_string(segments) -> str:
         else:
             ops.append([op, ln])
     return "".join(f"{n}{'N' if (o == 'D' and n >= 20) else o}" for o, n in ops)
+
+
+# --- FASTA / FASTQ records (seq_io/fasta_fastq.h readRecord loop) ------------------------------
+
+SEQIO_ALPHABETS = {"dna": 4, "dna5": 5, "aa": 27}
+
+
+class SeqParseError(Exception):
+    """ParseError (kind "parse") or UnexpectedEnd (kind "end") at text offset `offset`."""
+
+    def __init__(self, kind, offset):
+        super().__init__(f"{kind} at {offset}")
+        self.kind, self.offset = kind, offset
+
+
+def oracle_read_records(text: bytes, fmt: str, alphabet: str = "dna5", raw: bool = False):
+    """Records of FASTA ("fasta") or FASTQ ("fastq") text through the C restatement of the
+    reference's readRecord loop: a list of (id bytes, residue codes uint8, quality bytes), or with
+    raw the arrays (num, id_begin, id_end, seq_off, codes)."""
+    lib = liboracle()
+    lib.orc_read_records.restype = C.c_int32
+    text = bytes(text)
+    n = len(text)
+    rec_cap = text.count(b"@" if fmt == "fastq" else b">") + 2
+    res_cap = n + 1
+    ib, ie, so, qe = (np.zeros(rec_cap, np.int64) for _ in range(4))
+    codes = np.zeros(res_cap, np.uint8)
+    quals = np.zeros(res_cap, np.uint8)
+    num, res, err = C.c_int64(), C.c_int64(), C.c_int64()
+    buf = C.create_string_buffer(text, n + 1)
+    rc = lib.orc_read_records(C.c_int32(1 if fmt == "fastq" else 0), C.c_int32(SEQIO_ALPHABETS[alphabet]), buf,
+                              C.c_int64(n), C.c_int64(rec_cap), _ptr(ib), _ptr(ie), _ptr(so), _ptr(qe),
+                              C.c_int64(res_cap), _ptr(codes), _ptr(quals), C.byref(num), C.byref(res), C.byref(err))
+    if rc == -1:
+        raise SeqParseError("parse", err.value)
+    if rc == -2:
+        raise SeqParseError("end", err.value)
+    assert rc == 0, rc
+    if raw:
+        k = num.value
+        return k, ib[:k], ie[:k], so[:k + 1], codes[:res.value]
+    out = []
+    for k in range(num.value):
+        out.append((text[ib[k]:ie[k]], codes[so[k]:so[k + 1]].copy(), bytes(quals[so[k]:qe[k]])))
+    return out
+
+
+def ref_read_records(text: bytes, fmt: str, alphabet: str = "dna5"):
+    """The reference's readRecord loop on the same text (oracle/ref/units/seqio.cpp)."""
+    lib = libref()
+    lib.ref_read_records.restype = C.c_int64
+    text = bytes(text)
+    cap = 3 * len(text) + 64
+    out = C.create_string_buffer(cap)
+    nrec = C.c_int64()
+    r = lib.ref_read_records(C.c_int32(1 if fmt == "fastq" else 0), C.c_int32(SEQIO_ALPHABETS[alphabet]),
+                             C.c_char_p(text), C.c_int64(len(text)), out, C.c_int64(cap), C.byref(nrec))
+    if r == -1:
+        raise SeqParseError("parse", None)
+    if r == -2:
+        raise SeqParseError("end", None)
+    assert r >= 0, r
+    raw, p, recs = out.raw[:r], 0, []
+    while p < r:
+        parts = []
+        for _ in range(3):
+            L = int.from_bytes(raw[p:p + 4], "little")
+            parts.append(raw[p + 4:p + 4 + L])
+            p += 4 + L
+        recs.append((parts[0], np.frombuffer(parts[1], np.uint8).copy(), parts[2]))
+    return recs
+
+
+def ref_char_table(alphabet: str):
+    """The reference's IsInAlphabet / conversion per character: code or -1."""
+    lib = libref()
+    t = np.zeros(256, np.int16)
+    lib.ref_char_table(C.c_int32(SEQIO_ALPHABETS[alphabet]), _ptr(t))
+    return t

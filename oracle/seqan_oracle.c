@@ -1085,3 +1085,102 @@ int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const u
     return total;
 }
 
+
+/* ---------------------------------------------------------------------------------------------
+ * FASTA / FASTQ records: the loop `while (!atEnd(iter)) readRecord(id, seq, qual, iter, Fasta|Fastq)`
+ * of seq_io/fasta_fastq.h, seq a String<Dna|Dna5|AminoAcid>, qual a CharString.
+ *   Fasta (:265-283): skipUntil '>', skipOne, readLine(id), readUntil(seq, '>') ignoring
+ *     IsWhitespace (' ', '\t', '\n', '\r') and asserting IsInAlphabet on the rest.
+ *   Fastq (:354-392): skipUntil '@', skipOne, readLine(id), readUntil(seq, '+') as above,
+ *     skipOne '+' (UnexpectedEnd at the end of the text), skipLine, then as many non-newline
+ *     quality characters as the sequence has residues (fewer at the end of the text), skip
+ *     whitespace; the next character must be '@', 0xFF or the end, else ParseError.
+ * readLine (stream/tokenization.h:430-450) stops at '\r' or '\n' and consumes "\r\n", "\r" or "\n".
+ * IsInAlphabet<T>(c) is convert<char>(T(c)) == toupper(c) (stream/tokenization.h:51-63). */
+
+static int orc_residue_code(int32_t alphabet, unsigned char c)
+{
+    const unsigned char u = (c >= 'a' && c <= 'z') ? (unsigned char)(c - 32) : c;
+    if (alphabet == 27) {
+        static const char aa[] = "ABCDEFGHIJKLMNOPQRSTUVWYZX*";
+        for (int k = 0; k < 27; ++k)
+            if (aa[k] == (char)u) return k;
+        return -1;
+    }
+    switch (u) {
+    case 'A': return 0;
+    case 'C': return 1;
+    case 'G': return 2;
+    case 'T': return 3;
+    case 'N': return alphabet == 5 ? 4 : -1;
+    default: return -1;
+    }
+}
+
+static int orc_is_nl(unsigned char c) { return c == '\n' || c == '\r'; }
+static int orc_is_ws(unsigned char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; }
+
+int32_t orc_read_records(int32_t format, int32_t alphabet, const char *text_, int64_t n, int64_t rec_cap,
+                         int64_t *id_begin, int64_t *id_end, int64_t *seq_off, int64_t *qual_end,
+                         int64_t res_cap, uint8_t *codes, char *quals, int64_t *num, int64_t *residues,
+                         int64_t *err_off)
+{
+    const unsigned char *t = (const unsigned char *)text_;
+    const unsigned char start = format == 1 ? '@' : '>';
+    int16_t table[256];   /* the conversion as a table, as TranslateTableCharToDna5_ and the like */
+    for (int c = 0; c < 256; ++c) table[c] = (int16_t)orc_residue_code(alphabet, (unsigned char)c);
+    int64_t p = 0, rec = 0, res = 0;
+    int status = 0;
+    *err_off = -1;
+    while (p < n) {
+        while (p < n && t[p] != start) ++p;                     /* skipUntil */
+        if (p >= n) { *err_off = n; status = -2; break; }       /* skipOne at the end */
+        ++p;
+        const int64_t ib = p;                                   /* readLine(id) */
+        while (p < n && !orc_is_nl(t[p])) ++p;
+        const int64_t ie = p;
+        if (p < n && t[p] == '\r') ++p;
+        if (p < n && t[p] == '\n') ++p;
+        const int64_t sb = res;
+        const unsigned char stop = format == 1 ? '+' : '>';
+        for (; p < n && t[p] != stop; ++p) {                    /* readUntil(seq, stop) */
+            if (orc_is_ws(t[p])) continue;
+            const int code = table[t[p]];
+            if (code < 0) { *err_off = p; status = -1; break; }
+            if (res < res_cap) codes[res] = (uint8_t)code;
+            ++res;
+        }
+        if (status) break;
+        int64_t qe = sb;                                        /* FASTA: no qualities */
+        if (format == 1) {
+            if (p >= n) { *err_off = n; status = -2; break; }   /* skipOne('+') */
+            ++p;
+            while (p < n && !orc_is_nl(t[p])) ++p;              /* skipLine */
+            if (p < n && t[p] == '\r') ++p;
+            if (p < n && t[p] == '\n') ++p;
+            int64_t need = res - sb;
+            qe = sb;
+            for (; p < n && need > 0; ++p) {                    /* counted qualities */
+                if (orc_is_nl(t[p])) continue;
+                if (qe < res_cap && quals) quals[qe] = (char)t[p];
+                ++qe;
+                --need;
+            }
+            while (p < n && orc_is_ws(t[p])) ++p;
+            if (p < n && t[p] != '@' && t[p] != 0xFF) { *err_off = p; status = -1; break; }
+        }
+        if (rec < rec_cap) {
+            id_begin[rec] = ib;
+            id_end[rec] = ie;
+            seq_off[rec] = sb;
+            if (qual_end) qual_end[rec] = qe;
+        }
+        ++rec;
+    }
+    *num = rec;
+    *residues = res;
+    if (status) return status;
+    if (rec + 1 > rec_cap || res > res_cap) return -3;
+    seq_off[rec] = res;
+    return 0;
+}

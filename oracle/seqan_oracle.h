@@ -125,6 +125,17 @@ int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const u
                       int64_t ncontigs, const char *cnames, const int64_t *cnoff, char *out, int64_t cap,
                       int32_t threads);
 
+/* Records of FASTA (format 0) or FASTQ (format 1) text as the reference's readRecord loop reads
+ * them (seq_io/fasta_fastq.h:265-283, :354-392), alphabet 4 Dna, 5 Dna5, 27 AminoAcid: record k's
+ * id is text[id_begin[k], id_end[k]), its residues codes[seq_off[k], seq_off[k+1]), its qualities
+ * quals[seq_off[k], qual_end[k]).  Returns 0, -1 on ParseError, -2 on UnexpectedEnd (err_off =
+ * the text offset), -3 when rec_cap (>= num + 1) or res_cap is too small; *num and *residues are
+ * the counts read.  Sequential, as the reference's reader is. */
+int32_t orc_read_records(int32_t format, int32_t alphabet, const char *text, int64_t n, int64_t rec_cap,
+                         int64_t *id_begin, int64_t *id_end, int64_t *seq_off, int64_t *qual_end,
+                         int64_t res_cap, uint8_t *codes, char *quals, int64_t *num, int64_t *residues,
+                         int64_t *err_off);
+
 #ifdef __cplusplus
 }
 #endif

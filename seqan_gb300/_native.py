@@ -21,7 +21,8 @@ NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", 
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-shared", "-lgomp"]
 
 # Status codes (include/seqan_gb300.h)
-GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY = range(8)
+GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY, GBA_EPARSE = \
+    range(9)
 GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED, GBA_PAIR_FAILED = 0, 1, 2, 3
 GBA_GLOBAL, GBA_LOCAL = 0, 1
 GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE = 0, 1, 2
@@ -45,7 +46,7 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_server_create", "gba_server_submit", "gba_server_poll", "gba_server_get_stats",
             "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule",
             "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments", "gba_align_packed",
-            "gba_format_sam"]
+            "gba_format_sam", "gba_read_fasta", "gba_read_fastq"]
 
 
 class GbaConfig(C.Structure):
@@ -150,6 +151,12 @@ class GbaSamRecords(C.Structure):
                 ("contig_off", C.c_void_p), ("num_contigs", C.c_int64)]
 
 
+class GbaSeqRecords(C.Structure):
+    _fields_ = [("record_capacity", C.c_int64), ("residue_capacity", C.c_int64), ("id_begin", C.c_void_p),
+                ("id_end", C.c_void_p), ("seq_off", C.c_void_p), ("qual_end", C.c_void_p), ("codes", C.c_void_p),
+                ("quals", C.c_void_p), ("num", C.c_int64), ("residues", C.c_int64), ("error_offset", C.c_int64)]
+
+
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + \
         [os.path.join(INCLUDE, "seqan_gb300.h")]
@@ -224,6 +231,8 @@ def lib():
             L.gba_align_packed.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaPackedSet),
                                            C.POINTER(GbaPackedSet), C.c_int32, C.POINTER(GbaResult)]
             L.gba_format_sam.argtypes = [vp, C.POINTER(GbaSamRecords), vp, i64, vp]
+            L.gba_read_fasta.argtypes = [vp, vp, i64, i32, C.POINTER(GbaSeqRecords)]
+            L.gba_read_fastq.argtypes = [vp, vp, i64, i32, C.POINTER(GbaSeqRecords)]
             L.gba_clock_seconds.argtypes = []
             L.gba_clock_seconds.restype = C.c_double
             _lib = L

@@ -207,6 +207,7 @@ struct gba_context {
     bool device_codes = false;
     DevBuf pk_words, pk_off_h, pk_off_v;
     DevBuf sam_in, sam_len, sam_tmp, sam_out;   // gba_format_sam
+    DevBuf fa_text, fa_sum, fa_tmp, fa_out;     // gba_read_fasta
 };
 
 namespace {
@@ -1520,6 +1521,7 @@ GBA_API const char *gba_status_string(int s)
     case GBA_ETIMEOUT: return "timeout";
     case GBA_EUNSUPPORTED: return "unsupported";
     case GBA_ECAPACITY: return "output buffer too small";
+    case GBA_EPARSE: return "input text not in the format";
     default: return "unknown status";
     }
 }
@@ -1797,3 +1799,4 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 #include "extend_host.cuh"
 #include "packed_host.cuh"
 #include "sam_host.cuh"
+#include "seqio_host.cuh"

@@ -1,0 +1,473 @@
+// FASTA / FASTQ input into the engine's record layout (residue codes back to back with n + 1
+// offsets, the form gba_align_batch reads).  Semantics: the loop
+// `while (!atEnd(iter)) readRecord(id, seq, qual, iter, Fasta|Fastq)` of seq_io/fasta_fastq.h
+// (:265-283 FASTA, :354-392 FASTQ), seq a String<Dna|Dna5|AminoAcid>, qual a CharString.
+//
+// FASTA runs on the device.  Reading it is a three-state automaton over the bytes: BEFORE the
+// first record (skipUntil '>'), in a HEADER line (readLine: up to '\r' or '\n'), in a SEQUENCE
+// (readUntil '>': whitespace skipped, every other byte a residue or a ParseError).  A '>' outside a
+// header starts a record; a newline ends a header.  Each thread summarises a 128-byte chunk for all
+// three start states at once (one pass: the BEFORE and HEADER runs join the SEQUENCE run at the
+// chunk's first '>' / first newline), a block scan and a one-block scan over the 16 KB blocks'
+// summaries compose them, and a second pass re-reads each chunk from its known state, record and residue
+// index to write codes and record bounds.
+//
+// FASTQ runs on the host: where a record ends depends on counting its quality characters from the
+// record's start ('@' is also a quality value), so the text does not split into independent chunks.
+#pragma once
+
+namespace gba {
+
+constexpr int kFaChunk = 128;      // bytes per thread
+constexpr int kFaThreads = 128;    // threads per block: 16 KB of text per block
+
+enum : int8_t { FA_GT = -4, FA_NL = -3, FA_WS = -2, FA_BAD = -1 };
+enum : int32_t { FA_BEFORE = 0, FA_HEADER = 1, FA_SEQ = 2 };
+
+struct FaSum {
+    int64_t rec[3];   // records started in the chunk, per start state
+    int64_t res[3];   // residues (valid or not) read in the chunk, per start state
+    int32_t end[3];   // state after the chunk, per start state
+    int32_t pad;
+};
+
+// v[m] for a state m in 0..2 through selects (runtime indexing would put the summary in local
+// memory); any other m reads v[2].
+template <typename T>
+__host__ __device__ __forceinline__ T fa_pick(const T (&v)[3], int m)
+{
+    return m == 0 ? v[0] : m == 1 ? v[1] : v[2];
+}
+
+struct FaCompose {
+    __host__ __device__ FaSum operator()(const FaSum &a, const FaSum &b) const
+    {
+        FaSum r;
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+            const int m = a.end[s];
+            r.end[s] = fa_pick(b.end, m);
+            r.rec[s] = a.rec[s] + fa_pick(b.rec, m);
+            r.res[s] = a.res[s] + fa_pick(b.res, m);
+        }
+        r.pad = 0;
+        return r;
+    }
+};
+
+__host__ __device__ inline FaSum fa_identity()
+{
+    FaSum r{};
+    r.end[0] = 0;
+    r.end[1] = 1;
+    r.end[2] = 2;
+    return r;
+}
+
+struct FaArgs {
+    const uint8_t *text;
+    int64_t n;
+    int8_t cls[256];          // residue code, or FA_GT / FA_NL / FA_WS / FA_BAD
+    FaSum *block_sum;         // [blocks], inclusive-scanned in place between the two passes
+    uint8_t *codes;
+    int64_t *id_begin, *id_end, *seq_off;
+    unsigned long long *error;   // smallest offset of a ParseError byte
+    int64_t nrec, nres;          // totals of the scan: bounds of the second pass's writes
+    unsigned int *bounds;        // set when a write falls outside them (skipped)
+};
+
+// Calls f(byte, i) for the 128 bytes of a chunk held in registers, in order (all indices
+// compile-time constants after unrolling, so the chunk stays in registers).
+template <typename F>
+__device__ __forceinline__ void fa_for_bytes(const uint4 (&w)[kFaChunk / 16], F &&f)
+{
+#pragma unroll
+    for (int j = 0; j < kFaChunk / 16; ++j) {
+        const uint32_t xs[4] = {w[j].x, w[j].y, w[j].z, w[j].w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t x = xs[q];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                f(x & 0xffu, j * 16 + q * 4 + b);
+                x >>= 8;
+            }
+        }
+    }
+}
+
+// The SEQUENCE run over one byte, without branches: '>' starts a record outside a header, a
+// newline ends a header, any other non-whitespace byte is a residue outside a header.
+struct FaRun {
+    bool hdr = false, seen_gt = false, seen_nl = false;
+    int32_t rec = 0, res = 0, gt_res = 0, nl_rec = 0, nl_res = 0;
+    __device__ __forceinline__ void step(uint32_t c)
+    {
+        const bool g = c == '>';
+        const bool l = c == '\n' || c == '\r';
+        const bool r = !(g || l || c == ' ' || c == '\t');
+        gt_res = (g && !seen_gt) ? res : gt_res;
+        nl_rec = (l && !seen_nl) ? rec : nl_rec;
+        nl_res = (l && !seen_nl) ? res : nl_res;
+        seen_gt |= g;
+        seen_nl |= l;
+        rec += (g && !hdr) ? 1 : 0;
+        res += (r && !hdr) ? 1 : 0;
+        hdr = g || (hdr && !l);
+    }
+    __device__ __forceinline__ FaSum summary() const
+    {
+        FaSum o;
+        o.pad = 0;
+        const int s = hdr ? FA_HEADER : FA_SEQ;
+        o.end[FA_SEQ] = s;
+        o.rec[FA_SEQ] = rec;
+        o.res[FA_SEQ] = res;
+        // From BEFORE: nothing counts until the first '>', where the run joins the SEQUENCE run.
+        o.end[FA_BEFORE] = seen_gt ? s : FA_BEFORE;
+        o.rec[FA_BEFORE] = seen_gt ? rec : 0;
+        o.res[FA_BEFORE] = seen_gt ? res - gt_res : 0;
+        // From HEADER: nothing counts until the first newline, after which both runs are in SEQUENCE.
+        o.end[FA_HEADER] = seen_nl ? s : FA_HEADER;
+        o.rec[FA_HEADER] = seen_nl ? rec - nl_rec : 0;
+        o.res[FA_HEADER] = seen_nl ? res - nl_res : 0;
+        return o;
+    }
+};
+
+// Summary of the chunk at base: a full chunk through 16-byte loads kept in registers, the text's
+// last partial chunk through byte loads.
+__device__ __forceinline__ FaSum fa_summary_at(const uint8_t *text, int64_t n, int64_t base, uint4 (&w)[kFaChunk / 16],
+                                               bool &full)
+{
+    FaRun run;
+    full = n - base >= kFaChunk;
+    if (full) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(text + base);
+#pragma unroll
+        for (int i = 0; i < kFaChunk / 16; ++i) w[i] = __ldg(src + i);
+        fa_for_bytes(w, [&](uint32_t c, int) { run.step(c); });
+    } else {
+        for (int64_t i = base; i < n; ++i) run.step(text[i]);
+    }
+    return run.summary();
+}
+
+__global__ void __launch_bounds__(kFaThreads) k_fasta_summary(const uint8_t *__restrict__ text, int64_t n,
+                                                              FaSum *__restrict__ block_sum)
+{
+    using Scan = cub::BlockScan<FaSum, kFaThreads, cub::BLOCK_SCAN_WARP_SCANS>;
+    __shared__ typename Scan::TempStorage tmp;
+    const int64_t base = (int64_t(blockIdx.x) * kFaThreads + threadIdx.x) * kFaChunk;
+    FaSum mine = fa_identity();
+    if (base < n) {
+        uint4 w[kFaChunk / 16];
+        bool full;
+        mine = fa_summary_at(text, n, base, w, full);
+    }
+    FaSum incl;
+    Scan(tmp).InclusiveScan(mine, incl, FaCompose());
+    if (threadIdx.x == kFaThreads - 1) block_sum[blockIdx.x] = incl;
+}
+
+// One byte of the record pass: record bounds go to global memory (rare), residue codes to the
+// block's shared staging buffer at their offset from the block's first residue.
+struct FaWriter {
+    const int8_t *cls;
+    uint8_t *stage;
+    int64_t stage_base, nrec, nres;
+    int64_t *id_begin, *id_end, *seq_off;
+    unsigned long long *error;
+    unsigned int *bounds;
+    int s;
+    int64_t rec, res;
+    __device__ __forceinline__ void step(uint32_t c, int64_t pos)
+    {
+        const int k = cls[c];
+        if (k == FA_GT) {
+            if (s != FA_HEADER) {
+                ++rec;
+                s = FA_HEADER;
+                if (rec >= 0 && rec < nrec) {
+                    id_begin[rec] = pos + 1;
+                    seq_off[rec] = res;
+                } else {
+                    atomicOr(bounds, 1u);
+                }
+            }
+        } else if (k == FA_NL) {
+            if (s == FA_HEADER) {
+                if (rec >= 0 && rec < nrec) id_end[rec] = pos;
+                else atomicOr(bounds, 1u);
+                s = FA_SEQ;
+            }
+        } else if (k != FA_WS && s == FA_SEQ) {
+            if (k == FA_BAD) atomicMin(error, static_cast<unsigned long long>(pos));
+            const int64_t o = res - stage_base;
+            if (res < nres && o >= 0 && o < kFaThreads * kFaChunk) stage[o] = k == FA_BAD ? uint8_t(0) : uint8_t(k);
+            else atomicOr(bounds, 2u);
+            ++res;
+        }
+    }
+};
+
+__global__ void __launch_bounds__(kFaThreads) k_fasta_write(FaArgs a)
+{
+    using Scan = cub::BlockScan<FaSum, kFaThreads, cub::BLOCK_SCAN_WARP_SCANS>;
+    __shared__ typename Scan::TempStorage tmp;
+    __shared__ int8_t cls[256];
+    __shared__ uint8_t stage[kFaThreads * kFaChunk];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) cls[i] = a.cls[i];
+    __syncthreads();
+    const int64_t base = (int64_t(blockIdx.x) * kFaThreads + threadIdx.x) * kFaChunk;
+    uint4 w[kFaChunk / 16];
+    bool full = false;
+    FaSum mine = fa_identity();
+    if (base < a.n) mine = fa_summary_at(a.text, a.n, base, w, full);
+    FaSum before;
+    Scan(tmp).ExclusiveScan(mine, before, fa_identity(), FaCompose());
+    const FaSum blk = blockIdx.x ? a.block_sum[blockIdx.x - 1] : fa_identity();
+    const int64_t blk_res = blk.res[FA_BEFORE];
+    if (base < a.n) {
+        // State, records started and residues read before this chunk, from the start of the text.
+        const int mid = blk.end[FA_BEFORE];
+        FaWriter wr{cls, stage, blk_res, a.nrec, a.nres, a.id_begin, a.id_end, a.seq_off, a.error, a.bounds,
+                    fa_pick(before.end, mid), blk.rec[FA_BEFORE] + fa_pick(before.rec, mid) - 1,
+                    blk_res + fa_pick(before.res, mid)};
+        if (full) {
+            fa_for_bytes(w, [&](uint32_t c, int i) { wr.step(c, base + i); });
+        } else {
+            for (int64_t i = base; i < a.n; ++i) wr.step(a.text[i], i);
+        }
+    }
+    __syncthreads();
+    // The block's residues are one contiguous range of the output: copy it out coalesced.
+    const int64_t cnt = a.block_sum[blockIdx.x].res[FA_BEFORE] - blk_res;
+    uint8_t *out = a.codes + blk_res;
+    for (int64_t i = threadIdx.x; i < cnt && i < kFaThreads * kFaChunk && blk_res + i < a.nres; i += kFaThreads)
+        out[i] = stage[i];
+}
+
+// Inclusive scan of the block summaries in place, one block: thread t composes the summaries
+// [t * per, min((t + 1) * per, nb)) in order, a block scan over the threads' aggregates gives each
+// thread its prefix, and the thread rewrites its range with running inclusive values.
+constexpr int kFaScanThreads = 1024;
+
+__global__ void __launch_bounds__(kFaScanThreads) k_fasta_scan_blocks(FaSum *sums, int64_t nb)
+{
+    using Scan = cub::BlockScan<FaSum, kFaScanThreads, cub::BLOCK_SCAN_WARP_SCANS>;
+    __shared__ typename Scan::TempStorage tmp;
+    const int64_t per = (nb + kFaScanThreads - 1) / kFaScanThreads;
+    const int64_t lo = int64_t(threadIdx.x) * per;
+    const int64_t hi = lo + per < nb ? lo + per : nb;
+    const FaCompose op;
+    FaSum agg = fa_identity();
+    for (int64_t i = lo; i < hi; ++i) agg = op(agg, sums[i]);
+    FaSum pre;
+    Scan(tmp).ExclusiveScan(agg, pre, fa_identity(), op);
+    for (int64_t i = lo; i < hi; ++i) {
+        pre = op(pre, sums[i]);
+        sums[i] = pre;
+    }
+}
+
+// Residue code per character: the reference's IsInAlphabet<T>(c) ? ordValue(T(c)) : ParseError.
+inline bool seqio_classes(int32_t alphabet, int8_t *cls)
+{
+    if (alphabet != 4 && alphabet != 5 && alphabet != 27) return false;
+    for (int c = 0; c < 256; ++c) cls[c] = FA_BAD;
+    if (alphabet == 27) {
+        static const char aa[] = "ABCDEFGHIJKLMNOPQRSTUVWYZX*";
+        for (int k = 0; k < 27; ++k) {
+            cls[uint8_t(aa[k])] = int8_t(k);
+            if (aa[k] >= 'A' && aa[k] <= 'Z') cls[uint8_t(aa[k] + 32)] = int8_t(k);
+        }
+    } else {
+        const char *dna = alphabet == 5 ? "ACGTN" : "ACGT";
+        for (int k = 0; dna[k]; ++k) {
+            cls[uint8_t(dna[k])] = int8_t(k);
+            cls[uint8_t(dna[k] + 32)] = int8_t(k);
+        }
+    }
+    cls[uint8_t(' ')] = FA_WS;
+    cls[uint8_t('\t')] = FA_WS;
+    cls[uint8_t('\n')] = FA_NL;
+    cls[uint8_t('\r')] = FA_NL;
+    cls[uint8_t('>')] = FA_GT;
+    return true;
+}
+
+inline int seqio_check(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r,
+                       int8_t *cls)
+{
+    if (!r || n < 0 || (n > 0 && !text)) return fail(ctx, GBA_EINVAL, "null text or records, or negative length");
+    if (!seqio_classes(alphabet, cls)) return fail(ctx, GBA_EINVAL, "alphabet must be 4 (Dna), 5 (Dna5) or 27 (AminoAcid)");
+    r->num = 0;
+    r->residues = 0;
+    r->error_offset = -1;
+    return GBA_OK;
+}
+
+}  // namespace gba
+
+extern "C" {
+
+GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r)
+{
+    using namespace gba;
+    if (!ctx) return GBA_EINVAL;
+    FaArgs a{};
+    if (int rc = seqio_check(ctx, text, n, alphabet, r, a.cls)) return rc;
+    if (n == 0) {
+        if (r->record_capacity < 1 || !r->seq_off) return fail(ctx, GBA_ECAPACITY, "seq_off needs 1 entry");
+        r->seq_off[0] = 0;
+        return GBA_OK;
+    }
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int64_t chunks = (n + kFaChunk - 1) / kFaChunk;
+    const int64_t blocks = (chunks + kFaThreads - 1) / kFaThreads;
+    if (blocks > INT32_MAX) return fail(ctx, GBA_EINVAL, "text too long");
+    GBA_CUDA(ctx, ctx->fa_text.ensure(size_t(n) + 16));
+    GBA_CUDA(ctx, ctx->fa_sum.ensure(size_t(blocks) * sizeof(FaSum) + 16));
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(ctx->fa_text.ptr, text, size_t(n), cudaMemcpyHostToDevice, st));
+    a.text = ctx->fa_text.as<uint8_t>();
+    a.n = n;
+    a.block_sum = ctx->fa_sum.as<FaSum>();
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
+    k_fasta_summary<<<unsigned(blocks), kFaThreads, 0, st>>>(a.text, a.n, a.block_sum);
+    GBA_CUDA(ctx, cudaGetLastError());
+    k_fasta_scan_blocks<<<1, kFaScanThreads, 0, st>>>(a.block_sum, blocks);
+    GBA_CUDA(ctx, cudaGetLastError());
+    GBA_CUDA(ctx, ctx->fa_tmp.ensure(64));
+    FaSum total;
+    GBA_CUDA(ctx, cudaMemcpyAsync(&total, a.block_sum + (blocks - 1), sizeof(FaSum), cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaStreamSynchronize(st));
+    const int64_t nrec = total.rec[FA_BEFORE], nres = total.res[FA_BEFORE];
+    r->num = nrec;
+    r->residues = nres;
+    if (nrec == 0) {   // readRecord's skipOne('>') at the end of the text: UnexpectedEnd
+        r->error_offset = n;
+        return fail(ctx, GBA_EPARSE, "no '>' record start in the text");
+    }
+    if (nrec + 1 > r->record_capacity || nres > r->residue_capacity || !r->codes || !r->id_begin || !r->id_end ||
+        !r->seq_off)
+        return fail(ctx, GBA_ECAPACITY, "records need %lld record and %lld residue entries", (long long)nrec + 1,
+                    (long long)nres);
+    const size_t idx_bytes = (size_t(nrec) + 1) * 8;
+    GBA_CUDA(ctx, ctx->fa_out.ensure(size_t(nres) + 3 * idx_bytes + 64));
+    char *o = ctx->fa_out.as<char>();
+    a.id_begin = reinterpret_cast<int64_t *>(o);
+    a.id_end = reinterpret_cast<int64_t *>(o + idx_bytes);
+    a.seq_off = reinterpret_cast<int64_t *>(o + 2 * idx_bytes);
+    a.codes = reinterpret_cast<uint8_t *>(o + 3 * idx_bytes);
+    a.error = reinterpret_cast<unsigned long long *>(ctx->fa_tmp.ptr);
+    a.bounds = reinterpret_cast<unsigned int *>(ctx->fa_tmp.as<char>() + 8);
+    a.nrec = nrec;
+    a.nres = nres;
+    GBA_CUDA(ctx, cudaMemsetAsync(a.error, 0xff, 8, st));
+    GBA_CUDA(ctx, cudaMemsetAsync(a.bounds, 0, 4, st));
+    k_fasta_write<<<unsigned(blocks), kFaThreads, 0, st>>>(a);
+    GBA_CUDA(ctx, cudaGetLastError());
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
+    unsigned long long err = 0;
+    unsigned int bounds = 0;
+    GBA_CUDA(ctx, cudaMemcpyAsync(&err, a.error, 8, cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(&bounds, a.bounds, 4, cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(r->id_begin, a.id_begin, size_t(nrec) * 8, cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(r->id_end, a.id_end, size_t(nrec) * 8, cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(r->seq_off, a.seq_off, size_t(nrec) * 8, cudaMemcpyDeviceToHost, st));
+    if (nres) GBA_CUDA(ctx, cudaMemcpyAsync(r->codes, a.codes, size_t(nres), cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
+    GBA_CUDA(ctx, cudaStreamSynchronize(st));
+    r->seq_off[nrec] = nres;
+    if (total.end[FA_BEFORE] == FA_HEADER) r->id_end[nrec - 1] = n;   // last header runs to the end
+    if (r->qual_end)
+        for (int64_t k = 0; k < nrec; ++k) r->qual_end[k] = r->seq_off[k];
+    float ms = 0, call = 0;
+    GBA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+    GBA_CUDA(ctx, cudaEventElapsedTime(&call, ctx->ev[0], ctx->ev[1]));
+    ctx->stats = gba_stats{};
+    ctx->stats.dp_kernel_ms = ms;
+    ctx->stats.call_ms = call;
+    ctx->stats.kernel_launches = 3;
+    if (bounds) return fail(ctx, GBA_ECUDA, "FASTA record pass wrote outside the scanned totals (%u)", bounds);
+    if (err != ~0ull) {
+        r->error_offset = int64_t(err);
+        return fail(ctx, GBA_EPARSE, "character outside the alphabet at offset %lld", (long long)err);
+    }
+    return GBA_OK;
+}
+
+GBA_API int gba_read_fastq(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r)
+{
+    using namespace gba;
+    int8_t cls[256];
+    {
+        const int rc = seqio_check(ctx, text, n, alphabet, r, cls);
+        if (rc) return rc;
+    }
+    cls[uint8_t('>')] = FA_BAD;
+    auto err = [&](int status, int64_t at, const char *what) {
+        r->error_offset = at;
+        return ctx ? fail(ctx, status, "%s at offset %lld", what, (long long)at) : status;
+    };
+    const uint8_t *t = reinterpret_cast<const uint8_t *>(text);
+    const int64_t rcap = r->record_capacity, qcap = r->residue_capacity;
+    const bool write = r->codes && r->id_begin && r->id_end && r->seq_off;
+    int64_t p = 0, rec = 0, res = 0;
+    auto nl = [](uint8_t c) { return c == '\n' || c == '\r'; };
+    auto ws = [](uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; };
+    while (p < n) {
+        const void *at = memchr(t + p, '@', size_t(n - p));   // skipUntil '@'
+        if (!at) return err(GBA_EPARSE, n, "no '@' record start before the end");
+        p = static_cast<const uint8_t *>(at) - t + 1;
+        const int64_t ib = p;                                  // readLine(id)
+        while (p < n && !nl(t[p])) ++p;
+        const int64_t ie = p;
+        if (p < n && t[p] == '\r') ++p;
+        if (p < n && t[p] == '\n') ++p;
+        const int64_t sb = res;
+        for (; p < n && t[p] != '+'; ++p) {                    // readUntil(seq, '+')
+            const int k = cls[t[p]];
+            if (k == FA_WS || k == FA_NL) continue;
+            if (k < 0) return err(GBA_EPARSE, p, "character outside the alphabet");
+            if (write && res < qcap) r->codes[res] = uint8_t(k);
+            ++res;
+        }
+        if (p >= n) return err(GBA_EPARSE, n, "no '+' line before the end");
+        ++p;
+        while (p < n && !nl(t[p])) ++p;                        // skipLine
+        if (p < n && t[p] == '\r') ++p;
+        if (p < n && t[p] == '\n') ++p;
+        int64_t need = res - sb, qe = sb;
+        for (; p < n && need > 0; ++p) {                       // counted qualities
+            if (nl(t[p])) continue;
+            if (write && r->quals && qe < qcap) r->quals[qe] = char(t[p]);
+            ++qe;
+            --need;
+        }
+        while (p < n && ws(t[p])) ++p;
+        if (p < n && t[p] != '@' && t[p] != 0xFF)
+            return err(GBA_EPARSE, p, "quality string not as long as the sequence");
+        if (write && rec < rcap) {
+            r->id_begin[rec] = ib;
+            r->id_end[rec] = ie;
+            r->seq_off[rec] = sb;
+            if (r->qual_end) r->qual_end[rec] = qe;
+        }
+        ++rec;
+    }
+    r->num = rec;
+    r->residues = res;
+    if (!write || rec + 1 > rcap || res > qcap) {
+        return ctx ? fail(ctx, GBA_ECAPACITY, "records need %lld record and %lld residue entries",
+                          (long long)rec + 1, (long long)res)
+                   : GBA_ECAPACITY;
+    }
+    r->seq_off[rec] = res;
+    return GBA_OK;
+}
+
+}  // extern "C"

@@ -179,3 +179,30 @@ def serving_lengths(n: int, seed: int = 5):
     lens = np.where(u < 0.90, rng.integers(100, 501, size=n),
                     np.where(u < 0.99, rng.integers(1000, 5001, size=n), 10_000))
     return lens
+
+
+def records_text(seqs, fmt: str = "fasta", letters: str = "ACGTN", width: int = 0, seed: int = 0,
+                 lowercase: float = 0.0, crlf: bool = False, id_prefix: str = "read") -> bytes:
+    """FASTA or FASTQ text of code arrays: ids "<id_prefix><k> ...", sequences wrapped at `width`
+    columns (0: one line) with a fraction `lowercase` of lower-case letters, FASTQ qualities of the
+    sequence's length on one line, '\\n' or '\\r\\n' line ends."""
+    rng = _rng(seed)
+    nl = b"\r\n" if crlf else b"\n"
+    lut_up = np.frombuffer(letters.encode(), np.uint8)
+    lut_lo = np.frombuffer(letters.lower().encode(), np.uint8)
+    parts = []
+    for k, s in enumerate(seqs):
+        s = np.asarray(s, np.uint8)
+        chars = lut_up[s]
+        if lowercase:
+            low = rng.random(len(s)) < lowercase
+            chars = np.where(low, lut_lo[s], chars)
+        body = chars.tobytes()
+        if width and len(body) > width:
+            body = nl.join(body[i:i + width] for i in range(0, len(body), width))
+        if fmt == "fasta":
+            parts.append(b">%s%d len=%d" % (id_prefix.encode(), k, len(s)) + nl + body + nl)
+        else:
+            qual = (rng.integers(33, 74, len(s)).astype(np.uint8)).tobytes()
+            parts.append(b"@%s%d" % (id_prefix.encode(), k) + nl + body + nl + b"+" + nl + qual + nl)
+    return b"".join(parts)

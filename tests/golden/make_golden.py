@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|packed|sam]
+    python tests/golden/make_golden.py [--only seeds|extend|packed|sam|seqio]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -99,6 +99,9 @@ def main():
         return
     if only == "sam":
         write_sam_cases()
+        return
+    if only == "seqio":
+        write_seqio()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -441,6 +444,81 @@ def seed_cases(b62):
         add(O.SeedProblem(O.GAPPED_XDROP, direction, 1, -1, -1, 3), H, V, seeds, pos)
         add(O.SeedProblem(O.MATCH_EXTEND, direction), H, V, seeds, pos)
     return out
+
+
+
+# FASTA / FASTQ: the reference's readRecord loop (oracle/ref/units/seqio.cpp) on the reference's own
+# seq_io test files, hand-made edge cases and seeded random texts.
+SEQIO_LETTERS = {"dna5": "ACGTNacgtn", "dna": "ACGTacgt", "aa": "ACDEFGHIKLMNPQRSTVWYXBZJOU*acdx"}
+SEQIO_EDGE = [
+    ("fasta", b""), ("fasta", b"  \n"), ("fasta", b">"), ("fasta", b">id only"), ("fasta", b">a\r\nAC GT\n\nNN>b c>d\rAC\n"),
+    ("fasta", b"junk XX\n>x\nACGT\n"), ("fasta", b">x\nAC\n>y\n"), ("fasta", b">x\nACGU\n"), ("fasta", b">x\nac\tgt\r\n"),
+    ("fasta", b">x y\n\n\nACGT\n\n>z\n\n"), ("fasta", b">>>\n>\n>"), ("fasta", b"\xff>x\nA\xffC\n"),
+    ("fastq", b""), ("fastq", b"@r1\nACGT\n+\nIIII\n@r2\nAC\nGT\n+r2\nII\nI@\n"), ("fastq", b"@r\nACGT\n+\nII\n"),
+    ("fastq", b"@r\nAC\n+\nI I\n"), ("fastq", b"@r\nAC\n+\nII\n\n  @s\n\n+\n"), ("fastq", b"@r\nAC\n+\nIIX\n"),
+    ("fastq", b"@r\nAC"), ("fastq", b"@r\nAC\n+"), ("fastq", b"  "), ("fastq", b"@r\r\nAC\r\n+\r\n@@\r\n"),
+    ("fastq", b"@r\nA>C\n+\nII\n"), ("fastq", b"@r\nAC\n+\nII\xff"), ("fastq", b"x@r\n\n+\n@s\nA\n+\n+\n"),
+]
+
+
+def seqio_random_text(rng, fmt, alphabet):
+    letters = SEQIO_LETTERS[alphabet]
+    pick = lambda s: s[int(rng.integers(len(s)))]
+    parts = []
+    for _ in range(int(rng.integers(0, 6))):
+        if fmt == "fasta":
+            parts.append(">" + "".join(pick("ab >\t") for _ in range(int(rng.integers(0, 7)))) +
+                         pick(["\n", "\r\n", "\r", ""]))
+            out = []
+            for _ in range(int(rng.integers(0, 40))):
+                out.append(pick(letters))
+                if rng.random() < 0.15:
+                    out.append(pick(["\n", "\r\n", " ", "\t"]))
+            parts.append("".join(out))
+        else:
+            parts.append("@" + "".join(pick("ab @+") for _ in range(int(rng.integers(0, 5)))) + pick(["\n", "\r\n"]))
+            L = int(rng.integers(0, 20))
+            seq = "".join(pick(letters) for _ in range(L))
+            parts.append(seq + pick(["\n", "\r\n"]) + "+" + pick(["", "x"]) + "\n")
+            q = "".join(pick("I#@+ !") for _ in range(max(0, L + pick([0, 0, 0, 1, -1]))))
+            parts.append(q + pick(["\n", "\n\n", "\r\n", ""]))
+    t = "".join(parts)
+    if rng.random() < 0.2 and t:
+        i = int(rng.integers(len(t)))
+        t = t[:i] + pick(" \t\r\n>@+X-1\xff") + t[i:]
+    return t.encode("latin1")
+
+
+def write_seqio():
+    import base64
+    rng = np.random.Generator(np.random.PCG64(20261208))
+    texts = []
+    for name, fmt in (("test_dna.fa", "fasta"), ("test_dna.fq", "fastq"), ("adeno_genome.fa", "fasta")):
+        with open(os.path.join(REFERENCE, "tests", "seq_io", name), "rb") as f:
+            data = f.read()
+        for alph in ("dna5", "dna", "aa"):
+            texts.append((f"tests/seq_io/{name}", fmt, alph, data))
+    for k, (fmt, t) in enumerate(SEQIO_EDGE):
+        for alph in ("dna5", "dna", "aa"):
+            texts.append((f"edge {k}", fmt, alph, t))
+    for k in range(360):
+        fmt = ("fasta", "fastq")[k % 2]
+        alph = ("dna5", "dna", "aa")[(k // 2) % 3]
+        texts.append((f"random {k}", fmt, alph, seqio_random_text(rng, fmt, alph)))
+    cases = []
+    for src, fmt, alph, t in texts:
+        case = {"source": src, "format": fmt, "alphabet": alph, "text": base64.b64encode(t).decode()}
+        try:
+            recs = O.ref_read_records(t, fmt, alph)
+            case["records"] = [[i.decode("latin1"), c.tolist(), q.decode("latin1")] for i, c, q in recs]
+        except O.SeqParseError as e:
+            case["error"] = e.kind
+        cases.append(case)
+    tables = {a: O.ref_char_table(a).tolist() for a in ("dna5", "dna", "aa")}
+    with open(os.path.join(HERE, "seqio_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only seqio", "seed": 20261208, "char_tables": tables,
+                   "cases": cases}, f, separators=(",", ":"))
+    print(f"{len(cases)} FASTA/FASTQ cases written ({sum('error' in c for c in cases)} errors)")
 
 
 if __name__ == "__main__":

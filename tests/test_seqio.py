@@ -1,0 +1,123 @@
+"""FASTA / FASTQ records (CPU): the oracle's restatement of the reference's readRecord loop and the
+engine's host FASTQ reader (gba_read_fastq, no GPU), against readRecord outputs of the compiled
+reference (tests/golden/seqio_cases.json: the reference's seq_io test files, edge cases, seeded
+random texts) and the reference's IsInAlphabet tables."""
+import base64
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import golden_cases as G
+
+SEQIO = G.load("seqio_cases.json")
+CASES = SEQIO["cases"]
+
+
+def expected(c):
+    return [(i.encode("latin1"), np.asarray(s, np.uint8), q.encode("latin1")) for i, s, q in c["records"]]
+
+
+def same(got, want):
+    return len(got) == len(want) and all(a[0] == b[0] and np.array_equal(a[1], b[1]) and a[2] == b[2]
+                                         for a, b in zip(got, want))
+
+
+def test_fixtures_cover_the_formats_and_errors():
+    assert {(c["format"], c["alphabet"]) for c in CASES} == {(f, a) for f in ("fasta", "fastq")
+                                                            for a in ("dna5", "dna", "aa")}
+    assert any(c.get("error") == "parse" for c in CASES) and any(c.get("error") == "end" for c in CASES)
+    assert any(c["source"].startswith("tests/seq_io/") and "records" in c for c in CASES)
+
+
+@pytest.mark.parametrize("chunk", range(0, len(CASES), 150))
+def test_oracle_matches_reference_fixtures(chunk):
+    for c in CASES[chunk:chunk + 150]:
+        text = base64.b64decode(c["text"])
+        if "error" in c:
+            with pytest.raises(O.SeqParseError) as e:
+                O.oracle_read_records(text, c["format"], c["alphabet"])
+            assert e.value.kind == c["error"], c["source"]
+        else:
+            assert same(O.oracle_read_records(text, c["format"], c["alphabet"]), expected(c)), c["source"]
+
+
+@pytest.mark.parametrize("alphabet", ["dna5", "dna", "aa"])
+def test_oracle_alphabet_matches_reference_tables(alphabet):
+    """Every byte value as a one-residue FASTA sequence: its code where the reference's
+    IsInAlphabet accepts it, skipped as whitespace, a new record for '>', else ParseError."""
+    table = SEQIO["char_tables"][alphabet]
+    for c in range(256):
+        text = b">x\n" + bytes([c])
+        if c in b" \t\r\n":
+            assert len(O.oracle_read_records(text, "fasta", alphabet)[0][1]) == 0
+        elif c == ord(">"):
+            assert len(O.oracle_read_records(text, "fasta", alphabet)) == 2
+        elif table[c] >= 0:
+            assert O.oracle_read_records(text, "fasta", alphabet)[0][1].tolist() == [table[c]], c
+        else:
+            with pytest.raises(O.SeqParseError):
+                O.oracle_read_records(text, "fasta", alphabet)
+
+
+def test_fastq_host_reader_matches_reference_fixtures():
+    from seqan_gb300 import _native
+    from seqan_gb300 import seq_io as S
+    _native.build()
+    for c in CASES:
+        if c["format"] != "fastq":
+            continue
+        text = base64.b64decode(c["text"])
+        if "error" in c:
+            with pytest.raises(S.SeqParseError):
+                S.read_fastq(text, c["alphabet"])
+        else:
+            rec = S.read_fastq(text, c["alphabet"])
+            assert same(list(zip(rec.ids, rec.seqs, rec.quals_list)), expected(c)), c["source"]
+
+
+def test_fastq_host_reader_error_offsets_match_oracle():
+    from seqan_gb300 import _native
+    from seqan_gb300 import seq_io as S
+    _native.build()
+    for c in CASES:
+        if c["format"] != "fastq" or "error" not in c:
+            continue
+        text = base64.b64decode(c["text"])
+        with pytest.raises(O.SeqParseError) as want:
+            O.oracle_read_records(text, "fastq", c["alphabet"])
+        with pytest.raises(S.SeqParseError) as got:
+            S.read_fastq(text, c["alphabet"])
+        assert got.value.offset == want.value.offset, c["source"]
+
+
+def test_fastq_host_reader_capacity_and_arguments():
+    import ctypes as C
+    from seqan_gb300 import _native as N
+    N.build()
+    text = b"@r1\nACGT\n+\nIIII\n@r2\nAC\n+\n!!\n"
+    r = N.GbaSeqRecords(1, 2, None, None, None, None, None, None, 0, 0, -1)
+    buf = np.frombuffer(text, np.uint8)
+    assert N.lib().gba_read_fastq(None, buf.ctypes.data, len(text), 5, C.byref(r)) == N.GBA_ECAPACITY
+    assert (r.num, r.residues) == (2, 6)
+    assert N.lib().gba_read_fastq(None, buf.ctypes.data, len(text), 7, C.byref(r)) == N.GBA_EINVAL
+    assert N.lib().gba_read_fastq(None, None, 5, 5, C.byref(r)) == N.GBA_EINVAL
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="compiled reference not present")
+def test_oracle_matches_live_reference_random():
+    import sys
+    sys.path.insert(0, G.HERE)
+    import make_golden as MG
+    rng = np.random.Generator(np.random.PCG64(77))
+    for k in range(600):
+        fmt, alph = ("fasta", "fastq")[k % 2], ("dna5", "dna", "aa")[k % 3]
+        t = MG.seqio_random_text(rng, fmt, alph)
+        try:
+            want = O.ref_read_records(t, fmt, alph)
+        except O.SeqParseError as e:
+            with pytest.raises(O.SeqParseError) as got:
+                O.oracle_read_records(t, fmt, alph)
+            assert got.value.kind == e.kind
+            continue
+        assert same(O.oracle_read_records(t, fmt, alph), want), t
