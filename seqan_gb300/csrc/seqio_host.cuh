@@ -24,7 +24,7 @@ constexpr int kFaThreads = 128;    // threads per block: 16 KB of text per block
 enum : int8_t { FA_GT = -4, FA_NL = -3, FA_WS = -2, FA_BAD = -1 };
 enum : int32_t { FA_BEFORE = 0, FA_HEADER = 1, FA_SEQ = 2 };
 
-struct FaSum {
+struct alignas(16) FaSum {
     int64_t rec[3];   // records started in the chunk, per start state
     int64_t res[3];   // residues (valid or not) read in the chunk, per start state
     int32_t end[3];   // state after the chunk, per start state
@@ -76,24 +76,50 @@ struct FaArgs {
     unsigned int *bounds;        // set when a write falls outside them (skipped)
 };
 
-// Calls f(byte, i) for the 128 bytes of a chunk held in registers, in order (all indices
-// compile-time constants after unrolling, so the chunk stays in registers).
-template <typename F>
-__device__ __forceinline__ void fa_for_bytes(const uint4 (&w)[kFaChunk / 16], F &&f)
+// Byte classes of a 32-byte group as bit masks (bit i = byte i): '>' (g), '\n' or '\r' (l), residue
+// candidates (r: neither '>', a newline, ' ' nor '\t').  __vcmpeq4 compares four bytes at once;
+// the multiply gathers the low bit of each byte into four adjacent bits.
+struct FaMasks {
+    uint32_t g, l, r;
+};
+
+__device__ __forceinline__ uint32_t fa_bits4(uint32_t eq) { return ((eq & 0x01010101u) * 0x01020408u) >> 24; }
+
+__device__ __forceinline__ FaMasks fa_masks(const uint32_t (&x)[8])
 {
+    FaMasks m{0u, 0u, 0u};
 #pragma unroll
-    for (int j = 0; j < kFaChunk / 16; ++j) {
-        const uint32_t xs[4] = {w[j].x, w[j].y, w[j].z, w[j].w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            uint32_t x = xs[q];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                f(x & 0xffu, j * 16 + q * 4 + b);
-                x >>= 8;
-            }
-        }
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t g = __vcmpeq4(x[q], 0x3e3e3e3eu);
+        const uint32_t l = __vcmpeq4(x[q], 0x0a0a0a0au) | __vcmpeq4(x[q], 0x0d0d0d0du);
+        const uint32_t w = l | __vcmpeq4(x[q], 0x20202020u) | __vcmpeq4(x[q], 0x09090909u);
+        m.g |= fa_bits4(g) << (4 * q);
+        m.l |= fa_bits4(l) << (4 * q);
+        m.r |= fa_bits4(~(g | w)) << (4 * q);
     }
+    return m;
+}
+
+// Header state after each byte of a group, all 32 at once.  Header-or-not is a set ('>') / reset
+// (newline) flip-flop.  In each run of non-newline bytes the state is "not header" from the run's
+// start up to its first '>' (or the whole run): adding one at every run start to the run's
+// non-'>' bytes carries through exactly those bytes, which the sum clears.  A run that starts the
+// group inherits hdr_in, so it gets no carry when hdr_in is set.
+__device__ __forceinline__ uint32_t fa_after(uint32_t g, uint32_t l, bool hdr_in)
+{
+    const uint32_t z = ~l;
+    const uint32_t m = z & ~g;
+    uint32_t starts = z & ~(z << 1);
+    if (hdr_in) starts &= ~1u;
+    const uint32_t not_yet = m & ~(m + starts);
+    return z & ~not_yet;
+}
+
+__device__ __forceinline__ void fa_group_words(const uint4 (&w)[kFaChunk / 16], int grp, uint32_t (&x)[8])
+{
+    const uint4 a = w[2 * grp], b = w[2 * grp + 1];
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+    x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
 }
 
 // The SEQUENCE run over one byte, without branches: '>' starts a record outside a header, a
@@ -114,6 +140,27 @@ struct FaRun {
         rec += (g && !hdr) ? 1 : 0;
         res += (r && !hdr) ? 1 : 0;
         hdr = g || (hdr && !l);
+    }
+    // The same run over a 32-byte group given as masks.
+    __device__ __forceinline__ void group(const FaMasks &m)
+    {
+        const uint32_t after = fa_after(m.g, m.l, hdr);
+        const uint32_t before = (after << 1) | (hdr ? 1u : 0u);
+        const uint32_t starts = m.g & ~before, counted = m.r & ~before;
+        if (!seen_gt && m.g) {
+            const uint32_t below = (1u << (__ffs(m.g) - 1)) - 1u;
+            gt_res = res + __popc(counted & below);
+            seen_gt = true;
+        }
+        if (!seen_nl && m.l) {
+            const uint32_t below = (1u << (__ffs(m.l) - 1)) - 1u;
+            nl_rec = rec + __popc(starts & below);
+            nl_res = res + __popc(counted & below);
+            seen_nl = true;
+        }
+        rec += __popc(starts);
+        res += __popc(counted);
+        hdr = (after >> 31) != 0;
     }
     __device__ __forceinline__ FaSum summary() const
     {
@@ -146,7 +193,12 @@ __device__ __forceinline__ FaSum fa_summary_at(const uint8_t *text, int64_t n, i
         const uint4 *src = reinterpret_cast<const uint4 *>(text + base);
 #pragma unroll
         for (int i = 0; i < kFaChunk / 16; ++i) w[i] = __ldg(src + i);
-        fa_for_bytes(w, [&](uint32_t c, int) { run.step(c); });
+#pragma unroll
+        for (int grp = 0; grp < kFaChunk / 32; ++grp) {
+            uint32_t x[8];
+            fa_group_words(w, grp, x);
+            run.group(fa_masks(x));
+        }
     } else {
         for (int64_t i = base; i < n; ++i) run.step(text[i]);
     }
@@ -181,6 +233,7 @@ struct FaWriter {
     unsigned int *bounds;
     int s;
     int64_t rec, res;
+    int64_t first_bad;   // first byte outside the alphabet seen by the bit path, or -1
     __device__ __forceinline__ void step(uint32_t c, int64_t pos)
     {
         const int k = cls[c];
@@ -211,6 +264,65 @@ struct FaWriter {
     }
 };
 
+// The record pass over a full 32-byte group at text offset pos0: record starts and header ends
+// (rare) by walking their bits, residue codes into the staging buffer with the group's bytes at
+// compile-time positions.
+__device__ __forceinline__ void fa_write_group(FaWriter &wr, const uint32_t (&x)[8], int64_t pos0)
+{
+    const FaMasks m = fa_masks(x);
+    const bool hdr = wr.s == FA_HEADER;
+    const uint32_t after = fa_after(m.g, m.l, hdr);
+    const uint32_t before = (after << 1) | (hdr ? 1u : 0u);
+    uint32_t counted = m.r & ~before;
+    const uint32_t starts = m.g & ~before, ends = m.l & before;
+    bool still_before = false;
+    if (wr.s == FA_BEFORE) {   // nothing counts before the text's first '>'
+        counted &= m.g ? ~((1u << (__ffs(m.g) - 1)) - 1u) : 0u;
+        still_before = m.g == 0;
+    }
+    for (uint32_t ev = starts | ends; ev; ev &= ev - 1) {
+        const int i = __ffs(ev) - 1;
+        const int64_t pos = pos0 + i;
+        if ((starts >> i) & 1u) {
+            ++wr.rec;
+            if (wr.rec >= 0 && wr.rec < wr.nrec) {
+                wr.id_begin[wr.rec] = pos + 1;
+                wr.seq_off[wr.rec] = wr.res + __popc(counted & ((1u << i) - 1u));
+            } else {
+                atomicOr(wr.bounds, 1u);
+            }
+        } else {
+            if (wr.rec >= 0 && wr.rec < wr.nrec) wr.id_end[wr.rec] = pos;
+            else atomicOr(wr.bounds, 1u);
+        }
+    }
+    const int cnt = __popc(counted);
+    int64_t o = wr.res - wr.stage_base;
+    if (o < 0 || o + cnt > kFaThreads * kFaChunk || wr.res + cnt > wr.nres) {
+        if (cnt) atomicOr(wr.bounds, 2u);
+    } else {
+        // Predicated per byte: the store and the advance only for counted bytes; the first byte
+        // outside the alphabet is kept in a register (one atomic per chunk, by the caller).
+        uint32_t bad = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            uint32_t xq = x[q];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const bool take = (counted >> (4 * q + b)) & 1u;
+                const int k = wr.cls[xq & 0xffu];
+                if (take) wr.stage[o] = uint8_t(k < 0 ? 0 : k);
+                o += take ? 1 : 0;
+                bad |= (take && k == FA_BAD) ? (1u << (4 * q + b)) : 0u;
+                xq >>= 8;
+            }
+        }
+        if (bad && wr.first_bad < 0) wr.first_bad = pos0 + (__ffs(bad) - 1);
+    }
+    wr.res += cnt;
+    wr.s = still_before ? FA_BEFORE : ((after >> 31) ? FA_HEADER : FA_SEQ);
+}
+
 __global__ void __launch_bounds__(kFaThreads) k_fasta_write(FaArgs a)
 {
     using Scan = cub::BlockScan<FaSum, kFaThreads, cub::BLOCK_SCAN_WARP_SCANS>;
@@ -233,9 +345,15 @@ __global__ void __launch_bounds__(kFaThreads) k_fasta_write(FaArgs a)
         const int mid = blk.end[FA_BEFORE];
         FaWriter wr{cls, stage, blk_res, a.nrec, a.nres, a.id_begin, a.id_end, a.seq_off, a.error, a.bounds,
                     fa_pick(before.end, mid), blk.rec[FA_BEFORE] + fa_pick(before.rec, mid) - 1,
-                    blk_res + fa_pick(before.res, mid)};
+                    blk_res + fa_pick(before.res, mid), -1};
         if (full) {
-            fa_for_bytes(w, [&](uint32_t c, int i) { wr.step(c, base + i); });
+#pragma unroll
+            for (int grp = 0; grp < kFaChunk / 32; ++grp) {
+                uint32_t x[8];
+                fa_group_words(w, grp, x);
+                fa_write_group(wr, x, base + 32 * grp);
+            }
+            if (wr.first_bad >= 0) atomicMin(a.error, static_cast<unsigned long long>(wr.first_bad));
         } else {
             for (int64_t i = base; i < a.n; ++i) wr.step(a.text[i], i);
         }
