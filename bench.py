@@ -63,6 +63,116 @@ WORKLOADS["fasta_reads_2m"] = ("FASTA text of 2000000 reads of 150 bp (ids 'read
                                "columns, 3% lower case, 0.1% N), about 345 MB; readRecord loop into Dna5 codes + "
                                "record offsets")
 FASTA_WORKLOADS = {"fasta_reads_2m"}
+WORKLOADS["bam_records_1m"] = ("the 1000000 records of sam_records_1m as uncompressed BAM blocks "
+                               "(write(target, record, context, Bam()), no tags, no BGZF)")
+BAM_WORKLOADS = {"bam_records_1m"}
+
+
+def run_bam_bench(args, rank, world, local_rank, dist):
+    from seqan_gb300 import _native as N
+    from oracle import oracle as O
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    h = ctx.handle
+    n = args.pairs or 1_000_000
+    rec = make_sam_records(n, seed=21 + rank)
+    a = O.sam_arrays(rec)
+    pinned_bufs = {}
+    for key, arr in a.items():
+        p = C.c_void_p()
+        ctx.check(L.gba_host_alloc(h, C.byref(p), max(arr.nbytes, 1)), "alloc")
+        C.memmove(p, arr.ctypes.data, arr.nbytes)
+        pinned_bufs[key] = p
+    P = pinned_bufs
+    r = N.GbaSamRecords(n, P["qname"], P["qoff"], P["flag"], P["rid"], P["pos"], P["mapq"], P["cigar"], P["coff"],
+                        P["rnext"], P["pnext"], P["tlen"], P["seq"], P["soff"], P["letters"], P["qual"], P["quoff"],
+                        P["cnames"], P["cnoff"], len(rec.contigs))
+    rec_off = np.zeros(n + 1, np.int64)
+    L.gba_format_bam(h, C.byref(r), None, 0, rec_off.ctypes.data)
+    total = int(rec_off[-1])
+    p_out = C.c_void_p()
+    ctx.check(L.gba_host_alloc(h, C.byref(p_out), total + 16), "alloc")
+
+    def call():
+        ctx.check(L.gba_format_bam(h, C.byref(r), p_out, total + 16, rec_off.ctypes.data), "bam")
+
+    for _ in range(args.warmup):
+        call()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        wall.append(time.perf_counter() - t0)
+        kern.append(ctx.stats().dp_kernel_ms)
+    clocks = sampler.stop()
+    data = C.string_at(p_out, total)
+    threads = os.cpu_count() or 1
+    parity = data == O.oracle_write_bam_c(rec, threads=threads, arrays=a)
+    kernel_ms = sum(kern) / len(kern)
+    value = n * world / (kernel_ms * 1e-3) / 1e6
+    e2e = n * world * len(wall) / sum(wall) / 1e6
+    hbm = measured_hbm_gbs()
+    in_bytes = sum(int(x.nbytes) for x in a.values())
+    line = {"metric": "M BAM records/s, device formatting", "value": value, "unit": "M records/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "records": n,
+                       "bam_bytes": total, "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "M records/s", "h2d_bytes_per_step": in_bytes,
+                    "d2h_bytes_per_step": total + 8 * (n + 1), "ms_per_step": 1e3 * sum(wall) / len(wall)},
+            "gpu_launches": args.steps * 4,
+            "roofline": {"bound": "hbm", "achieved": (in_bytes + total) / (kernel_ms * 1e-3) / 1e9,
+                         "peak": hbm, "unit": "GB/s",
+                         "frac": ((in_bytes + total) / (kernel_ms * 1e-3) / 1e9 / hbm) if hbm else None,
+                         "traffic": None, "kernel": "k_bam_lengths + CUB scan + k_bam_write",
+                         "algorithmic_bytes": "record fields read once + BAM blocks written once",
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "clocks": clocks, "parity_vs_oracle": parity}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            O.oracle_write_bam_c(rec, threads=threads, arrays=a)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        line["cpu_baseline"] = {"value": n / best / 1e6, "unit": "M records/s", "cores": threads, "kind": "port",
+                                "sample": f"all {n} records, orc_write_bam (oracle/seqan_oracle.c, the reference's "
+                                          f"BAM writer restated) with OpenMP over {threads} threads, best of 2",
+                                "seconds": best}
+    for p in list(pinned_bufs.values()) + [p_out]:
+        L.gba_host_free(h, p)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_bam_reference(args):
+    from oracle import oracle as O
+    n = min(args.pairs or 1_000_000, 1_000_000)
+    rec = make_sam_records(n)
+    a = O.sam_arrays(rec)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.oracle_write_bam_c(rec, threads=threads, arrays=a)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.oracle_write_bam_c(rec, threads=threads, arrays=a)
+        times.append(time.perf_counter() - t0)
+    rate = n * len(times) / sum(times) / 1e6
+    print(json.dumps({"metric": "M BAM records/s, device formatting", "value": rate, "unit": "M records/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "u8", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload, "records_per_step": n,
+                                 "description": WORKLOADS[args.workload]},
+                      "cpu_baseline": {"value": rate, "unit": "M records/s", "cores": threads, "kind": "port",
+                                       "sample": f"{n} records per step, the reference's BAM writer restated in C "
+                                                 "(orc_write_bam), OpenMP"},
+                      "e2e": {"value": rate, "unit": "M records/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
 
 
 def fasta_reads_text(n, seed=3):
@@ -967,7 +1077,10 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
-        if args.workload in FASTA_WORKLOADS:
+        if args.workload in BAM_WORKLOADS:
+            if rank == 0:
+                run_bam_reference(args)
+        elif args.workload in FASTA_WORKLOADS:
             if rank == 0:
                 run_fasta_reference(args)
         elif args.workload in SAM_WORKLOADS:
@@ -991,6 +1104,11 @@ def main():
         return
     if args.workload in EXTEND_WORKLOADS:
         run_extend_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in BAM_WORKLOADS:
+        run_bam_bench(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
         return

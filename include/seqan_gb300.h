@@ -500,6 +500,16 @@ typedef struct {
     int64_t error_offset;      /* out: text offset of a GBA_EPARSE, else -1 */
 } gba_seq_records;
 
+/* BAM records of the same fields: write(target, record, context, Bam()) for a BamAlignmentRecord
+ * without tags (bam_io/write_bam.h:100-271), the uncompressed record blocks (block_size, the
+ * 32-byte core with bin = reg2bin(beginPos, beginPos + max(1, length in the reference)), name and
+ * NUL, CIGAR words, Iupac sequence two codes per byte, qualities minus '!' or 0xFF), formatted on
+ * the device; rec_off[num + 1] gets each record's byte offset.  Names of more than 254 characters,
+ * more than 65535 CIGAR operations and more qualities than residues are GBA_EINVAL (the core's
+ * fields cannot hold them; the reference asserts on the last).  BGZF compression is not done. */
+GBA_API int gba_format_bam(gba_context *ctx, const gba_sam_records *records, char *out, int64_t capacity,
+                           int64_t *rec_off);
+
 GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t length, int32_t alphabet,
                            gba_seq_records *records);
 GBA_API int gba_read_fastq(gba_context *ctx, const char *text, int64_t length, int32_t alphabet,

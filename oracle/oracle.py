@@ -693,3 +693,64 @@ def ref_char_table(alphabet: str):
     t = np.zeros(256, np.int16)
     lib.ref_char_table(C.c_int32(SEQIO_ALPHABETS[alphabet]), _ptr(t))
     return t
+
+
+# --- BAM records (bam_io/write_bam.h) ------------------------------------------------------------
+
+def oracle_write_bam_c(rec, threads: int = 0, arrays=None) -> bytes:
+    """The C restatement of the BAM record writer (OpenMP): the uncompressed record blocks."""
+    lib = liboracle()
+    lib.orc_write_bam.restype = C.c_int64
+    a = arrays or sam_arrays(rec)
+    n = len(rec.qname)
+    args = [C.c_int64(n), _ptr(a["qname"]), _ptr(a["qoff"]), _ptr(a["flag"]), _ptr(a["rid"]), _ptr(a["pos"]),
+            _ptr(a["mapq"]), _ptr(a["cigar"]), _ptr(a["coff"]), _ptr(a["rnext"]), _ptr(a["pnext"]), _ptr(a["tlen"]),
+            _ptr(a["seq"]), _ptr(a["soff"]), _ptr(a["letters"]), _ptr(a["qual"]), _ptr(a["quoff"])]
+    total = lib.orc_write_bam(*args, None, C.c_int64(0), C.c_int32(threads))
+    out = np.zeros(total + 1, np.uint8)
+    lib.orc_write_bam(*args, _ptr(out), C.c_int64(total + 1), C.c_int32(threads))
+    return bytes(out[:total])
+
+
+def ref_write_bam(rec) -> bytes:
+    """The reference's BAM writer on the same records (oracle/ref/units/bam.cpp)."""
+    lib = libref()
+    lib.ref_write_bam.restype = C.c_int64
+    n = len(rec.qname)
+    enc = lambda parts: [p.encode("latin1") for p in parts]
+    qn = enc(rec.qname)
+    qoff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in qn], out=qoff[1:])
+    cig = np.concatenate([np.asarray(c, np.uint32) for c in rec.cigar] + [np.zeros(1, np.uint32)])
+    coff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(c) for c in rec.cigar], out=coff[1:])
+    seqs = enc(["".join(rec.letters[int(x)] for x in s) for s in rec.seq])
+    soff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in seqs], out=soff[1:])
+    quals = enc(rec.qual if rec.qual is not None else [""] * n)
+    quoff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in quals], out=quoff[1:])
+    cn = enc(rec.contigs)
+    cnoff = np.zeros(len(cn) + 1, np.int64)
+    np.cumsum([len(x) for x in cn], out=cnoff[1:])
+    arr = lambda a, t: np.ascontiguousarray(a, t)
+    flag, rid, pos = arr(rec.flag, np.uint16), arr(rec.ref_id, np.int32), arr(rec.pos, np.int32)
+    mapq, rn, pn, tl = arr(rec.mapq, np.uint8), arr(rec.next_ref_id, np.int32), arr(rec.next_pos, np.int32), \
+        arr(rec.tlen, np.int32)
+    cap = int(qoff[-1] + 2 * soff[-1] + quoff[-1] + 40 * n + 4 * int(coff[-1]) + 64)
+    out = C.create_string_buffer(cap)
+    args = [C.c_int64(n), C.c_char_p(b"".join(qn) or b"\0"), _ptr(qoff), _ptr(flag), _ptr(rid), _ptr(pos),
+            _ptr(mapq), _ptr(cig), _ptr(coff), _ptr(rn), _ptr(pn), _ptr(tl), C.c_char_p(b"".join(seqs) or b"\0"),
+            _ptr(soff), C.c_char_p(b"".join(quals) or b"\0"), _ptr(quoff), C.c_int64(len(cn)),
+            C.c_char_p(b"".join(cn) or b"\0"), _ptr(cnoff), out, C.c_int64(cap)]
+    length = lib.ref_write_bam(*args)
+    assert length <= cap
+    return out.raw[:length]
+
+
+def ref_iupac_table():
+    """ordValue(Iupac(c)) of the reference for each of the 256 characters."""
+    lib = libref()
+    t = np.zeros(256, np.uint8)
+    lib.ref_iupac_table(_ptr(t))
+    return t

@@ -1184,3 +1184,97 @@ int32_t orc_read_records(int32_t format, int32_t alphabet, const char *text_, in
     seq_off[rec] = res;
     return 0;
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * BAM records: write(target, record, context, Bam()) for a BamAlignmentRecord without tags
+ * (bam_io/write_bam.h:100-271): block_size, the 32-byte core (rID, beginPos, l_qname | mapQ << 8 |
+ * bin << 16, n_cigar | flag << 16, l_qseq, rNextId, pNext, tLen), the name and a NUL, the CIGAR
+ * words, the sequence as Iupac codes two per byte (high nibble first), the qualities minus '!'
+ * (0xFF for the ones missing), all little-endian.  bin = reg2bin(beginPos, beginPos + max(1, l)) in
+ * uint32 arithmetic, l the CIGAR's length in the reference (every operation but S, H and I:
+ * bam_io/cigar.h:601-612), kept to its 16-bit field. */
+
+static uint8_t orc_iupac(unsigned char c)
+{
+    static const char iu[] = "=ACMGRSVTWYHKDBN";
+    const unsigned char u = (c >= 'a' && c <= 'z') ? (unsigned char)(c - 32) : c;
+    if (u == 'U') return 0;
+    for (int k = 0; k < 16; ++k)
+        if (iu[k] == (char)u) return (uint8_t)k;
+    return 15;
+}
+
+static uint32_t orc_reg2bin(uint32_t beg, uint32_t end)
+{
+    --end;
+    if (beg >> 14 == end >> 14) return 4681 + (beg >> 14);
+    if (beg >> 17 == end >> 17) return 585 + (beg >> 17);
+    if (beg >> 20 == end >> 20) return 73 + (beg >> 20);
+    if (beg >> 23 == end >> 23) return 9 + (beg >> 23);
+    if (beg >> 26 == end >> 26) return 1 + (beg >> 26);
+    return 0;
+}
+
+static void orc_put32(char *p, uint32_t v)
+{
+    p[0] = (char)(v & 0xff);
+    p[1] = (char)((v >> 8) & 0xff);
+    p[2] = (char)((v >> 16) & 0xff);
+    p[3] = (char)(v >> 24);
+}
+
+int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const uint16_t *flag, const int32_t *rid,
+                      const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
+                      const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
+                      const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
+                      char *out, int64_t cap, int32_t threads)
+{
+    int64_t k, total;
+    int64_t *off;
+    uint8_t iu[32];
+    if (n < 0) return -1;
+    if (threads <= 0) threads = omp_get_max_threads();
+    for (k = 0; k < 32; ++k) iu[k] = orc_iupac((unsigned char)letters[k]);
+    off = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n + 1));
+    off[0] = 0;
+    for (k = 0; k < n; ++k) {
+        const int64_t lq = qoff[k + 1] - qoff[k], nc = coff[k + 1] - coff[k], ls = soff[k + 1] - soff[k];
+        off[k + 1] = off[k] + 4 + 32 + lq + 1 + 4 * nc + (ls + 1) / 2 + ls;
+    }
+    total = off[n];
+    if (out && total <= cap) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (k = 0; k < n; ++k) {
+            char *p = out + off[k];
+            const int64_t lq = qoff[k + 1] - qoff[k], nc = coff[k + 1] - coff[k], ls = soff[k + 1] - soff[k];
+            const int64_t lqual = quoff ? quoff[k + 1] - quoff[k] : 0;
+            uint32_t l = 0, bin;
+            int64_t i;
+            for (i = coff[k]; i < coff[k + 1]; ++i) {
+                const uint32_t op = cigar[i] & 15u;
+                if (op != 1 && op != 4 && op != 5) l += cigar[i] >> 4;
+            }
+            bin = orc_reg2bin((uint32_t)pos[k], (uint32_t)pos[k] + (l > 1 ? l : 1u)) & 0xffffu;
+            orc_put32(p, (uint32_t)(32 + ((lq + 1) & 0xff) + 4 * (nc & 0xffff) + (ls + 1) / 2 + ls));
+            orc_put32(p + 4, (uint32_t)rid[k]);
+            orc_put32(p + 8, (uint32_t)pos[k]);
+            orc_put32(p + 12, (uint32_t)((lq + 1) & 0xff) | ((uint32_t)mapq[k] << 8) | (bin << 16));
+            orc_put32(p + 16, (uint32_t)(nc & 0xffff) | ((uint32_t)flag[k] << 16));
+            orc_put32(p + 20, (uint32_t)ls);
+            orc_put32(p + 24, (uint32_t)rnext[k]);
+            orc_put32(p + 28, (uint32_t)pnext[k]);
+            orc_put32(p + 32, (uint32_t)tlen[k]);
+            p += 36;
+            memcpy(p, qname + qoff[k], (size_t)lq);
+            p += lq;
+            *p++ = 0;
+            for (i = coff[k]; i < coff[k + 1]; ++i, p += 4) orc_put32(p, cigar[i]);
+            for (i = 0; i + 1 < ls; i += 2)
+                *p++ = (char)((iu[seq[soff[k] + i] & 31] << 4) | iu[seq[soff[k] + i + 1] & 31]);
+            if (ls & 1) *p++ = (char)(iu[seq[soff[k] + ls - 1] & 31] << 4);
+            for (i = 0; i < ls; ++i) *p++ = i < lqual ? (char)(qual[quoff[k] + i] - '!') : (char)0xff;
+        }
+    }
+    free(off);
+    return total;
+}

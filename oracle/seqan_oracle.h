@@ -125,6 +125,14 @@ int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const u
                       int64_t ncontigs, const char *cnames, const int64_t *cnoff, char *out, int64_t cap,
                       int32_t threads);
 
+/* BAM records of the same fields (bam_io/write_bam.h:100-271, no tags): the uncompressed record
+ * blocks.  Returns the byte length (the bytes are written when they fit cap), or -1. */
+int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const uint16_t *flag, const int32_t *rid,
+                      const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
+                      const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
+                      const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
+                      char *out, int64_t cap, int32_t threads);
+
 /* Records of FASTA (format 0) or FASTQ (format 1) text as the reference's readRecord loop reads
  * them (seq_io/fasta_fastq.h:265-283, :354-392), alphabet 4 Dna, 5 Dna5, 27 AminoAcid: record k's
  * id is text[id_begin[k], id_end[k]), its residues codes[seq_off[k], seq_off[k+1]), its qualities

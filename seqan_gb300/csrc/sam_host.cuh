@@ -165,18 +165,113 @@ __global__ void __launch_bounds__(128) k_sam_write(SamArgs a, const int64_t *lin
     if (lane == 0) p[0] = '\n';
 }
 
-}  // namespace gba
+// --- BAM: write(target, record, context, Bam()) without tags (bam_io/write_bam.h:100-271) --------
+// A record is block_size, the 32-byte core (rID, beginPos, l_qname | mapQ << 8 | bin << 16,
+// n_cigar | flag << 16, l_qseq, rNextId, pNext, tLen), the name and a NUL, the CIGAR words, the
+// sequence as Iupac codes two per byte (high nibble first), the qualities minus '!' (0xFF where
+// missing), little-endian.  bin = reg2bin(beginPos, beginPos + max(1, l)) in uint32 arithmetic,
+// l the CIGAR's length in the reference (operations other than S, H, I: bam_io/cigar.h:601-612),
+// kept to its 16-bit field.
 
-extern "C" {
+struct BamArgs {
+    SamArgs s;
+    uint8_t iupac[32];   // Iupac code of each residue code's letter
+};
 
-GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out, int64_t capacity, int64_t *line_off)
+__host__ __device__ __forceinline__ uint32_t bam_reg2bin(uint32_t beg, uint32_t end)
 {
-    if (!ctx || !r || !line_off) return GBA_EINVAL;
-    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    --end;
+    if (beg >> 14 == end >> 14) return 4681 + (beg >> 14);
+    if (beg >> 17 == end >> 17) return 585 + (beg >> 17);
+    if (beg >> 20 == end >> 20) return 73 + (beg >> 20);
+    if (beg >> 23 == end >> 23) return 9 + (beg >> 23);
+    if (beg >> 26 == end >> 26) return 1 + (beg >> 26);
+    return 0;
+}
+
+__device__ __forceinline__ void bam_put32(char *p, uint32_t v)
+{
+    p[0] = char(v & 0xffu);
+    p[1] = char((v >> 8) & 0xffu);
+    p[2] = char((v >> 16) & 0xffu);
+    p[3] = char(v >> 24);
+}
+
+__global__ void __launch_bounds__(128) k_bam_lengths(BamArgs b, int64_t *len)
+{
+    const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= b.s.num) return;
+    const int64_t lq = b.s.qname_off[k + 1] - b.s.qname_off[k];
+    const int64_t nc = b.s.cigar_off[k + 1] - b.s.cigar_off[k];
+    const int64_t ls = b.s.seq_off[k + 1] - b.s.seq_off[k];
+    len[k] = 36 + lq + 1 + 4 * nc + (ls + 1) / 2 + ls;
+}
+
+__global__ void __launch_bounds__(128) k_bam_write(BamArgs b, const int64_t *rec_off, char *out)
+{
+    __shared__ uint8_t iu[32];
+    if (threadIdx.x < 32) iu[threadIdx.x] = b.iupac[threadIdx.x];
+    __syncthreads();
+    const int64_t k = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= b.s.num) return;
+    char *p = out + rec_off[k];
+    const int64_t q0 = b.s.qname_off[k], lq = b.s.qname_off[k + 1] - q0;
+    const int64_t c0 = b.s.cigar_off[k], nc = b.s.cigar_off[k + 1] - c0;
+    const int64_t s0 = b.s.seq_off[k], ls = b.s.seq_off[k + 1] - s0;
+    const int64_t u0 = b.s.qual_off ? b.s.qual_off[k] : 0;
+    const int64_t lqual = b.s.qual_off ? b.s.qual_off[k + 1] - u0 : 0;
+    if (lane == 0) {
+        uint32_t l = 0;
+        for (int64_t i = c0; i < c0 + nc; ++i) {
+            const uint32_t op = b.s.cigar[i] & 15u;
+            if (op != 1u && op != 4u && op != 5u) l += b.s.cigar[i] >> 4;
+        }
+        const uint32_t beg = uint32_t(b.s.pos[k]);
+        const uint32_t bin = bam_reg2bin(beg, beg + (l > 1u ? l : 1u)) & 0xffffu;
+        bam_put32(p, uint32_t(32 + ((lq + 1) & 0xff) + 4 * (nc & 0xffff) + (ls + 1) / 2 + ls));
+        bam_put32(p + 4, uint32_t(b.s.ref_id[k]));
+        bam_put32(p + 8, beg);
+        bam_put32(p + 12, uint32_t((lq + 1) & 0xff) | (uint32_t(b.s.mapq[k]) << 8) | (bin << 16));
+        bam_put32(p + 16, uint32_t(nc & 0xffff) | (uint32_t(b.s.flag[k]) << 16));
+        bam_put32(p + 20, uint32_t(ls));
+        bam_put32(p + 24, uint32_t(b.s.next_ref_id[k]));
+        bam_put32(p + 28, uint32_t(b.s.next_pos[k]));
+        bam_put32(p + 32, uint32_t(b.s.tlen[k]));
+        p[36 + lq] = 0;
+    }
+    char *q = p + 36;
+    for (int64_t i = lane; i < lq; i += 32) q[i] = b.s.qname[q0 + i];
+    q += lq + 1;
+    for (int64_t i = lane; i < nc; i += 32) bam_put32(q + 4 * i, b.s.cigar[c0 + i]);
+    q += 4 * nc;
+    const int64_t pairs = (ls + 1) / 2;
+    for (int64_t j = lane; j < pairs; j += 32) {
+        const uint32_t hi = iu[b.s.seq[s0 + 2 * j] & 31u];
+        const uint32_t lo = 2 * j + 1 < ls ? iu[b.s.seq[s0 + 2 * j + 1] & 31u] : 0u;
+        q[j] = char((hi << 4) | lo);
+    }
+    q += pairs;
+    for (int64_t i = lane; i < ls; i += 32) q[i] = i < lqual ? char(b.s.qual[u0 + i] - '!') : char(0xff);
+}
+
+// ordValue(Iupac(c)): the position of the upper-cased letter in "=ACMGRSVTWYHKDBN", 'U' as '=',
+// anything else N (the reference's char-to-Iupac conversion).
+inline uint8_t bam_iupac(char c)
+{
+    static const char iu[] = "=ACMGRSVTWYHKDBN";
+    const char u = (c >= 'a' && c <= 'z') ? char(c - 32) : c;
+    if (u == 'U') return 0;
+    for (int k = 0; k < 16; ++k)
+        if (iu[k] == u) return uint8_t(k);
+    return 15;
+}
+
+// Validates the records and uploads their fields into one device buffer; a holds the device
+// pointers.  Shared by the SAM and BAM writers.
+inline int sam_upload(gba_context *ctx, const gba_sam_records *r, SamArgs &a)
+{
     const int64_t n = r->num;
-    if (n < 0) return fail(ctx, GBA_EINVAL, "negative record count");
-    line_off[0] = 0;
-    if (n == 0) return GBA_OK;
     if (!r->qname_off || !r->flag || !r->ref_id || !r->pos || !r->mapq || !r->cigar_off || !r->next_ref_id ||
         !r->next_pos || !r->tlen || !r->seq_off || !r->seq_letters || (r->num_contigs > 0 && !r->contig_off))
         return fail(ctx, GBA_EINVAL, "null record field");
@@ -218,7 +313,7 @@ GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out
     for (size_t i = 0; i < sizeof(ups) / sizeof(ups[0]); ++i)
         if (ups[i].bytes && ups[i].src)
             GBA_CUDA(ctx, cudaMemcpyAsync(base + at[i], ups[i].src, ups[i].bytes, cudaMemcpyHostToDevice, st));
-    SamArgs a{};
+    a = SamArgs{};
     a.num = n;
     a.qname = base + at[0];
     a.qname_off = reinterpret_cast<const int64_t *>(base + at[1]);
@@ -239,6 +334,24 @@ GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out
     a.cnames = base + at[16];
     a.cname_off = reinterpret_cast<const int64_t *>(base + at[17]);
     a.num_contigs = nc;
+    return GBA_OK;
+}
+
+}  // namespace gba
+
+extern "C" {
+
+GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out, int64_t capacity, int64_t *line_off)
+{
+    if (!ctx || !r || !line_off) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t n = r->num;
+    if (n < 0) return fail(ctx, GBA_EINVAL, "negative record count");
+    line_off[0] = 0;
+    if (n == 0) return GBA_OK;
+    SamArgs a{};
+    if (int rc = sam_upload(ctx, r, a)) return rc;
+    cudaStream_t st = ctx->stream;
     // lengths, offsets (exclusive scan), text
     GBA_CUDA(ctx, ctx->sam_len.ensure(size_t(n + 1) * 8 * 2));
     int64_t *len = ctx->sam_len.as<int64_t>();
@@ -257,6 +370,63 @@ GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out
     if (bytes > capacity || !out) return fail(ctx, GBA_ECAPACITY, "SAM text needs %lld bytes", (long long)bytes);
     GBA_CUDA(ctx, ctx->sam_out.ensure(size_t(bytes) + 16));
     k_sam_write<<<unsigned((n * 32 + 127) / 128), 128, 0, st>>>(a, off, ctx->sam_out.as<char>());
+    GBA_CUDA(ctx, cudaGetLastError());
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(out, ctx->sam_out.ptr, size_t(bytes), cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaStreamSynchronize(st));
+    float ms = 0;
+    GBA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+    ctx->stats = gba_stats{};
+    ctx->stats.dp_kernel_ms = ms;
+    ctx->stats.kernel_launches = 4;
+    return GBA_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+GBA_API int gba_format_bam(gba_context *ctx, const gba_sam_records *r, char *out, int64_t capacity, int64_t *rec_off)
+{
+    if (!ctx || !r || !rec_off) return GBA_EINVAL;
+    GBA_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int64_t n = r->num;
+    if (n < 0) return fail(ctx, GBA_EINVAL, "negative record count");
+    rec_off[0] = 0;
+    if (n == 0) return GBA_OK;
+    if (r->qname_off && r->cigar_off && r->seq_off) {
+        for (int64_t k = 0; k < n; ++k) {
+            // the core's l_qname (8 bits) and n_cigar (16 bits) fields; the reference's qualities
+            // may not outnumber the residues
+            if (r->qname_off[k + 1] - r->qname_off[k] > 254)
+                return fail(ctx, GBA_EINVAL, "record %lld: name longer than 254", (long long)k);
+            if (r->cigar_off[k + 1] - r->cigar_off[k] > 65535)
+                return fail(ctx, GBA_EINVAL, "record %lld: more than 65535 CIGAR operations", (long long)k);
+            if (r->qual_off && r->qual_off[k + 1] - r->qual_off[k] > r->seq_off[k + 1] - r->seq_off[k])
+                return fail(ctx, GBA_EINVAL, "record %lld: more qualities than residues", (long long)k);
+        }
+    }
+    BamArgs b{};
+    if (int rc = sam_upload(ctx, r, b.s)) return rc;
+    for (int c = 0; c < 32; ++c) b.iupac[c] = bam_iupac(r->seq_letters[c]);
+    cudaStream_t st = ctx->stream;
+    GBA_CUDA(ctx, ctx->sam_len.ensure(size_t(n + 1) * 8 * 2));
+    int64_t *len = ctx->sam_len.as<int64_t>();
+    int64_t *off = len + (n + 1);
+    GBA_CUDA(ctx, cudaMemsetAsync(len + n, 0, 8, st));
+    GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+    k_bam_lengths<<<unsigned((n + 127) / 128), 128, 0, st>>>(b, len);
+    GBA_CUDA(ctx, cudaGetLastError());
+    size_t tmp_bytes = 0;
+    GBA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, len, off, n + 1, st));
+    GBA_CUDA(ctx, ctx->sam_tmp.ensure(tmp_bytes + 16));
+    GBA_CUDA(ctx, cub::DeviceScan::ExclusiveSum(ctx->sam_tmp.ptr, tmp_bytes, len, off, n + 1, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(rec_off, off, size_t(n + 1) * 8, cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaStreamSynchronize(st));
+    const int64_t bytes = rec_off[n];
+    if (bytes > capacity || !out) return fail(ctx, GBA_ECAPACITY, "BAM records need %lld bytes", (long long)bytes);
+    GBA_CUDA(ctx, ctx->sam_out.ensure(size_t(bytes) + 16));
+    k_bam_write<<<unsigned((n * 32 + 127) / 128), 128, 0, st>>>(b, off, ctx->sam_out.as<char>());
     GBA_CUDA(ctx, cudaGetLastError());
     GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     GBA_CUDA(ctx, cudaMemcpyAsync(out, ctx->sam_out.ptr, size_t(bytes), cudaMemcpyDeviceToHost, st));

@@ -1,5 +1,6 @@
 """SAM output on the device (``gba_format_sam``): BamAlignmentRecord fields -> SAM lines as the
-reference's SAM writer writes them (bam_io/write_sam.h:126-217).
+reference's SAM writer writes them (bam_io/write_sam.h:126-217); ``gba_format_bam``: the same
+records as uncompressed BAM blocks (bam_io/write_bam.h:100-271).
 
 :class:`SamRecords` holds the fields as arrays (0-based positions, -1 for none, BAM-packed CIGARs
 as ``gba_result.cigar`` returns them); :func:`format_sam` returns the text.
@@ -44,6 +45,51 @@ class SamRecords:
     qual: list | None      # per record: str, or None for '*'
     contigs: list          # contig names
     letters: str = "ACGTN"
+
+
+def _records_struct(rec: SamRecords):
+    """The gba_sam_records of rec and the arrays it points into (kept alive by the caller)."""
+    n = len(rec.qname)
+    qn = [q.encode("latin1") for q in rec.qname]
+    qname, qoff = _cat([np.frombuffer(q, np.uint8) for q in qn], np.uint8), _off(qn)
+    cig, coff = _cat(rec.cigar, np.uint32), _off(rec.cigar)
+    seq, soff = _cat(rec.seq, np.uint8), _off(rec.seq)
+    letters = np.zeros(32, dtype=np.uint8)
+    letters[:len(rec.letters)] = np.frombuffer(rec.letters.encode(), np.uint8)
+    if rec.qual is not None:
+        qb = [q.encode("latin1") for q in rec.qual]
+        qual, quoff = _cat([np.frombuffer(q, np.uint8) for q in qb], np.uint8), _off(qb)
+    else:
+        qual = quoff = None
+    cb = [c.encode() for c in rec.contigs]
+    cnames, cnoff = _cat([np.frombuffer(c, np.uint8) for c in cb], np.uint8), _off(cb)
+    arrs = dict(flag=np.ascontiguousarray(rec.flag, np.uint16), ref_id=np.ascontiguousarray(rec.ref_id, np.int32),
+                pos=np.ascontiguousarray(rec.pos, np.int32), mapq=np.ascontiguousarray(rec.mapq, np.uint8),
+                next_ref_id=np.ascontiguousarray(rec.next_ref_id, np.int32),
+                next_pos=np.ascontiguousarray(rec.next_pos, np.int32), tlen=np.ascontiguousarray(rec.tlen, np.int32))
+    p = lambda a: None if a is None else a.ctypes.data
+    r = N.GbaSamRecords(n, p(qname), p(qoff), p(arrs["flag"]), p(arrs["ref_id"]), p(arrs["pos"]), p(arrs["mapq"]),
+                        p(cig), p(coff), p(arrs["next_ref_id"]), p(arrs["next_pos"]), p(arrs["tlen"]), p(seq),
+                        p(soff), p(letters), p(qual), p(quoff), p(cnames), p(cnoff), len(rec.contigs))
+    keep = [qname, qoff, cig, coff, seq, soff, letters, qual, quoff, cnames, cnoff, arrs]
+    return r, keep
+
+
+def format_bam(rec: SamRecords, ctx=None) -> bytes:
+    """The records' uncompressed BAM blocks as the reference's BAM writer writes them
+    (bam_io/write_bam.h:100-271, no tags), formatted on the device (gba_format_bam)."""
+    ctx = ctx or N.default_context()
+    n = len(rec.qname)
+    r, keep = _records_struct(rec)
+    rec_off = np.zeros(n + 1, dtype=np.int64)
+    rc = N.lib().gba_format_bam(ctx.handle, C.byref(r), None, 0, rec_off.ctypes.data)
+    if rc not in (N.GBA_OK, N.GBA_ECAPACITY):
+        ctx.check(rc, "gba_format_bam")
+    out = np.zeros(int(rec_off[-1]) + 1, dtype=np.uint8)
+    ctx.check(N.lib().gba_format_bam(ctx.handle, C.byref(r), out.ctypes.data, len(out), rec_off.ctypes.data),
+              "gba_format_bam")
+    del keep
+    return bytes(out[:int(rec_off[-1])])
 
 
 def format_sam(rec: SamRecords, ctx=None) -> str:

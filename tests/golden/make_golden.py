@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|packed|sam|seqio]
+    python tests/golden/make_golden.py [--only seeds|extend|packed|sam|seqio|bam]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -102,6 +102,9 @@ def main():
         return
     if only == "seqio":
         write_seqio()
+        return
+    if only == "bam":
+        write_bam_cases()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -519,6 +522,49 @@ def write_seqio():
         json.dump({"generator": "tests/golden/make_golden.py --only seqio", "seed": 20261208, "char_tables": tables,
                    "cases": cases}, f, separators=(",", ":"))
     print(f"{len(cases)} FASTA/FASTQ cases written ({sum('error' in c for c in cases)} errors)")
+
+
+
+def bam_records(rng):
+    """SAM fixture records plus the BAM writer's own cases: unmapped records at position -1,
+    positions on every bin level, qualities shorter than the sequence, odd lengths, every CIGAR
+    operation, and Iupac letters (lower case, 'U', characters outside the alphabet)."""
+    rec = sam_records(rng, 400)
+    n = len(rec.qname)
+    pos = rec.pos.copy()
+    edges = [-1, 0, 1, (1 << 14) - 1, 1 << 14, (1 << 17) - 3, 1 << 20, (1 << 23) + 5, (1 << 26) - 2, (1 << 29) - 7,
+             2_000_000_000]
+    for j, e in enumerate(edges):
+        pos[j * 7] = e
+    quals = list(rec.qual)
+    for k in range(0, n, 9):
+        quals[k] = quals[k][:len(rec.seq[k]) // 2]
+    cig = list(rec.cigar)
+    for k in range(3, n, 17):
+        cig[k] = [(int(rng.integers(1, 50)) << 4) | op for op in range(9)]
+    rec.pos, rec.qual, rec.cigar = pos, quals, cig
+    rec2 = sam_records(rng, 120)
+    rec2.letters = "=ACMGRSVTWYHKDBNacgtuUX*n-"
+    rec2.seq = [rng.integers(0, len(rec2.letters), len(s)).astype(np.uint8) for s in rec2.seq]
+    return rec, rec2
+
+
+def write_bam_cases():
+    import base64
+    rng = np.random.Generator(np.random.PCG64(20261209))
+    cases = []
+    for rec in bam_records(rng):
+        data = O.ref_write_bam(rec)
+        cases.append({"contigs": rec.contigs, "letters": rec.letters, "qname": rec.qname, "flag": rec.flag.tolist(),
+                      "ref_id": rec.ref_id.tolist(), "pos": rec.pos.tolist(), "mapq": rec.mapq.tolist(),
+                      "cigar": [list(map(int, c)) for c in rec.cigar], "next_ref_id": rec.next_ref_id.tolist(),
+                      "next_pos": rec.next_pos.tolist(), "tlen": rec.tlen.tolist(),
+                      "seq": [s.tolist() for s in rec.seq], "qual": rec.qual,
+                      "bam": base64.b64encode(data).decode()})
+    with open(os.path.join(HERE, "bam_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only bam", "seed": 20261209,
+                   "iupac": O.ref_iupac_table().tolist(), "cases": cases}, f, separators=(",", ":"))
+    print(f"{sum(len(c['qname']) for c in cases)} BAM records written")
 
 
 if __name__ == "__main__":
