@@ -8,7 +8,7 @@
 // (readUntil '>': whitespace skipped, every other byte a residue or a ParseError).  A '>' outside a
 // header starts a record; a newline ends a header.  Each thread summarises a 128-byte chunk for all
 // three start states at once (one pass: the BEFORE and HEADER runs join the SEQUENCE run at the
-// chunk's first '>' / first newline), a block scan and a one-block scan over the 16 KB blocks'
+// chunk's first '>' / first newline), a block scan and a two-level scan over the 16 KB blocks'
 // summaries compose them, and a second pass re-reads each chunk from its known state, record and residue
 // index to write codes and record bounds.
 //
@@ -20,6 +20,7 @@ namespace gba {
 
 constexpr int kFaChunk = 128;      // bytes per thread
 constexpr int kFaThreads = 128;    // threads per block: 16 KB of text per block
+constexpr int kFaTile = 256;       // block summaries per tile of the summary scan
 
 enum : int8_t { FA_GT = -4, FA_NL = -3, FA_WS = -2, FA_BAD = -1 };
 enum : int32_t { FA_BEFORE = 0, FA_HEADER = 1, FA_SEQ = 2 };
@@ -68,7 +69,8 @@ struct FaArgs {
     const uint8_t *text;
     int64_t n;
     int8_t cls[256];          // residue code, or FA_GT / FA_NL / FA_WS / FA_BAD
-    FaSum *block_sum;         // [blocks], inclusive-scanned in place between the two passes
+    FaSum *block_sum;         // [blocks]: after the scans, inclusive within tiles of kFaTile blocks
+    const FaSum *tile_sum;    // [tiles]: inclusive over the tiles
     uint8_t *codes;
     int64_t *id_begin, *id_end, *seq_off;
     unsigned long long *error;   // smallest offset of a ParseError byte
@@ -338,7 +340,11 @@ __global__ void __launch_bounds__(kFaThreads) k_fasta_write(FaArgs a)
     if (base < a.n) mine = fa_summary_at(a.text, a.n, base, w, full);
     FaSum before;
     Scan(tmp).ExclusiveScan(mine, before, fa_identity(), FaCompose());
-    const FaSum blk = blockIdx.x ? a.block_sum[blockIdx.x - 1] : fa_identity();
+    // Prefix of the blocks before this one: the tiles before this block's tile, then the blocks
+    // before it in its tile.
+    const unsigned tile = blockIdx.x / kFaTile;
+    const FaSum tile_before = tile ? a.tile_sum[tile - 1] : fa_identity();
+    const FaSum blk = blockIdx.x % kFaTile ? FaCompose()(tile_before, a.block_sum[blockIdx.x - 1]) : tile_before;
     const int64_t blk_res = blk.res[FA_BEFORE];
     if (base < a.n) {
         // State, records started and residues read before this chunk, from the start of the text.
@@ -360,24 +366,36 @@ __global__ void __launch_bounds__(kFaThreads) k_fasta_write(FaArgs a)
     }
     __syncthreads();
     // The block's residues are one contiguous range of the output: copy it out coalesced.
-    const int64_t cnt = a.block_sum[blockIdx.x].res[FA_BEFORE] - blk_res;
+    const int64_t cnt = FaCompose()(tile_before, a.block_sum[blockIdx.x]).res[FA_BEFORE] - blk_res;
     uint8_t *out = a.codes + blk_res;
     for (int64_t i = threadIdx.x; i < cnt && i < kFaThreads * kFaChunk && blk_res + i < a.nres; i += kFaThreads)
         out[i] = stage[i];
 }
 
-// Inclusive scan of the block summaries in place, one block: thread t composes the summaries
-// [t * per, min((t + 1) * per, nb)) in order, a block scan over the threads' aggregates gives each
-// thread its prefix, and the thread rewrites its range with running inclusive values.
-constexpr int kFaScanThreads = 1024;
-
-__global__ void __launch_bounds__(kFaScanThreads) k_fasta_scan_blocks(FaSum *sums, int64_t nb)
+// Scan of the block summaries in two levels.  k_fasta_scan_tiles: one block of kFaTile threads per
+// tile of kFaTile consecutive block summaries (coalesced loads, one summary per thread) rewrites them
+// as inclusive prefixes within the tile and writes the tile's total.  k_fasta_scan_top: one block
+// scans the tile totals in place (thread t composes a contiguous range, a block scan gives each
+// range its prefix).  The record pass composes the two.
+__global__ void __launch_bounds__(kFaTile) k_fasta_scan_tiles(FaSum *sums, int64_t nb, FaSum *tile_sum)
 {
-    using Scan = cub::BlockScan<FaSum, kFaScanThreads, cub::BLOCK_SCAN_WARP_SCANS>;
+    using Scan = cub::BlockScan<FaSum, kFaTile, cub::BLOCK_SCAN_WARP_SCANS>;
     __shared__ typename Scan::TempStorage tmp;
-    const int64_t per = (nb + kFaScanThreads - 1) / kFaScanThreads;
+    const int64_t i = int64_t(blockIdx.x) * kFaTile + threadIdx.x;
+    const FaSum mine = i < nb ? sums[i] : fa_identity();
+    FaSum incl;
+    Scan(tmp).InclusiveScan(mine, incl, FaCompose());
+    if (i < nb) sums[i] = incl;
+    if (threadIdx.x == kFaTile - 1) tile_sum[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(kFaTile) k_fasta_scan_top(FaSum *sums, int64_t nt)
+{
+    using Scan = cub::BlockScan<FaSum, kFaTile, cub::BLOCK_SCAN_WARP_SCANS>;
+    __shared__ typename Scan::TempStorage tmp;
+    const int64_t per = (nt + kFaTile - 1) / kFaTile;
     const int64_t lo = int64_t(threadIdx.x) * per;
-    const int64_t hi = lo + per < nb ? lo + per : nb;
+    const int64_t hi = lo + per < nt ? lo + per : nt;
     const FaCompose op;
     FaSum agg = fa_identity();
     for (int64_t i = lo; i < hi; ++i) agg = op(agg, sums[i]);
@@ -447,7 +465,8 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
     const int64_t blocks = (chunks + kFaThreads - 1) / kFaThreads;
     if (blocks > INT32_MAX) return fail(ctx, GBA_EINVAL, "text too long");
     GBA_CUDA(ctx, ctx->fa_text.ensure(size_t(n) + 16));
-    GBA_CUDA(ctx, ctx->fa_sum.ensure(size_t(blocks) * sizeof(FaSum) + 16));
+    const int64_t tiles = (blocks + kFaTile - 1) / kFaTile;
+    GBA_CUDA(ctx, ctx->fa_sum.ensure(size_t(blocks + tiles) * sizeof(FaSum) + 16));
     GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
     GBA_CUDA(ctx, cudaMemcpyAsync(ctx->fa_text.ptr, text, size_t(n), cudaMemcpyHostToDevice, st));
     a.text = ctx->fa_text.as<uint8_t>();
@@ -456,11 +475,15 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
     GBA_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
     k_fasta_summary<<<unsigned(blocks), kFaThreads, 0, st>>>(a.text, a.n, a.block_sum);
     GBA_CUDA(ctx, cudaGetLastError());
-    k_fasta_scan_blocks<<<1, kFaScanThreads, 0, st>>>(a.block_sum, blocks);
+    FaSum *tile_sum = a.block_sum + blocks;
+    a.tile_sum = tile_sum;
+    k_fasta_scan_tiles<<<unsigned(tiles), kFaTile, 0, st>>>(a.block_sum, blocks, tile_sum);
+    GBA_CUDA(ctx, cudaGetLastError());
+    k_fasta_scan_top<<<1, kFaTile, 0, st>>>(tile_sum, tiles);
     GBA_CUDA(ctx, cudaGetLastError());
     GBA_CUDA(ctx, ctx->fa_tmp.ensure(64));
     FaSum total;
-    GBA_CUDA(ctx, cudaMemcpyAsync(&total, a.block_sum + (blocks - 1), sizeof(FaSum), cudaMemcpyDeviceToHost, st));
+    GBA_CUDA(ctx, cudaMemcpyAsync(&total, tile_sum + (tiles - 1), sizeof(FaSum), cudaMemcpyDeviceToHost, st));
     GBA_CUDA(ctx, cudaStreamSynchronize(st));
     const int64_t nrec = total.rec[FA_BEFORE], nres = total.res[FA_BEFORE];
     r->num = nrec;
@@ -509,7 +532,7 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
     ctx->stats = gba_stats{};
     ctx->stats.dp_kernel_ms = ms;
     ctx->stats.call_ms = call;
-    ctx->stats.kernel_launches = 3;
+    ctx->stats.kernel_launches = 4;
     if (bounds) return fail(ctx, GBA_ECUDA, "FASTA record pass wrote outside the scanned totals (%u)", bounds);
     if (err != ~0ull) {
         r->error_offset = int64_t(err);
