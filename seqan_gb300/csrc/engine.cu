@@ -207,7 +207,7 @@ struct gba_context {
     bool device_codes = false;
     DevBuf pk_words, pk_off_h, pk_off_v;
     DevBuf sam_in, sam_len, sam_tmp, sam_out;   // gba_format_sam
-    DevBuf fa_text, fa_sum, fa_tmp, fa_out;     // gba_read_fasta
+    DevBuf fa_text, fa_sum, fa_tmp, fa_out, fa_chunk;   // gba_read_fasta
 };
 
 namespace {

@@ -10,7 +10,8 @@
 // three start states at once (one pass: the BEFORE and HEADER runs join the SEQUENCE run at the
 // chunk's first '>' / first newline), a block scan and a two-level scan over the 16 KB blocks'
 // summaries compose them, and a second pass re-reads each chunk from its known state, record and residue
-// index to write codes and record bounds.
+// index to write codes and record bounds (the first pass keeps each chunk's summary in one word, so
+// the second reads it back instead of recomputing it).
 //
 // FASTQ runs on the host: where a record ends depends on counting its quality characters from the
 // record's start ('@' is also a quality value), so the text does not split into independent chunks.
@@ -65,12 +66,39 @@ __host__ __device__ inline FaSum fa_identity()
     return r;
 }
 
+// A chunk's summary in one word: per start state 8 bits of records, 8 of residues (a chunk of 128
+// bytes holds at most 128 of either) and 2 of end state.
+__device__ __forceinline__ unsigned long long fa_pack(const FaSum &v)
+{
+    unsigned long long w = 0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s)
+        w |= (static_cast<unsigned long long>(v.rec[s]) | (static_cast<unsigned long long>(v.res[s]) << 8) |
+              (static_cast<unsigned long long>(v.end[s]) << 16)) << (18 * s);
+    return w;
+}
+
+__device__ __forceinline__ FaSum fa_unpack(unsigned long long w)
+{
+    FaSum v;
+    v.pad = 0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const unsigned long long f = w >> (18 * s);
+        v.rec[s] = int64_t(f & 0xffu);
+        v.res[s] = int64_t((f >> 8) & 0xffu);
+        v.end[s] = int32_t((f >> 16) & 3u);
+    }
+    return v;
+}
+
 struct FaArgs {
     const uint8_t *text;
     int64_t n;
     int8_t cls[256];          // residue code, or FA_GT / FA_NL / FA_WS / FA_BAD
     FaSum *block_sum;         // [blocks]: after the scans, inclusive within tiles of kFaTile blocks
     const FaSum *tile_sum;    // [tiles]: inclusive over the tiles
+    const unsigned long long *chunk_sum;   // [chunks]: each chunk's summary from the first pass
     uint8_t *codes;
     int64_t *id_begin, *id_end, *seq_off;
     unsigned long long *error;   // smallest offset of a ParseError byte
@@ -208,7 +236,8 @@ __device__ __forceinline__ FaSum fa_summary_at(const uint8_t *text, int64_t n, i
 }
 
 __global__ void __launch_bounds__(kFaThreads) k_fasta_summary(const uint8_t *__restrict__ text, int64_t n,
-                                                              FaSum *__restrict__ block_sum)
+                                                              FaSum *__restrict__ block_sum,
+                                                              unsigned long long *__restrict__ chunk_sum)
 {
     using Scan = cub::BlockScan<FaSum, kFaThreads, cub::BLOCK_SCAN_WARP_SCANS>;
     __shared__ typename Scan::TempStorage tmp;
@@ -218,6 +247,7 @@ __global__ void __launch_bounds__(kFaThreads) k_fasta_summary(const uint8_t *__r
         uint4 w[kFaChunk / 16];
         bool full;
         mine = fa_summary_at(text, n, base, w, full);
+        chunk_sum[int64_t(blockIdx.x) * kFaThreads + threadIdx.x] = fa_pack(mine);
     }
     FaSum incl;
     Scan(tmp).InclusiveScan(mine, incl, FaCompose());
@@ -335,9 +365,16 @@ __global__ void __launch_bounds__(kFaThreads) k_fasta_write(FaArgs a)
     __syncthreads();
     const int64_t base = (int64_t(blockIdx.x) * kFaThreads + threadIdx.x) * kFaChunk;
     uint4 w[kFaChunk / 16];
-    bool full = false;
+    const bool full = a.n - base >= kFaChunk;
     FaSum mine = fa_identity();
-    if (base < a.n) mine = fa_summary_at(a.text, a.n, base, w, full);
+    if (base < a.n) {
+        mine = fa_unpack(a.chunk_sum[int64_t(blockIdx.x) * kFaThreads + threadIdx.x]);
+        if (full) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(a.text + base);
+#pragma unroll
+            for (int i = 0; i < kFaChunk / 16; ++i) w[i] = __ldg(src + i);
+        }
+    }
     FaSum before;
     Scan(tmp).ExclusiveScan(mine, before, fa_identity(), FaCompose());
     // Prefix of the blocks before this one: the tiles before this block's tile, then the blocks
@@ -473,7 +510,10 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
     a.n = n;
     a.block_sum = ctx->fa_sum.as<FaSum>();
     GBA_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
-    k_fasta_summary<<<unsigned(blocks), kFaThreads, 0, st>>>(a.text, a.n, a.block_sum);
+    GBA_CUDA(ctx, ctx->fa_chunk.ensure(size_t(blocks) * kFaThreads * 8 + 16));
+    a.chunk_sum = ctx->fa_chunk.as<unsigned long long>();
+    k_fasta_summary<<<unsigned(blocks), kFaThreads, 0, st>>>(a.text, a.n, a.block_sum,
+                                                           ctx->fa_chunk.as<unsigned long long>());
     GBA_CUDA(ctx, cudaGetLastError());
     FaSum *tile_sum = a.block_sum + blocks;
     a.tile_sum = tile_sum;
