@@ -38,9 +38,13 @@
 #define SEQAN_GB300_SEQAN_H_
 
 #include <seqan/align.h>
+#include <seqan/bam_io.h>
 #include <seqan/seeds.h>
+#include <seqan/seq_io.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -589,6 +593,157 @@ void extendSeed(ExecutionPolicy<GB300, TVec> const &, String<Seed<Simple, TConfi
                                     gb300_impl::is_gapped<TXDropTag>::value ? GBA_GAPPED_XDROP
                                                                                 : GBA_UNGAPPED_XDROP,
                                     &sc, int(scoreDropOff));
+}
+
+// ---- FASTA / FASTQ input: readRecord loop of seq_io/fasta_fastq.h (:265-283, :354-392) ----------
+// readRecords(GB300, ids, seqs[, quals], text, Fasta() | Fastq()) reads every record of an
+// in-memory text as `while (!atEnd(iter)) readRecord(id, seq[, qual], iter, tag)` does, with seq a
+// String<Dna | Dna5 | AminoAcid>; ParseError / UnexpectedEnd are thrown where the reference throws
+// them.  FASTA is parsed on the device, FASTQ on the host.
+namespace gb300_impl {
+
+template <typename TAlph>
+struct ReaderAlphabet;
+template <>
+struct ReaderAlphabet<Dna> { static const int32_t VALUE = 4; };
+template <>
+struct ReaderAlphabet<Dna5> { static const int32_t VALUE = 5; };
+template <>
+struct ReaderAlphabet<AminoAcid> { static const int32_t VALUE = 27; };
+
+template <typename TIdSet, typename TSeqSet, typename TQualSet>
+void read_records(bool fastq, TIdSet &ids, TSeqSet &seqs, TQualSet *quals, std::string const &text)
+{
+    typedef typename Value<TSeqSet>::Type TSeq;
+    typedef typename Value<TSeq>::Type TAlph;
+    const int64_t n = int64_t(text.size());
+    const int64_t rcap = int64_t(std::count(text.begin(), text.end(), fastq ? '@' : '>')) + 1;
+    const size_t cap = static_cast<size_t>(rcap);
+    std::vector<int64_t> ib(cap), ie(cap), so(cap), qe(cap);
+    std::vector<uint8_t> codes(size_t(n) + 1);
+    std::vector<char> qual(fastq ? size_t(n) + 1 : 1);
+    gba_seq_records r{rcap, n + 1, ib.data(), ie.data(), so.data(), qe.data(), codes.data(),
+                      fastq ? qual.data() : nullptr, 0, 0, -1};
+    const int rc = fastq ? gba_read_fastq(context(), text.data(), n, ReaderAlphabet<TAlph>::VALUE, &r)
+                         : gba_read_fasta(context(), text.data(), n, ReaderAlphabet<TAlph>::VALUE, &r);
+    if (rc == GBA_EPARSE) {
+        if (r.error_offset >= n) throw UnexpectedEnd();
+        throw ParseError("record text not in the format at offset " + std::to_string(r.error_offset));
+    }
+    check(rc, fastq ? "gba_read_fastq" : "gba_read_fasta");
+    for (int64_t k = 0; k < r.num; ++k) {
+        appendValue(ids, CharString(text.substr(size_t(ib[k]), size_t(ie[k] - ib[k]))));
+        TSeq s;
+        resize(s, size_t(so[k + 1] - so[k]));
+        for (int64_t i = so[k]; i < so[k + 1]; ++i) s[size_t(i - so[k])] = TAlph(unsigned(codes[size_t(i)]));
+        appendValue(seqs, s);
+        if (quals) appendValue(*quals, CharString(std::string(qual.data() + so[k], qual.data() + qe[k])));
+    }
+}
+
+// ---- SAM / BAM output of BamAlignmentRecords (bam_io/write_sam.h:126-217, write_bam.h:100-271) ---
+
+struct RecordArrays {
+    std::vector<char> qname, seq_letters, qual, cnames;
+    std::vector<int64_t> qoff{0}, coff{0}, soff{0}, quoff{0}, cnoff{0};
+    std::vector<uint16_t> flag;
+    std::vector<int32_t> rid, pos, rnext, pnext, tlen;
+    std::vector<uint8_t> mapq, seq;
+    std::vector<uint32_t> cigar;
+    gba_sam_records rec{};
+};
+
+template <typename TNameStore, typename TNameStoreCache, typename TStorageSpec>
+void record_arrays(RecordArrays &a, String<BamAlignmentRecord> const &records,
+                   BamIOContext<TNameStore, TNameStoreCache, TStorageSpec> &context)
+{
+    static char const ops[] = "MIDNSHP=X";
+    for (size_t k = 0; k < length(records); ++k) {
+        BamAlignmentRecord const &r = records[k];
+        if (!empty(r.tags)) throw std::runtime_error("GB300 SAM/BAM output: records with tags are not supported");
+        for (size_t i = 0; i < length(r.qName); ++i) a.qname.push_back(r.qName[i]);
+        a.qoff.push_back(int64_t(a.qname.size()));
+        a.flag.push_back(uint16_t(r.flag));
+        a.rid.push_back(r.rID);
+        a.pos.push_back(r.beginPos);
+        a.mapq.push_back(uint8_t(r.mapQ));
+        for (size_t i = 0; i < length(r.cigar); ++i) {
+            char const *op = std::strchr(ops, r.cigar[i].operation);
+            if (!op || !*op) throw std::runtime_error("GB300 SAM/BAM output: CIGAR operation outside MIDNSHP=X");
+            a.cigar.push_back((uint32_t(r.cigar[i].count) << 4) | uint32_t(op - ops));
+        }
+        a.coff.push_back(int64_t(a.cigar.size()));
+        a.rnext.push_back(r.rNextId);
+        a.pnext.push_back(r.pNext);
+        a.tlen.push_back(r.tLen);
+        for (size_t i = 0; i < length(r.seq); ++i) a.seq.push_back(uint8_t(ordValue(r.seq[i])));
+        a.soff.push_back(int64_t(a.seq.size()));
+        for (size_t i = 0; i < length(r.qual); ++i) a.qual.push_back(r.qual[i]);
+        a.quoff.push_back(int64_t(a.qual.size()));
+    }
+    for (size_t c = 0; c < length(contigNames(context)); ++c) {
+        for (size_t i = 0; i < length(contigNames(context)[c]); ++i) a.cnames.push_back(contigNames(context)[c][i]);
+        a.cnoff.push_back(int64_t(a.cnames.size()));
+    }
+    a.seq_letters.assign(32, 'N');
+    for (unsigned v = 0; v < 16; ++v) a.seq_letters[v] = convert<char>(Iupac(v));   // IupacString letters
+    for (auto *v : {&a.qname, &a.qual, &a.cnames}) v->push_back(0);
+    a.seq.push_back(0);
+    a.cigar.push_back(0);
+    const int64_t n = int64_t(length(records));
+    a.rec = gba_sam_records{n, a.qname.data(), a.qoff.data(), a.flag.data(), a.rid.data(), a.pos.data(), a.mapq.data(),
+                            a.cigar.data(), a.coff.data(), a.rnext.data(), a.pnext.data(), a.tlen.data(),
+                            a.seq.data(), a.soff.data(), a.seq_letters.data(), a.qual.data(), a.quoff.data(),
+                            a.cnames.data(), a.cnoff.data(), int64_t(length(contigNames(context)))};
+}
+
+}  // namespace gb300_impl
+
+template <typename TVec, typename TIdSet, typename TSeqSet>
+void readRecords(ExecutionPolicy<GB300, TVec> const &, TIdSet &ids, TSeqSet &seqs, std::string const &text, Fasta)
+{
+    gb300_impl::read_records(false, ids, seqs, static_cast<TIdSet *>(nullptr), text);
+}
+
+template <typename TVec, typename TIdSet, typename TSeqSet, typename TQualSet>
+void readRecords(ExecutionPolicy<GB300, TVec> const &, TIdSet &ids, TSeqSet &seqs, TQualSet &quals,
+                 std::string const &text, Fastq)
+{
+    gb300_impl::read_records(true, ids, seqs, &quals, text);
+}
+
+// Appends the SAM lines of the records (no header) to target, as write(target, record, context,
+// Sam()) for each record does.
+template <typename TVec, typename TTarget, typename TNameStore, typename TNameStoreCache, typename TStorageSpec>
+void write(ExecutionPolicy<GB300, TVec> const &, TTarget &target, String<BamAlignmentRecord> const &records,
+           BamIOContext<TNameStore, TNameStoreCache, TStorageSpec> &context, Sam const &)
+{
+    gb300_impl::RecordArrays a;
+    gb300_impl::record_arrays(a, records, context);
+    std::vector<int64_t> off(length(records) + 1);
+    int rc = gba_format_sam(gb300_impl::context(), &a.rec, nullptr, 0, off.data());
+    if (rc != GBA_ECAPACITY) gb300_impl::check(rc, "gba_format_sam");
+    std::vector<char> text(size_t(off.back()) + 1);
+    gb300_impl::check(gba_format_sam(gb300_impl::context(), &a.rec, text.data(), int64_t(text.size()), off.data()),
+                      "gba_format_sam");
+    for (int64_t i = 0; i < off.back(); ++i) appendValue(target, text[size_t(i)]);
+}
+
+// Appends the BAM record blocks (uncompressed, no header) to target, as write(target, record,
+// context, Bam()) for each record does.
+template <typename TVec, typename TTarget, typename TNameStore, typename TNameStoreCache, typename TStorageSpec>
+void write(ExecutionPolicy<GB300, TVec> const &, TTarget &target, String<BamAlignmentRecord> const &records,
+           BamIOContext<TNameStore, TNameStoreCache, TStorageSpec> &context, Bam const &)
+{
+    gb300_impl::RecordArrays a;
+    gb300_impl::record_arrays(a, records, context);
+    std::vector<int64_t> off(length(records) + 1);
+    int rc = gba_format_bam(gb300_impl::context(), &a.rec, nullptr, 0, off.data());
+    if (rc != GBA_ECAPACITY) gb300_impl::check(rc, "gba_format_bam");
+    std::vector<char> bytes(size_t(off.back()) + 1);
+    gb300_impl::check(gba_format_bam(gb300_impl::context(), &a.rec, bytes.data(), int64_t(bytes.size()), off.data()),
+                      "gba_format_bam");
+    for (int64_t i = 0; i < off.back(); ++i) appendValue(target, bytes[size_t(i)]);
 }
 
 }  // namespace seqan2

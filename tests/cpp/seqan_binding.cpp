@@ -39,6 +39,34 @@ static void seeds_demo(ExecutionPolicy<GB300, Vectorial> const &gpu)
     std::cout << beginPositionH(onShared[0]) << " " << endPositionH(onShared[0]) << "\n";
 }
 
+// FASTA / FASTQ input and SAM / BAM output through the GB300 overloads.
+static void io_demo(ExecutionPolicy<GB300, Vectorial> const &gpu)
+{
+    StringSet<CharString> ids, quals;
+    StringSet<Dna5String> seqs;
+    readRecords(gpu, ids, seqs, std::string(">r1 first\nACGT\nNN\n>r2\nacgt\n"), Fasta());
+    StringSet<String<AminoAcid>> prot;
+    readRecords(gpu, ids, prot, std::string(">p\nMKV*\n"), Fasta());
+    readRecords(gpu, ids, seqs, quals, std::string("@q1\nACGT\n+\nIIII\n"), Fastq());
+    StringSet<CharString> names;
+    appendValue(names, "chr1");
+    NameStoreCache<StringSet<CharString>> cache(names);
+    BamIOContext<StringSet<CharString>> context(names, cache);
+    String<BamAlignmentRecord> records;
+    BamAlignmentRecord r;
+    r.qName = "q1";
+    r.rID = 0;
+    r.beginPos = 10;
+    appendValue(r.cigar, CigarElement<>('M', 4));
+    r.seq = "ACGT";
+    r.qual = "IIII";
+    appendValue(records, r);
+    CharString sam, bam;
+    write(gpu, sam, records, context, Sam());
+    write(gpu, bam, records, context, Bam());
+    std::cout << length(ids) << ' ' << length(seqs) << ' ' << length(sam) << ' ' << length(bam) << '\n';
+}
+
 int main()
 {
     ExecutionPolicy<GB300, Vectorial> gpu;
@@ -95,5 +123,6 @@ int main()
               << n2[0] << ' ' << n3[0] << ' ' << n4[0] << '\n'
               << gapsH[0] << '\n' << gapsV[0] << '\n' << aligns[0] << '\n';
     seeds_demo(gpu);
+    io_demo(gpu);
     return 0;
 }
