@@ -202,6 +202,50 @@ def fasta_reads_text(n, seed=3):
     return out.tobytes(), codes
 
 
+def fastq_reads_text(codes, seed=4):
+    """FASTQ text of the reads (one sequence line, '+', one quality line per record)."""
+    rng = np.random.default_rng(seed)
+    n, L = codes.shape
+    letters = np.frombuffer(b"ACGTN", np.uint8)[codes]
+    quals = rng.integers(33, 74, (n, L), dtype=np.uint8)
+    heads = [b"@read%d\n" % k for k in range(n)]
+    hl = np.fromiter((len(h) for h in heads), np.int64, n)
+    body = 2 * L + 4   # sequence, '\n+\n', qualities, '\n'
+    rows = np.empty((n, body), np.uint8)
+    rows[:, :L] = letters
+    rows[:, L:L + 3] = np.frombuffer(b"\n+\n", np.uint8)
+    rows[:, L + 3:2 * L + 3] = quals
+    rows[:, 2 * L + 3] = 10
+    out = np.empty(int(hl.sum()) + body * n, np.uint8)
+    starts = np.zeros(n, np.int64)
+    np.cumsum(hl[:-1] + body, out=starts[1:])
+    hb = np.frombuffer(b"".join(heads), np.uint8)
+    hoff = np.zeros(n, np.int64)
+    np.cumsum(hl[:-1], out=hoff[1:])
+    out[np.repeat(starts - hoff, hl) + np.arange(len(hb))] = hb
+    out[((starts + hl)[:, None] + np.arange(body)[None, :]).ravel()] = rows.ravel()
+    return out.tobytes()
+
+
+def time_fastq_host(L, text, n_reads, reps=3):
+    """gba_read_fastq (the host FASTQ reader) on the text: GB/s of text, best of reps."""
+    from seqan_gb300 import _native as N
+    n = len(text)
+    buf = np.frombuffer(text, np.uint8)
+    ib, ie, so, qe = (np.zeros(n_reads + 1, np.int64) for _ in range(4))
+    codes = np.zeros(n, np.uint8)
+    quals = np.zeros(n, np.uint8)
+    r = N.GbaSeqRecords(n_reads + 1, n, ib.ctypes.data, ie.ctypes.data, so.ctypes.data, qe.ctypes.data,
+                        codes.ctypes.data, quals.ctypes.data, 0, 0, -1)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        rc = L.gba_read_fastq(None, buf.ctypes.data, n, 5, C.byref(r))
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return (n / best / 1e9 if rc == N.GBA_OK and r.num == n_reads else None), codes[:r.residues]
+
+
 def run_fasta_bench(args, rank, world, local_rank, dist):
     from seqan_gb300 import _native as N
     from oracle import oracle as O
@@ -270,6 +314,11 @@ def run_fasta_bench(args, rank, world, local_rank, dist):
                          "algorithmic_bytes": "text read once + codes and 3 x 8 B per record written once",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
             "clocks": clocks, "parity_vs_generated_codes_and_oracle_ids": parity}
+    fq = fastq_reads_text(codes)
+    fq_gbs, fq_codes = time_fastq_host(L, fq, n_reads)
+    line["fastq_host"] = {"value": fq_gbs, "unit": "GB/s", "text_bytes": len(fq), "cores": 1,
+                          "reader": "gba_read_fastq (host: a record's end is found by counting its qualities)",
+                          "parity_vs_generated_codes": bool(np.array_equal(fq_codes, codes.ravel()))}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         best = None
         for _ in range(2):
