@@ -481,6 +481,204 @@ inline int seqio_check(gba_context *ctx, const char *text, int64_t n, int32_t al
     return GBA_OK;
 }
 
+// ---- FASTQ on the host ------------------------------------------------------------------------
+
+struct FqResult {
+    int status = GBA_OK;
+    int64_t err_at = -1;
+    const char *what = "";
+    int64_t end = 0;   // parser position after the last record read: the next '@' or the end
+};
+
+// Writes records straight into the caller's buffers (counting past their capacities).
+struct FqCallerSink {
+    gba_seq_records *r;
+    bool write;
+    int64_t rec = 0, res = 0, qe = 0;
+    void code(uint8_t k)
+    {
+        if (write && res < r->residue_capacity) r->codes[res] = k;
+        ++res;
+    }
+    void qual_begin() { qe = seq_begin; }
+    void qual(char c)
+    {
+        if (write && r->quals && qe < r->residue_capacity) r->quals[qe] = c;
+        ++qe;
+    }
+    int64_t seq_begin = 0;
+    void record_begin() { seq_begin = res; }
+    void record(int64_t ib, int64_t ie)
+    {
+        if (write && rec < r->record_capacity) {
+            r->id_begin[rec] = ib;
+            r->id_end[rec] = ie;
+            r->seq_off[rec] = seq_begin;
+            if (r->qual_end) r->qual_end[rec] = qe;
+        }
+        ++rec;
+    }
+};
+
+// Collects one thread's records (residue and quality offsets local to the thread).
+struct FqLocalSink {
+    std::vector<int64_t> ib, ie, sb, qe;
+    std::vector<uint8_t> codes;
+    std::vector<char> quals;
+    int64_t seq_begin = 0;
+    void code(uint8_t k) { codes.push_back(k); }
+    void qual_begin() { quals.resize(size_t(seq_begin)); }
+    void qual(char c) { quals.push_back(c); }
+    void record_begin() { seq_begin = int64_t(codes.size()); }
+    void record(int64_t b, int64_t e)
+    {
+        ib.push_back(b);
+        ie.push_back(e);
+        sb.push_back(seq_begin);
+        qe.push_back(int64_t(quals.size()));
+        quals.resize(codes.size());   // keep qualities at their residues' offsets
+    }
+};
+
+// The reference's readRecord loop for FASTQ from position p: records are read while the next one
+// starts before stop (a record's start is the '@' that skipUntil reaches).
+template <typename Sink>
+FqResult fastq_parse(const uint8_t *t, int64_t n, int64_t p, int64_t stop, const int8_t *cls, Sink &sink)
+{
+    FqResult out;
+    auto nl = [](uint8_t c) { return c == '\n' || c == '\r'; };
+    auto ws = [](uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; };
+    auto err = [&](int64_t at, const char *what) {
+        out.status = GBA_EPARSE;
+        out.err_at = at;
+        out.what = what;
+        out.end = at;
+        return out;
+    };
+    while (p < n) {
+        const void *at = memchr(t + p, '@', size_t(n - p));   // skipUntil '@'
+        if (!at) return err(n, "no '@' record start before the end");
+        if (static_cast<const uint8_t *>(at) - t >= stop) {
+            out.end = static_cast<const uint8_t *>(at) - t;
+            return out;
+        }
+        p = static_cast<const uint8_t *>(at) - t + 1;
+        const int64_t ib = p;                                  // readLine(id)
+        while (p < n && !nl(t[p])) ++p;
+        const int64_t ie = p;
+        if (p < n && t[p] == '\r') ++p;
+        if (p < n && t[p] == '\n') ++p;
+        sink.record_begin();
+        int64_t len = 0;
+        for (; p < n && t[p] != '+'; ++p) {                    // readUntil(seq, '+')
+            const int k = cls[t[p]];
+            if (k == FA_WS || k == FA_NL) continue;
+            if (k < 0) return err(p, "character outside the alphabet");
+            sink.code(uint8_t(k));
+            ++len;
+        }
+        if (p >= n) return err(n, "no '+' line before the end");
+        ++p;
+        while (p < n && !nl(t[p])) ++p;                        // skipLine
+        if (p < n && t[p] == '\r') ++p;
+        if (p < n && t[p] == '\n') ++p;
+        sink.qual_begin();
+        for (int64_t need = len; p < n && need > 0; ++p) {     // counted qualities
+            if (nl(t[p])) continue;
+            sink.qual(char(t[p]));
+            --need;
+        }
+        while (p < n && ws(t[p])) ++p;
+        if (p < n && t[p] != '@' && t[p] != 0xFF) return err(p, "quality string not as long as the sequence");
+        sink.record(ib, ie);
+    }
+    out.end = n;
+    return out;
+}
+
+// A plausible record start at or after from: '@' at a line start, then a line, a line, a line
+// starting with '+', and a line as long as the second.
+inline int64_t fastq_sync(const uint8_t *t, int64_t n, int64_t from)
+{
+    auto line_end = [&](int64_t q) {
+        while (q < n && t[q] != '\n') ++q;
+        return q;
+    };
+    for (int64_t p = from; p < n; ++p) {
+        if (t[p] != '@' || (p > 0 && t[p - 1] != '\n')) continue;
+        const int64_t e1 = line_end(p);
+        const int64_t e2 = line_end(e1 + 1);
+        if (e2 >= n || t[e2 + 1] != '+') continue;
+        const int64_t e3 = line_end(e2 + 1);
+        const int64_t e4 = line_end(e3 + 1);
+        if (e4 - (e3 + 1) == e2 - (e1 + 1)) return p;
+    }
+    return n;
+}
+
+// Reads a large text with the threads of the host: each thread starts at a plausible record start
+// in its slice and reads until the next thread's start.  The result stands only if every thread's
+// reading ends exactly on the next thread's start (thread 0 starts where the reference starts, so
+// each start is then a true record start) and no thread met an error; otherwise it returns false
+// and the caller reads the text sequentially.
+template <typename Sink>
+bool fastq_read_parallel(const uint8_t *t, int64_t n, const int8_t *cls, Sink &sink, FqResult &result)
+{
+    const int threads = omp_get_max_threads();
+    if (threads < 2 || n < (int64_t(4) << 20)) return false;
+    std::vector<int64_t> start(size_t(threads) + 1);
+    start[0] = 0;
+    start[size_t(threads)] = n;
+#pragma omp parallel for num_threads(threads)
+    for (int k = 1; k < threads; ++k) start[size_t(k)] = fastq_sync(t, n, n / threads * k);
+    for (int k = 1; k <= threads; ++k)
+        if (start[size_t(k)] < start[size_t(k - 1)]) start[size_t(k)] = start[size_t(k - 1)];
+    std::vector<FqLocalSink> local(static_cast<size_t>(threads));
+    std::vector<FqResult> res(static_cast<size_t>(threads));
+#pragma omp parallel for num_threads(threads)
+    for (int k = 0; k < threads; ++k) {
+        const size_t slice = size_t(start[size_t(k + 1)] - start[size_t(k)]) + 4096;
+        FqLocalSink &l = local[size_t(k)];
+        l.codes.reserve(slice);
+        l.quals.reserve(slice);
+        for (auto *v : {&l.ib, &l.ie, &l.sb, &l.qe}) v->reserve(slice / 64 + 16);
+        res[size_t(k)] = fastq_parse(t, n, start[size_t(k)], k + 1 < threads ? start[size_t(k + 1)] : INT64_MAX, cls,
+                                     l);
+    }
+    for (int k = 0; k < threads; ++k) {
+        if (res[size_t(k)].status) return false;
+        if (k + 1 < threads && res[size_t(k)].end != start[size_t(k + 1)]) return false;
+    }
+    // Concatenate the threads' records in order into the caller's buffers, each thread its part.
+    std::vector<int64_t> rec0(size_t(threads) + 1, 0), res0(size_t(threads) + 1, 0);
+    for (int k = 0; k < threads; ++k) {
+        rec0[size_t(k + 1)] = rec0[size_t(k)] + int64_t(local[size_t(k)].ib.size());
+        res0[size_t(k + 1)] = res0[size_t(k)] + int64_t(local[size_t(k)].codes.size());
+    }
+    const int64_t nrec = rec0[size_t(threads)], nres = res0[size_t(threads)];
+    if (sink.write && nrec <= sink.r->record_capacity && nres <= sink.r->residue_capacity) {
+        gba_seq_records *r = sink.r;
+#pragma omp parallel for num_threads(threads)
+        for (int k = 0; k < threads; ++k) {
+            const FqLocalSink &l = local[size_t(k)];
+            const int64_t b = res0[size_t(k)], q = rec0[size_t(k)];
+            memcpy(r->codes + b, l.codes.data(), l.codes.size());
+            if (r->quals) memcpy(r->quals + b, l.quals.data(), std::min(l.quals.size(), l.codes.size()));
+            for (size_t j = 0; j < l.ib.size(); ++j) {
+                r->id_begin[q + int64_t(j)] = l.ib[j];
+                r->id_end[q + int64_t(j)] = l.ie[j];
+                r->seq_off[q + int64_t(j)] = b + l.sb[j];
+                if (r->qual_end) r->qual_end[q + int64_t(j)] = b + l.qe[j];
+            }
+        }
+    }
+    sink.rec = nrec;
+    sink.res = nres;
+    result = FqResult{};
+    result.end = n;
+    return true;
+}
+
 }  // namespace gba
 
 extern "C" {
@@ -590,64 +788,23 @@ GBA_API int gba_read_fastq(gba_context *ctx, const char *text, int64_t n, int32_
         if (rc) return rc;
     }
     cls[uint8_t('>')] = FA_BAD;
-    auto err = [&](int status, int64_t at, const char *what) {
-        r->error_offset = at;
-        return ctx ? fail(ctx, status, "%s at offset %lld", what, (long long)at) : status;
-    };
     const uint8_t *t = reinterpret_cast<const uint8_t *>(text);
-    const int64_t rcap = r->record_capacity, qcap = r->residue_capacity;
-    const bool write = r->codes && r->id_begin && r->id_end && r->seq_off;
-    int64_t p = 0, rec = 0, res = 0;
-    auto nl = [](uint8_t c) { return c == '\n' || c == '\r'; };
-    auto ws = [](uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; };
-    while (p < n) {
-        const void *at = memchr(t + p, '@', size_t(n - p));   // skipUntil '@'
-        if (!at) return err(GBA_EPARSE, n, "no '@' record start before the end");
-        p = static_cast<const uint8_t *>(at) - t + 1;
-        const int64_t ib = p;                                  // readLine(id)
-        while (p < n && !nl(t[p])) ++p;
-        const int64_t ie = p;
-        if (p < n && t[p] == '\r') ++p;
-        if (p < n && t[p] == '\n') ++p;
-        const int64_t sb = res;
-        for (; p < n && t[p] != '+'; ++p) {                    // readUntil(seq, '+')
-            const int k = cls[t[p]];
-            if (k == FA_WS || k == FA_NL) continue;
-            if (k < 0) return err(GBA_EPARSE, p, "character outside the alphabet");
-            if (write && res < qcap) r->codes[res] = uint8_t(k);
-            ++res;
-        }
-        if (p >= n) return err(GBA_EPARSE, n, "no '+' line before the end");
-        ++p;
-        while (p < n && !nl(t[p])) ++p;                        // skipLine
-        if (p < n && t[p] == '\r') ++p;
-        if (p < n && t[p] == '\n') ++p;
-        int64_t need = res - sb, qe = sb;
-        for (; p < n && need > 0; ++p) {                       // counted qualities
-            if (nl(t[p])) continue;
-            if (write && r->quals && qe < qcap) r->quals[qe] = char(t[p]);
-            ++qe;
-            --need;
-        }
-        while (p < n && ws(t[p])) ++p;
-        if (p < n && t[p] != '@' && t[p] != 0xFF)
-            return err(GBA_EPARSE, p, "quality string not as long as the sequence");
-        if (write && rec < rcap) {
-            r->id_begin[rec] = ib;
-            r->id_end[rec] = ie;
-            r->seq_off[rec] = sb;
-            if (r->qual_end) r->qual_end[rec] = qe;
-        }
-        ++rec;
+    FqCallerSink sink{r, r->codes && r->id_begin && r->id_end && r->seq_off};
+    FqResult res;
+    if (!fastq_read_parallel(t, n, cls, sink, res)) res = fastq_parse(t, n, 0, INT64_MAX, cls, sink);
+    if (res.status) {
+        r->error_offset = res.err_at;
+        return ctx ? fail(ctx, res.status, "%s at offset %lld", res.what, (long long)res.err_at) : res.status;
     }
+    const int64_t rec = sink.rec, nres = sink.res;
     r->num = rec;
-    r->residues = res;
-    if (!write || rec + 1 > rcap || res > qcap) {
+    r->residues = nres;
+    if (!sink.write || rec + 1 > r->record_capacity || nres > r->residue_capacity) {
         return ctx ? fail(ctx, GBA_ECAPACITY, "records need %lld record and %lld residue entries",
-                          (long long)rec + 1, (long long)res)
+                          (long long)rec + 1, (long long)nres)
                    : GBA_ECAPACITY;
     }
-    r->seq_off[rec] = res;
+    r->seq_off[rec] = nres;
     return GBA_OK;
 }
 

@@ -121,3 +121,43 @@ def test_oracle_matches_live_reference_random():
             assert got.value.kind == e.kind
             continue
         assert same(O.oracle_read_records(t, fmt, alph), want), t
+
+
+def _big_fastq(seed, n_records, adversarial):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for k in range(n_records):
+        L = int(rng.integers(0, 120))
+        seq = bytes(np.frombuffer(b"ACGTN", np.uint8)[rng.integers(0, 5, L)])
+        q = bytearray(rng.integers(33, 74, L).astype(np.uint8).tobytes())
+        if adversarial and L and rng.random() < 0.3:
+            q[0] = ord("@")                      # quality lines that start like a record
+        if adversarial and rng.random() < 0.1 and L > 10:
+            seq = seq[:L // 2] + b"\n" + seq[L // 2:]   # records over several lines
+            q = q[:L // 3] + b"\n" + q[L // 3:]
+        parts.append(b"@r%d x\n" % k + seq + b"\n+\n" + bytes(q) + b"\n")
+    return b"".join(parts)
+
+
+@pytest.mark.parametrize("adversarial", [False, True])
+def test_fastq_host_reader_large_texts_match_oracle(adversarial):
+    """Texts above the size where the host reader splits the work across threads (speculative
+    record starts, checked against the previous slice's reading, sequential fallback)."""
+    from seqan_gb300 import _native
+    from seqan_gb300 import seq_io as S
+    _native.build()
+    text = _big_fastq(3 if adversarial else 4, 70_000, adversarial)
+    assert len(text) > 4 << 20
+    rec = S.read_fastq(text)
+    assert same(list(zip(rec.ids, rec.seqs, rec.quals_list)), O.oracle_read_records(text, "fastq", "dna5"))
+    bad = bytearray(text)
+    pos = len(bad) * 3 // 4
+    while bad[pos] not in b"ACGT":
+        pos += 1
+    for ch in (b"X", b"@"):
+        t = bytes(bad[:pos] + ch + bad[pos + 1:])
+        with pytest.raises(O.SeqParseError) as want:
+            O.oracle_read_records(t, "fastq", "dna5")
+        with pytest.raises(S.SeqParseError) as got:
+            S.read_fastq(t)
+        assert got.value.offset == want.value.offset
