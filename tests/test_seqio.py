@@ -151,9 +151,10 @@ def test_fastq_host_reader_large_texts_match_oracle(adversarial):
     rec = S.read_fastq(text)
     assert same(list(zip(rec.ids, rec.seqs, rec.quals_list)), O.oracle_read_records(text, "fastq", "dna5"))
     bad = bytearray(text)
-    pos = len(bad) * 3 // 4
-    while bad[pos] not in b"ACGT":
-        pos += 1
+    pos = bytes(bad).index(b"\n+\n", len(bad) * 3 // 4)
+    while bad[pos - 1] not in b"ACGTN":   # the last residue of a record's sequence
+        pos = bytes(bad).index(b"\n+\n", pos + 1)
+    pos -= 1
     for ch in (b"X", b"@"):
         t = bytes(bad[:pos] + ch + bad[pos + 1:])
         with pytest.raises(O.SeqParseError) as want:
