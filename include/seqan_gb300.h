@@ -486,7 +486,9 @@ GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *records, cha
  * error_offset at it, as the reference's ParseError; a non-empty text without a record start is
  * GBA_EPARSE with error_offset = length (UnexpectedEnd).  When a capacity is too small the call
  * returns GBA_ECAPACITY with num and residues set.  gba_read_fasta parses on the device;
- * gba_read_fastq parses on the host (ctx may be NULL). */
+ * gba_read_fastq parses on the host (ctx may be NULL), texts of 4 MB and more with the host's
+ * threads: speculative record starts per slice, each confirmed by the previous slice's reading
+ * ending on it, else one sequential reading (results are always the sequential ones). */
 typedef struct {
     int64_t record_capacity;   /* entries of id_begin / id_end / qual_end (>= num) and seq_off (>= num + 1) */
     int64_t residue_capacity;  /* bytes of codes (and quals) */
