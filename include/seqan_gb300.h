@@ -517,6 +517,15 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t length, i
 GBA_API int gba_read_fastq(gba_context *ctx, const char *text, int64_t length, int32_t alphabet,
                            gba_seq_records *records);
 
+/* gba_align_batch on the records of two FASTA texts: pair k is (record k of text_h, record k of
+ * text_v), or (the single record of text_h, record k of text_v) with h_shared.  Both texts are read
+ * on the device as gba_read_fasta reads them and aligned from the codes left in HBM (only the record
+ * offsets come back to the host, for the plan).  *num_pairs = the records of text_v; the result's
+ * per-pair arrays hold pair_capacity entries (GBA_ECAPACITY when fewer). */
+GBA_API int gba_align_fasta(gba_context *ctx, const gba_params *params, const char *text_h, int64_t len_h,
+                            const char *text_v, int64_t len_v, int32_t alphabet, int32_t h_shared,
+                            int64_t pair_capacity, int64_t *num_pairs, gba_result *result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -161,7 +161,8 @@ ALPHABET_SIZE = {"dna": 4, "dna5": 5, "aa": 27}
 
 def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None,
                 traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None,
-                alphabet_size: int | None = None, flags: int = 0, packed_bits: int | None = None) -> BatchOutput:
+                alphabet_size: int | None = None, flags: int = 0, packed_bits: int | None = None,
+                fasta_texts=None) -> BatchOutput:
     """Aligns lists of code arrays through gba_align_batch.
 
     alphabet_size bounds the codes (the reference's ValueSize of the alphabet); when None it is
@@ -196,6 +197,13 @@ def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=No
             res.cigar = np.zeros(cap, np.uint32)
             res.cigar_offsets = np.zeros(n + 1, np.int64)
             r.cigar, r.cigar_capacity, r.cigar_offsets = _vp(res.cigar), cap, _vp(res.cigar_offsets)
+    if fasta_texts is not None:
+        th, tv, alph = fasta_texts
+        bh, bv = np.frombuffer(bytes(th) or b"\0", np.uint8), np.frombuffer(bytes(tv) or b"\0", np.uint8)
+        npairs = C.c_int64()
+        ctx.check(N.lib().gba_align_fasta(ctx.handle, C.byref(params), _vp(bh), len(th), _vp(bv), len(tv), alph,
+                                          1 if h_shared else 0, n, C.byref(npairs), C.byref(r)), "gba_align_fasta")
+        return res
     if packed_bits:
         from . import packed as P
         hw, hoff = P.pack_set(codes_h[:1] if h_shared else codes_h, packed_bits)
@@ -303,3 +311,14 @@ def getCigarString(gapsRef: Gaps, gapsRead: Gaps, spliced_gap_thresh: int = 20) 
         else:
             ops.append([op, ln])
     return "".join(f"{n}{'N' if (o == 'D' and n >= spliced_gap_thresh) else o}" for o, n in ops)
+
+
+def align_fasta(text_h: bytes, text_v: bytes, score, alphabet: str = "dna5", **kw) -> BatchOutput:
+    """Aligns the records of two FASTA texts pairwise (record k of text_h with record k of text_v,
+    or the single record of text_h with every record of text_v when h_shared) through
+    gba_align_fasta: both texts are parsed on the device and aligned from the codes left there.
+    The records are read once more here, only to size the result arrays."""
+    from . import seq_io as S
+    codes_h, codes_v = S.read_fasta(text_h, alphabet).seqs, S.read_fasta(text_v, alphabet).seqs
+    kw.setdefault("alphabet_size", S.ALPHABETS[alphabet])
+    return align_codes(codes_h, codes_v, score, fasta_texts=(text_h, text_v, S.ALPHABETS[alphabet]), **kw)

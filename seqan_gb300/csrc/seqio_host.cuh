@@ -683,15 +683,21 @@ bool fastq_read_parallel(const uint8_t *t, int64_t n, const int8_t *cls, Sink &s
 
 extern "C" {
 
-GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r)
+}  // extern "C"
+
+namespace gba {
+
+// gba_read_fasta's work; with dst the residue codes also go to that device buffer (from offset 0)
+// and r->codes may be null.
+int fasta_parse(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r, DevBuf *dst)
 {
-    using namespace gba;
     if (!ctx) return GBA_EINVAL;
     FaArgs a{};
     if (int rc = seqio_check(ctx, text, n, alphabet, r, a.cls)) return rc;
     if (n == 0) {
         if (r->record_capacity < 1 || !r->seq_off) return fail(ctx, GBA_ECAPACITY, "seq_off needs 1 entry");
         r->seq_off[0] = 0;
+        if (dst) GBA_CUDA(ctx, dst->ensure(16));
         return GBA_OK;
     }
     GBA_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -730,8 +736,8 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
         r->error_offset = n;
         return fail(ctx, GBA_EPARSE, "no '>' record start in the text");
     }
-    if (nrec + 1 > r->record_capacity || nres > r->residue_capacity || !r->codes || !r->id_begin || !r->id_end ||
-        !r->seq_off)
+    if (nrec + 1 > r->record_capacity || (!dst && (nres > r->residue_capacity || !r->codes)) || !r->id_begin ||
+        !r->id_end || !r->seq_off)
         return fail(ctx, GBA_ECAPACITY, "records need %lld record and %lld residue entries", (long long)nrec + 1,
                     (long long)nres);
     const size_t idx_bytes = (size_t(nrec) + 1) * 8;
@@ -757,7 +763,12 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
     GBA_CUDA(ctx, cudaMemcpyAsync(r->id_begin, a.id_begin, size_t(nrec) * 8, cudaMemcpyDeviceToHost, st));
     GBA_CUDA(ctx, cudaMemcpyAsync(r->id_end, a.id_end, size_t(nrec) * 8, cudaMemcpyDeviceToHost, st));
     GBA_CUDA(ctx, cudaMemcpyAsync(r->seq_off, a.seq_off, size_t(nrec) * 8, cudaMemcpyDeviceToHost, st));
-    if (nres) GBA_CUDA(ctx, cudaMemcpyAsync(r->codes, a.codes, size_t(nres), cudaMemcpyDeviceToHost, st));
+    if (nres && r->codes && nres <= r->residue_capacity)
+        GBA_CUDA(ctx, cudaMemcpyAsync(r->codes, a.codes, size_t(nres), cudaMemcpyDeviceToHost, st));
+    if (dst) {
+        GBA_CUDA(ctx, dst->ensure(size_t(nres) + 16));
+        if (nres) GBA_CUDA(ctx, cudaMemcpyAsync(dst->ptr, a.codes, size_t(nres), cudaMemcpyDeviceToDevice, st));
+    }
     GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     GBA_CUDA(ctx, cudaStreamSynchronize(st));
     r->seq_off[nrec] = nres;
@@ -777,6 +788,59 @@ GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_
         return fail(ctx, GBA_EPARSE, "character outside the alphabet at offset %lld", (long long)err);
     }
     return GBA_OK;
+}
+
+}  // namespace gba
+
+extern "C" {
+
+GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r)
+{
+    return gba::fasta_parse(ctx, text, n, alphabet, r, nullptr);
+}
+
+GBA_API int gba_align_fasta(gba_context *ctx, const gba_params *params, const char *text_h, int64_t len_h,
+                            const char *text_v, int64_t len_v, int32_t alphabet, int32_t h_shared,
+                            int64_t pair_capacity, int64_t *num_pairs, gba_result *result)
+{
+    using namespace gba;
+    if (!ctx || !params || !num_pairs || !result) return GBA_EINVAL;
+    std::vector<int64_t> off[2], ib[2], ie[2];
+    const char *texts[2] = {text_h, text_v};
+    const int64_t lens[2] = {len_h, len_v};
+    DevBuf *dst[2] = {&ctx->seq_h, &ctx->seq_v};
+    for (int side = 0; side < 2; ++side) {
+        // first call: the record count (GBA_ECAPACITY), then the parse into the sequence buffer
+        gba_seq_records r{};
+        r.record_capacity = 0;
+        int rc = fasta_parse(ctx, texts[side], lens[side], alphabet, &r, dst[side]);
+        if (rc != GBA_ECAPACITY) return rc == GBA_OK ? fail(ctx, GBA_EINVAL, "FASTA text without records") : rc;
+        const size_t cap = static_cast<size_t>(r.num) + 1;
+        off[side].assign(cap, 0);
+        ib[side].assign(cap, 0);
+        ie[side].assign(cap, 0);
+        r = gba_seq_records{};
+        r.record_capacity = int64_t(cap);
+        r.id_begin = ib[side].data();
+        r.id_end = ie[side].data();
+        r.seq_off = off[side].data();
+        if ((rc = fasta_parse(ctx, texts[side], lens[side], alphabet, &r, dst[side]))) return rc;
+    }
+    const int64_t nh = int64_t(off[0].size()) - 1, nv = int64_t(off[1].size()) - 1;
+    *num_pairs = nv;
+    if (h_shared ? nh != 1 : nh != nv)
+        return fail(ctx, GBA_EINVAL, "FASTA texts hold %lld and %lld records", (long long)nh, (long long)nv);
+    if (nv > pair_capacity) return fail(ctx, GBA_ECAPACITY, "%lld pairs, result arrays hold %lld", (long long)nv,
+                                        (long long)pair_capacity);
+    gba_batch b{};
+    b.num_pairs = nv;
+    b.off_h = off[0].data();
+    b.off_v = off[1].data();
+    b.h_shared = h_shared;
+    ctx->device_codes = true;
+    const int rc = gba_align_batch(ctx, params, &b, result);
+    ctx->device_codes = false;
+    return rc;
 }
 
 GBA_API int gba_read_fastq(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r)

@@ -120,3 +120,36 @@ def test_empty_text_capacity_and_arguments(engine):
     assert N.lib().gba_read_fasta(engine.handle, text.ctypes.data, len(text), 5, C.byref(r)) == N.GBA_ECAPACITY
     assert (r.num, r.residues) == (2, 6)
     assert N.lib().gba_read_fasta(engine.handle, text.ctypes.data, len(text), 3, C.byref(r)) == N.GBA_EINVAL
+
+
+@pytest.mark.parametrize("h_shared", [False, True])
+def test_align_fasta_equals_align_of_codes(engine, h_shared):
+    """gba_align_fasta (both texts parsed on the device, aligned from the codes left in HBM): the
+    scores, ends, trace segments and CIGARs of aligning the same records as code arrays."""
+    import seqan_gb300 as sg
+    from seqan_gb300 import align as A
+    from seqan_gb300 import workloads as W
+    wins, reads = W.read_windows(3000, ref_len=1_000_000, seed=21)
+    H = [wins[0]] if h_shared else list(wins)
+    th = W.records_text(H, "fasta", width=70, seed=5, lowercase=0.05, id_prefix="win")
+    tv = W.records_text(reads, "fasta", width=0, seed=6, crlf=True)
+    sc = sg.Score(2, -4, -1, -6)
+    cfg = sg.AlignConfig(True, False, False, True)
+    got = A.align_fasta(th, tv, sc, config=cfg, traceback=True, cigar=True, h_shared=h_shared)
+    want = A.align_codes(H, list(reads), sc, config=cfg, traceback=True, cigar=True, h_shared=h_shared,
+                         alphabet_size=5)
+    assert np.array_equal(got.score, want.score) and np.array_equal(got.end_h, want.end_h)
+    assert np.array_equal(got.end_v, want.end_v)
+    assert np.array_equal(got.segment_offsets, want.segment_offsets)
+    assert np.array_equal(got.segments[:got.segment_offsets[-1]], want.segments[:want.segment_offsets[-1]])
+    assert np.array_equal(got.cigar[:got.cigar_offsets[-1]], want.cigar[:want.cigar_offsets[-1]])
+
+
+def test_align_fasta_refuses_mismatched_texts(engine):
+    import seqan_gb300 as sg
+    from seqan_gb300 import _native as N
+    from seqan_gb300 import align as A
+    with pytest.raises(N.GbaError) as e:
+        A.align_codes([np.zeros(3, np.uint8)] * 2, [np.zeros(3, np.uint8)], sg.Score(1, -1, -1),
+                      fasta_texts=(b">a\nACG\n>b\nACG\n", b">c\nACG\n", 5), alphabet_size=5)
+    assert e.value.status == N.GBA_EINVAL
