@@ -1355,6 +1355,32 @@ def main():
                       "d2h_bytes_per_step": 3 * npairs * 4, "ms_per_step": 1e3 * sum(pk_s) / len(pk_s),
                       "input": "String<Dna, Packed<>> host words (gba_align_packed)"}
         extra_pinned += pk
+    # The same pairs as two FASTA texts (60-column lines) from pinned memory: gba_align_fasta reads
+    # both on the device and aligns from the codes left in HBM.
+    e2e_fasta = None
+    if spec.alphabet_size <= 5 and not spec.traceback and not getattr(spec, "h_shared", False):
+        from seqan_gb300 import workloads as Wl
+        th = Wl.records_text(H, "fasta", width=60, seed=7, id_prefix="h")
+        tv = Wl.records_text(V, "fasta", width=60, seed=8, id_prefix="v")
+        ft = [pinned(len(th)), pinned(len(tv))]
+        C.memmove(ft[0], th, len(th))
+        C.memmove(ft[1], tv, len(tv))
+        npairs_out = C.c_int64()
+        fa_call = lambda: ctx.check(L.gba_align_fasta(h, C.byref(params), ft[0], len(th), ft[1], len(tv), 5, 0, npairs,
+                                                      C.byref(npairs_out), C.byref(host_res)), "fa")
+        for _ in range(max(1, args.warmup)):
+            fa_call()
+        fa_s = []
+        for _ in range(args.steps):
+            flush_l2()
+            t0 = time.perf_counter()
+            fa_call()
+            fa_s.append(time.perf_counter() - t0)
+        e2e_fasta = {"value": cells * world * len(fa_s) / sum(fa_s) / 1e9, "unit": "GCUPS",
+                     "h2d_bytes_per_step": len(th) + len(tv), "d2h_bytes_per_step": 3 * npairs * 4,
+                     "ms_per_step": 1e3 * sum(fa_s) / len(fa_s),
+                     "input": "two FASTA texts, 60-column lines (gba_align_fasta)"}
+        extra_pinned += ft
     e2e_breakdown = {"host_plan_ms": est.host_plan_ms, "dp_kernel_ms": est.dp_kernel_ms, "call_ms": est.call_ms}
     e2e_gcups = cells * world * len(e2e_s) / sum(e2e_s) / 1e9
     h2d = sh.nbytes + sv.nbytes + oh.nbytes + ov.nbytes
@@ -1410,6 +1436,8 @@ def main():
         line["config"]["tiling"] = tile
     if e2e_packed:
         line["e2e_packed"] = e2e_packed
+    if e2e_fasta:
+        line["e2e_fasta"] = e2e_fasta
     if plain:
         line["plain_gpu_form"] = plain
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
