@@ -687,14 +687,26 @@ extern "C" {
 
 namespace gba {
 
+// Host arrays for the record bounds that fasta_parse sizes itself once the scan has counted the
+// records (one reading of the text instead of a counting call and a reading call).
+struct FaHostRecords {
+    std::vector<int64_t> id_begin, id_end, seq_off;
+};
+
 // gba_read_fasta's work; with dst the residue codes also go to that device buffer (from offset 0)
-// and r->codes may be null.
-int fasta_parse(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r, DevBuf *dst)
+// and r->codes may be null; with grow the record arrays are grow's, sized to the records found.
+int fasta_parse(gba_context *ctx, const char *text, int64_t n, int32_t alphabet, gba_seq_records *r, DevBuf *dst,
+                FaHostRecords *grow = nullptr)
 {
     if (!ctx) return GBA_EINVAL;
     FaArgs a{};
     if (int rc = seqio_check(ctx, text, n, alphabet, r, a.cls)) return rc;
     if (n == 0) {
+        if (grow) {
+            grow->seq_off.assign(1, 0);
+            r->seq_off = grow->seq_off.data();
+            r->record_capacity = 1;
+        }
         if (r->record_capacity < 1 || !r->seq_off) return fail(ctx, GBA_ECAPACITY, "seq_off needs 1 entry");
         r->seq_off[0] = 0;
         if (dst) GBA_CUDA(ctx, dst->ensure(16));
@@ -735,6 +747,16 @@ int fasta_parse(gba_context *ctx, const char *text, int64_t n, int32_t alphabet,
     if (nrec == 0) {   // readRecord's skipOne('>') at the end of the text: UnexpectedEnd
         r->error_offset = n;
         return fail(ctx, GBA_EPARSE, "no '>' record start in the text");
+    }
+    if (grow) {
+        const size_t cap = static_cast<size_t>(nrec) + 1;
+        grow->id_begin.assign(cap, 0);
+        grow->id_end.assign(cap, 0);
+        grow->seq_off.assign(cap, 0);
+        r->id_begin = grow->id_begin.data();
+        r->id_end = grow->id_end.data();
+        r->seq_off = grow->seq_off.data();
+        r->record_capacity = int64_t(cap);
     }
     if (nrec + 1 > r->record_capacity || (!dst && (nres > r->residue_capacity || !r->codes)) || !r->id_begin ||
         !r->id_end || !r->seq_off)
@@ -805,27 +827,15 @@ GBA_API int gba_align_fasta(gba_context *ctx, const gba_params *params, const ch
 {
     using namespace gba;
     if (!ctx || !params || !num_pairs || !result) return GBA_EINVAL;
-    std::vector<int64_t> off[2], ib[2], ie[2];
+    FaHostRecords rec[2];
     const char *texts[2] = {text_h, text_v};
     const int64_t lens[2] = {len_h, len_v};
     DevBuf *dst[2] = {&ctx->seq_h, &ctx->seq_v};
     for (int side = 0; side < 2; ++side) {
-        // first call: the record count (GBA_ECAPACITY), then the parse into the sequence buffer
         gba_seq_records r{};
-        r.record_capacity = 0;
-        int rc = fasta_parse(ctx, texts[side], lens[side], alphabet, &r, dst[side]);
-        if (rc != GBA_ECAPACITY) return rc == GBA_OK ? fail(ctx, GBA_EINVAL, "FASTA text without records") : rc;
-        const size_t cap = static_cast<size_t>(r.num) + 1;
-        off[side].assign(cap, 0);
-        ib[side].assign(cap, 0);
-        ie[side].assign(cap, 0);
-        r = gba_seq_records{};
-        r.record_capacity = int64_t(cap);
-        r.id_begin = ib[side].data();
-        r.id_end = ie[side].data();
-        r.seq_off = off[side].data();
-        if ((rc = fasta_parse(ctx, texts[side], lens[side], alphabet, &r, dst[side]))) return rc;
+        if (int rc = fasta_parse(ctx, texts[side], lens[side], alphabet, &r, dst[side], &rec[side])) return rc;
     }
+    std::vector<int64_t> off[2] = {std::move(rec[0].seq_off), std::move(rec[1].seq_off)};
     const int64_t nh = int64_t(off[0].size()) - 1, nv = int64_t(off[1].size()) - 1;
     *num_pairs = nv;
     if (h_shared ? nh != 1 : nh != nv)
