@@ -12,10 +12,17 @@ position.  A step is one pass of the engine over the whole batch.
   of the codes and offsets, the kernels, and the device->host copy of scores and end positions
   are inside the timed region (wall clock around the blocking call).
 * ``roofline``: the DP kernel against the measured 32-bit integer add/max rate (the DP is
-  integer-issue bound; algorithmic ops per cell are stated in the design doc).
+  integer-issue bound; add and max each count one op: affine global 9 ops per cell, affine
+  local 10, linear global 5, linear local 6).
+* ``plain_gpu_form``: the same kernels launched once per 8-residue length bucket (no sorting
+  across buckets, no split slots, no autotune, no graph) -- what the persistent, length-sorted,
+  graph-replayed batch is compared with.
+* ``parity``: every pair of the timed runs (device-resident and end to end) compared with the
+  oracle, outside the timed regions; the run exits non-zero when any result differs.
 * ``cpu_baseline``: the oracle (CPU restatement of the reference, OpenMP over all host cores)
   timed on a sample of the same workload.
-``--impl reference`` times that CPU implementation alone, in the same JSON shape.
+``--impl reference`` times the reference's own batch call (SeqAn compiled from its headers on
+this host) when its headers are available, else the CPU restatement, in the same JSON shape.
 """
 from __future__ import annotations
 
@@ -630,6 +637,80 @@ def concat(seqs):
     return np.concatenate(seqs).astype(np.uint8), off
 
 
+def fetch_results(L, ctx, plan, npairs, d_score, d_eh, d_ev, spec, oh, ov):
+    """Copies a device-resident run's results back: scores and best cells from the device
+    buffers, begin positions, segments and CIGARs from the plan (gba_plan_fetch)."""
+    h = ctx.handle
+    out = {}
+    for key, ptr in (("score", d_score), ("end_h", d_eh), ("end_v", d_ev)):
+        a = np.zeros(npairs, np.int32)
+        ctx.check(L.gba_copy_to_host(h, a.ctypes.data, ptr, 4 * npairs), "copy")
+        out[key] = a
+    if spec.traceback:
+        from seqan_gb300 import _native as N
+        cap = int(((oh[1:] - oh[:-1]) + (ov[1:] - ov[:-1]) + 4).sum()) + 1
+        r = N.GbaResult()
+        out["begin_h"], out["begin_v"] = np.zeros(npairs, np.int32), np.zeros(npairs, np.int32)
+        out["segments"] = np.zeros((cap, 4), np.uint32)
+        out["segment_offsets"] = np.zeros(npairs + 1, np.int64)
+        r.begin_h, r.begin_v = out["begin_h"].ctypes.data, out["begin_v"].ctypes.data
+        r.segments, r.segment_capacity = out["segments"].ctypes.data, cap
+        r.segment_offsets = out["segment_offsets"].ctypes.data
+        if spec.cigar:
+            out["cigar"] = np.zeros(cap, np.uint32)
+            out["cigar_offsets"] = np.zeros(npairs + 1, np.int64)
+            r.cigar, r.cigar_capacity, r.cigar_offsets = out["cigar"].ctypes.data, cap, out["cigar_offsets"].ctypes.data
+        ctx.check(L.gba_plan_fetch(h, plan, C.byref(r)), "gba_plan_fetch")
+        out["segments"] = out["segments"][:int(out["segment_offsets"][-1])]
+        if spec.cigar:
+            out["cigar"] = out["cigar"][:int(out["cigar_offsets"][-1])]
+    return out
+
+
+def host_results(res, npairs, spec, as_np):
+    """Copies of the results gba_align_batch (or a sibling call) left in pinned host buffers."""
+    out = {k: as_np(getattr(res, k), npairs, np.int32).copy() for k in ("score", "end_h", "end_v")}
+    if spec.traceback:
+        out["begin_h"] = as_np(res.begin_h, npairs, np.int32).copy()
+        out["begin_v"] = as_np(res.begin_v, npairs, np.int32).copy()
+        out["segment_offsets"] = as_np(res.segment_offsets, npairs + 1, np.int64).copy()
+        tot = int(out["segment_offsets"][-1])
+        out["segments"] = as_np(res.segments, 4 * tot, np.uint32).reshape(-1, 4).copy()
+        if spec.cigar:
+            out["cigar_offsets"] = as_np(res.cigar_offsets, npairs + 1, np.int64).copy()
+            out["cigar"] = as_np(res.cigar, int(out["cigar_offsets"][-1]), np.uint32).copy()
+    return out
+
+
+def results_equal(a, b) -> bool:
+    return a.keys() == b.keys() and all(np.array_equal(a[k], b[k]) for k in a)
+
+
+def check_parity(spec: Spec, runs: dict):
+    """Compares every pair of the timed batch with the oracle (all host threads): scores and best
+    cells, and for traceback workloads begin positions, TraceSegment_ lists and CIGAR words.  Runs
+    outside every timed region."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    ref = O.oracle_batch(oracle_problem(spec), spec.H, spec.V, traceback=spec.traceback,
+                         threads=os.cpu_count() or 1, flat=True)
+    want = {"score": ref.score, "end_h": ref.end_h, "end_v": ref.end_v}
+    if spec.traceback:
+        want.update(begin_h=ref.begin_h, begin_v=ref.begin_v, segments=ref.seg_flat, segment_offsets=ref.seg_offsets)
+        if spec.cigar:
+            want["cigar"], want["cigar_offsets"] = O.cigar_words_flat(ref.seg_flat, ref.seg_offsets)
+    out = {"pairs_checked": len(spec.H), "checked": sorted(want), "oracle_s": round(time.perf_counter() - t0, 2)}
+    ok = True
+    for name, got in runs.items():
+        diff = [k for k in want if not np.array_equal(np.asarray(got[k]), np.asarray(want[k]).astype(got[k].dtype))]
+        bad = int(np.count_nonzero((got["score"] != want["score"]) | (got["end_h"] != want["end_h"]) |
+                                   (got["end_v"] != want["end_v"])))
+        out[name] = {"equal": not diff, "fields_differing": diff, "pairs_with_score_or_end_differing": bad}
+        ok = ok and not diff
+    out["equal"] = ok
+    return out
+
+
 def cpu_baseline(spec: Spec, seconds_target: float = 10.0):
     """Times the oracle (CPU restatement, all host threads) on a sample of the workload."""
     from oracle import oracle as O
@@ -656,34 +737,88 @@ def cpu_baseline(spec: Spec, seconds_target: float = 10.0):
             "cells": cells, "seconds": best}
 
 
-def run_reference(args, rank):
-    if rank != 0:
-        return
-    spec = make_workload(args.workload)
+def _reference_call(spec: Spec, H, V, threads: int, lib):
+    """One call of the reference's own batch interface, compiled from its headers on this host:
+    globalAlignmentScore(ExecutionPolicy<Parallel, Vectorial>, ...) for score-only workloads,
+    globalAlignment / localAlignment over StringSet<Gaps> (+ getCigarString) for the others."""
     from oracle import oracle as O
     pb = oracle_problem(spec)
+    if spec.traceback:
+        return O.ref_batch_gaps(pb, H, V, threads=threads, cigar=spec.cigar, lib=lib, decode=False)[0]
+    return O.ref_batch_score(pb, H, V, threads=threads, lib=lib)
+
+
+def run_reference(args, rank):
+    """The reference arm: SeqAn's own batch call on all host cores when its headers are available
+    (compiled here by oracle/ref/Makefile's bench target), else the CPU restatement."""
+    if rank != 0:
+        return
+    import platform
+    spec = make_workload(args.workload)
+    from oracle import oracle as O
     threads = os.cpu_count() or 1
-    n = min(len(spec.H), args.ref_pairs)
+    lib = None
+    why = None
+    try:
+        if O.build_ref_bench():
+            lib = O.libref_bench()
+        else:
+            why = "no copy of the reference's headers (baseline/_ref/include) on this host"
+    except (subprocess.CalledProcessError, OSError) as e:
+        why = f"compiling the reference failed: {e}"
+    pb = oracle_problem(spec)
+    N = len(spec.H)
+
+    def call(n):
+        if lib is not None:
+            return _reference_call(spec, spec.H[:n], spec.V[:n], threads, lib)
+        return O.oracle_batch(pb, spec.H[:n], spec.V[:n], traceback=spec.traceback, threads=threads).score
+
+    # Size a step to about 4 s of host work: the whole workload when it fits.
+    n0 = min(N, 4000)
+    t0 = time.perf_counter()
+    call(n0)
+    dt = time.perf_counter() - t0
+    cells0 = algorithmic_cells(Spec(spec.H[:n0], spec.V[:n0], spec.score, spec.mode, spec.kind, spec.config,
+                                    spec.band))
+    rate = cells0 / max(dt, 1e-6)
+    n = N
+    if algorithmic_cells(spec) / rate > 4.0:
+        n = int(min(N, max(n0, N * 4.0 * rate / algorithmic_cells(spec))))
     H, V = spec.H[:n], spec.V[:n]
     cells = algorithmic_cells(Spec(H, V, spec.score, spec.mode, spec.kind, spec.config, spec.band))
     for _ in range(args.warmup):
-        O.oracle_batch(pb, H, V, traceback=spec.traceback, threads=threads)
+        call(n)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        O.oracle_batch(pb, H, V, traceback=spec.traceback, threads=threads)
+        got = call(n)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     gcups = cells * len(times) / total / 1e9
+    # The reference's scores on a sample against the oracle (outside the timed steps).
+    m = min(n, 2000)
+    agrees = bool(np.array_equal(np.asarray(got[:m], np.int32), O.oracle_batch(pb, H[:m], V[:m], threads=threads).score))
+    if lib is not None:
+        simd = int(lib.ref_simd_bytes())
+        kind = "reference"
+        sample = (f"SeqAn compiled from its own headers on this host ({platform.machine()}, g++ -O3, "
+                  f"{'SIMD vectors of ' + str(simd) + ' bytes' if simd else 'no SIMD: the Vectorial policy runs its scalar DP'}"
+                  f"), ExecutionPolicy<Parallel, Vectorial> with {threads} threads, "
+                  f"{'globalAlignment/localAlignment over StringSet<Gaps>' + (' + getCigarString' if spec.cigar else '') if spec.traceback else 'globalAlignmentScore'}"
+                  f"; {n} of {N} pairs per step")
+    else:
+        kind = "port"
+        sample = (f"the reference could not run here ({why}); its CPU restatement oracle/seqan_oracle.c with OpenMP "
+                  f"over {threads} threads; {n} of {N} pairs per step")
     line = {"metric": "GCUPS, batched affine DNA align", "value": gcups, "unit": "GCUPS", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int16" if spec.score.bits == 16 else "int32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "pairs_per_step": n, "description": WORKLOADS[args.workload]},
-            "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": "port",
-                             "sample": f"first {n} pairs of the workload per step; the reference's own SIMD "
-                                       "path is x86-only and cannot build on the Arm host, so its CPU "
-                                       "restatement (oracle/seqan_oracle.c) runs with OpenMP"},
+            "config": {"workload": args.workload, "pairs_per_step": n, "same_config": n == N,
+                       "description": WORKLOADS[args.workload]},
+            "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": kind, "sample": sample,
+                             "scores_agree_with_oracle_on_first_pairs": {"pairs": m, "equal": agrees}},
             "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1112,6 +1247,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-bucket comparison")
     ap.add_argument("--pairs", type=int, default=0, help="use only the first N pairs (small profiling cases)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison of the timed results")
     ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16", "plain"],
                     help="auto: persistent packed 16-bit kernel (32-row strips), graph-replayed; "
                          "plain: general kernel, one launch per length bucket")
@@ -1277,31 +1413,46 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = cells * world * args.steps / (total_ms * 1e-3) / 1e9
+    # The timed runs' results (outside the timed region), for the parity check against the oracle.
+    value_out = fetch_results(L, ctx, plan, npairs, d_score, d_eh, d_ev, spec, oh, ov)
 
-    # The plain GPU form on the same device-resident batch: the general one-pair-per-thread
-    # kernel, one launch per 8-residue length bucket (comparison for the persistent form).
-    plain = None
-    if args.kernel == "auto" and not args.no_plain and not spec.traceback and spec.band is None:
-        pparams = sg.align.make_params(score, mode, spec.config, None, N.GBA_OUT_SCORE | N.GBA_OUT_END,
-                                       alphabet_size=spec.alphabet_size,
-                                       flags=N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH)
-        pplan = C.c_void_p()
-        ctx.check(L.gba_plan_create(h, C.byref(pparams), C.byref(host_batch), C.byref(pplan)), "plain plan")
-        ctx.check(L.gba_plan_execute(h, pplan, C.byref(dev_batch), C.byref(dev_res)), "plain")
-        ctx.check(L.gba_synchronize(h), "sync")
-        pms = []
-        for _ in range(2):
-            flush_l2()
-            ctx.check(L.gba_timer_start(h), "timer")
+    # The plain GPU form on the same device-resident batch (comparison for the persistent form):
+    # the same kernels, launched once per 8-residue length bucket of max(|H|, |V|), pairs in input
+    # order inside a bucket, no split slots, default tiling, no autotune, no CUDA graph.  A second
+    # plain form runs the one-pair-per-thread 32-bit kernel per bucket (the form of a first GPU
+    # port).  Each must give the same results as the timed runs.
+    plain = plain_strip = None
+    if args.kernel == "auto" and not args.no_plain and spec.band is None:
+        def time_plain(extra_flags):
+            pparams = sg.align.make_params(score, mode, spec.config, None, outputs, alphabet_size=spec.alphabet_size,
+                                           flags=N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH | extra_flags)
+            pplan = C.c_void_p()
+            ctx.check(L.gba_plan_create(h, C.byref(pparams), C.byref(host_batch), C.byref(pplan)), "plain plan")
             ctx.check(L.gba_plan_execute(h, pplan, C.byref(dev_batch), C.byref(dev_res)), "plain")
-            ctx.check(L.gba_timer_stop(h, C.byref(ms)), "timer")
-            pms.append(ms.value)
-        plain_launches = ctx.stats().kernel_launches
-        L.gba_plan_destroy(h, pplan)
-        pg = cells / (sum(pms) / len(pms) * 1e-3) / 1e9
-        plain = {"value": pg, "unit": "GCUPS", "launches_per_step": plain_launches,
-                 "speedup_of_value": value / pg,
-                 "form": "general one-pair-per-thread kernel, one launch per 8-residue length bucket"}
+            ctx.check(L.gba_synchronize(h), "sync")
+            pms, pdp = [], []
+            for _ in range(3):
+                flush_l2()
+                ctx.check(L.gba_timer_start(h), "timer")
+                ctx.check(L.gba_plan_execute(h, pplan, C.byref(dev_batch), C.byref(dev_res)), "plain")
+                ctx.check(L.gba_timer_stop(h, C.byref(ms)), "timer")
+                pms.append(ms.value)
+                pdp.append(ctx.stats().dp_kernel_ms)
+            pst = ctx.stats()
+            same = results_equal(fetch_results(L, ctx, pplan, npairs, d_score, d_eh, d_ev, spec, oh, ov), value_out)
+            L.gba_plan_destroy(h, pplan)
+            pg = cells / (sum(pms) / len(pms) * 1e-3) / 1e9
+            return {"value": pg, "unit": "GCUPS", "ms_per_step": sum(pms) / len(pms),
+                    "dp_kernel_ms": sum(pdp) / len(pdp), "launches_per_step": pst.kernel_launches,
+                    "kernel": kernel_label(pst.dp_kernels), "speedup_of_value": value / pg,
+                    "results_equal_timed_runs": same}
+        plain = time_plain(0)
+        plain["form"] = ("the same kernels as the timed runs, one launch per 8-residue bucket of max(|H|,|V|), input "
+                         "order inside a bucket, no split slots, default tiling, no autotune, no CUDA graph")
+        if not spec.traceback:
+            plain_strip = time_plain(N.GBA_FLAG_GENERAL_KERNEL)
+            plain_strip["form"] = "one-pair-per-thread int32 kernel (k_dp_strip), one launch per 8-residue bucket"
+        # Restore the timed results in the device buffers (the plain runs wrote the same values).
 
     # End to end through the public C-ABI call with host buffers.
     host_res = N.GbaResult()
@@ -1330,6 +1481,7 @@ def main():
         e2e_s.append(time.perf_counter() - t0)
     est = ctx.stats()
     e2e_launches = est.kernel_launches
+    e2e_out = host_results(host_res, npairs, spec, as_np)
     # The same call on String<Dna, Packed<>> host words (2 bits per residue) from pinned memory:
     # gba_align_packed uploads the words and unpacks them on the device.
     e2e_packed = None
@@ -1350,7 +1502,9 @@ def main():
             t0 = time.perf_counter()
             ctx.check(L.gba_align_packed(h, C.byref(params), C.byref(ph), C.byref(pv), 0, C.byref(host_res)), "pk")
             pk_s.append(time.perf_counter() - t0)
+        pk_same = results_equal(host_results(host_res, npairs, spec, as_np), e2e_out)
         e2e_packed = {"value": cells * world * len(pk_s) / sum(pk_s) / 1e9, "unit": "GCUPS",
+                      "results_equal_codes_path": pk_same,
                       "h2d_bytes_per_step": int(hw.nbytes + vw.nbytes + hwo.nbytes + vwo.nbytes),
                       "d2h_bytes_per_step": 3 * npairs * 4, "ms_per_step": 1e3 * sum(pk_s) / len(pk_s),
                       "input": "String<Dna, Packed<>> host words (gba_align_packed)"}
@@ -1376,7 +1530,9 @@ def main():
             t0 = time.perf_counter()
             fa_call()
             fa_s.append(time.perf_counter() - t0)
+        fa_same = npairs_out.value == npairs and results_equal(host_results(host_res, npairs, spec, as_np), e2e_out)
         e2e_fasta = {"value": cells * world * len(fa_s) / sum(fa_s) / 1e9, "unit": "GCUPS",
+                     "results_equal_codes_path": fa_same,
                      "h2d_bytes_per_step": len(th) + len(tv), "d2h_bytes_per_step": 3 * npairs * 4,
                      "ms_per_step": 1e3 * sum(fa_s) / len(fa_s),
                      "input": "two FASTA texts, 60-column lines (gba_align_fasta)"}
@@ -1440,6 +1596,10 @@ def main():
         line["e2e_fasta"] = e2e_fasta
     if plain:
         line["plain_gpu_form"] = plain
+    if plain_strip:
+        line["plain_strip_form"] = plain_strip
+    if rank == 0 and not args.no_parity:
+        line["parity"] = check_parity(spec, {"value_runs": value_out, "e2e_runs": e2e_out})
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(spec)
     if rank == 0 and world == 1 and args.workload == "affine_dna_100k" and not args.no_serving and not args.pairs:
@@ -1463,6 +1623,12 @@ def main():
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+    mismatches = [k for k, v in (("parity", line.get("parity")), ("plain_gpu_form", plain), ("plain_strip_form", plain_strip),
+                                 ("e2e_packed", e2e_packed), ("e2e_fasta", e2e_fasta))
+                  if v and not v.get("equal", v.get("results_equal_timed_runs", v.get("results_equal_codes_path", True)))]
+    if mismatches:
+        print(f"results differ: {mismatches}", file=sys.stderr, flush=True)
+        sys.exit(1)
 
 
 if __name__ == "__main__":

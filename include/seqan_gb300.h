@@ -60,7 +60,9 @@ enum {
     GBA_PAIR_INVALID = 1,   /* empty sequence or band outside the matrix: score = numeric min */
     GBA_PAIR_PROMOTED = 2,  /* 16-bit cells were requested but the pair may leave the exact
                                int16 range; it ran with 32-bit cells (exact result) */
-    GBA_PAIR_FAILED = 3     /* serving only: the request's batch failed (no result) */
+    GBA_PAIR_FAILED = 3,    /* serving only: the request's batch failed (no result) */
+    GBA_PAIR_SKIPPED = 4    /* gba_align_score_noalloc only: |H| above the call's max_h_len, not
+                               computed (score = numeric min) */
 };
 
 enum { GBA_GLOBAL = 0, GBA_LOCAL = 1 };
@@ -95,8 +97,14 @@ typedef struct {
     int32_t score_bits;        /* 16 or 32: the reference's TScoreValue width */
     int32_t outputs;           /* GBA_OUT_* bits */
     int32_t flags;             /* GBA_FLAG_* kernel selection (0 = automatic) */
-    int32_t reserved[2];
+    int32_t tile_variant;      /* packed kernel tiling: 0 = automatic (tuning table / autotune /
+                                  default); v in 1..GBA_TILE_VARIANTS forces variant v - 1 */
+    int32_t reserved;
 } gba_params;
+
+/* Tiling variants of the packed kernel (rows per register strip x minimum resident blocks per
+ * SM): 1 = 32 x 2, 2 = 32 x 3, 3 = 24 x 3, 4 = 24 x 4, 5 = 16 x 4. */
+#define GBA_TILE_VARIANTS 5
 
 /* Kernel selection flags (gba_params.flags); results are identical either way.
  * With equality scoring the engine uses its packed two-pairs-per-thread 16-bit kernel when
@@ -107,8 +115,11 @@ typedef struct {
 enum {
     GBA_FLAG_GENERAL_KERNEL = 1,   /* force the one-pair-per-thread 32-bit kernel */
     GBA_FLAG_STRIP16 = 2,          /* packed kernel with 16-row strips instead of 32 */
-    GBA_FLAG_PLAIN_BUCKETS = 4,    /* the plain GPU form: general kernel, one launch per
-                                      8-residue length bucket (comparison baseline) */
+    GBA_FLAG_PLAIN_BUCKETS = 4,    /* the plain GPU form (comparison baseline): the kernels the
+                                      automatic routing picks, launched once per 8-residue
+                                      bucket of max(|H|, |V|), input order inside a bucket, no
+                                      split slots, default tiling, no graph; with
+                                      GBA_FLAG_GENERAL_KERNEL the one-pair-per-thread kernel */
     GBA_FLAG_NO_GRAPH = 8,         /* launch kernels directly instead of replaying a CUDA graph */
     GBA_FLAG_AUTOTUNE = 16,        /* time the packed kernel's tiling variants on the first run
                                       of a plan and remember the fastest per batch shape */
@@ -302,11 +313,17 @@ GBA_API double gba_clock_seconds(void);
  * GBA_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit; one warp of
  * lanes needs 32 * (max_h_len + 1) * 8 bytes of it, and a max_h_len that does not fit is
  * refused with GBA_ECAPACITY.  Pairs longer than max_h_len are not computed and come back
- * with score numeric_limits<T>::min() and GBA_PAIR_INVALID.  Scores and end positions only
- * (no band, no traceback): the same values gba_align_batch returns.
- * The first call on a device looks up the array's device address; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race and must be
- * serialized by the caller.  Asynchronous on `stream` (a cudaStream_t; NULL = legacy default
+ * with score numeric_limits<T>::min() and GBA_PAIR_SKIPPED; empty pairs get numeric min and
+ * GBA_PAIR_INVALID as in gba_align_batch.  Scores and end positions only (no band, no
+ * traceback); for every pair within max_h_len the score, end positions and status equal
+ * gba_align_batch's.
+ * Set-up: the first call on a device looks up the array's device address.  Under CUDA's lazy
+ * module loading (the default) that is also when the array's memory is committed on the device,
+ * so the first call may allocate and synchronize: make it once at start-up, before any stream
+ * capture and before a host pool takes the GPU's memory; later calls allocate nothing.  All
+ * calls share the array: calls that overlap on the GPU race and must be serialized by the
+ * caller.  An error already pending on the calling thread is left in place and reported as
+ * GBA_ECUDA without a launch.  Asynchronous on `stream` (a cudaStream_t; NULL = legacy default
  * stream). */
 #define GBA_NOALLOC_SCRATCH_BYTES (64u << 20)
 

@@ -115,6 +115,41 @@ def ref_available() -> bool:
     return os.path.exists(REF_LIB)
 
 
+REF_BENCH_LIB = os.path.join(HERE, "_ref", "libseqan_ref_bench.so")
+REF_HEADERS_COPY = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "include")
+_ref_bench = None
+
+
+def build_ref_bench(include: str | None = None) -> str | None:
+    """Builds oracle/_ref/libseqan_ref_bench.so (the reference compiled from its own headers, only
+    the benchmark workloads' call shapes) when missing; returns its path, or None when no copy of
+    the reference's headers is available (SEQAN_INCLUDE, else baseline/_ref/include)."""
+    if os.path.exists(REF_BENCH_LIB):
+        return REF_BENCH_LIB
+    include = include or os.environ.get("SEQAN_INCLUDE") or REF_HEADERS_COPY
+    if not os.path.isdir(os.path.join(include, "seqan")):
+        return None
+    subprocess.check_call(["make", "-C", os.path.join(HERE, "ref"), "bench", f"-j{os.cpu_count() or 4}",
+                           f"SEQAN_INCLUDE={os.path.abspath(include)}"], stdout=subprocess.DEVNULL)
+    return REF_BENCH_LIB
+
+
+def libref_bench():
+    """The benchmark-shape reference library (see build_ref_bench), with libref()'s signatures."""
+    global _ref_bench
+    if _ref_bench is None:
+        lib = C.CDLL(REF_BENCH_LIB)
+        lib.ref_batch_score.argtypes = [C.POINTER(RefParams), C.c_int64, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ref_batch_gaps.argtypes = [C.POINTER(RefParams), C.c_int64, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_int64]
+        lib.ref_has_shape.argtypes = [C.c_int32, C.POINTER(RefParams)]
+        lib.ref_simd_bytes.restype = C.c_int32
+        _ref_bench = lib
+    return _ref_bench
+
+
 def libref():
     global _ref
     if _ref is None:
@@ -178,10 +213,15 @@ class BatchResult:
     begin_v: np.ndarray | None = None
     valid: np.ndarray | None = None
     segments: list = field(default_factory=list)   # per pair: list of (h, v, len, type)
+    seg_flat: np.ndarray | None = None             # flat=True: [total, 4] uint32, pairs back to back
+    seg_offsets: np.ndarray | None = None          # flat=True: [n + 1] int64
 
 
-def oracle_batch(pb: Problem, H, V, traceback: bool = False, threads: int = 0) -> BatchResult:
-    """Runs the C restatement on pairs (H[k], V[k])."""
+def oracle_batch(pb: Problem, H, V, traceback: bool = False, threads: int = 0, flat: bool = False) -> BatchResult:
+    """Runs the C restatement on pairs (H[k], V[k]).
+
+    flat=True returns the segments as one dense array (seg_flat, seg_offsets) in the layout of the
+    engine's gba_result instead of per-pair tuple lists (for batches of a million pairs)."""
     lib = liboracle()
     n = len(H)
     sh, oh = concat(H)
@@ -201,11 +241,47 @@ def oracle_batch(pb: Problem, H, V, traceback: bool = False, threads: int = 0) -
     arr = np.frombuffer(out, dtype=np.int32).reshape(-1, 7)[:n]
     res = BatchResult(score=arr[:, 0].copy(), end_h=arr[:, 1].copy(), end_v=arr[:, 2].copy(),
                       begin_h=arr[:, 3].copy(), begin_v=arr[:, 4].copy(), valid=arr[:, 6].copy())
-    if traceback:
+    if traceback and flat:
+        cnt = np.maximum(arr[:, 5], 0).astype(np.int64)
+        res.seg_offsets = np.zeros(n + 1, dtype=np.int64)
+        np.cumsum(cnt, out=res.seg_offsets[1:])
+        pair = np.repeat(np.arange(n, dtype=np.int64), cnt)
+        local = np.arange(int(res.seg_offsets[-1]), dtype=np.int64) - res.seg_offsets[pair]
+        res.seg_flat = segs[seg_off[pair] + local].copy()
+    elif traceback:
         for k in range(n):
             cnt = arr[k, 5]
             res.segments.append([tuple(int(x) for x in segs[seg_off[k] + i]) for i in range(max(cnt, 0))])
     return res
+
+
+def cigar_words_flat(seg_flat, seg_offsets, spliced_gap_thresh: int = 20):
+    """CIGARs of many pairs at once, as BAM words (length << 4 | op index into "MIDNSHP=X"), from
+    dense TraceSegment_ lists (traceback order): the same operations as cigar_string -- the
+    segments from the alignment begin on, runs of one operation joined, D runs of at least
+    spliced_gap_thresh as N (bam_io/cigar.h:261-339).  Returns (words, offsets[n + 1])."""
+    seg_flat = np.asarray(seg_flat, dtype=np.uint32).reshape(-1, 4)
+    off = np.asarray(seg_offsets, dtype=np.int64)
+    n = len(off) - 1
+    cnt = np.diff(off)
+    total = int(off[-1])
+    if total == 0:
+        return np.zeros(0, np.uint32), np.zeros(n + 1, np.int64)
+    pair = np.repeat(np.arange(n, dtype=np.int64), cnt)
+    i = np.arange(total, dtype=np.int64)
+    rs = seg_flat[2 * off[pair] + cnt[pair] - 1 - i]          # each pair's list reversed
+    tp = rs[:, 3]
+    op = np.where(tp == SEG_DIAGONAL, 0, np.where(tp == SEG_VERTICAL, 1, 2)).astype(np.int64)
+    start = np.ones(total, dtype=bool)
+    start[1:] = (op[1:] != op[:-1]) | (pair[1:] != pair[:-1])
+    first = np.nonzero(start)[0]
+    run_len = np.add.reduceat(rs[:, 2].astype(np.int64), first)
+    run_op = op[first]
+    run_op = np.where((run_op == 2) & (run_len >= spliced_gap_thresh), 3, run_op)
+    words = ((run_len << 4) | run_op).astype(np.uint32)
+    coff = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(np.bincount(pair[first], minlength=n), out=coff[1:])
+    return words, coff
 
 
 def _ref_params(pb: Problem, threads: int) -> RefParams:
@@ -227,8 +303,8 @@ def ref_has_shape(kind: int, pb: Problem) -> bool:
     return bool(libref().ref_has_shape(kind, C.byref(p)))
 
 
-def ref_batch_score(pb: Problem, H, V, threads: int = 1) -> np.ndarray:
-    lib = libref()
+def ref_batch_score(pb: Problem, H, V, threads: int = 1, lib=None) -> np.ndarray:
+    lib = lib or libref()
     n = len(H)
     sh, oh = concat(H)
     sv, ov = concat(V)
@@ -240,9 +316,10 @@ def ref_batch_score(pb: Problem, H, V, threads: int = 1) -> np.ndarray:
     return out[:n]
 
 
-def ref_batch_gaps(pb: Problem, H, V, threads: int = 1, cigar: bool = False):
-    """Returns (scores, clip[n,4] = hb,he,vb,ve, rows[list of (rowH, rowV)], cigars)."""
-    lib = libref()
+def ref_batch_gaps(pb: Problem, H, V, threads: int = 1, cigar: bool = False, lib=None, decode: bool = True):
+    """Returns (scores, clip[n,4] = hb,he,vb,ve, rows[list of (rowH, rowV)], cigars); decode=False
+    skips turning the rows and CIGARs into Python strings (returns None for both)."""
+    lib = lib or libref()
     n = len(H)
     sh, oh = concat(H)
     sv, ov = concat(V)
@@ -259,6 +336,8 @@ def ref_batch_gaps(pb: Problem, H, V, threads: int = 1, cigar: bool = False):
     if rc != 0:
         raise RuntimeError(f"reference call shape not instantiated (rc={rc}): {pb}")
     arr = np.frombuffer(out, dtype=np.int32).reshape(-1, 5)[:n]
+    if not decode:
+        return arr[:, 0].copy(), arr[:, 1:5].copy(), None, None
     row_strs = []
     for k in range(n):
         raw = bytes(rows[row_off[k]:row_off[k + 1]]).split(b"\0", 1)[0].decode()

@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", 
 # Status codes (include/seqan_gb300.h)
 GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY, GBA_EPARSE = \
     range(9)
-GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED, GBA_PAIR_FAILED = 0, 1, 2, 3
+GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED, GBA_PAIR_FAILED, GBA_PAIR_SKIPPED = 0, 1, 2, 3, 4
 GBA_GLOBAL, GBA_LOCAL = 0, 1
 GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE = 0, 1, 2
 GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
@@ -60,7 +60,7 @@ class GbaParams(C.Structure):
                 ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
                 ("gap_extend", C.c_int32), ("matrix", C.c_void_p), ("alphabet_size", C.c_int32),
                 ("score_bits", C.c_int32), ("outputs", C.c_int32), ("flags", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("tile_variant", C.c_int32), ("reserved", C.c_int32)]
 
 
 class GbaBatch(C.Structure):

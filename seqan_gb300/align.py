@@ -162,7 +162,7 @@ ALPHABET_SIZE = {"dna": 4, "dna5": 5, "aa": 27}
 def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None,
                 traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None,
                 alphabet_size: int | None = None, flags: int = 0, packed_bits: int | None = None,
-                fasta_texts=None) -> BatchOutput:
+                fasta_texts=None, tile_variant: int = 0) -> BatchOutput:
     """Aligns lists of code arrays through gba_align_batch.
 
     alphabet_size bounds the codes (the reference's ValueSize of the alphabet); when None it is
@@ -180,6 +180,7 @@ def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=No
     if alphabet_size is None:
         alphabet_size = int(max(sh.max(initial=0), sv.max(initial=0))) + 1 if n else 0
     params = make_params(score, mode, config, band, outputs, alphabet_size, flags)
+    params.tile_variant = tile_variant
     b = N.GbaBatch(n, _vp(sh), _vp(oh), _vp(sv), _vp(ov), 1 if h_shared else 0, 0)
     res = BatchOutput(score=np.zeros(n, np.int32), end_h=np.zeros(n, np.int32), end_v=np.zeros(n, np.int32),
                       status=np.zeros(n, np.int32))
@@ -215,6 +216,75 @@ def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=No
         return res
     ctx.check(N.lib().gba_align_batch(ctx.handle, C.byref(params), C.byref(b), C.byref(r)), "gba_align_batch")
     return res
+
+
+def align_codes_resident(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None, traceback=False,
+                         cigar=False, alphabet_size: int | None = None, flags: int = 0, tile_variant: int = 0,
+                         runs: int = 2, ctx: N.Context | None = None) -> BatchOutput:
+    """align_codes on the device-resident path: the codes are copied to HBM once, a plan is built
+    from the host offsets (gba_plan_create) and run `runs` times on the device buffers
+    (gba_plan_execute; from the second run on, a CUDA-graph replay unless GBA_FLAG_NO_GRAPH), and
+    the last run's results are copied back (gba_plan_fetch for segments and CIGARs)."""
+    ctx = ctx or N.default_context()
+    L = N.lib()
+    h = ctx.handle
+    n = len(codes_v)
+    sh, oh = _concat(codes_h)
+    sv, ov = _concat(codes_v)
+    outputs = N.GBA_OUT_SCORE | N.GBA_OUT_END
+    if traceback or cigar:
+        outputs |= N.GBA_OUT_SEGMENTS
+    if cigar:
+        outputs |= N.GBA_OUT_CIGAR
+    if alphabet_size is None:
+        alphabet_size = int(max(sh.max(initial=0), sv.max(initial=0))) + 1 if n else 0
+    params = make_params(score, mode, config, band, outputs, alphabet_size, flags)
+    params.tile_variant = tile_variant
+    host_batch = N.GbaBatch(n, _vp(sh), _vp(oh), _vp(sv), _vp(ov), 0, 0)
+    bufs = []
+
+    def dev(nbytes):
+        ptr = C.c_void_p()
+        ctx.check(L.gba_device_alloc(h, C.byref(ptr), max(int(nbytes), 16)), "gba_device_alloc")
+        bufs.append(ptr)
+        return ptr
+
+    plan = C.c_void_p()
+    try:
+        d_sh, d_sv = dev(sh.nbytes), dev(sv.nbytes)
+        ctx.check(L.gba_copy_to_device(h, d_sh, _vp(sh), sh.nbytes), "copy")
+        ctx.check(L.gba_copy_to_device(h, d_sv, _vp(sv), sv.nbytes), "copy")
+        d_score, d_eh, d_ev = dev(4 * n), dev(4 * n), dev(4 * n)
+        ctx.check(L.gba_plan_create(h, C.byref(params), C.byref(host_batch), C.byref(plan)), "gba_plan_create")
+        dev_batch = N.GbaBatch(n, d_sh, None, d_sv, None, 0, 0)
+        dres = N.GbaResult()
+        dres.score, dres.end_h, dres.end_v = d_score, d_eh, d_ev
+        for _ in range(max(1, runs)):
+            ctx.check(L.gba_plan_execute(h, plan, C.byref(dev_batch), C.byref(dres)), "gba_plan_execute")
+        ctx.check(L.gba_synchronize(h), "gba_synchronize")
+        res = BatchOutput(score=np.zeros(n, np.int32), end_h=np.zeros(n, np.int32), end_v=np.zeros(n, np.int32),
+                          status=np.zeros(n, np.int32))
+        for arr, ptr in ((res.score, d_score), (res.end_h, d_eh), (res.end_v, d_ev)):
+            ctx.check(L.gba_copy_to_host(h, _vp(arr), ptr, 4 * n), "copy")
+        if traceback or cigar:
+            cap = int(((oh[1:] - oh[:-1]) + (ov[1:] - ov[:-1]) + 4).sum()) + 1
+            res.begin_h, res.begin_v = np.zeros(n, np.int32), np.zeros(n, np.int32)
+            res.segments = np.zeros((cap, 4), np.uint32)
+            res.segment_offsets = np.zeros(n + 1, np.int64)
+            r = N.GbaResult()
+            r.begin_h, r.begin_v = _vp(res.begin_h), _vp(res.begin_v)
+            r.segments, r.segment_capacity, r.segment_offsets = _vp(res.segments), cap, _vp(res.segment_offsets)
+            if cigar:
+                res.cigar = np.zeros(cap, np.uint32)
+                res.cigar_offsets = np.zeros(n + 1, np.int64)
+                r.cigar, r.cigar_capacity, r.cigar_offsets = _vp(res.cigar), cap, _vp(res.cigar_offsets)
+            ctx.check(L.gba_plan_fetch(h, plan, C.byref(r)), "gba_plan_fetch")
+        return res
+    finally:
+        if plan:
+            L.gba_plan_destroy(h, plan)
+        for ptr in bufs:
+            L.gba_device_free(h, ptr)
 
 
 def _band(args):

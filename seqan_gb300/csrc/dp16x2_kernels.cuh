@@ -162,7 +162,9 @@ __global__ void __launch_bounds__(128) k_pack16(Dp16Args a)
 {
     const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= a.num_slots) return;
-    pack_slot(a, a.slots[s], s >> 5, int(s & 31));
+    const Slot16 sl = a.slots[s];
+    if (sl.pa < 0) return;   // padding slot of the plain per-bucket form
+    pack_slot(a, sl, s >> 5, int(s & 31));
 }
 
 constexpr int kBndAhead = 4;   // columns between a boundary load and its use

@@ -122,8 +122,10 @@ struct gba_plan {
     int64_t tune_key = 0;
     int32_t launches = 0;           // kernels one run launches
     int err_slot = 0;               // word of the context's error buffer this plan's kernels use
-    // Plain per-bucket mode: general kernel launched once per length bucket.
-    std::vector<int64_t> bucket_start, bucket_count;
+    // Plain per-bucket mode: one launch per 8-residue length bucket.  bucket_*: slot ranges of
+    // the one-pair-per-thread kernel; b16_*: slot ranges of the packed kernel; wb_*: task
+    // ranges of the warp kernel.
+    std::vector<int64_t> bucket_start, bucket_count, b16_start, b16_count, wb_start, wb_count;
     // Captured launch sequence (replayed while the device pointers stay the same).
     cudaGraphExec_t graph = nullptr;
     const void *graph_key[5] = {};
@@ -324,6 +326,8 @@ int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
         if (int64_t(p->band_upper) - p->band_lower + 1 > kMaxBandWidth)
             return fail(ctx, GBA_EUNSUPPORTED, "band wider than %d diagonals", kMaxBandWidth);
     }
+    if (p->tile_variant < 0 || p->tile_variant > GBA_TILE_VARIANTS)
+        return fail(ctx, GBA_EINVAL, "tile_variant must be in 0..%d", GBA_TILE_VARIANTS);
     if ((p->outputs & GBA_OUT_CIGAR) && !(p->outputs & GBA_OUT_SEGMENTS))
         return fail(ctx, GBA_EINVAL, "GBA_OUT_CIGAR requires GBA_OUT_SEGMENTS");
     return GBA_OK;
@@ -422,6 +426,7 @@ struct Variant16 {
 };
 constexpr Variant16 kVariants16[] = {{32, 2}, {32, 3}, {24, 3}, {24, 4}, {16, 4}};
 constexpr int kNumVariants16 = int(sizeof(kVariants16) / sizeof(kVariants16[0]));
+static_assert(kNumVariants16 == GBA_TILE_VARIANTS, "tiling variants and the header disagree");
 
 const void *dp16_fn(int v, bool affine)
 {
@@ -526,8 +531,9 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // The packed 16-bit path: global score-only runs with equality scoring over an alphabet of
     // at most 8 codes (the caller's alphabet_size), table entries that fit a byte, and gaps that
     // keep int16 arithmetic exact (checked per pair below).
+    const bool plain = (p->flags & GBA_FLAG_PLAIN_BUCKETS) != 0;
     const bool packed_ok = !plan->local && !plan->traceback && !plan->matrix && !p->band_on &&
-                           !(p->flags & (GBA_FLAG_GENERAL_KERNEL | GBA_FLAG_PLAIN_BUCKETS)) &&
+                           !(p->flags & GBA_FLAG_GENERAL_KERNEL) &&
                            (N >= kPackedMinPairs || (p->flags & (GBA_FLAG_STRIP16 | GBA_FLAG_PACKED))) &&
                            p->alphabet_size >= 1 &&
                            p->alphabet_size <= 8 && p->match >= -128 && p->match <= 127 &&
@@ -536,7 +542,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->rows16 = 32;
     // Pairs that are neither banded nor on the packed path run one warp per pair, unless the
     // one-pair-per-thread kernel is forced.
-    plan->use_warp = !p->band_on && !(p->flags & (GBA_FLAG_GENERAL_KERNEL | GBA_FLAG_PLAIN_BUCKETS));
+    plan->use_warp = !p->band_on && !(p->flags & GBA_FLAG_GENERAL_KERNEL);
     plan->warp_rows = 8;
     // Host arrays live in the plan and keep their capacity between builds (no zero fill).
     auto &keys16 = plan->h_keys16;
@@ -666,7 +672,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     timer.mark("pairs");
     plan->bucket_start.clear();
     plan->bucket_count.clear();
-    if (p->flags & GBA_FLAG_PLAIN_BUCKETS) {
+    if (plain) {
         // The plain GPU form: pairs grouped into 8-residue buckets of max(m, n), in input order
         // inside a bucket, one launch per bucket.  Buckets start on a warp boundary (padding
         // slots hold -1).
@@ -719,14 +725,14 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // Packed path: neighbours in the length-sorted order share a thread; per warp, the code
     // words (4 residues per word, both pairs' codes per byte) and the boundary row are
     // interleaved by lane.
-    sort_desc(keys16, idx16);
+    if (!plain) sort_desc(keys16, idx16);
     timer.mark("sort");
     // Split slots: a thread holds two pairs, so its time is set by its larger pair; pairs whose
     // cells exceed the batch's average work per resident thread (the batch cannot finish before
     // its longest thread) run one per thread as a split slot, two strips at once.  They are a
     // prefix of the length-sorted order, rounded down to whole warps.
     int64_t nsplit = 0;
-    if (!idx16.empty() && !(p->flags & GBA_FLAG_PACKED_NO_SPLIT)) {
+    if (!idx16.empty() && !plain && !(p->flags & GBA_FLAG_PACKED_NO_SPLIT)) {
         if (p->flags & GBA_FLAG_PACKED_SPLIT) {
             nsplit = int64_t(idx16.size());
         } else {
@@ -742,9 +748,43 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     }
     const int64_t rest16 = int64_t(idx16.size()) - nsplit;
     auto &slots16 = plan->h_slots16;
-    slots16.resize(size_t(nsplit + (rest16 + 1) / 2));
+    plan->b16_start.clear();
+    plan->b16_count.clear();
+    if (plain) {
+        // Plain form: two pairs per slot inside each 8-residue bucket (input order), each
+        // bucket's slots padded to whole warps (padding slots have pa = -1 and are never run).
+        std::vector<std::vector<int32_t>> bk;
+        for (int32_t k : idx16) {
+            const int b = std::max(desc[k].m, desc[k].n) / 8;
+            if (b >= int(bk.size())) bk.resize(b + 1);
+            bk[b].push_back(k);
+        }
+        slots16.clear();
+        for (auto &v : bk) {
+            if (v.empty()) continue;
+            const int64_t start = int64_t(slots16.size());
+            for (size_t i = 0; i < v.size(); i += 2) {
+                Slot16 sl{};
+                sl.pa = v[i];
+                sl.pb = i + 1 < v.size() ? v[i + 1] : -1;
+                sl.split = 0;
+                sl.m = desc[sl.pa].m;
+                sl.n = desc[sl.pa].n;
+                if (sl.pb >= 0) {
+                    sl.m = std::max(sl.m, desc[sl.pb].m);
+                    sl.n = std::max(sl.n, desc[sl.pb].n);
+                }
+                slots16.push_back(sl);
+            }
+            plan->b16_start.push_back(start);
+            plan->b16_count.push_back(int64_t(slots16.size()) - start);
+            while (slots16.size() % 32) slots16.push_back(Slot16{-1, -1, 0, 0, 0});
+        }
+    } else {
+        slots16.resize(size_t(nsplit + (rest16 + 1) / 2));
+    }
 #pragma omp parallel for num_threads(plan_threads(int64_t(slots16.size()))) schedule(static)
-    for (size_t q = 0; q < slots16.size(); ++q) {
+    for (size_t q = 0; q < (plain ? size_t(0) : slots16.size()); ++q) {
         Slot16 &sl = slots16[q];
         if (int64_t(q) < nsplit) {
             sl.pa = idx16[q];
@@ -809,7 +849,20 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         bbase.assign(N + 1, 0);
         const int band_rows = 32 * plan->warp_rows;
         wtasks.reserve(idx.size());
+        plan->wb_start.clear();
+        plan->wb_count.clear();
+        int last_bucket = -1;
         for (int32_t k : idx) {
+            if (k < 0) continue;   // plain-form padding slot
+            if (plain) {
+                const int bucket = std::max(desc[k].m, desc[k].n) / 8;
+                if (bucket != last_bucket) {
+                    if (!plan->wb_start.empty()) plan->wb_count.back() = int64_t(wtasks.size()) - plan->wb_start.back();
+                    plan->wb_start.push_back(int64_t(wtasks.size()));
+                    plan->wb_count.push_back(0);
+                    last_bucket = bucket;
+                }
+            }
             const int nb = (desc[k].n + band_rows - 1) / band_rows;
             const bool pipe = nb > 1 && (few_pairs || desc[k].m >= kPipelineMinCols);
             if (pipe) {
@@ -824,6 +877,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                 rbtot += 2 * (int64_t(desc[k].m) + 1);
             }
         }
+        if (!plan->wb_start.empty()) plan->wb_count.back() = int64_t(wtasks.size()) - plan->wb_start.back();
     }
     plan->num_warp_tasks = int64_t(wtasks.size());
     plan->num_band_states = nstates;
@@ -881,7 +935,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         GBA_CUDA(ctx, plan->rowbuf.ensure(size_t(std::max<int64_t>(rbtot, 1)) * sizeof(int2)));
         GBA_CUDA(ctx, plan->band_state.ensure(size_t(std::max<int64_t>(nstates, 1)) * sizeof(BandState)));
         GBA_CUDA(ctx, ctx->err_word.ensure(kMaxChunks * sizeof(int32_t)));
-        GBA_CUDA(ctx, plan->counter_warp.ensure(16));
+        GBA_CUDA(ctx, plan->counter_warp.ensure(std::max<size_t>(16, plan->wb_start.size() * sizeof(int32_t))));
     }
     if (plan->num16 > 0) {
         if ((rc = upload(ctx, plan->slots16, slots16))) return rc;
@@ -890,7 +944,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         if ((rc = upload(ctx, plan->warp_bnd16, wbnd))) return rc;
         GBA_CUDA(ctx, plan->codes16.ensure(size_t(std::max<int64_t>(ctot, 1)) * 4));
         GBA_CUDA(ctx, plan->bnd16.ensure(size_t(std::max<int64_t>(btot, 1)) * sizeof(int2)));
-        GBA_CUDA(ctx, plan->counter16.ensure(16));
+        GBA_CUDA(ctx, plan->counter16.ensure(std::max<size_t>(16, plan->b16_start.size() * sizeof(int32_t))));
         for (int v = 0; v < kNumVariants16; ++v) plan->grid16[v] = persistent_grid(ctx, dp16_fn(v, plan->affine));
         // Variant: forced by flags, else the context's tuning table for this batch shape, else
         // the default; GBA_FLAG_AUTOTUNE times all variants at the first run.
@@ -900,8 +954,12 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         plan->tune_key = (int64_t(plan->affine) << 40) | ((mm / 32) << 20) | (mn / 32);
         plan->variant16 = 0;
         plan->tune_pending = false;
-        if (p->flags & GBA_FLAG_STRIP16) {
+        if (p->tile_variant >= 1 && p->tile_variant <= kNumVariants16) {
+            plan->variant16 = p->tile_variant - 1;
+        } else if (p->flags & GBA_FLAG_STRIP16) {
             plan->variant16 = kNumVariants16 - 1;
+        } else if (plain) {
+            plan->variant16 = 0;
         } else {
             auto it = ctx->tuning.find(plan->tune_key);
             if (it != ctx->tuning.end()) plan->variant16 = it->second;
@@ -1088,14 +1146,35 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         a.num_tasks = plan->tasks16;
         a.task_counter = plan->counter16.as<int32_t>();
         a.rows = kVariants16[plan->variant16].rows;
-        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter16.ptr, 0, sizeof(int32_t), ctx->stream));
-        const int grid = int(std::min<int64_t>(plan->grid16[plan->variant16],
-                                                (int64_t(plan->tasks16) * 32 + kBlock - 1) / kBlock));
+        const size_t nb16 = plan->b16_start.size();
+        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter16.ptr, 0, sizeof(int32_t) * std::max<size_t>(nb16, 1),
+                                      ctx->stream));
         k_pack16<<<int((plan->num16 + kBlock - 1) / kBlock), kBlock, 0, ctx->stream>>>(a);
-        launch_dp16(plan->variant16, plan->affine, grid, a, ctx->stream);
         ++launches;
+        if (nb16 == 0) {
+            const int grid = int(std::min<int64_t>(plan->grid16[plan->variant16],
+                                                    (int64_t(plan->tasks16) * 32 + kBlock - 1) / kBlock));
+            launch_dp16(plan->variant16, plan->affine, grid, a, ctx->stream);
+            ++launches;
+        } else {
+            // Plain form: one launch per length bucket (its slots start on a warp boundary).
+            for (size_t b = 0; b < nb16; ++b) {
+                Dp16Args ab = a;
+                const int64_t w0 = plan->b16_start[b] / 32;
+                ab.slots = a.slots + plan->b16_start[b];
+                ab.warp_codes = a.warp_codes + w0;
+                ab.warp_hwords = a.warp_hwords + w0;
+                ab.warp_bnd = a.warp_bnd + w0;
+                ab.num_slots = plan->b16_count[b];
+                ab.num_tasks = int32_t((plan->b16_count[b] + 31) / 32);
+                ab.task_counter = a.task_counter + b;
+                const int grid = int(std::min<int64_t>(plan->grid16[plan->variant16],
+                                                        (int64_t(ab.num_tasks) * 32 + kBlock - 1) / kBlock));
+                launch_dp16(plan->variant16, plan->affine, grid, ab, ctx->stream);
+                ++launches;
+            }
+        }
         GBA_CUDA(ctx, cudaGetLastError());
-        launches += 1;
     }
     if (plan->num_slots > 0 && plan->params.band_on) {
         BandArgs b{};
@@ -1150,19 +1229,36 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         w.gap_extend = plan->params.gap_extend;
         w.free_ends = plan->free_ends;
         w.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
-        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter_warp.ptr, 0, sizeof(int32_t), ctx->stream));
+        const size_t nbw = plan->wb_start.size();
+        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter_warp.ptr, 0, sizeof(int32_t) * std::max<size_t>(nbw, 1),
+                                      ctx->stream));
         if (plan->num_band_states > 0) {
             GBA_CUDA(ctx, cudaMemsetAsync(plan->band_state.ptr, 0, plan->num_band_states * sizeof(BandState),
                                           ctx->stream));
             GBA_CUDA(ctx, cudaMemsetAsync(ctx->err_word.as<int32_t>() + plan->err_slot, 0, sizeof(int32_t),
                                           ctx->stream));
         }
-        const int grid =
-            int(std::min<int64_t>(plan->grid_warp, (plan->num_warp_tasks * 32 + kBlock - 1) / kBlock));
         const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
-        pick_warp(plan->affine, plan->local, plan->matrix, plan->traceback)(w, grid, smem, ctx->stream);
+        const WarpLauncher wl = pick_warp(plan->affine, plan->local, plan->matrix, plan->traceback);
+        if (nbw == 0) {
+            const int grid =
+                int(std::min<int64_t>(plan->grid_warp, (plan->num_warp_tasks * 32 + kBlock - 1) / kBlock));
+            wl(w, grid, smem, ctx->stream);
+            ++launches;
+        } else {
+            // Plain form: one launch per length bucket over that bucket's tasks.
+            for (size_t b = 0; b < nbw; ++b) {
+                WarpArgs wb = w;
+                wb.tasks = w.tasks + plan->wb_start[b];
+                wb.num_tasks = int32_t(plan->wb_count[b]);
+                wb.task_counter = w.task_counter + b;
+                const int grid =
+                    int(std::min<int64_t>(plan->grid_warp, (plan->wb_count[b] * 32 + kBlock - 1) / kBlock));
+                wl(wb, grid, smem, ctx->stream);
+                ++launches;
+            }
+        }
         GBA_CUDA(ctx, cudaGetLastError());
-        ++launches;
     } else if (plan->num_slots > 0) {
         DpArgs a{};
         a.seq_h = dseq_h;
@@ -1314,7 +1410,7 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         plan->drop_graph();
     }
     const void *key[5] = {dseq_h, dseq_v, dscore, dend_h, dend_v};
-    const bool use_graph = allow_graph && !(plan->params.flags & GBA_FLAG_NO_GRAPH);
+    const bool use_graph = allow_graph && !(plan->params.flags & (GBA_FLAG_NO_GRAPH | GBA_FLAG_PLAIN_BUCKETS));
     if (use_graph && plan->graph && std::equal(key, key + 5, plan->graph_key)) {
         GBA_CUDA(ctx, cudaGraphLaunch(plan->graph, ctx->stream));
     } else if (use_graph) {
@@ -1603,7 +1699,8 @@ GBA_API int gba_align_batch(gba_context *ctx, const gba_params *params, const gb
         if (hb) GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_h.ptr, batch->seq_h, hb, cudaMemcpyHostToDevice, ctx->stream));
         if (vb) GBA_CUDA(ctx, cudaMemcpyAsync(ctx->seq_v.ptr, batch->seq_v, vb, cudaMemcpyHostToDevice, ctx->stream));
     }
-    if (params && batch && !(params->outputs & GBA_OUT_SEGMENTS) && batch->num_pairs >= 2 * kChunkPairs)
+    if (params && batch && !(params->outputs & GBA_OUT_SEGMENTS) && !(params->flags & GBA_FLAG_PLAIN_BUCKETS) &&
+        batch->num_pairs >= 2 * kChunkPairs)
         return align_batch_chunked(ctx, params, batch, result, t0);
     plan->err_slot = 0;
     int rc = build_plan(ctx, params, batch, plan);

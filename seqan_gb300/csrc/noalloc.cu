@@ -11,8 +11,11 @@
 // this library holds until the process exits.
 //
 // Set-up: the first call on each device looks up that device's address of the array with
-// cudaGetSymbolAddress (the device must be current).  Make that first call before any
-// stream capture starts.  All calls share the array and it keeps the previous call's
+// cudaGetSymbolAddress (the device must be current).  With CUDA's lazy module loading (the
+// default) that lookup is also when this file's module is loaded on the device and the array's
+// 64 MiB are committed, so the first call may allocate and synchronize: make it once at start-up,
+// before any stream capture starts and before a host pool reserves the GPU's memory.  Every
+// later call allocates nothing.  All calls share the array and it keeps the previous call's
 // contents; the kernel writes every scratch element before reading it, so nothing has to be
 // cleared.  Calls that overlap on the GPU (on different streams, or from several threads)
 // race on the array and must be serialized by the caller.
@@ -84,12 +87,14 @@ __global__ void __launch_bounds__(128) k_dp_noalloc(NoAllocArgs a)
         const int64_t m64 = a.off_h[p + 1] - h0, n64 = a.off_v[p + 1] - v0;
         const int32_t minval = a.score_bits == 16 ? -32768 : INT_MIN;
         if (m64 <= 0 || n64 <= 0 || m64 > a.max_h_len || n64 > (int64_t(1) << 30)) {
-            // Empty pairs score numeric min like the reference; pairs longer than the caller's
-            // bound are not computed (their scratch column would not fit) and are flagged too.
+            // Empty pairs score numeric min like the reference (GBA_PAIR_INVALID); pairs longer
+            // than the caller's bound are not computed -- their scratch column would not fit --
+            // and get numeric min with GBA_PAIR_SKIPPED, so the two cases stay apart.
+            const bool empty = m64 <= 0 || n64 <= 0;
             a.score[p] = minval;
             if (a.end_h) a.end_h[p] = 0;
             if (a.end_v) a.end_v[p] = 0;
-            if (a.status) a.status[p] = GBA_PAIR_INVALID;
+            if (a.status) a.status[p] = empty ? GBA_PAIR_INVALID : GBA_PAIR_SKIPPED;
             continue;
         }
         const int m = int(m64), n = int(n64);
@@ -289,6 +294,9 @@ extern "C" GBA_API int gba_align_score_noalloc(const gba_params *params, const g
                                 launch<false, true, false>,  launch<false, true, true>,
                                 launch<true, false, false>,  launch<true, false, true>,
                                 launch<true, true, false>,   launch<true, true, true>};
+    // An error already pending on this thread (the caller's own) is left in place for the caller
+    // and reported as GBA_ECUDA without launching; only this call's launch error is consumed.
+    if (cudaPeekAtLastError() != cudaSuccess) return GBA_ECUDA;
     table[(affine ? 4 : 0) | (local ? 2 : 0) | (mat ? 1 : 0)](a, grid, s);
     return cudaGetLastError() == cudaSuccess ? GBA_OK : GBA_ECUDA;
 }

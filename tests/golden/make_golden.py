@@ -15,6 +15,8 @@ Outputs (all small, committed):
                         (the bits that hold no value, undefined there, masked to zero).
   extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
                         (align_extend/align_extend.h) with and without X-drop: score and rows.
+  cpp_binding_expected.txt  the output of tests/cpp/seqan_binding.cpp built with
+                        -DGBA_AS_REFERENCE: the binding's calls run by the reference itself.
   aa_background.json    residue counts of the reference's T-Coffee test FASTA files, the
                         stand-in for background amino-acid frequencies.
 """
@@ -32,7 +34,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("SEQAN_REF_ROOT", "/root/reference")
 
 from oracle import oracle as O  # noqa: E402
 
@@ -85,7 +87,8 @@ def main():
     if not os.path.isdir(REFERENCE):
         sys.exit("the reference tree is needed to generate fixtures")
     if not O.ref_available():
-        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"-j{os.cpu_count()}"])
+        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle", "ref"), f"-j{os.cpu_count()}",
+                               f"SEQAN_INCLUDE={os.path.join(REFERENCE, 'include')}"])
     b62 = O.ref_blosum62()
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     if only == "seeds":
@@ -105,6 +108,9 @@ def main():
         return
     if only == "bam":
         write_bam_cases()
+        return
+    if only == "cpp":
+        write_cpp_binding()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -565,6 +571,21 @@ def write_bam_cases():
         json.dump({"generator": "tests/golden/make_golden.py --only bam", "seed": 20261209,
                    "iupac": O.ref_iupac_table().tolist(), "cases": cases}, f, separators=(",", ":"))
     print(f"{sum(len(c['qname']) for c in cases)} BAM records written")
+
+
+def write_cpp_binding():
+    """Builds tests/cpp/seqan_binding.cpp against the reference's headers with -DGBA_AS_REFERENCE
+    (every call run by the reference) and records its output."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(tmp, "binding_ref")
+        subprocess.check_call(["g++", "-std=c++17", "-O1", "-fopenmp", "-w", "-DGBA_AS_REFERENCE",
+                               "-I", os.path.join(REFERENCE, "include"), "-I", os.path.join(ROOT, "include"),
+                               os.path.join(ROOT, "tests", "cpp", "seqan_binding.cpp"), "-o", exe])
+        out = subprocess.run([exe], check=True, capture_output=True).stdout
+    with open(os.path.join(HERE, "cpp_binding_expected.txt"), "wb") as f:
+        f.write(out)
+    print(f"{out.count(b'\n')} lines of reference output written")
 
 
 if __name__ == "__main__":

@@ -3,10 +3,11 @@
 The allocation-free entry point serves callers that cannot allocate device memory on their
 call path (hosts that own all device memory through their own pool, and latency-bound
 request loops that keep cudaMalloc/cudaFree out of their requests).  The test allocates the
-inputs and outputs itself, as such a caller would, then checks two calls in a row against
-the regular entry point.  Integer results, so the tolerance is zero: every score and end
-position must be identical.  The second call uses a different batch, so a stale scratch
-array from the first call would show up as a mismatch.
+inputs and outputs itself, as such a caller would, then checks calls in a row against the
+regular entry point: global, local and Blosum62 scoring, int16 and int32 cells, pairs past
+the exact int16 range, pairs over the caller's length bound.  Integer results, so the
+tolerance is zero: every score, end position and status must be identical.  Each call uses a
+different batch, so a stale scratch array from the call before would show up as a mismatch.
 """
 import ctypes as C
 
@@ -21,12 +22,19 @@ def _device_sync():
     assert cuda.cuCtxSynchronize() == 0
 
 
+def _free_device_bytes():
+    cuda = C.CDLL("libcuda.so.1")
+    free, total = C.c_size_t(), C.c_size_t()
+    assert cuda.cuMemGetInfo_v2(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
 def _regular(score, H, V, mode, config):
     import seqan_gb300 as sg
     return sg.align_codes(H, V, score, mode=mode, config=config)
 
 
-def _noalloc(ctx, score, H, V, mode, config, max_h_len):
+def _noalloc(ctx, score, H, V, mode, config, max_h_len, free_bytes=None):
     import seqan_gb300 as sg
     from seqan_gb300 import _native as N
     L, h = N.lib(), ctx.handle
@@ -47,9 +55,13 @@ def _noalloc(ctx, score, H, V, mode, config, max_h_len):
     ctx.check(L.gba_synchronize(h), "sync")
     params = sg.align.make_params(score, mode, config, None, N.GBA_OUT_SCORE | N.GBA_OUT_END)
     batch = N.GbaNoAllocBatch(n, d_sh, d_oh, d_sv, d_ov, max_h_len, 0)
+    _device_sync()
+    before = _free_device_bytes()
     rc = L.gba_align_score_noalloc(C.byref(params), C.byref(batch), *outs, None)
     assert rc == N.GBA_OK
     _device_sync()
+    if free_bytes is not None:
+        free_bytes.append((before, _free_device_bytes()))
     res = []
     for p in outs:
         a = np.zeros(n, np.int32)
@@ -60,26 +72,69 @@ def _noalloc(ctx, score, H, V, mode, config, max_h_len):
     return res
 
 
-def _pairs(seed, n, lo, hi):
+def _pairs(seed, n, lo, hi, alpha=4, codes=None):
     rng = np.random.default_rng(seed)
-    H = [rng.integers(0, 4, rng.integers(lo, hi + 1)).astype(np.uint8) for _ in range(n)]
-    V = [np.where(rng.random(len(x)) < 0.1, (x + 1) % 4, x).astype(np.uint8) for x in H]
+    draw = (lambda k: rng.integers(0, alpha, k)) if codes is None else (lambda k: codes[rng.integers(0, len(codes), k)])
+    H = [draw(rng.integers(lo, hi + 1)).astype(np.uint8) for _ in range(n)]
+    V = [np.where(rng.random(len(x)) < 0.3, draw(len(x)), x).astype(np.uint8) for x in H]
     return H, V
 
 
-def test_noalloc_matches_regular_entry_point_twice(engine):
+AA20 = np.array([0, 2, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 15, 16, 17, 18, 19, 21, 22, 23], np.uint8)
+
+
+def _cases():
     import seqan_gb300 as sg
-    cases = [
-        (sg.Score(2, -4, -1, -6, dtype=np.int16), _pairs(1, 3000, 100, 300), 0, sg.AlignConfig(), 300),
-        (sg.Score(2, -3, -5, dtype=np.int32), _pairs(2, 1500, 1, 120), 0,
+    b62 = sg.Blosum62(-1, -11, dtype=np.int16)
+    return [
+        ("affine global int16", sg.Score(2, -4, -1, -6, dtype=np.int16), _pairs(1, 3000, 100, 300), 0,
+         sg.AlignConfig(), 300),
+        ("linear global int32, free first/last row", sg.Score(2, -3, -5, dtype=np.int32), _pairs(2, 1500, 1, 120), 0,
          sg.AlignConfig(True, False, False, True), 400),
+        ("affine local int16", sg.Score(2, -4, -1, -6, dtype=np.int16), _pairs(3, 2000, 20, 250), 1, None, 250),
+        ("Blosum62 local int16", b62, _pairs(4, 1200, 30, 400, codes=AA20), 1, None, 400),
+        ("Blosum62 global int16", b62, _pairs(5, 1200, 30, 400, codes=AA20), 0, sg.AlignConfig(), 400),
+        # 6,000 x 6,000 bp global pairs leave the exact int16 range: promoted to 32-bit cells.
+        ("int16 past the exact bound", sg.Score(2, -4, -1, -6, dtype=np.int16), _pairs(6, 40, 5900, 6000), 0,
+         sg.AlignConfig(), 6000),
     ]
-    for score, (H, V), mode, cfg, max_h in cases:
+
+
+def test_noalloc_matches_regular_entry_point_twice(engine):
+    """Each case is one call of the allocation-free entry point after the previous case's call
+    (two and more calls in a row on the shared scratch), compared with gba_align_batch with zero
+    tolerance; from the second call on, free device memory is unchanged across the call."""
+    free = []
+    for name, score, (H, V), mode, cfg, max_h in _cases():
         ref = _regular(score, H, V, mode, cfg)
-        got_score, got_eh, got_ev, got_status = _noalloc(engine, score, H, V, mode, cfg, max_h)
-        assert np.array_equal(got_score, ref.score)
-        assert np.array_equal(got_eh, ref.end_h) and np.array_equal(got_ev, ref.end_v)
-        assert np.array_equal(got_status, ref.status)
+        got_score, got_eh, got_ev, got_status = _noalloc(engine, score, H, V, mode, cfg, max_h, free)
+        assert np.array_equal(got_score, ref.score), name
+        assert np.array_equal(got_eh, ref.end_h) and np.array_equal(got_ev, ref.end_v), name
+        assert np.array_equal(got_status, ref.status), name
+        if name.startswith("int16 past"):
+            assert (got_status == 2).all(), name
+    for before, after in free[1:]:
+        assert after == before, "a call after the first changed the device's free memory"
+
+
+def test_noalloc_pairs_over_the_bound_are_skipped(engine):
+    """Pairs with |H| above max_h_len are not computed: numeric min and GBA_PAIR_SKIPPED; empty
+    pairs keep GBA_PAIR_INVALID; every other pair equals gba_align_batch."""
+    import seqan_gb300 as sg
+    from seqan_gb300 import _native as N
+    score = sg.Score(2, -4, -1, -6, dtype=np.int16)
+    H, V = _pairs(7, 500, 50, 200)
+    H[17] = np.zeros(0, np.uint8)
+    for k in (3, 250, 499):
+        H[k] = np.random.default_rng(k).integers(0, 4, 260).astype(np.uint8)
+    ref = _regular(score, H, V, 0, sg.AlignConfig())
+    got_score, got_eh, got_ev, got_status = _noalloc(engine, score, H, V, 0, sg.AlignConfig(), 200)
+    over = np.array([len(h) > 200 for h in H])
+    assert (got_status[over] == N.GBA_PAIR_SKIPPED).all() and (got_score[over] == -32768).all()
+    assert got_status[17] == N.GBA_PAIR_INVALID == ref.status[17] and got_score[17] == ref.score[17]
+    ok = ~over
+    assert np.array_equal(got_score[ok], ref.score[ok]) and np.array_equal(got_status[ok], ref.status[ok])
+    assert np.array_equal(got_eh[ok], ref.end_h[ok]) and np.array_equal(got_ev[ok], ref.end_v[ok])
 
 
 def test_noalloc_rejects_bound_beyond_scratch(engine):
