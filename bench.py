@@ -1604,16 +1604,15 @@ def main():
         line["cpu_baseline"] = cpu_baseline(spec)
     if rank == 0 and world == 1 and args.workload == "affine_dna_100k" and not args.no_serving and not args.pairs:
         # Serving: the stated load (50,000 req/s, mixed lengths incl. 1% 10 kbp x 10 kbp, global
-        # affine with traceback) for a short arrival window, then half the measured capacity.
-        stated = run_serving(50_000.0, 0.2)
-        # Capacity: 20,000 requests offered at once; then half of it as a steady load.
+        # affine with traceback) for a 2 s arrival window (100,000 requests), then the capacity.
+        stated = run_serving(50_000.0, 2.0)
+        # Capacity: 20,000 requests offered at once.
         saturated = run_serving(1e9, 20_000 / 1e9, seed=13)
-        sustained = run_serving(max(50.0, 0.5 * saturated["throughput_req_s"]), 2.0, seed=11)
         line["serving"] = {"workload": "Poisson arrivals; lengths 90% U[100,500], 9% U[1000,5000], 1% 10000; "
                                        "5% subs + 1% indels; Score(2,-4,-1,-6) int16 (10 kbp pairs promoted to "
                                        "int32); global; score + traceback; 64 GB HBM admission budget; "
                                        "8 batches in flight",
-                           "stated_load": stated, "capacity": saturated, "half_capacity_load": sustained}
+                           "stated_load": stated, "capacity": saturated}
     L.gba_plan_destroy(h, plan)
     for p in (d_sh, d_sv, d_score, d_eh, d_ev, d_flush):
         L.gba_device_free(h, p)

@@ -33,7 +33,7 @@ class OrcParams(C.Structure):
                 ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
                 ("gap_extend", C.c_int32), ("matrix", C.POINTER(C.c_int32)),
                 ("alphabet_size", C.c_int32), ("score_bits", C.c_int32), ("traceback", C.c_int32),
-                ("xdrop_on", C.c_int32), ("xdrop", C.c_int32)]
+                ("xdrop_on", C.c_int32), ("xdrop", C.c_int32), ("trace4", C.c_int32)]
 
 
 class OrcResult(C.Structure):
@@ -75,6 +75,7 @@ class Problem:
     score_bits: int = 32
     alphabet: str = "dna"           # "dna" (Dna5 codes) | "aa" (AminoAcid codes)
     xdrop: int | None = None        # mode "extend": the X-drop terminator's threshold
+    trace4: bool = False            # trace values through the 4-bit code before the traceback
 
     @property
     def affine(self) -> bool:
@@ -201,6 +202,7 @@ def _orc_params(pb: Problem, traceback: bool) -> OrcParams:
         p.alphabet_size = int(round(np.sqrt(mat.size)))
     p.score_bits = pb.score_bits
     p.traceback = 1 if traceback else 0
+    p.trace4 = 1 if pb.trace4 else 0
     return p
 
 

@@ -636,6 +636,27 @@ static void dp_unbanded(const ctx_t *c, int fe, const uint8_t *h, int m, const u
     }
 }
 
+/* 4-bit trace code (see seqan_oracle.h).  _doTraceback (align/dp_traceback_impl.h:376-450) reads
+ * DIAGONAL, MAX_FROM_V with VERTICAL / VERTICAL_OPEN and MAX_FROM_H with HORIZONTAL /
+ * HORIZONTAL_OPEN, and its gap walks continue while !(open) || (extend) (:242-255, :320-332);
+ * SingleTrace sets exactly one bit of each open/extend pair in inner cells (dp_formula.h:179-181). */
+uint8_t orc_trace4_encode(uint8_t tv)
+{
+    int src = (tv & TV_DIAG) ? 1 : (tv & TV_MFV) ? 2 : (tv & TV_MFH) ? 3 : 0;
+    int eo = (tv & TV_HO) && !(tv & TV_H);
+    int fo = (tv & TV_VO) && !(tv & TV_V);
+    return (uint8_t)(src | (eo << 2) | (fo << 3));
+}
+
+uint8_t orc_trace4_decode(uint8_t code, int32_t affine)
+{
+    static const uint8_t src_bits[4] = {TV_NONE, TV_DIAG, TV_MFV, TV_MFH};
+    int src = code & 3;
+    if (src == 0) return TV_NONE;
+    if (!affine) return (uint8_t)(src == 1 ? TV_DIAG : src == 2 ? (TV_V | TV_MFV) : (TV_H | TV_MFH));
+    return (uint8_t)(src_bits[src] | ((code & 4) ? TV_HO : TV_H) | ((code & 8) ? TV_VO : TV_V));
+}
+
 int orc_align_pair(const orc_params *p,
                    const uint8_t *h, int32_t m,
                    const uint8_t *v, int32_t n,
@@ -689,6 +710,10 @@ int orc_align_pair(const orc_params *p,
     if (T) {
         segbuf_t sb;
         uint8_t *cell = &T[(size_t)b.col * (size_t)(n + 1) + (size_t)b.row];
+        if (p->trace4) {
+            size_t q, cells = (size_t)(m + 1) * (size_t)(n + 1);
+            for (q = 0; q < cells; ++q) T[q] = orc_trace4_decode(orc_trace4_encode(T[q]), c.affine);
+        }
         /* _correctTraceValue (align/dp_algorithm_impl.h:1188-1205), affine only. */
         if (c.affine) {
             if (b.f == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFV; }

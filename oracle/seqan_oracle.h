@@ -49,7 +49,17 @@ typedef struct {
     int32_t traceback;      /* 0 = score only, 1 = trace segments */
     int32_t xdrop_on;       /* ORC_EXTEND: the X-drop terminator (align_extend/dp_scout_xdrop.h) */
     int32_t xdrop;
+    int32_t trace4;         /* 1: pass every trace value through the 4-bit code (orc_trace4_encode /
+                               orc_trace4_decode) before the traceback, to check that 4 bits per
+                               cell keep every traceback decision */
 } orc_params;
+
+/* The 4-bit trace code: bits 0-1 the source of S (0 none, 1 diagonal, 2 vertical = MAX_FROM_V,
+ * 3 horizontal = MAX_FROM_H), bit 2 "E opened" (H_OPEN without H), bit 3 "F opened" (V_OPEN
+ * without V).  Decoding gives back the reference's TraceBitMap_ byte of every inner cell; a cell
+ * that lacks an open/extend pair (borders, band edges) decodes with "extend" for it. */
+uint8_t orc_trace4_encode(uint8_t tv);
+uint8_t orc_trace4_decode(uint8_t code, int32_t affine);
 
 typedef struct {
     uint32_t h_begin, v_begin, length, type;  /* TraceSegment_<unsigned, unsigned> */

@@ -319,6 +319,9 @@ int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
     if (p->matrix && (p->alphabet_size <= 0 || p->alphabet_size > 32))
         return fail(ctx, GBA_EINVAL, "alphabet_size must be in 1..32");
     if (b->num_pairs < 0) return fail(ctx, GBA_EINVAL, "negative num_pairs");
+    // Pair indices are 32-bit (slot orders, task lists) and the output scans count num_pairs + 1
+    // items in an int.
+    if (b->num_pairs > int64_t(INT32_MAX) - 1) return fail(ctx, GBA_EINVAL, "more than 2^31 - 2 pairs in one batch");
     if (b->num_pairs > 0 && (!b->off_h || !b->off_v || ((!b->seq_h || !b->seq_v) && !ctx->device_codes)))
         return fail(ctx, GBA_EINVAL, "null sequence or offset pointer");
     if (p->band_on) {

@@ -15,8 +15,8 @@ import numpy as np
 
 # BLOSUM62 over the 27-letter AminoAcid alphabet (A B C D E F G H I J K L M N O P Q R S T U V W
 # Y Z X *), row = first (H) residue.  The values must equal the reference's table
-# (score/score_matrix_data.h:311-400) for scores to match; tests/test_scoring.py checks them
-# against a fixture dumped from the compiled reference.
+# (score/score_matrix_data.h:311-400) for scores to match; tests/test_oracle_golden.py checks
+# them against a fixture dumped from the compiled reference (tests/golden/blosum62.json).
 BLOSUM62_AA27 = np.array([
     [ 4, -2,  0, -2, -1, -2,  0, -2, -1, -1, -1, -1, -1, -2,  0, -1, -1, -1,  1,  0,  0,  0, -3, -2, -1,  0, -4],
     [-2,  4, -3,  4,  1, -3, -1,  0, -3, -4,  0, -4, -3,  3, -1, -2,  0, -1,  0, -1, -1, -3, -4, -3,  1, -1, -4],

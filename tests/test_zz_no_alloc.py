@@ -94,9 +94,10 @@ def _cases():
         ("affine local int16", sg.Score(2, -4, -1, -6, dtype=np.int16), _pairs(3, 2000, 20, 250), 1, None, 250),
         ("Blosum62 local int16", b62, _pairs(4, 1200, 30, 400, codes=AA20), 1, None, 400),
         ("Blosum62 global int16", b62, _pairs(5, 1200, 30, 400, codes=AA20), 0, sg.AlignConfig(), 400),
-        # 6,000 x 6,000 bp global pairs leave the exact int16 range: promoted to 32-bit cells.
-        ("int16 past the exact bound", sg.Score(2, -4, -1, -6, dtype=np.int16), _pairs(6, 40, 5900, 6000), 0,
-         sg.AlignConfig(), 6000),
+        # With gap extension -3, 3,000 x 3,000 bp global pairs can reach values below the int16
+        # "infinity" (all-gap paths cost 3 * (m + n)): promoted to 32-bit cells.
+        ("int16 past the exact bound", sg.Score(2, -4, -3, -6, dtype=np.int16), _pairs(6, 40, 2900, 3000), 0,
+         sg.AlignConfig(), 3000),
     ]
 
 
