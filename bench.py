@@ -510,6 +510,7 @@ OPS_PER_CELL = {"affine_global": 9, "linear_global": 5, "affine_local": 10, "lin
 
 
 KERNEL_NAMES = [(2, "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)"),
+                (16, "k_dp_warp2 (64 strips per warp in int16x2 halves, 4-bit trace)"),
                 (4, "k_dp_warp (one warp per 256-row band, anti-diagonal front)"),
                 (8, "k_dp_banded (one pair per thread, band in per-thread slots)"),
                 (1, "k_dp_strip (one pair per thread, int32)")]
@@ -1248,9 +1249,10 @@ def main():
     ap.add_argument("--pairs", type=int, default=0, help="use only the first N pairs (small profiling cases)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison of the timed results")
-    ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16", "plain"],
-                    help="auto: persistent packed 16-bit kernel (32-row strips), graph-replayed; "
-                         "plain: general kernel, one launch per length bucket")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16", "plain", "warp32"],
+                    help="auto: the engine's routing (packed 16-bit kernels), graph-replayed; "
+                         "plain: the same kernels, one launch per length bucket; "
+                         "warp32: the 32-bit warp kernel instead of the packed 16-bit warp kernel")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -1353,7 +1355,8 @@ def main():
     p_score, p_eh, p_ev = pinned(npairs * 4), pinned(npairs * 4), pinned(npairs * 4)
 
     flags = {"auto": N.GBA_FLAG_AUTOTUNE, "general": N.GBA_FLAG_GENERAL_KERNEL, "packed16": N.GBA_FLAG_STRIP16,
-             "plain": N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH}[args.kernel]
+             "plain": N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH,
+             "warp32": N.GBA_FLAG_AUTOTUNE | N.GBA_FLAG_NO_WARP16}[args.kernel]
     params = sg.align.make_params(score, mode, spec.config, spec.band, outputs,
                                   alphabet_size=spec.alphabet_size, flags=flags)
     host_batch = N.GbaBatch(npairs, p_sh, p_oh, p_sv, p_ov, 0, 0)

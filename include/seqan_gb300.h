@@ -107,11 +107,14 @@ typedef struct {
 #define GBA_TILE_VARIANTS 5
 
 /* Kernel selection flags (gba_params.flags); results are identical either way.
- * With equality scoring the engine uses its packed two-pairs-per-thread 16-bit kernel when
- * alphabet_size is between 1 and 8 (the caller's promise that every code is below it, as the
- * reference's alphabet types guarantee), the pair's values stay in the exact int16 range and
- * the batch holds at least 32768 pairs; other unbanded pairs run one warp per pair, banded
- * pairs one thread per pair. */
+ * With equality scoring the engine uses its packed two-pairs-per-thread 16-bit kernel for global
+ * score-only pairs when alphabet_size is between 1 and 8 (the caller's promise that every code is
+ * below it, as the reference's alphabet types guarantee), the pair's values stay in the exact
+ * int16 range and the batch holds at least 32768 pairs.  Other unbanded pairs with 16-bit cells in
+ * the exact range, fewer than 1024 columns and at most 4096 rows, in batches of at least 4096
+ * pairs, run the packed 16-bit warp kernel (two strips per lane, 4-bit trace; equality scoring
+ * needs alphabet_size 1..8 there too); the remaining unbanded pairs run the 32-bit warp kernel,
+ * banded pairs one thread per pair. */
 enum {
     GBA_FLAG_GENERAL_KERNEL = 1,   /* force the one-pair-per-thread 32-bit kernel */
     GBA_FLAG_STRIP16 = 2,          /* packed kernel with 16-row strips instead of 32 */
@@ -127,7 +130,11 @@ enum {
                                       too small to fill the GPU with it */
     GBA_FLAG_PACKED_SPLIT = 64,    /* packed kernel: every pair runs as a split slot (one pair per
                                       thread, two strips at once) instead of only the longest */
-    GBA_FLAG_PACKED_NO_SPLIT = 128 /* packed kernel: no split slots (two pairs per thread only) */
+    GBA_FLAG_PACKED_NO_SPLIT = 128,/* packed kernel: no split slots (two pairs per thread only) */
+    GBA_FLAG_NO_WARP16 = 256,      /* pairs the packed 16-bit warp kernel would take run on the
+                                      32-bit warp kernel instead */
+    GBA_FLAG_WARP16 = 512          /* packed 16-bit warp kernel for eligible pairs even in batches
+                                      smaller than 4096 pairs */
 };
 
 /* A batch: concatenated residue codes with n+1 offsets for each side. */
@@ -228,7 +235,8 @@ enum {
     GBA_KERNEL_STRIP = 1,      /* one pair per thread, 16-row register strips, int32 */
     GBA_KERNEL_PACKED = 2,     /* two pairs per thread, int16x2 DPX */
     GBA_KERNEL_WARP = 4,       /* bands of 256 rows, one warp per band, anti-diagonal front */
-    GBA_KERNEL_BANDED = 8      /* banded DP, one pair per thread */
+    GBA_KERNEL_BANDED = 8,     /* banded DP, one pair per thread */
+    GBA_KERNEL_WARP16 = 16     /* bands of 64 strips, one warp per band, int16x2 DPX, 4-bit trace */
 };
 GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
 

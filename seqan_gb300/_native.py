@@ -32,8 +32,8 @@ GBA_SEG_DIAGONAL, GBA_SEG_HORIZONTAL, GBA_SEG_VERTICAL = 1, 2, 4
 GBA_NOALLOC_SCRATCH_BYTES = 64 << 20
 GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16, GBA_FLAG_PLAIN_BUCKETS, GBA_FLAG_NO_GRAPH, GBA_FLAG_AUTOTUNE = 1, 2, 4, 8, 16
 GBA_FLAG_PACKED = 32
-GBA_FLAG_PACKED_SPLIT, GBA_FLAG_PACKED_NO_SPLIT = 64, 128
-GBA_KERNEL_STRIP, GBA_KERNEL_PACKED, GBA_KERNEL_WARP, GBA_KERNEL_BANDED = 1, 2, 4, 8
+GBA_FLAG_PACKED_SPLIT, GBA_FLAG_PACKED_NO_SPLIT, GBA_FLAG_NO_WARP16, GBA_FLAG_WARP16 = 64, 128, 256, 512
+GBA_KERNEL_STRIP, GBA_KERNEL_PACKED, GBA_KERNEL_WARP, GBA_KERNEL_BANDED, GBA_KERNEL_WARP16 = 1, 2, 4, 8, 16
 GBA_MATCH_EXTEND, GBA_UNGAPPED_XDROP, GBA_GAPPED_XDROP = 0, 1, 2
 GBA_EXTEND_NONE, GBA_EXTEND_LEFT, GBA_EXTEND_RIGHT, GBA_EXTEND_BOTH = 0, 1, 2, 3
 

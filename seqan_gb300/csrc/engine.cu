@@ -11,6 +11,7 @@
 #include "dp16x2_kernels.cuh"
 #include "dp_banded_kernels.cuh"
 #include "dp_warp_kernels.cuh"
+#include "dp_warp2_kernels.cuh"
 #include "seed_kernels.cuh"
 #include "extend_kernels.cuh"
 #include "int_peak.cuh"
@@ -113,6 +114,14 @@ struct gba_plan {
     int warp_rows = 8;
     int64_t grid_warp = 0;
     DevBuf rowbuf, rowbuf_off, counter_warp, tasks_warp, band_base, band_state;
+    // Packed 16-bit warp path (dp_warp2_kernels.cuh): pairs in cost order, one task each.
+    int64_t num_w2 = 0;             // pairs
+    int64_t num_w2_tasks = 0;       // (pair, band) tasks
+    int64_t num_w2_states = 0;      // bands of pipelined pairs
+    int64_t grid_w2 = 0;
+    DevBuf tasks_w2, order_w2, rowbuf_w2, rowbuf_w2_off, counter_w2, band_w2, band_w2_base;
+    std::vector<int2> h_w2tasks;
+    std::vector<int64_t> w2b_start, w2b_count;   // plain form: task ranges per length bucket
     int64_t num_warp_tasks = 0;     // (pair, band) work items
     int64_t num_band_states = 0;    // bands of pairs that span more than one band
     int64_t num_tiled_tb = 0;       // leading slots whose traceback a whole warp walks
@@ -133,8 +142,8 @@ struct gba_plan {
     std::vector<int64_t> seg_off_host;   // per-pair segment slot offsets (num_pairs + 1)
     // Host-side planning arrays, reused by the next build of this plan.
     std::vector<PairDesc> h_desc;
-    std::vector<uint32_t> h_keys16, h_keys, h_key;
-    std::vector<int32_t> h_idx16, h_idx;
+    std::vector<uint32_t> h_keys16, h_keys, h_key, h_keys2;
+    std::vector<int32_t> h_idx16, h_idx, h_idx2;
     std::vector<uint8_t> h_cls;
     std::vector<Slot16> h_slots16;
     bool owned = true;
@@ -145,7 +154,8 @@ struct gba_plan {
                          &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
                          &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
                          &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16,
-                         &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state};
+                         &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state,
+                         &tasks_w2, &order_w2, &rowbuf_w2, &rowbuf_w2_off, &counter_w2, &band_w2, &band_w2_base};
         for (DevBuf *b : all) b->release();
         drop_graph();
     }
@@ -156,7 +166,8 @@ struct gba_plan {
                          &seg_count, &seg_dense_off, &seg_dense, &seg_count64, &cig_slots,
                          &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense, &cig_count64, &cub_tmp,
                          &slots16, &warp_codes, &warp_hwords, &codes16, &warp_bnd16, &bnd16, &counter16,
-                         &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state};
+                         &rowbuf, &rowbuf_off, &counter_warp, &tasks_warp, &band_base, &band_state,
+                         &tasks_w2, &order_w2, &rowbuf_w2, &rowbuf_w2_off, &counter_w2, &band_w2, &band_w2_base};
         for (DevBuf *b : all)
             if (!b->async || b->stream != s) b->bind(s);
     }
@@ -174,7 +185,8 @@ struct gba_plan {
                                &cig_slots, &cig_slot_off, &cig_count, &cig_dense_off, &cig_dense,
                                &cig_count64, &cub_tmp, &slots16, &warp_codes, &warp_hwords, &codes16,
                                &warp_bnd16, &bnd16, &counter16, &rowbuf, &rowbuf_off, &counter_warp,
-                               &tasks_warp, &band_base, &band_state};
+                               &tasks_warp, &band_base, &band_state, &tasks_w2, &order_w2, &rowbuf_w2,
+                               &rowbuf_w2_off, &counter_w2, &band_w2, &band_w2_base};
         size_t s = 0;
         for (const DevBuf *b : all) s += b->cap;
         return s;
@@ -249,6 +261,12 @@ constexpr int64_t kChunkPairs = 200000;
 // Pairs at least this wide pipeline their bands across warps even in large batches: the ~130
 // steps a pipelined band waits before its first column are then a small share of its work.
 constexpr int kPipelineMinCols = 1024;
+// The packed 16-bit warp kernel takes pairs narrower than kPipelineMinCols with at most kW2MaxRows
+// rows, in batches of at least kW2MinPairs pairs (it runs each pair's bands in order on one warp).
+constexpr int kW2MaxRows = 4096;
+// Pairs of at least this many 256-row bands pipeline their bands across warps.
+constexpr int kW2PipeBands = 3;
+constexpr int64_t kW2MinPairs = 4096;
 
 // _checkBandProperties (align/dp_algorithm_impl.h:193-234): the band must meet the matrix and
 // may leave it only across sides whose end gaps are free.
@@ -477,6 +495,7 @@ int64_t persistent_grid(gba_context *ctx, const void *fn)
 }
 
 const void *warp_fn(bool a, bool l, bool m, bool t);
+const void *warp2_fn(bool a, bool l, bool m, bool t);
 
 // Host threads for a planning loop over `work` items: serial below 16,384 items.
 int plan_threads(int64_t work)
@@ -547,9 +566,23 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // one-pair-per-thread kernel is forced.
     plan->use_warp = !p->band_on && !(p->flags & GBA_FLAG_GENERAL_KERNEL);
     plan->warp_rows = 8;
+    // The packed 16-bit warp path: 16-bit cells, a batch large enough to fill the GPU with one
+    // warp per pair, equality scoring over at most 8 codes (PRMT lookup) or a table whose entries
+    // fit int16, and gap scores small enough for the int16 range checks.
+    bool w2_ok = plan->use_warp && p->score_bits == 16 && (N >= kW2MinPairs || (p->flags & GBA_FLAG_WARP16)) &&
+                 !(p->flags & GBA_FLAG_NO_WARP16) &&
+                 std::abs(p->gap_open) <= 1024 && std::abs(p->gap_extend) <= 1024;
+    if (w2_ok && plan->matrix) {
+        for (int32_t v : plan->matrix_host) w2_ok = w2_ok && v >= -1024 && v <= 1024;
+    } else if (w2_ok) {
+        w2_ok = p->alphabet_size >= 1 && p->alphabet_size <= 8 && p->match >= -128 && p->match <= 127 &&
+                p->mismatch >= -128 && p->mismatch <= 127;
+    }
     // Host arrays live in the plan and keep their capacity between builds (no zero fill).
     auto &keys16 = plan->h_keys16;
     auto &idx16 = plan->h_idx16;
+    auto &keys2 = plan->h_keys2;
+    auto &idx2 = plan->h_idx2;
     auto &desc = plan->h_desc;
     auto &keys = plan->h_keys;
     auto &idx = plan->h_idx;
@@ -571,7 +604,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     cls.resize(N);
     key.resize(N);
     std::vector<int64_t> tbytes(plan->traceback ? N : 0);
-    std::vector<int64_t> c16(nth + 1, 0), cot(nth + 1, 0), ctr(nth + 1, 0);
+    std::vector<int64_t> c16(nth + 1, 0), cot(nth + 1, 0), ctr(nth + 1, 0), cw2(nth + 1, 0);
     int64_t first_bad = N, cells = 0;
     double cells16 = 0;   // cells of the packed-path pairs
     const int fe_all = plan->local ? 15 : p->free_ends;
@@ -580,7 +613,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         const int t = omp_get_thread_num();
         const int64_t k0 = N * t / nth, k1 = N * (t + 1) / nth;
         std::map<uint64_t, int64_t> band_cache;
-        int64_t n16 = 0, not16 = 0, tsum = 0;
+        int64_t n16 = 0, not16 = 0, nw2 = 0, tsum = 0;
         for (int64_t k = k0; k < k1; ++k) {
             const int64_t h0 = b->h_shared ? hs0 : b->off_h[k];
             const int64_t h1 = b->h_shared ? hs1 : b->off_h[k + 1];
@@ -615,12 +648,6 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             } else {
                 cells += int64_t(d.m) * d.n;
             }
-            if (plan->traceback) {
-                tbytes[k] = p->band_on ? int64_t(d.m + 1) * band_trace_stride(p->band_upper - p->band_lower + 1)
-                            : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
-                                             : trace_bytes(d.m, d.n);
-                tsum += tbytes[k];
-            }
             // (packed_ok excludes local mode, so exact16 is the global-mode check here)
             if (packed_ok && (p->score_bits == 16 ? exact16 : int16_exact(*p, max_pos, d.m, d.n, false))) {
                 const int64_t strips = (d.n + plan->rows16 - 1) / plan->rows16;
@@ -628,21 +655,35 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                 cls[k] = 1;
                 ++n16;
                 cells16 += double(d.m) * d.n;
+            } else if (w2_ok && exact16 && d.m < kPipelineMinCols && d.n <= kW2MaxRows) {
+                const int64_t bands = (d.n + kW2BandRows - 1) / kW2BandRows;
+                key[k] = uint32_t(std::min<int64_t>(bands * (d.m + 64), 0xffffffffLL));
+                cls[k] = 3;
+                ++nw2;
             } else {
                 const int64_t strips = (d.n + STRIP_ROWS - 1) / STRIP_ROWS;
                 key[k] = uint32_t(std::min<int64_t>(strips * (d.m + 1), 0xffffffffLL));
                 cls[k] = 2;
                 ++not16;
             }
+            if (plan->traceback) {
+                tbytes[k] = p->band_on ? int64_t(d.m + 1) * band_trace_stride(p->band_upper - p->band_lower + 1)
+                            : cls[k] == 3 ? warp2_trace_bytes(d.m, d.n)
+                            : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
+                                             : trace_bytes(d.m, d.n);
+                tsum += tbytes[k];
+            }
         }
         c16[t + 1] = n16;
         cot[t + 1] = not16;
+        cw2[t + 1] = nw2;
         ctr[t + 1] = tsum;
 #pragma omp barrier
 #pragma omp single
         for (int i = 0; i < nth; ++i) {
             c16[i + 1] += c16[i];
             cot[i + 1] += cot[i];
+            cw2[i + 1] += cw2[i];
             ctr[i + 1] += ctr[i];
         }
 #pragma omp single
@@ -651,8 +692,10 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             idx16.resize(c16[nth]);
             keys.resize(cot[nth]);
             idx.resize(cot[nth]);
+            keys2.resize(cw2[nth]);
+            idx2.resize(cw2[nth]);
         }
-        int64_t q16 = c16[t], qot = cot[t], toff = ctr[t];
+        int64_t q16 = c16[t], qot = cot[t], qw2 = cw2[t], toff = ctr[t];
         for (int64_t k = k0; k < k1; ++k) {
             if (cls[k] == 1) {
                 keys16[q16] = key[k];
@@ -660,6 +703,9 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             } else if (cls[k] == 2) {
                 keys[qot] = key[k];
                 idx[qot++] = int32_t(k);
+            } else if (cls[k] == 3) {
+                keys2[qw2] = key[k];
+                idx2[qw2++] = int32_t(k);
             }
             if (plan->traceback && cls[k] != 0) {
                 desc[k].trace_off = toff;
@@ -884,6 +930,75 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     }
     plan->num_warp_tasks = int64_t(wtasks.size());
     plan->num_band_states = nstates;
+
+    // Packed 16-bit warp path: one task per pair, costliest first (plain form: 8-residue buckets
+    // of max(m, n) in input order); a pair of more than one band gets a row buffer of m + 1 words.
+    plan->w2b_start.clear();
+    plan->w2b_count.clear();
+    if (plain && !idx2.empty()) {
+        std::vector<std::vector<int32_t>> bk;
+        for (int32_t k : idx2) {
+            const int bb = std::max(desc[k].m, desc[k].n) / 8;
+            if (bb >= int(bk.size())) bk.resize(bb + 1);
+            bk[bb].push_back(k);
+        }
+        idx2.clear();
+        for (auto &v : bk) {
+            if (v.empty()) continue;
+            plan->w2b_start.push_back(int64_t(idx2.size()));
+            plan->w2b_count.push_back(int64_t(v.size()));
+            idx2.insert(idx2.end(), v.begin(), v.end());
+        }
+    } else {
+        sort_desc(keys2, idx2);
+    }
+    plan->num_w2 = int64_t(idx2.size());
+    // Tasks: (pair, -1) runs the pair's bands in order on one warp; a pair of at least
+    // kW2PipeBands bands, or of two or more in a batch too small to keep the GPU busy otherwise,
+    // becomes one task per band, pipelined across warps.  Row buffers: one slot of m + 1 words for
+    // in-order pairs, two for pipelined ones; pipelined bands get a BandState each.
+    std::vector<int64_t> rb2off, bs2base;
+    std::vector<int2> &w2tasks = plan->h_w2tasks;
+    w2tasks.clear();
+    int64_t rb2tot = 0, ns2 = 0;
+    if (plan->num_w2 > 0) {
+        plan->grid_w2 = persistent_grid(ctx, warp2_fn(plan->affine, plan->local, plan->matrix, plan->traceback));
+        const bool few = plan->num_w2 < 2 * plan->grid_w2 * (kBlock / 32);
+        rb2off.assign(N + 1, 0);
+        bs2base.assign(N + 1, 0);
+        std::vector<int64_t> bstart(plan->w2b_start.size() + 1, 0);
+        size_t bk = 0;
+        for (int64_t q = 0; q < plan->num_w2; ++q) {
+            if (!plan->w2b_start.empty()) {
+                while (bk < plan->w2b_start.size() && plan->w2b_start[bk] + plan->w2b_count[bk] <= q) ++bk;
+                if (q == plan->w2b_start[bk]) bstart[bk] = int64_t(w2tasks.size());
+            }
+            const int32_t k = idx2[q];
+            const int nb = (desc[k].n + kW2BandRows - 1) / kW2BandRows;
+            const bool pipe = nb >= kW2PipeBands || (nb > 1 && few);
+            if (pipe) {
+                for (int bb = 0; bb < nb; ++bb) w2tasks.push_back(make_int2(k, bb));
+                bs2base[k] = ns2;
+                ns2 += nb;
+            } else {
+                w2tasks.push_back(make_int2(k, -1));
+            }
+            if (nb > 1) {
+                rb2off[k] = rb2tot;
+                rb2tot += (pipe ? 2 : 1) * (int64_t(desc[k].m) + 1);
+            }
+        }
+        // Plain form: task ranges per bucket.
+        if (!plan->w2b_start.empty()) {
+            bstart[plan->w2b_start.size()] = int64_t(w2tasks.size());
+            for (size_t i = 0; i < plan->w2b_start.size(); ++i) {
+                plan->w2b_start[i] = bstart[i];
+                plan->w2b_count[i] = bstart[i + 1] - bstart[i];
+            }
+        }
+    }
+    plan->num_w2_tasks = int64_t(w2tasks.size());
+    plan->num_w2_states = ns2;
     // Per-warp interleaved boundary rows: warp w holds 32 lanes x (max m + 1) int2.
     // (only the one-pair-per-thread strip kernel uses these boundary rows)
     const int64_t warps = (plan->use_warp || p->band_on) ? 0 : (plan->num_slots + 31) / 32;
@@ -921,7 +1036,8 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                          plan->codes_total * 4 + plan->bnd16_total * 8 + plan->num16 * int64_t(sizeof(Slot16)) +
                          plan->seg_slots_total * 16 * 2 + plan->cigar_slots_total * 4 * 2 +
                          plan->seq_h_bytes + plan->seq_v_bytes + rbtot * 8 + nstates * int64_t(sizeof(BandState)) +
-                         plan->num_warp_tasks * 8;
+                         plan->num_warp_tasks * 8 + rb2tot * 4 + plan->num_w2 * 12 + plan->num_w2_tasks * 8 +
+                         ns2 * int64_t(sizeof(BandState));
     if (ctx->budget > 0 && need > ctx->budget)
         return fail(ctx, GBA_EBUDGET, "batch needs %lld bytes of HBM, budget is %lld", (long long)need,
                     (long long)ctx->budget);
@@ -939,6 +1055,16 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         GBA_CUDA(ctx, plan->band_state.ensure(size_t(std::max<int64_t>(nstates, 1)) * sizeof(BandState)));
         GBA_CUDA(ctx, ctx->err_word.ensure(kMaxChunks * sizeof(int32_t)));
         GBA_CUDA(ctx, plan->counter_warp.ensure(std::max<size_t>(16, plan->wb_start.size() * sizeof(int32_t))));
+    }
+    if (plan->num_w2 > 0) {
+        if ((rc = upload(ctx, plan->tasks_w2, w2tasks))) return rc;
+        if ((rc = upload(ctx, plan->order_w2, idx2))) return rc;
+        if ((rc = upload(ctx, plan->rowbuf_w2_off, rb2off))) return rc;
+        if ((rc = upload(ctx, plan->band_w2_base, bs2base))) return rc;
+        GBA_CUDA(ctx, plan->rowbuf_w2.ensure(size_t(std::max<int64_t>(rb2tot, 1)) * sizeof(uint32_t)));
+        GBA_CUDA(ctx, plan->band_w2.ensure(size_t(std::max<int64_t>(ns2, 1)) * sizeof(BandState)));
+        GBA_CUDA(ctx, plan->counter_w2.ensure(std::max<size_t>(16, plan->w2b_start.size() * sizeof(int32_t))));
+        GBA_CUDA(ctx, ctx->err_word.ensure(kMaxChunks * sizeof(int32_t)));
     }
     if (plan->num16 > 0) {
         if ((rc = upload(ctx, plan->slots16, slots16))) return rc;
@@ -1044,6 +1170,42 @@ WarpLauncher pick_warp(bool a, bool l, bool m, bool t)
     return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
 }
 
+template <bool A, bool L, bool M, bool T>
+void launch_warp2(const Warp2Args &args, int grid, cudaStream_t s)
+{
+    k_dp_warp2<A, L, M, T><<<grid, kBlock, 0, s>>>(args);
+}
+using Warp2Launcher = void (*)(const Warp2Args &, int, cudaStream_t);
+
+Warp2Launcher pick_warp2(bool a, bool l, bool m, bool t)
+{
+    static const Warp2Launcher table[16] = {
+        launch_warp2<false, false, false, false>, launch_warp2<false, false, false, true>,
+        launch_warp2<false, false, true, false>,  launch_warp2<false, false, true, true>,
+        launch_warp2<false, true, false, false>,  launch_warp2<false, true, false, true>,
+        launch_warp2<false, true, true, false>,   launch_warp2<false, true, true, true>,
+        launch_warp2<true, false, false, false>,  launch_warp2<true, false, false, true>,
+        launch_warp2<true, false, true, false>,   launch_warp2<true, false, true, true>,
+        launch_warp2<true, true, false, false>,   launch_warp2<true, true, false, true>,
+        launch_warp2<true, true, true, false>,    launch_warp2<true, true, true, true>};
+    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
+const void *warp2_fn(bool a, bool l, bool m, bool t)
+{
+#define GBA_W2F(A, L, M, T) (const void *)k_dp_warp2<A, L, M, T>
+    const void *table[16] = {GBA_W2F(false, false, false, false), GBA_W2F(false, false, false, true),
+                             GBA_W2F(false, false, true, false),  GBA_W2F(false, false, true, true),
+                             GBA_W2F(false, true, false, false),  GBA_W2F(false, true, false, true),
+                             GBA_W2F(false, true, true, false),   GBA_W2F(false, true, true, true),
+                             GBA_W2F(true, false, false, false),  GBA_W2F(true, false, false, true),
+                             GBA_W2F(true, false, true, false),   GBA_W2F(true, false, true, true),
+                             GBA_W2F(true, true, false, false),   GBA_W2F(true, true, false, true),
+                             GBA_W2F(true, true, true, false),    GBA_W2F(true, true, true, true)};
+#undef GBA_W2F
+    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
 const void *warp_fn(bool a, bool l, bool m, bool t)
 {
 #define GBA_WF(A, L, M, T) (const void *)k_dp_warp<A, L, M, T, kWarpRows>
@@ -1125,6 +1287,9 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
     const int32_t minval = plan->params.score_bits == 16 ? -32768 : INT32_MIN;
     int launches = 0;
 
+    // The error word of this plan's bounded waits between bands (both warp kernels).
+    if ((plan->use_warp && plan->num_band_states > 0) || plan->num_w2_states > 0)
+        GBA_CUDA(ctx, cudaMemsetAsync(ctx->err_word.as<int32_t>() + plan->err_slot, 0, sizeof(int32_t), ctx->stream));
     GBA_CUDA(ctx, cudaEventRecordWithFlags(ctx->ev[0], ctx->stream, evflags));
     if (plan->num16 > 0) {
         Dp16Args a{};
@@ -1174,6 +1339,54 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
                 const int grid = int(std::min<int64_t>(plan->grid16[plan->variant16],
                                                         (int64_t(ab.num_tasks) * 32 + kBlock - 1) / kBlock));
                 launch_dp16(plan->variant16, plan->affine, grid, ab, ctx->stream);
+                ++launches;
+            }
+        }
+        GBA_CUDA(ctx, cudaGetLastError());
+    }
+    if (plan->num_w2 > 0) {
+        Warp2Args w{};
+        w.seq_h = dseq_h;
+        w.seq_v = dseq_v;
+        w.pairs = plan->pairs.as<PairDesc>();
+        w.tasks = plan->tasks_w2.as<int2>();
+        w.rowbuf = plan->rowbuf_w2.as<uint32_t>();
+        w.rowbuf_off = plan->rowbuf_w2_off.as<int64_t>();
+        w.bands = plan->band_w2.as<BandState>();
+        w.band_base = plan->band_w2_base.as<int64_t>();
+        w.error = ctx->err_word.as<int32_t>() + plan->err_slot;
+        w.trace = plan->traceback ? plan->trace.as<uint8_t>() : nullptr;
+        w.score = dscore;
+        w.end_h = end_h;
+        w.end_v = end_v;
+        w.best_e = plan->traceback ? plan->best_e.as<int32_t>() : nullptr;
+        w.best_f = plan->traceback ? plan->best_f.as<int32_t>() : nullptr;
+        w.matrix = plan->matrix ? plan->matrix_dev.as<int32_t>() : nullptr;
+        w.task_counter = plan->counter_w2.as<int32_t>();
+        w.num_tasks = int32_t(plan->num_w2_tasks);
+        w.match = plan->params.match;
+        w.mismatch = plan->params.mismatch;
+        w.gap_open = plan->params.gap_open;
+        w.gap_extend = plan->params.gap_extend;
+        w.free_ends = plan->free_ends;
+        w.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
+        const size_t nb2 = plan->w2b_start.size();
+        GBA_CUDA(ctx, cudaMemsetAsync(plan->counter_w2.ptr, 0, sizeof(int32_t) * std::max<size_t>(nb2, 1), ctx->stream));
+        if (plan->num_w2_states > 0)
+            GBA_CUDA(ctx, cudaMemsetAsync(plan->band_w2.ptr, 0, plan->num_w2_states * sizeof(BandState), ctx->stream));
+        const Warp2Launcher wl = pick_warp2(plan->affine, plan->local, plan->matrix, plan->traceback);
+        if (nb2 == 0) {
+            wl(w, int(std::min<int64_t>(plan->grid_w2, (plan->num_w2_tasks * 32 + kBlock - 1) / kBlock)), ctx->stream);
+            ++launches;
+        } else {
+            // Plain form: one launch per length bucket.
+            for (size_t b = 0; b < nb2; ++b) {
+                Warp2Args wb = w;
+                wb.tasks = w.tasks + plan->w2b_start[b];
+                wb.num_tasks = int32_t(plan->w2b_count[b]);
+                wb.task_counter = w.task_counter + b;
+                wl(wb, int(std::min<int64_t>(plan->grid_w2, (plan->w2b_count[b] * 32 + kBlock - 1) / kBlock)),
+                   ctx->stream);
                 ++launches;
             }
         }
@@ -1235,12 +1448,9 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         const size_t nbw = plan->wb_start.size();
         GBA_CUDA(ctx, cudaMemsetAsync(plan->counter_warp.ptr, 0, sizeof(int32_t) * std::max<size_t>(nbw, 1),
                                       ctx->stream));
-        if (plan->num_band_states > 0) {
+        if (plan->num_band_states > 0)
             GBA_CUDA(ctx, cudaMemsetAsync(plan->band_state.ptr, 0, plan->num_band_states * sizeof(BandState),
                                           ctx->stream));
-            GBA_CUDA(ctx, cudaMemsetAsync(ctx->err_word.as<int32_t>() + plan->err_slot, 0, sizeof(int32_t),
-                                          ctx->stream));
-        }
         const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
         const WarpLauncher wl = pick_warp(plan->affine, plan->local, plan->matrix, plan->traceback);
         if (nbw == 0) {
@@ -1339,6 +1549,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
             t.band_w = plan->params.band_on ? plan->params.band_upper - plan->params.band_lower + 1 : 0;
             t.band_upper = plan->params.band_upper;
             t.warp_rows = plan->use_warp ? plan->warp_rows : 0;
+            t.warp2 = 0;
             const int64_t L = plan->num_tiled_tb;
             if (L > 0) {
                 TraceArgs tl = t;
@@ -1353,6 +1564,32 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
                 k_traceback<<<int((ts.num_slots + kBlock - 1) / kBlock), kBlock, 0, ctx->stream>>>(ts);
                 ++launches;
             }
+            GBA_CUDA(ctx, cudaGetLastError());
+        }
+        if (plan->num_w2 > 0) {
+            TraceArgs t{};
+            t.pairs = plan->pairs.as<PairDesc>();
+            t.order = plan->order_w2.as<int32_t>();
+            t.trace = plan->trace.as<uint8_t>();
+            t.score = dscore;
+            t.end_h = end_h;
+            t.end_v = end_v;
+            t.best_e = plan->best_e.as<int32_t>();
+            t.best_f = plan->best_f.as<int32_t>();
+            t.begin_h = plan->begin_h.as<int32_t>();
+            t.begin_v = plan->begin_v.as<int32_t>();
+            t.seg_slots = plan->seg_slots.as<uint32_t>();
+            t.seg_slot_off = plan->seg_slot_off.as<int64_t>();
+            t.seg_count = plan->seg_count.as<int32_t>();
+            t.cigar_slots = plan->cigar ? plan->cig_slots.as<uint32_t>() : nullptr;
+            t.cigar_slot_off = plan->cigar ? plan->cig_slot_off.as<int64_t>() : nullptr;
+            t.cigar_count = plan->cigar ? plan->cig_count.as<int32_t>() : nullptr;
+            t.num_slots = plan->num_w2;
+            t.affine = plan->affine;
+            t.local = plan->local;
+            t.warp2 = 1;
+            k_traceback<<<int((plan->num_w2 + kBlock - 1) / kBlock), kBlock, 0, ctx->stream>>>(t);
+            ++launches;
             GBA_CUDA(ctx, cudaGetLastError());
         }
         // Dense packing: exclusive scan of the counts, then a copy per pair.
@@ -1438,11 +1675,11 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
         const int rc = enqueue_plan(ctx, plan, dseq_h, dseq_v, dscore, dend_h, dend_v, false);
         if (rc) return rc;
     }
-    if (plan->use_warp && plan->num_band_states > 0) ctx->check_err |= 1u << plan->err_slot;
+    if ((plan->use_warp && plan->num_band_states > 0) || plan->num_w2_states > 0) ctx->check_err |= 1u << plan->err_slot;
     ctx->stats.kernel_launches = plan->launches;
     ctx->stats.tile_rows = plan->num16 ? kVariants16[plan->variant16].rows : 0;
     ctx->stats.tile_min_blocks = plan->num16 ? kVariants16[plan->variant16].minb : 0;
-    ctx->stats.dp_kernels = (plan->num16 > 0 ? GBA_KERNEL_PACKED : 0) |
+    ctx->stats.dp_kernels = (plan->num16 > 0 ? GBA_KERNEL_PACKED : 0) | (plan->num_w2 > 0 ? GBA_KERNEL_WARP16 : 0) |
                             (plan->num_slots > 0 ? (plan->params.band_on ? GBA_KERNEL_BANDED
                                                     : plan->use_warp ? GBA_KERNEL_WARP : GBA_KERNEL_STRIP)
                                                  : 0);

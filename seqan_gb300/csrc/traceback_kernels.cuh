@@ -19,6 +19,7 @@
 #include "dp_common.cuh"
 #include "dp_banded_kernels.cuh"
 #include "dp_warp_kernels.cuh"
+#include "dp_warp2_kernels.cuh"
 
 namespace gba {
 
@@ -174,7 +175,9 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     const int m = d.m;
     const uint8_t *T = a.trace + d.trace_off;
     const int bw = a.band_w, bu = a.band_upper, wr = a.warp_rows;
+    const bool w2 = a.warp2 != 0, affine = a.affine != 0;
     auto TAT = [&](int c, int r) -> int {
+        if (w2) return int(trace_at_warp2(T, m, d.n, affine, c, r));
         if (wr) return int(trace_at_warp(T, m, d.n, wr, c, r));
         return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
     };

@@ -124,7 +124,7 @@ def test_protein_local_traceback_20k(engine):
         _assert_scores(out, ref, f"flags {flags}")
         assert np.array_equal(out.begin_h, ref.begin_h) and np.array_equal(out.begin_v, ref.begin_v)
         _assert_segments(out, ref, f"flags {flags}")
-        assert sg.default_context().stats().dp_kernels & N.GBA_KERNEL_WARP
+        assert sg.default_context().stats().dp_kernels & (N.GBA_KERNEL_WARP | N.GBA_KERNEL_WARP16)
 
 
 # --- Banded semi-global read verification, 1,000,000 reads vs 170 bp windows, band (-6, 26) ---
