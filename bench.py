@@ -70,6 +70,9 @@ WORKLOADS["fasta_reads_2m"] = ("FASTA text of 2000000 reads of 150 bp (ids 'read
                                "columns, 3% lower case, 0.1% N), about 345 MB; readRecord loop into Dna5 codes + "
                                "record offsets")
 FASTA_WORKLOADS = {"fasta_reads_2m"}
+WORKLOADS["dynamic_dna_tb_100k"] = ("the 100000 pairs of affine_dna_100k with DynamicGaps cells (one score and two gap "
+                                    "flags per cell; align/dp_formula_dynamic.h), Score(2,-4,-1,-6) int16, global, score + "
+                                    "end position + trace segments")
 WORKLOADS["bam_records_1m"] = ("the 1000000 records of sam_records_1m as uncompressed BAM blocks "
                                "(write(target, record, context, Bam()), no tags, no BGZF)")
 BAM_WORKLOADS = {"bam_records_1m"}
@@ -506,14 +509,17 @@ XDROP_OPS_PER_CELL = 6
 # Algorithmic integer ops per cell (add and max each count one): affine global 9
 # (E: 2 adds + 1 max, F: 2 + 1, S: 1 add + 2 max), affine local 10 (+ max with 0),
 # linear global 5, linear local 6.
-OPS_PER_CELL = {"affine_global": 9, "linear_global": 5, "affine_local": 10, "linear_local": 6}
+OPS_PER_CELL = {"affine_global": 9, "linear_global": 5, "affine_local": 10, "linear_local": 6,
+                # DynamicGaps: two flag-selected gap adds, the gap max, the diagonal add and max
+                "dynamic_global": 5}
 
 
 KERNEL_NAMES = [(2, "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)"),
                 (16, "k_dp_warp2 (64 strips per warp in int16x2 halves, 4-bit trace)"),
                 (4, "k_dp_warp (one warp per 256-row band, anti-diagonal front)"),
                 (8, "k_dp_banded (one pair per thread, band in per-thread slots)"),
-                (1, "k_dp_strip (one pair per thread, int32)")]
+                (1, "k_dp_strip (one pair per thread, int32)"),
+                (32, "k_dp_dynamic (DynamicGaps cells, one pair per thread, int32)")]
 
 
 def measured_hbm_gbs():
@@ -532,10 +538,16 @@ def kernel_label(bits: int) -> str:
 
 class Spec:
     def __init__(self, H, V, score, mode, kind, config=None, band=None, traceback=False, cigar=False,
-                 alphabet_size=4):
+                 alphabet_size=4, dynamic=False):
         self.H, self.V, self.score, self.mode, self.kind = H, V, score, mode, kind
         self.config, self.band, self.traceback, self.cigar = config, band, traceback, cigar
         self.alphabet_size = alphabet_size
+        self.dynamic = dynamic      # DynamicGaps cells
+
+    @property
+    def gaps(self):
+        from seqan_gb300 import _native as N
+        return N.GBA_GAPS_DYNAMIC if self.dynamic else N.GBA_GAPS_AUTO
 
 
 def make_workload(name: str, seed_offset: int = 0) -> Spec:
@@ -555,6 +567,9 @@ def make_workload(name: str, seed_offset: int = 0) -> Spec:
         wins, reads = W.read_windows(1_000_000, seed=4 + seed_offset)
         return Spec(wins, reads, sg.Score(2, -4, -1, -6, dtype=np.int16), 0, "affine_global",
                     config=sg.AlignConfig(True, False, False, True), band=(-6, 26), traceback=True, cigar=True)
+    if name == "dynamic_dna_tb_100k":
+        H, V = W.mutated_dna_pairs(100_000, 100, 300, 0.05, 0.01, seed=2 + seed_offset)
+        return Spec(H, V, sg.Score(2, -4, -1, -6, dtype=np.int16), 0, "dynamic_global", traceback=True, dynamic=True)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -563,7 +578,7 @@ def oracle_problem(spec: Spec):
     fe = spec.config.bits if spec.config is not None else 0
     return O.Problem("local" if spec.mode == 1 else "global", fe, spec.band, spec.score.match,
                      spec.score.mismatch, spec.score.gap_open, spec.score.gap_extend, spec.score.matrix,
-                     spec.score.bits, "aa" if spec.alphabet_size > 5 else "dna")
+                     spec.score.bits, "aa" if spec.alphabet_size > 5 else "dna", dynamic=spec.dynamic)
 
 
 def algorithmic_cells(spec: Spec) -> int:
@@ -761,7 +776,9 @@ def run_reference(args, rank):
     lib = None
     why = None
     try:
-        if O.build_ref_bench():
+        if spec.dynamic:
+            why = "no public batch function of the reference selects DynamicGaps cells"
+        elif O.build_ref_bench():
             lib = O.libref_bench()
         else:
             why = "no copy of the reference's headers (baseline/_ref/include) on this host"
@@ -1249,6 +1266,8 @@ def main():
     ap.add_argument("--pairs", type=int, default=0, help="use only the first N pairs (small profiling cases)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle comparison of the timed results")
+    ap.add_argument("--tile-variant", type=int, default=0,
+                    help="packed kernel tiling variant 1..5 instead of the autotuned one (profiling captures)")
     ap.add_argument("--kernel", default="auto", choices=["auto", "general", "packed16", "plain", "warp32"],
                     help="auto: the engine's routing (packed 16-bit kernels), graph-replayed; "
                          "plain: the same kernels, one launch per length bucket; "
@@ -1357,8 +1376,9 @@ def main():
     flags = {"auto": N.GBA_FLAG_AUTOTUNE, "general": N.GBA_FLAG_GENERAL_KERNEL, "packed16": N.GBA_FLAG_STRIP16,
              "plain": N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH,
              "warp32": N.GBA_FLAG_AUTOTUNE | N.GBA_FLAG_NO_WARP16}[args.kernel]
-    params = sg.align.make_params(score, mode, spec.config, spec.band, outputs,
+    params = sg.align.make_params(score, mode, spec.config, spec.band, outputs, gaps=spec.gaps,
                                   alphabet_size=spec.alphabet_size, flags=flags)
+    params.tile_variant = args.tile_variant
     host_batch = N.GbaBatch(npairs, p_sh, p_oh, p_sv, p_ov, 0, 0)
 
     # Device-resident inputs for `value`.
@@ -1427,7 +1447,8 @@ def main():
     plain = plain_strip = None
     if args.kernel == "auto" and not args.no_plain and spec.band is None:
         def time_plain(extra_flags):
-            pparams = sg.align.make_params(score, mode, spec.config, None, outputs, alphabet_size=spec.alphabet_size,
+            pparams = sg.align.make_params(score, mode, spec.config, None, outputs, gaps=spec.gaps,
+                                           alphabet_size=spec.alphabet_size,
                                            flags=N.GBA_FLAG_PLAIN_BUCKETS | N.GBA_FLAG_NO_GRAPH | extra_flags)
             pplan = C.c_void_p()
             ctx.check(L.gba_plan_create(h, C.byref(pparams), C.byref(host_batch), C.byref(pplan)), "plain plan")

@@ -67,8 +67,11 @@ enum {
 
 enum { GBA_GLOBAL = 0, GBA_LOCAL = 1 };
 /* GBA_GAPS_AUTO picks affine iff gap_open != gap_extend, as the reference's
- * interfaces do (align/global_alignment_unbanded.h:801-810). */
-enum { GBA_GAPS_AUTO = 0, GBA_GAPS_LINEAR = 1, GBA_GAPS_AFFINE = 2 };
+ * interfaces do (align/global_alignment_unbanded.h:801-810).  GBA_GAPS_DYNAMIC selects the
+ * reference's DynamicGaps cells (align/dp_cell_dynamic.h, align/dp_formula_dynamic.h): one score and
+ * two gap flags per cell, a gap extended when the neighbour's flag for its direction is set and
+ * opened otherwise; unbanded global and local alignments (a band is GBA_EUNSUPPORTED). */
+enum { GBA_GAPS_AUTO = 0, GBA_GAPS_LINEAR = 1, GBA_GAPS_AFFINE = 2, GBA_GAPS_DYNAMIC = 3 };
 /* AlignConfig<TOP, LEFT, RIGHT, BOTTOM> (align/align_config.h:52-94). */
 enum { GBA_FREE_TOP = 1, GBA_FREE_LEFT = 2, GBA_FREE_RIGHT = 4, GBA_FREE_BOTTOM = 8 };
 /* Output selection bits. */
@@ -236,7 +239,8 @@ enum {
     GBA_KERNEL_PACKED = 2,     /* two pairs per thread, int16x2 DPX */
     GBA_KERNEL_WARP = 4,       /* bands of 256 rows, one warp per band, anti-diagonal front */
     GBA_KERNEL_BANDED = 8,     /* banded DP, one pair per thread */
-    GBA_KERNEL_WARP16 = 16     /* bands of 64 strips, one warp per band, int16x2 DPX, 4-bit trace */
+    GBA_KERNEL_WARP16 = 16,    /* bands of 64 strips, one warp per band, int16x2 DPX, 4-bit trace */
+    GBA_KERNEL_DYNAMIC = 32    /* DynamicGaps cells, one pair per thread */
 };
 GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats);
 
@@ -327,8 +331,10 @@ GBA_API double gba_clock_seconds(void);
  * gba_align_batch's.
  * Set-up: the first call on a device looks up the array's device address.  Under CUDA's lazy
  * module loading (the default) that is also when the array's memory is committed on the device,
- * so the first call may allocate and synchronize: make it once at start-up, before any stream
- * capture and before a host pool takes the GPU's memory; later calls allocate nothing.  All
+ * and the first call with a given scoring shape (gap model, mode, table or not) loads that shape's
+ * kernel code, so first calls may allocate and synchronize: make one call per shape at start-up
+ * (or run with CUDA_MODULE_LOADING=EAGER), before any stream capture and before a host pool takes
+ * the GPU's memory; repeated calls allocate nothing.  All
  * calls share the array: calls that overlap on the GPU race and must be serialized by the
  * caller.  An error already pending on the calling thread is left in place and reported as
  * GBA_ECUDA without a launch.  Asynchronous on `stream` (a cudaStream_t; NULL = legacy default

@@ -76,6 +76,7 @@ class Problem:
     alphabet: str = "dna"           # "dna" (Dna5 codes) | "aa" (AminoAcid codes)
     xdrop: int | None = None        # mode "extend": the X-drop terminator's threshold
     trace4: bool = False            # trace values through the 4-bit code before the traceback
+    dynamic: bool = False           # DynamicGaps cells (gap open / extend chosen by the neighbour's flag)
 
     @property
     def affine(self) -> bool:
@@ -163,6 +164,9 @@ def libref():
         _ref.ref_pair_segments.argtypes = [C.POINTER(RefParams), C.c_void_p, C.c_int32, C.c_void_p,
                                            C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
         _ref.ref_has_shape.argtypes = [C.c_int32, C.POINTER(RefParams)]
+        if hasattr(_ref, "ref_dynamic_segments"):
+            _ref.ref_dynamic_segments.argtypes = [C.POINTER(RefParams), C.c_void_p, C.c_int32, C.c_void_p,
+                                                  C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
         _ref.ref_blosum62.argtypes = [C.c_void_p]
         _ref.ref_encode.argtypes = [C.c_int32, C.c_char_p, C.c_int64, C.c_void_p]
         _ref.ref_extend_seeds.argtypes = [C.c_int32] * 8 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -190,7 +194,7 @@ def _orc_params(pb: Problem, traceback: bool) -> OrcParams:
     p.mode = {"global": 0, "local": 1, "extend": 2}[pb.mode]
     p.xdrop_on = 0 if pb.xdrop is None else 1
     p.xdrop = 0 if pb.xdrop is None else int(pb.xdrop)
-    p.gap_model = 1 if pb.affine else 0
+    p.gap_model = 2 if pb.dynamic else (1 if pb.affine else 0)
     p.free_ends = pb.free_ends
     p.band_on = 1 if pb.band is not None else 0
     p.band_lower, p.band_upper = (pb.band if pb.band is not None else (0, 0))
@@ -362,6 +366,23 @@ def ref_pair_segments(pb: Problem, h, v):
     p = _ref_params(pb, 1)
     rc = lib.ref_pair_segments(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), C.byref(score),
                                _ptr(segs), cap, C.byref(nseg))
+    if rc != 0:
+        raise RuntimeError(f"reference call shape not instantiated (rc={rc}): {pb}")
+    return score.value, [tuple(int(x) for x in segs[i]) for i in range(nseg.value)]
+
+
+def ref_dynamic_segments(pb: Problem, h, v):
+    """The reference's single-pair DP with DynamicGaps cells: (score, TraceSegment_ list)."""
+    lib = libref()
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    cap = len(h) + len(v) + 8
+    segs = np.zeros((cap, 4), dtype=np.uint32)
+    score = C.c_int32(0)
+    nseg = C.c_int32(0)
+    p = _ref_params(pb, 1)
+    rc = lib.ref_dynamic_segments(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), C.byref(score), _ptr(segs), cap,
+                                  C.byref(nseg))
     if rc != 0:
         raise RuntimeError(f"reference call shape not instantiated (rc={rc}): {pb}")
     return score.value, [tuple(int(x) for x in segs[i]) for i in range(nseg.value)]

@@ -55,6 +55,15 @@ int ref_pair_segments(const ref_params * pp, const uint8_t * h, int32_t m, const
     return reinterpret_cast<seqan_ref::seg_fn>(f)(*pp, h, m, v, n, score, segs, cap, nseg);
 }
 
+// DynamicGaps cells (kind 3): score and raw TraceSegment_ list of the single-pair DP.
+int ref_dynamic_segments(const ref_params * pp, const uint8_t * h, int32_t m, const uint8_t * v, int32_t n,
+                         int32_t * score, uint32_t * segs, int32_t cap, int32_t * nseg)
+{
+    void * f = seqan_ref::find(3, *pp);
+    if (!f) return -1;
+    return reinterpret_cast<seqan_ref::seg_fn>(f)(*pp, h, m, v, n, score, segs, cap, nseg);
+}
+
 // 1 if the call shape is instantiated.
 int ref_has_shape(int32_t kind, const ref_params * pp)
 {

@@ -49,6 +49,7 @@ typedef struct {
     int local;
     int extend;     /* AlignExtend_: every cell tracked, no zero floor */
     int affine;
+    int dynamic;    /* DynamicGaps: one score and two gap-extension flags per cell */
     int ext, open;
     int match, mismatch;
     const int32_t *mat;
@@ -77,6 +78,90 @@ typedef struct {
     int vS, vF;      /* cacheVert._score, cacheVert._verticalScore */
 } caches_t;
 
+/* DynamicGaps cell flags (align/dp_cell_dynamic.h: MASK_VERTICAL_GAP, MASK_HORIZONTAL_GAP). */
+#define DYN_V 1
+#define DYN_H 2
+
+/* One DynamicGaps cell (align/dp_formula_dynamic.h, scalar SingleTrace overloads).  A cell holds a
+ * score and two flags telling whether it ends in a vertical / horizontal gap; a gap from a
+ * neighbour is extended when the neighbour's flag for that direction is set, else opened.
+ * colS/colE hold the previous column's score and flags at row i; k->vS / k->vF the cell above. */
+static inline int compute_cell_dynamic(const ctx_t *c, int dir, int *colS, int *colE, caches_t *k,
+                                       uint8_t hv, uint8_t vv, int *fOut)
+{
+    int tv = TV_NONE, s = 0, fl = 0, tmp, tvGap;
+    const int hS = *colS, hF = *colE;
+    switch (dir) {
+    case DIR_ZERO:   /* align/dp_formula_dynamic.h: RecursionDirectionZero */
+        *colS = 0;
+        *colE = 0;
+        k->dS = 0;
+        k->vS = 0;
+        k->vF = 0;
+        *fOut = 0;
+        return TV_NONE;
+    case DIR_ALL: {  /* _computeScore [RecursionDirectionAll, DynamicGaps] */
+        int inter = wr(c, (long)k->dS + sub_score(c, hv, vv));
+        k->dS = hS;
+        if (hF & DYN_H) { tmp = wr(c, (long)hS + c->ext); tvGap = TV_H; }
+        else { tmp = wr(c, (long)hS + c->open); tvGap = TV_HO; }
+        if (k->vF & DYN_V) { s = wr(c, (long)k->vS + c->ext); tvGap |= TV_V; }
+        else { s = wr(c, (long)k->vS + c->open); tvGap |= TV_VO; }
+        if (s < tmp) { s = tmp; fl = DYN_H; tv = TV_MFH; }
+        else { fl = DYN_V; tv = TV_MFV; }
+        if (s <= inter) { s = inter; fl = 0; tv = TV_DIAG | tvGap; }
+        else tv = tvGap | tv;
+        break;
+    }
+    case DIR_HORIZONTAL:   /* row 0: extend when the left cell ended in a horizontal gap */
+        k->dS = hS;
+        fl = DYN_H;
+        if (hF & DYN_H) { s = wr(c, (long)hS + c->ext); tv = TV_H; }
+        else { s = wr(c, (long)hS + c->open); tv = TV_HO; }
+        tv |= TV_MFH;
+        *colS = s;
+        *colE = fl;
+        k->vS = s;
+        k->vF = fl;
+        *fOut = fl;
+        return tv;         /* no zero floor in this overload */
+    case DIR_VERTICAL:     /* column 0 */
+        fl = DYN_V;
+        if (k->vF & DYN_V) { s = wr(c, (long)k->vS + c->ext); tv = TV_V; }
+        else { s = wr(c, (long)k->vS + c->open); tv = TV_VO; }
+        tv |= TV_MFV;
+        break;
+    case DIR_UPPER: {      /* banded: no vertical predecessor */
+        int inter = wr(c, (long)k->dS + sub_score(c, hv, vv));
+        k->dS = hS;
+        if (hF & DYN_H) { s = wr(c, (long)hS + c->ext); tv = TV_H; }
+        else { s = wr(c, (long)hS + c->open); tv = TV_HO; }
+        fl = DYN_H;
+        if (s <= inter) { s = inter; fl = 0; tv = TV_DIAG | tv; }
+        else tv = tv | TV_MFH;
+        break;
+    }
+    default: {             /* DIR_LOWER: no horizontal predecessor; the cell above is kept */
+        if (k->vF & DYN_V) { s = wr(c, (long)k->vS + c->ext); tv = TV_V; }
+        else { s = wr(c, (long)k->vS + c->open); tv = TV_VO; }
+        fl = DYN_V;
+        tmp = wr(c, (long)k->dS + sub_score(c, hv, vv));
+        if (s <= tmp) { s = tmp; fl = 0; tv = TV_DIAG | tv; }
+        else tv = tv | TV_MFV;
+        break;
+    }
+    }
+    if (c->local) {
+        /* _maxScore(score, NONE, score, NONE, tv): 0 wins ties; the flags stay as they are. */
+        if (!(0 < s)) { s = 0; tv = TV_NONE; }
+    }
+    *colS = s;
+    *colE = fl;
+    if (dir != DIR_LOWER) { k->vS = s; k->vF = fl; }
+    *fOut = fl;
+    return tv;
+}
+
 /* Computes one cell in place.  colS/colE hold the previous column's S/E at row i on entry
  * (the sparse matrix cell) and this column's on exit.  Returns the trace value. */
 static inline int compute_cell(const ctx_t *c, int dir, int *colS, int *colE, caches_t *k,
@@ -85,6 +170,7 @@ static inline int compute_cell(const ctx_t *c, int dir, int *colS, int *colE, ca
     int tv = TV_NONE, t2, s, e, f;
     int hS = *colS, hE = *colE;   /* previous horizontal cell (same row, previous column) */
 
+    if (c->dynamic) return compute_cell_dynamic(c, dir, colS, colE, k, hv, vv, fOut);
     switch (dir) {
     case DIR_ZERO:
         /* align/dp_formula.h:295-309: score 0; E of the cell and F of cacheVert stay. */
@@ -602,11 +688,11 @@ static void dp_unbanded(const ctx_t *c, int fe, const uint8_t *h, int m, const u
 {
     int i, j;
     int terminated = 0, colmax = INT_MIN;
-    for (i = 0; i <= n; ++i) { colS[i] = c->inf; colE[i] = c->inf; }
+    for (i = 0; i <= n; ++i) { colS[i] = c->inf; colE[i] = c->dynamic ? 0 : c->inf; }
     for (j = 0; j <= m; ++j) {
         caches_t k;
         int finalCol = (j == m);
-        k.dS = c->inf; k.vS = c->inf; k.vF = c->inf;
+        k.dS = c->inf; k.vS = c->inf; k.vF = c->dynamic ? 0 : c->inf;
         for (i = 0; i <= n; ++i) {
             int dir, tv, f;
             int tracked;
@@ -674,6 +760,7 @@ int orc_align_pair(const orc_params *p,
     c.local = (p->mode == ORC_LOCAL);
     c.extend = (p->mode == ORC_EXTEND);
     c.affine = (p->gap_model == ORC_AFFINE);
+    c.dynamic = (p->gap_model == ORC_DYNAMIC);
     c.ext = p->gap_extend;
     c.open = p->gap_open;
     c.match = p->match;
@@ -682,6 +769,7 @@ int orc_align_pair(const orc_params *p,
     c.asz = p->alphabet_size;
     fe = c.local ? (ORC_FREE_TOP | ORC_FREE_LEFT | ORC_FREE_RIGHT | ORC_FREE_BOTTOM) : (c.extend ? 0 : p->free_ends);
     if (c.extend && p->band_on) return -1;   /* the banded extension is not restated */
+    if (c.dynamic && (p->band_on || c.extend)) return -1;   /* DynamicGaps: unbanded global / local */
 
     if (m <= 0 || n <= 0 || !band_valid(p, m, n, fe)) {
         out->score = c.bits16 ? -32768 : INT_MIN;
@@ -714,10 +802,14 @@ int orc_align_pair(const orc_params *p,
             size_t q, cells = (size_t)(m + 1) * (size_t)(n + 1);
             for (q = 0; q < cells; ++q) T[q] = orc_trace4_decode(orc_trace4_encode(T[q]), c.affine);
         }
-        /* _correctTraceValue (align/dp_algorithm_impl.h:1188-1205), affine only. */
+        /* _correctTraceValue (align/dp_algorithm_impl.h:1188-1205) for affine cells; for DynamicGaps
+         * cells the best cell's flags decide (:1235-1249; the scout keeps the flags in b.e). */
         if (c.affine) {
             if (b.f == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFV; }
             else if (b.e == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFH; }
+        } else if (c.dynamic) {
+            if (b.e & DYN_V) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFV; }
+            else if (b.e & DYN_H) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFH; }
         }
         sb.segs = segs; sb.cap = segs ? seg_cap : 0; sb.n = 0; sb.overflow = 0;
         traceback(&c, T, n, m, b.col, b.row, &sb, !c.local && !c.extend, !c.local);

@@ -30,14 +30,14 @@ enum {
  * profile (align_extend/align_extend_base.h), i.e. a gap-initialised first row and column, every
  * cell tracked without a zero floor, traceback to (0, 0) with no tail; unbanded. */
 enum { ORC_GLOBAL = 0, ORC_LOCAL = 1, ORC_EXTEND = 2 };
-enum { ORC_LINEAR = 0, ORC_AFFINE = 1 };
+enum { ORC_LINEAR = 0, ORC_AFFINE = 1, ORC_DYNAMIC = 2 };
 
 /* TraceSegment_ direction values (align/dp_profile.h:121-135). */
 enum { ORC_SEG_DIAGONAL = 1, ORC_SEG_HORIZONTAL = 2, ORC_SEG_VERTICAL = 4 };
 
 typedef struct {
     int32_t mode;           /* ORC_GLOBAL / ORC_LOCAL / ORC_EXTEND */
-    int32_t gap_model;      /* ORC_LINEAR / ORC_AFFINE */
+    int32_t gap_model;      /* ORC_LINEAR / ORC_AFFINE / ORC_DYNAMIC (DPCell_<T, DynamicGaps>) */
     int32_t free_ends;      /* ORC_FREE_* bits, ignored for local (all free) */
     int32_t band_on;        /* 0 / 1 */
     int32_t band_lower;     /* lower diagonal, col - row convention */

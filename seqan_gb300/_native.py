@@ -25,7 +25,7 @@ GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUP
     range(9)
 GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED, GBA_PAIR_FAILED, GBA_PAIR_SKIPPED = 0, 1, 2, 3, 4
 GBA_GLOBAL, GBA_LOCAL = 0, 1
-GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE = 0, 1, 2
+GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE, GBA_GAPS_DYNAMIC = 0, 1, 2, 3
 GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
 GBA_OUT_SCORE, GBA_OUT_END, GBA_OUT_SEGMENTS, GBA_OUT_CIGAR = 1, 2, 4, 8
 GBA_SEG_DIAGONAL, GBA_SEG_HORIZONTAL, GBA_SEG_VERTICAL = 1, 2, 4
@@ -34,6 +34,7 @@ GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16, GBA_FLAG_PLAIN_BUCKETS, GBA_FLAG_NO_G
 GBA_FLAG_PACKED = 32
 GBA_FLAG_PACKED_SPLIT, GBA_FLAG_PACKED_NO_SPLIT, GBA_FLAG_NO_WARP16, GBA_FLAG_WARP16 = 64, 128, 256, 512
 GBA_KERNEL_STRIP, GBA_KERNEL_PACKED, GBA_KERNEL_WARP, GBA_KERNEL_BANDED, GBA_KERNEL_WARP16 = 1, 2, 4, 8, 16
+GBA_KERNEL_DYNAMIC = 32
 GBA_MATCH_EXTEND, GBA_UNGAPPED_XDROP, GBA_GAPPED_XDROP = 0, 1, 2
 GBA_EXTEND_NONE, GBA_EXTEND_LEFT, GBA_EXTEND_RIGHT, GBA_EXTEND_BOTH = 0, 1, 2, 3
 

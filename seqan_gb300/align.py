@@ -114,10 +114,10 @@ def _vp(a):
 
 
 def make_params(score, mode: int, config: AlignConfig | None, band, outputs: int,
-                alphabet_size: int = 0, flags: int = 0) -> N.GbaParams:
+                alphabet_size: int = 0, flags: int = 0, gaps: int = N.GBA_GAPS_AUTO) -> N.GbaParams:
     p = N.GbaParams()
     p.mode = mode
-    p.gap_model = N.GBA_GAPS_AUTO
+    p.gap_model = gaps
     p.free_ends = config.bits if (config is not None and mode == N.GBA_GLOBAL) else 0
     if band is not None:
         p.band_on, p.band_lower, p.band_upper = 1, int(band[0]), int(band[1])
@@ -162,12 +162,13 @@ ALPHABET_SIZE = {"dna": 4, "dna5": 5, "aa": 27}
 def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=None,
                 traceback=False, cigar=False, h_shared=False, ctx: N.Context | None = None,
                 alphabet_size: int | None = None, flags: int = 0, packed_bits: int | None = None,
-                fasta_texts=None, tile_variant: int = 0) -> BatchOutput:
+                fasta_texts=None, tile_variant: int = 0, gaps: int = N.GBA_GAPS_AUTO) -> BatchOutput:
     """Aligns lists of code arrays through gba_align_batch.
 
     alphabet_size bounds the codes (the reference's ValueSize of the alphabet); when None it is
     taken from the codes themselves.  packed_bits (2 Dna, 3 Dna5, 5 AminoAcid) sends the sequences
-    as String<TValue, Packed<>> host words through gba_align_packed instead."""
+    as String<TValue, Packed<>> host words through gba_align_packed instead.  gaps selects the gap
+    cost model (N.GBA_GAPS_DYNAMIC: the reference's DynamicGaps cells)."""
     ctx = ctx or N.default_context()
     n = len(codes_v)
     sh, oh = _concat(codes_h)
@@ -179,7 +180,7 @@ def align_codes(codes_h, codes_v, score, mode=N.GBA_GLOBAL, config=None, band=No
         outputs |= N.GBA_OUT_CIGAR | N.GBA_OUT_SEGMENTS
     if alphabet_size is None:
         alphabet_size = int(max(sh.max(initial=0), sv.max(initial=0))) + 1 if n else 0
-    params = make_params(score, mode, config, band, outputs, alphabet_size, flags)
+    params = make_params(score, mode, config, band, outputs, alphabet_size, flags, gaps)
     params.tile_variant = tile_variant
     b = N.GbaBatch(n, _vp(sh), _vp(oh), _vp(sv), _vp(ov), 1 if h_shared else 0, 0)
     res = BatchOutput(score=np.zeros(n, np.int32), end_h=np.zeros(n, np.int32), end_v=np.zeros(n, np.int32),

@@ -80,6 +80,7 @@ struct TraceArgs {
     int32_t band_upper;
     int32_t warp_rows;     // warp layout: rows per lane strip (0: not the warp layout)
     int32_t warp2;         // 1: the packed 16-bit warp layout with 4-bit cells (dp_warp2_kernels.cuh)
+    int32_t dynamic;       // 1: DynamicGaps cells; best_e holds the best cell's gap flags
 };
 
 __host__ __device__ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }

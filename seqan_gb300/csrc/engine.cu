@@ -12,6 +12,7 @@
 #include "dp_banded_kernels.cuh"
 #include "dp_warp_kernels.cuh"
 #include "dp_warp2_kernels.cuh"
+#include "dp_dynamic_kernels.cuh"
 #include "seed_kernels.cuh"
 #include "extend_kernels.cuh"
 #include "int_peak.cuh"
@@ -83,6 +84,7 @@ struct gba_plan {
     bool traceback = false;
     bool cigar = false;
     bool affine = false;
+    bool dynamic = false;           // DynamicGaps cells (dp_dynamic_kernels.cuh)
     bool local = false;
     bool matrix = false;
     int32_t free_ends = 0;
@@ -292,7 +294,7 @@ int64_t band_cells(int64_t m, int64_t n, int64_t lo, int64_t up)
 
 bool is_affine(const gba_params &p)
 {
-    if (p.gap_model == GBA_GAPS_LINEAR) return false;
+    if (p.gap_model == GBA_GAPS_LINEAR || p.gap_model == GBA_GAPS_DYNAMIC) return false;
     if (p.gap_model == GBA_GAPS_AFFINE) return true;
     return p.gap_open != p.gap_extend;
 }
@@ -331,7 +333,9 @@ int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
 {
     if (!p || !b) return fail(ctx, GBA_EINVAL, "null params or batch");
     if (p->mode != GBA_GLOBAL && p->mode != GBA_LOCAL) return fail(ctx, GBA_EINVAL, "bad mode %d", p->mode);
-    if (p->gap_model < 0 || p->gap_model > 2) return fail(ctx, GBA_EINVAL, "bad gap model");
+    if (p->gap_model < 0 || p->gap_model > 3) return fail(ctx, GBA_EINVAL, "bad gap model");
+    if (p->gap_model == GBA_GAPS_DYNAMIC && p->band_on)
+        return fail(ctx, GBA_EUNSUPPORTED, "DynamicGaps cells are supported unbanded only");
     if (p->score_bits != 16 && p->score_bits != 32) return fail(ctx, GBA_EINVAL, "score_bits must be 16 or 32");
     if (p->free_ends & ~15) return fail(ctx, GBA_EINVAL, "bad free_ends bits");
     if (p->matrix && (p->alphabet_size <= 0 || p->alphabet_size > 32))
@@ -539,6 +543,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->params = *p;
     plan->num_pairs = N;
     plan->affine = is_affine(*p);
+    plan->dynamic = p->gap_model == GBA_GAPS_DYNAMIC;
     plan->local = p->mode == GBA_LOCAL;
     plan->free_ends = p->free_ends;
     plan->traceback = (p->outputs & GBA_OUT_SEGMENTS) != 0;
@@ -554,7 +559,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     // at most 8 codes (the caller's alphabet_size), table entries that fit a byte, and gaps that
     // keep int16 arithmetic exact (checked per pair below).
     const bool plain = (p->flags & GBA_FLAG_PLAIN_BUCKETS) != 0;
-    const bool packed_ok = !plan->local && !plan->traceback && !plan->matrix && !p->band_on &&
+    const bool packed_ok = !plan->local && !plan->traceback && !plan->matrix && !p->band_on && !plan->dynamic &&
                            !(p->flags & GBA_FLAG_GENERAL_KERNEL) &&
                            (N >= kPackedMinPairs || (p->flags & (GBA_FLAG_STRIP16 | GBA_FLAG_PACKED))) &&
                            p->alphabet_size >= 1 &&
@@ -564,7 +569,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->rows16 = 32;
     // Pairs that are neither banded nor on the packed path run one warp per pair, unless the
     // one-pair-per-thread kernel is forced.
-    plan->use_warp = !p->band_on && !(p->flags & GBA_FLAG_GENERAL_KERNEL);
+    plan->use_warp = !p->band_on && !(p->flags & GBA_FLAG_GENERAL_KERNEL) && !plan->dynamic;
     plan->warp_rows = 8;
     // The packed 16-bit warp path: 16-bit cells, a batch large enough to fill the GPU with one
     // warp per pair, equality scoring over at most 8 codes (PRMT lookup) or a table whose entries
@@ -1249,6 +1254,21 @@ DpLauncher pick_dp(bool a, bool l, bool m, bool t)
     return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
 }
 
+template <bool L, bool M, bool T>
+void launch_dynamic(const DpArgs &args, int grid, size_t smem, cudaStream_t s)
+{
+    k_dp_dynamic<L, M, T><<<grid, kBlock, smem, s>>>(args);
+}
+
+DpLauncher pick_dynamic(bool l, bool m, bool t)
+{
+    static const DpLauncher table[8] = {launch_dynamic<false, false, false>, launch_dynamic<false, false, true>,
+                                        launch_dynamic<false, true, false>,  launch_dynamic<false, true, true>,
+                                        launch_dynamic<true, false, false>,  launch_dynamic<true, false, true>,
+                                        launch_dynamic<true, true, false>,   launch_dynamic<true, true, true>};
+    return table[(l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
 __global__ void k_widen(const int32_t *src, int64_t *dst, int64_t n)
 {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -1495,7 +1515,8 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         a.free_ends = plan->free_ends;
         a.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
         const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
-        DpLauncher launch = pick_dp(plan->affine, plan->local, plan->matrix, plan->traceback);
+        DpLauncher launch = plan->dynamic ? pick_dynamic(plan->local, plan->matrix, plan->traceback)
+                                          : pick_dp(plan->affine, plan->local, plan->matrix, plan->traceback);
         if (!plan->bucket_start.empty()) {
             for (size_t b = 0; b < plan->bucket_start.size(); ++b) {
                 DpArgs ab = a;
@@ -1550,6 +1571,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
             t.band_upper = plan->params.band_upper;
             t.warp_rows = plan->use_warp ? plan->warp_rows : 0;
             t.warp2 = 0;
+            t.dynamic = plan->dynamic;
             const int64_t L = plan->num_tiled_tb;
             if (L > 0) {
                 TraceArgs tl = t;
@@ -1681,7 +1703,8 @@ int run_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const uint
     ctx->stats.tile_min_blocks = plan->num16 ? kVariants16[plan->variant16].minb : 0;
     ctx->stats.dp_kernels = (plan->num16 > 0 ? GBA_KERNEL_PACKED : 0) | (plan->num_w2 > 0 ? GBA_KERNEL_WARP16 : 0) |
                             (plan->num_slots > 0 ? (plan->params.band_on ? GBA_KERNEL_BANDED
-                                                    : plan->use_warp ? GBA_KERNEL_WARP : GBA_KERNEL_STRIP)
+                                                    : plan->use_warp ? GBA_KERNEL_WARP
+                                                    : plan->dynamic ? GBA_KERNEL_DYNAMIC : GBA_KERNEL_STRIP)
                                                  : 0);
     ctx->stats_pending = true;
     return GBA_OK;

@@ -13,9 +13,11 @@
 // Set-up: the first call on each device looks up that device's address of the array with
 // cudaGetSymbolAddress (the device must be current).  With CUDA's lazy module loading (the
 // default) that lookup is also when this file's module is loaded on the device and the array's
-// 64 MiB are committed, so the first call may allocate and synchronize: make it once at start-up,
-// before any stream capture starts and before a host pool reserves the GPU's memory.  Every
-// later call allocates nothing.  All calls share the array and it keeps the previous call's
+// 64 MiB are committed, and the first call of each scoring shape (affine or linear, global or
+// local, table or not) loads that kernel's code, so first calls may allocate and synchronize: make
+// one per shape at start-up (or run with CUDA_MODULE_LOADING=EAGER), before any stream capture
+// starts and before a host pool reserves the GPU's memory.  Repeated calls allocate nothing.  All
+// calls share the array and it keeps the previous call's
 // contents; the kernel writes every scratch element before reading it, so nothing has to be
 // cleared.  Calls that overlap on the GPU (on different streams, or from several threads)
 // race on the array and must be serialized by the caller.
@@ -225,6 +227,7 @@ extern "C" GBA_API int gba_align_score_noalloc(const gba_params *params, const g
     if (batch->num_pairs < 0) return GBA_EINVAL;
     if (params->mode != GBA_GLOBAL && params->mode != GBA_LOCAL) return GBA_EINVAL;
     if (params->score_bits != 16 && params->score_bits != 32) return GBA_EINVAL;
+    if (params->gap_model < 0 || params->gap_model > GBA_GAPS_AFFINE) return GBA_EUNSUPPORTED;
     if (params->free_ends & ~15) return GBA_EINVAL;
     if (params->band_on || (params->outputs & (GBA_OUT_SEGMENTS | GBA_OUT_CIGAR))) return GBA_EUNSUPPORTED;
     if (batch->max_h_len < 1) return GBA_EINVAL;

@@ -69,6 +69,12 @@ __device__ __forceinline__ void traceback_pair(const TraceArgs &a, int p, Cell &
         const int s = a.score[p];
         if (a.best_f[p] == s) { tv &= ~TV_DIAG; tv |= TV_MFV; }
         else if (a.best_e[p] == s) { tv &= ~TV_DIAG; tv |= TV_MFH; }
+    } else if (a.dynamic) {
+        // DynamicGaps: the best cell's flags (vertical first) decide
+        // (align/dp_algorithm_impl.h:1235-1249).
+        const int fl = a.best_e[p];
+        if (fl & 1) { tv &= ~TV_DIAG; tv |= TV_MFV; }
+        else if (fl & 2) { tv &= ~TV_DIAG; tv |= TV_MFH; }
     }
     int last;
     if (affine) {

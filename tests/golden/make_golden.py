@@ -15,6 +15,9 @@ Outputs (all small, committed):
                         (the bits that hold no value, undefined there, masked to zero).
   extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
                         (align_extend/align_extend.h) with and without X-drop: score and rows.
+  dynamic_cases.json    pairs aligned by the reference's single-pair DP with DynamicGaps cells
+                        (score and raw TraceSegment_ list) for the shapes oracle/ref/units/dynamic_*.cpp
+                        instantiate.
   cpp_binding_expected.txt  the output of tests/cpp/seqan_binding.cpp built with
                         -DGBA_AS_REFERENCE: the binding's calls run by the reference itself.
   aa_background.json    residue counts of the reference's T-Coffee test FASTA files, the
@@ -111,6 +114,9 @@ def main():
         return
     if only == "cpp":
         write_cpp_binding()
+        return
+    if only == "dynamic":
+        write_dynamic_cases(b62)
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -571,6 +577,32 @@ def write_bam_cases():
         json.dump({"generator": "tests/golden/make_golden.py --only bam", "seed": 20261209,
                    "iupac": O.ref_iupac_table().tolist(), "cases": cases}, f, separators=(",", ":"))
     print(f"{sum(len(c['qname']) for c in cases)} BAM records written")
+
+
+def write_dynamic_cases(b62):
+    """Seeded pairs through the reference's DP with DynamicGaps cells, for every instantiated shape."""
+    rng = np.random.Generator(np.random.PCG64(20261205))
+    shapes = [("global", fe, 32, "dna") for fe in (0, 15, 9, 6)] + [("local", 0, 32, "dna"), ("global", 0, 16, "dna"),
+                                                                   ("local", 0, 16, "dna"), ("local", 0, 16, "aa"),
+                                                                   ("global", 0, 16, "aa")]
+    schemes = [(2, -3, -5, -5), (2, -4, -6, -1), (4, -2, -10, -4), (1, -1, -2, -2), (3, -2, -4, -1), (2, -3, -1, -7)]
+    cases = []
+    for mode, fe, bits, alph in shapes:
+        for sc in schemes if alph == "dna" else [(0, 0, -11, -1), (0, 0, -8, -2)]:
+            mt, mm, go, ge = sc
+            mat = b62 if alph == "aa" else None
+            pb = O.Problem(mode, fe, None, mt, mm, go, ge, mat, bits, alph, dynamic=True)
+            H, V = rand_pairs(rng, 25, 1, 70, alph)
+            out = []
+            for h, v in zip(H, V):
+                score, segs = O.ref_dynamic_segments(pb, h, v)
+                out.append({"score": score, "segments": [list(x) for x in segs]})
+            cases.append({"problem": problem_dict(pb), "H": [text(h, alph) for h in H], "V": [text(v, alph) for v in V],
+                          "results": out})
+    with open(os.path.join(HERE, "dynamic_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only dynamic", "seed": 20261205, "cases": cases}, f,
+                  separators=(",", ":"))
+    print(f"{sum(len(c['results']) for c in cases)} DynamicGaps pairs written")
 
 
 def write_cpp_binding():
