@@ -1146,10 +1146,17 @@ void launch_dp(const DpArgs &args, int grid, size_t smem, cudaStream_t s)
 
 using DpLauncher = void (*)(const DpArgs &, int, size_t, cudaStream_t);
 
+// Bands of at most kSmallBandWidth diagonals keep their slot arrays in a 64-entry instance: the
+// arrays sit in local memory (indexed per cell), and the 512-entry ones of wide bands (6 KB per
+// thread) overflow L1 and turn into L2 traffic.
+constexpr int kSmallBandWidth = 64;
 template <bool A, bool L, bool M, bool T>
 void launch_banded(const BandArgs &args, int grid, size_t smem, cudaStream_t s)
 {
-    k_dp_banded<A, L, M, T, kMaxBandWidth><<<grid, kBlock, smem, s>>>(args);
+    if (args.upper - args.lower + 1 <= kSmallBandWidth)
+        k_dp_banded<A, L, M, T, kSmallBandWidth><<<grid, kBlock, smem, s>>>(args);
+    else
+        k_dp_banded<A, L, M, T, kMaxBandWidth><<<grid, kBlock, smem, s>>>(args);
 }
 using BandLauncher = void (*)(const BandArgs &, int, size_t, cudaStream_t);
 
