@@ -65,7 +65,16 @@ enum {
                                computed (score = numeric min) */
 };
 
-enum { GBA_GLOBAL = 0, GBA_LOCAL = 1 };
+/* GBA_ALIGN_EXTEND: the AlignExtend_ DP of extendAlignment's banded overloads
+ * (align_extend/align_extend.h:137-206, align_extend/align_extend_base.h): a gap-initialised
+ * first row and column, every cell tracked without a zero floor, traceback from the first maximum
+ * to (0, 0) with the head gaps but no tail, and with GBA_FLAG_XDROP the X-drop terminator of
+ * align_extend/dp_scout_xdrop.h (threshold gba_params.xdrop).  Banded only (band_on), 32-bit cells;
+ * the band is valid when band_lower <= 0 <= band_upper (a free last row and column, not a free
+ * first row or column), otherwise the pair is GBA_PAIR_INVALID with score INT32_MIN as the
+ * reference returns.  gba_extend_alignments runs both sides of extendAlignment on it when its
+ * params carry a band. */
+enum { GBA_GLOBAL = 0, GBA_LOCAL = 1, GBA_ALIGN_EXTEND = 2 };
 /* GBA_GAPS_AUTO picks affine iff gap_open != gap_extend, as the reference's
  * interfaces do (align/global_alignment_unbanded.h:801-810).  GBA_GAPS_DYNAMIC selects the
  * reference's DynamicGaps cells (align/dp_cell_dynamic.h, align/dp_formula_dynamic.h): one score and
@@ -87,7 +96,7 @@ typedef struct {
 } gba_config;
 
 typedef struct {
-    int32_t mode;              /* GBA_GLOBAL / GBA_LOCAL */
+    int32_t mode;              /* GBA_GLOBAL / GBA_LOCAL / GBA_ALIGN_EXTEND */
     int32_t gap_model;         /* GBA_GAPS_* */
     int32_t free_ends;         /* GBA_FREE_* bits (global only; local treats all four as free) */
     int32_t band_on;           /* 1: DPBandConfig<BandOn>(band_lower, band_upper) */
@@ -102,7 +111,7 @@ typedef struct {
     int32_t flags;             /* GBA_FLAG_* kernel selection (0 = automatic) */
     int32_t tile_variant;      /* packed kernel tiling: 0 = automatic (tuning table / autotune /
                                   default); v in 1..GBA_TILE_VARIANTS forces variant v - 1 */
-    int32_t reserved;
+    int32_t xdrop;             /* GBA_ALIGN_EXTEND with GBA_FLAG_XDROP: the X-drop threshold */
 } gba_params;
 
 /* Tiling variants of the packed kernel (rows per register strip x minimum resident blocks per
@@ -136,8 +145,10 @@ enum {
     GBA_FLAG_PACKED_NO_SPLIT = 128,/* packed kernel: no split slots (two pairs per thread only) */
     GBA_FLAG_NO_WARP16 = 256,      /* pairs the packed 16-bit warp kernel would take run on the
                                       32-bit warp kernel instead */
-    GBA_FLAG_WARP16 = 512          /* packed 16-bit warp kernel for eligible pairs even in batches
+    GBA_FLAG_WARP16 = 512,         /* packed 16-bit warp kernel for eligible pairs even in batches
                                       smaller than 4096 pairs */
+    /* Not a kernel selection: GBA_ALIGN_EXTEND's X-drop terminator, threshold gba_params.xdrop. */
+    GBA_FLAG_XDROP = 1024
 };
 
 /* A batch: concatenated residue codes with n+1 offsets for each side. */
@@ -419,8 +430,10 @@ GBA_API int gba_extend_seeds_device(gba_context *ctx, const gba_extend_params *p
                                     const gba_seed_batch *dev_batch, gba_seed *dev_seeds, int32_t *dev_scores);
 
 /* --- Alignment extension ------------------------------------------------------------------
- * extendAlignment(align, hSeq, vSeq, positions, direction, [xDrop,] scoreScheme)
- * (align_extend/align_extend.h:211-372, 494-600), unbanded, over a batch.  For alignment k the
+ * extendAlignment(align, [origScore,] hSeq, vSeq, positions, direction, [lowerDiag, upperDiag,]
+ * [xDrop,] scoreScheme) (align_extend/align_extend.h:211-372, 494-620) over a batch; origScore and
+ * the aligned part's own gaps only enter the returned score, which the caller forms (the Python
+ * and C++ mirrors do).  For alignment k the
  * aligned part spans hSeq[begin_h, end_h) / vSeq[begin_v, end_v) (positions from
  * seeds[k]; the alignment itself is the caller's).  The left side runs the AlignExtend DP on the
  * reversed prefixes when direction has LEFT and both begins are > 0, the right side on the
@@ -437,7 +450,9 @@ typedef struct {
     int32_t gap_open, gap_extend;   /* Gotoh iff open != extend, as the reference picks */
     const int32_t *matrix;     /* optional host alphabet_size^2 table (row = H residue) */
     int32_t alphabet_size;     /* 1..32 with a matrix */
-    int32_t reserved;
+    int32_t band_on;           /* 1: the (lowerDiag, upperDiag) overloads: both sides run the banded
+                                  AlignExtend_ DP (GBA_ALIGN_EXTEND) with this band */
+    int32_t band_lower, band_upper;
 } gba_extend_align_params;
 
 typedef struct {

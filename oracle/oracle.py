@@ -522,18 +522,45 @@ def reverse_partial_trace(segments, len_h, len_v):
     return out[::-1]
 
 
-def oracle_extend_alignment(pb: Problem, h, v, positions, direction, letters="ACGTN") -> ExtendResult:
-    """The reference's _extendAlignmentImpl (align_extend/align_extend.h:211-372) for an ungapped
-    seed, restated on the oracle's DP (pb.mode must be "extend")."""
+def center_score(pb: Problem, row0: str, row1: str, letters="ACGTN") -> int:
+    """The aligned part's score as _extendAlignmentImpl computes it when origScore is omitted
+    (align_extend/align_extend.h:250-270): gap open for a gap column that starts the row pair's
+    gap pattern anew (first column, or either row's gap state changed), gap extend otherwise,
+    the substitution score for the rest."""
+    code = {ch: k for k, ch in enumerate(letters)}
+    sub = (lambda a, b: int(pb.matrix[a, b])) if pb.matrix is not None else \
+        (lambda a, b: pb.match if a == b else pb.mismatch)
+    total = 0
+    for i, (a, b) in enumerate(zip(row0, row1)):
+        g0, g1 = a == "-", b == "-"
+        if g0 or g1:
+            if i == 0 or (row0[i - 1] == "-") != g0 or (row1[i - 1] == "-") != g1:
+                total += pb.gap_open
+            else:
+                total += pb.gap_extend
+        else:
+            total += sub(code[a], code[b])
+    return total
+
+
+def _wrap32(x: int) -> int:
+    return (x + 2 ** 31) % 2 ** 32 - 2 ** 31
+
+
+def oracle_extend_alignment(pb: Problem, h, v, positions, direction, letters="ACGTN", orig_score=None,
+                            center=None) -> ExtendResult:
+    """The reference's _extendAlignmentImpl (align_extend/align_extend.h:211-372), restated on the
+    oracle's DP (pb.mode must be "extend"; pb.band gives the lowerDiag / upperDiag overloads and
+    pb.xdrop the X-drop ones).  center: the aligned part's rows as text with '-' for gaps (None:
+    ungapped); orig_score: the origScore argument (None: computed from the rows)."""
     h = np.ascontiguousarray(h, dtype=np.uint8)
     v = np.ascontiguousarray(v, dtype=np.uint8)
     hb, vb, he, ve = (int(x) for x in positions)
     ext_left = bool(direction & EXTEND_LEFT) and hb > 0 and vb > 0
     ext_right = bool(direction & EXTEND_RIGHT) and he < len(h) and ve < len(v)
-    sub = (lambda a, b: int(pb.matrix[a, b])) if pb.matrix is not None else \
-        (lambda a, b: pb.match if a == b else pb.mismatch)
-    center = sum(sub(int(h[hb + i]), int(v[vb + i])) for i in range(he - hb))
     text = lambda codes: "".join(letters[int(c)] for c in codes)
+    c0, c1 = center if center is not None else (text(h[hb:he]), text(v[vb:ve]))
+    center_sc = center_score(pb, c0, c1, letters) if orig_score is None else int(orig_score)
     left = ([], 0)
     if ext_left:
         r = oracle_batch(pb, [h[:hb][::-1].copy()], [v[:vb][::-1].copy()], traceback=True)
@@ -548,17 +575,18 @@ def oracle_extend_alignment(pb: Problem, h, v, positions, direction, letters="AC
     lv = sum(s[2] for s in left[0] if s[3] in (SEG_DIAGONAL, SEG_VERTICAL))
     rh = sum(s[2] for s in right[0] if s[3] in (SEG_DIAGONAL, SEG_HORIZONTAL))
     rv = sum(s[2] for s in right[0] if s[3] in (SEG_DIAGONAL, SEG_VERTICAL))
-    return ExtendResult(left[1] + center + right[1], l0 + text(h[hb:he]) + r0, l1 + text(v[vb:ve]) + r1,
+    return ExtendResult(_wrap32(left[1] + center_sc + right[1]), l0 + c0 + r0, l1 + c1 + r1,
                         hb - lh, he + rh, vb - lv, ve + rv, left[1], right[1], left[0], right[0])
 
 
-def ref_extend_alignment(pb: Problem, h, v, positions, direction) -> ExtendResult:
-    """The reference's extendAlignment on an ungapped seed (oracle/ref/units/align_extend.cpp)."""
+def ref_extend_alignment(pb: Problem, h, v, positions, direction, orig_score=None, center=None) -> ExtendResult:
+    """The reference's extendAlignment (oracle/ref/units/align_extend.cpp): the overload with
+    origScore when orig_score is given, (lowerDiag, upperDiag) with pb.band, xDrop with
+    pb.xdrop; center: the aligned part's rows with '-' for gaps (None: ungapped)."""
     lib = libref()
-    lib.ref_extend_alignment.argtypes = [C.c_int32] * 6 + [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
-                                                            C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
-                                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
-                                                            C.c_void_p]
+    lib.ref_extend_alignment_ex.argtypes = (
+        [C.c_int32] * 6 + [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p] + [C.c_int32] * 8 +
+        [C.c_char_p, C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p])
     h = np.ascontiguousarray(h, dtype=np.uint8)
     v = np.ascontiguousarray(v, dtype=np.uint8)
     pos = np.array(positions, dtype=np.int64)
@@ -567,11 +595,15 @@ def ref_extend_alignment(pb: Problem, h, v, positions, direction) -> ExtendResul
     row1 = C.create_string_buffer(cap)
     ends = np.zeros(4, dtype=np.int64)
     score = C.c_int32(0)
-    rc = lib.ref_extend_alignment(0 if pb.alphabet == "dna" else 1, 1 if pb.matrix is not None else 0, pb.match,
-                                  pb.mismatch, pb.gap_open, pb.gap_extend, _ptr(h), len(h), _ptr(v), len(v),
-                                  _ptr(pos), int(direction), 0 if pb.xdrop is None else 1,
-                                  0 if pb.xdrop is None else int(pb.xdrop), C.byref(score), row0, row1, cap,
-                                  _ptr(ends))
+    lo, up = pb.band if pb.band is not None else (0, 0)
+    c0 = center[0].encode() if center is not None else None
+    c1 = center[1].encode() if center is not None else None
+    rc = lib.ref_extend_alignment_ex(0 if pb.alphabet == "dna" else 1, 1 if pb.matrix is not None else 0, pb.match,
+                                     pb.mismatch, pb.gap_open, pb.gap_extend, _ptr(h), len(h), _ptr(v), len(v),
+                                     _ptr(pos), int(direction), 0 if pb.band is None else 1, int(lo), int(up),
+                                     0 if pb.xdrop is None else 1, 0 if pb.xdrop is None else int(pb.xdrop),
+                                     0 if orig_score is None else 1, 0 if orig_score is None else int(orig_score),
+                                     c0, c1, C.byref(score), row0, row1, cap, _ptr(ends))
     if rc != 0:
         raise RuntimeError(f"reference returned {rc}")
     return ExtendResult(score.value, row0.value.decode(), row1.value.decode(), int(ends[0]), int(ends[1]),

@@ -408,6 +408,11 @@ typedef struct {
     int upper;
     int *Fslot;          /* F field of the band column's storage, one slot per diagonal */
     int nslots;
+    int trk;             /* every cell tracked: local, or the AlignExtend_ profile */
+    /* X-drop terminator of an AlignExtend_ DP (align_extend/dp_scout_xdrop.h:127-143): every
+     * offer raises colmax; an offer of a column's last cell (and the reference's extra offers
+     * made with IsLastRow) sets term when best - colmax >= xdrop and resets colmax otherwise. */
+    int xd_on, xd, colmax, term;
 } band_t;
 
 #define BAT(bt, arr, col, row) (bt)->arr[(size_t)(col) * (size_t)((bt)->n + 1) + (size_t)(row)]
@@ -428,17 +433,36 @@ static int last_dir(const band_t *bt, int type, int loc)
     if (type == COL_INITIAL) return (bt->fe & ORC_FREE_LEFT) ? DIR_ZERO : DIR_VERTICAL;
     return (loc == LOC_TOP || loc == LOC_MIDDLE) ? DIR_LOWER : DIR_ALL;
 }
-/* Tracking flags of DPMetaColumn_ for first / inner / last cells. */
+/* Tracking flags of DPMetaColumn_ for first / inner / last cells (every cell for local and for
+ * AlignExtend_, align_extend/align_extend_base.h:86-190). */
 static int track_flag(const band_t *bt, int type, int loc, int which /* 0 first 1 inner 2 last */)
 {
-    if (bt->c->local) return 1;
+    if (bt->trk) return 1;
     int lastColFree = (type == COL_FINAL) && (bt->fe & ORC_FREE_RIGHT);
     if (which < 2) return lastColFree;
     if (loc == LOC_FULL || loc == LOC_BOTTOM) return (type == COL_FINAL) || (bt->fe & ORC_FREE_BOTTOM);
     return lastColFree;
 }
 
+/* One offer to the scout; last_row: the XDrop scout's IsLastRow (termination check). */
+static void band_offer(band_t *bt, int s, int e, int f, int col, int row, int last_row)
+{
+    scout(bt->b, s, e, f, col, row);
+    if (!bt->xd_on) return;
+    if (s > bt->colmax) bt->colmax = s;
+    if (last_row) {
+        if (bt->b->s - bt->colmax >= bt->xd) bt->term = 1;
+        else bt->colmax = INT_MIN;
+    }
+}
+
+static void band_cell_x(band_t *bt, int dir, int col, int row, int tracked, int last_row);
 static void band_cell(band_t *bt, int dir, int col, int row, int tracked)
+{
+    band_cell_x(bt, dir, col, row, tracked, 0);
+}
+
+static void band_cell_x(band_t *bt, int dir, int col, int row, int tracked, int last_row)
 {
     int f;
     /* The horizontal neighbour (row, col-1): its S/E are read through the dense arrays. */
@@ -459,7 +483,7 @@ static void band_cell(band_t *bt, int dir, int col, int row, int tracked)
          * (align/dp_algorithm_impl.h:303-311). */
         int slot = bt->upper - col + row;
         if (slot >= 0 && slot < bt->nslots) bt->Fslot[slot] = f;
-        scout(bt->b, sh, eh, f, col, row);
+        band_offer(bt, sh, eh, f, col, row, last_row);
     }
 }
 
@@ -474,24 +498,28 @@ static void band_track(band_t *bt, int col, int type, int loc, int r0, int r1)
         bt->k.dS = BAT(bt, S, col - 1, r0 - 1);
     band_cell(bt, first_dir(bt, type, loc), col, r0, track_flag(bt, type, loc, 0));
     for (i = r0 + 1; i < r1; ++i) band_cell(bt, inner_dir(bt, type), col, i, track_flag(bt, type, loc, 1));
-    band_cell(bt, last_dir(bt, type, loc), col, r1, track_flag(bt, type, loc, 2));
+    band_cell_x(bt, last_dir(bt, type, loc), col, r1, track_flag(bt, type, loc, 2), 1);
 }
 
 /* Re-offers the last computed cell to the scout (the reference's extra _scoutBestScore calls
  * at phase boundaries).  The scout copies the stored cell: its F is what the band column's
  * slot holds (written only by tracked cells of that diagonal), unless the call site refreshes
  * it from cacheVert first (set_f). */
-static void band_retrack_f(band_t *bt, int col, int row, int set_f)
+static void band_retrack_x(band_t *bt, int col, int row, int set_f, int last_row)
 {
     int slot = bt->upper - col + row;
     int inside = slot >= 0 && slot < bt->nslots;
     if (set_f && inside) bt->Fslot[slot] = bt->lastF;
-    scout(bt->b, BAT(bt, S, col, row), BAT(bt, E, col, row), inside ? bt->Fslot[slot] : bt->c->inf, col, row);
+    band_offer(bt, BAT(bt, S, col, row), BAT(bt, E, col, row), inside ? bt->Fslot[slot] : bt->c->inf, col, row,
+               last_row);
 }
-#define band_retrack(bt, col, row) band_retrack_f((bt), (col), (row), 0)
+#define band_retrack_f(bt, col, row, set_f) band_retrack_x((bt), (col), (row), (set_f), 1)
+#define band_retrack(bt, col, row) band_retrack_x((bt), (col), (row), 0, 1)
+#define band_retrack_nocheck(bt, col, row) band_retrack_x((bt), (col), (row), 0, 0)
 
 static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
-                           int lower, int upper, int *S, int *E, uint8_t *T, best_t *b, int *Fslot)
+                           int lower, int upper, int *S, int *E, uint8_t *T, best_t *b, int *Fslot,
+                           int xdrop_on, int xdrop)
 {
     band_t bt;
     int hb, hTop, hMid, hBot, hIt, vb, ve, tmp;
@@ -500,6 +528,11 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
     bt.upper = upper;
     bt.Fslot = Fslot;
     bt.nslots = upper - lower + 1;
+    bt.trk = c->local || c->extend;
+    bt.xd_on = xdrop_on;
+    bt.xd = xdrop;
+    bt.colmax = INT_MIN;
+    bt.term = 0;
     {
         size_t cells = (size_t)(m + 1) * (size_t)(n + 1), q;
         for (q = 0; q < cells; ++q) { S[q] = c->inf; E[q] = c->inf; }
@@ -517,16 +550,17 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
         row = upper >= 0 ? 0 : MIN(n, -upper);
         bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
         band_cell(&bt, DIR_ZERO, col, row, 0);
+        /* _computeHammingDistance offers cells with no IsLastRow: no X-drop check here. */
         if (upper < 0) {
-            if (upper == -n) { if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, col, row); return; }
-            if (c->local) band_retrack(&bt, col, row);
+            if (upper == -n) { if (bt.trk || (fe & ORC_FREE_BOTTOM)) band_retrack_nocheck(&bt, col, row); return; }
+            if (bt.trk) band_retrack_nocheck(&bt, col, row);
         } else if (lower > 0) {
-            if (lower == m) { if (c->local || (fe & ORC_FREE_RIGHT)) band_retrack(&bt, col, row); return; }
-            if (c->local) band_retrack(&bt, col, row);
+            if (lower == m) { if (bt.trk || (fe & ORC_FREE_RIGHT)) band_retrack_nocheck(&bt, col, row); return; }
+            if (bt.trk) band_retrack_nocheck(&bt, col, row);
         } else {
-            if (c->local) band_retrack(&bt, col, row);
+            if (bt.trk) band_retrack_nocheck(&bt, col, row);
         }
-        tr = c->local;
+        tr = bt.trk;
         while (ih != ihEnd && iv != ivEnd) {
             int prev = BAT(&bt, S, col, row);
             ++col; ++row;
@@ -537,7 +571,7 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
                 BAT(&bt, S, col, row) = s;
                 if (T) BAT(&bt, T, col, row) = (uint8_t)t;
             }
-            if (tr) scout(b, BAT(&bt, S, col, row), c->inf, c->inf, col, row);
+            if (tr) band_offer(&bt, BAT(&bt, S, col, row), c->inf, c->inf, col, row, 0);
             ++ih; ++iv;
         }
         /* The reference computes one more diagonal cell here.  When the diagonal leaves the
@@ -554,10 +588,10 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
             BAT(&bt, S, col, row) = s;
             if (T) BAT(&bt, T, col, row) = (uint8_t)t;
             if (ih == ihEnd) {
-                if (iv == ivEnd) scout(b, s, c->inf, c->inf, col, row);   /* final column, last cell: always */
-                if (c->local || (fe & ORC_FREE_BOTTOM)) scout(b, s, c->inf, c->inf, col, row);
+                if (iv == ivEnd) band_offer(&bt, s, c->inf, c->inf, col, row, 0);   /* final column, last cell: always */
+                if (bt.trk || (fe & ORC_FREE_BOTTOM)) band_offer(&bt, s, c->inf, c->inf, col, row, 0);
             } else {
-                if (c->local || (fe & ORC_FREE_RIGHT)) scout(b, s, c->inf, c->inf, col, row);
+                if (bt.trk || (fe & ORC_FREE_RIGHT)) band_offer(&bt, s, c->inf, c->inf, col, row, 0);
             }
         }
         return;
@@ -579,15 +613,15 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
     if (hb == m - 1) {
         int col = MAX(0, MIN(m, lower));
         bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
-        band_cell(&bt, DIR_ZERO, col, 0, c->local);
-        if (c->local || (fe & ORC_FREE_RIGHT)) band_retrack(&bt, col, 0);
+        band_cell(&bt, DIR_ZERO, col, 0, bt.trk);
+        if (bt.trk || (fe & ORC_FREE_RIGHT)) band_retrack_nocheck(&bt, col, 0);   /* (True, False) */
         return;
     }
     if (hBot == 0) {
         int row = MIN(n, -upper);
         bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
-        band_cell(&bt, DIR_ZERO, 0, row, c->local);
-        if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, 0, row);
+        band_cell(&bt, DIR_ZERO, 0, row, bt.trk);
+        if (bt.trk || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, 0, row);
         return;
     }
 
@@ -596,42 +630,51 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
         band_track(&bt, 0, COL_INITIAL, lower > -n ? LOC_MIDDLE : LOC_BOTTOM, vb, ve);
     } else if (lower >= 0) {
         bt.k.dS = c->inf; bt.k.vS = c->inf; bt.k.vF = c->inf;
-        band_cell(&bt, DIR_ZERO, hb, 0, c->local);
-        if (c->local) band_retrack(&bt, hb, 0);
+        band_cell(&bt, DIR_ZERO, hb, 0, bt.trk);
+        if (bt.trk) band_retrack_nocheck(&bt, hb, 0);
     } else {
         band_track(&bt, 0, COL_INITIAL, lower <= -n ? LOC_FULL : LOC_TOP, vb, ve);
     }
+    /* _computeAlignmentHelperCheckTerminate after the initial column and after each column of
+     * the three band phases (align/dp_algorithm_impl.h:746-836). */
+    if (bt.term) return;
 
     hIt = hb;
     for (; hIt != hTop; ++hIt) {
         ++ve;
         band_track(&bt, hIt + 1, COL_INNER, LOC_TOP, vb, ve);
+        if (bt.term) return;
     }
     if (upper > n + lower) {
-        if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, hIt, ve);
-        for (; hIt != hMid; ++hIt) band_track(&bt, hIt + 1, COL_INNER, LOC_FULL, vb, ve);
+        if (bt.trk || (fe & ORC_FREE_BOTTOM)) band_retrack(&bt, hIt, ve);
+        for (; hIt != hMid; ++hIt) {
+            band_track(&bt, hIt + 1, COL_INNER, LOC_FULL, vb, ve);
+            if (bt.term) return;
+        }
     } else {
         for (; hIt != hMid; ++hIt) {
             ++vb; ++ve;
             band_track(&bt, hIt + 1, COL_INNER, LOC_MIDDLE, vb, ve);
+            if (bt.term) return;
         }
-        if ((c->local || (fe & ORC_FREE_BOTTOM)) && lower + n < m) band_retrack(&bt, hIt, ve);
+        if ((bt.trk || (fe & ORC_FREE_BOTTOM)) && lower + n < m) band_retrack(&bt, hIt, ve);
     }
     for (; hIt != hBot; ++hIt) {
         ++vb;
         band_track(&bt, hIt + 1, COL_INNER, LOC_BOTTOM, vb, ve);
+        if (bt.term) return;
     }
 
     /* Last band column. */
     if (hIt < m - 1) {
         /* The band ends before the final column: one cell (first cell of a bottom column). */
         bt.k.dS = BAT(&bt, S, hIt, vb); bt.k.vS = c->inf; bt.k.vF = c->inf;
-        band_cell(&bt, DIR_UPPER, hIt + 1, vb + 1, c->local);
-        if (c->local || (fe & ORC_FREE_BOTTOM)) band_retrack_f(&bt, hIt + 1, vb + 1, 1);
+        band_cell(&bt, DIR_UPPER, hIt + 1, vb + 1, bt.trk);
+        if (bt.trk || (fe & ORC_FREE_BOTTOM)) band_retrack_f(&bt, hIt + 1, vb + 1, 1);
     } else if (hIt == m - 1) {
         if (upper == m - n) {
             bt.k.dS = BAT(&bt, S, hIt, vb); bt.k.vS = c->inf; bt.k.vF = c->inf;
-            band_cell(&bt, DIR_UPPER, m, vb + 1, c->local || (fe & ORC_FREE_RIGHT));
+            band_cell(&bt, DIR_UPPER, m, vb + 1, bt.trk || (fe & ORC_FREE_RIGHT));
             band_retrack_f(&bt, m, vb + 1, 1);
         } else if (upper >= m) {
             if (lower + n > m) {
@@ -665,12 +708,12 @@ static void dp_banded_impl(const ctx_t *c, int fe, const uint8_t *h, int m, cons
 }
 
 static void dp_banded(const ctx_t *c, int fe, const uint8_t *h, int m, const uint8_t *v, int n,
-                      int lower, int upper, int *S, int *E, uint8_t *T, best_t *b)
+                      int lower, int upper, int *S, int *E, uint8_t *T, best_t *b, int xdrop_on, int xdrop)
 {
     int slots = upper - lower + 1, q;
     int *Fslot = (int *)malloc(sizeof(int) * (size_t)(slots > 0 ? slots : 1));
     for (q = 0; q < slots; ++q) Fslot[q] = c->inf;
-    dp_banded_impl(c, fe, h, m, v, n, lower, upper, S, E, T, b, Fslot);
+    dp_banded_impl(c, fe, h, m, v, n, lower, upper, S, E, T, b, Fslot, xdrop_on, xdrop);
     free(Fslot);
 }
 
@@ -767,8 +810,10 @@ int orc_align_pair(const orc_params *p,
     c.mismatch = p->mismatch;
     c.mat = p->matrix;
     c.asz = p->alphabet_size;
-    fe = c.local ? (ORC_FREE_TOP | ORC_FREE_LEFT | ORC_FREE_RIGHT | ORC_FREE_BOTTOM) : (c.extend ? 0 : p->free_ends);
-    if (c.extend && p->band_on) return -1;   /* the banded extension is not restated */
+    /* AlignExtend_ has free last row and column (align_extend/align_extend_base.h:75-81): they
+     * only decide band validity and the extra offers, since it tracks every cell anyway. */
+    fe = c.local ? (ORC_FREE_TOP | ORC_FREE_LEFT | ORC_FREE_RIGHT | ORC_FREE_BOTTOM)
+                 : (c.extend ? (ORC_FREE_RIGHT | ORC_FREE_BOTTOM) : p->free_ends);
     if (c.dynamic && (p->band_on || c.extend)) return -1;   /* DynamicGaps: unbanded global / local */
 
     if (m <= 0 || n <= 0 || !band_valid(p, m, n, fe)) {
@@ -786,7 +831,8 @@ int orc_align_pair(const orc_params *p,
     if (p->band_on) {
         int *S = (int *)malloc(sizeof(int) * (size_t)(m + 1) * (size_t)(n + 1) * 2);
         if (!T) T = NULL;
-        dp_banded(&c, fe, h, m, v, n, p->band_lower, p->band_upper, S, S + (size_t)(m + 1) * (size_t)(n + 1), T, &b);
+        dp_banded(&c, fe, h, m, v, n, p->band_lower, p->band_upper, S, S + (size_t)(m + 1) * (size_t)(n + 1), T, &b,
+                  c.extend && p->xdrop_on, p->xdrop);
         free(S);
     } else {
         dp_unbanded(&c, fe, h, m, v, n, colS, colE, T, &b, c.extend && p->xdrop_on, p->xdrop);

@@ -28,7 +28,8 @@ enum {
 
 /* ORC_EXTEND: the DP of extendAlignment (align_extend/align_extend.h:115-206): AlignExtend_
  * profile (align_extend/align_extend_base.h), i.e. a gap-initialised first row and column, every
- * cell tracked without a zero floor, traceback to (0, 0) with no tail; unbanded. */
+ * cell tracked without a zero floor, traceback to (0, 0) with no tail; unbanded, or banded
+ * (the lowerDiag / upperDiag overloads) with the free last row and column of the profile. */
 enum { ORC_GLOBAL = 0, ORC_LOCAL = 1, ORC_EXTEND = 2 };
 enum { ORC_LINEAR = 0, ORC_AFFINE = 1, ORC_DYNAMIC = 2 };
 

@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", 
 GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY, GBA_EPARSE = \
     range(9)
 GBA_PAIR_OK, GBA_PAIR_INVALID, GBA_PAIR_PROMOTED, GBA_PAIR_FAILED, GBA_PAIR_SKIPPED = 0, 1, 2, 3, 4
-GBA_GLOBAL, GBA_LOCAL = 0, 1
+GBA_GLOBAL, GBA_LOCAL, GBA_ALIGN_EXTEND = 0, 1, 2
 GBA_GAPS_AUTO, GBA_GAPS_LINEAR, GBA_GAPS_AFFINE, GBA_GAPS_DYNAMIC = 0, 1, 2, 3
 GBA_FREE_TOP, GBA_FREE_LEFT, GBA_FREE_RIGHT, GBA_FREE_BOTTOM = 1, 2, 4, 8
 GBA_OUT_SCORE, GBA_OUT_END, GBA_OUT_SEGMENTS, GBA_OUT_CIGAR = 1, 2, 4, 8
@@ -33,6 +33,7 @@ GBA_NOALLOC_SCRATCH_BYTES = 64 << 20
 GBA_FLAG_GENERAL_KERNEL, GBA_FLAG_STRIP16, GBA_FLAG_PLAIN_BUCKETS, GBA_FLAG_NO_GRAPH, GBA_FLAG_AUTOTUNE = 1, 2, 4, 8, 16
 GBA_FLAG_PACKED = 32
 GBA_FLAG_PACKED_SPLIT, GBA_FLAG_PACKED_NO_SPLIT, GBA_FLAG_NO_WARP16, GBA_FLAG_WARP16 = 64, 128, 256, 512
+GBA_FLAG_XDROP = 1024
 GBA_KERNEL_STRIP, GBA_KERNEL_PACKED, GBA_KERNEL_WARP, GBA_KERNEL_BANDED, GBA_KERNEL_WARP16 = 1, 2, 4, 8, 16
 GBA_KERNEL_DYNAMIC = 32
 GBA_MATCH_EXTEND, GBA_UNGAPPED_XDROP, GBA_GAPPED_XDROP = 0, 1, 2
@@ -61,7 +62,7 @@ class GbaParams(C.Structure):
                 ("match", C.c_int32), ("mismatch", C.c_int32), ("gap_open", C.c_int32),
                 ("gap_extend", C.c_int32), ("matrix", C.c_void_p), ("alphabet_size", C.c_int32),
                 ("score_bits", C.c_int32), ("outputs", C.c_int32), ("flags", C.c_int32),
-                ("tile_variant", C.c_int32), ("reserved", C.c_int32)]
+                ("tile_variant", C.c_int32), ("xdrop", C.c_int32)]
 
 
 class GbaBatch(C.Structure):
@@ -131,7 +132,8 @@ class GbaSeedBatch(C.Structure):
 class GbaExtendAlignParams(C.Structure):
     _fields_ = [("direction", C.c_int32), ("xdrop_on", C.c_int32), ("xdrop", C.c_int32), ("match", C.c_int32),
                 ("mismatch", C.c_int32), ("gap_open", C.c_int32), ("gap_extend", C.c_int32),
-                ("matrix", C.c_void_p), ("alphabet_size", C.c_int32), ("reserved", C.c_int32)]
+                ("matrix", C.c_void_p), ("alphabet_size", C.c_int32), ("band_on", C.c_int32),
+                ("band_lower", C.c_int32), ("band_upper", C.c_int32)]
 
 
 class GbaExtendAlignResult(C.Structure):

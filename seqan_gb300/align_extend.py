@@ -2,11 +2,12 @@
 
 :func:`extend_alignments` extends a batch of aligned parts -- hSeq[beginH, endH) over
 vSeq[beginV, endV), given as int64 [n, 4] or [n, 6] position rows -- to the left and right with
-the AlignExtend DP (optionally X-drop terminated) in one GPU call (``gba_extend_alignments``)
-and returns, per alignment, the two sides' scores and TraceSegment_ lists.
-:func:`extendAlignment` is ``extendAlignment(align, hSeq, vSeq, positions, direction, [xDrop,]
-score)`` for an ungapped aligned part: it returns the reference's score (left + aligned part +
-right) and the extended rows with their begin and end positions.
+the AlignExtend DP (optionally X-drop terminated, optionally banded) in one GPU call
+(``gba_extend_alignments``) and returns, per alignment, the two sides' scores and TraceSegment_
+lists.  :func:`extendAlignment` is ``extendAlignment(align, [origScore,] hSeq, vSeq, positions,
+direction, [lowerDiag, upperDiag,] [xDrop,] score)``: it returns the reference's score (left +
+aligned part + right) and the extended rows with their begin and end positions; the aligned
+part may carry gaps (``center`` rows).
 """
 from __future__ import annotations
 
@@ -39,8 +40,10 @@ def _concat(seqs, alphabet):
 
 
 def extend_alignments(databases, queries, positions, direction, score, xdrop=None, seed_h=None, seed_v=None,
-                      alphabet="dna5", context=None):
-    """One GPU call for a batch; positions rows are (beginH, beginV, endH, endV[, ...])."""
+                      alphabet="dna5", context=None, band=None):
+    """One GPU call for a batch; positions rows are (beginH, beginV, endH, endV[, ...]); band =
+    (lowerDiag, upperDiag) for the banded overloads.  A side whose band misses its matrix gets
+    the reference's invalid value (INT32_MIN) and no segments."""
     pos = np.asarray(positions, dtype=np.int64).reshape(len(positions), -1)
     seeds = np.zeros((len(pos), 6), dtype=np.int64)
     seeds[:, :4] = pos[:, :4]
@@ -52,6 +55,9 @@ def extend_alignments(databases, queries, positions, direction, score, xdrop=Non
     p.xdrop = 0 if xdrop is None else int(xdrop)
     p.match, p.mismatch = score.match, score.mismatch
     p.gap_open, p.gap_extend = score.gap_open, score.gap_extend
+    if band is not None:
+        p.band_on = 1
+        p.band_lower, p.band_upper = int(band[0]), int(band[1])
     keep = None
     if score.matrix is not None:
         keep = np.ascontiguousarray(score.matrix, dtype=np.int32)
@@ -112,31 +118,61 @@ class ExtendedAlignment:
     v_end: int
 
 
-def assemble(ext: SideExtension, h, v, positions, score, alphabet="dna5") -> ExtendedAlignment:
-    """Joins the sides around an ungapped aligned part as _extendAlignmentImpl does
-    (align_extend/align_extend.h:264-369): rows, begin/end positions and the returned score."""
+def _center_score(row0, row1, score, alphabet):
+    """The aligned part's score when origScore is omitted (align_extend/align_extend.h:250-270):
+    a gap column opens a gap when it is the first column or either row's gap state changes there,
+    and extends one otherwise; other columns score their residues."""
+    total = 0
+    for i, (a, b) in enumerate(zip(row0, row1)):
+        g0, g1 = a == "-", b == "-"
+        if g0 or g1:
+            fresh = i == 0 or (row0[i - 1] == "-") != g0 or (row1[i - 1] == "-") != g1
+            total += score.gap_open if fresh else score.gap_extend
+        else:
+            x, y = int(encode(a, alphabet)[0]), int(encode(b, alphabet)[0])
+            total += int(score.matrix[x, y]) if score.matrix is not None else \
+                (score.match if x == y else score.mismatch)
+    return total
+
+
+def _int32(x):
+    return (x + 2 ** 31) % 2 ** 32 - 2 ** 31
+
+
+def assemble(ext: SideExtension, h, v, positions, score, alphabet="dna5", orig_score=None,
+             center=None) -> ExtendedAlignment:
+    """Joins the sides around the aligned part as _extendAlignmentImpl does
+    (align_extend/align_extend.h:264-369): rows, begin/end positions and the returned score
+    (left + origScore, or the part's own score, + right, in the reference's int arithmetic).
+    center: the part's rows with '-' for gaps (None: ungapped)."""
     h = encode(h, alphabet)
     v = encode(v, alphabet)
     hb, vb, he, ve = (int(x) for x in positions[:4])
-    sub = (lambda a, b: int(score.matrix[a, b])) if score.matrix is not None else \
-        (lambda a, b: score.match if a == b else score.mismatch)
-    center = sum(sub(int(h[hb + i]), int(v[vb + i])) for i in range(he - hb))
     text = lambda c: decode(c, alphabet)
+    c0, c1 = center if center is not None else (text(h[hb:he]), text(v[vb:ve]))
+    mid = _center_score(c0, c1, score, alphabet) if orig_score is None else int(orig_score)
     l0, l1, llh, llv = _render(ext.left_segments, text(h[:hb]), text(v[:vb]))
     r0, r1, rlh, rlv = _render(ext.right_segments, text(h[he:]), text(v[ve:]))
-    return ExtendedAlignment(ext.left_score + center + ext.right_score, l0 + text(h[hb:he]) + r0,
-                             l1 + text(v[vb:ve]) + r1, hb - llh, he + rlh, vb - llv, ve + rlv)
+    return ExtendedAlignment(_int32(ext.left_score + mid + ext.right_score), l0 + c0 + r0, l1 + c1 + r1,
+                             hb - llh, he + rlh, vb - llv, ve + rlv)
 
 
-def extendAlignment(h, v, positions, direction, *args, alphabet="dna5", context=None):
-    """extendAlignment(align, hSeq, vSeq, positions, direction, [xDrop,] score) for an ungapped
-    aligned part hSeq[positions[0], positions[2]) / vSeq[positions[1], positions[3])."""
+def extendAlignment(h, v, positions, direction, *args, orig_score=None, center=None, alphabet="dna5",
+                    context=None):
+    """extendAlignment(align, [origScore,] hSeq, vSeq, positions, direction, [lowerDiag,
+    upperDiag,] [xDrop,] score) on the aligned part hSeq[positions[0], positions[2]) /
+    vSeq[positions[1], positions[3]); origScore as orig_score=, the part's gapped rows as
+    center=(row0, row1)."""
     if len(args) == 1:
-        xdrop, score = None, args[0]
+        band, xdrop, score = None, None, args[0]
     elif len(args) == 2:
-        xdrop, score = args
+        band, (xdrop, score) = None, args
+    elif len(args) == 3:
+        band, xdrop, score = (args[0], args[1]), None, args[2]
+    elif len(args) == 4:
+        band, xdrop, score = (args[0], args[1]), args[2], args[3]
     else:
-        raise TypeError("extendAlignment(h, v, positions, direction, [xDrop,] score)")
+        raise TypeError("extendAlignment(h, v, positions, direction, [lowerDiag, upperDiag,] [xDrop,] score)")
     ext = extend_alignments([h], [v], [list(positions)[:4]], direction, score, xdrop, alphabet=alphabet,
-                            context=context)[0]
-    return assemble(ext, h, v, positions, score, alphabet)
+                            context=context, band=band)[0]
+    return assemble(ext, h, v, positions, score, alphabet, orig_score=orig_score, center=center)

@@ -10,6 +10,15 @@
 // stored one slot per diagonal, so a slot keeps the F of the last tracked cell on its
 // diagonal unless the call site refreshes it).
 //
+// XT: the AlignExtend_ profile of extendAlignment's banded overloads
+// (align_extend/align_extend.h:137-206, align_extend/align_extend_base.h): global directions with a
+// free last row and column, every cell tracked, no zero floor, and with xdrop_on the X-drop
+// terminator (align_extend/dp_scout_xdrop.h:127-143): every offer raises the column maximum, an
+// offer with IsLastRow (a track's last cell, and the reference's extra offers that pass it) ends
+// the DP when best - column maximum >= xdrop and resets the maximum otherwise, and the DP stops
+// at the reference's column checks (after the initial column and after each column of the three
+// band phases, align/dp_algorithm_impl.h:746-836).
+//
 // Band state: per thread, slot k = upper - col + row (one per diagonal) of S, E and the stored
 // F, in per-thread arrays (local memory).  Trace: one byte per band slot per column (the
 // reference's TraceBitMap_ bits), columns band_trace_stride(W) = W rounded up to 16 bytes
@@ -40,6 +49,7 @@ struct BandArgs {
     int32_t free_ends;
     int32_t alphabet;
     int32_t lower, upper;
+    int32_t xdrop_on, xdrop;       // XT instances only
 };
 
 constexpr int kBandFastW = 40;   // widest band of the middle-phase fast path
@@ -60,8 +70,9 @@ enum { BCOL_INITIAL = 0, BCOL_INNER = 1, BCOL_FINAL = 2 };
 enum { BLOC_FULL = 0, BLOC_TOP = 1, BLOC_MIDDLE = 2, BLOC_BOTTOM = 3 };
 enum { BDIR_ZERO = 0, BDIR_ALL, BDIR_HORIZONTAL, BDIR_VERTICAL, BDIR_UPPER, BDIR_LOWER };
 
-template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX>
+template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX, bool XT = false>
 struct BandedPair {
+    static constexpr bool TRK = LOCAL || XT;   // every cell tracked
     const BandArgs &a;
     const int *smat;
     const uint8_t *H, *V;
@@ -74,6 +85,9 @@ struct BandedPair {
     int dS, vS, vF, lastF;
     // scout (strict '>' in the reference's visiting order)
     int bs, be, bf, bcol, brow;
+    // X-drop terminator (XT)
+    int colmax;
+    bool term;
 
     __device__ BandedPair(const BandArgs &args, const int *sm) : a(args), smat(sm) {}
 
@@ -87,12 +101,24 @@ struct BandedPair {
     {
         if (s > bs) { bs = s; be = e; bf = f; bcol = col; brow = row; }
     }
+    // An offer of the X-drop scout; last_row: the reference's IsLastRow (termination check).
+    __device__ __forceinline__ void offer(int s, int e, int f, int col, int row, bool last_row)
+    {
+        scout(s, e, f, col, row);
+        if (XT && a.xdrop_on) {
+            colmax = max(colmax, s);
+            if (last_row) {
+                if (bs - colmax >= a.xdrop) term = true;
+                else colmax = INT_MIN;
+            }
+        }
+    }
     __device__ __forceinline__ int slot(int col, int row) const { return upper - col + row; }
     __device__ __forceinline__ bool in_slots(int k) const { return k >= 0 && k < W; }
 
     // One cell; the horizontal neighbour (row, col - 1) is slot k + 1 of the previous column,
     // which still holds it because slots are overwritten in increasing k within a column.
-    __device__ void cell(int dir, int col, int row, bool tracked)
+    __device__ void cell(int dir, int col, int row, bool tracked, bool last_row = false)
     {
         const int k = slot(col, row);
         const int hS = in_slots(k + 1) ? S[k + 1] : INF;
@@ -199,22 +225,23 @@ struct BandedPair {
         }
         if (tracked) {
             if (inside) Fs[k] = f;
-            scout(s, e, f, col, row);
+            offer(s, e, f, col, row, last_row);
         }
     }
 
     // The reference's extra best-cell offers at phase boundaries (see the file comment).
-    __device__ void retrack(int col, int row, bool set_f)
+    // last_row: the reference's call passes IsLastRow (an X-drop check in XT mode).
+    __device__ void retrack(int col, int row, bool set_f, bool last_row = true)
     {
         const int k = slot(col, row);
         if (!in_slots(k)) {
             // A degenerate single-cell band whose one cell lies outside the band: the cell
             // just computed (direction Zero) is offered with its values.
-            scout(0, INF, INF, col, row);
+            offer(0, INF, INF, col, row, last_row);
             return;
         }
         if (set_f) Fs[k] = lastF;
-        scout(S[k], E[k], Fs[k], col, row);
+        offer(S[k], E[k], Fs[k], col, row, last_row);
     }
 
     // Middle-phase columns hIt + 1 .. hMid with every track covering slots 0 .. W - 1 (first
@@ -398,7 +425,7 @@ struct BandedPair {
     }
     __device__ bool track_flag(int type, int loc, int which) const
     {
-        if (LOCAL) return true;
+        if (TRK) return true;
         const bool lastColFree = type == BCOL_FINAL && fRight;
         if (which < 2) return lastColFree;
         if (loc == BLOC_FULL || loc == BLOC_BOTTOM) return type == BCOL_FINAL || fBottom;
@@ -414,7 +441,7 @@ struct BandedPair {
         }
         cell(first_dir(type, loc), col, r0, track_flag(type, loc, 0));
         for (int i = r0 + 1; i < r1; ++i) cell(inner_dir(type), col, i, track_flag(type, loc, 1));
-        cell(last_dir(type, loc), col, r1, track_flag(type, loc, 2));
+        cell(last_dir(type, loc), col, r1, track_flag(type, loc, 2), true);
     }
 
     __device__ void single(int dir, int col, int row, int diag_from_col, int diag_from_row, bool tracked)
@@ -432,6 +459,8 @@ struct BandedPair {
         for (int k = 0; k < W; ++k) { S[k] = INF; E[k] = INF; Fs[k] = INF; }
         bs = INF; be = INF; bf = INF; bcol = 0; brow = 0;
         lastF = INF;
+        colmax = INT_MIN;
+        term = false;
         const int lo = lower, up = upper;
         if (up == lo) {
             // Band of one diagonal (align/dp_algorithm_impl.h:970-1110).
@@ -439,15 +468,16 @@ struct BandedPair {
             int iv = max(0, min(n - 1, -lo)), ivEnd = min(n - 1, lo + m);
             int col = up >= 0 ? min(m, up) : 0;
             int row = up >= 0 ? 0 : min(n, -up);
+            // _computeHammingDistance offers its cells without IsLastRow (no X-drop check).
             single(BDIR_ZERO, col, row, -1, 0, false);
             if (up < 0) {
-                if (up == -n) { if (LOCAL || fBottom) retrack(col, row, false); return; }
-                if (LOCAL) retrack(col, row, false);
+                if (up == -n) { if (TRK || fBottom) retrack(col, row, false, false); return; }
+                if (TRK) retrack(col, row, false, false);
             } else if (lo > 0) {
-                if (lo == m) { if (LOCAL || fRight) retrack(col, row, false); return; }
-                if (LOCAL) retrack(col, row, false);
+                if (lo == m) { if (TRK || fRight) retrack(col, row, false, false); return; }
+                if (TRK) retrack(col, row, false, false);
             } else {
-                if (LOCAL) retrack(col, row, false);
+                if (TRK) retrack(col, row, false, false);
             }
             int prev = 0;
             while (ih != ihEnd && iv != ivEnd) {
@@ -456,7 +486,7 @@ struct BandedPair {
                 int tv = TV_DIAG;
                 if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
                 if (TRACE) T[band_trace_pos(Wt, col, 0)] = uint8_t(tv);
-                if (LOCAL) scout(s, INF, INF, col, row);
+                if (TRK) offer(s, INF, INF, col, row, false);
                 prev = s;
                 ++ih; ++iv;
             }
@@ -467,10 +497,10 @@ struct BandedPair {
             if (LOCAL && s <= 0) { s = 0; tv = TV_NONE; }
             if (TRACE) T[band_trace_pos(Wt, col, 0)] = uint8_t(tv);
             if (ih == ihEnd) {
-                if (iv == ivEnd) scout(s, INF, INF, col, row);
-                if (LOCAL || fBottom) scout(s, INF, INF, col, row);
+                if (iv == ivEnd) offer(s, INF, INF, col, row, false);
+                if (TRK || fBottom) offer(s, INF, INF, col, row, false);
             } else {
-                if (LOCAL || fRight) scout(s, INF, INF, col, row);
+                if (TRK || fRight) offer(s, INF, INF, col, row, false);
             }
             return;
         }
@@ -485,52 +515,60 @@ struct BandedPair {
 
         if (hb == m - 1) {
             const int col = max(0, min(m, lo));
-            single(BDIR_ZERO, col, 0, -1, 0, LOCAL);
-            if (LOCAL || fRight) retrack(col, 0, false);
+            single(BDIR_ZERO, col, 0, -1, 0, TRK);
+            if (TRK || fRight) retrack(col, 0, false, false);   // (IsLastColumn, not IsLastRow)
             return;
         }
         if (hBot == 0) {
             const int row = min(n, -up);
-            single(BDIR_ZERO, 0, row, -1, 0, LOCAL);
-            if (LOCAL || fBottom) retrack(0, row, false);
+            single(BDIR_ZERO, 0, row, -1, 0, TRK);
+            if (TRK || fBottom) retrack(0, row, false);
             return;
         }
         if (up < 0) {
             ++vb;
             track(0, BCOL_INITIAL, lo > -n ? BLOC_MIDDLE : BLOC_BOTTOM, vb, ve);
         } else if (lo >= 0) {
-            single(BDIR_ZERO, hb, 0, -1, 0, LOCAL);
-            if (LOCAL) retrack(hb, 0, false);
+            single(BDIR_ZERO, hb, 0, -1, 0, TRK);
+            if (TRK) retrack(hb, 0, false, false);
         } else {
             track(0, BCOL_INITIAL, lo <= -n ? BLOC_FULL : BLOC_TOP, vb, ve);
         }
+        if (XT && term) return;
         int hIt = hb;
         for (; hIt != hTop; ++hIt) {
             ++ve;
             track(hIt + 1, BCOL_INNER, BLOC_TOP, vb, ve);
+            if (XT && term) return;
         }
         if (up > n + lo) {
-            if (LOCAL || fBottom) retrack(hIt, ve, false);
-            for (; hIt != hMid; ++hIt) track(hIt + 1, BCOL_INNER, BLOC_FULL, vb, ve);
+            if (TRK || fBottom) retrack(hIt, ve, false);
+            for (; hIt != hMid; ++hIt) {
+                track(hIt + 1, BCOL_INNER, BLOC_FULL, vb, ve);
+                if (XT && term) return;
+            }
         } else {
-            if (W >= 2 && W <= kBandFastW && hIt != hMid && ve - vb + 1 == W && upper - (hIt + 1) + (vb + 1) == 0)
+            if (!XT && W >= 2 && W <= kBandFastW && hIt != hMid && ve - vb + 1 == W &&
+                upper - (hIt + 1) + (vb + 1) == 0)
                 middle_fast(hIt, hMid, vb, ve);
             for (; hIt != hMid; ++hIt) {
                 ++vb; ++ve;
                 track(hIt + 1, BCOL_INNER, BLOC_MIDDLE, vb, ve);
+                if (XT && term) return;
             }
-            if ((LOCAL || fBottom) && lo + n < m) retrack(hIt, ve, false);
+            if ((TRK || fBottom) && lo + n < m) retrack(hIt, ve, false);
         }
         for (; hIt != hBot; ++hIt) {
             ++vb;
             track(hIt + 1, BCOL_INNER, BLOC_BOTTOM, vb, ve);
+            if (XT && term) return;
         }
         if (hIt < m - 1) {
-            single(BDIR_UPPER, hIt + 1, vb + 1, hIt, vb, LOCAL);
-            if (LOCAL || fBottom) retrack(hIt + 1, vb + 1, true);
+            single(BDIR_UPPER, hIt + 1, vb + 1, hIt, vb, TRK);
+            if (TRK || fBottom) retrack(hIt + 1, vb + 1, true);
         } else if (hIt == m - 1) {
             if (up == m - n) {
-                single(BDIR_UPPER, m, vb + 1, hIt, vb, LOCAL || fRight);
+                single(BDIR_UPPER, m, vb + 1, hIt, vb, TRK || fRight);
                 retrack(m, vb + 1, true);
             } else if (up >= m) {
                 if (lo + n > m) {
@@ -562,7 +600,7 @@ struct BandedPair {
     }
 };
 
-template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX>
+template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX, bool XT = false>
 __global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
 {
     extern __shared__ int smat[];
@@ -578,7 +616,7 @@ __global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
     const int p = a.order[slot];
     if (p < 0) return;
     const PairDesc d = a.pairs[p];
-    BandedPair<AFFINE, LOCAL, MATRIX, TRACE, WMAX> bp(a, smat);
+    BandedPair<AFFINE, LOCAL, MATRIX, TRACE, WMAX, XT> bp(a, smat);
     bp.m = d.m;
     bp.n = d.n;
     bp.W = a.upper - a.lower + 1;
@@ -589,7 +627,8 @@ __global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
     bp.H = a.seq_h + d.h_off;
     bp.V = a.seq_v + d.v_off;
     bp.T = TRACE ? a.trace + d.trace_off : nullptr;
-    const int fe = LOCAL ? (FREE_TOP | FREE_LEFT | FREE_RIGHT | FREE_BOTTOM) : a.free_ends;
+    const int fe = LOCAL ? (FREE_TOP | FREE_LEFT | FREE_RIGHT | FREE_BOTTOM)
+                         : XT ? (FREE_RIGHT | FREE_BOTTOM) : a.free_ends;
     bp.fTop = fe & FREE_TOP;
     bp.fLeft = fe & FREE_LEFT;
     bp.fRight = fe & FREE_RIGHT;

@@ -4,6 +4,7 @@
 // device traceback makes exactly the reference's decisions.
 #pragma once
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -81,6 +82,7 @@ struct TraceArgs {
     int32_t warp_rows;     // warp layout: rows per lane strip (0: not the warp layout)
     int32_t warp2;         // 1: the packed 16-bit warp layout with 4-bit cells (dp_warp2_kernels.cuh)
     int32_t dynamic;       // 1: DynamicGaps cells; best_e holds the best cell's gap flags
+    int32_t extend;        // 1: AlignExtend_ (TraceHead_ but no TraceTail_, align_extend_base.h:67-73)
 };
 
 __host__ __device__ inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }

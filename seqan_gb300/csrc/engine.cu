@@ -86,6 +86,7 @@ struct gba_plan {
     bool affine = false;
     bool dynamic = false;           // DynamicGaps cells (dp_dynamic_kernels.cuh)
     bool local = false;
+    bool extend = false;            // GBA_ALIGN_EXTEND (banded kernel in its AlignExtend_ mode)
     bool matrix = false;
     int32_t free_ends = 0;
     gba_params params{};
@@ -332,7 +333,19 @@ bool int16_exact(const gba_params &p, int max_pos, int64_t m, int64_t n, bool lo
 int validate(gba_context *ctx, const gba_params *p, const gba_batch *b)
 {
     if (!p || !b) return fail(ctx, GBA_EINVAL, "null params or batch");
-    if (p->mode != GBA_GLOBAL && p->mode != GBA_LOCAL) return fail(ctx, GBA_EINVAL, "bad mode %d", p->mode);
+    if (p->mode != GBA_GLOBAL && p->mode != GBA_LOCAL && p->mode != GBA_ALIGN_EXTEND)
+        return fail(ctx, GBA_EINVAL, "bad mode %d", p->mode);
+    if (p->mode == GBA_ALIGN_EXTEND) {
+        if (!p->band_on)
+            return fail(ctx, GBA_EUNSUPPORTED, "GBA_ALIGN_EXTEND is banded only (unbanded: gba_extend_alignments)");
+        if (p->score_bits != 32) return fail(ctx, GBA_EUNSUPPORTED, "GBA_ALIGN_EXTEND runs 32-bit cells");
+        if (p->gap_model == GBA_GAPS_DYNAMIC)
+            return fail(ctx, GBA_EUNSUPPORTED, "DynamicGaps cells are not an extension profile");
+        if ((p->flags & GBA_FLAG_XDROP) && std::abs(int64_t(p->xdrop)) >= (int64_t(1) << 30))
+            return fail(ctx, GBA_EUNSUPPORTED, "xdrop beyond +-2^30");
+    } else if (p->flags & GBA_FLAG_XDROP) {
+        return fail(ctx, GBA_EINVAL, "GBA_FLAG_XDROP needs mode GBA_ALIGN_EXTEND");
+    }
     if (p->gap_model < 0 || p->gap_model > 3) return fail(ctx, GBA_EINVAL, "bad gap model");
     if (p->gap_model == GBA_GAPS_DYNAMIC && p->band_on)
         return fail(ctx, GBA_EUNSUPPORTED, "DynamicGaps cells are supported unbanded only");
@@ -545,7 +558,9 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     plan->affine = is_affine(*p);
     plan->dynamic = p->gap_model == GBA_GAPS_DYNAMIC;
     plan->local = p->mode == GBA_LOCAL;
-    plan->free_ends = p->free_ends;
+    plan->extend = p->mode == GBA_ALIGN_EXTEND;
+    // AlignExtend_ has a free last row and column (align_extend/align_extend_base.h:75-81).
+    plan->free_ends = plan->extend ? (GBA_FREE_RIGHT | GBA_FREE_BOTTOM) : p->free_ends;
     plan->traceback = (p->outputs & GBA_OUT_SEGMENTS) != 0;
     plan->cigar = (p->outputs & GBA_OUT_CIGAR) != 0;
     plan->matrix = p->matrix != nullptr;
@@ -612,7 +627,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
     std::vector<int64_t> c16(nth + 1, 0), cot(nth + 1, 0), ctr(nth + 1, 0), cw2(nth + 1, 0);
     int64_t first_bad = N, cells = 0;
     double cells16 = 0;   // cells of the packed-path pairs
-    const int fe_all = plan->local ? 15 : p->free_ends;
+    const int fe_all = plan->local ? 15 : plan->free_ends;
 #pragma omp parallel num_threads(nth) reduction(+ : cells, cells16) reduction(min : first_bad)
     {
         const int t = omp_get_thread_num();
@@ -1233,6 +1248,26 @@ const void *warp_fn(bool a, bool l, bool m, bool t)
     return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
 }
 
+// The AlignExtend_ instances of the banded kernel (GBA_ALIGN_EXTEND).
+template <bool A, bool M, bool T>
+void launch_banded_ext(const BandArgs &args, int grid, size_t smem, cudaStream_t s)
+{
+    if (args.upper - args.lower + 1 <= kSmallBandWidth)
+        k_dp_banded<A, false, M, T, kSmallBandWidth, true><<<grid, kBlock, smem, s>>>(args);
+    else
+        k_dp_banded<A, false, M, T, kMaxBandWidth, true><<<grid, kBlock, smem, s>>>(args);
+}
+
+BandLauncher pick_banded_ext(bool a, bool m, bool t)
+{
+    static const BandLauncher table[8] = {
+        launch_banded_ext<false, false, false>, launch_banded_ext<false, false, true>,
+        launch_banded_ext<false, true, false>,  launch_banded_ext<false, true, true>,
+        launch_banded_ext<true, false, false>,  launch_banded_ext<true, false, true>,
+        launch_banded_ext<true, true, false>,   launch_banded_ext<true, true, true>};
+    return table[(a ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
+}
+
 BandLauncher pick_banded(bool a, bool l, bool m, bool t)
 {
     static const BandLauncher table[16] = {
@@ -1441,9 +1476,14 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
         b.alphabet = plan->matrix ? plan->params.alphabet_size : 0;
         b.lower = plan->params.band_lower;
         b.upper = plan->params.band_upper;
+        b.xdrop_on = plan->extend && (plan->params.flags & GBA_FLAG_XDROP) ? 1 : 0;
+        b.xdrop = plan->params.xdrop;
         const int grid = int((plan->num_slots + kBlock - 1) / kBlock);
         const size_t smem = plan->matrix ? size_t(32 * 32) * sizeof(int) : 0;
-        pick_banded(plan->affine, plan->local, plan->matrix, plan->traceback)(b, grid, smem, ctx->stream);
+        if (plan->extend)
+            pick_banded_ext(plan->affine, plan->matrix, plan->traceback)(b, grid, smem, ctx->stream);
+        else
+            pick_banded(plan->affine, plan->local, plan->matrix, plan->traceback)(b, grid, smem, ctx->stream);
         GBA_CUDA(ctx, cudaGetLastError());
         ++launches;
     } else if (plan->num_slots > 0 && plan->use_warp) {
@@ -1574,6 +1614,7 @@ int enqueue_plan(gba_context *ctx, gba_plan *plan, const uint8_t *dseq_h, const 
             t.num_slots = plan->num_slots;
             t.affine = plan->affine;
             t.local = plan->local;
+            t.extend = plan->extend;
             t.band_w = plan->params.band_on ? plan->params.band_upper - plan->params.band_lower + 1 : 0;
             t.band_upper = plan->params.band_upper;
             t.warp_rows = plan->use_warp ? plan->warp_rows : 0;

@@ -5,7 +5,8 @@
 // finds each task's best cell and last computed column; the host then sizes the trace
 // (last column + 1 columns of round8(rows + 1) bytes per task) and the segment slots, and a trace
 // pass recomputes exactly those columns with trace, followed by the traceback.  Tasks are cut
-// into chunks whose trace fits kExtTraceBudget.
+// into chunks whose trace fits kExtTraceBudget.  With a band, both sides run as one
+// GBA_ALIGN_EXTEND batch on the banded kernel instead (ext_banded).
 #pragma once
 
 namespace {
@@ -77,6 +78,115 @@ int64_t ext_max_groups(gba_context *ctx, int W)
     return int64_t(std::max(sms, 1)) * 2048 / W;   // 2,048 resident threads per SM at most
 }
 
+// The banded overloads (lowerDiag, upperDiag): each side is one pair of a GBA_ALIGN_EXTEND batch
+// -- the reversed prefixes for the left side, the suffixes for the right one -- aligned by the
+// banded kernel in its AlignExtend_ mode with the engine's traceback; the left side's segments
+// are then mapped back as _reversePartialTrace does.
+int ext_banded(gba_context *ctx, const gba_extend_align_params *params, const std::vector<int32_t> &mat,
+               const gba_seed_batch *b, const gba_seed *seeds, gba_extend_align_result *res)
+{
+    const int64_t ns = b->num_seeds;
+    std::vector<uint8_t> hcat, vcat;
+    std::vector<int64_t> hoff(1, 0), voff(1, 0);
+    std::vector<int64_t> task_of(size_t(ns) * 2, -1);
+    int64_t cap = 0;
+    for (int64_t k = 0; k < ns; ++k) {
+        const int64_t hi = b->seed_h ? b->seed_h[k] : k, vi = b->seed_v ? b->seed_v[k] : k;
+        if (hi < 0 || hi >= b->num_h || vi < 0 || vi >= b->num_v)
+            return fail(ctx, GBA_EINVAL, "alignment %lld names a missing sequence", (long long)k);
+        const int64_t m = b->off_h[hi + 1] - b->off_h[hi], n = b->off_v[vi + 1] - b->off_v[vi];
+        if (m > kExtMaxLen || n > kExtMaxLen) return fail(ctx, GBA_EUNSUPPORTED, "sequences longer than 2^28");
+        const gba_seed &sd = seeds[k];
+        if (!(0 <= sd.begin_h && sd.begin_h <= sd.end_h && sd.end_h <= m && 0 <= sd.begin_v &&
+              sd.begin_v <= sd.end_v && sd.end_v <= n))
+            return fail(ctx, GBA_EINVAL, "alignment %lld lies outside its sequences", (long long)k);
+        const uint8_t *h = b->seq_h + b->off_h[hi], *v = b->seq_v + b->off_v[vi];
+        if ((params->direction & GBA_EXTEND_LEFT) && sd.begin_h > 0 && sd.begin_v > 0) {
+            task_of[2 * k] = int64_t(hoff.size()) - 1;
+            for (int64_t i = sd.begin_h - 1; i >= 0; --i) hcat.push_back(h[i]);
+            for (int64_t i = sd.begin_v - 1; i >= 0; --i) vcat.push_back(v[i]);
+            hoff.push_back(int64_t(hcat.size()));
+            voff.push_back(int64_t(vcat.size()));
+            cap += sd.begin_h + sd.begin_v + 2;
+        }
+        if ((params->direction & GBA_EXTEND_RIGHT) && sd.end_h < m && sd.end_v < n) {
+            task_of[2 * k + 1] = int64_t(hoff.size()) - 1;
+            hcat.insert(hcat.end(), h + sd.end_h, h + m);
+            vcat.insert(vcat.end(), v + sd.end_v, v + n);
+            hoff.push_back(int64_t(hcat.size()));
+            voff.push_back(int64_t(vcat.size()));
+            cap += (m - sd.end_h) + (n - sd.end_v) + 2;
+        }
+    }
+    const int64_t nt = int64_t(hoff.size()) - 1;
+    std::vector<int32_t> score(size_t(std::max<int64_t>(nt, 1))), status(size_t(std::max<int64_t>(nt, 1)));
+    std::vector<gba_segment> segs(size_t(std::max<int64_t>(cap, 1)));
+    std::vector<int64_t> seg_off(size_t(nt) + 1, 0);
+    if (nt > 0) {
+        if (hcat.empty()) hcat.push_back(0);
+        if (vcat.empty()) vcat.push_back(0);
+        gba_params gp{};
+        gp.mode = GBA_ALIGN_EXTEND;
+        gp.gap_model = GBA_GAPS_AUTO;   // Gotoh iff open != extend, as _extendAlignmentImpl picks
+        gp.band_on = 1;
+        gp.band_lower = params->band_lower;
+        gp.band_upper = params->band_upper;
+        gp.match = params->match;
+        gp.mismatch = params->mismatch;
+        gp.gap_open = params->gap_open;
+        gp.gap_extend = params->gap_extend;
+        gp.matrix = mat.empty() ? nullptr : mat.data();
+        gp.alphabet_size = mat.empty() ? 0 : params->alphabet_size;
+        gp.score_bits = 32;
+        gp.outputs = GBA_OUT_SCORE | GBA_OUT_END | GBA_OUT_SEGMENTS;
+        gp.flags = params->xdrop_on ? GBA_FLAG_XDROP : 0;
+        gp.xdrop = params->xdrop;
+        gba_batch gb{};
+        gb.num_pairs = nt;
+        gb.seq_h = hcat.data();
+        gb.off_h = hoff.data();
+        gb.seq_v = vcat.data();
+        gb.off_v = voff.data();
+        gba_result gr{};
+        gr.score = score.data();
+        gr.pair_status = status.data();
+        gr.segments = segs.data();
+        gr.segment_capacity = cap;
+        gr.segment_offsets = seg_off.data();
+        if (int rc = gba_align_batch(ctx, &gp, &gb, &gr)) return rc;
+    }
+    int64_t w = 0;
+    for (int64_t k = 0; k < ns; ++k) {
+        for (int side = 0; side < 2; ++side) {
+            const int64_t t = task_of[2 * k + side];
+            int32_t sc = 0;
+            if (t >= 0) {
+                sc = score[t];   // INT32_MIN with no segments for a band outside the side's matrix
+                const int64_t c = seg_off[t + 1] - seg_off[t];
+                if (w + c > res->segment_capacity || (c && !res->segments))
+                    return fail(ctx, GBA_ECAPACITY, "segment_capacity too small");
+                const gba_segment *sg = segs.data() + seg_off[t];
+                if (side == 1) {
+                    for (int64_t q = 0; q < c; ++q) res->segments[w + q] = sg[q];
+                } else {
+                    const uint32_t lh = uint32_t(hoff[t + 1] - hoff[t]), lv = uint32_t(voff[t + 1] - voff[t]);
+                    for (int64_t q = 0; q < c; ++q) {
+                        const gba_segment &x = sg[c - 1 - q];
+                        const uint32_t eh = x.h_begin + ((x.type == GBA_SEG_DIAGONAL || x.type == GBA_SEG_HORIZONTAL) ? x.length : 0);
+                        const uint32_t ev = x.v_begin + ((x.type == GBA_SEG_DIAGONAL || x.type == GBA_SEG_VERTICAL) ? x.length : 0);
+                        res->segments[w + q] = gba_segment{lh - eh, lv - ev, x.length, x.type};
+                    }
+                }
+                w += c;
+            }
+            if (side == 0 && res->left_score) res->left_score[k] = sc;
+            if (side == 1 && res->right_score) res->right_score[k] = sc;
+            res->segment_offsets[2 * k + side + 1] = w;
+        }
+    }
+    return GBA_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -103,6 +213,10 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
     const int64_t hb_total = b->off_h[b->num_h], vb_total = b->off_v[b->num_v];
     if (b->off_h[0] < 0 || b->off_v[0] < 0) return fail(ctx, GBA_EINVAL, "negative offset");
     if ((hb_total && !b->seq_h) || (vb_total && !b->seq_v)) return fail(ctx, GBA_EINVAL, "null sequence codes");
+    if (params->band_on) {
+        if (params->band_lower > params->band_upper) return fail(ctx, GBA_EINVAL, "band_lower > band_upper");
+        return ext_banded(ctx, params, mat, b, seeds, res);
+    }
     const bool affine = params->gap_open != params->gap_extend;
     const bool matrix = !mat.empty();
     cudaStream_t st = ctx->stream;

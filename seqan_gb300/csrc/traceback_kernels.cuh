@@ -3,7 +3,8 @@
 // One thread per pair walks back from the best cell exactly as the reference does:
 //   start-cell correction          align/dp_algorithm_impl.h:1188-1205 (affine only)
 //   initial direction              align/dp_traceback_impl.h:456-483 (PreferGapsAtEnd_ for affine)
-//   tail / head gap segments       align/dp_traceback_impl.h:522-545 (global only)
+//   tail / head gap segments       align/dp_traceback_impl.h:522-545 (global only; the
+//                                  AlignExtend_ profile records the head only)
 //   walk order and gap walkers     align/dp_traceback_impl.h:190-450 (GapsLeft)
 //   segment recording              align/dp_trace_segment.h:318-337
 // and writes the segments in the reference's order (traceback order).  Pairs of the warp layout
@@ -87,7 +88,7 @@ __device__ __forceinline__ void traceback_pair(const TraceArgs &a, int p, Cell &
         else if (tv & (TV_H | TV_MFH)) last = TV_H;
         else last = TV_NONE;
     }
-    if (global) {
+    if (global && !a.extend) {
         if (row != n) w.record(m, row, n - row, TV_V);
         if (col != m) w.record(col, row, m - col, TV_H);
     }

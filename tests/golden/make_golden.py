@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|packed|sam|seqio|bam]
+    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|packed|sam|seqio|bam|cpp|dynamic]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -15,6 +15,8 @@ Outputs (all small, committed):
                         (the bits that hold no value, undefined there, masked to zero).
   extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
                         (align_extend/align_extend.h) with and without X-drop: score and rows.
+  extend_banded_cases.json  the other extendAlignment overloads: (lowerDiag, upperDiag) with and
+                        without xDrop, origScore, aligned parts with gaps.
   dynamic_cases.json    pairs aligned by the reference's single-pair DP with DynamicGaps cells
                         (score and raw TraceSegment_ list) for the shapes oracle/ref/units/dynamic_*.cpp
                         instantiate.
@@ -99,6 +101,9 @@ def main():
         return
     if only == "extend":
         write_extend(b62)
+        return
+    if only == "extend_banded":
+        write_extend_banded(b62)
         return
     if only == "packed":
         write_packed()
@@ -254,6 +259,7 @@ def main():
     print(f"{len(cases)} alignment cases written")
     write_seeds(b62)
     write_extend(b62)
+    write_extend_banded(b62)
     write_packed()
     write_sam_cases()
 
@@ -365,6 +371,80 @@ def write_extend(b62):
         json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261205, "cases": cases}, f,
                   separators=(",", ":"))
     print(f"{len(cases)} extendAlignment cases written")
+
+
+def write_extend_banded(b62):
+    """extendAlignment's other overloads: (lowerDiag, upperDiag) with and without xDrop, origScore,
+    and aligned parts with gaps (rows given as text).  Bands include one-diagonal bands, bands
+    wider than the matrices and bands that miss a side's matrix (lowerDiag > 0: the reference's
+    invalid value; the aligned part's score is then set high enough that the reference's int sum
+    stays in range)."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(20261207))
+    cases = []
+    for trial in range(700):
+        aa = trial % 5 == 4
+        A = 20 if aa else 4
+        L = int(rng.integers(2, 160))
+        h = rng.integers(0, A, L).astype(np.uint8)
+        v = W.mutate(rng, h, float(rng.uniform(0, 0.3)), float(rng.uniform(0, 0.08)), alphabet=A)
+        if trial % 6 == 0:
+            v = rng.integers(0, A, int(rng.integers(2, 160))).astype(np.uint8)
+        if aa:
+            h, v = W.AA20_CODES[h], W.AA20_CODES[v]
+        letters = "ABCDEFGHIJKLMNOPQRSTUVWYZX*" if aa else "ACGTN"
+        sl = int(rng.integers(0, min(len(h), len(v), 14) + 1))
+        hb = int(rng.integers(0, len(h) - sl + 1))
+        vb = min(max(hb + int(rng.integers(-3, 4)), 0), len(v) - sl)
+        pos = (hb, vb, hb + sl, vb + sl)
+        kind = trial % 8
+        if kind == 0:
+            band = (0, 0)
+        elif kind == 1:
+            band = (-int(rng.integers(0, 3)), int(rng.integers(0, 3)))
+        elif kind == 2:
+            band = (int(rng.integers(1, 4)), int(rng.integers(4, 9)))          # misses the matrices
+        elif kind == 3:
+            band = (-int(rng.integers(40, 300)), int(rng.integers(40, 300)))   # wider than them
+        else:
+            band = (-int(rng.integers(0, 25)), int(rng.integers(0, 25)))
+        xd = None if trial % 3 == 0 else int(rng.integers(0, 31))
+        if aa:
+            go = int(rng.choice([-11, -9, -4]))
+            pb = O.Problem("extend", 0, band, 0, 0, go, int(rng.choice([-1, go])), b62, 32, "aa", xd)
+        else:
+            go = int(rng.integers(-8, 0))
+            pb = O.Problem("extend", 0, band, int(rng.integers(1, 4)), int(rng.integers(-4, 0)), go,
+                           int(rng.choice([go, -1, -2])), None, 32, "dna", xd)
+        center = None
+        if trial % 4 == 1 and sl >= 2:
+            t0 = "".join(letters[c] for c in h[hb:hb + sl])
+            t1 = "".join(letters[c] for c in v[vb:vb + sl])
+            i, g = int(rng.integers(1, sl)), int(rng.integers(1, 4))
+            if rng.random() < 0.5:
+                t0 = t0[:i] + "-" * g + t0[i:]
+                j = int(rng.integers(0, len(t1) + 1))
+                t1 = t1[:j] + "-" * g + t1[j:]
+            else:
+                t1 = t1[:i] + "-" * g + t1[i:]
+                j = int(rng.integers(0, len(t0) + 1))
+                t0 = t0[:j] + "-" * g + t0[j:]
+            center = [t0, t1]
+        orig = None if trial % 3 != 2 else int(rng.integers(-40, 60))
+        if kind == 2:
+            orig = 1 << 20
+        d = int(rng.integers(0, 4))
+        r = O.ref_extend_alignment(pb, h, v, pos, d, orig_score=orig, center=center)
+        cases.append({"alphabet": pb.alphabet, "blosum62": pb.matrix is not None, "match": pb.match,
+                      "mismatch": pb.mismatch, "gap_open": pb.gap_open, "gap_extend": pb.gap_extend,
+                      "xdrop": pb.xdrop, "band": list(band), "orig_score": orig, "center": center,
+                      "H": text(h, pb.alphabet), "V": text(v, pb.alphabet), "positions": [int(x) for x in pos],
+                      "direction": d, "score": r.score, "row0": r.row0, "row1": r.row1,
+                      "ends": [r.h_begin, r.h_end, r.v_begin, r.v_end]})
+    with open(os.path.join(HERE, "extend_banded_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261207, "cases": cases}, f,
+                  separators=(",", ":"))
+    print(f"{len(cases)} banded / origScore / gapped extendAlignment cases written")
 
 
 def write_seeds(b62):

@@ -7,7 +7,7 @@ import pytest
 
 from oracle import oracle as O
 from tests import golden_cases as G
-from tests.test_extend_oracle import EXTEND_CASES, KNOWN, extend_problem
+from tests.test_extend_oracle import BANDED_CASES, EXTEND_CASES, KNOWN, banded_problem, extend_problem
 
 pytestmark = pytest.mark.gpu
 
@@ -24,7 +24,7 @@ def engine_score(pb):
 def check_batch(pb, H, V, positions, direction, letters="ACGTN", alphabet="dna5", seed_h=None):
     from seqan_gb300 import align_extend as X
     exts = X.extend_alignments(H, V, positions, direction, engine_score(pb), pb.xdrop, seed_h=seed_h,
-                               alphabet=alphabet)
+                               alphabet=alphabet, band=pb.band)
     for k, ext in enumerate(exts):
         h = H[seed_h[k]] if seed_h is not None else H[k]
         got = X.assemble(ext, h, V[k], positions[k], engine_score(pb), alphabet)
@@ -145,3 +145,65 @@ def test_refusals(engine):
     assert e.value.status == N.GBA_EINVAL
     out = X.extendAlignment("ACGTACGT", "ACGTACGT", (3, 3, 5, 5), X.EXTEND_BOTH, sg.Score(1, -1, -1))
     assert (out.score, out.row0, out.h_begin, out.h_end) == (8, "ACGTACGT", 0, 8)
+
+
+# --- The other overloads: (lowerDiag, upperDiag), origScore, aligned parts with gaps -----------
+
+@pytest.mark.parametrize("chunk", range(0, len(BANDED_CASES), 140))
+def test_banded_origscore_gapped_fixtures_through_c_abi(engine, chunk):
+    """The reference's extendAlignment overloads with (lowerDiag, upperDiag) [and xDrop], with
+    origScore and with gapped aligned parts: one gba_extend_alignments call per case (the banded
+    kernel in its AlignExtend_ mode, GBA_ALIGN_EXTEND)."""
+    from seqan_gb300 import align_extend as X
+    for c in BANDED_CASES[chunk:chunk + 140]:
+        pb = banded_problem(c)
+        alph = "aa" if c["alphabet"] == "aa" else "dna5"
+        args = tuple(c["band"]) + (() if c["xdrop"] is None else (c["xdrop"],)) + (engine_score(pb),)
+        got = X.extendAlignment(c["H"], c["V"], c["positions"], c["direction"], *args, alphabet=alph,
+                                orig_score=c["orig_score"],
+                                center=None if c["center"] is None else tuple(c["center"]))
+        assert (got.score, got.row0, got.row1, [got.h_begin, got.h_end, got.v_begin, got.v_end]) == \
+            (c["score"], c["row0"], c["row1"], c["ends"]), c
+
+
+@pytest.mark.parametrize("band", [(-10, 10), (-3, 3), (0, 0), (-30, 5), (-200, 200)])
+@pytest.mark.parametrize("xdrop", [None, 8])
+def test_banded_read_seeds_batch(engine, band, xdrop):
+    """3,000 read seeds in 250 bp windows, both sides extended inside a band, vs the oracle."""
+    from seqan_gb300 import workloads as W
+    wins, reads, seeds, _ = W.seed_windows(3000, ref_len=1_000_000, seed=37)
+    pos = [(int(s[0]), int(s[1]), int(s[0] + s[2]), int(s[1] + s[2])) for s in seeds]
+    pb = O.Problem("extend", 0, band, 1, -2, -4, -1, None, 32, "dna", xdrop)
+    check_batch(pb, wins, reads, pos, O.EXTEND_BOTH)
+    assert _kernels() & _flags().GBA_KERNEL_BANDED
+
+
+def test_banded_protein_and_invalid_bands(engine):
+    """Blosum62 sides in a band, and a band that misses the sides' matrices (lowerDiag > 0): the
+    side scores are the reference's invalid value and no segments."""
+    from seqan_gb300 import align_extend as X
+    from seqan_gb300 import workloads as W
+    B62 = np.array(G.load("blosum62.json")["matrix"], dtype=np.int32)
+    H, V = W.protein_pairs(300, seed=43, related=0.9, identity=0.6)
+    pos = []
+    for h, v in zip(H, V):
+        b = min(len(h), len(v)) // 3
+        pos.append((b, b, b + 4, b + 4))
+    for band, xd in (((-15, 15), None), ((-15, 15), 25), ((-2, 6), 12)):
+        pb = O.Problem("extend", 0, band, 0, 0, -11, -1, B62, 32, "aa", xd)
+        check_batch(pb, H, V, pos, O.EXTEND_BOTH, letters=AA, alphabet="aa")
+    exts = X.extend_alignments(H[:5], V[:5], pos[:5], X.EXTEND_BOTH, engine_score(
+        O.Problem("extend", 0, None, 0, 0, -11, -1, B62, 32, "aa")), band=(1, 4), alphabet="aa")
+    for e in exts:
+        assert e.left_score == e.right_score == -2 ** 31
+        assert e.left_segments == [] and e.right_segments == []
+
+
+def _flags():
+    from seqan_gb300 import _native as N
+    return N
+
+
+def _kernels():
+    import seqan_gb300 as sg
+    return sg.default_context().stats().dp_kernels
