@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-shared", "-lgomp"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp"]
 
 # Status codes (include/seqan_gb300.h)
 GBA_OK, GBA_EINVAL, GBA_ENOMEM, GBA_EBUDGET, GBA_ECUDA, GBA_ETIMEOUT, GBA_EUNSUPPORTED, GBA_ECAPACITY, GBA_EPARSE = \
@@ -167,19 +167,39 @@ def _sources():
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles the engine for sm_103a into seqan_gb300/_lib/ (no-op when up to date)."""
+    """Compiles the engine for sm_103a into seqan_gb300/_lib/ (no-op when up to date): each
+    translation unit to an object file in parallel, then one link."""
     srcs = _sources()
     newest = max(os.path.getmtime(s) for s in srcs)
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
     os.makedirs(LIB_DIR, exist_ok=True)
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    tag = f"tmp{os.getpid()}"
     units = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith(".cu")]
-    cmd = ["nvcc", *NVCC_FLAGS, "-o", tmp, *units]
-    if verbose:
-        print(" ".join(cmd))
-    subprocess.check_call(cmd)
-    os.replace(tmp, LIB_PATH)
+    objs = [os.path.join(LIB_DIR, os.path.basename(u)[:-3] + f".{tag}.o") for u in units]
+    procs = []
+    try:
+        for u, o in zip(units, objs):
+            cmd = ["nvcc", *NVCC_FLAGS, "-c", "-o", o, u]
+            if verbose:
+                print(" ".join(cmd))
+            procs.append((cmd, subprocess.Popen(cmd)))
+        failed = [cmd for cmd, pr in procs if pr.wait() != 0]
+        if failed:
+            raise subprocess.CalledProcessError(1, failed[0])
+        tmp = LIB_PATH + f".{tag}"
+        link = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", tmp, *objs, "-lgomp"]
+        if verbose:
+            print(" ".join(link))
+        subprocess.check_call(link)
+        os.replace(tmp, LIB_PATH)
+    finally:
+        for cmd, pr in procs:
+            if pr.poll() is None:
+                pr.wait()
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
     return LIB_PATH
 
 

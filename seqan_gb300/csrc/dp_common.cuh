@@ -19,6 +19,28 @@ constexpr uint8_t TV_VO = 16;
 constexpr uint8_t TV_MFH = 32;
 constexpr uint8_t TV_MFV = 64;
 
+// The 4-bit trace code: bits 0-1 the source of S (0 none, 1 diagonal, 2 MAX_FROM_V, 3
+// MAX_FROM_H), bit 2 "E opened" (H_OPEN without H), bit 3 "F opened" (V_OPEN without V).  With
+// SingleTrace exactly one bit of each open/extend pair is set in inner cells (align/dp_formula.h:
+// 179-181), and _doTraceback (align/dp_traceback_impl.h:376-450) reads nothing else, so decoding
+// gives back every decision it makes; border and band-edge cells, which lack a pair, decode with
+// "extend" for it.
+__host__ __device__ __forceinline__ uint32_t trace4_encode(uint32_t tv)
+{
+    const uint32_t src = (tv & TV_DIAG) ? 1u : (tv & TV_MFV) ? 2u : (tv & TV_MFH) ? 3u : 0u;
+    const uint32_t eo = ((tv & TV_HO) && !(tv & TV_H)) ? 4u : 0u;
+    const uint32_t fo = ((tv & TV_VO) && !(tv & TV_V)) ? 8u : 0u;
+    return src | eo | fo;
+}
+__host__ __device__ __forceinline__ uint8_t trace4_decode(uint32_t code, bool affine)
+{
+    const uint32_t src = code & 3u;
+    if (src == 0) return TV_NONE;
+    if (!affine) return src == 1 ? TV_DIAG : (src == 2 ? uint8_t(TV_V | TV_MFV) : uint8_t(TV_H | TV_MFH));
+    const uint8_t sb = src == 1 ? TV_DIAG : (src == 2 ? TV_MFV : TV_MFH);
+    return uint8_t(sb | ((code & 4u) ? TV_HO : TV_H) | ((code & 8u) ? TV_VO : TV_V));
+}
+
 constexpr int FREE_TOP = 1, FREE_LEFT = 2, FREE_RIGHT = 4, FREE_BOTTOM = 8;
 
 // Rows per register strip of the one-pair-per-thread kernels.  16 trace bytes per strip

@@ -9,6 +9,7 @@
 #include "dp_kernels.cuh"
 #include "traceback_kernels.cuh"
 #include "dp16x2_kernels.cuh"
+#include "banded_launch.cuh"
 #include "dp_banded_kernels.cuh"
 #include "dp_warp_kernels.cuh"
 #include "dp_warp2_kernels.cuh"
@@ -227,6 +228,17 @@ struct gba_context {
     DevBuf fa_text, fa_sum, fa_tmp, fa_out, fa_chunk;   // gba_read_fasta
 };
 
+// Banded kernel launchers (banded_launch_*.cu, translation units of their own).
+BandLauncher pick_banded(bool a, bool l, bool m, bool t)
+{
+    return a ? (l ? pick_banded_affine_local(m, t) : pick_banded_affine_global(m, t))
+             : (l ? pick_banded_linear_local(m, t) : pick_banded_linear_global(m, t));
+}
+BandLauncher pick_banded_ext(bool a, bool m, bool t)
+{
+    return a ? pick_banded_ext_affine(m, t) : pick_banded_ext_linear(m, t);
+}
+
 namespace {
 
 int fail(gba_context *ctx, int code, const char *fmt, ...)
@@ -273,6 +285,10 @@ constexpr int64_t kW2MinPairs = 4096;
 
 // _checkBandProperties (align/dp_algorithm_impl.h:193-234): the band must meet the matrix and
 // may leave it only across sides whose end gaps are free.
+// Trace bytes of one band column for the 32 lanes of a warp: 4-bit codes for bands of at most
+// kBandFastW diagonals, otherwise one byte per slot.
+int band_col_bytes(int W) { return band_trace4(W) ? band4_col_bytes(W) : band_trace_stride(W) * 32; }
+
 bool band_valid(const gba_params &p, int64_t m, int64_t n, int fe)
 {
     const int64_t lo = p.band_lower, up = p.band_upper;
@@ -687,7 +703,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
                 ++not16;
             }
             if (plan->traceback) {
-                tbytes[k] = p->band_on ? int64_t(d.m + 1) * band_trace_stride(p->band_upper - p->band_lower + 1)
+                tbytes[k] = p->band_on ? int64_t(d.m + 1) * band_col_bytes(p->band_upper - p->band_lower + 1) / 32
                             : cls[k] == 3 ? warp2_trace_bytes(d.m, d.n)
                             : plan->use_warp ? warp_trace_bytes(d.m, d.n, plan->warp_rows)
                                              : trace_bytes(d.m, d.n);
@@ -763,10 +779,11 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
         sort_desc(keys, idx);
     }
     plan->num_slots = int64_t(idx.size());
-    // Banded traces are interleaved by lane within each warp of 32 slots (see band_trace_pos):
-    // a warp's region holds 32 x (its largest m + 1) columns of band_trace_stride(W) bytes.
+    // Banded traces are interleaved by lane within each warp of 32 slots (see band_trace_pos and
+    // band4_pos): a warp's region holds (its largest m + 1) columns of band_col_bytes(W) bytes
+    // for the 32 lanes, rounded up to 512 bytes so that a pair's lane is (trace_off >> 4) & 31.
     if (p->band_on && plan->traceback && plan->num_slots > 0) {
-        const int Wt = band_trace_stride(p->band_upper - p->band_lower + 1);
+        const int CB = band_col_bytes(p->band_upper - p->band_lower + 1);
         const int64_t nw = (plan->num_slots + 31) / 32;
         std::vector<int64_t> wsize(nw + 1, 0);
 #pragma omp parallel for num_threads(plan_threads(plan->num_slots)) schedule(static)
@@ -774,7 +791,7 @@ int build_plan(gba_context *ctx, const gba_params *p, const gba_batch *b, gba_pl
             int maxm = -1;
             for (int64_t s = 32 * w; s < std::min(plan->num_slots, 32 * w + 32); ++s)
                 if (idx[s] >= 0) maxm = std::max(maxm, desc[idx[s]].m);
-            wsize[w + 1] = maxm < 0 ? 0 : int64_t(maxm + 1) * Wt * 32;
+            wsize[w + 1] = maxm < 0 ? 0 : (int64_t(maxm + 1) * CB + 511) / 512 * 512;
         }
         for (int64_t w = 0; w < nw; ++w) wsize[w + 1] += wsize[w];
 #pragma omp parallel for num_threads(plan_threads(plan->num_slots)) schedule(static)
@@ -1161,19 +1178,6 @@ void launch_dp(const DpArgs &args, int grid, size_t smem, cudaStream_t s)
 
 using DpLauncher = void (*)(const DpArgs &, int, size_t, cudaStream_t);
 
-// Bands of at most kSmallBandWidth diagonals keep their slot arrays in a 64-entry instance: the
-// arrays sit in local memory (indexed per cell), and the 512-entry ones of wide bands (6 KB per
-// thread) overflow L1 and turn into L2 traffic.
-constexpr int kSmallBandWidth = 64;
-template <bool A, bool L, bool M, bool T>
-void launch_banded(const BandArgs &args, int grid, size_t smem, cudaStream_t s)
-{
-    if (args.upper - args.lower + 1 <= kSmallBandWidth)
-        k_dp_banded<A, L, M, T, kSmallBandWidth><<<grid, kBlock, smem, s>>>(args);
-    else
-        k_dp_banded<A, L, M, T, kMaxBandWidth><<<grid, kBlock, smem, s>>>(args);
-}
-using BandLauncher = void (*)(const BandArgs &, int, size_t, cudaStream_t);
 
 constexpr int kWarpRows = 8;
 template <bool A, bool L, bool M, bool T>
@@ -1245,40 +1249,6 @@ const void *warp_fn(bool a, bool l, bool m, bool t)
                              GBA_WF(true, true, false, false),   GBA_WF(true, true, false, true),
                              GBA_WF(true, true, true, false),    GBA_WF(true, true, true, true)};
 #undef GBA_WF
-    return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
-}
-
-// The AlignExtend_ instances of the banded kernel (GBA_ALIGN_EXTEND).
-template <bool A, bool M, bool T>
-void launch_banded_ext(const BandArgs &args, int grid, size_t smem, cudaStream_t s)
-{
-    if (args.upper - args.lower + 1 <= kSmallBandWidth)
-        k_dp_banded<A, false, M, T, kSmallBandWidth, true><<<grid, kBlock, smem, s>>>(args);
-    else
-        k_dp_banded<A, false, M, T, kMaxBandWidth, true><<<grid, kBlock, smem, s>>>(args);
-}
-
-BandLauncher pick_banded_ext(bool a, bool m, bool t)
-{
-    static const BandLauncher table[8] = {
-        launch_banded_ext<false, false, false>, launch_banded_ext<false, false, true>,
-        launch_banded_ext<false, true, false>,  launch_banded_ext<false, true, true>,
-        launch_banded_ext<true, false, false>,  launch_banded_ext<true, false, true>,
-        launch_banded_ext<true, true, false>,   launch_banded_ext<true, true, true>};
-    return table[(a ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
-}
-
-BandLauncher pick_banded(bool a, bool l, bool m, bool t)
-{
-    static const BandLauncher table[16] = {
-        launch_banded<false, false, false, false>, launch_banded<false, false, false, true>,
-        launch_banded<false, false, true, false>,  launch_banded<false, false, true, true>,
-        launch_banded<false, true, false, false>,  launch_banded<false, true, false, true>,
-        launch_banded<false, true, true, false>,   launch_banded<false, true, true, true>,
-        launch_banded<true, false, false, false>,  launch_banded<true, false, false, true>,
-        launch_banded<true, false, true, false>,   launch_banded<true, false, true, true>,
-        launch_banded<true, true, false, false>,   launch_banded<true, true, false, true>,
-        launch_banded<true, true, true, false>,    launch_banded<true, true, true, true>};
     return table[(a ? 8 : 0) | (l ? 4 : 0) | (m ? 2 : 0) | (t ? 1 : 0)];
 }
 

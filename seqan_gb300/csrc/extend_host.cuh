@@ -128,9 +128,28 @@ int ext_banded(gba_context *ctx, const gba_extend_align_params *params, const st
         gba_params gp{};
         gp.mode = GBA_ALIGN_EXTEND;
         gp.gap_model = GBA_GAPS_AUTO;   // Gotoh iff open != extend, as _extendAlignmentImpl picks
+        // Diagonals beyond every side's matrix change nothing the banded DP decides (its phase
+        // tests, the tracked cells, which cells are in the band), so a band wider than the
+        // matrices is narrowed to up' = min(up, max over sides of max(m, n + lo + 1)) and then
+        // lo' = max(lo, min over sides of min(-n, up' - n - 1)): each test on (lo, up) --
+        // up < 0, lo >= 0, lo > -n, up > n + lo, up == m - n, up >= m, lo + n vs m -- and the
+        // band's validity keep their value for every side.
+        int64_t lo = params->band_lower, up = params->band_upper;
+        int64_t U = INT64_MIN;
+        for (int64_t t = 0; t < nt; ++t)
+            U = std::max(U, std::max(hoff[t + 1] - hoff[t], (voff[t + 1] - voff[t]) + lo + 1));
+        if (up > U && U > lo) up = U;
+        int64_t L = INT64_MAX;
+        for (int64_t t = 0; t < nt; ++t) {
+            const int64_t n = voff[t + 1] - voff[t];
+            L = std::min(L, std::min(-n, up - n - 1));
+        }
+        if (lo < L) lo = L;
+        if (up - lo + 1 > int64_t(1) << 20)
+            return fail(ctx, GBA_EUNSUPPORTED, "band wider than the engine's band slots");
         gp.band_on = 1;
-        gp.band_lower = params->band_lower;
-        gp.band_upper = params->band_upper;
+        gp.band_lower = int32_t(lo);
+        gp.band_upper = int32_t(up);
         gp.match = params->match;
         gp.mismatch = params->mismatch;
         gp.gap_open = params->gap_open;

@@ -94,7 +94,7 @@ int64_t request_bytes(const gba_params &p, int64_t m, int64_t n)
 {
     int64_t b = m + n + int64_t(sizeof(PairDesc)) + 128;
     if (p.outputs & GBA_OUT_SEGMENTS) {
-        if (p.band_on) b += (m + 1) * band_trace_stride(p.band_upper - p.band_lower + 1);
+        if (p.band_on) b += (m + 1) * band_col_bytes(p.band_upper - p.band_lower + 1) / 32;
         else b += warp_trace_bytes(int(m), int(n), kWarpRows);
         b += (m + n + 4) * 16 * 2;
     }

@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(128) k_traceback(TraceArgs a)
     auto TAT = [&](int c, int r) -> int {
         if (w2) return int(trace_at_warp2(T, m, d.n, affine, c, r));
         if (wr) return int(trace_at_warp(T, m, d.n, wr, c, r));
-        return bw ? int(trace_at_band(T, bw, bu, c, r)) : int(trace_at(T, m, c, r));
+        return bw ? int(trace_at_band(T, d.trace_off, bw, bu, affine, c, r)) : int(trace_at(T, m, c, r));
     };
     traceback_pair(a, p, TAT, true);
 }
