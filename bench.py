@@ -514,6 +514,14 @@ OPS_PER_CELL = {"affine_global": 9, "linear_global": 5, "affine_local": 10, "lin
                 "dynamic_global": 5}
 
 
+# DRAM traffic and ALU-pipe share of the DP kernel from the committed ncu captures (a bench run
+# cannot profile itself): bytes read + written per algorithmic cell of the captured launch, scaled
+# to the timed launch's cells for roofline.traffic.  Workloads without a capture report None.
+CAPTURED = {
+    "affine_dna_100k": {"dram_bytes_per_cell": (143.7e6 + 361.7e6) / 4.336e9, "alu_pipe_pct": 80.8,
+                        "profile": "profiles/k_dp16x2_affine_dna_100k.md"},
+}
+
 KERNEL_NAMES = [(2, "k_pack16 + k_dp16x2 (two pairs per thread, DPX int16x2)"),
                 (16, "k_dp_warp2 (64 strips per warp in int16x2 halves, 4-bit trace)"),
                 (4, "k_dp_warp (one warp per 256-row band, anti-diagonal front)"),
@@ -1580,11 +1588,19 @@ def main():
     st_last = ctx.stats()
     ops = cells * OPS_PER_CELL[kind]
     achieved = ops / (dp_avg_ms * 1e-3) / 1e12
+    cap = CAPTURED.get(args.workload) if not args.pairs and not args.tile_variant else None
     roofline = {"bound": "int32", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
-                "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                "frac": achieved / peak.value if peak.value else None,
+                "traffic": int(cap["dram_bytes_per_cell"] * cells) if cap else None,
                 "kernel": kernel_label(st_last.dp_kernels), "ops_per_cell": OPS_PER_CELL[kind],
                 "dp_kernel_ms": dp_avg_ms,
                 "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"}
+    if cap:
+        # k_int_peak counts an add and a max as two ops; a DPX add-max on int16x2 halves does four
+        # algorithmic ops in one ALU instruction, so the captured ALU-pipe share is the direct
+        # measure of how busy the bound unit is.
+        roofline["traffic_source"] = f"dram__bytes_read.sum + dram__bytes_write.sum per cell of {cap['profile']}"
+        roofline["alu_pipe_pct_captured"] = cap["alu_pipe_pct"]
 
     if spec.traceback:
         roofline["trace_bytes_per_launch"] = int(st_last.trace_bytes)

@@ -20,16 +20,20 @@
 // band phases, align/dp_algorithm_impl.h:746-836).
 //
 // Band state: per thread, slot k = upper - col + row (one per diagonal) of S, E and the stored
-// F, in per-thread arrays (local memory).  Trace: one byte per band slot per column (the
-// reference's TraceBitMap_ bits), columns band_trace_stride(W) = W rounded up to 16 bytes
-// apart so a column can be written with 16-byte stores.
+// F, in per-thread arrays (local memory).  Trace: for bands of at most kBandFastW diagonals the
+// 4-bit trace code of each cell (trace4_encode: 0.5 byte per band slot per column, band4_pos),
+// for wider bands one byte per band slot per column (the reference's TraceBitMap_ bits), columns
+// band_trace_stride(W) = W rounded up to 16 bytes apart; both interleaved by lane per warp so a
+// warp's column stores coalesce.
 //
 // Middle phase fast path: the columns whose track covers all W slots (first cell Upper, inner
 // cells All, last cell Lower, every cell tracked in local mode and none otherwise) are most of
 // a banded alignment.  For W <= kBandFastW they run with slots 0 .. W-2 in register arrays
 // (static indices), the last slot in scalars, a window of V codes packed four per register
-// and shifted one code per column, and the column's trace bytes packed into registers and
-// written with 16-byte stores; the per-cell rules are the generic cell()'s, ties included.
+// and shifted one code per column, and the column's 4-bit trace codes packed into registers and
+// written with one 16-byte store (and a 4-byte one for W > 32); the per-cell rules are the
+// generic cell()'s, ties included.  (A form with every phase in register arrays was measured
+// slower: its per-phase unrolled column code overflowed the instruction cache.)
 #pragma once
 
 #include "dp_common.cuh"
@@ -271,6 +275,171 @@ struct BandedPair {
         offer(S[k], E[k], Fs[k], col, row, last_row);
     }
 
+    // Middle-phase columns hIt + 1 .. hMid with every track covering slots 0 .. W - 1 (first
+    // row in slot 0); advances hIt, vb and ve as the generic loop does.  Same per-cell rules as
+    // cell(): Upper for slot 0, All for slots 1 .. W - 2, Lower for slot W - 1.
+    __device__ void middle_fast(int &hIt, const int hMid, int &vb, int &ve)
+    {
+        constexpr int FW = kBandFastW;
+        constexpr int NW = FW / 4;                    // V window words (4 codes each)
+        constexpr int NT = (FW + 7) / 8;              // trace words of one column (8 codes each)
+        static_assert(FW % 4 == 0, "whole window words");
+        const int WL = W - 1;                         // register slots 0 .. W - 2
+        int Sr[FW], Er[FW];
+#pragma unroll
+        for (int k = 0; k < FW - 1; ++k)
+            if (k < WL) {
+                Sr[k] = S[k];
+                Er[k] = AFFINE ? E[k] : INF;
+            }
+        int sLast = S[WL], eLast = E[WL];
+        // V window of the next column: code k = V[first row - 1 + k] (0 past the end of V).
+        uint32_t vw[NW];
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            uint32_t w = 0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int idx = vb + 4 * q + c;
+                w |= uint32_t(idx < n ? V[idx] : 0) << (8 * c);
+            }
+            vw[q] = w;
+        }
+        // Codes of the next column are loaded one column ahead (their latency hides behind a
+        // column of W cells): H, the last row's V code and the window's incoming V code.
+        int hcN = H[hIt];
+        int vLowN = V[ve];                               // V[ve + 1 - 1] of the first fast column
+        int vInN = (vb + FW < n) ? V[vb + FW] : 0;       // incoming window code after it
+        for (; hIt != hMid; ++hIt) {
+            ++vb;
+            ++ve;
+            const int col = hIt + 1;
+            const int hc = hcN;
+            const int vLow = vLowN;
+            const int vIn = vInN;
+            if (col < hMid) {
+                hcN = H[col];
+                vLowN = ve < n ? V[ve] : 0;
+                vInN = (vb + FW < n) ? V[vb + FW] : 0;
+            }
+            const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
+            int dS = Sr[0];
+            int vS = INF, vF = INF;
+            uint32_t tw[NT];
+#pragma unroll
+            for (int q = 0; q < NT; ++q) tw[q] = 0;
+#pragma unroll
+            for (int k = 0; k < FW - 1; ++k) {
+                if (k >= WL) break;
+                const int vc = int((vw[k >> 2] >> (8 * (k & 3))) & 0xffu);
+                const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
+                const int inter = dS + sub;
+                const int hS = (k + 1 < WL) ? Sr[k + 1] : sLast;   // S(row, col - 1): slot k + 1
+                const int hE = (k + 1 < WL) ? Er[k + 1] : eLast;
+                dS = hS;
+                int s, e, f = INF;
+                uint32_t tv = 0;
+                if (k == 0) {
+                    // Upper: diagonal or horizontal.
+                    if (AFFINE) {
+                        const int eExt = hE + EXT, eOpn = hS + OPEN;
+                        e = max(eExt, eOpn);
+                        s = max(inter, e);
+                        tv = (eExt < eOpn ? 4u : 0u) | (inter < e ? 3u : 1u);
+                        vF = INF;
+                    } else {
+                        const int gh = hS + EXT;
+                        s = max(inter, gh);
+                        tv = inter < gh ? 3u : 1u;
+                        e = hE;
+                    }
+                } else {
+                    // All directions.
+                    if (AFFINE) {
+                        const int eExt = hE + EXT, eOpn = hS + OPEN;
+                        e = max(eExt, eOpn);
+                        const int fExt = vF + EXT, fOpn = vS + OPEN;
+                        f = max(fExt, fOpn);
+                        s = __vimax3_s32(inter, e, f);
+                        if (TRACE) {
+                            tv = (eExt < eOpn ? 4u : 0u) | (fExt < fOpn ? 8u : 0u);
+                            tv |= s == inter ? 1u : (f < e ? 3u : 2u);
+                        }
+                        vF = f;
+                    } else {
+                        const int gv = vS + EXT, gh = hS + EXT;
+                        s = __vimax3_s32(inter, gv, gh);
+                        if (TRACE) tv = s == inter ? 1u : (gv < gh ? 3u : 2u);
+                        e = hE;
+                    }
+                }
+                if (LOCAL && s <= 0) {
+                    s = 0;
+                    tv = 0u;
+                }
+                vS = s;
+                Sr[k] = s;
+                if (AFFINE) Er[k] = e;
+                if (TRACE) tw[k >> 3] |= tv << (4 * (k & 7));
+                if (LOCAL) {
+                    Fs[k] = f;
+                    scout(s, e, f, col, vb + k);
+                }
+            }
+            // Lower: diagonal or vertical (slot W - 1, row ve).
+            {
+                const int vc = vLow;
+                const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
+                const int inter = dS + sub;
+                int s, f = INF;
+                uint32_t tv;
+                if (AFFINE) {
+                    const int fExt = vF + EXT, fOpn = vS + OPEN;
+                    f = max(fExt, fOpn);
+                    s = max(inter, f);
+                    tv = (fExt < fOpn ? 8u : 0u) | (inter < f ? 2u : 1u);
+                } else {
+                    const int gv = vS + EXT;
+                    s = max(inter, gv);
+                    tv = inter < gv ? 2u : 1u;
+                }
+                if (LOCAL && s <= 0) {
+                    s = 0;
+                    tv = 0u;
+                }
+                sLast = s;
+                eLast = INF;
+                lastF = f;
+                if (LOCAL) {
+                    Fs[WL] = f;
+                    scout(s, INF, f, col, ve);
+                }
+                if (TRACE) {
+                    // The last slot's code into its word, then the column: codes 0..31 as a 16-byte
+                    // chunk, 32..39 as a 4-byte word (band4_pos).
+#pragma unroll
+                    for (int q = 0; q < NT; ++q)
+                        if (q == (WL >> 3)) tw[q] |= tv << (4 * (WL & 7));
+                    uint8_t *c = T + int64_t(col) * band4_col_bytes(W);
+                    *reinterpret_cast<uint4 *>(c) = make_uint4(tw[0], tw[1], NT > 2 ? tw[2] : 0u, NT > 3 ? tw[3] : 0u);
+                    if (NT > 4 && W > 32) *reinterpret_cast<uint32_t *>(c + 512 - 12 * lane) = tw[NT > 4 ? 4 : 0];
+                }
+            }
+            // Shift the V window by one row: code k <- code k + 1, the new last code from V.
+#pragma unroll
+            for (int q = 0; q < NW - 1; ++q) vw[q] = __funnelshift_r(vw[q], vw[q + 1], 8);
+            vw[NW - 1] = (vw[NW - 1] >> 8) | (uint32_t(vIn) << 24);   // V[vb + FW - 1]
+        }
+#pragma unroll
+        for (int k = 0; k < FW - 1; ++k)
+            if (k < WL) {
+                S[k] = Sr[k];
+                if (AFFINE) E[k] = Er[k];
+            }
+        S[WL] = sLast;
+        E[WL] = eLast;
+    }
+
     __device__ int first_dir(int type, int loc) const
     {
         if (type == BCOL_INITIAL) return BDIR_ZERO;
@@ -412,6 +581,9 @@ struct BandedPair {
                 if (XT && term) return;
             }
         } else {
+            if (!XT && W >= 2 && W <= kBandFastW && hIt != hMid && ve - vb + 1 == W &&
+                upper - (hIt + 1) + (vb + 1) == 0)
+                middle_fast(hIt, hMid, vb, ve);
             for (; hIt != hMid; ++hIt) {
                 ++vb; ++ve;
                 track(hIt + 1, BCOL_INNER, BLOC_MIDDLE, vb, ve);
@@ -461,406 +633,6 @@ struct BandedPair {
     }
 };
 
-// Register-resident form for bands of at most FW diagonals: the same phases, tracks, cell rules,
-// tracked cells and extra offers as BandedPair::run, with the band's S and E in register arrays
-// indexed by static slot numbers (every slot of a column is visited; slots outside the track are
-// left as they are), a window of FW V codes shifted one row per column, and the column's 4-bit
-// trace codes written with one 16-byte store (plus a 4-byte one for W > 32).  The extra offers
-// at phase boundaries always re-offer the cell computed last; the F they carry is that cell's
-// when it was tracked (the band storage's F slot of its diagonal holds it) or when the call
-// refreshes the slot, and infinity otherwise (no earlier cell of its diagonal was tracked: every
-// such cell lies in row n, which a diagonal meets once).  Pairs whose band reduces to one cell or
-// one diagonal run BandedPair.
-template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, bool XT, int FW>
-struct BandedRegs {
-    static constexpr bool TRK = LOCAL || XT;
-    static constexpr int NW = FW / 4;          // V window words (4 codes each)
-    static constexpr int NT = (FW + 7) / 8;    // trace words of a column (8 codes each)
-    static_assert(FW % 4 == 0 && FW <= 40, "window words; at most 40 slots in the 4-bit layout");
-    const BandArgs &a;
-    const int *smat;
-    const uint8_t *H, *V;
-    uint8_t *T;
-    int lane;
-    int m, n, W, lower, upper, INF, OPEN, EXT;
-    bool fTop, fLeft, fRight, fBottom;
-    int Sr[FW], Er[FW];
-    uint32_t vw[NW];            // code k = V[col - upper - 1 + k] of the current column (0 outside V)
-    int bs, be, bf, bcol, brow;
-    int colmax;
-    bool term;
-    // the cell computed last (the extra offers re-offer it)
-    int lastS, lastE, lastF, lastCol, lastRow;
-    bool lastTracked;
-
-    __device__ BandedRegs(const BandArgs &args, const int *sm) : a(args), smat(sm) {}
-
-    __device__ __forceinline__ void offer(int s, int e, int f, int col, int row, bool last_row)
-    {
-        if (s > bs) { bs = s; be = e; bf = f; bcol = col; brow = row; }
-        if (XT && a.xdrop_on) {
-            colmax = max(colmax, s);
-            if (last_row) {
-                if (bs - colmax >= a.xdrop) term = true;
-                else colmax = INT_MIN;
-            }
-        }
-    }
-    // An extra offer of the cell computed last (see the struct comment).
-    __device__ __forceinline__ void retrack(bool set_f, bool last_row)
-    {
-        offer(lastS, lastE, (set_f || lastTracked) ? lastF : INF, lastCol, lastRow, last_row);
-    }
-    __device__ __forceinline__ int vcode(int k) const { return int((vw[k >> 2] >> (8 * (k & 3))) & 0xffu); }
-    __device__ __forceinline__ int load_v(int idx) const { return (idx >= 0 && idx < n) ? V[idx] : 0; }
-    __device__ __forceinline__ void win_init(int col)
-    {
-        const int base = col - upper - 1;
-#pragma unroll
-        for (int q = 0; q < NW; ++q) {
-            uint32_t w = 0;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) w |= uint32_t(load_v(base + 4 * q + c)) << (8 * c);
-            vw[q] = w;
-        }
-    }
-    // From column col - 1 to col: code k <- code k + 1, the new last code from V.
-    __device__ __forceinline__ void win_shift(int col)
-    {
-        const uint32_t in = uint32_t(load_v(col - upper - 1 + FW - 1));
-#pragma unroll
-        for (int q = 0; q < NW - 1; ++q) vw[q] = __funnelshift_r(vw[q], vw[q + 1], 8);
-        vw[NW - 1] = (vw[NW - 1] >> 8) | (in << 24);
-    }
-    __device__ __forceinline__ void put_column(int col, const uint32_t (&tw)[NT])
-    {
-        if (!TRACE) return;
-        uint8_t *c = T + int64_t(col) * band4_col_bytes(W);
-        *reinterpret_cast<uint4 *>(c) = make_uint4(tw[0], tw[1], NT > 2 ? tw[2] : 0u, NT > 3 ? tw[3] : 0u);
-        if (NT > 4 && W > 32) *reinterpret_cast<uint32_t *>(c + 512 - 12 * lane) = tw[NT > 4 ? 4 : 0];
-    }
-
-    // Column col >= 1 over slots k0..k1, restricted to rows 0..n.  Each cell's recursion direction
-    // follows from where it lies, as DPMetaColumn_ assigns it per track location: row 0 is the
-    // horizontal border (Zero with a free first row), slot 0 below row 0 has no upper neighbour in
-    // the band (UpperDiagonal, its diagonal neighbour from the previous column), slot W - 1 has no
-    // left neighbour (LowerDiagonal), everything else All.  Tracked cells: every cell with TRK,
-    // every cell of the final column with a free last column, and row n when it is not the band's
-    // last slot (the last cell of a full or bottom track) with a free last row or in the final
-    // column; force >= 0 overrides this for single cells.  check: the track's last cell is an
-    // IsLastRow offer for the X-drop terminator.
-    __device__ __forceinline__ void column_any(int col, int k0, int k1, bool check, int force, bool final_col)
-    {
-        const int hc = int(H[col - 1]);
-        const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
-        int dS = INF, vS = INF, vF = INF;
-        uint32_t tw[NT];
-#pragma unroll
-        for (int q = 0; q < NT; ++q) tw[q] = 0;
-        const int rowOf0 = col - upper;
-#pragma unroll
-        for (int k = 0; k < FW; ++k) {
-            const int row = rowOf0 + k;
-            if (k < W && k >= k0 && k <= k1 && row >= 0 && row <= n) {
-                const int hS = (k + 1 < W) ? Sr[(k + 1) % FW] : INF;
-                const int hE = (k + 1 < W) ? Er[(k + 1) % FW] : INF;
-                const bool isR0 = row == 0;
-                const bool isZ = isR0 && fTop, isH = isR0 && !fTop;
-                const bool isU = !isR0 && k == 0, isL = !isR0 && k != 0 && k == W - 1;
-                const bool isA = !isR0 && !isU && !isL;
-                if (isU) dS = Sr[0];
-                const int vc = vcode(k);
-                const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
-                const int inter = dS + sub;
-                const bool hasE = isA || isU || isH, hasF = isA || isL;
-                int s, e, f;
-                uint32_t code;
-                if (AFFINE) {
-                    const int eExt = hE + EXT, eOpn = hS + OPEN;
-                    const int fExt = vF + EXT, fOpn = vS + OPEN;
-                    const int eA = max(eExt, eOpn), fA = max(fExt, fOpn);
-                    const int eM = hasE ? eA : INT_MIN, fM = hasF ? fA : INT_MIN;
-                    const int g = max(eM, fM);
-                    s = isZ ? 0 : (isH ? g : max(inter, g));
-                    const uint32_t src = isH ? 3u : (inter < g ? (fM < eM ? 3u : 2u) : 1u);
-                    code = isZ ? 0u : (src | (hasE && eExt < eOpn ? 4u : 0u) | (hasF && fExt < fOpn ? 8u : 0u));
-                    e = hasE ? eA : (isZ ? Er[k] : INF);
-                    f = hasF ? fA : (isZ ? vF : INF);
-                    if (!isZ) vF = hasF ? fA : INF;
-                } else {
-                    const int gv = isA || isL ? vS + EXT : INT_MIN;
-                    const int gh = hasE ? hS + EXT : INT_MIN;
-                    const int g = max(gv, gh);
-                    s = isZ ? 0 : (isH ? g : max(inter, g));
-                    code = isZ ? 0u : (isH ? 3u : (inter < g ? (gv < gh ? 3u : 2u) : 1u));
-                    e = INF;
-                    f = INF;
-                }
-                if (LOCAL && !isZ && s <= 0) {
-                    s = 0;
-                    code = 0;
-                }
-                if (hasE) dS = hS;
-                else if (isZ) dS = 0;
-                if (!isL) vS = s;
-                Sr[k] = s;
-                if (AFFINE) Er[k] = e;
-                if (TRACE) tw[k >> 3] |= code << (4 * (k & 7));
-                const bool tracked = force >= 0 ? force != 0
-                                                : (TRK || (final_col && fRight) ||
-                                                   (row == n && k != W - 1 && (fBottom || final_col)));
-                const bool lastCell = k == k1 || row == n;
-                if (tracked) offer(s, e, f, col, row, check && lastCell);
-                lastS = s;
-                lastE = e;
-                lastF = f;
-                lastCol = col;
-                lastRow = row;
-                lastTracked = tracked;
-            }
-        }
-        put_column(col, tw);
-    }
-
-    // Column 0 over rows r0..r1 (DPInitialColumn): the first cell Zero, the others vertical gaps
-    // (Zero with a free first column); tracked as track_flag gives for the column's location.
-    __device__ __forceinline__ void column_init(int r0, int r1, int loc)
-    {
-        int vS = INF, vF = INF;
-        uint32_t tw[NT];
-#pragma unroll
-        for (int q = 0; q < NT; ++q) tw[q] = 0;
-        const int k0 = upper + r0, k1 = upper + r1;
-        const bool trF = track_flag(BCOL_INITIAL, loc, 0), trI = track_flag(BCOL_INITIAL, loc, 1);
-        const bool trL = track_flag(BCOL_INITIAL, loc, 2);
-#pragma unroll
-        for (int k = 0; k < FW; ++k) {
-            if (k < W && k >= k0 && k <= k1) {
-                const bool zero = k == k0 || fLeft;
-                int s, e, f;
-                uint32_t code = 0;
-                if (zero) {
-                    s = 0;
-                    e = Er[k];
-                    f = vF;
-                } else if (AFFINE) {
-                    const int fExt = vF + EXT, fOpn = vS + OPEN;
-                    f = max(fExt, fOpn);
-                    s = f;
-                    e = INF;
-                    vF = f;
-                    code = 2u | (fExt < fOpn ? 8u : 0u);
-                } else {
-                    s = vS + EXT;
-                    e = INF;
-                    f = INF;
-                    code = 2u;
-                }
-                vS = s;
-                Sr[k] = s;
-                if (AFFINE) Er[k] = e;
-                if (TRACE) tw[k >> 3] |= code << (4 * (k & 7));
-                const bool tracked = k == k0 ? trF : (k == k1 ? trL : trI);
-                const int row = k - upper;
-                if (tracked) offer(s, e, f, 0, row, k == k1);
-                lastS = s;
-                lastE = e;
-                lastF = f;
-                lastCol = 0;
-                lastRow = row;
-                lastTracked = tracked;
-            }
-        }
-        put_column(0, tw);
-    }
-
-    // The middle phase: tracks over all W slots (first cell Upper with its diagonal neighbour
-    // from the previous column, inner cells All, last cell Lower); tracked only with TRK.
-    __device__ __forceinline__ void column_mid(int col)
-    {
-        const int hc = int(H[col - 1]);
-        const int hrow = MATRIX ? ((hc & 31) << 5) : hc;
-        int dS = Sr[0];
-        int vS = INF, vF = INF;
-        uint32_t tw[NT];
-#pragma unroll
-        for (int q = 0; q < NT; ++q) tw[q] = 0;
-        int s = INF, e = INF, f = INF;
-#pragma unroll
-        for (int k = 0; k < FW; ++k) {
-            if (k < W) {
-                const int hS = (k + 1 < W) ? Sr[(k + 1) % FW] : INF;
-                const int hE = (k + 1 < W) ? Er[(k + 1) % FW] : INF;
-                const int vc = vcode(k);
-                const int sub = MATRIX ? smat[hrow | (vc & 31)] : (hc == vc ? a.match : a.mismatch);
-                const int inter = dS + sub;
-                uint32_t code;
-                const bool first = k == 0, last = k == W - 1;
-                if (AFFINE) {
-                    const int eExt = hE + EXT, eOpn = hS + OPEN;
-                    const int fExt = vF + EXT, fOpn = vS + OPEN;
-                    const int eA = max(eExt, eOpn), fA = max(fExt, fOpn);
-                    const uint32_t eo = eExt < eOpn ? 4u : 0u, fo = fExt < fOpn ? 8u : 0u;
-                    if (first) {
-                        e = eA;
-                        f = INF;
-                        s = max(inter, e);
-                        code = (inter < e ? 3u : 1u) | eo;
-                    } else if (last) {
-                        e = INF;
-                        f = fA;
-                        s = max(inter, f);
-                        code = (inter < f ? 2u : 1u) | fo;
-                    } else {
-                        e = eA;
-                        f = fA;
-                        const int g = max(e, f);
-                        s = __vimax3_s32(inter, e, f);
-                        code = (inter < g ? (f < e ? 3u : 2u) : 1u) | eo | fo;
-                    }
-                    vF = f;
-                } else {
-                    const int gv = vS + EXT, gh = hS + EXT;
-                    if (first) {
-                        s = max(inter, gh);
-                        code = inter < gh ? 3u : 1u;
-                    } else if (last) {
-                        s = max(inter, gv);
-                        code = inter < gv ? 2u : 1u;
-                    } else {
-                        const int g = max(gv, gh);
-                        s = max(inter, g);
-                        code = inter < g ? (gv < gh ? 3u : 2u) : 1u;
-                    }
-                }
-                if (LOCAL && s <= 0) {
-                    s = 0;
-                    code = 0;
-                }
-                dS = hS;
-                vS = s;
-                Sr[k] = s;
-                if (AFFINE) Er[k] = e;
-                if (TRACE) tw[k >> 3] |= code << (4 * (k & 7));
-                if (TRK) offer(s, e, f, col, col - upper + k, XT && last);
-            }
-        }
-        lastS = s;
-        lastE = e;
-        lastF = f;
-        lastCol = col;
-        lastRow = col - upper + W - 1;
-        lastTracked = TRK;
-        put_column(col, tw);
-    }
-
-    __device__ __forceinline__ bool track_flag(int type, int loc, int which) const
-    {
-        if (TRK) return true;
-        const bool lastColFree = type == BCOL_FINAL && fRight;
-        if (which < 2) return lastColFree;
-        if (loc == BLOC_FULL || loc == BLOC_BOTTOM) return type == BCOL_FINAL || fBottom;
-        return lastColFree;
-    }
-    // True for the band shapes BandedPair handles instead (one diagonal, or a band that starts in
-    // the last column or ends in the first one).
-    __device__ static bool degenerate(int m, int n, int lo, int up)
-    {
-        return up == lo || max(0, min(m - 1, lo)) == m - 1 || max(0, min(m, up + n) - 1) == 0;
-    }
-
-    __device__ __forceinline__ void run()
-    {
-#pragma unroll
-        for (int k = 0; k < FW; ++k) {
-            Sr[k] = INF;
-            Er[k] = INF;
-        }
-        bs = INF; be = INF; bf = INF; bcol = 0; brow = 0;
-        colmax = INT_MIN;
-        term = false;
-        lastS = INF; lastE = INF; lastF = INF; lastCol = 0; lastRow = 0; lastTracked = false;
-        const int lo = lower, up = upper;
-        int vb = -min(0, 1 + up);
-        int ve = -min(0, max(-n, lo));
-        const int hb = max(0, min(m - 1, lo));
-        int hTop = min(m - 1, max(0, up));
-        int hMid = min(m - 1, max(0, n + lo));
-        const bool full = up > n + lo;   // the band spans whole columns in its middle phase
-        if (full) { const int t = hTop; hTop = hMid; hMid = t; }
-        const int hBot = max(0, min(m, up + n) - 1);
-        const bool endRetrack = full ? (TRK || fBottom) : ((TRK || fBottom) && lo + n < m);
-        const int endCol = full ? hTop : hMid;   // the extra offer follows this column
-
-        // Initial column (or, for a band right of column 0, its single first cell).
-        win_init(hb);
-        if (lo >= 0 && up >= 0) {
-            // Zero at (hb, 0), slot W - 1; its E stays as stored (infinity).  (Every slot is
-            // assigned: a store to the one slot W - 1 alone would become a dynamically indexed
-            // store and move the arrays to local memory.)
-#pragma unroll
-            for (int k = 0; k < FW; ++k) Sr[k] = k == W - 1 ? 0 : INF;
-            if (TRK) offer(0, INF, INF, hb, 0, false);
-            lastS = 0; lastE = INF; lastF = INF; lastCol = hb; lastRow = 0; lastTracked = TRK;
-            if (TRK) retrack(false, false);
-        } else {
-            if (up < 0) ++vb;
-            column_init(vb, ve, up < 0 ? (lo > -n ? BLOC_MIDDLE : BLOC_BOTTOM) : (lo <= -n ? BLOC_FULL : BLOC_TOP));
-        }
-        if (XT && term) return;
-        if (endCol == hb && endRetrack) retrack(false, true);
-
-        // Columns hb + 1 .. hBot (top, middle or full, bottom phases), then the last computed
-        // column (align/dp_algorithm_impl.h:837-967); one call site per column routine.
-        for (int col = hb + 1; col <= m; ++col) {
-            win_shift(col);
-            const bool inner = col <= hBot;
-            bool mid = false, check = true, fin = false, after = false;
-            int k0 = 0, k1 = W - 1, force = -1;
-            if (inner) {
-                if (col <= hTop) ++ve;                           // top phase
-                else if (!full && col <= hMid) { ++vb; ++ve; }   // middle phase
-                else if (col > hMid) ++vb;                        // bottom phase
-                mid = !full && col > hTop && col <= hMid;
-            } else if (hBot < m - 1) {
-                // The band ends before the final column: one Upper cell.
-                k0 = k1 = up - hBot + vb;
-                check = false;
-                force = TRK ? 1 : 0;
-                after = TRK || fBottom;
-            } else {
-                fin = true;
-                if (up == m - n) {
-                    k0 = k1 = up - m + vb + 1;
-                    check = false;
-                    force = (TRK || fRight) ? 1 : 0;
-                    after = true;
-                } else if (up >= m) {
-                    if (lo + n + 1 > m) ++ve;
-                    after = lo + n <= m && lo + n + 1 > m;
-                } else {
-                    ++vb;
-                    if (lo + n >= m) ++ve;
-                    after = lo + n == m;
-                }
-                if (up != m - n) {
-                    k0 = up - m + vb;
-                    k1 = up - m + ve;
-                }
-            }
-            if (mid) column_mid(col);
-            else column_any(col, k0, k1, check, force, fin);
-            if (inner) {
-                if (XT && term) return;
-                if (col == endCol && endRetrack) retrack(false, true);
-                continue;
-            }
-            if (after) retrack(true, true);
-            break;
-        }
-    }
-};
-
 template <bool AFFINE, bool LOCAL, bool MATRIX, bool TRACE, int WMAX, bool XT = false>
 __global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
 {
@@ -881,35 +653,6 @@ __global__ void __launch_bounds__(128) k_dp_banded(BandArgs a)
     const int fe = LOCAL ? (FREE_TOP | FREE_LEFT | FREE_RIGHT | FREE_BOTTOM)
                          : XT ? (FREE_RIGHT | FREE_BOTTOM) : a.free_ends;
     const int lane = int((d.trace_off >> 4) & 31);
-    if constexpr (WMAX <= 64) {
-      if (W <= kBandFastW &&
-          !BandedRegs<AFFINE, LOCAL, MATRIX, TRACE, XT, kBandFastW>::degenerate(d.m, d.n, a.lower, a.upper)) {
-        BandedRegs<AFFINE, LOCAL, MATRIX, TRACE, XT, kBandFastW> br(a, smat);
-        br.m = d.m;
-        br.n = d.n;
-        br.W = W;
-        br.lower = a.lower;
-        br.upper = a.upper;
-        br.INF = d.inf;
-        br.H = a.seq_h + d.h_off;
-        br.V = a.seq_v + d.v_off;
-        br.T = TRACE ? a.trace + d.trace_off : nullptr;
-        br.lane = lane;
-        br.fTop = fe & FREE_TOP;
-        br.fLeft = fe & FREE_LEFT;
-        br.fRight = fe & FREE_RIGHT;
-        br.fBottom = fe & FREE_BOTTOM;
-        br.OPEN = AFFINE ? a.gap_open : a.gap_extend;
-        br.EXT = a.gap_extend;
-        br.run();
-        a.score[p] = br.bs;
-        if (a.end_h) a.end_h[p] = br.bcol;
-        if (a.end_v) a.end_v[p] = br.brow;
-        if (a.best_e) a.best_e[p] = br.be;
-        if (a.best_f) a.best_f[p] = br.bf;
-        return;
-      }
-    }
     BandedPair<AFFINE, LOCAL, MATRIX, TRACE, WMAX, XT> bp(a, smat);
     bp.lane = lane;
     bp.m = d.m;
