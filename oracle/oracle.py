@@ -611,6 +611,107 @@ def ref_extend_alignment(pb: Problem, h, v, positions, direction, orig_score=Non
 
 
 # ---------------------------------------------------------------------------------------------
+# Waterman-Eggert suboptimal local alignments (LocalAlignmentEnumerator<Score, Unbanded>).
+# ---------------------------------------------------------------------------------------------
+
+class OrcWeParams(C.Structure):
+    _fields_ = [("match", C.c_int32), ("mismatch", C.c_int32), ("gap", C.c_int32), ("matrix", C.POINTER(C.c_int32)),
+                ("alphabet_size", C.c_int32), ("cutoff", C.c_int32)]
+
+
+@dataclass
+class LocalAlignment:
+    score: int
+    row0: str
+    row1: str
+    h_begin: int
+    h_end: int
+    v_begin: int
+    v_end: int
+    segments: list = field(default_factory=list)   # runs in alignment order (h, v, len, type)
+
+
+def _we_rows(segments, h_text, v_text):
+    r0, r1 = [], []
+    for hb, vb, ln, tp in segments:
+        if tp == SEG_DIAGONAL:
+            r0.append(h_text[hb:hb + ln]); r1.append(v_text[vb:vb + ln])
+        elif tp == SEG_HORIZONTAL:
+            r0.append(h_text[hb:hb + ln]); r1.append("-" * ln)
+        else:
+            r0.append("-" * ln); r1.append(v_text[vb:vb + ln])
+    return "".join(r0), "".join(r1)
+
+
+def oracle_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, matrix=None, max_count=1000,
+                           letters="ACGTN") -> list:
+    """Waterman-Eggert alignments of the oracle restatement (orc_waterman_eggert): each with its
+    score, gapped rows, clipped source positions and runs of alignment columns.  A trailing None
+    marks an enumeration stopped where the reference's next step is undefined."""
+    lib = liboracle()
+    lib.orc_waterman_eggert.restype = C.c_int32
+    lib.orc_waterman_eggert.argtypes = [C.POINTER(OrcWeParams), C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                        C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_void_p]
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    p = OrcWeParams(match, mismatch, gap, None, 0, cutoff)
+    keep = None
+    if matrix is not None:
+        keep = np.ascontiguousarray(matrix, dtype=np.int32)
+        p.matrix = keep.ctypes.data_as(C.POINTER(C.c_int32))
+        p.alphabet_size = int(round(np.sqrt(keep.size)))
+    cap = max_count * (len(h) + len(v) + 2) + 8
+    scores = np.zeros(max(max_count, 1), np.int32)
+    begins = np.zeros(2 * max(max_count, 1), np.int32)
+    ends = np.zeros(2 * max(max_count, 1), np.int32)
+    segs = np.zeros((cap, 4), np.uint32)
+    off = np.zeros(max_count + 1, np.int64)
+    undef = C.c_int32(0)
+    k = lib.orc_waterman_eggert(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), max_count, _ptr(scores),
+                                _ptr(begins), _ptr(ends), _ptr(segs), cap, _ptr(off), C.byref(undef))
+    if k < 0:
+        raise RuntimeError("segment buffer too small")
+    ht = "".join(letters[int(c)] for c in h)
+    vt = "".join(letters[int(c)] for c in v)
+    out = []
+    for i in range(k):
+        sg = [tuple(int(x) for x in segs[q]) for q in range(off[i], off[i + 1])]
+        r0, r1 = _we_rows(sg, ht, vt)
+        # each row's clipped region starts at its first residue (after an alignment whose first
+        # column is a gap the two rows differ in length, as the reference prints them)
+        r0, r1 = r0.lstrip("-"), r1.lstrip("-")
+        out.append(LocalAlignment(int(scores[i]), r0, r1, int(begins[2 * i]), int(ends[2 * i]),
+                                  int(begins[2 * i + 1]), int(ends[2 * i + 1]), sg))
+    del keep
+    if undef.value:
+        out.append(None)   # marker: asking the reference for another alignment is undefined here
+    return out
+
+
+def ref_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, blosum62=False, alphabet="dna",
+                        max_count=1000) -> list:
+    """The reference's LocalAlignmentEnumerator (oracle/ref/units/waterman_eggert.cpp)."""
+    lib = libref()
+    lib.ref_local_enumerate.argtypes = [C.c_int32] * 7 + [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
+                                                          C.c_void_p, C.c_void_p, C.c_char_p, C.c_int64]
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    scores = np.zeros(max(max_count, 1), np.int32)
+    pos = np.zeros(4 * max(max_count, 1), np.int32)
+    cap = max_count * 2 * (len(h) + len(v) + 2) + 8
+    rows = C.create_string_buffer(cap)
+    k = lib.ref_local_enumerate(0 if alphabet == "dna" else 1, 1 if blosum62 else 0, match, mismatch, gap, gap,
+                                cutoff, _ptr(h), len(h), _ptr(v), len(v), max_count, _ptr(scores), _ptr(pos), rows,
+                                cap)
+    if k < 0:
+        raise RuntimeError("row buffer too small")
+    lines = rows.value.decode().split("\n")
+    return [LocalAlignment(int(scores[i]), lines[2 * i], lines[2 * i + 1], int(pos[4 * i]), int(pos[4 * i + 1]),
+                           int(pos[4 * i + 2]), int(pos[4 * i + 3])) for i in range(k)]
+
+
+# ---------------------------------------------------------------------------------------------
 # SAM lines (bam_io/write_sam.h:126-217) of BamAlignmentRecord fields given as plain lists.
 # ---------------------------------------------------------------------------------------------
 

@@ -1,0 +1,73 @@
+// Waterman-Eggert suboptimal local alignments through the UNMODIFIED reference (test
+// infrastructure, see ref_common.h): LocalAlignmentEnumerator<Score, Unbanded> with
+// nextLocalAlignment / getScore (align/local_alignment_enumeration_unbanded.h).
+#include "../ref_common.h"
+
+#include <seqan/align.h>
+
+#include <sstream>
+#include <string>
+
+namespace seqan_ref {
+namespace {
+
+template <typename TAlph, typename TScore>
+int enumerate(TScore const & sc, int32_t cutoff, const uint8_t * h, int64_t m, const uint8_t * v, int64_t n,
+              int32_t max_count, int32_t * scores, int32_t * pos, char * out_rows, int64_t cap)
+{
+    typedef String<TAlph> TStr;
+    TStr hs, vs;
+    resize(hs, m);
+    resize(vs, n);
+    for (int64_t i = 0; i < m; ++i) assignValue(hs, i, TAlph(unsigned(h[i])));
+    for (int64_t i = 0; i < n; ++i) assignValue(vs, i, TAlph(unsigned(v[i])));
+    Align<TStr> align;
+    resize(rows(align), 2);
+    assignSource(row(align, 0), hs);
+    assignSource(row(align, 1), vs);
+    LocalAlignmentEnumerator<TScore, Unbanded> enumerator(sc, cutoff);
+    std::string text;
+    int32_t k = 0;
+    for (; k < max_count && nextLocalAlignment(align, enumerator); ++k)
+    {
+        scores[k] = getScore(enumerator);
+        pos[4 * k + 0] = int32_t(beginPosition(row(align, 0)));
+        pos[4 * k + 1] = int32_t(endPosition(row(align, 0)));
+        pos[4 * k + 2] = int32_t(beginPosition(row(align, 1)));
+        pos[4 * k + 3] = int32_t(endPosition(row(align, 1)));
+        std::stringstream s0, s1;
+        s0 << row(align, 0);
+        s1 << row(align, 1);
+        text += s0.str() + "\n" + s1.str() + "\n";
+    }
+    if (int64_t(text.size()) + 1 > cap) return -1;
+    std::memcpy(out_rows, text.c_str(), text.size() + 1);
+    return k;
+}
+
+}  // namespace
+}  // namespace seqan_ref
+
+extern "C" {
+
+// Up to max_count alignments: scores, pos = (H begin, H end, V begin, V end) source positions of
+// the clipped rows, rows = the two rows of each alignment as text lines.  Returns the count.
+int ref_local_enumerate(int32_t alphabet, int32_t blosum62, int32_t match, int32_t mismatch, int32_t gap_extend,
+                        int32_t gap_open, int32_t cutoff, const uint8_t * h, int64_t m, const uint8_t * v, int64_t n,
+                        int32_t max_count, int32_t * scores, int32_t * pos, char * out_rows, int64_t cap)
+{
+    if (alphabet == 1)
+    {
+        if (blosum62)
+        {
+            Score<int, ScoreMatrix<AminoAcid, ScoreSpecBlosum62>> sc(gap_extend, gap_open);
+            return seqan_ref::enumerate<AminoAcid>(sc, cutoff, h, m, v, n, max_count, scores, pos, out_rows, cap);
+        }
+        Score<int, Simple> sc(match, mismatch, gap_extend, gap_open);
+        return seqan_ref::enumerate<AminoAcid>(sc, cutoff, h, m, v, n, max_count, scores, pos, out_rows, cap);
+    }
+    Score<int, Simple> sc(match, mismatch, gap_extend, gap_open);
+    return seqan_ref::enumerate<Dna5>(sc, cutoff, h, m, v, n, max_count, scores, pos, out_rows, cap);
+}
+
+}  // extern "C"

@@ -1441,3 +1441,366 @@ int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const u
     free(off);
     return total;
 }
+
+/* ===================================================================================== */
+/* Waterman-Eggert suboptimal local alignments                                            */
+/* ===================================================================================== */
+
+/* The reference's binary heap (misc/priority_type_heap.h) of (score, matrix position) entries,
+ * ordered by score only (ScoreAndID::operator<, align/local_alignment_waterman_eggert_impl.h:
+ * 62-100): the maximum on top; ties fall where push / pop / adjustTop put them. */
+typedef struct { int32_t value; int64_t id; } we_entry;
+typedef struct { we_entry *a; int64_t n, cap; } we_heap;
+
+static void we_reserve(we_heap *hp, int64_t need)
+{
+    if (need <= hp->cap) return;
+    hp->cap = need > 2 * hp->cap ? need : 2 * hp->cap;
+    hp->a = (we_entry *)realloc(hp->a, sizeof(we_entry) * (size_t)hp->cap);
+}
+
+static void we_push(we_heap *hp, we_entry e)   /* push + _adjustHeapTowardRoot */
+{
+    int64_t h;
+    we_reserve(hp, hp->n + 1);
+    h = hp->n++;
+    while (h > 0) {
+        const int64_t i = (h - 1) / 2;
+        if (hp->a[i].value < e.value) { hp->a[h] = hp->a[i]; h = i; }
+        else break;
+    }
+    hp->a[h] = e;
+}
+
+static void we_toward_leaves(we_heap *hp, we_entry e, int64_t h, int64_t i)   /* _adjustHeapTowardLeaves */
+{
+    const int64_t n = hp->n;
+    while (i < n) {
+        if (e.value < hp->a[i].value) {
+            if (hp->a[i - 1].value < hp->a[i].value) { hp->a[h] = hp->a[i]; h = i; }
+            else { hp->a[h] = hp->a[i - 1]; h = i - 1; }
+        } else if (e.value < hp->a[i - 1].value) {
+            hp->a[h] = hp->a[i - 1]; h = i - 1;
+        } else {
+            break;
+        }
+        i = 2 * (h + 1);
+    }
+    if (i == n && e.value < hp->a[i - 1].value) { hp->a[h] = hp->a[i - 1]; h = i - 1; }
+    hp->a[h] = e;
+}
+
+static void we_pop(we_heap *hp)
+{
+    const we_entry e = hp->a[hp->n - 1];
+    hp->n -= 1;
+    if (hp->n > 0) we_toward_leaves(hp, e, 0, 2);
+}
+
+typedef struct {
+    const orc_we_params *p;
+    const uint8_t *h, *v;
+    int32_t m, n;
+    int64_t W;            /* row stride of the matrix: m + 1 (dimension 0 is H) */
+    int32_t *M;           /* (m + 1) x (n + 1) scores, position x + y * W */
+    uint8_t *F;           /* forbidden cells */
+    we_heap pq;
+    int64_t best_end;     /* bestEndPos */
+    int64_t best_begin;   /* bestBeginPos (where the last trace stopped) */
+    /* the last alignment: per trace step, the H / V source index or -1 (a gap) */
+    int32_t *stepH, *stepV;
+    int64_t T;            /* trace steps */
+    int64_t bH, bV;       /* first step of each row's clipped region */
+    int32_t x0, y0;       /* the trace's start cell: step t of the H row is view position x0 + t */
+    int32_t endH, endV;   /* clipped end source positions */
+} we_t;
+
+static int we_score(const we_t *w, int a, int b)
+{
+    if (w->p->matrix) return w->p->matrix[a * w->p->alphabet_size + b];
+    return a == b ? w->p->match : w->p->mismatch;
+}
+
+/* _smithWatermanGetMatrix (:112-175): the matrix from the sequence ends, every cell of value
+ * >= cutoff pushed. */
+static int32_t we_matrix(we_t *w)
+{
+    const int32_t gap = w->p->gap, cutoff = w->p->cutoff;
+    int32_t x, y;
+    for (x = 0; x <= w->m; ++x) w->M[x + (int64_t)w->n * w->W] = 0;
+    for (y = w->n - 1; y >= 0; --y) {
+        const int cy = w->v[y];
+        int32_t hh = 0, vv = 0;
+        w->M[w->m + (int64_t)y * w->W] = vv;
+        for (x = w->m - 1; x >= 0; --x) {
+            const int64_t f1 = x + (int64_t)y * w->W, f2 = f1 + w->W;
+            const int32_t cs = we_score(w, w->h[x], cy);
+            if (w->h[x] == cy) {
+                vv = hh + cs;
+                hh = w->M[f2];
+            } else {
+                const int32_t s1 = hh + cs;
+                int32_t s2;
+                hh = w->M[f2];
+                s2 = gap + (hh > vv ? hh : vv);
+                vv = s1 > s2 ? s1 : s2;
+                if (vv < 0) vv = 0;
+            }
+            w->M[f1] = vv;
+            if (vv >= cutoff) { we_entry e; e.value = vv; e.id = f1; we_push(&w->pq, e); }
+        }
+    }
+    if (w->pq.n > 0) {
+        w->best_end = w->pq.a[0].id;
+        return w->M[w->best_end];
+    }
+    return 0;
+}
+
+/* _smithWatermanTrace (:300-371): forward from src while the cell is non-zero and both sequences
+ * have residues left; a gap is inserted in the row that does not advance.  Records the steps and
+ * each row's clipped region (begin = the view position of its first residue, end = the view
+ * position after the last step). */
+static int64_t we_trace(we_t *w, int64_t src)
+{
+    const int32_t gap = w->p->gap;
+    int32_t i0 = (int32_t)(src % w->W), i1 = (int32_t)(src / w->W);
+    int64_t t = 0;
+    w->x0 = i0;
+    w->y0 = i1;
+    while (w->M[src] != 0 && i0 != w->m && i1 != w->n) {
+        const int forb = w->F[src];
+        int gv, gh;
+        if (w->h[i0] == w->v[i1] && !forb) {
+            gv = gh = 1;
+        } else {
+            const int32_t vr = w->M[src + 1] + gap;
+            const int32_t d = forb ? 0 : w->M[src + 1 + w->W] + we_score(w, w->h[i0], w->v[i1]);
+            const int32_t hd = w->M[src + w->W] + gap;
+            gv = (vr >= hd) | (d >= hd);
+            gh = (hd > vr) | (d >= vr);
+        }
+        w->stepH[t] = gv ? i0 : -1;
+        w->stepV[t] = gh ? i1 : -1;
+        if (gv) { ++i0; src += 1; }
+        if (gh) { ++i1; src += w->W; }
+        ++t;
+    }
+    w->T = t;
+    w->bH = 0;
+    while (w->bH < t && w->stepH[w->bH] < 0) ++w->bH;
+    w->bV = 0;
+    while (w->bV < t && w->stepV[w->bV] < 0) ++w->bV;
+    w->endH = i0;
+    w->endV = i1;
+    return src;
+}
+
+/* isGap of a row iterator at step index a (view positions before the trace's start are
+ * residues). */
+static int we_is_gap(const int32_t *step, int64_t a) { return a >= 0 && step[a] < 0; }
+
+/* _smithWatermanDeclump (:176-299): forbids the last alignment's residue pairs, walking it from
+ * its end, and recomputes the rows from the alignment's last V residue upwards, each from its
+ * right end leftwards until a recomputed cell left of every earlier stop keeps its value. */
+static int we_declump(we_t *w)
+{
+    const int32_t gap = w->p->gap;
+    int64_t a0 = w->T, a1 = w->T;
+    const int64_t s0 = w->bH, s1 = w->bV;
+    int64_t finger0, finger1, end_col, forb;
+    int32_t xe = w->endH - 1, ye = w->endV - 1, x_stop, y;
+    int different, forbidden_reached = 1, end_reached = 0, skip_row = 0;
+    finger0 = end_col = finger1 = forb = w->best_begin;
+    (void)finger1;
+    x_stop = xe;
+    for (y = ye; y != -1; --y) {
+        int32_t hh, vv, x;
+        int cy;
+        different = 1;
+        if (forbidden_reached && !end_reached) {
+            if (a0 == s0 && a1 == s1) end_reached = 1;
+            if (!end_reached) {
+                /* The walk stops only where both rows' clipped regions start; when they start at
+                 * different steps (an alignment whose first column is a gap) it runs on into the
+                 * rows' unaligned prefixes, and past their first view position the reference's
+                 * iterators (and its forbidden-cell write) leave their arrays: undefined. */
+#define WE_CHECK() do { if (w->x0 + a0 < 0 || w->y0 + a1 < 0 || forb < 0) return -1; } while (0)
+                --a0;
+                forb -= w->W;
+                WE_CHECK();
+                while (we_is_gap(w->stepH, a0) && a0 != s0) {
+                    skip_row = 1;
+                    --a0;
+                    --a1;
+                    forb -= w->W;
+                    WE_CHECK();
+                }
+                --a1;
+                forb -= 1;
+                WE_CHECK();
+                while (we_is_gap(w->stepV, a1) && a1 != s1) {
+                    --a1;
+                    --a0;
+                    forb -= 1;
+                    WE_CHECK();
+                }
+#undef WE_CHECK
+                w->F[forb] = 1;
+                forbidden_reached = 0;
+            }
+        }
+        cy = w->v[y];
+        hh = w->M[end_col];
+        finger1 = end_col;
+        end_col -= w->W;
+        finger0 = end_col;
+        vv = w->M[finger0];
+        x = xe;
+        while (x != -1 && different) {
+            int32_t cs;
+            --finger0;
+            --finger1;
+            cs = we_score(w, w->h[x], cy);
+            if (w->h[x] == cy && !w->F[finger0]) {
+                vv = hh + cs;
+                hh = w->M[finger1];
+            } else {
+                int32_t sa, sb;
+                if (finger0 == forb) {
+                    skip_row = 0;
+                    forbidden_reached = 1;
+                    sa = 0;
+                } else {
+                    sa = w->F[finger0] ? 0 : hh + cs;
+                }
+                hh = w->M[finger1];
+                sb = gap + (hh > vv ? hh : vv);
+                vv = sa > sb ? sa : sb;
+                if (vv < 0) vv = 0;
+            }
+            if (w->M[finger0] == vv) {
+                if (x < x_stop) {
+                    different = 0;
+                } else if (x == xe && ((!forbidden_reached && !skip_row) || end_reached)) {
+                    --xe;
+                    end_col -= 1;
+                }
+            }
+            if (x < x_stop) x_stop = x;
+            w->M[finger0] = vv;
+            --x;
+        }
+        if (xe == -1) break;
+    }
+    return 0;
+}
+
+/* _getNextBestEndPosition (:372-403): lazily refreshes the heap's top until its entry holds the
+ * cell's current score (dropping cells below cutoff); 0 (also a real position!) means none. */
+static int64_t we_next_end(we_t *w)
+{
+    int32_t top_score = 0;
+    if (w->pq.n > 0) top_score = w->M[w->pq.a[0].id];
+    if (w->pq.n > 0) {
+        while (w->pq.a[0].value != top_score) {
+            if (top_score >= w->p->cutoff) {
+                w->pq.a[0].value = top_score;
+                we_toward_leaves(&w->pq, w->pq.a[0], 0, 2);
+            } else {
+                we_pop(&w->pq);
+            }
+            if (w->pq.n > 0) top_score = w->M[w->pq.a[0].id];
+            else break;
+        }
+    }
+    if (w->pq.n == 0) return 0;
+    {
+        const int64_t ret = w->pq.a[0].id;
+        w->best_end = ret;
+        we_pop(&w->pq);
+        return ret;
+    }
+}
+
+int32_t orc_waterman_eggert(const orc_we_params *p, const uint8_t *h, int32_t m, const uint8_t *v, int32_t n,
+                            int32_t max_count, int32_t *scores, int32_t *begins, int32_t *ends,
+                            orc_segment *segs, int64_t seg_cap, int64_t *seg_off, int32_t *undefined_next)
+{
+    we_t w;
+    int32_t k = 0, ret = 0;
+    int64_t ns = 0;
+    if (seg_off) seg_off[0] = 0;
+    if (undefined_next) *undefined_next = 0;
+    if (m <= 0 || n <= 0 || max_count <= 0) return 0;
+    memset(&w, 0, sizeof(w));
+    w.p = p; w.h = h; w.v = v; w.m = m; w.n = n; w.W = (int64_t)m + 1;
+    w.M = (int32_t *)malloc(sizeof(int32_t) * (size_t)w.W * (size_t)(n + 1));
+    w.F = (uint8_t *)calloc((size_t)w.W * (size_t)(n + 1), 1);
+    w.stepH = (int32_t *)malloc(sizeof(int32_t) * (size_t)(m + n + 2));
+    w.stepV = (int32_t *)malloc(sizeof(int32_t) * (size_t)(m + n + 2));
+    for (k = 0; k < max_count; ++k) {
+        int32_t sc;
+        int64_t t, t0;
+        if (k == 0) {
+            /* _smithWaterman (:404-432) */
+            sc = we_matrix(&w);
+            if (sc == 0) break;
+            w.best_begin = we_trace(&w, w.pq.a[0].id);
+            we_pop(&w.pq);
+        } else {
+            /* _smithWatermanGetNext (:433-456) */
+            int64_t e;
+            if (we_declump(&w)) {
+                if (undefined_next) *undefined_next = 1;
+                break;
+            }
+            e = we_next_end(&w);
+            if (e == 0) break;
+            w.best_begin = we_trace(&w, e);
+            sc = w.M[e];
+            if (sc == 0) break;   /* nextLocalAlignment's bool */
+        }
+        scores[k] = w.M[w.best_end];
+        begins[2 * k] = w.bH < w.T ? w.stepH[w.bH] : w.endH;
+        begins[2 * k + 1] = w.bV < w.T ? w.stepV[w.bV] : w.endV;
+        ends[2 * k] = w.endH;
+        ends[2 * k + 1] = w.endV;
+        /* the columns as runs in alignment order, from the earlier of the two rows' begins */
+        t0 = w.bH < w.bV ? w.bH : w.bV;
+        for (t = t0; t < w.T;) {
+            const int type = (w.stepH[t] >= 0 && w.stepV[t] >= 0) ? ORC_SEG_DIAGONAL
+                             : (w.stepH[t] >= 0 ? ORC_SEG_HORIZONTAL : ORC_SEG_VERTICAL);
+            int64_t u = t + 1;
+            uint32_t hb = 0, vb = 0;
+            int64_t q;
+            while (u < w.T) {
+                const int ty = (w.stepH[u] >= 0 && w.stepV[u] >= 0) ? ORC_SEG_DIAGONAL
+                               : (w.stepH[u] >= 0 ? ORC_SEG_HORIZONTAL : ORC_SEG_VERTICAL);
+                if (ty != type) break;
+                ++u;
+            }
+            /* run start positions: the next residue of each row at step t */
+            for (q = t; q < w.T && w.stepH[q] < 0; ++q) {}
+            hb = (uint32_t)(q < w.T ? w.stepH[q] : w.endH);
+            for (q = t; q < w.T && w.stepV[q] < 0; ++q) {}
+            vb = (uint32_t)(q < w.T ? w.stepV[q] : w.endV);
+            if (ns >= seg_cap) { ret = -1; goto done; }
+            segs[ns].h_begin = hb;
+            segs[ns].v_begin = vb;
+            segs[ns].length = (uint32_t)(u - t);
+            segs[ns].type = (uint32_t)type;
+            ++ns;
+            t = u;
+        }
+        if (seg_off) seg_off[k + 1] = ns;
+    }
+    ret = k;
+done:
+    free(w.M);
+    free(w.F);
+    free(w.stepH);
+    free(w.stepV);
+    free(w.pq.a);
+    return ret;
+}

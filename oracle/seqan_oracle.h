@@ -155,6 +155,33 @@ int32_t orc_read_records(int32_t format, int32_t alphabet, const char *text, int
                          int64_t res_cap, uint8_t *codes, char *quals, int64_t *num, int64_t *residues,
                          int64_t *err_off);
 
+/* Waterman-Eggert suboptimal local alignments: the reference's LocalAlignmentEnumerator<Score,
+ * Unbanded> (align/local_alignment_enumeration_unbanded.h) driving _smithWaterman /
+ * _smithWatermanGetNext (align/local_alignment_waterman_eggert_impl.h).  Linear gaps (the
+ * scheme's gap extension score), the matrix filled from the sequence ends, every cell with a value
+ * of at least cutoff pushed on the reference's binary heap (misc/priority_type_heap.h), each
+ * alignment traced forward from the heap's current maximum, and the cells of the last alignment
+ * forbidden and their neighbourhood recomputed ("declumping") before the next.  Up to max_count
+ * alignments: scores[k] (the enumerator's getScore), begins[2k] / ends[2k] the clipped source
+ * begin / end in H, begins[2k+1] / ends[2k+1] in V, and the alignment columns as TraceSegment_-like
+ * runs in alignment order: segs[seg_off[k] .. seg_off[k+1]) of {h_begin, v_begin, length, type}.
+ * Returns the number of alignments (or -1 when seg_cap is too small).  *undefined_next is set
+ * when the enumeration stopped because the reference's next step is undefined: after an
+ * alignment whose first column is a gap its two rows start at different steps, the declumping
+ * walk back over it (which stops only where both rows start) runs on into the rows' unaligned
+ * prefixes, and when it passes their first position the reference's iterators leave their
+ * arrays. */
+typedef struct {
+    int32_t match, mismatch, gap;   /* Score<int, Simple>; gap = scoreGapExtend */
+    const int32_t *matrix;          /* alphabet_size^2 table (row = H residue) or NULL */
+    int32_t alphabet_size;
+    int32_t cutoff;
+} orc_we_params;
+
+int32_t orc_waterman_eggert(const orc_we_params *p, const uint8_t *h, int32_t m, const uint8_t *v, int32_t n,
+                            int32_t max_count, int32_t *scores, int32_t *begins, int32_t *ends,
+                            orc_segment *segs, int64_t seg_cap, int64_t *seg_off, int32_t *undefined_next);
+
 #ifdef __cplusplus
 }
 #endif
