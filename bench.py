@@ -62,6 +62,10 @@ WORKLOADS["extend_reads_250k"] = ("250000 read alignments: 150 bp reads (3% subs
                                   "extendAlignment EXTEND_BOTH, xDrop 20, Score<int,Simple>(2,-4,-1,-6); scores + "
                                   "trace segments of both sides")
 EXTEND_WORKLOADS = {"extend_reads_250k"}
+WORKLOADS["waterman_eggert_10k"] = ("10000 DNA pairs of 100-200 bp (half related: 10% subs, 2% indels), "
+                                    "LocalAlignmentEnumerator<Score<int,Simple>(2,-1,-2,-2), Unbanded>, cutoff 10, "
+                                    "up to 10 suboptimal local alignments per pair (scores, rows, positions)")
+WE_WORKLOADS = {"waterman_eggert_10k"}
 WORKLOADS["sam_records_1m"] = ("1000000 SAM records of read alignments: names read<k>, flag 0/16, one contig, "
                                "positions < 10^7, MAPQ 60, 1-3 CIGAR operations, 150 bp SEQ and QUAL; "
                                "BamAlignmentRecord -> SAM text as the reference's writer")
@@ -1206,6 +1210,145 @@ def run_extend_reference(args):
                               "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def we_pairs(n: int, seed: int):
+    """The Waterman-Eggert workload's pairs: 100-200 bp, every other one a mutated copy."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(seed))
+    H, V = [], []
+    for k in range(n):
+        h = rng.integers(0, 4, int(rng.integers(100, 201))).astype(np.uint8)
+        v = W.mutate(rng, h, 0.1, 0.02) if k % 2 else rng.integers(0, 4, int(rng.integers(100, 201))).astype(np.uint8)
+        H.append(h)
+        V.append(v)
+    return H, V
+
+
+WE_SCORE, WE_CUTOFF, WE_COUNT = (2, -1, -2), 10, 10
+
+
+def we_cpu_time(H, V, kind, lib=None):
+    """Seconds for the enumeration of every pair: the oracle ("port") or the compiled reference
+    ("reference", through lib), one pair after another, as the reference's enumerator runs."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    for h, v in zip(H, V):
+        if kind == "reference":
+            O.ref_local_enumerate(h, v, *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT, lib=lib)
+        else:
+            O.oracle_local_enumerate(h, v, *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT)
+    return time.perf_counter() - t0
+
+
+def run_we_bench(args, rank, world, local_rank, dist):
+    import seqan_gb300 as sg
+    from seqan_gb300 import _native as N
+    from seqan_gb300 import local_enum as LE
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    n = args.pairs or 10_000
+    H, V = we_pairs(n, 70 + rank)
+    cells = int(sum(len(h) * len(v) for h, v in zip(H, V)))
+    score = sg.Score(WE_SCORE[0], WE_SCORE[1], WE_SCORE[2], WE_SCORE[2])
+
+    def call():
+        return LE.local_enumerate(H, V, score, WE_CUTOFF, WE_COUNT, alphabet="dna5", context=ctx)
+
+    for _ in range(args.warmup):
+        out = call()
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    sampler.start()
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = call()
+        wall.append(time.perf_counter() - t0)
+        kern.append(ctx.stats().dp_kernel_ms)
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    st = ctx.stats()
+    kernel_ms = sum(kern) / len(kern)
+    value = n * world / (kernel_ms * 1e-3)
+    e2e = n * world * len(wall) / sum(wall)
+    alignments = sum(len(e.alignments) for e in out)
+    # parity: the first 300 pairs against the oracle
+    from oracle import oracle as O
+    parity = True
+    for k in range(min(n, 300)):
+        ref = O.oracle_local_enumerate(H[k], V[k], *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT)
+        und = bool(ref) and ref[-1] is None
+        ref = ref[:-1] if und else ref
+        if out[k].undefined_next != und or [(a.score, a.row0, a.row1, a.h_begin, a.h_end, a.v_begin, a.v_end)
+                                             for a in out[k].alignments] != \
+                [(a.score, a.row0, a.row1, a.h_begin, a.h_end, a.v_begin, a.v_end) for a in ref]:
+            parity = False
+            break
+    peak = C.c_double()
+    ctx.check(L.gba_measure_int_peak(ctx.handle, C.byref(peak)), "int peak")
+    # the initial fill alone: linear local, 6 ops per cell (two gap adds, diagonal add, two maxima,
+    # the zero floor); the heap, the traces and the declumping come on top
+    achieved = cells * OPS_PER_CELL["linear_local"] / (kernel_ms * 1e-3) / 1e12
+    line = {"metric": "pairs/s, Waterman-Eggert enumeration (LocalAlignmentEnumerator)", "value": value,
+            "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "pairs": n,
+                       "alignments_per_step": alignments, "cells_per_step": cells,
+                       "value_timing": "CUDA events around the enumeration kernel inside gba_local_enumerate "
+                                       "(inputs in HBM)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": int(sum(len(h) + len(v) for h, v in zip(H, V))),
+                    "d2h_bytes_per_step": int(alignments * 5 * 4 + sum(len(a.segments) for e in out
+                                                                       for a in e.alignments) * 16),
+                    "ms_per_step": 1e3 * sum(wall) / len(wall), "last_call_ms": st.call_ms},
+            "gpu_launches": args.steps * int(st.kernel_launches),
+            "roofline": {"bound": "latency", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "kernel": "k_waterman_eggert (one thread per pair: heap, forward traces and declumping "
+                                   "are sequential per pair) + k_enum_pack",
+                         "ops_per_cell": OPS_PER_CELL["linear_local"], "dp_kernel_ms": kernel_ms,
+                         "note": "achieved counts the initial matrix fill only",
+                         "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"},
+            "clocks": clocks, "parity_first_300_vs_oracle": parity}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        k = min(n, 1000)
+        t = we_cpu_time(H[:k], V[:k], "port")
+        line["cpu_baseline"] = {"value": k / t, "unit": "pairs/s", "cores": 1, "kind": "port",
+                                "sample": f"the first {k} pairs, the oracle's enumeration one pair after another",
+                                "seconds": t}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_we_reference(args):
+    from oracle import oracle as O
+    n = min(args.pairs or 10_000, 1000)
+    H, V = we_pairs(n, 70)
+    if O.ref_available():
+        lib = O.libref()
+    elif O.build_ref_bench():
+        lib = O.libref_bench()
+    else:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's headers are not on this host "
+                                                              "(baseline/_ref/include)"}), flush=True)
+        return
+    for _ in range(args.warmup):
+        we_cpu_time(H[:50], V[:50], "reference", lib)
+    times = [we_cpu_time(H, V, "reference", lib) for _ in range(args.steps)]
+    rate = n * len(times) / sum(times)
+    print(json.dumps({"metric": "pairs/s, Waterman-Eggert enumeration (LocalAlignmentEnumerator)", "value": rate,
+                      "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload, "pairs_per_step": n, "description": WORKLOADS[args.workload]},
+                      "cpu_baseline": {"value": rate, "unit": "pairs/s", "cores": 1, "kind": "reference",
+                                       "sample": f"{n} pairs per step through the compiled reference's "
+                                                 "LocalAlignmentEnumerator, one pair after another"},
+                      "e2e": {"value": rate, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 def serving_requests(n: int, seed: int):
     """Mixed-length affine DNA requests: 90% U[100,500], 9% U[1000,5000], 1% 10,000 bp; the
     partner has 5% substitutions and 1% indels."""
@@ -1304,6 +1447,9 @@ def main():
         elif args.workload in EXTEND_WORKLOADS:
             if rank == 0:
                 run_extend_reference(args)
+        elif args.workload in WE_WORKLOADS:
+            if rank == 0:
+                run_we_reference(args)
         elif args.workload in SEED_WORKLOADS:
             if rank == 0:
                 run_seed_reference(args)
@@ -1319,6 +1465,11 @@ def main():
         return
     if args.workload in EXTEND_WORKLOADS:
         run_extend_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in WE_WORKLOADS:
+        run_we_bench(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
         return

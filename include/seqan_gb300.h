@@ -471,6 +471,43 @@ GBA_API int gba_extend_alignments(gba_context *ctx, const gba_extend_align_param
                                   const gba_seed_batch *batch, const gba_seed *seeds,
                                   gba_extend_align_result *result);
 
+/* --- Suboptimal local alignments (Waterman-Eggert) --------------------------------------------
+ * The reference's LocalAlignmentEnumerator<Score, Unbanded> driven by nextLocalAlignment until it
+ * returns false or max_count alignments were taken (align/local_alignment_enumeration_unbanded.h,
+ * align/local_alignment_waterman_eggert_impl.h), for every pair of a batch: linear gaps (gap =
+ * the scheme's gap extension score), the score matrix filled from the sequence ends, each
+ * alignment traced forward from the largest remaining score, its residue pairs forbidden and the
+ * matrix declumped before the next.  Pair k's alignment i (i < count[k]) has score
+ * score[k * max_count + i] (getScore), clipped source positions [begin_h, end_h) / [begin_v,
+ * end_v), and its columns as runs in alignment order in segments[segment_offsets[k * max_count +
+ * i] .. segment_offsets[k * max_count + i + 1]) ({h_begin, v_begin, length, type}: a run starts at
+ * the next residue of each row; the two rows of an alignment whose first column is a gap start
+ * at different columns, each at its first residue, as the reference's rows do).  status[k] =
+ * GBA_ENUM_UNDEFINED_NEXT when the enumeration stopped because the reference's next step is
+ * undefined (after an alignment whose first column is a gap, its declumping walk runs past the
+ * rows' first positions). */
+typedef struct {
+    int32_t match, mismatch;   /* Score<int, Simple> (ignored with a matrix) */
+    int32_t gap;               /* scoreGapExtend: every gap column costs this */
+    int32_t cutoff;            /* the enumerator's cutoff: cells below it never become alignment ends */
+    const int32_t *matrix;     /* optional host alphabet_size^2 table (row = H residue) */
+    int32_t alphabet_size;     /* 1..32 with a matrix */
+    int32_t max_count;         /* alignments per pair, 1..65536 */
+} gba_enum_params;
+
+enum { GBA_ENUM_DONE = 0, GBA_ENUM_UNDEFINED_NEXT = 1 };
+
+typedef struct {
+    int32_t *count, *status;                        /* [num_pairs] */
+    int32_t *score, *begin_h, *end_h, *begin_v, *end_v;   /* [num_pairs * max_count] */
+    gba_segment *segments;
+    int64_t segment_capacity;
+    int64_t *segment_offsets;                       /* [num_pairs * max_count + 1] */
+} gba_enum_result;
+
+GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params, const gba_batch *batch,
+                                gba_enum_result *result);
+
 /* --- Packed input ---------------------------------------------------------------------------
  * String<TValue, Packed<>> (sequence/string_packed.h) as the engine's input, uploaded as is: the
  * host string of a packed string is a 64-bit length word followed by data words, each holding

@@ -690,9 +690,10 @@ def oracle_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, matrix=
 
 
 def ref_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, blosum62=False, alphabet="dna",
-                        max_count=1000) -> list:
-    """The reference's LocalAlignmentEnumerator (oracle/ref/units/waterman_eggert.cpp)."""
-    lib = libref()
+                        max_count=1000, lib=None) -> list:
+    """The reference's LocalAlignmentEnumerator (oracle/ref/units/waterman_eggert.cpp); lib: the
+    library to call (default libref(); libref_bench() holds the same entry)."""
+    lib = lib or libref()
     lib.ref_local_enumerate.argtypes = [C.c_int32] * 7 + [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int32,
                                                           C.c_void_p, C.c_void_p, C.c_char_p, C.c_int64]
     h = np.ascontiguousarray(h, dtype=np.uint8)

@@ -136,6 +136,20 @@ class GbaExtendAlignParams(C.Structure):
                 ("band_lower", C.c_int32), ("band_upper", C.c_int32)]
 
 
+class GbaEnumParams(C.Structure):
+    _fields_ = [("match", C.c_int32), ("mismatch", C.c_int32), ("gap", C.c_int32), ("cutoff", C.c_int32),
+                ("matrix", C.c_void_p), ("alphabet_size", C.c_int32), ("max_count", C.c_int32)]
+
+
+class GbaEnumResult(C.Structure):
+    _fields_ = [("count", C.c_void_p), ("status", C.c_void_p), ("score", C.c_void_p), ("begin_h", C.c_void_p),
+                ("end_h", C.c_void_p), ("begin_v", C.c_void_p), ("end_v", C.c_void_p), ("segments", C.c_void_p),
+                ("segment_capacity", C.c_int64), ("segment_offsets", C.c_void_p)]
+
+
+GBA_ENUM_DONE, GBA_ENUM_UNDEFINED_NEXT = 0, 1
+
+
 class GbaExtendAlignResult(C.Structure):
     _fields_ = [("left_score", C.c_void_p), ("right_score", C.c_void_p), ("segments", C.c_void_p),
                 ("segment_capacity", C.c_int64), ("segment_offsets", C.c_void_p)]
@@ -252,6 +266,8 @@ def lib():
             L.gba_extend_seeds_device.argtypes = [vp, C.POINTER(GbaExtendParams), C.POINTER(GbaSeedBatch), vp, vp]
             L.gba_extend_alignments.argtypes = [vp, C.POINTER(GbaExtendAlignParams), C.POINTER(GbaSeedBatch), vp,
                                                 C.POINTER(GbaExtendAlignResult)]
+            L.gba_local_enumerate.argtypes = [vp, C.POINTER(GbaEnumParams), C.POINTER(GbaBatch),
+                                              C.POINTER(GbaEnumResult)]
             L.gba_align_packed.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaPackedSet),
                                            C.POINTER(GbaPackedSet), C.c_int32, C.POINTER(GbaResult)]
             L.gba_format_sam.argtypes = [vp, C.POINTER(GbaSamRecords), vp, i64, vp]

@@ -221,6 +221,7 @@ struct gba_context {
     std::map<std::pair<const void *, size_t>, int64_t> xs_grid;   // (kernel, smem) -> resident blocks
     // alignment extension: tasks, per-task results, trace, segments, scratch
     DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next, xa_packoff, xa_packed;
+    DevBuf en_pairs, en_mat, en_forb, en_heap, en_steps, en_slots, en_out, en_dense, en_offs, en_cnt;   // gba_local_enumerate
     // packed input: the codes are already in seq_h / seq_v (gba_align_packed unpacked them)
     bool device_codes = false;
     DevBuf pk_words, pk_off_h, pk_off_v;
@@ -2175,6 +2176,7 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 #include "server.cuh"
 #include "seeds_host.cuh"
 #include "extend_host.cuh"
+#include "enum_host.cuh"
 #include "packed_host.cuh"
 #include "sam_host.cuh"
 #include "seqio_host.cuh"
