@@ -66,6 +66,12 @@ WORKLOADS["waterman_eggert_10k"] = ("10000 DNA pairs of 100-200 bp (half related
                                     "LocalAlignmentEnumerator<Score<int,Simple>(2,-1,-2,-2), Unbanded>, cutoff 10, "
                                     "up to 10 suboptimal local alignments per pair (scores, rows, positions)")
 WE_WORKLOADS = {"waterman_eggert_10k"}
+WORKLOADS["banded_chain_20k"] = ("20000 genomic pairs of 1-3 kbp (5% subs, 1% indels) with LAGAN-style anchor chains (the "
+                                 "exact matches of >= 20 bp on the true alignment, at most 64 per pair, 35 on average), "
+                                 "bandedChainAlignment(align, chain, Score<int,Simple>(2,-3,-1,-5), AlignConfig<>(), 15): "
+                                 "score + trace segments (the Align rows) per pair")
+CHAIN_WORKLOADS = {"banded_chain_20k"}
+CHAIN_SCORE, CHAIN_K = (2, -3, -1, -5), 15
 WORKLOADS["sam_records_1m"] = ("1000000 SAM records of read alignments: names read<k>, flag 0/16, one contig, "
                                "positions < 10^7, MAPQ 60, 1-3 CIGAR operations, 150 bp SEQ and QUAL; "
                                "BamAlignmentRecord -> SAM text as the reference's writer")
@@ -1349,6 +1355,146 @@ def run_we_reference(args):
           flush=True)
 
 
+def chain_data(n: int, seed: int):
+    from seqan_gb300 import workloads as W
+    return W.chain_pairs(n, 1000, 3000, seed=seed)
+
+
+def run_chain_bench(args, rank, world, local_rank, dist):
+    import seqan_gb300 as sg
+    from seqan_gb300 import _native as N
+    from seqan_gb300.banded_chain import banded_chain_codes
+    N.build()
+    L = N.lib()
+    ctx = N.Context(local_rank)
+    n = args.pairs or 20_000
+    H, V, chains = chain_data(n, 90 + rank)
+    sc = sg.Score(*CHAIN_SCORE)
+
+    def call():
+        return banded_chain_codes(H, V, chains, sc, sc, None, CHAIN_K, context=ctx)
+
+    for _ in range(max(args.warmup, 1)):
+        out = call()
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    sampler.start()
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = call()
+        wall.append(time.perf_counter() - t0)
+        kern.append(ctx.stats().dp_kernel_ms)
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    st = ctx.stats()
+    kernel_ms = sum(kern) / len(kern)
+    value = n * world / (kernel_ms * 1e-3)
+    e2e = n * world * len(wall) / sum(wall)
+    score, status, ntr, segs = out
+    cells = int(st.cells)
+    parity = None
+    if not args.no_parity:
+        from oracle import oracle as O
+        parity = True
+        for k in range(min(n, 300)):
+            o = O.oracle_banded_chain(H[k], V[k], chains[k], CHAIN_SCORE, CHAIN_SCORE, 0, CHAIN_K)
+            if (int(status[k]), int(score[k]), int(ntr[k]), segs[k]) != (o.status, o.score, o.n_traces, o.segments):
+                parity = False
+                break
+    peak = C.c_double()
+    ctx.check(L.gba_measure_int_peak(ctx.handle, C.byref(peak)), "int peak")
+    achieved = cells * OPS_PER_CELL["affine_global"] / (kernel_ms * 1e-3) / 1e12
+    line = {"metric": "pairs/s, banded chain alignment (bandedChainAlignment)", "value": value, "unit": "pairs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "pairs": n,
+                       "seeds": int(sum(len(c) for c in chains)), "cells_per_step": cells,
+                       "gcups": cells / (kernel_ms * 1e-3) / 1e9, "trace_bytes_per_step": int(st.trace_bytes),
+                       "l2": "not flushed: each step's scratch (trace matrices, score columns, traces; several GB) "
+                             "is far larger than L2",
+                       "value_timing": "CUDA events around k_banded_chain inside gba_banded_chain (inputs in HBM)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "pairs/s",
+                    "h2d_bytes_per_step": int(sum(len(h) + len(v) for h, v in zip(H, V)) +
+                                              16 * sum(len(c) for c in chains)),
+                    "d2h_bytes_per_step": int(12 * n + 16 * sum(len(x) for x in segs)),
+                    "ms_per_step": 1e3 * sum(wall) / len(wall), "last_call_ms": st.call_ms},
+            "gpu_launches": args.steps * int(st.kernel_launches),
+            "roofline": {"bound": "latency", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
+                         "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                         "kernel": "k_banded_chain (one thread per chain: its grids, tracebacks and glue in order) "
+                                   "+ k_chain_pack",
+                         "ops_per_cell": OPS_PER_CELL["affine_global"], "dp_kernel_ms": kernel_ms,
+                         "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"},
+            "clocks": clocks, "parity_first_300_vs_oracle": parity,
+            "statuses": {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))}}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        k = min(n, 2000)
+        t0 = time.perf_counter()
+        for q in range(k):
+            O.oracle_banded_chain(H[q], V[q], chains[q], CHAIN_SCORE, CHAIN_SCORE, 0, CHAIN_K)
+        t = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": k / t, "unit": "pairs/s", "cores": 1, "kind": "port",
+                                "sample": f"the first {k} pairs, the oracle's banded chain alignment one pair after "
+                                          "another", "seconds": t}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_chain_reference(args):
+    from oracle import oracle as O
+    n = min(args.pairs or 20_000, 4000)
+    H, V, chains = chain_data(n, 90)
+    if O.ref_available():
+        lib = O.libref()
+    elif O.build_ref_bench():
+        lib = O.libref_bench()
+    else:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's headers are not on this host "
+                                                              "(baseline/_ref/include)"}), flush=True)
+        return
+    lib.ref_banded_chain_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_int32]
+    sh, oh = O.concat(H)
+    sv, ov = O.concat(V)
+    so = np.zeros(n + 1, np.int64)
+    np.cumsum([len(c) for c in chains], out=so[1:])
+    seeds = np.ascontiguousarray(np.concatenate(chains + [np.zeros((1, 4), np.int32)]), dtype=np.int32)
+    a = np.array(CHAIN_SCORE, np.int32)
+    score = np.zeros(n, np.int32)
+    status = np.zeros(n, np.int32)
+    threads = os.cpu_count() or 1
+
+    def step(k):
+        lib.ref_banded_chain_batch(a.ctypes.data, a.ctypes.data, 0, CHAIN_K, k, sh.ctypes.data, oh.ctypes.data,
+                                   sv.ctypes.data, ov.ctypes.data, seeds.ctypes.data, so.ctypes.data,
+                                   score.ctypes.data, status.ctypes.data, threads)
+
+    for _ in range(args.warmup):
+        step(min(n, 200))
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step(n)
+        times.append(time.perf_counter() - t0)
+    rate = n * len(times) / sum(times)
+    print(json.dumps({"metric": "pairs/s, banded chain alignment (bandedChainAlignment)", "value": rate,
+                      "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload, "pairs_per_step": n, "description": WORKLOADS[args.workload]},
+                      "cpu_baseline": {"value": rate, "unit": "pairs/s", "cores": threads, "kind": "reference",
+                                       "sample": f"the first {n} pairs of the workload per step through the compiled "
+                                                 f"reference's bandedChainAlignment, {threads} OpenMP threads"},
+                      "e2e": {"value": rate, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 def serving_requests(n: int, seed: int):
     """Mixed-length affine DNA requests: 90% U[100,500], 9% U[1000,5000], 1% 10,000 bp; the
     partner has 5% substitutions and 1% indels."""
@@ -1450,6 +1596,9 @@ def main():
         elif args.workload in WE_WORKLOADS:
             if rank == 0:
                 run_we_reference(args)
+        elif args.workload in CHAIN_WORKLOADS:
+            if rank == 0:
+                run_chain_reference(args)
         elif args.workload in SEED_WORKLOADS:
             if rank == 0:
                 run_seed_reference(args)
@@ -1470,6 +1619,11 @@ def main():
         return
     if args.workload in WE_WORKLOADS:
         run_we_bench(args, rank, world, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.workload in CHAIN_WORKLOADS:
+        run_chain_bench(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
         return

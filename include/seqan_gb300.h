@@ -508,6 +508,48 @@ typedef struct {
 GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params, const gba_batch *batch,
                                 gba_enum_result *result);
 
+/* --- Banded chain alignment ------------------------------------------------------------------
+ * bandedChainAlignment(align, seedChain, scoreAnchor, scoreGap, AlignConfig, bandExtension)
+ * (seeds/banded_chain_alignment.h:184-214) for every pair of a batch, each with its own seed
+ * chain: the rectangle before the first anchor, a band of the anchor's diagonals widened by
+ * bandExtension around each anchor and the rectangle to the next one, and the rectangle to the
+ * matrix end, each grid started from the cells the previous grid's traceback reached; linear or
+ * affine gaps (affine when either scheme's gap open differs from its gap extension).  Per pair:
+ * the score (numeric_limits<int>::min() for an empty chain), the first trace of the reference's
+ * trace set as TraceSegment_ runs in the reference's order (the rows _adaptTraceSegmentsTo builds
+ * from them), and how many co-optimal traces the set held.  status[k]: GBA_CHAIN_NO_GLUE where
+ * the reference throws std::logic_error (two grids' traces share no cell); GBA_CHAIN_UNDEFINED
+ * where its behaviour is undefined (a grid past the sequences, an index past its vectors);
+ * GBA_CHAIN_CAPACITY when more than max_traces co-optimal traces were open at once. */
+typedef struct {
+    int32_t match, mismatch, gap_extend, gap_open;   /* Score<int, Simple>(match, mismatch, ext, open) */
+} gba_simple_score;
+
+typedef struct {
+    gba_simple_score anchor;   /* scores in the bands around the anchors */
+    gba_simple_score gap;      /* scores in the rectangles between them */
+    int32_t free_ends;         /* GBA_FREE_* (AlignConfig<TOP, LEFT, RIGHT, BOTTOM>) */
+    int32_t band_extension;    /* >= 1; the reference's default is 15 */
+    int32_t max_traces;        /* co-optimal traces kept per pair, 1..32 (0: 8) */
+} gba_chain_params;
+
+typedef struct {
+    const int32_t *seeds;            /* host: 4 per seed (beginH, beginV, endH, endV of Seed<Simple>) */
+    const int64_t *seed_offsets;     /* num_pairs + 1: pair k's chain is seeds [off[k], off[k+1]) */
+} gba_chain_seeds;
+
+enum { GBA_CHAIN_OK = 0, GBA_CHAIN_NO_GLUE = 1, GBA_CHAIN_UNDEFINED = 2, GBA_CHAIN_CAPACITY = 3 };
+
+typedef struct {
+    int32_t *score, *status, *num_traces;   /* [num_pairs] */
+    gba_segment *segments;                  /* pair k: segments[segment_offsets[k] .. [k+1]) */
+    int64_t segment_capacity;
+    int64_t *segment_offsets;               /* [num_pairs + 1] */
+} gba_chain_result;
+
+GBA_API int gba_banded_chain(gba_context *ctx, const gba_chain_params *params, const gba_batch *batch,
+                             const gba_chain_seeds *seeds, gba_chain_result *result);
+
 /* --- Packed input ---------------------------------------------------------------------------
  * String<TValue, Packed<>> (sequence/string_packed.h) as the engine's input, uploaded as is: the
  * host string of a packed string is a 64-bit length word followed by data words, each holding

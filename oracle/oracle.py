@@ -84,12 +84,16 @@ class Problem:
         return self.gap_open != self.gap_extend
 
 
+ORACLE_SOURCES = ("seqan_oracle.c", "banded_chain_oracle.c")
+
+
 def _compile_oracle(force: bool = False) -> str:
-    src = os.path.join(HERE, "seqan_oracle.c")
-    if force or not os.path.exists(ORACLE_LIB) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, s) for s in ORACLE_SOURCES]
+    newest = max(os.path.getmtime(s) for s in srcs + [os.path.join(HERE, "seqan_oracle.h")])
+    if force or not os.path.exists(ORACLE_LIB) or os.path.getmtime(ORACLE_LIB) < newest:
         os.makedirs(BUILD, exist_ok=True)
         tmp = ORACLE_LIB + f".tmp{os.getpid()}"
-        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-o", tmp, src])
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-shared", "-fPIC", "-o", tmp] + srcs)
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 
@@ -990,3 +994,78 @@ def ref_iupac_table():
     t = np.zeros(256, np.uint8)
     lib.ref_iupac_table(_ptr(t))
     return t
+
+
+# ---------------------------------------------------------------------------------------------
+# Banded chain alignment (seeds/banded_chain_alignment.h:184-214).
+# ---------------------------------------------------------------------------------------------
+
+class OrcSimpleScore(C.Structure):
+    _fields_ = [("match", C.c_int32), ("mismatch", C.c_int32), ("gap_extend", C.c_int32), ("gap_open", C.c_int32)]
+
+
+class OrcChainParams(C.Structure):
+    _fields_ = [("anchor", OrcSimpleScore), ("gap", OrcSimpleScore), ("free_ends", C.c_int32),
+                ("band_extension", C.c_int32)]
+
+
+@dataclass
+class ChainResult:
+    status: int            # 0 ok, 1 the reference throws (no glue point), 2 undefined in the reference
+    score: int
+    segments: list         # TraceSegment_ runs (h, v, length, type) in the reference's order
+    n_traces: int
+    rows: tuple | None = None
+
+
+def _chain_seeds(seeds):
+    return np.ascontiguousarray(np.asarray(seeds, dtype=np.int32).reshape(-1, 4))
+
+
+def oracle_banded_chain(h, v, seeds, anchor, gap=None, free_ends=0, k=15) -> ChainResult:
+    """The restatement (oracle/banded_chain_oracle.c).  anchor / gap: (match, mismatch, gap_extend,
+    gap_open); seeds: (beginH, beginV, endH, endV) per seed in chain order."""
+    lib = liboracle()
+    lib.orc_banded_chain.argtypes = [C.POINTER(OrcChainParams), C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                     C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                     C.c_void_p]
+    gap = gap or anchor
+    p = OrcChainParams(OrcSimpleScore(*anchor), OrcSimpleScore(*gap), free_ends, k)
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    sd = _chain_seeds(seeds)
+    cap = 4 * (len(h) + len(v)) + 64
+    segs = np.zeros((cap, 4), np.uint32)
+    out = np.zeros(3, np.int32)
+    rc = lib.orc_banded_chain(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), len(sd), _ptr(sd), _ptr(out[0:]),
+                              _ptr(segs), cap, _ptr(out[1:]), _ptr(out[2:]))
+    if rc < 0:
+        raise RuntimeError("segment buffer too small")
+    return ChainResult(int(rc), int(out[0]), [tuple(int(x) for x in s) for s in segs[:out[1]]], int(out[2]))
+
+
+def ref_banded_chain(h, v, seeds, anchor, gap=None, free_ends=0, k=15, lib=None) -> ChainResult:
+    """The reference's bandedChainAlignment (oracle/ref/units/banded_chain.cpp): score, the first
+    trace of its trace set, the number of traces and the Align rows it prints."""
+    lib = lib or libref()
+    lib.ref_banded_chain.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                     C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_int32, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int64]
+    gap = gap or anchor
+    a = np.asarray(anchor, np.int32)
+    g = np.asarray(gap, np.int32)
+    h = np.ascontiguousarray(h, dtype=np.uint8)
+    v = np.ascontiguousarray(v, dtype=np.uint8)
+    sd = _chain_seeds(seeds)
+    cap = 4 * (len(h) + len(v)) + 64
+    segs = np.zeros((cap, 4), np.uint32)
+    out = np.zeros(3, np.int32)
+    tcap = 4 * (len(h) + len(v)) + 16
+    rows = C.create_string_buffer(tcap)
+    rc = lib.ref_banded_chain(_ptr(a), _ptr(g), free_ends, k, _ptr(h), len(h), _ptr(v), len(v), len(sd), _ptr(sd),
+                              _ptr(out[0:]), _ptr(segs), cap, _ptr(out[1:]), _ptr(out[2:]), rows, tcap)
+    if rc < 0:
+        raise RuntimeError(f"ref_banded_chain failed ({rc})")
+    r = rows.value.decode().split("\n")
+    return ChainResult(int(rc), int(out[0]), [tuple(int(x) for x in s) for s in segs[:out[1]]], int(out[2]),
+                       (r[0], r[1]) if rc == 0 else None)

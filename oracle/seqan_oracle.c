@@ -48,6 +48,7 @@ typedef struct {
     int inf;
     int local;
     int extend;     /* AlignExtend_: every cell tracked, no zero floor */
+    int complete;   /* CompleteTrace: ties keep every source's trace bits (dp_formula.h:205-220) */
     int affine;
     int dynamic;    /* DynamicGaps: one score and two gap-extension flags per cell */
     int ext, open;
@@ -67,9 +68,11 @@ static inline int sub_score(const ctx_t *c, uint8_t hv, uint8_t vv)
     return hv == vv ? c->match : c->mismatch;
 }
 
-/* _maxScore with SingleTrace: the left operand wins ties (align/dp_formula.h:171-182). */
+/* _maxScore with SingleTrace: the left operand wins ties (align/dp_formula.h:171-182); with
+ * CompleteTrace a tie keeps the left value and the union of both traces (:205-220). */
 #define MAXTL(target, tv, left, right, tl, tr) \
     do { if ((left) < (right)) { (target) = (right); (tv) = (tr); } \
+         else if (c->complete && (left) == (right)) { (target) = (left); (tv) = (tl) | (tr); } \
          else { (target) = (left); (tv) = (tl); } } while (0)
 
 /* Per-column caches and the one sparse column (align/dp_matrix.h:137-147). */
@@ -786,10 +789,10 @@ uint8_t orc_trace4_decode(uint8_t code, int32_t affine)
     return (uint8_t)(src_bits[src] | ((code & 4) ? TV_HO : TV_H) | ((code & 8) ? TV_VO : TV_V));
 }
 
-int orc_align_pair(const orc_params *p,
-                   const uint8_t *h, int32_t m,
-                   const uint8_t *v, int32_t n,
-                   orc_result *out, orc_segment *segs, int32_t seg_cap)
+static int align_pair_impl(const orc_params *p, int complete,
+                           const uint8_t *h, int32_t m,
+                           const uint8_t *v, int32_t n,
+                           orc_result *out, orc_segment *segs, int32_t seg_cap)
 {
     ctx_t c;
     int fe;
@@ -802,6 +805,7 @@ int orc_align_pair(const orc_params *p,
     c.inf = c.bits16 ? -16384 : -(1 << 30);
     c.local = (p->mode == ORC_LOCAL);
     c.extend = (p->mode == ORC_EXTEND);
+    c.complete = complete;
     c.affine = (p->gap_model == ORC_AFFINE);
     c.dynamic = (p->gap_model == ORC_DYNAMIC);
     c.ext = p->gap_extend;
@@ -850,7 +854,9 @@ int orc_align_pair(const orc_params *p,
         }
         /* _correctTraceValue (align/dp_algorithm_impl.h:1188-1205) for affine cells; for DynamicGaps
          * cells the best cell's flags decide (:1235-1249; the scout keeps the flags in b.e). */
-        if (c.affine) {
+        if (c.complete) {
+            /* CompleteTrace: _finishAlignment corrects no trace value (dp_algorithm_impl.h:1352). */
+        } else if (c.affine) {
             if (b.f == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFV; }
             else if (b.e == b.s) { *cell &= (uint8_t)~TV_DIAG; *cell |= TV_MFH; }
         } else if (c.dynamic) {
@@ -871,6 +877,22 @@ int orc_align_pair(const orc_params *p,
     }
     free(colS);
     return 0;
+}
+
+int orc_align_pair(const orc_params *p,
+                   const uint8_t *h, int32_t m,
+                   const uint8_t *v, int32_t n,
+                   orc_result *out, orc_segment *segs, int32_t seg_cap)
+{
+    return align_pair_impl(p, 0, h, m, v, n, out, segs, seg_cap);
+}
+
+int orc_align_pair_complete(const orc_params *p,
+                            const uint8_t *h, int32_t m,
+                            const uint8_t *v, int32_t n,
+                            orc_result *out, orc_segment *segs, int32_t seg_cap)
+{
+    return align_pair_impl(p, 1, h, m, v, n, out, segs, seg_cap);
 }
 
 int orc_align_batch(const orc_params *p, int64_t n_pairs,

@@ -182,6 +182,36 @@ int32_t orc_waterman_eggert(const orc_we_params *p, const uint8_t *h, int32_t m,
                             int32_t max_count, int32_t *scores, int32_t *begins, int32_t *ends,
                             orc_segment *segs, int64_t seg_cap, int64_t *seg_off, int32_t *undefined_next);
 
+/* orc_align_pair with CompleteTrace (ties keep the trace bits of every source, no start-cell
+ * correction): the DP of a banded chain's grid that spans the whole matrix. */
+int orc_align_pair_complete(const orc_params *p,
+                            const uint8_t *h, int32_t m,
+                            const uint8_t *v, int32_t n,
+                            orc_result *out, orc_segment *segs, int32_t seg_cap);
+
+/* Banded chain alignment (bandedChainAlignment, seeds/banded_chain_alignment.h:184-214;
+ * banded_chain_oracle.c).  Two Score<int, Simple> schemes -- the anchors' and the
+ * gaps' -- the AlignConfig free-end bits and the band extension k.  seeds: n_seeds x (beginH,
+ * beginV, endH, endV) of Seed<Simple> in chain order.  Outputs: the score (numeric min for an
+ * empty chain), the first trace of the reference's trace set as TraceSegment_ runs (type =
+ * 1 diagonal, 2 horizontal, 4 vertical) in the reference's order, and the number of traces.
+ * Returns 0; 1 where the reference throws (no glue point between two grids' traces); 2 where its
+ * behaviour is undefined (a grid or an index past its sequences or vectors); -1 when the trace
+ * does not fit seg_cap. */
+typedef struct {
+    int32_t match, mismatch, gap_extend, gap_open;
+} orc_simple_score;
+
+typedef struct {
+    orc_simple_score anchor, gap;
+    int32_t free_ends;        /* ORC_FREE_* */
+    int32_t band_extension;   /* k >= 1 */
+} orc_chain_params;
+
+int32_t orc_banded_chain(const orc_chain_params *p, const uint8_t *h, int32_t m, const uint8_t *v, int32_t n,
+                         int32_t n_seeds, const int32_t *seeds, int32_t *score, orc_segment *segs,
+                         int32_t seg_cap, int32_t *n_segs, int32_t *n_traces);
+
 #ifdef __cplusplus
 }
 #endif

@@ -150,6 +150,27 @@ class GbaEnumResult(C.Structure):
 GBA_ENUM_DONE, GBA_ENUM_UNDEFINED_NEXT = 0, 1
 
 
+class GbaSimpleScore(C.Structure):
+    _fields_ = [("match", C.c_int32), ("mismatch", C.c_int32), ("gap_extend", C.c_int32), ("gap_open", C.c_int32)]
+
+
+class GbaChainParams(C.Structure):
+    _fields_ = [("anchor", GbaSimpleScore), ("gap", GbaSimpleScore), ("free_ends", C.c_int32),
+                ("band_extension", C.c_int32), ("max_traces", C.c_int32)]
+
+
+class GbaChainSeeds(C.Structure):
+    _fields_ = [("seeds", C.c_void_p), ("seed_offsets", C.c_void_p)]
+
+
+class GbaChainResult(C.Structure):
+    _fields_ = [("score", C.c_void_p), ("status", C.c_void_p), ("num_traces", C.c_void_p), ("segments", C.c_void_p),
+                ("segment_capacity", C.c_int64), ("segment_offsets", C.c_void_p)]
+
+
+GBA_CHAIN_OK, GBA_CHAIN_NO_GLUE, GBA_CHAIN_UNDEFINED, GBA_CHAIN_CAPACITY = 0, 1, 2, 3
+
+
 class GbaExtendAlignResult(C.Structure):
     _fields_ = [("left_score", C.c_void_p), ("right_score", C.c_void_p), ("segments", C.c_void_p),
                 ("segment_capacity", C.c_int64), ("segment_offsets", C.c_void_p)]
@@ -268,6 +289,8 @@ def lib():
                                                 C.POINTER(GbaExtendAlignResult)]
             L.gba_local_enumerate.argtypes = [vp, C.POINTER(GbaEnumParams), C.POINTER(GbaBatch),
                                               C.POINTER(GbaEnumResult)]
+            L.gba_banded_chain.argtypes = [vp, C.POINTER(GbaChainParams), C.POINTER(GbaBatch),
+                                           C.POINTER(GbaChainSeeds), C.POINTER(GbaChainResult)]
             L.gba_align_packed.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaPackedSet),
                                            C.POINTER(GbaPackedSet), C.c_int32, C.POINTER(GbaResult)]
             L.gba_format_sam.argtypes = [vp, C.POINTER(GbaSamRecords), vp, i64, vp]

@@ -12,7 +12,6 @@ extension score.
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -20,22 +19,50 @@ from . import _native as N
 from .alphabet import decode, encode
 
 
-@dataclass
 class LocalAlignment:
-    score: int
-    row0: str
-    row1: str
-    h_begin: int
-    h_end: int
-    v_begin: int
-    v_end: int
-    segments: list = field(default_factory=list)   # runs in alignment order (h, v, length, type)
+    """One suboptimal local alignment: the enumerator's score, the clipped source positions and
+    the alignment's columns as runs (h, v, length, type) in alignment order.  The two gapped rows
+    (``row0`` / ``row1``, as the reference prints them) are rendered on first access."""
+    __slots__ = ("score", "h_begin", "h_end", "v_begin", "v_end", "segments", "_texts", "_rows")
+
+    def __init__(self, score, h_begin, h_end, v_begin, v_end, segments, texts):
+        self.score, self.h_begin, self.h_end, self.v_begin, self.v_end = score, h_begin, h_end, v_begin, v_end
+        self.segments = segments
+        self._texts = texts          # (H text, V text) or a callable giving them
+        self._rows = None
+
+    def _render(self):
+        if self._rows is None:
+            t = self._texts() if callable(self._texts) else self._texts
+            self._rows = _rows(self.segments, t[0], t[1])
+        return self._rows
+
+    @property
+    def row0(self):
+        return self._render()[0]
+
+    @property
+    def row1(self):
+        return self._render()[1]
+
+    def __repr__(self):
+        return (f"LocalAlignment(score={self.score}, h=[{self.h_begin},{self.h_end}), "
+                f"v=[{self.v_begin},{self.v_end}), segments={len(self.segments)})")
 
 
-@dataclass
 class PairEnumeration:
-    alignments: list
-    undefined_next: bool = False   # stopped where the reference's next step is undefined
+    """The enumeration of one pair.  ``alignments`` is built from the call's output arrays on first
+    access; ``undefined_next``: stopped where the reference's next step is undefined."""
+
+    def __init__(self, batch, k, undefined_next=False):
+        self._batch, self._k, self.undefined_next = batch, k, undefined_next
+        self._alignments = None
+
+    @property
+    def alignments(self):
+        if self._alignments is None:
+            self._alignments = self._batch.alignments_of(self._k)
+        return self._alignments
 
 
 def _rows(segments, h_text, v_text):
@@ -83,18 +110,40 @@ def local_enumerate(H, V, score, cutoff: int = 0, max_count: int = 25, alphabet:
     ctx = context or N.default_context()
     ctx.check(N.lib().gba_local_enumerate(ctx.handle, C.byref(p), C.byref(b), C.byref(r)), "gba_local_enumerate")
     del keep
-    sc, bh, eh, bv, ev = arrs
-    out = []
-    for k in range(n):
-        ht, vt = decode(ch[k], alphabet), decode(cv[k], alphabet)
+    out = _Batch(ch, cv, alphabet, max_count, count, arrs, segs, off)
+    return [PairEnumeration(out, k, int(status[k]) == N.GBA_ENUM_UNDEFINED_NEXT) for k in range(n)]
+
+
+class _Batch:
+    """Output arrays of one gba_local_enumerate call, turned into LocalAlignment objects per pair on
+    demand."""
+
+    def __init__(self, ch, cv, alphabet, max_count, count, arrs, segs, off):
+        self.ch, self.cv, self.alphabet, self.max_count = ch, cv, alphabet, max_count
+        self.count, self.arrs, self.segs, self.off = count, arrs, segs, off
+
+    def alignments_of(self, k):
+        sc, bh, eh, bv, ev = self.arrs
+        texts = _Texts(self, k)
         als = []
-        for i in range(int(count[k])):
-            g = k * max_count + i
-            sg = [tuple(int(x) for x in segs[q]) for q in range(off[g], off[g + 1])]
-            r0, r1 = _rows(sg, ht, vt)
-            als.append(LocalAlignment(int(sc[g]), r0, r1, int(bh[g]), int(eh[g]), int(bv[g]), int(ev[g]), sg))
-        out.append(PairEnumeration(als, int(status[k]) == N.GBA_ENUM_UNDEFINED_NEXT))
-    return out
+        for i in range(int(self.count[k])):
+            g = k * self.max_count + i
+            sg = [tuple(x) for x in self.segs[self.off[g]:self.off[g + 1]].tolist()]
+            als.append(LocalAlignment(int(sc[g]), int(bh[g]), int(eh[g]), int(bv[g]), int(ev[g]), sg, texts))
+        return als
+
+
+class _Texts:
+    """The decoded texts of pair k, decoded once for all its alignments."""
+
+    def __init__(self, batch, k):
+        self.batch, self.k, self.t = batch, k, None
+
+    def __call__(self):
+        if self.t is None:
+            b = self.batch
+            self.t = (decode(b.ch[self.k], b.alphabet), decode(b.cv[self.k], b.alphabet))
+        return self.t
 
 
 class LocalAlignmentEnumerator:

@@ -206,3 +206,45 @@ def records_text(seqs, fmt: str = "fasta", letters: str = "ACGTN", width: int = 
             qual = (rng.integers(33, 74, len(s)).astype(np.uint8)).tobytes()
             parts.append(b"@%s%d" % (id_prefix.encode(), k) + nl + body + nl + b"+" + nl + qual + nl)
     return b"".join(parts)
+
+
+def chain_pairs(n: int, lo: int = 1000, hi: int = 3000, sub_rate: float = 0.05, indel_rate: float = 0.01,
+                min_seed: int = 20, max_seeds: int = 64, seed: int = 31):
+    """Genomic pairs with seed chains for banded chain alignment (LAGAN-style anchors): H random of
+    lo..hi bp, V = H with substitutions and single-base indels, and per pair the exact matches of at
+    least min_seed bp along the true alignment as Seed<Simple>(beginH, beginV, endH, endV), in chain
+    order (colinear, non-overlapping), at most max_seeds evenly picked.  Returns (H, V, chains)."""
+    rng = _rng(seed)
+    H, V, chains = [], [], []
+    for _ in range(n):
+        m = int(rng.integers(lo, hi + 1))
+        h = rng.integers(0, 4, m).astype(np.uint8)
+        r = rng.random(m)
+        dele = r < indel_rate / 2                       # h[i] dropped
+        ins = (r >= indel_rate / 2) & (r < indel_rate)  # a random base before h[i]
+        kept = ~dele
+        sub = rng.random(m) < sub_rate
+        hv = np.where(sub, (h + rng.integers(1, 4, m)) % 4, h).astype(np.uint8)
+        width = kept.astype(np.int64) + ins.astype(np.int64)
+        start = np.concatenate([[0], np.cumsum(width)[:-1]])
+        vpos = np.where(kept, start + ins, -1)         # V position of each kept residue
+        v = np.empty(int(width.sum()) or 1, np.uint8)
+        v[:] = rng.integers(0, 4, v.size)               # inserted bases (and a filler for an empty V)
+        v[vpos[kept]] = hv[kept]
+        # maximal runs of equal residues on one diagonal of the true alignment
+        match = kept & ~sub
+        cont = match[:-1] & match[1:] & (vpos[1:] == vpos[:-1] + 1)
+        seeds = []
+        if match.any():
+            starts = np.flatnonzero(match & ~np.concatenate([[False], cont]))
+            ends = np.flatnonzero(match & ~np.concatenate([cont, [False]]))
+            for i, j in zip(starts, ends):
+                if j - i + 1 >= min_seed:
+                    seeds.append((int(i), int(vpos[i]), int(j) + 1, int(vpos[j]) + 1))
+        if len(seeds) > max_seeds:
+            pick = np.linspace(0, len(seeds) - 1, max_seeds).round().astype(int)
+            seeds = [seeds[q] for q in pick]
+        H.append(h)
+        V.append(v)
+        chains.append(np.array(seeds, np.int32).reshape(-1, 4))
+    return H, V, chains

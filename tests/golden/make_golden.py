@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|packed|sam|seqio|bam|cpp|dynamic]
+    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|packed|sam|seqio|bam|cpp|dynamic|banded_chain]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -127,6 +127,9 @@ def main():
         return
     if only == "dynamic":
         write_dynamic_cases(b62)
+        return
+    if only == "banded_chain":
+        write_banded_chain()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -495,6 +498,77 @@ def write_waterman_eggert(b62):
         json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261208, "cases": cases}, f,
                   separators=(",", ":"))
     print(f"{len(cases)} Waterman-Eggert cases written")
+
+
+def chain_case(rng, max_len=200, max_seeds=8, max_seed_len=30):
+    """A random pair with a random colinear seed chain (seeds need not match the sequences)."""
+    m = int(rng.integers(5, max_len))
+    h = rng.integers(0, 4, m).astype(np.uint8)
+    v = []
+    for x in h:
+        r = rng.random()
+        if r < 0.05:
+            continue
+        if r < 0.10:
+            v.append(int(rng.integers(0, 4)))
+        v.append(int(x) if rng.random() > 0.08 else int(rng.integers(0, 4)))
+    v = np.array(v if v else [0], np.uint8)
+    n = len(v)
+    k = int(rng.integers(1, 16))
+    ns = int(rng.integers(1, max_seeds + 1))
+    seeds, ph, pv = [], 0, 0
+    for _ in range(ns):
+        if ph >= m - 2 or pv >= n - 2:
+            break
+        bh = int(rng.integers(ph, min(m - 1, ph + max(2, m // ns))))
+        bv = int(rng.integers(pv, min(n - 1, pv + max(2, n // ns))))
+        ln = int(rng.integers(1, 1 + max(1, min(m - bh, n - bv, max_seed_len))))
+        eh = min(m, bh + ln + int(rng.integers(0, 3)))
+        ev = min(n, bv + ln + int(rng.integers(0, 3)))
+        if eh <= bh or ev <= bv:
+            break
+        seeds.append((bh, bv, eh, ev))
+        ph, pv = eh, ev
+    if not seeds:
+        seeds = [(0, 0, 1, 1)]
+    schemes = [(2, -1, -2, -2), (5, -3, -1, -5), (1, -1, -1, -1), (2, -3, -1, -4), (5, -3, -5, -5)]
+    a = schemes[int(rng.integers(0, len(schemes)))]
+    g = schemes[int(rng.integers(0, len(schemes)))] if rng.random() < 0.3 else a
+    return h, v, seeds, a, g, int(rng.integers(0, 16)), k
+
+
+def write_banded_chain():
+    """bandedChainAlignment through the compiled reference: random pairs with random colinear
+    chains (every AlignConfig, linear and affine schemes, separate anchor / gap schemes, band
+    extensions 1..15, chains whose grids the reference cannot glue), and genomic pairs with the
+    exact-match anchors of workloads.chain_pairs."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(20261210))
+    cases = []
+
+    def add(h, v, seeds, a, g, fe, k):
+        r = O.ref_banded_chain(h, v, seeds, a, g, fe, k)
+        cases.append({"H": text(h, "dna"), "V": text(v, "dna"), "seeds": [list(map(int, s)) for s in seeds],
+                      "anchor": list(a), "gap": list(g), "free_ends": fe, "k": k, "status": r.status,
+                      "score": r.score if r.status == 0 else None,
+                      "segments": [list(s) for s in r.segments] if r.status == 0 else None,
+                      "n_traces": r.n_traces if r.status == 0 else None,
+                      "rows": list(r.rows) if r.status == 0 else None})
+
+    for trial in range(360):
+        add(*chain_case(rng, 60 if trial % 3 == 0 else 200, 12 if trial % 3 == 0 else 8,
+                        8 if trial % 3 == 0 else 30))
+    for trial in range(40):
+        add(*chain_case(rng, 1200, 20, 120))
+    H, V, chains = W.chain_pairs(40, 300, 900, min_seed=12, seed=77)
+    for k in range(40):
+        add(H[k], V[k], [tuple(s) for s in chains[k]], (2, -3, -1, -5), (2, -3, -1, -5), [0, 15, 5, 10][k % 4],
+            [15, 5, 10, 3][k % 4])
+    with open(os.path.join(HERE, "banded_chain_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only banded_chain", "seed": 20261210,
+                   "cases": cases}, f, separators=(",", ":"))
+    print(f"{len(cases)} banded chain cases written ({sum(c['status'] == 1 for c in cases)} where the reference "
+          f"throws)")
 
 
 def write_seeds(b62):
