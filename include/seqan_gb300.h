@@ -530,7 +530,8 @@ typedef struct {
     gba_simple_score gap;      /* scores in the rectangles between them */
     int32_t free_ends;         /* GBA_FREE_* (AlignConfig<TOP, LEFT, RIGHT, BOTTOM>) */
     int32_t band_extension;    /* >= 1; the reference's default is 15 */
-    int32_t max_traces;        /* co-optimal traces kept per pair, 1..32 (0: 8) */
+    int32_t max_traces;        /* co-optimal traces kept per pair, 1..32; 0: 8, and the pairs that need
+                                  more run again with 32 */
 } gba_chain_params;
 
 typedef struct {

@@ -637,6 +637,7 @@ typedef struct { grid_t *g; long pos; int tv, last; long frag; coord_t c; int ba
 
 static void w_step(walk_t *w, long delta)
 {
+    if (delta <= 0) { w->bad = 1; w->tv = T_NONE; return; }   /* a one-row band: the walk would not move */
     w->pos -= delta;
     if (w->pos < 0 || w->pos >= w->g->L * w->g->Hlen) { w->bad = 1; w->tv = T_NONE; return; }
     w->tv = w->g->T[w->pos];

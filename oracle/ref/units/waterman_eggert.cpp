@@ -7,6 +7,9 @@
 
 #include <sstream>
 #include <string>
+#include <vector>
+
+#include <omp.h>
 
 namespace seqan_ref {
 namespace {
@@ -68,6 +71,30 @@ int ref_local_enumerate(int32_t alphabet, int32_t blosum62, int32_t match, int32
     }
     Score<int, Simple> sc(match, mismatch, gap_extend, gap_open);
     return seqan_ref::enumerate<Dna5>(sc, cutoff, h, m, v, n, max_count, scores, pos, out_rows, cap);
+}
+
+// A batch of pairs (codes concatenated with offsets) on `threads` OpenMP threads (<= 0: all):
+// the enumeration of every pair as above; count[k] = the alignments pair k gave.
+int ref_local_enumerate_batch(int32_t match, int32_t mismatch, int32_t gap, int32_t cutoff, int64_t n_pairs,
+                              const uint8_t * seq_h, const int64_t * off_h, const uint8_t * seq_v,
+                              const int64_t * off_v, int32_t max_count, int32_t * count, int32_t threads)
+{
+    const int nt = threads > 0 ? threads : omp_get_max_threads();
+    Score<int, Simple> sc(match, mismatch, gap, gap);
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<int32_t> scores(size_t(max_count > 0 ? max_count : 1)), pos(size_t(4 * (max_count > 0 ? max_count : 1)));
+        std::vector<char> rows;
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t k = 0; k < n_pairs; ++k)
+        {
+            const int64_t m = off_h[k + 1] - off_h[k], n = off_v[k + 1] - off_v[k];
+            rows.resize(size_t(max_count) * size_t(2 * (m + n + 2)) + 8);
+            count[k] = seqan_ref::enumerate<Dna5>(sc, cutoff, seq_h + off_h[k], m, seq_v + off_v[k], n, max_count,
+                                                  scores.data(), pos.data(), rows.data(), int64_t(rows.size()));
+        }
+    }
+    return 0;
 }
 
 }  // extern "C"

@@ -47,7 +47,7 @@ def _seed_array(chain):
 
 
 def banded_chain_codes(codes_h, codes_v, chains, score_anchor, score_gap=None, config: AlignConfig | None = None,
-                       band_extension: int = 15, max_traces: int = 8, context=None):
+                       band_extension: int = 15, max_traces: int = 0, context=None):
     """One GPU call over code arrays; returns (score, status, num_traces, segment lists)."""
     score_gap = score_gap or score_anchor
     for s in (score_anchor, score_gap):
@@ -92,7 +92,7 @@ def banded_chain_codes(codes_h, codes_v, chains, score_anchor, score_gap=None, c
 
 
 def bandedChainAlignment(seqsH, seqsV, chains, scoreAnchor, scoreGap=None, alignConfig: AlignConfig | None = None,
-                         bandExtension: int = 15, alphabet: str = "dna5", max_traces: int = 8, context=None):
+                         bandExtension: int = 15, alphabet: str = "dna5", max_traces: int = 0, context=None):
     """bandedChainAlignment(align, seedChain, scoreAnchor[, scoreGap][, alignConfig][, bandExtension])
     for a batch: seqsH[k], seqsV[k] with chains[k] = [(beginH, beginV, endH, endV), ...] in chain
     order.  Returns one ChainAlignment per pair; raises ChainError for a pair the reference does

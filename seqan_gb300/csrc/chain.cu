@@ -7,7 +7,7 @@
 
 void launch_banded_chain(const ChainArgs &a, cudaStream_t st)
 {
-    k_banded_chain<<<unsigned((a.num_chains + 63) / 64), 64, 0, st>>>(a);
+    k_banded_chain<<<unsigned((a.num_chains * 32 + 127) / 128), 128, 0, st>>>(a);   // one warp per chain
 }
 
 void launch_chain_pack(const chain::ChainDesc *chains, int64_t num_chains, const uint8_t *arena, int32_t max_traces,

@@ -77,6 +77,8 @@ GBA_API int gba_banded_chain(gba_context *ctx, const gba_chain_params *params, c
         pl.gseg_cap = d.m + d.n + 8;
         chain::Engine e{};
         e.plan = true;
+        e.warp = false;
+        e.lane = 0;
         e.anchor = anchor;
         e.gap = gap;
         e.fe = params->free_ends;
@@ -184,6 +186,67 @@ GBA_API int gba_banded_chain(gba_context *ctx, const gba_chain_params *params, c
         for (int64_t i = 0; i < nc; ++i) res->segment_offsets[c0 + i + 1] = wseg + dense[i + 1];
         wseg += total;
         c0 = c1;
+    }
+    // With the default trace budget, chains that held more co-optimal traces at once run again with
+    // 32 trace slots (only those chains; their outputs are spliced into place).
+    std::vector<int64_t> retry;
+    if (params->max_traces == 0)
+        for (int64_t k = 0; k < N; ++k)
+            if (res->status[k] == chain::ST_CAPACITY) retry.push_back(k);
+    if (!retry.empty()) {
+        const int64_t R = int64_t(retry.size());
+        std::vector<uint8_t> rh, rv;
+        std::vector<int64_t> roh(size_t(R) + 1, 0), rov(size_t(R) + 1, 0), rso(size_t(R) + 1, 0);
+        std::vector<int32_t> rseeds;
+        for (int64_t i = 0; i < R; ++i) {
+            const chain::ChainDesc &d = desc[retry[i]];
+            rh.insert(rh.end(), b->seq_h + d.h_off, b->seq_h + d.h_off + d.m);
+            rv.insert(rv.end(), b->seq_v + d.v_off, b->seq_v + d.v_off + d.n);
+            rseeds.insert(rseeds.end(), sd->seeds + 4 * d.seed_off, sd->seeds + 4 * (d.seed_off + d.n_seeds));
+            roh[i + 1] = int64_t(rh.size());
+            rov[i + 1] = int64_t(rv.size());
+            rso[i + 1] = rso[i] + d.n_seeds;
+        }
+        rh.push_back(0);
+        rv.push_back(0);
+        rseeds.resize(rseeds.size() + 4);
+        gba_batch b2{R, rh.data(), roh.data(), rv.data(), rov.data(), 0, 0};
+        gba_chain_seeds s2{rseeds.data(), rso.data()};
+        gba_chain_params p2 = *params;
+        p2.max_traces = 32;
+        std::vector<int32_t> sc2(static_cast<size_t>(R)), st2(static_cast<size_t>(R)), nt2(static_cast<size_t>(R));
+        std::vector<int64_t> off2(static_cast<size_t>(R) + 1);
+        const int64_t cap2 = roh[R] + rov[R] + 8 * R + 8;
+        std::vector<gba_segment> seg2(static_cast<size_t>(cap2));
+        gba_chain_result r2{sc2.data(), st2.data(), nt2.data(), seg2.data(), cap2, off2.data()};
+        const int rc = gba_banded_chain(ctx, &p2, &b2, &s2, &r2);
+        if (rc != GBA_OK) return rc;
+        dp_ms += ctx->stats.dp_kernel_ms;
+        launches += ctx->stats.kernel_launches;
+        // splice: the retried chains' segments replace their empty slots
+        std::vector<gba_segment> old(res->segments, res->segments + wseg);
+        std::vector<int64_t> oldoff(res->segment_offsets, res->segment_offsets + N + 1);
+        int64_t total = 0;
+        for (int64_t i = 0; i < R; ++i) total += off2[i + 1] - off2[i];
+        if (wseg + total > res->segment_capacity || (total && !res->segments))
+            return fail(ctx, GBA_ECAPACITY, "segment_capacity too small");
+        int64_t w = 0, ri = 0;
+        for (int64_t k = 0; k < N; ++k) {
+            if (ri < R && retry[ri] == k) {
+                const int64_t c = off2[ri + 1] - off2[ri];
+                std::copy(seg2.begin() + off2[ri], seg2.begin() + off2[ri + 1], res->segments + w);
+                res->score[k] = sc2[ri];
+                res->status[k] = st2[ri];
+                if (res->num_traces) res->num_traces[k] = nt2[ri];
+                w += c;
+                ++ri;
+            } else {
+                const int64_t c = oldoff[k + 1] - oldoff[k];
+                std::copy(old.begin() + oldoff[k], old.begin() + oldoff[k + 1], res->segments + w);
+                w += c;
+            }
+            res->segment_offsets[k + 1] = w;
+        }
     }
     ctx->stats = gba_stats{};
     ctx->stats.dp_kernel_ms = dp_ms;

@@ -61,9 +61,20 @@ struct Plan {
     int32_t mp_cap;        // positions of the maximum of one grid
     int32_t gseg_cap;      // segments of one global trace (m + n + 8)
     int32_t lseg_cap;      // segments of one local trace (largest grid m + n + 8)
+    int32_t col_cap;       // largest m + 1 (columns of one grid)
     int32_t status;        // ST_UNDEFINED when the geometry leaves the sequences
     int64_t cells;         // DP cells of all grids (in-band cells for a band)
     int64_t trace_total;   // trace bytes of all grids
+};
+
+// One column of a grid as the reference's loop visits it: rows r0..r1 (r1 = r0 for a single
+// cell), its column type and location, the trace navigator's position at its first cell and the
+// lane leap its cells see.
+struct ColDesc {
+    int r0, r1;
+    int64_t pos0;
+    int leap;
+    int8_t type, loc, single, present;
 };
 
 // One chain's scratch slices (device or host memory) and its inputs.
@@ -79,7 +90,14 @@ struct Work {
     Seg *lseg;      // local traces: slot q at lseg + q * lseg_cap, reference order
     int *llen;      // [traces]
     int *erase;     // [traces]
+    // warp-cooperative fill: per-column descriptors, three rolling anti-diagonals of (S, E, F)
+    // indexed by column, candidate cells for the maximum (last cell per column, the final column)
+    ColDesc *cols;
+    int *aS, *aE, *aF;       // [3 * col_cap]
+    int *ccS, *ccP, *ccF;    // [col_cap]
+    int *fcS, *fcP, *fcF;    // [col_rows]
 };
+
 
 struct ChainDesc {
     int64_t h_off, v_off, seed_off;   // into the batch's codes and seeds (4 int32 per seed)
@@ -104,6 +122,8 @@ __host__ __device__ inline int mxc(int &target, int left, int right, int tl, int
 struct Engine {
     // ---- configuration ----
     bool plan;                  // plan mode: geometry only
+    bool warp;                  // one warp per chain: grids filled by anti-diagonals across the lanes
+    int lane;                   // this thread's lane (0 on the host)
     Scheme anchor, gap;
     int fe, affine, k;
     int max_traces;
@@ -482,7 +502,7 @@ struct Engine {
             else
                 dir = (loc == LOC_TOP || loc == LOC_MIDDLE) ? DIR_LOWER : DIR_ALL;
         }
-        if (dir >= 0) tv = compute(dir, col, row, hS, hE, cur);
+        if (dir >= 0) tv = compute(dir, col, row, hS, hE, cur, dS, vS, vF);
         const int k1 = col & 1;
         if (k1) { if (row < lo1) lo1 = row; if (row > hi1) hi1 = row; w.cS1[row] = cur.s; w.cE1[row] = cur.e; }
         else { if (row < lo0) lo0 = row; if (row > hi0) hi0 = row; w.cS0[row] = cur.s; w.cE0[row] = cur.e; }
@@ -495,7 +515,7 @@ struct Engine {
 
     // the recurrences (align/dp_formula_affine.h, dp_formula_linear.h, dp_formula.h Zero) with
     // CompleteTrace ties; cur.f gets cacheVert's vertical score (_setVerticalScoreOfCell)
-    __host__ __device__ int compute(int dir, int col, int row, int hS, int hE, Cell &cur)
+    __host__ __device__ int compute(int dir, int col, int row, int hS, int hE, Cell &cur, int &dS, int &vS, int &vF) const
     {
         int tv = T_NONE;
         const int ext = sc->ext, open = sc->open;
@@ -748,6 +768,7 @@ struct Engine {
 
     __host__ __device__ void w_step(Walk &wk, int64_t d) const
     {
+        if (d <= 0) { wk.bad = true; wk.tv = T_NONE; return; }   // a one-row band: the walk would not move
         wk.pos -= d;
         if (wk.pos < 0 || wk.pos >= L * Hlen) { wk.bad = true; wk.tv = T_NONE; return; }
         wk.tv = w.T[wk.pos];
@@ -938,10 +959,13 @@ struct Engine {
             const int64_t mpb = pm + L + 4;
             if (pl->mp_cap < mpb) pl->mp_cap = int32_t(mpb);
             if (pl->lseg_cap < pm + pn + 8) pl->lseg_cap = int32_t(pm + pn + 8);
+            if (pl->col_cap < pm + 1) pl->col_cap = int32_t(pm + 1);
             return 0;
         }
         if (L * Hlen > pl->trace_bytes || pn + 1 > pl->col_rows) { fail(ST_CAPACITY); return INT_MIN; }
-        for (int64_t q = 0; q < L * Hlen; ++q) w.T[q] = 0;
+        if (!warp || kd == KIND_GLOBAL) {
+            for (int64_t q = 0; q < L * Hlen; ++q) w.T[q] = 0;
+        }
         lo0 = lo1 = INT_MAX;
         hi0 = hi1 = -1;
         maxS = INF;
@@ -949,7 +973,8 @@ struct Engine {
         bestS = INF;
         bestPos = 0;
         bestCol = bestRow = 0;
-        if (bd) run_banded();
+        if (warp && kd != KIND_GLOBAL) fill_warp();
+        else if (bd) run_banded();
         else run_unbanded();
         if (err) return INT_MIN;
         if (kd == KIND_GLOBAL) {
@@ -959,6 +984,271 @@ struct Engine {
         nset = 0;
         for (int i = 0; i < nmp && !err; ++i) chain_trace_one(w.mp[i]);
         return maxS;
+    }
+
+    // ---------------- warp-cooperative fill ----------------
+    // The cells of one anti-diagonal (c + r = d) depend only on the two before it, so the lanes of a
+    // warp take the cells of a diagonal together.  Every cell gets the inputs the column-major loop
+    // gives it -- the horizontal and diagonal neighbours from the previous column's computed rows,
+    // the cell above as cacheVert (none for a column's first cell), the diagonal preset of middle /
+    // bottom columns -- so values, trace bytes and init-vector stores are the loop's.  The candidates
+    // for the maximum are kept per column and scanned afterwards in column-major order, which gives
+    // the scout's list of positions in the loop's order.
+
+    static __host__ __device__ int64_t floor2(int64_t a) { return a >= 0 ? a / 2 : -((-a + 1) / 2); }
+
+    __host__ __device__ void desc_col(int col, int coltype, int loc, int r0, int r1, bool single, int64_t &p,
+                                      int64_t &lp)
+    {
+        if (col < 0 || col > gm || col >= pl->col_cap) { fail(ST_UNDEFINED); return; }
+        if (!single && r1 <= r0) { fail(ST_UNDEFINED); return; }   // the reference's track needs two cells
+        if (coltype != COL_INITIAL) {
+            if (banded && loc == LOC_TOP) { lp -= 1; p += lp; }
+            else p += lp;
+        }
+        ColDesc &d = w.cols[col];
+        d.r0 = r0;
+        d.r1 = single ? r0 : r1;
+        d.pos0 = p;
+        d.leap = int(lp);
+        d.type = int8_t(coltype);
+        d.loc = int8_t(loc);
+        d.single = single;
+        d.present = 1;
+        if (!single) {
+            p += r1 - r0;
+            if (banded && loc == LOC_BOTTOM && coltype != COL_INITIAL) lp += 1;
+        }
+    }
+
+    // the columns of run_banded / run_unbanded, with the navigator's positions
+    __host__ __device__ void describe(int &cfirst, int &clast)
+    {
+        int64_t p = pos, lp = leap;
+        cfirst = 0;
+        clast = gm;
+        if (!banded) {
+            desc_col(0, COL_INITIAL, LOC_FULL, 0, gn, false, p, lp);
+            for (int c = 1; c < gm; ++c) desc_col(c, COL_INNER, LOC_FULL, 0, gn, false, p, lp);
+            desc_col(gm, COL_FINAL, LOC_FULL, 0, gn, false, p, lp);
+            return;
+        }
+        const int mm = gm, nn = gn, lw = lower, up = upper;
+        int vb = -cmin(0, 1 + up), ve = -cmin(0, cmax(-nn, lw));
+        const int hb = cmax(0, cmin(mm - 1, lw));
+        int hTop = cmin(mm - 1, cmax(0, up)), hMid = cmin(mm - 1, cmax(0, nn + lw));
+        if (up > nn + lw) { const int t = hTop; hTop = hMid; hMid = t; }
+        const int hBot = cmax(0, cmin(mm, up + nn) - 1);
+        if (hb == mm - 1) {
+            const int col = cmax(0, cmin(mm, lw));
+            cfirst = clast = col;
+            desc_col(col, COL_INITIAL, LOC_TOP, 0, 0, true, p, lp);
+            return;
+        }
+        if (hBot == 0) {
+            const int row = cmin(nn, -up);
+            cfirst = clast = 0;
+            desc_col(0, COL_INITIAL, LOC_BOTTOM, row, row, true, p, lp);
+            return;
+        }
+        if (up < 0) {
+            ++vb;
+            desc_col(0, COL_INITIAL, lw > -nn ? LOC_MIDDLE : LOC_BOTTOM, vb, ve, false, p, lp);
+        } else if (lw >= 0) {
+            cfirst = hb;
+            desc_col(hb, COL_INITIAL, LOC_TOP, 0, 0, true, p, lp);
+        } else {
+            desc_col(0, COL_INITIAL, lw <= -nn ? LOC_FULL : LOC_TOP, vb, ve, false, p, lp);
+        }
+        int hIt = hb;
+        for (; hIt != hTop && !err; ++hIt) { ++ve; desc_col(hIt + 1, COL_INNER, LOC_TOP, vb, ve, false, p, lp); }
+        if (up > nn + lw) {
+            for (; hIt != hMid && !err; ++hIt) desc_col(hIt + 1, COL_INNER, LOC_FULL, vb, ve, false, p, lp);
+        } else {
+            for (; hIt != hMid && !err; ++hIt) {
+                ++vb; ++ve;
+                desc_col(hIt + 1, COL_INNER, LOC_MIDDLE, vb, ve, false, p, lp);
+            }
+        }
+        for (; hIt != hBot && !err; ++hIt) { ++vb; desc_col(hIt + 1, COL_INNER, LOC_BOTTOM, vb, ve, false, p, lp); }
+        clast = hIt;
+        if (hIt < mm - 1) {
+            clast = hIt + 1;
+            desc_col(hIt + 1, COL_INNER, LOC_BOTTOM, vb + 1, vb + 1, true, p, lp);
+        } else if (hIt == mm - 1) {
+            clast = mm;
+            if (up == mm - nn) desc_col(mm, COL_FINAL, LOC_BOTTOM, vb + 1, vb + 1, true, p, lp);
+            else if (up >= mm) {
+                if (lw + nn > mm) { ++ve; desc_col(mm, COL_FINAL, LOC_TOP, vb, ve, false, p, lp); }
+                else if (lw + nn + 1 > mm) { ++ve; desc_col(mm, COL_FINAL, LOC_TOP, vb, ve, false, p, lp); }
+                else desc_col(mm, COL_FINAL, LOC_FULL, vb, ve, false, p, lp);
+            } else {
+                ++vb;
+                if (lw + nn <= mm) {
+                    if (lw + nn == mm) { ++ve; desc_col(mm, COL_FINAL, LOC_MIDDLE, vb, ve, false, p, lp); }
+                    else desc_col(mm, COL_FINAL, LOC_BOTTOM, vb, ve, false, p, lp);
+                } else {
+                    ++ve;
+                    desc_col(mm, COL_FINAL, LOC_MIDDLE, vb, ve, false, p, lp);
+                }
+            }
+        }
+    }
+
+    __host__ __device__ bool computed(int c, int r, int cfirst, int clast) const
+    {
+        if (c < cfirst || c > clast) return false;
+        const ColDesc &d = w.cols[c];
+        return d.present && r >= d.r0 && r <= d.r1;
+    }
+
+    // the cells of anti-diagonal d that lane l takes
+    __host__ __device__ void fill_diag(int64_t d, int l, int cfirst, int clast)
+    {
+        const int k3 = int(d % 3), k1 = int((d + 2) % 3), k2 = int((d + 1) % 3);   // d, d - 1, d - 2
+        const int cap = pl->col_cap;
+        int64_t clo = cmax<int64_t>(cfirst, d - gn), chi = cmin<int64_t>(clast, d);
+        if (banded) {
+            clo = cmax(clo, -floor2(-(d + lower)));
+            chi = cmin(chi, floor2(d + upper));
+        }
+        for (int64_t c64 = clo + l; c64 <= chi; c64 += 32) {
+            const int c = int(c64), r = int(d - c64);
+            if (!computed(c, r, cfirst, clast)) continue;
+            const ColDesc &cd = w.cols[c];
+            const int cellk = (r == cd.r0) ? CELL_FIRST : (r == cd.r1 ? CELL_LAST : CELL_INNER);
+            const int64_t p = cd.pos0 + (r - cd.r0);
+            const int64_t lp = cd.leap + ((cellk == CELL_LAST && cd.loc == LOC_BOTTOM && cd.type != COL_INITIAL) ? 1 : 0);
+            if (p < 0 || p >= L * Hlen) { fail(ST_UNDEFINED); continue; }
+            const bool hv = computed(c - 1, r, cfirst, clast);
+            const int hS = hv ? w.aS[k1 * cap + c - 1] : INF, hE = hv ? w.aE[k1 * cap + c - 1] : INF;
+            int kdS = INF, kvS = INF, kvF = INF;
+            if (cellk != CELL_FIRST) {
+                kvS = w.aS[k1 * cap + c];
+                kvF = w.aF[k1 * cap + c];
+                if (computed(c - 1, r - 1, cfirst, clast)) kdS = w.aS[k2 * cap + c - 1];
+            } else if (cd.type != COL_INITIAL && (cd.loc == LOC_MIDDLE || cd.loc == LOC_BOTTOM) && r > 0 && c > 0) {
+                if (computed(c - 1, r - 1, cfirst, clast)) kdS = w.aS[k2 * cap + c - 1];
+            }
+            Cell cur{INF, INF, INF};
+            int tv = T_NONE;
+            if (cd.type == COL_INITIAL) {
+                const int64_t idx = (p % L) - (lp - 1);
+                if (idx < 0 || idx >= n4[1]) { fail(ST_UNDEFINED); continue; }
+                cur = w.v4[1][idx];
+            } else if (cellk == CELL_FIRST && (cd.loc == LOC_TOP || cd.loc == LOC_FULL)) {
+                const int64_t idx = p / L;
+                if (idx >= n4[0]) { fail(ST_UNDEFINED); continue; }
+                cur = w.v4[0][idx];
+            } else {
+                const int dir = (cellk == CELL_INNER) ? DIR_ALL
+                              : (cellk == CELL_FIRST) ? DIR_UPPER
+                              : (cd.loc == LOC_TOP || cd.loc == LOC_MIDDLE) ? DIR_LOWER : DIR_ALL;
+                tv = compute(dir, c, r, hS, hE, cur, kdS, kvS, kvF);
+            }
+            w.aS[k3 * cap + c] = cur.s;
+            w.aE[k3 * cap + c] = cur.e;
+            w.aF[k3 * cap + c] = cur.f;
+            w.T[p] = uint8_t(tv);
+            // the chain's tracking options
+            const int64_t cH = p / L, cV = p % L;
+            bool storeRow = false, storeCol = false, lastCol = false, lastRow = false;
+            const bool finalM = kind == KIND_FINAL;
+            if (cH >= hNext) {
+                if (cd.loc == LOC_BOTTOM) { if (cV + lp == vNext) storeRow = true; }
+                else if (cV == vNext) storeRow = true;
+                if (cH == hNext && cV >= vNext) storeCol = true;
+                if (cellk == CELL_LAST && (!finalM || (fe & FREE_BOTTOM))) lastRow = true;
+                if (cd.type == COL_FINAL) {
+                    if (cellk == CELL_LAST) { lastCol = true; lastRow = true; }
+                    else if (cd.loc != LOC_FULL || cV >= vNext) {
+                        if (!finalM || (fe & FREE_RIGHT)) lastCol = true;
+                    }
+                }
+            }
+            if (storeCol) {
+                const int64_t q = cV - vNext;
+                if (q >= n4[3]) { fail(ST_UNDEFINED); continue; }
+                w.v4[3][q] = cur;
+            }
+            if (storeRow) {
+                const int64_t q = cH - hNext;
+                if (q >= n4[2]) { fail(ST_UNDEFINED); continue; }
+                w.v4[2][q] = cur;
+            }
+            if (lastCol || lastRow) {
+                if (cd.type == COL_FINAL) {
+                    w.fcS[r] = cur.s;
+                    w.fcP[r] = int(p);
+                    w.fcF[r] = 1;
+                } else {
+                    w.ccS[c] = cur.s;
+                    w.ccP[c] = int(p);
+                    w.ccF[c] = 1;
+                }
+            }
+        }
+    }
+
+    __host__ __device__ void offer_chain(int s_, int p_)
+    {
+        if (s_ >= maxS) {
+            if (s_ != maxS) { nmp = 0; maxS = s_; }
+            if (nmp >= pl->mp_cap) { fail(ST_CAPACITY); return; }
+            w.mp[nmp++] = p_;
+        }
+    }
+
+    __host__ __device__ void fill_warp()
+    {
+        if (gm + 1 > pl->col_cap || gn + 1 > pl->col_rows) { fail(ST_CAPACITY); return; }
+        const int64_t cells = L * Hlen;
+#ifdef __CUDA_ARCH__
+        for (int64_t q = lane; q < cells; q += 32) w.T[q] = 0;
+        for (int c = lane; c <= gm; c += 32) { w.cols[c].present = 0; w.ccF[c] = 0; }
+        for (int r = lane; r <= gn; r += 32) w.fcF[r] = 0;
+        __syncwarp();
+#else
+        for (int64_t q = 0; q < cells; ++q) w.T[q] = 0;
+        for (int c = 0; c <= gm; ++c) { w.cols[c].present = 0; w.ccF[c] = 0; }
+        for (int r = 0; r <= gn; ++r) w.fcF[r] = 0;
+#endif
+        int cfirst = 0, clast = 0;
+        describe(cfirst, clast);   // every lane writes the same descriptors
+#ifdef __CUDA_ARCH__
+        __syncwarp();
+#endif
+        if (err) return;
+        int64_t dmin = INT64_MAX, dmax = -1;
+        for (int c = cfirst; c <= clast; ++c) {
+            const ColDesc &cd = w.cols[c];
+            if (!cd.present) continue;
+            dmin = cmin<int64_t>(dmin, int64_t(c) + cd.r0);
+            dmax = cmax<int64_t>(dmax, int64_t(c) + cd.r1);
+        }
+        for (int64_t d = dmin; d <= dmax; ++d) {
+#ifdef __CUDA_ARCH__
+            fill_diag(d, lane, cfirst, clast);
+            __syncwarp();
+#else
+            for (int l = 0; l < 32; ++l) fill_diag(d, l, cfirst, clast);
+#endif
+        }
+#ifdef __CUDA_ARCH__
+        err = __reduce_max_sync(0xffffffffu, err);
+#endif
+        if (err) return;
+        // the scout's positions of the maximum, in the loop's order
+        for (int c = cfirst; c <= clast && !err; ++c) {
+            const ColDesc &cd = w.cols[c];
+            if (!cd.present) continue;
+            if (cd.type == COL_FINAL) {
+                for (int r = cd.r0; r <= cd.r1; ++r)
+                    if (w.fcF[r]) offer_chain(w.fcS[r], w.fcP[r]);
+            } else if (w.ccF[c]) {
+                offer_chain(w.ccS[c], w.ccP[c]);
+            }
+        }
     }
 
     // ---------------- the chain driver ----------------
@@ -1214,7 +1504,19 @@ __host__ __device__ inline int64_t layout(const Plan &p, int max_traces, uint8_t
     Seg *lseg = reinterpret_cast<Seg *>(take(int64_t(max_traces) * p.lseg_cap * int64_t(sizeof(Seg))));
     int *llen = reinterpret_cast<int *>(take(int64_t(max_traces) * 4));
     int *erase = reinterpret_cast<int *>(take(int64_t(max_traces) * 4));
+    ColDesc *cols = reinterpret_cast<ColDesc *>(take(int64_t(p.col_cap) * int64_t(sizeof(ColDesc))));
+    int *aS = reinterpret_cast<int *>(take(int64_t(p.col_cap) * 12));
+    int *aE = reinterpret_cast<int *>(take(int64_t(p.col_cap) * 12));
+    int *aF = reinterpret_cast<int *>(take(int64_t(p.col_cap) * 12));
+    int *ccS = reinterpret_cast<int *>(take(int64_t(p.col_cap) * 4));
+    int *ccP = reinterpret_cast<int *>(take(int64_t(p.col_cap) * 4));
+    int *ccF = reinterpret_cast<int *>(take(int64_t(p.col_cap) * 4));
+    int *fcS = reinterpret_cast<int *>(take(int64_t(p.col_rows) * 4));
+    int *fcP = reinterpret_cast<int *>(take(int64_t(p.col_rows) * 4));
+    int *fcF = reinterpret_cast<int *>(take(int64_t(p.col_rows) * 4));
     if (w) {
+        w->cols = cols; w->aS = aS; w->aE = aE; w->aF = aF;
+        w->ccS = ccS; w->ccP = ccP; w->ccF = ccF; w->fcS = fcS; w->fcP = fcP; w->fcF = fcF;
         w->T = T; w->cS0 = c0; w->cS1 = c1; w->cE0 = e0; w->cE1 = e1;
         for (int q = 0; q < 4; ++q) w->v4[q] = v4[q];
         w->set = set; w->mp = mp; w->gseg = gseg; w->glen = glen; w->gorder = gorder;
@@ -1231,14 +1533,17 @@ void launch_chain_pack(const chain::ChainDesc *chains, int64_t num_chains, const
                        const int32_t *seg_count, const int64_t *dense_off, chain::Seg *dense, cudaStream_t st);
 
 #ifdef SEQAN_GB300_CHAIN_KERNELS
-__global__ void __launch_bounds__(64) k_banded_chain(ChainArgs a)
+__global__ void __launch_bounds__(128) k_banded_chain(ChainArgs a)
 {
-    const int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= a.num_chains) return;
+    const int64_t c = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = int(threadIdx.x & 31);
+    if (c >= a.num_chains) return;   // whole warps leave together
     const chain::ChainDesc &d = a.chains[c];
     chain::Plan pl = d.plan;
     chain::Engine e;
     e.plan = false;
+    e.warp = true;
+    e.lane = lane;
     e.anchor = a.anchor;
     e.gap = a.gap;
     e.fe = a.free_ends;
@@ -1254,10 +1559,13 @@ __global__ void __launch_bounds__(64) k_banded_chain(ChainArgs a)
     int score = INT_MIN;
     if (pl.status == chain::ST_OK) score = e.run(a.seeds + 4 * d.seed_off, d.n_seeds);
     else e.err = pl.status;
-    a.score[c] = score;
-    a.status[c] = e.err;
-    a.n_traces[c] = e.ng;
-    a.seg_count[c] = (!e.err && e.ng > 0) ? e.w.glen[e.w.gorder[0]] : 0;
+    __syncwarp();
+    if (lane == 0) {
+        a.score[c] = score;
+        a.status[c] = e.err;
+        a.n_traces[c] = e.ng;
+        a.seg_count[c] = (!e.err && e.ng > 0) ? e.w.glen[e.w.gorder[0]] : 0;
+    }
 }
 
 // Copies the first trace of each chain's set (kept reversed in its scratch) to the dense output in

@@ -37,7 +37,7 @@ def test_empty_chain_keeps_rows(engine):
     assert r.score == -2 ** 31 and r.row0 == "ACGATCGATCGACTGACT" and r.segments == []
 
 
-def _run(cases, max_traces=8):
+def _run(cases, max_traces=0):
     from seqan_gb300.banded_chain import banded_chain_codes
     from seqan_gb300 import AlignConfig
     # one call per (schemes, free ends, k) group
