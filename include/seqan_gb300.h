@@ -571,8 +571,8 @@ GBA_API int gba_align_packed(gba_context *ctx, const gba_params *params, const g
 /* --- SAM output -----------------------------------------------------------------------------
  * The SAM lines of alignment records as the reference's SAM writer writes a BamAlignmentRecord
  * (bam_io/write_sam.h:126-217: QNAME, FLAG, RNAME or '*', POS + 1, MAPQ, CIGAR or '*', RNEXT as
- * '*', '=' or a name, PNEXT + 1, TLEN or '0', SEQ or '*', QUAL or '*'; no tags), formatted on the
- * device.  Positions are 0-based with -1 for none, as in BamAlignmentRecord; the CIGAR is the
+ * '*', '=' or a name, PNEXT + 1, TLEN or '0', SEQ or '*', QUAL or '*', then the tags as
+ * appendTagsBamToSam writes them: bam_io/bam_sam_conversion.h:250-360), formatted on the device.  Positions are 0-based with -1 for none, as in BamAlignmentRecord; the CIGAR is the
  * BAM-packed form of gba_result.cigar; SEQ is residue codes turned into seq_letters[code]. */
 typedef struct {
     int64_t num;                               /* records */
@@ -592,6 +592,13 @@ typedef struct {
     const char *contig_names;                  /* the context's contig names back to back */
     const int64_t *contig_off;                 /* num_contigs + 1 */
     int64_t num_contigs;
+    /* BamAlignmentRecord.tags: each record's tags in BAM form (two name characters, a type
+     * character, the value), back to back; NULL tags_off: no record has tags.  SAM writes them as
+     * NAME:TYPE:VALUE separated by tabs (c, s, i, C, S, I as 'i'; Z and H up to their NUL; B arrays
+     * as the element type and ","-prefixed values); float values (f, B:f) and malformed tags are
+     * GBA_EUNSUPPORTED / GBA_EINVAL there.  BAM appends the bytes as they are. */
+    const char *tags;
+    const int64_t *tags_off;                   /* num + 1, or NULL */
 } gba_sam_records;
 
 /* Writes the lines to out and their offsets to line_off[0..num] (line k is out[line_off[k] ..
@@ -629,10 +636,10 @@ typedef struct {
 } gba_seq_records;
 
 /* BAM records of the same fields: write(target, record, context, Bam()) for a BamAlignmentRecord
- * without tags (bam_io/write_bam.h:100-271), the uncompressed record blocks (block_size, the
+ * (bam_io/write_bam.h:100-271), the uncompressed record blocks (block_size, the
  * 32-byte core with bin = reg2bin(beginPos, beginPos + max(1, length in the reference)), name and
- * NUL, CIGAR words, Iupac sequence two codes per byte, qualities minus '!' or 0xFF), formatted on
- * the device; rec_off[num + 1] gets each record's byte offset.  Names of more than 254 characters,
+ * NUL, CIGAR words, Iupac sequence two codes per byte, qualities minus '!' or 0xFF, the tag
+ * bytes), formatted on the device; rec_off[num + 1] gets each record's byte offset.  Names of more than 254 characters,
  * more than 65535 CIGAR operations and more qualities than residues are GBA_EINVAL (the core's
  * fields cannot hold them; the reference asserts on the last).  BGZF compression is not done. */
 GBA_API int gba_format_bam(gba_context *ctx, const gba_sam_records *records, char *out, int64_t capacity,

@@ -720,6 +720,41 @@ def ref_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, blosum62=F
 # SAM lines (bam_io/write_sam.h:126-217) of BamAlignmentRecord fields given as plain lists.
 # ---------------------------------------------------------------------------------------------
 
+_TAG_FMT = {"c": ("<b", 1), "C": ("<B", 1), "s": ("<h", 2), "S": ("<H", 2), "i": ("<i", 4), "I": ("<I", 4)}
+
+
+def tags_bam_to_sam(t: bytes) -> str:
+    """appendTagsBamToSam (bam_io/bam_sam_conversion.h:250-360) of one record's BAM tag bytes (no
+    float values)."""
+    import struct
+    out, i = [], 0
+    while i < len(t):
+        name, ty = t[i:i + 2].decode("latin1"), chr(t[i + 2])
+        i += 3
+        shown = "i" if ty.lower() in "csi" else ty
+        if ty in "ZH":
+            j = t.index(0, i)
+            val = t[i:j].decode("latin1")
+            i = j + 1
+        elif ty == "B":
+            et = chr(t[i])
+            cnt = struct.unpack_from("<I", t, i + 1)[0]
+            i += 5
+            fmt, sz = _TAG_FMT[et]
+            vals = [struct.unpack_from(fmt, t, i + q * sz)[0] for q in range(cnt)]
+            i += cnt * sz
+            val = et + "".join("," + str(x) for x in vals)
+        elif ty == "A":
+            val = chr(t[i])
+            i += 1
+        else:
+            fmt, sz = _TAG_FMT[ty]
+            val = str(struct.unpack_from(fmt, t, i)[0])
+            i += sz
+        out.append(f"{name}:{shown}:{val}")
+    return "\t".join(out)
+
+
 def write_sam(rec) -> str:
     """Restates the reference's SAM record writer for rec (a seqan_gb300.sam.SamRecords)."""
     lines = []
@@ -729,10 +764,13 @@ def write_sam(rec) -> str:
         seq = "".join(rec.letters[int(x)] for x in rec.seq[k]) or "*"
         qual = (rec.qual[k] if rec.qual is not None else "") or "*"
         tlen = int(rec.tlen[k])
+        tags = getattr(rec, "tags", None)
+        tail = ("\t" + tags_bam_to_sam(tags[k])) if tags is not None and len(tags[k]) else ""
         lines.append("\t".join([rec.qname[k], str(int(rec.flag[k])), "*" if rid == -1 else rec.contigs[rid],
                                  str(int(rec.pos[k]) + 1), str(int(rec.mapq[k])), cig,
                                  "*" if rn == -1 else ("=" if rn == rid else rec.contigs[rn]),
-                                 str(int(rec.next_pos[k]) + 1), "0" if tlen == 0 else str(tlen), seq, qual]) + "\n")
+                                 str(int(rec.next_pos[k]) + 1), "0" if tlen == 0 else str(tlen), seq, qual]) + tail
+                     + "\n")
     return "".join(lines)
 
 
@@ -756,7 +794,13 @@ def sam_arrays(rec):
     np.cumsum([len(x) for x in cb], out=cnoff[1:])
     letters = np.zeros(32, np.uint8)
     letters[:len(rec.letters)] = np.frombuffer(rec.letters.encode(), np.uint8)
-    return dict(qname=np.frombuffer(b"".join(enc) + b"\0", np.uint8), qoff=qoff,
+    tg = getattr(rec, "tags", None)
+    tags, toff = None, None
+    if tg is not None:
+        toff = np.zeros(n + 1, np.int64)
+        np.cumsum([len(x) for x in tg], out=toff[1:])
+        tags = np.frombuffer(b"".join(bytes(x) for x in tg) + b"\0", np.uint8)
+    return dict(tags=tags, toff=toff, qname=np.frombuffer(b"".join(enc) + b"\0", np.uint8), qoff=qoff,
                 flag=np.ascontiguousarray(rec.flag, np.uint16), rid=np.ascontiguousarray(rec.ref_id, np.int32),
                 pos=np.ascontiguousarray(rec.pos, np.int32), mapq=np.ascontiguousarray(rec.mapq, np.uint8),
                 cigar=cig, coff=coff, rnext=np.ascontiguousarray(rec.next_ref_id, np.int32),
@@ -774,11 +818,28 @@ def oracle_write_sam_c(rec, threads: int = 0, arrays=None) -> str:
     args = [C.c_int64(n), _ptr(a["qname"]), _ptr(a["qoff"]), _ptr(a["flag"]), _ptr(a["rid"]), _ptr(a["pos"]),
             _ptr(a["mapq"]), _ptr(a["cigar"]), _ptr(a["coff"]), _ptr(a["rnext"]), _ptr(a["pnext"]), _ptr(a["tlen"]),
             _ptr(a["seq"]), _ptr(a["soff"]), _ptr(a["letters"]), _ptr(a["qual"]), _ptr(a["quoff"]),
-            C.c_int64(len(rec.contigs)), _ptr(a["cnames"]), _ptr(a["cnoff"])]
+            C.c_int64(len(rec.contigs)), _ptr(a["cnames"]), _ptr(a["cnoff"]), _ptr(a["tags"]), _ptr(a["toff"])]
     total = lib.orc_write_sam(*args, None, C.c_int64(0), C.c_int32(threads))
+    if total < 0:
+        raise ValueError("tags the restatement does not write")
     out = np.zeros(total + 1, np.uint8)
     lib.orc_write_sam(*args, _ptr(out), C.c_int64(total + 1), C.c_int32(threads))
     return bytes(out[:total]).decode()
+
+
+_TAG_KEEP = []
+
+
+def _tags_ptrs(rec, n):
+    """(tags, offsets) pointers of rec.tags for the C writers, or (None, None)."""
+    tg = getattr(rec, "tags", None)
+    if tg is None:
+        return None, None
+    toff = np.zeros(n + 1, np.int64)
+    np.cumsum([len(x) for x in tg], out=toff[1:])
+    buf = np.frombuffer(b"".join(bytes(x) for x in tg) + b"\0", np.uint8)
+    _TAG_KEEP[:] = [toff, buf]
+    return _ptr(buf), _ptr(toff)
 
 
 def ref_write_sam(rec) -> str:
@@ -807,12 +868,13 @@ def ref_write_sam(rec) -> str:
     flag, rid, pos = arr(rec.flag, np.uint16), arr(rec.ref_id, np.int32), arr(rec.pos, np.int32)
     mapq, rn, pn, tl = arr(rec.mapq, np.uint8), arr(rec.next_ref_id, np.int32), arr(rec.next_pos, np.int32), \
         arr(rec.tlen, np.int32)
-    cap = int(qoff[-1] + soff[-1] + quoff[-1] + 64 * n + 16 * int(coff[-1]) + 1024)
+    tp, to = _tags_ptrs(rec, n)
+    cap = 8 * sum(len(x) for x in (getattr(rec, "tags", None) or [])) + int(qoff[-1] + soff[-1] + quoff[-1] + 64 * n + 16 * int(coff[-1]) + 1024)
     out = C.create_string_buffer(cap)
     args = [C.c_int64(n), C.c_char_p(qname), _ptr(qoff), _ptr(flag), _ptr(rid), _ptr(pos), _ptr(mapq), _ptr(cig),
             _ptr(coff), _ptr(rn), _ptr(pn), _ptr(tl), C.c_char_p(b"".join(seqs) or b"\0"), _ptr(soff),
             C.c_char_p(b"".join(quals) or b"\0"), _ptr(quoff), C.c_int64(len(cn)), C.c_char_p(b"".join(cn) or b"\0"),
-            _ptr(cnoff), out, C.c_int64(cap)]
+            _ptr(cnoff), tp, to, out, C.c_int64(cap)]
     length = lib.ref_write_sam(*args)
     return out.raw[:length].decode()
 
@@ -945,7 +1007,8 @@ def oracle_write_bam_c(rec, threads: int = 0, arrays=None) -> bytes:
     n = len(rec.qname)
     args = [C.c_int64(n), _ptr(a["qname"]), _ptr(a["qoff"]), _ptr(a["flag"]), _ptr(a["rid"]), _ptr(a["pos"]),
             _ptr(a["mapq"]), _ptr(a["cigar"]), _ptr(a["coff"]), _ptr(a["rnext"]), _ptr(a["pnext"]), _ptr(a["tlen"]),
-            _ptr(a["seq"]), _ptr(a["soff"]), _ptr(a["letters"]), _ptr(a["qual"]), _ptr(a["quoff"])]
+            _ptr(a["seq"]), _ptr(a["soff"]), _ptr(a["letters"]), _ptr(a["qual"]), _ptr(a["quoff"]),
+            _ptr(a["tags"]), _ptr(a["toff"])]
     total = lib.orc_write_bam(*args, None, C.c_int64(0), C.c_int32(threads))
     out = np.zeros(total + 1, np.uint8)
     lib.orc_write_bam(*args, _ptr(out), C.c_int64(total + 1), C.c_int32(threads))
@@ -977,12 +1040,13 @@ def ref_write_bam(rec) -> bytes:
     flag, rid, pos = arr(rec.flag, np.uint16), arr(rec.ref_id, np.int32), arr(rec.pos, np.int32)
     mapq, rn, pn, tl = arr(rec.mapq, np.uint8), arr(rec.next_ref_id, np.int32), arr(rec.next_pos, np.int32), \
         arr(rec.tlen, np.int32)
-    cap = int(qoff[-1] + 2 * soff[-1] + quoff[-1] + 40 * n + 4 * int(coff[-1]) + 64)
+    tp, to = _tags_ptrs(rec, n)
+    cap = 8 * sum(len(x) for x in (getattr(rec, "tags", None) or [])) + int(qoff[-1] + 2 * soff[-1] + quoff[-1] + 40 * n + 4 * int(coff[-1]) + 64)
     out = C.create_string_buffer(cap)
     args = [C.c_int64(n), C.c_char_p(b"".join(qn) or b"\0"), _ptr(qoff), _ptr(flag), _ptr(rid), _ptr(pos),
             _ptr(mapq), _ptr(cig), _ptr(coff), _ptr(rn), _ptr(pn), _ptr(tl), C.c_char_p(b"".join(seqs) or b"\0"),
             _ptr(soff), C.c_char_p(b"".join(quals) or b"\0"), _ptr(quoff), C.c_int64(len(cn)),
-            C.c_char_p(b"".join(cn) or b"\0"), _ptr(cnoff), out, C.c_int64(cap)]
+            C.c_char_p(b"".join(cn) or b"\0"), _ptr(cnoff), tp, to, out, C.c_int64(cap)]
     length = lib.ref_write_bam(*args)
     assert length <= cap
     return out.raw[:length]

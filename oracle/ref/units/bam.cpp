@@ -13,7 +13,8 @@ int64_t ref_write_bam(int64_t n, const char * qname, const int64_t * qoff, const
                       const int32_t * rid, const int32_t * pos, const uint8_t * mapq, const uint32_t * cigar,
                       const int64_t * coff, const int32_t * rnext, const int32_t * pnext, const int32_t * tlen,
                       const char * seq, const int64_t * soff, const char * qual, const int64_t * quoff,
-                      int64_t ncontigs, const char * cnames, const int64_t * cnoff, char * out, int64_t cap)
+                      int64_t ncontigs, const char * cnames, const int64_t * cnoff, const char * tags,
+                      const int64_t * toff, char * out, int64_t cap)
 {
     typedef StringSet<CharString> TNameStore;
     typedef NameStoreCache<TNameStore> TNameStoreCache;
@@ -39,6 +40,7 @@ int64_t ref_write_bam(int64_t n, const char * qname, const int64_t * qoff, const
         r.tLen = tlen[k];
         r.seq = std::string(seq + soff[k], seq + soff[k + 1]);
         r.qual = std::string(qual + quoff[k], qual + quoff[k + 1]);
+        if (toff) r.tags = std::string(tags + toff[k], tags + toff[k + 1]);
         write(bytes, r, context, Bam());
     }
     const int64_t len = int64_t(length(bytes));

@@ -9,13 +9,15 @@ extern "C" {
 
 // Fields of record k: qname chars [qoff[k], qoff[k+1]), flag, rid, pos (0-based), mapq, cigar
 // (BAM-packed length << 4 | op into "MIDNSHP=X") [coff[k], coff[k+1]), rnext, pnext, tlen, seq
-// letters [soff[k], soff[k+1]), qual [quoff[k], quoff[k+1]).  Contig names back to back.  Writes
+// letters [soff[k], soff[k+1]), qual [quoff[k], quoff[k+1]), BAM tag bytes [toff[k], toff[k+1]) (toff
+// NULL: none).  Contig names back to back.  Writes
 // the SAM lines to out (NUL-terminated if it fits); returns their total length.
 int64_t ref_write_sam(int64_t n, const char * qname, const int64_t * qoff, const uint16_t * flag,
                       const int32_t * rid, const int32_t * pos, const uint8_t * mapq, const uint32_t * cigar,
                       const int64_t * coff, const int32_t * rnext, const int32_t * pnext, const int32_t * tlen,
                       const char * seq, const int64_t * soff, const char * qual, const int64_t * quoff,
-                      int64_t ncontigs, const char * cnames, const int64_t * cnoff, char * out, int64_t cap)
+                      int64_t ncontigs, const char * cnames, const int64_t * cnoff, const char * tags,
+                      const int64_t * toff, char * out, int64_t cap)
 {
     typedef StringSet<CharString> TNameStore;
     typedef NameStoreCache<TNameStore> TNameStoreCache;
@@ -41,6 +43,7 @@ int64_t ref_write_sam(int64_t n, const char * qname, const int64_t * qoff, const
         r.tLen = tlen[k];
         r.seq = std::string(seq + soff[k], seq + soff[k + 1]);
         r.qual = std::string(qual + quoff[k], qual + quoff[k + 1]);
+        if (toff) r.tags = std::string(tags + toff[k], tags + toff[k + 1]);
         write(text, r, context, Sam());
     }
     const int64_t len = int64_t(length(text));

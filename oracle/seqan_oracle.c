@@ -1195,13 +1195,92 @@ static int sam_num(char *p, int64_t v)
     return k;
 }
 
-/* write(target, record, context, Sam()) of bam_io/write_sam.h:126-217 (no tags); p == NULL only
- * counts. */
+/* appendTagsBamToSam (bam_io/bam_sam_conversion.h:250-360) on one record's BAM tag bytes: per tag
+ * the two name characters, ':', the type ('c', 's', 'i', 'C', 'S', 'I' all written as 'i'), ':'
+ * and the value -- Z and H strings up to their NUL, B arrays as the element type and ","-prefixed
+ * values, numbers in decimal, A as the character; tags separated by tabs.  p == NULL only counts.
+ * Returns -1 for bytes that are not well-formed tags and for float values (f, B:f), which this
+ * restatement does not format. */
+static int64_t tag_size(char t)
+{
+    switch (t) {
+    case 'A': case 'c': case 'C': return 1;
+    case 's': case 'S': return 2;
+    case 'i': case 'I': case 'f': return 4;
+    default: return 0;
+    }
+}
+
+static int64_t tag_num(const char *q, char t)
+{
+    const unsigned char *u = (const unsigned char *)q;
+    const uint32_t v = (uint32_t)u[0] | ((uint32_t)u[1] << 8) | ((uint32_t)u[2] << 16) | ((uint32_t)u[3] << 24);
+    switch (t) {
+    case 'c': return (int8_t)u[0];
+    case 'C': return u[0];
+    case 's': return (int16_t)(uint16_t)(u[0] | (u[1] << 8));
+    case 'S': return (uint16_t)(u[0] | (u[1] << 8));
+    case 'i': return (int32_t)v;
+    default: return v;   /* 'I' */
+    }
+}
+
+static int64_t sam_tags(char *p, const char *t, int64_t len)
+{
+    int64_t w = 0, i = 0;
+#define TPUT(c) do { if (p) p[w] = (c); ++w; } while (0)
+    while (i < len) {
+        char ty, lo;
+        if (i + 3 > len) return -1;
+        TPUT(t[i]);
+        TPUT(t[i + 1]);
+        TPUT(':');
+        ty = t[i + 2];
+        lo = (ty >= 'A' && ty <= 'Z') ? (char)(ty + 32) : ty;
+        TPUT((lo == 'c' || lo == 's' || lo == 'i') ? 'i' : ty);
+        TPUT(':');
+        i += 3;
+        if (ty == 'Z' || ty == 'H') {
+            while (i < len && t[i] != 0) { TPUT(t[i]); ++i; }
+            if (i >= len) return -1;
+            ++i;
+        } else if (ty == 'B') {
+            char et;
+            uint32_t cnt, e;
+            int64_t sz;
+            if (i + 5 > len) return -1;
+            et = t[i];
+            sz = tag_size(et);
+            if (sz == 0 || et == 'f' || et == 'A') return -1;
+            TPUT(et);
+            cnt = (uint32_t)tag_num(t + i + 1, 'I');
+            i += 5;
+            if ((int64_t)cnt * sz > len - i) return -1;
+            for (e = 0; e < cnt; ++e) {
+                TPUT(',');
+                w += sam_num(p ? p + w : NULL, tag_num(t + i, et));
+                i += sz;
+            }
+        } else {
+            const int64_t sz = tag_size(ty);
+            if (sz == 0 || ty == 'f' || i + sz > len) return -1;
+            if (ty == 'A') TPUT(t[i]);
+            else w += sam_num(p ? p + w : NULL, tag_num(t + i, ty));
+            i += sz;
+        }
+        if (i < len) TPUT('\t');
+    }
+#undef TPUT
+    return w;
+}
+
+/* write(target, record, context, Sam()) of bam_io/write_sam.h:126-217; p == NULL only counts. */
 static int64_t sam_line(char *p, int64_t k, const char *qname, const int64_t *qoff, const uint16_t *flag,
                         const int32_t *rid, const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar,
                         const int64_t *coff, const int32_t *rnext, const int32_t *pnext, const int32_t *tlen,
                         const uint8_t *seq, const int64_t *soff, const char *letters, const char *qual,
-                        const int64_t *quoff, const char *cnames, const int64_t *cnoff)
+                        const int64_t *quoff, const char *cnames, const int64_t *cnoff, const char *tags,
+                        const int64_t *toff)
 {
     int64_t w = 0, i;
 #define PUT(c) do { if (p) p[w] = (c); ++w; } while (0)
@@ -1234,6 +1313,13 @@ static int64_t sam_line(char *p, int64_t k, const char *qname, const int64_t *qo
     PUT('\t');
     if (!quoff || quoff[k] == quoff[k + 1]) PUT('*');
     else for (i = quoff[k]; i < quoff[k + 1]; ++i) PUT(qual[i]);
+    if (toff && toff[k + 1] > toff[k]) {
+        int64_t tl;
+        PUT('\t');
+        tl = sam_tags(p ? p + w : NULL, tags + toff[k], toff[k + 1] - toff[k]);
+        if (tl < 0) return -1;
+        w += tl;
+    }
     PUT('\n');
 #undef PUT
 #undef NUM
@@ -1244,11 +1330,12 @@ int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const u
                       const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
                       const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
                       const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
-                      int64_t ncontigs, const char *cnames, const int64_t *cnoff, char *out, int64_t cap,
-                      int32_t threads)
+                      int64_t ncontigs, const char *cnames, const int64_t *cnoff, const char *tags,
+                      const int64_t *toff, char *out, int64_t cap, int32_t threads)
 {
     int64_t k, total;
     int64_t *off;
+    int bad = 0;
     (void)ncontigs;
     if (n < 0) return -1;
     if (threads <= 0) threads = omp_get_max_threads();
@@ -1257,14 +1344,18 @@ int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const u
 #pragma omp parallel for schedule(static) num_threads(threads)
     for (k = 0; k < n; ++k)
         off[k + 1] = sam_line(NULL, k, qname, qoff, flag, rid, pos, mapq, cigar, coff, rnext, pnext, tlen, seq,
-                              soff, letters, qual, quoff, cnames, cnoff);
-    for (k = 0; k < n; ++k) off[k + 1] += off[k];
+                              soff, letters, qual, quoff, cnames, cnoff, tags, toff);
+    for (k = 0; k < n; ++k) {
+        if (off[k + 1] < 0) bad = 1;
+        off[k + 1] += off[k];
+    }
+    if (bad) { free(off); return -1; }
     total = off[n];
     if (out && total <= cap) {
 #pragma omp parallel for schedule(static) num_threads(threads)
         for (k = 0; k < n; ++k)
             sam_line(out + off[k], k, qname, qoff, flag, rid, pos, mapq, cigar, coff, rnext, pnext, tlen, seq, soff,
-                     letters, qual, quoff, cnames, cnoff);
+                     letters, qual, quoff, cnames, cnoff, tags, toff);
     }
     free(off);
     return total;
@@ -1412,7 +1503,7 @@ int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const u
                       const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
                       const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
                       const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
-                      char *out, int64_t cap, int32_t threads)
+                      const char *tags, const int64_t *toff, char *out, int64_t cap, int32_t threads)
 {
     int64_t k, total;
     int64_t *off;
@@ -1424,7 +1515,8 @@ int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const u
     off[0] = 0;
     for (k = 0; k < n; ++k) {
         const int64_t lq = qoff[k + 1] - qoff[k], nc = coff[k + 1] - coff[k], ls = soff[k + 1] - soff[k];
-        off[k + 1] = off[k] + 4 + 32 + lq + 1 + 4 * nc + (ls + 1) / 2 + ls;
+        const int64_t lt = toff ? toff[k + 1] - toff[k] : 0;
+        off[k + 1] = off[k] + 4 + 32 + lq + 1 + 4 * nc + (ls + 1) / 2 + ls + lt;
     }
     total = off[n];
     if (out && total <= cap) {
@@ -1433,6 +1525,7 @@ int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const u
             char *p = out + off[k];
             const int64_t lq = qoff[k + 1] - qoff[k], nc = coff[k + 1] - coff[k], ls = soff[k + 1] - soff[k];
             const int64_t lqual = quoff ? quoff[k + 1] - quoff[k] : 0;
+            const int64_t lt = toff ? toff[k + 1] - toff[k] : 0;
             uint32_t l = 0, bin;
             int64_t i;
             for (i = coff[k]; i < coff[k + 1]; ++i) {
@@ -1440,7 +1533,7 @@ int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const u
                 if (op != 1 && op != 4 && op != 5) l += cigar[i] >> 4;
             }
             bin = orc_reg2bin((uint32_t)pos[k], (uint32_t)pos[k] + (l > 1 ? l : 1u)) & 0xffffu;
-            orc_put32(p, (uint32_t)(32 + ((lq + 1) & 0xff) + 4 * (nc & 0xffff) + (ls + 1) / 2 + ls));
+            orc_put32(p, (uint32_t)(32 + ((lq + 1) & 0xff) + 4 * (nc & 0xffff) + (ls + 1) / 2 + ls + lt));
             orc_put32(p + 4, (uint32_t)rid[k]);
             orc_put32(p + 8, (uint32_t)pos[k]);
             orc_put32(p + 12, (uint32_t)((lq + 1) & 0xff) | ((uint32_t)mapq[k] << 8) | (bin << 16));
@@ -1458,6 +1551,7 @@ int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const u
                 *p++ = (char)((iu[seq[soff[k] + i] & 31] << 4) | iu[seq[soff[k] + i + 1] & 31]);
             if (ls & 1) *p++ = (char)(iu[seq[soff[k] + ls - 1] & 31] << 4);
             for (i = 0; i < ls; ++i) *p++ = i < lqual ? (char)(qual[quoff[k] + i] - '!') : (char)0xff;
+            if (lt) memcpy(p, tags + toff[k], (size_t)lt);   /* the tags as they are (write_bam.h:202-203) */
         }
     }
     free(off);

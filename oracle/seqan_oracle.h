@@ -126,23 +126,25 @@ int orc_extend_seeds(const orc_xdrop_params *p, int64_t n_h, const uint8_t *seq_
                      const int32_t *seed_h, const int32_t *seed_v, orc_seed *seeds, int32_t *xscores,
                      int32_t threads);
 
-/* SAM lines of BamAlignmentRecord fields (bam_io/write_sam.h:126-217), no tags: record k's
- * fields as in the engine's gba_sam_records.  Returns the text length (the text is written when
- * it fits cap), or -1.  threads <= 0: all. */
+/* SAM lines of BamAlignmentRecord fields (bam_io/write_sam.h:126-217): record k's fields as in
+ * the engine's gba_sam_records, its BAM tag bytes tags[toff[k], toff[k+1]) (toff NULL: none)
+ * written as appendTagsBamToSam writes them.  Returns the text length (the text is written when it
+ * fits cap), or -1 (also for malformed tags and float tag values).  threads <= 0: all. */
 int64_t orc_write_sam(int64_t n, const char *qname, const int64_t *qoff, const uint16_t *flag, const int32_t *rid,
                       const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
                       const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
                       const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
-                      int64_t ncontigs, const char *cnames, const int64_t *cnoff, char *out, int64_t cap,
-                      int32_t threads);
+                      int64_t ncontigs, const char *cnames, const int64_t *cnoff, const char *tags,
+                      const int64_t *toff, char *out, int64_t cap, int32_t threads);
 
-/* BAM records of the same fields (bam_io/write_bam.h:100-271, no tags): the uncompressed record
- * blocks.  Returns the byte length (the bytes are written when they fit cap), or -1. */
+/* BAM records of the same fields (bam_io/write_bam.h:100-271): the uncompressed record blocks,
+ * each record's tag bytes at its end.  Returns the byte length (the bytes are written when they
+ * fit cap), or -1. */
 int64_t orc_write_bam(int64_t n, const char *qname, const int64_t *qoff, const uint16_t *flag, const int32_t *rid,
                       const int32_t *pos, const uint8_t *mapq, const uint32_t *cigar, const int64_t *coff,
                       const int32_t *rnext, const int32_t *pnext, const int32_t *tlen, const uint8_t *seq,
                       const int64_t *soff, const char *letters, const char *qual, const int64_t *quoff,
-                      char *out, int64_t cap, int32_t threads);
+                      const char *tags, const int64_t *toff, char *out, int64_t cap, int32_t threads);
 
 /* Records of FASTA (format 0) or FASTQ (format 1) text as the reference's readRecord loop reads
  * them (seq_io/fasta_fastq.h:265-283, :354-392), alphabet 4 Dna, 5 Dna5, 27 AminoAcid: record k's

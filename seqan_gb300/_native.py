@@ -187,7 +187,8 @@ class GbaSamRecords(C.Structure):
                 ("cigar_off", C.c_void_p), ("next_ref_id", C.c_void_p), ("next_pos", C.c_void_p),
                 ("tlen", C.c_void_p), ("seq", C.c_void_p), ("seq_off", C.c_void_p), ("seq_letters", C.c_void_p),
                 ("qual", C.c_void_p), ("qual_off", C.c_void_p), ("contig_names", C.c_void_p),
-                ("contig_off", C.c_void_p), ("num_contigs", C.c_int64)]
+                ("contig_off", C.c_void_p), ("num_contigs", C.c_int64), ("tags", C.c_void_p),
+                ("tags_off", C.c_void_p)]
 
 
 class GbaSeqRecords(C.Structure):

@@ -195,8 +195,17 @@ struct Engine {
                 if (pl->vlen[q] < n4[q]) pl->vlen[q] = n4[q];
                 continue;
             }
+#ifdef __CUDA_ARCH__
+            if (warp) {
+                for (int i = lane; i < n4[q]; i += 32) w.v4[q][i] = Cell{INF, INF, INF};
+                continue;
+            }
+#endif
             for (int i = 0; i < n4[q]; ++i) w.v4[q][i] = Cell{INF, INF, INF};
         }
+#ifdef __CUDA_ARCH__
+        if (warp) __syncwarp();
+#endif
         if (plan) return;
         for (int i = 0; i < nset; ++i) {
             const InitCell &e = w.set[i];

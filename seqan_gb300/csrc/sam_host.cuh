@@ -26,6 +26,8 @@ struct SamArgs {
     const char *cnames;
     const int64_t *cname_off;
     int64_t num_contigs;
+    const char *tags;           // BAM-form tag bytes of every record, back to back
+    const int64_t *tags_off;    // null: no record has tags
 };
 
 __device__ __forceinline__ int dec_digits_u(uint64_t v)
@@ -54,6 +56,110 @@ __device__ __forceinline__ char *dec_write(char *p, int64_t v)
     return p + d;
 }
 
+// --- tags: appendTagsBamToSam (bam_io/bam_sam_conversion.h:250-360) ---------------------------
+__host__ __device__ __forceinline__ int tag_size(char t)
+{
+    switch (t) {
+    case 'A': case 'c': case 'C': return 1;
+    case 's': case 'S': return 2;
+    case 'i': case 'I': case 'f': return 4;
+    default: return 0;
+    }
+}
+
+__host__ __device__ __forceinline__ int64_t tag_value(const char *q, char t)
+{
+    const unsigned char *u = reinterpret_cast<const unsigned char *>(q);
+    const uint32_t v = uint32_t(u[0]) | (uint32_t(u[1]) << 8) | (uint32_t(u[2]) << 16) | (uint32_t(u[3]) << 24);
+    switch (t) {
+    case 'c': return int8_t(u[0]);
+    case 'C': return u[0];
+    case 's': return int16_t(uint16_t(u[0] | (u[1] << 8)));
+    case 'S': return uint16_t(u[0] | (u[1] << 8));
+    case 'i': return int32_t(v);
+    default: return v;   // 'I'
+    }
+}
+
+// 0 when t[0, len) are tags the SAM writer formats here; 1 malformed; 2 a float value.
+inline int tags_check(const char *t, int64_t len)
+{
+    int64_t i = 0;
+    while (i < len) {
+        if (i + 3 > len) return 1;
+        const char ty = t[i + 2];
+        i += 3;
+        if (ty == 'Z' || ty == 'H') {
+            while (i < len && t[i] != 0) ++i;
+            if (i >= len) return 1;
+            ++i;
+        } else if (ty == 'B') {
+            if (i + 5 > len) return 1;
+            const char et = t[i];
+            const int sz = tag_size(et);
+            if (et == 'f') return 2;
+            if (sz == 0 || et == 'A') return 1;
+            const int64_t cnt = tag_value(t + i + 1, 'I');
+            i += 5;
+            if (cnt * sz > len - i) return 1;
+            i += cnt * sz;
+        } else {
+            const int sz = tag_size(ty);
+            if (ty == 'f') return 2;
+            if (sz == 0 || i + sz > len) return 1;
+            i += sz;
+        }
+    }
+    return 0;
+}
+
+// The SAM text of checked tags; w == nullptr only counts.
+__device__ int64_t sam_tags_text(const char *t, int64_t len, char *w)
+{
+    int64_t n = 0, i = 0;
+    auto put = [&](char c) {
+        if (w) w[n] = c;
+        ++n;
+    };
+    auto num = [&](int64_t v) {
+        if (w) dec_write(w + n, v);
+        n += dec_len(v);
+    };
+    while (i < len) {
+        put(t[i]);
+        put(t[i + 1]);
+        put(':');
+        const char ty = t[i + 2];
+        const char lo = (ty >= 'A' && ty <= 'Z') ? char(ty + 32) : ty;
+        put((lo == 'c' || lo == 's' || lo == 'i') ? 'i' : ty);
+        put(':');
+        i += 3;
+        if (ty == 'Z' || ty == 'H') {
+            while (t[i] != 0) put(t[i++]);
+            ++i;
+        } else if (ty == 'B') {
+            const char et = t[i];
+            const int sz = tag_size(et);
+            put(et);
+            const int64_t cnt = tag_value(t + i + 1, 'I');
+            i += 5;
+            for (int64_t e = 0; e < cnt; ++e) {
+                put(',');
+                num(tag_value(t + i, et));
+                i += sz;
+            }
+        } else if (ty == 'A') {
+            put(t[i]);
+            i += 1;
+        } else {
+            num(tag_value(t + i, ty));
+            i += tag_size(ty);
+        }
+        if (i < len) put('\t');
+    }
+    return n;
+}
+
 __device__ __forceinline__ int64_t contig_len(const SamArgs &a, int32_t id)
 {
     return (id < 0 || id >= a.num_contigs) ? 1 : a.cname_off[id + 1] - a.cname_off[id];
@@ -80,6 +186,10 @@ __device__ int64_t sam_line_len(const SamArgs &a, int64_t k)
     n += (sl == 0 ? 1 : sl) + 1;
     const int64_t ql = a.qual_off ? a.qual_off[k + 1] - a.qual_off[k] : 0;
     n += (ql == 0 ? 1 : ql) + 1;
+    if (a.tags_off) {
+        const int64_t t0 = a.tags_off[k], tl = a.tags_off[k + 1] - t0;
+        if (tl) n += 1 + sam_tags_text(a.tags + t0, tl, nullptr);
+    }
     return n;
 }
 
@@ -162,7 +272,13 @@ __global__ void __launch_bounds__(128) k_sam_write(SamArgs a, const int64_t *lin
         for (int64_t i = lane; i < ul; i += 32) p[i] = a.qual[u0 + i];
         p += ul;
     }
-    if (lane == 0) p[0] = '\n';
+    if (lane == 0) {
+        if (a.tags_off && a.tags_off[k + 1] > a.tags_off[k]) {
+            *p++ = '\t';
+            p += sam_tags_text(a.tags + a.tags_off[k], a.tags_off[k + 1] - a.tags_off[k], p);
+        }
+        p[0] = '\n';
+    }
 }
 
 // --- BAM: write(target, record, context, Bam()) without tags (bam_io/write_bam.h:100-271) --------
@@ -204,7 +320,8 @@ __global__ void __launch_bounds__(128) k_bam_lengths(BamArgs b, int64_t *len)
     const int64_t lq = b.s.qname_off[k + 1] - b.s.qname_off[k];
     const int64_t nc = b.s.cigar_off[k + 1] - b.s.cigar_off[k];
     const int64_t ls = b.s.seq_off[k + 1] - b.s.seq_off[k];
-    len[k] = 36 + lq + 1 + 4 * nc + (ls + 1) / 2 + ls;
+    const int64_t lt = b.s.tags_off ? b.s.tags_off[k + 1] - b.s.tags_off[k] : 0;
+    len[k] = 36 + lq + 1 + 4 * nc + (ls + 1) / 2 + ls + lt;
 }
 
 __global__ void __launch_bounds__(128) k_bam_write(BamArgs b, const int64_t *rec_off, char *out)
@@ -221,6 +338,7 @@ __global__ void __launch_bounds__(128) k_bam_write(BamArgs b, const int64_t *rec
     const int64_t s0 = b.s.seq_off[k], ls = b.s.seq_off[k + 1] - s0;
     const int64_t u0 = b.s.qual_off ? b.s.qual_off[k] : 0;
     const int64_t lqual = b.s.qual_off ? b.s.qual_off[k + 1] - u0 : 0;
+    const int64_t t0 = b.s.tags_off ? b.s.tags_off[k] : 0, lt = b.s.tags_off ? b.s.tags_off[k + 1] - t0 : 0;
     if (lane == 0) {
         uint32_t l = 0;
         for (int64_t i = c0; i < c0 + nc; ++i) {
@@ -229,7 +347,7 @@ __global__ void __launch_bounds__(128) k_bam_write(BamArgs b, const int64_t *rec
         }
         const uint32_t beg = uint32_t(b.s.pos[k]);
         const uint32_t bin = bam_reg2bin(beg, beg + (l > 1u ? l : 1u)) & 0xffffu;
-        bam_put32(p, uint32_t(32 + ((lq + 1) & 0xff) + 4 * (nc & 0xffff) + (ls + 1) / 2 + ls));
+        bam_put32(p, uint32_t(32 + ((lq + 1) & 0xff) + 4 * (nc & 0xffff) + (ls + 1) / 2 + ls + lt));
         bam_put32(p + 4, uint32_t(b.s.ref_id[k]));
         bam_put32(p + 8, beg);
         bam_put32(p + 12, uint32_t((lq + 1) & 0xff) | (uint32_t(b.s.mapq[k]) << 8) | (bin << 16));
@@ -253,6 +371,8 @@ __global__ void __launch_bounds__(128) k_bam_write(BamArgs b, const int64_t *rec
     }
     q += pairs;
     for (int64_t i = lane; i < ls; i += 32) q[i] = i < lqual ? char(b.s.qual[u0 + i] - '!') : char(0xff);
+    q += ls;
+    for (int64_t i = lane; i < lt; i += 32) q[i] = b.s.tags[t0 + i];   // the tags as they are
 }
 
 // ordValue(Iupac(c)): the position of the upper-cased letter in "=ACMGRSVTWYHKDBN", 'U' as '=',
@@ -293,6 +413,8 @@ inline int sam_upload(gba_context *ctx, const gba_sam_records *r, SamArgs &a)
     const int64_t qn = r->qname_off[n], cn = r->cigar_off[n], sn = r->seq_off[n];
     const int64_t un = r->qual_off ? r->qual_off[n] : 0;
     const int64_t nc = r->num_contigs, cnb = nc ? r->contig_off[nc] : 0;
+    const int64_t tn = r->tags_off ? r->tags_off[n] : 0;
+    if (tn > 0 && !r->tags) return fail(ctx, GBA_EINVAL, "null tags");
     const Up ups[] = {{r->qname, size_t(qn)},           {r->qname_off, size_t(n + 1) * 8},
                       {r->flag, size_t(n) * 2},         {r->ref_id, size_t(n) * 4},
                       {r->pos, size_t(n) * 4},          {r->next_ref_id, size_t(n) * 4},
@@ -301,7 +423,8 @@ inline int sam_upload(gba_context *ctx, const gba_sam_records *r, SamArgs &a)
                       {r->cigar_off, size_t(n + 1) * 8}, {r->seq, size_t(sn)},
                       {r->seq_off, size_t(n + 1) * 8},  {r->seq_letters, 32},
                       {r->qual, size_t(un)},            {r->qual_off, r->qual_off ? size_t(n + 1) * 8 : 0},
-                      {r->contig_names, size_t(cnb)},   {r->contig_off, nc ? size_t(nc + 1) * 8 : 0}};
+                      {r->contig_names, size_t(cnb)},   {r->contig_off, nc ? size_t(nc + 1) * 8 : 0},
+                      {r->tags, size_t(tn)},            {r->tags_off, r->tags_off ? size_t(n + 1) * 8 : 0}};
     size_t total = 0;
     size_t at[sizeof(ups) / sizeof(ups[0])];
     for (size_t i = 0; i < sizeof(ups) / sizeof(ups[0]); ++i) {
@@ -334,6 +457,8 @@ inline int sam_upload(gba_context *ctx, const gba_sam_records *r, SamArgs &a)
     a.cnames = base + at[16];
     a.cname_off = reinterpret_cast<const int64_t *>(base + at[17]);
     a.num_contigs = nc;
+    a.tags = base + at[18];
+    a.tags_off = r->tags_off ? reinterpret_cast<const int64_t *>(base + at[19]) : nullptr;
     return GBA_OK;
 }
 
@@ -349,6 +474,14 @@ GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out
     if (n < 0) return fail(ctx, GBA_EINVAL, "negative record count");
     line_off[0] = 0;
     if (n == 0) return GBA_OK;
+    if (r->tags_off) {
+        for (int64_t k = 0; k < n; ++k) {
+            if (r->tags_off[k + 1] < r->tags_off[k]) return fail(ctx, GBA_EINVAL, "record %lld: bad tag offsets", (long long)k);
+            const int c = r->tags ? tags_check(r->tags + r->tags_off[k], r->tags_off[k + 1] - r->tags_off[k]) : 0;
+            if (c == 1) return fail(ctx, GBA_EINVAL, "record %lld: malformed tags", (long long)k);
+            if (c == 2) return fail(ctx, GBA_EUNSUPPORTED, "record %lld: float tag values are not written", (long long)k);
+        }
+    }
     SamArgs a{};
     if (int rc = sam_upload(ctx, r, a)) return rc;
     cudaStream_t st = ctx->stream;

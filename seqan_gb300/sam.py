@@ -45,6 +45,14 @@ class SamRecords:
     qual: list | None      # per record: str, or None for '*'
     contigs: list          # contig names
     letters: str = "ACGTN"
+    tags: list | None = None   # per record: BamAlignmentRecord.tags bytes (BAM form), or None
+
+
+def _tags(rec: SamRecords):
+    if rec.tags is None:
+        return None, None
+    tb = [bytes(t) for t in rec.tags]
+    return _cat([np.frombuffer(t, np.uint8) for t in tb], np.uint8), _off(tb)
 
 
 def _records_struct(rec: SamRecords):
@@ -71,13 +79,15 @@ def _records_struct(rec: SamRecords):
     r = N.GbaSamRecords(n, p(qname), p(qoff), p(arrs["flag"]), p(arrs["ref_id"]), p(arrs["pos"]), p(arrs["mapq"]),
                         p(cig), p(coff), p(arrs["next_ref_id"]), p(arrs["next_pos"]), p(arrs["tlen"]), p(seq),
                         p(soff), p(letters), p(qual), p(quoff), p(cnames), p(cnoff), len(rec.contigs))
-    keep = [qname, qoff, cig, coff, seq, soff, letters, qual, quoff, cnames, cnoff, arrs]
+    tags, toff = _tags(rec)
+    r.tags, r.tags_off = p(tags), p(toff)
+    keep = [qname, qoff, cig, coff, seq, soff, letters, qual, quoff, cnames, cnoff, arrs, tags, toff]
     return r, keep
 
 
 def format_bam(rec: SamRecords, ctx=None) -> bytes:
     """The records' uncompressed BAM blocks as the reference's BAM writer writes them
-    (bam_io/write_bam.h:100-271, no tags), formatted on the device (gba_format_bam)."""
+    (bam_io/write_bam.h:100-271, tags appended as they are), formatted on the device (gba_format_bam)."""
     ctx = ctx or N.default_context()
     n = len(rec.qname)
     r, keep = _records_struct(rec)
@@ -116,6 +126,8 @@ def format_sam(rec: SamRecords, ctx=None) -> str:
     r = N.GbaSamRecords(n, p(qname), p(qoff), p(arrs["flag"]), p(arrs["ref_id"]), p(arrs["pos"]), p(arrs["mapq"]),
                         p(cig), p(coff), p(arrs["next_ref_id"]), p(arrs["next_pos"]), p(arrs["tlen"]), p(seq),
                         p(soff), p(letters), p(qual), p(quoff), p(cnames), p(cnoff), len(rec.contigs))
+    tags, toff = _tags(rec)
+    r.tags, r.tags_off = p(tags), p(toff)
     line_off = np.zeros(n + 1, dtype=np.int64)
     rc = N.lib().gba_format_sam(ctx.handle, C.byref(r), None, 0, line_off.ctypes.data)
     if rc not in (N.GBA_OK, N.GBA_ECAPACITY):

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|packed|sam|seqio|bam|cpp|dynamic|banded_chain]
+    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|packed|sam|seqio|bam|cpp|dynamic|banded_chain|tags]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -130,6 +130,9 @@ def main():
         return
     if only == "banded_chain":
         write_banded_chain()
+        return
+    if only == "tags":
+        write_tag_cases()
         return
     rng = np.random.Generator(np.random.PCG64(20261203))
     cases = []
@@ -307,6 +310,59 @@ def write_sam_cases():
                    "tlen": rec.tlen.tolist(), "seq": [s.tolist() for s in rec.seq], "qual": rec.qual,
                    "text": text}, f, separators=(",", ":"))
     print(f"{len(rec.qname)} SAM records written")
+
+
+def random_tags(rng, floats=False):
+    """BAM-form tag bytes: 0-5 tags of every type the SAM conversion writes (A, c, C, s, S, i, I,
+    Z, H, B arrays of integers; f and B:f when floats)."""
+    import struct
+    out = b""
+    kinds = list("AcCsSiIZHB") + (["f", "Bf"] if floats else [])
+    for _ in range(int(rng.integers(0, 6))):
+        name = bytes([int(rng.integers(65, 91)), int(rng.integers(48, 91))])
+        kd = kinds[int(rng.integers(0, len(kinds)))]
+        if kd == "A":
+            out += name + b"A" + bytes([int(rng.integers(33, 127))])
+        elif kd in "cCsSiI":
+            fmt = {"c": "<b", "C": "<B", "s": "<h", "S": "<H", "i": "<i", "I": "<I"}[kd]
+            lo, hi = {"c": (-128, 128), "C": (0, 256), "s": (-32768, 32768), "S": (0, 65536),
+                      "i": (-2 ** 31, 2 ** 31), "I": (0, 2 ** 32)}[kd]
+            out += name + kd.encode() + struct.pack(fmt, int(rng.integers(lo, hi)))
+        elif kd in "ZH":
+            ln = int(rng.integers(0, 12))
+            alphabet = b"0123456789ABCDEF" if kd == "H" else bytes(range(33, 127))
+            out += name + kd.encode() + bytes(alphabet[int(x)] for x in rng.integers(0, len(alphabet), ln)) + b"\0"
+        elif kd == "f":
+            out += name + b"f" + struct.pack("<f", float(rng.normal()))
+        else:
+            et = "f" if kd == "Bf" else "cCsSiI"[int(rng.integers(0, 6))]
+            cnt = int(rng.integers(0, 6))
+            fmt = {"c": "<b", "C": "<B", "s": "<h", "S": "<H", "i": "<i", "I": "<I", "f": "<f"}[et]
+            lim = {"c": 127, "C": 255, "s": 32767, "S": 65535, "i": 2 ** 31 - 1, "I": 2 ** 32 - 1, "f": 1}[et]
+            vals = [float(rng.normal()) if et == "f" else int(rng.integers(0 if et.isupper() else -lim, lim))
+                    for _ in range(cnt)]
+            out += name + b"B" + et.encode() + struct.pack("<I", cnt) + b"".join(struct.pack(fmt, x) for x in vals)
+    return out
+
+
+def write_tag_cases():
+    """SAM lines and BAM records with tags, through the reference's writers (appendTagsBamToSam and
+    the raw tag bytes of write_bam.h)."""
+    import base64
+    rng = np.random.Generator(np.random.PCG64(20261211))
+    rec = sam_records(rng, 300)
+    rec.tags = [random_tags(rng) for _ in rec.qname]
+    text = O.ref_write_sam(rec)
+    data = O.ref_write_bam(rec)
+    with open(os.path.join(HERE, "sam_tag_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only tags", "seed": 20261211, "contigs": rec.contigs,
+                   "qname": rec.qname, "flag": rec.flag.tolist(), "ref_id": rec.ref_id.tolist(),
+                   "pos": rec.pos.tolist(), "mapq": rec.mapq.tolist(), "cigar": [list(map(int, c)) for c in rec.cigar],
+                   "next_ref_id": rec.next_ref_id.tolist(), "next_pos": rec.next_pos.tolist(),
+                   "tlen": rec.tlen.tolist(), "seq": [s.tolist() for s in rec.seq], "qual": rec.qual,
+                   "tags": [base64.b64encode(t).decode() for t in rec.tags], "text": text,
+                   "bam": base64.b64encode(data).decode()}, f, separators=(",", ":"))
+    print(f"{len(rec.qname)} SAM/BAM records with tags written")
 
 
 def write_packed():
