@@ -74,6 +74,7 @@ struct ColDesc {
     int r0, r1;
     int64_t pos0;
     int leap;
+    int hcol, vrow0;   // storage column and storage row of the first cell (a column never wraps)
     int8_t type, loc, single, present;
 };
 
@@ -953,6 +954,7 @@ struct Engine {
             leap = 1;
             pos = 0;
         }
+        if (L * Hlen >= (int64_t(1) << 31)) { fail(ST_CAPACITY); return INT_MIN; }   // positions are 32-bit
         if (plan) {
             if (bd) {
                 for (int64_t j = 0; j <= pm; ++j) {
@@ -1020,6 +1022,9 @@ struct Engine {
         d.r1 = single ? r0 : r1;
         d.pos0 = p;
         d.leap = int(lp);
+        d.hcol = int(p / L);
+        d.vrow0 = int(p % L);
+        if (!single && d.vrow0 + (r1 - r0) >= L) { fail(ST_UNDEFINED); return; }
         d.type = int8_t(coltype);
         d.loc = int8_t(loc);
         d.single = single;
@@ -1104,95 +1109,93 @@ struct Engine {
         }
     }
 
-    __host__ __device__ bool computed(int c, int r, int cfirst, int clast) const
+    // the cells of anti-diagonal d that lane l takes; k3 / k1 / k2: the rolling slots of d, d - 1, d - 2
+    __host__ __device__ void fill_diag(int d, int l, int cfirst, int clast, int k3, int k1, int k2)
     {
-        if (c < cfirst || c > clast) return false;
-        const ColDesc &d = w.cols[c];
-        return d.present && r >= d.r0 && r <= d.r1;
-    }
-
-    // the cells of anti-diagonal d that lane l takes
-    __host__ __device__ void fill_diag(int64_t d, int l, int cfirst, int clast)
-    {
-        const int k3 = int(d % 3), k1 = int((d + 2) % 3), k2 = int((d + 1) % 3);   // d, d - 1, d - 2
-        const int cap = pl->col_cap;
-        int64_t clo = cmax<int64_t>(cfirst, d - gn), chi = cmin<int64_t>(clast, d);
+        const int cap = pl->col_cap, gnn = gn, Li = int(L);
+        const int hN = int(hNext), vN = int(vNext);
+        const bool finalM = kind == KIND_FINAL;
+        const bool freeB = (fe & FREE_BOTTOM) != 0, freeR = (fe & FREE_RIGHT) != 0;
+        const ColDesc *cols = w.cols;
+        int *aS = w.aS, *aE = w.aE, *aF = w.aF;
+        int clo = cmax(cfirst, d - gnn), chi = cmin(clast, d);
         if (banded) {
-            clo = cmax(clo, -floor2(-(d + lower)));
-            chi = cmin(chi, floor2(d + upper));
+            clo = cmax(clo, int(-floor2(-(int64_t(d) + lower))));
+            chi = cmin(chi, int(floor2(int64_t(d) + upper)));
         }
-        for (int64_t c64 = clo + l; c64 <= chi; c64 += 32) {
-            const int c = int(c64), r = int(d - c64);
-            if (!computed(c, r, cfirst, clast)) continue;
-            const ColDesc &cd = w.cols[c];
+        for (int c = clo + l; c <= chi; c += 32) {
+            const int r = d - c;
+            const ColDesc cd = cols[c];
+            if (!cd.present || r < cd.r0 || r > cd.r1) continue;
             const int cellk = (r == cd.r0) ? CELL_FIRST : (r == cd.r1 ? CELL_LAST : CELL_INNER);
-            const int64_t p = cd.pos0 + (r - cd.r0);
-            const int64_t lp = cd.leap + ((cellk == CELL_LAST && cd.loc == LOC_BOTTOM && cd.type != COL_INITIAL) ? 1 : 0);
-            if (p < 0 || p >= L * Hlen) { fail(ST_UNDEFINED); continue; }
-            const bool hv = computed(c - 1, r, cfirst, clast);
-            const int hS = hv ? w.aS[k1 * cap + c - 1] : INF, hE = hv ? w.aE[k1 * cap + c - 1] : INF;
+            const int dr = r - cd.r0;
+            const int p = int(cd.pos0) + dr;
+            const int lp = cd.leap + ((cellk == CELL_LAST && cd.loc == LOC_BOTTOM && cd.type != COL_INITIAL) ? 1 : 0);
+            // the previous column's computed rows
+            bool hv = false, dv = false;
+            if (c > cfirst) {
+                const ColDesc &pc = cols[c - 1];
+                hv = pc.present && r >= pc.r0 && r <= pc.r1;
+                dv = pc.present && r - 1 >= pc.r0 && r - 1 <= pc.r1;
+            }
+            const int hS = hv ? aS[k1 * cap + c - 1] : INF, hE = hv ? aE[k1 * cap + c - 1] : INF;
             int kdS = INF, kvS = INF, kvF = INF;
             if (cellk != CELL_FIRST) {
-                kvS = w.aS[k1 * cap + c];
-                kvF = w.aF[k1 * cap + c];
-                if (computed(c - 1, r - 1, cfirst, clast)) kdS = w.aS[k2 * cap + c - 1];
-            } else if (cd.type != COL_INITIAL && (cd.loc == LOC_MIDDLE || cd.loc == LOC_BOTTOM) && r > 0 && c > 0) {
-                if (computed(c - 1, r - 1, cfirst, clast)) kdS = w.aS[k2 * cap + c - 1];
+                kvS = aS[k1 * cap + c];
+                kvF = aF[k1 * cap + c];
+                if (dv) kdS = aS[k2 * cap + c - 1];
+            } else if (cd.type != COL_INITIAL && (cd.loc == LOC_MIDDLE || cd.loc == LOC_BOTTOM) && r > 0 && dv) {
+                kdS = aS[k2 * cap + c - 1];
             }
             Cell cur{INF, INF, INF};
             int tv = T_NONE;
+            const int cV = cd.vrow0 + dr, cH = cd.hcol;
             if (cd.type == COL_INITIAL) {
-                const int64_t idx = (p % L) - (lp - 1);
+                const int idx = cV - (lp - 1);
                 if (idx < 0 || idx >= n4[1]) { fail(ST_UNDEFINED); continue; }
                 cur = w.v4[1][idx];
             } else if (cellk == CELL_FIRST && (cd.loc == LOC_TOP || cd.loc == LOC_FULL)) {
-                const int64_t idx = p / L;
-                if (idx >= n4[0]) { fail(ST_UNDEFINED); continue; }
-                cur = w.v4[0][idx];
+                if (cH >= n4[0]) { fail(ST_UNDEFINED); continue; }
+                cur = w.v4[0][cH];
             } else {
                 const int dir = (cellk == CELL_INNER) ? DIR_ALL
                               : (cellk == CELL_FIRST) ? DIR_UPPER
                               : (cd.loc == LOC_TOP || cd.loc == LOC_MIDDLE) ? DIR_LOWER : DIR_ALL;
                 tv = compute(dir, c, r, hS, hE, cur, kdS, kvS, kvF);
             }
-            w.aS[k3 * cap + c] = cur.s;
-            w.aE[k3 * cap + c] = cur.e;
-            w.aF[k3 * cap + c] = cur.f;
+            aS[k3 * cap + c] = cur.s;
+            aE[k3 * cap + c] = cur.e;
+            aF[k3 * cap + c] = cur.f;
             w.T[p] = uint8_t(tv);
+            if (cH < hN) continue;
             // the chain's tracking options
-            const int64_t cH = p / L, cV = p % L;
-            bool storeRow = false, storeCol = false, lastCol = false, lastRow = false;
-            const bool finalM = kind == KIND_FINAL;
-            if (cH >= hNext) {
-                if (cd.loc == LOC_BOTTOM) { if (cV + lp == vNext) storeRow = true; }
-                else if (cV == vNext) storeRow = true;
-                if (cH == hNext && cV >= vNext) storeCol = true;
-                if (cellk == CELL_LAST && (!finalM || (fe & FREE_BOTTOM))) lastRow = true;
-                if (cd.type == COL_FINAL) {
-                    if (cellk == CELL_LAST) { lastCol = true; lastRow = true; }
-                    else if (cd.loc != LOC_FULL || cV >= vNext) {
-                        if (!finalM || (fe & FREE_RIGHT)) lastCol = true;
-                    }
-                }
+            bool storeRow, lastCol = false, lastRow = false;
+            if (cd.loc == LOC_BOTTOM) storeRow = cV + lp == vN;
+            else storeRow = cV == vN;
+            const bool storeCol = cH == hN && cV >= vN;
+            if (cellk == CELL_LAST && (!finalM || freeB)) lastRow = true;
+            if (cd.type == COL_FINAL) {
+                if (cellk == CELL_LAST) { lastCol = true; lastRow = true; }
+                else if ((cd.loc != LOC_FULL || cV >= vN) && (!finalM || freeR)) lastCol = true;
             }
             if (storeCol) {
-                const int64_t q = cV - vNext;
+                const int q = cV - vN;
                 if (q >= n4[3]) { fail(ST_UNDEFINED); continue; }
                 w.v4[3][q] = cur;
             }
             if (storeRow) {
-                const int64_t q = cH - hNext;
+                const int q = cH - hN;
                 if (q >= n4[2]) { fail(ST_UNDEFINED); continue; }
                 w.v4[2][q] = cur;
             }
             if (lastCol || lastRow) {
                 if (cd.type == COL_FINAL) {
                     w.fcS[r] = cur.s;
-                    w.fcP[r] = int(p);
+                    w.fcP[r] = p;
                     w.fcF[r] = 1;
                 } else {
                     w.ccS[c] = cur.s;
-                    w.ccP[c] = int(p);
+                    w.ccP[c] = p;
                     w.ccF[c] = 1;
                 }
             }
@@ -1235,13 +1238,18 @@ struct Engine {
             dmin = cmin<int64_t>(dmin, int64_t(c) + cd.r0);
             dmax = cmax<int64_t>(dmax, int64_t(c) + cd.r1);
         }
-        for (int64_t d = dmin; d <= dmax; ++d) {
+        int k3 = int(dmin % 3), k1 = (k3 + 2) % 3, k2 = (k3 + 1) % 3;
+        for (int d = int(dmin); d <= int(dmax); ++d) {
 #ifdef __CUDA_ARCH__
-            fill_diag(d, lane, cfirst, clast);
+            fill_diag(d, lane, cfirst, clast, k3, k1, k2);
             __syncwarp();
 #else
-            for (int l = 0; l < 32; ++l) fill_diag(d, l, cfirst, clast);
+            for (int l = 0; l < 32; ++l) fill_diag(d, l, cfirst, clast, k3, k1, k2);
 #endif
+            const int t = k2;   // d + 1: its d - 1 is this d, its d - 2 this d - 1
+            k2 = k1;
+            k1 = k3;
+            k3 = t;
         }
 #ifdef __CUDA_ARCH__
         err = __reduce_max_sync(0xffffffffu, err);
