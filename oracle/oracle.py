@@ -648,7 +648,7 @@ def _we_rows(segments, h_text, v_text):
 
 
 def oracle_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, matrix=None, max_count=1000,
-                           letters="ACGTN") -> list:
+                           letters="ACGTN", band=None) -> list:
     """Waterman-Eggert alignments of the oracle restatement (orc_waterman_eggert): each with its
     score, gapped rows, clipped source positions and runs of alignment columns.  A trailing None
     marks an enumeration stopped where the reference's next step is undefined."""
@@ -672,8 +672,16 @@ def oracle_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, matrix=
     segs = np.zeros((cap, 4), np.uint32)
     off = np.zeros(max_count + 1, np.int64)
     undef = C.c_int32(0)
-    k = lib.orc_waterman_eggert(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), max_count, _ptr(scores),
-                                _ptr(begins), _ptr(ends), _ptr(segs), cap, _ptr(off), C.byref(undef))
+    if band is None:
+        k = lib.orc_waterman_eggert(C.byref(p), _ptr(h), len(h), _ptr(v), len(v), max_count, _ptr(scores),
+                                    _ptr(begins), _ptr(ends), _ptr(segs), cap, _ptr(off), C.byref(undef))
+    else:
+        lib.orc_waterman_eggert_banded.restype = C.c_int32
+        lib.orc_waterman_eggert_banded.argtypes = [C.POINTER(OrcWeParams), C.c_int32, C.c_int32] + \
+            lib.orc_waterman_eggert.argtypes[1:]
+        k = lib.orc_waterman_eggert_banded(C.byref(p), int(band[0]), int(band[1]), _ptr(h), len(h), _ptr(v), len(v),
+                                           max_count, _ptr(scores), _ptr(begins), _ptr(ends), _ptr(segs), cap,
+                                           _ptr(off), C.byref(undef))
     if k < 0:
         raise RuntimeError("segment buffer too small")
     ht = "".join(letters[int(c)] for c in h)
@@ -684,7 +692,7 @@ def oracle_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, matrix=
         r0, r1 = _we_rows(sg, ht, vt)
         # each row's clipped region starts at its first residue (after an alignment whose first
         # column is a gap the two rows differ in length, as the reference prints them)
-        r0, r1 = r0.lstrip("-"), r1.lstrip("-")
+        r0, r1 = r0.strip("-"), r1.strip("-")
         out.append(LocalAlignment(int(scores[i]), r0, r1, int(begins[2 * i]), int(ends[2 * i]),
                                   int(begins[2 * i + 1]), int(ends[2 * i + 1]), sg))
     del keep
@@ -694,7 +702,7 @@ def oracle_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, matrix=
 
 
 def ref_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, blosum62=False, alphabet="dna",
-                        max_count=1000, lib=None) -> list:
+                        max_count=1000, lib=None, band=None) -> list:
     """The reference's LocalAlignmentEnumerator (oracle/ref/units/waterman_eggert.cpp); lib: the
     library to call (default libref(); libref_bench() holds the same entry)."""
     lib = lib or libref()
@@ -706,9 +714,17 @@ def ref_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, blosum62=F
     pos = np.zeros(4 * max(max_count, 1), np.int32)
     cap = max_count * 2 * (len(h) + len(v) + 2) + 8
     rows = C.create_string_buffer(cap)
-    k = lib.ref_local_enumerate(0 if alphabet == "dna" else 1, 1 if blosum62 else 0, match, mismatch, gap, gap,
-                                cutoff, _ptr(h), len(h), _ptr(v), len(v), max_count, _ptr(scores), _ptr(pos), rows,
-                                cap)
+    if band is None:
+        k = lib.ref_local_enumerate(0 if alphabet == "dna" else 1, 1 if blosum62 else 0, match, mismatch, gap, gap,
+                                    cutoff, _ptr(h), len(h), _ptr(v), len(v), max_count, _ptr(scores), _ptr(pos),
+                                    rows, cap)
+    else:
+        lib.ref_local_enumerate_banded.argtypes = [C.c_int32] * 8 + [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                                                     C.c_int32, C.c_void_p, C.c_void_p, C.c_char_p,
+                                                                     C.c_int64]
+        k = lib.ref_local_enumerate_banded(0 if alphabet == "dna" else 1, 1 if blosum62 else 0, match, mismatch, gap,
+                                           int(band[0]), int(band[1]), cutoff, _ptr(h), len(h), _ptr(v), len(v),
+                                           max_count, _ptr(scores), _ptr(pos), rows, cap)
     if k < 0:
         raise RuntimeError("row buffer too small")
     lines = rows.value.decode().split("\n")

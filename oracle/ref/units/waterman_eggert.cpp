@@ -14,9 +14,21 @@
 namespace seqan_ref {
 namespace {
 
+template <typename TAlph, typename TEnumerator>
+int enumerate_with(TEnumerator & enumerator, const uint8_t * h, int64_t m, const uint8_t * v, int64_t n,
+                   int32_t max_count, int32_t * scores, int32_t * pos, char * out_rows, int64_t cap);
+
 template <typename TAlph, typename TScore>
 int enumerate(TScore const & sc, int32_t cutoff, const uint8_t * h, int64_t m, const uint8_t * v, int64_t n,
               int32_t max_count, int32_t * scores, int32_t * pos, char * out_rows, int64_t cap)
+{
+    LocalAlignmentEnumerator<TScore, Unbanded> enumerator(sc, cutoff);
+    return enumerate_with<TAlph>(enumerator, h, m, v, n, max_count, scores, pos, out_rows, cap);
+}
+
+template <typename TAlph, typename TEnumerator>
+int enumerate_with(TEnumerator & enumerator, const uint8_t * h, int64_t m, const uint8_t * v, int64_t n,
+                   int32_t max_count, int32_t * scores, int32_t * pos, char * out_rows, int64_t cap)
 {
     typedef String<TAlph> TStr;
     TStr hs, vs;
@@ -28,7 +40,6 @@ int enumerate(TScore const & sc, int32_t cutoff, const uint8_t * h, int64_t m, c
     resize(rows(align), 2);
     assignSource(row(align, 0), hs);
     assignSource(row(align, 1), vs);
-    LocalAlignmentEnumerator<TScore, Unbanded> enumerator(sc, cutoff);
     std::string text;
     int32_t k = 0;
     for (; k < max_count && nextLocalAlignment(align, enumerator); ++k)
@@ -71,6 +82,26 @@ int ref_local_enumerate(int32_t alphabet, int32_t blosum62, int32_t match, int32
     }
     Score<int, Simple> sc(match, mismatch, gap_extend, gap_open);
     return seqan_ref::enumerate<Dna5>(sc, cutoff, h, m, v, n, max_count, scores, pos, out_rows, cap);
+}
+
+// The banded enumerator LocalAlignmentEnumerator<Score, Banded>(score, lowerDiag, upperDiag, cutoff)
+// (align/local_alignment_enumeration_banded.h), outputs as ref_local_enumerate.
+int ref_local_enumerate_banded(int32_t alphabet, int32_t blosum62, int32_t match, int32_t mismatch, int32_t gap,
+                               int32_t lower, int32_t upper, int32_t cutoff, const uint8_t * h, int64_t m,
+                               const uint8_t * v, int64_t n, int32_t max_count, int32_t * scores, int32_t * pos,
+                               char * out_rows, int64_t cap)
+{
+    if (alphabet == 1 && blosum62)
+    {
+        typedef Score<int, ScoreMatrix<AminoAcid, ScoreSpecBlosum62>> TSc;
+        LocalAlignmentEnumerator<TSc, Banded> e(TSc(gap, gap), lower, upper, cutoff);
+        return seqan_ref::enumerate_with<AminoAcid>(e, h, m, v, n, max_count, scores, pos, out_rows, cap);
+    }
+    Score<int, Simple> sc(match, mismatch, gap, gap);
+    LocalAlignmentEnumerator<Score<int, Simple>, Banded> e(sc, lower, upper, cutoff);
+    if (alphabet == 1)
+        return seqan_ref::enumerate_with<AminoAcid>(e, h, m, v, n, max_count, scores, pos, out_rows, cap);
+    return seqan_ref::enumerate_with<Dna5>(e, h, m, v, n, max_count, scores, pos, out_rows, cap);
 }
 
 // A batch of pairs (codes concatenated with offsets) on `threads` OpenMP threads (<= 0: all):

@@ -1920,3 +1920,357 @@ done:
     free(w.pq.a);
     return ret;
 }
+
+/* ===================================================================================== */
+/* Banded Waterman-Eggert (LocalAlignmentEnumerator<Score, Banded>)                        */
+/* ===================================================================================== */
+
+/* align/local_alignment_banded_waterman_eggert_impl.h: the matrix in band storage (diagonalWidth
+ * columns per row, row r covers H positions col + lowerDiag + r + lo_row), filled forward row by row
+ * (_alignBandedSmithWaterman :68-151), traced back from the maximum into a (size, direction) trace
+ * (_alignBandedSmithWatermanTrace :368-470), declumped forward from where that trace stopped
+ * (_alignBandedSmithWatermanDeclump :175-350), the next maximum taken from the same heap as the
+ * unbanded enumerator (_getNextBestEndPosition, local_alignment_waterman_eggert_impl.h:643-676). */
+enum { WB_DIAG = 0, WB_HORI = 1, WB_VERT = 2, WB_STOP = 3 };
+
+typedef struct {
+    const orc_we_params *p;
+    const uint8_t *h, *v;
+    int64_t len1, len2;      /* |H|, |V| */
+    int64_t lo, up;          /* lowerDiag, upperDiag */
+    int64_t W, lo_row;       /* diagonalWidth, first row */
+    int64_t height_fill;     /* rows the fill and the declump visit */
+    int64_t cells;           /* matrix size */
+    int32_t *M;
+    uint8_t *F;
+    we_heap pq;
+    int64_t best_end, best_begin;
+    int64_t *tsz;            /* the trace: sizes and directions in the order _alignTracePrint appends */
+    uint8_t *ttv;
+    int64_t nt, tcap;
+    int64_t aCol, eCol, aRow, eRow;   /* alignmentPositions */
+    int undef;
+} wb_t;
+
+static int wb_score(const wb_t *w, int64_t a, int64_t b)
+{
+    if (w->p->matrix) return w->p->matrix[(int)w->h[a] * w->p->alphabet_size + (int)w->v[b]];
+    return w->h[a] == w->v[b] ? w->p->match : w->p->mismatch;
+}
+
+static void wb_print(wb_t *w, int64_t size, int tv)
+{
+    if (w->nt == w->tcap) {
+        w->tcap = w->tcap ? 2 * w->tcap : 64;
+        w->tsz = (int64_t *)realloc(w->tsz, sizeof(int64_t) * (size_t)w->tcap);
+        w->ttv = (uint8_t *)realloc(w->ttv, (size_t)w->tcap);
+    }
+    w->tsz[w->nt] = size;
+    w->ttv[w->nt] = (uint8_t)tv;
+    w->nt++;
+}
+
+/* _alignBandedSmithWaterman: returns the heap's top score or 0 */
+static int32_t wb_fill(wb_t *w)
+{
+    const int32_t gap = w->p->gap, cutoff = w->p->cutoff;
+    int64_t row, col, it = w->W, it2 = 0;
+    for (row = 1; row < w->height_fill; ++row) {
+        const int64_t ar = row + w->lo_row;
+        int32_t hori = 0;
+        for (col = 0; col < w->W; ++col, ++it) {
+            int64_t ac;
+            if (col + w->lo + ar < 0) { ++it2; continue; }
+            ac = col + w->lo + ar;
+            if (ac > w->len1) { ++it2; continue; }
+            if (ac != 0) {
+                int32_t val = w->M[it2] + wb_score(w, ac - 1, ar - 1);
+                ++it2;
+                if (col < w->W - 1) { const int32_t vv = w->M[it2] + gap; if (vv > val) val = vv; }
+                if (col > 0) { hori = hori + gap; if (hori > val) val = hori; }
+                if (0 > val) val = 0;
+                w->M[it] = val;
+                if (val >= cutoff) { we_entry e; e.value = val; e.id = it; we_push(&w->pq, e); }
+            } else {
+                ++it2;
+            }
+            hori = w->M[it];
+        }
+    }
+    if (w->pq.n > 0) { w->best_end = w->pq.a[0].id; return w->pq.a[0].value; }
+    return 0;
+}
+
+/* _alignBandedSmithWatermanTrace from best_end; sets the alignment positions and best_begin */
+static void wb_trace(wb_t *w)
+{
+    const int32_t gap = w->p->gap;
+    int64_t it = w->best_end, it2 = w->best_end - w->W;
+    int64_t row = it / w->W, col = it % w->W;
+    int64_t ar, ac, segLen = 0;
+    int tv, next;
+    w->nt = 0;
+    w->eRow = row + w->lo_row;
+    w->eCol = col + w->lo + w->eRow;
+    ar = w->eRow;
+    ac = w->eCol;
+    if (ac == 0 || ar == 0) { w->aCol = w->eCol = w->aRow = w->eRow = 0; return; }
+    if (ac < w->len1) wb_print(w, w->len1 - ac, WB_HORI);
+    if (ar < w->len2) wb_print(w, w->len2 - ar, WB_VERT);
+    tv = WB_STOP;
+    next = WB_HORI;
+    while (next != WB_STOP) {
+        tv = next;
+        if (it < 0 || it >= w->cells) { w->undef = 1; return; }
+        if (w->M[it] == 0) {
+            next = WB_STOP;
+        } else if (it2 < 0 || it2 + 1 >= w->cells || ac <= 0 || ar <= 0) {
+            /* the reference reads outside the band storage, or a character at position -1 after
+             * a vertical step at the band's last column wrapped into the next stored row */
+            w->undef = 1;
+            return;
+        } else if (w->M[it] == w->M[it2] + wb_score(w, ac - 1, ar - 1)) {
+            next = WB_DIAG;
+            --ar; --ac; --row;
+            it -= w->W; it2 -= w->W;
+        } else if (w->M[it] == w->M[it2 + 1] + gap) {
+            next = WB_VERT;
+            --ar; --row; ++col;
+            it += 1 - w->W; it2 += 1 - w->W;
+        } else {
+            next = WB_HORI;
+            --ac; --col;
+            it -= 1; it2 -= 1;
+        }
+        if (tv == next) ++segLen;
+        else { wb_print(w, segLen, tv); segLen = 1; }
+    }
+    if (ac != 0) wb_print(w, ac, WB_HORI);
+    if (ar != 0) wb_print(w, ar, WB_VERT);
+    w->best_begin = it + w->W;
+    w->aCol = ac;
+    w->aRow = ar;
+}
+
+/* _alignBandedSmithWatermanDeclump */
+static void wb_declump(wb_t *w)
+{
+    const int32_t gap = w->p->gap, cutoff = w->p->cutoff;
+    const int64_t W = w->W;
+    int64_t it = w->best_begin, it2;
+    int64_t minCol = W, newMinCol = W, maxCol = 0, newMaxCol = 0;
+    int64_t row = it / W, col = it % W, traceCol, tracePos, traceSize;
+    int traceValue;
+    traceCol = col;
+    it -= col;
+    tracePos = w->nt;
+    while (tracePos > 0 && w->ttv[tracePos - 1] != WB_DIAG) --tracePos;
+    if (tracePos == 0) return;
+    traceSize = w->tsz[tracePos - 1];
+    traceValue = w->ttv[tracePos - 1];
+    while (row < w->height_fill && (maxCol > minCol || tracePos > 0)) {
+        const int64_t ar = row + w->lo_row;
+        while (traceSize == 0 && tracePos > 1) {
+            --tracePos;
+            traceValue = w->ttv[tracePos - 1];
+            if (traceValue == WB_HORI) traceCol += w->tsz[tracePos - 1];
+            else traceSize = w->tsz[tracePos - 1];
+        }
+        if (tracePos > 0) {
+            if (traceValue == WB_DIAG) {
+                const int64_t f = row * W + traceCol;
+                --traceSize;
+                if (f < 0 || f >= w->cells) { w->undef = 1; return; }
+                w->F[f] = 1;
+                if (traceCol < minCol) minCol = traceCol;
+                if (traceCol + 1 > maxCol) maxCol = traceCol + 1;
+            } else if (traceValue == WB_VERT) {
+                if (traceCol > 0) --traceCol;
+                --traceSize;
+            }
+            if (traceCol >= maxCol) maxCol = traceCol + 1;
+        }
+        if (maxCol > minCol) {
+            col = minCol;
+            it += col;
+            it2 = it - W;
+            while (col < maxCol) {
+                const int64_t ac = col + w->lo + ar;   /* unsigned in the reference: negative reads as huge */
+                int32_t nv = 0;
+                if (ac < 0 || ac > w->len1) break;
+                if (it < 0 || it >= w->cells || it2 < 0 || it2 + 1 >= w->cells) { w->undef = 1; return; }
+                if (!w->F[it]) {
+                    int32_t d;
+                    if (ac == 0) { w->undef = 1; return; }   /* the reference reads H[-1] */
+                    d = w->M[it2] + wb_score(w, ac - 1, ar - 1);
+                    if (d > nv) nv = d;
+                }
+                ++it2;
+                if (col > 0) { const int32_t hh = w->M[it - 1] + gap; if (hh > nv) nv = hh; }
+                if (col + 1 < maxCol) { const int32_t vv = w->M[it2] + gap; if (vv > nv) nv = vv; }
+                if (nv != w->M[it]) {
+                    w->M[it] = nv;
+                    maxCol = (maxCol > col + 2 ? maxCol : col + 2);
+                    if (maxCol > W) maxCol = W;
+                    if (col + 1 > newMaxCol) newMaxCol = col + 1;
+                    newMinCol = col != 0 ? (newMinCol < col - 1 ? newMinCol : col - 1) : 0;
+                    if (nv >= cutoff) { we_entry e; e.value = nv; e.id = it; we_push(&w->pq, e); }
+                } else if (col == minCol) {
+                    ++minCol;
+                }
+                ++col;
+                ++it;
+            }
+            it += W - col;
+        } else {
+            it += W;
+        }
+        minCol = newMinCol > 0 ? newMinCol : 0;
+        maxCol = newMaxCol < W ? newMaxCol : W;
+        newMinCol = W;
+        newMaxCol = 0;
+        ++row;
+    }
+}
+
+static int64_t wb_next_end(wb_t *w)   /* _getNextBestEndPosition */
+{
+    int32_t top_score = 0;
+    if (w->pq.n > 0) top_score = w->M[w->pq.a[0].id];
+    if (w->pq.n > 0) {
+        while (w->pq.a[0].value != top_score) {
+            if (top_score >= w->p->cutoff) {
+                w->pq.a[0].value = top_score;
+                we_toward_leaves(&w->pq, w->pq.a[0], 0, 2);
+            } else {
+                we_pop(&w->pq);
+            }
+            if (w->pq.n > 0) top_score = w->M[w->pq.a[0].id];
+            else break;
+        }
+    }
+    if (w->pq.n == 0) return 0;
+    {
+        const int64_t ret = w->pq.a[0].id;
+        w->best_end = ret;
+        we_pop(&w->pq);
+        return ret;
+    }
+}
+
+/* The alignment's columns from the trace (_pumpTraceToGaps, align/gaps_base.h:979-1016) and the
+ * two rows' clipped views (toViewPosition of the begin and of the end with rightOfGaps false):
+ * the runs over the union of both views, as orc_waterman_eggert gives them. */
+static int wb_emit(const wb_t *w, orc_segment *segs, int64_t seg_cap, int64_t *ns)
+{
+    int64_t total = 0, i, t, vh0 = -1, vh1 = 0, vv0 = -1, vv1 = 0, lo, hi;
+    int64_t *sh, *sv, ch = 0, cv = 0;
+    for (i = 0; i < w->nt; ++i) total += w->tsz[i];
+    sh = (int64_t *)malloc(sizeof(int64_t) * (size_t)(total + 1));
+    sv = (int64_t *)malloc(sizeof(int64_t) * (size_t)(total + 1));
+    t = 0;
+    for (i = w->nt; i > 0; --i) {
+        const int64_t sz = w->tsz[i - 1];
+        const int tv = w->ttv[i - 1];
+        int64_t q;
+        for (q = 0; q < sz; ++q, ++t) {
+            sh[t] = (tv == WB_VERT) ? -1 : ch++;
+            sv[t] = (tv == WB_HORI) ? -1 : cv++;
+        }
+    }
+    /* view positions of the begins (the column of the source character) and the ends (after the
+     * previous character) */
+    for (t = 0; t < total; ++t) {
+        if (sh[t] == w->aCol && vh0 < 0) vh0 = t;
+        if (sv[t] == w->aRow && vv0 < 0) vv0 = t;
+        if (sh[t] >= 0 && sh[t] == w->eCol - 1) vh1 = t + 1;
+        if (sv[t] >= 0 && sv[t] == w->eRow - 1) vv1 = t + 1;
+    }
+    if (vh0 < 0) vh0 = vh1;
+    if (vv0 < 0) vv0 = vv1;
+    lo = vh0 < vv0 ? vh0 : vv0;
+    hi = vh1 > vv1 ? vh1 : vv1;
+    for (t = lo; t < hi;) {
+        const int type = (sh[t] >= 0 && sv[t] >= 0) ? ORC_SEG_DIAGONAL : (sh[t] >= 0 ? ORC_SEG_HORIZONTAL : ORC_SEG_VERTICAL);
+        int64_t u = t + 1, q;
+        while (u < hi) {
+            const int ty = (sh[u] >= 0 && sv[u] >= 0) ? ORC_SEG_DIAGONAL : (sh[u] >= 0 ? ORC_SEG_HORIZONTAL : ORC_SEG_VERTICAL);
+            if (ty != type) break;
+            ++u;
+        }
+        if (*ns >= seg_cap) { free(sh); free(sv); return -1; }
+        for (q = t; q < total && sh[q] < 0; ++q) {}
+        segs[*ns].h_begin = (uint32_t)(q < total ? sh[q] : w->len1);
+        for (q = t; q < total && sv[q] < 0; ++q) {}
+        segs[*ns].v_begin = (uint32_t)(q < total ? sv[q] : w->len2);
+        segs[*ns].length = (uint32_t)(u - t);
+        segs[*ns].type = (uint32_t)type;
+        ++*ns;
+        t = u;
+    }
+    free(sh);
+    free(sv);
+    return 0;
+}
+
+int32_t orc_waterman_eggert_banded(const orc_we_params *p, int32_t lower, int32_t upper, const uint8_t *h, int32_t m,
+                                   const uint8_t *v, int32_t n, int32_t max_count, int32_t *scores, int32_t *begins,
+                                   int32_t *ends, orc_segment *segs, int64_t seg_cap, int64_t *seg_off,
+                                   int32_t *undefined_next)
+{
+    wb_t w;
+    int32_t k = 0, ret = 0;
+    int64_t ns = 0, hi_init, hi_fill, height_init;
+    if (seg_off) seg_off[0] = 0;
+    if (undefined_next) *undefined_next = 0;
+    if (m <= 0 || n <= 0 || max_count <= 0 || upper < lower) return 0;
+    memset(&w, 0, sizeof(w));
+    w.p = p; w.h = h; w.v = v; w.len1 = m; w.len2 = n; w.lo = lower; w.up = upper;
+    /* _initLocalAlignmentFinder [BandedWatermanEggert] (:480-505) and the fill's own row bound */
+    w.lo_row = upper <= 0 ? -(int64_t)upper : 0;
+    hi_init = (int64_t)n + 1;
+    if ((int64_t)m - lower >= 0 && (int64_t)m - lower < hi_init) hi_init = (int64_t)m - lower;
+    height_init = hi_init - w.lo_row + 1;
+    hi_fill = n;
+    if ((int64_t)m - lower >= 0 && (int64_t)m - lower < hi_fill) hi_fill = (int64_t)m - lower;
+    w.height_fill = hi_fill - w.lo_row + 1;
+    w.W = (int64_t)upper - lower + 1;
+    if (height_init <= 0 || w.height_fill <= 0) return 0;
+    w.cells = w.W * height_init;
+    w.M = (int32_t *)calloc((size_t)w.cells, sizeof(int32_t));
+    w.F = (uint8_t *)calloc((size_t)w.cells, 1);
+    for (k = 0; k < max_count; ++k) {
+        int32_t sc;
+        if (k == 0) {
+            sc = wb_fill(&w);
+            if (sc < p->cutoff || sc == 0) break;    /* _localAlignment returns 0: false */
+            wb_trace(&w);
+            we_pop(&w.pq);
+        } else {
+            int64_t e;
+            wb_declump(&w);
+            if (w.undef) { if (undefined_next) *undefined_next = 1; break; }
+            e = wb_next_end(&w);
+            if (e == 0) break;
+            sc = w.M[e];
+            if (sc == 0) break;
+            wb_trace(&w);
+        }
+        if (w.undef) { if (undefined_next) *undefined_next = 1; break; }
+        scores[k] = w.M[w.best_end];
+        begins[2 * k] = (int32_t)w.aCol;
+        begins[2 * k + 1] = (int32_t)w.aRow;
+        ends[2 * k] = (int32_t)w.eCol;
+        ends[2 * k + 1] = (int32_t)w.eRow;
+        if (wb_emit(&w, segs, seg_cap, &ns)) { ret = -1; goto done; }
+        if (seg_off) seg_off[k + 1] = ns;
+    }
+    ret = k;
+done:
+    free(w.M);
+    free(w.F);
+    free(w.tsz);
+    free(w.ttv);
+    free(w.pq.a);
+    return ret;
+}

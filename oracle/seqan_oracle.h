@@ -184,6 +184,15 @@ int32_t orc_waterman_eggert(const orc_we_params *p, const uint8_t *h, int32_t m,
                             int32_t max_count, int32_t *scores, int32_t *begins, int32_t *ends,
                             orc_segment *segs, int64_t seg_cap, int64_t *seg_off, int32_t *undefined_next);
 
+/* The banded enumerator LocalAlignmentEnumerator<Score, Banded>(score, lower, upper, cutoff)
+ * (align/local_alignment_enumeration_banded.h, align/local_alignment_banded_waterman_eggert_impl.h),
+ * outputs as orc_waterman_eggert: per alignment the score, the clipped source positions of the two
+ * rows and the runs over the union of the rows' clipped views. */
+int32_t orc_waterman_eggert_banded(const orc_we_params *p, int32_t lower, int32_t upper, const uint8_t *h, int32_t m,
+                                   const uint8_t *v, int32_t n, int32_t max_count, int32_t *scores, int32_t *begins,
+                                   int32_t *ends, orc_segment *segs, int64_t seg_cap, int64_t *seg_off,
+                                   int32_t *undefined_next);
+
 /* orc_align_pair with CompleteTrace (ties keep the trace bits of every source, no start-cell
  * correction): the DP of a banded chain's grid that spans the whole matrix. */
 int orc_align_pair_complete(const orc_params *p,

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|packed|sam|seqio|bam|cpp|dynamic|banded_chain|tags]
+    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|waterman_eggert_banded|packed|sam|seqio|bam|cpp|dynamic|banded_chain|tags]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -19,6 +19,8 @@ Outputs (all small, committed):
                         without xDrop, origScore, aligned parts with gaps.
   waterman_eggert_cases.json  suboptimal local alignments of the reference's
                         LocalAlignmentEnumerator<Score, Unbanded> (scores, rows, positions).
+  waterman_eggert_banded_cases.json  the same for LocalAlignmentEnumerator<Score, Banded> with
+                        random diagonal bands.
   dynamic_cases.json    pairs aligned by the reference's single-pair DP with DynamicGaps cells
                         (score and raw TraceSegment_ list) for the shapes oracle/ref/units/dynamic_*.cpp
                         instantiate.
@@ -109,6 +111,9 @@ def main():
         return
     if only == "waterman_eggert":
         write_waterman_eggert(b62)
+        return
+    if only == "waterman_eggert_banded":
+        write_waterman_eggert_banded(b62)
         return
     if only == "packed":
         write_packed()
@@ -272,6 +277,7 @@ def main():
     write_extend(b62)
     write_extend_banded(b62)
     write_waterman_eggert(b62)
+    write_waterman_eggert_banded(b62)
     write_packed()
     write_sam_cases()
 
@@ -554,6 +560,54 @@ def write_waterman_eggert(b62):
         json.dump({"generator": "tests/golden/make_golden.py", "seed": 20261208, "cases": cases}, f,
                   separators=(",", ":"))
     print(f"{len(cases)} Waterman-Eggert cases written")
+
+
+def write_waterman_eggert_banded(b62):
+    """Suboptimal local alignments from the reference's LocalAlignmentEnumerator<Score, Banded>:
+    random DNA and protein pairs with random bands [lowerDiag, upperDiag] that cross the matrix
+    (lowerDiag < len(H), upperDiag > -len(V): the reference crashes on a band outside it), up to 25
+    alignments each, cut where the oracle marks the reference's next step undefined."""
+    from seqan_gb300 import workloads as W
+    rng = np.random.Generator(np.random.PCG64(20261212))
+    cases = []
+    for trial in range(300):
+        aa = trial % 4 == 3
+        A = 20 if aa else 4
+        m = int(rng.integers(1, 60))
+        h = rng.integers(0, A, m).astype(np.uint8)
+        if rng.random() < 0.6:
+            v = W.mutate(rng, h, float(rng.uniform(0, 0.3)), float(rng.uniform(0, 0.08)), alphabet=A)
+        else:
+            v = rng.integers(0, A, int(rng.integers(1, 60))).astype(np.uint8)
+        if len(v) == 0:
+            v = rng.integers(0, A, 1).astype(np.uint8)
+        lo = int(rng.integers(-len(v) + 1, len(h)))
+        up = int(rng.integers(max(lo, -len(v) + 1), len(h) + 6))
+        if trial % 7 == 0:
+            lo, up = -len(v) - int(rng.integers(0, 5)), len(h) + int(rng.integers(0, 5))
+        if aa:
+            h, v = W.AA20_CODES[h], W.AA20_CODES[v]
+            mt, mm, gap = 0, 0, -int(rng.integers(1, 12))
+            letters = "ABCDEFGHIJKLMNOPQRSTUVWYZX*"
+        else:
+            mt, mm, gap = int(rng.integers(1, 4)), -int(rng.integers(1, 4)), -int(rng.integers(1, 5))
+            letters = "ACGTN"
+        cutoff = int(rng.integers(-1, 12))
+        o = O.oracle_local_enumerate(h, v, mt, mm, gap, cutoff, matrix=b62 if aa else None, max_count=25,
+                                     letters=letters, band=(lo, up))
+        truncated = bool(o) and o[-1] is None
+        if truncated:
+            o = o[:-1]
+        r = O.ref_local_enumerate(h, v, mt, mm, gap, cutoff, blosum62=aa, alphabet="aa" if aa else "dna",
+                                  max_count=len(o) if truncated else 25, band=(lo, up))
+        cases.append({"alphabet": "aa" if aa else "dna", "blosum62": aa, "match": mt, "mismatch": mm, "gap": gap,
+                      "cutoff": cutoff, "band": [lo, up], "H": text(h, "aa" if aa else "dna"),
+                      "V": text(v, "aa" if aa else "dna"), "max_count": 25, "undefined_next": truncated,
+                      "alignments": [[a.score, a.row0, a.row1, a.h_begin, a.h_end, a.v_begin, a.v_end] for a in r]})
+    with open(os.path.join(HERE, "waterman_eggert_banded_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only waterman_eggert_banded", "seed": 20261212,
+                   "cases": cases}, f, separators=(",", ":"))
+    print(f"{len(cases)} banded Waterman-Eggert cases written")
 
 
 def chain_case(rng, max_len=200, max_seeds=8, max_seed_len=30):
