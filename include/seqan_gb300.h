@@ -508,6 +508,18 @@ typedef struct {
 GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params, const gba_batch *batch,
                                 gba_enum_result *result);
 
+/* The reference's LocalAlignmentEnumerator<Score, Banded>(score, lowerDiag, upperDiag, cutoff)
+ * driven by nextLocalAlignment (align/local_alignment_enumeration_banded.h:56-121,
+ * align/local_alignment_banded_waterman_eggert_impl.h): the matrix kept in band storage over the
+ * diagonals lower_diag .. upper_diag (column - row), filled from the sequence begins, each
+ * alignment traced backward from the largest remaining score, its diagonal cells forbidden and the
+ * rows below re-filled while values change.  Same parameters and result layout as
+ * gba_local_enumerate; status[k] = GBA_ENUM_UNDEFINED_NEXT where the reference's walk reads outside
+ * its band storage or a character outside a sequence.  A band that does not cross the matrix
+ * (lower_diag >= len(H) or upper_diag <= -len(V)) gives no alignment; the reference crashes there. */
+GBA_API int gba_local_enumerate_banded(gba_context *ctx, const gba_enum_params *params, int32_t lower_diag,
+                                       int32_t upper_diag, const gba_batch *batch, gba_enum_result *result);
+
 /* --- Banded chain alignment ------------------------------------------------------------------
  * bandedChainAlignment(align, seedChain, scoreAnchor, scoreGap, AlignConfig, bandExtension)
  * (seeds/banded_chain_alignment.h:184-214) for every pair of a batch, each with its own seed

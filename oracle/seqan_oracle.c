@@ -2024,9 +2024,10 @@ static void wb_trace(wb_t *w)
         if (it < 0 || it >= w->cells) { w->undef = 1; return; }
         if (w->M[it] == 0) {
             next = WB_STOP;
-        } else if (it2 < 0 || it2 + 1 >= w->cells || ac <= 0 || ar <= 0) {
-            /* the reference reads outside the band storage, or a character at position -1 after
-             * a vertical step at the band's last column wrapped into the next stored row */
+        } else if (it2 < 0 || it2 + 1 >= w->cells || ac <= 0 || ar <= 0 || ac > w->len1 || ar > w->len2) {
+            /* the reference reads outside the band storage, or a character before a sequence's
+             * begin or after its end: a step at the band's last column wraps into the next stored
+             * row, and the declump can write one cell past a row's last column */
             w->undef = 1;
             return;
         } else if (w->M[it] == w->M[it2] + wb_score(w, ac - 1, ar - 1)) {

@@ -290,6 +290,8 @@ def lib():
                                                 C.POINTER(GbaExtendAlignResult)]
             L.gba_local_enumerate.argtypes = [vp, C.POINTER(GbaEnumParams), C.POINTER(GbaBatch),
                                               C.POINTER(GbaEnumResult)]
+            L.gba_local_enumerate_banded.argtypes = [vp, C.POINTER(GbaEnumParams), C.c_int32, C.c_int32,
+                                                     C.POINTER(GbaBatch), C.POINTER(GbaEnumResult)]
             L.gba_banded_chain.argtypes = [vp, C.POINTER(GbaChainParams), C.POINTER(GbaBatch),
                                            C.POINTER(GbaChainSeeds), C.POINTER(GbaChainResult)]
             L.gba_align_packed.argtypes = [vp, C.POINTER(GbaParams), C.POINTER(GbaPackedSet),

@@ -1112,7 +1112,7 @@ struct Engine {
     // the cells of anti-diagonal d that lane l takes; k3 / k1 / k2: the rolling slots of d, d - 1, d - 2
     __host__ __device__ void fill_diag(int d, int l, int cfirst, int clast, int k3, int k1, int k2)
     {
-        const int cap = pl->col_cap, gnn = gn, Li = int(L);
+        const int cap = pl->col_cap, gnn = gn;
         const int hN = int(hNext), vN = int(vNext);
         const bool finalM = kind == KIND_FINAL;
         const bool freeB = (fe & FREE_BOTTOM) != 0, freeR = (fe & FREE_RIGHT) != 0;

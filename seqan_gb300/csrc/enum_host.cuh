@@ -24,12 +24,21 @@ __global__ void __launch_bounds__(128) k_enum_pack(const uint32_t *slots, const 
     for (int32_t q = 0; q < 4 * c; ++q) dst[q] = src[q];
 }
 
-}  // namespace
+// Band storage of LocalAlignmentEnumerator<Score, Banded> for an m x n pair: cells of the
+// stored matrix (diagonalWidth x rows, _initLocalAlignmentFinder), 0 when the band misses it.
+int64_t enum_band_cells(int64_t m, int64_t n, int64_t lower, int64_t upper)
+{
+    const int64_t W = upper - lower + 1, lo_row = upper <= 0 ? -upper : 0;
+    int64_t hi_init = n + 1, hi_fill = n;
+    if (m - lower >= 0 && m - lower < hi_init) hi_init = m - lower;
+    if (m - lower >= 0 && m - lower < hi_fill) hi_fill = m - lower;
+    if (m <= 0 || n <= 0 || hi_init - lo_row + 1 <= 0 || hi_fill - lo_row + 1 <= 0) return 0;
+    return W * (hi_init - lo_row + 1);
+}
 
-extern "C" {
-
-GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params, const gba_batch *b,
-                                gba_enum_result *res)
+// gba_local_enumerate (band == nullptr) and gba_local_enumerate_banded (band = {lower, upper}).
+int enumerate_impl(gba_context *ctx, const gba_enum_params *params, const int32_t *band, const gba_batch *b,
+                   gba_enum_result *res)
 {
     if (!ctx || !params || !b || !res) return GBA_EINVAL;
     const auto t0 = std::chrono::steady_clock::now();
@@ -42,6 +51,11 @@ GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params,
     if (std::abs(params->match) > lim || std::abs(params->mismatch) > lim || std::abs(params->gap) > lim ||
         std::abs(params->cutoff) > lim)
         return fail(ctx, GBA_EUNSUPPORTED, "scores beyond +-2^20");
+    if (band) {
+        if (band[1] < band[0]) return fail(ctx, GBA_EINVAL, "upper_diag below lower_diag");
+        if (std::abs(band[0]) > (1 << 30) || std::abs(band[1]) > (1 << 30))
+            return fail(ctx, GBA_EUNSUPPORTED, "diagonals beyond +-2^30");
+    }
     std::vector<int32_t> mat;
     if (params->matrix) {
         if (params->alphabet_size < 1 || params->alphabet_size > 32)
@@ -68,20 +82,28 @@ GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params,
     }
     std::vector<EnumPair> pairs(static_cast<size_t>(N));
     std::vector<size_t> need(static_cast<size_t>(N));
+    std::vector<int64_t> cells_of(static_cast<size_t>(N));
     for (int64_t k = 0; k < N; ++k) {
         const int64_t h0 = b->h_shared ? b->off_h[0] : b->off_h[k], h1 = b->h_shared ? b->off_h[1] : b->off_h[k + 1];
         const int64_t v0 = b->off_v[k], v1 = b->off_v[k + 1];
         if (h0 < 0 || v0 < 0 || h1 < h0 || v1 < v0) return fail(ctx, GBA_EINVAL, "bad offsets of pair %lld", (long long)k);
         const int64_t m = h1 - h0, n = v1 - v0;
-        if ((m + 1) * (n + 1) > (int64_t(1) << 31) - 1)
+        if (m > (int64_t(1) << 30) || n > (int64_t(1) << 30))
+            return fail(ctx, GBA_EUNSUPPORTED, "pair %lld: sequence of more than 2^30 residues", (long long)k);
+        const int64_t cells = band ? enum_band_cells(m, n, band[0], band[1]) : (m + 1) * (n + 1);
+        if (cells > (int64_t(1) << 31) - 1)
             return fail(ctx, GBA_EUNSUPPORTED, "pair %lld: matrix of more than 2^31 cells", (long long)k);
         EnumPair &d = pairs[k];
         d.h_off = h0;
         d.v_off = v0;
         d.m = int32_t(m);
         d.n = int32_t(n);
-        const int64_t cells = (m + 1) * (n + 1);
-        need[k] = size_t(cells) * 5 + size_t(m * n) * 8 + size_t(2 * (m + n + 1)) * 4 +
+        // banded: the fill pushes each cell once, a declump at most each cell again; the first
+        // launch gives room for one declump's pushes, a pair that needs more is rerun with the
+        // bound of max_count pushes per cell
+        d.heap_cap = band ? 2 * cells + 16 : m * n;
+        cells_of[k] = cells;
+        need[k] = size_t(cells) * 5 + size_t(d.heap_cap) * 8 + size_t(2 * (m + n + 5)) * 4 +
                   size_t(K) * size_t(m + n + 1) * 16 + 64;
         if (need[k] > kEnumScratchBudget) return fail(ctx, GBA_EUNSUPPORTED, "pair %lld needs more scratch than one chunk", (long long)k);
     }
@@ -95,23 +117,26 @@ GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params,
         int64_t c1 = c0;
         size_t tot = 0;
         while (c1 < N && tot + need[c1] <= kEnumScratchBudget) tot += need[c1++];
+        const int64_t nc = c1 - c0, na = nc * K;
+        int32_t *o = nullptr;
+        std::vector<int32_t> outh(size_t(na) * 6 + size_t(nc) * 2);
+        for (int attempt = 0;; ++attempt) {
         int64_t mo = 0, fo = 0, ho = 0, so = 0, go = 0;
         for (int64_t k = c0; k < c1; ++k) {
             EnumPair &d = pairs[k];
-            const int64_t cells = int64_t(d.m + 1) * (d.n + 1);
+            const int64_t cells = cells_of[k];
             d.mat_off = mo;
             mo += cells;
             d.forb_off = fo;
             fo += cells;
             d.heap_off = ho;
-            ho += int64_t(d.m) * d.n;
+            ho += d.heap_cap;
             d.step_off = so;
-            so += 2 * int64_t(d.m + d.n + 1);
+            so += 2 * int64_t(d.m + d.n + 5);
             d.seg_off = go;
             for (int32_t i = 0; i < K; ++i) slot_off[k * K + i] = go + int64_t(i) * (d.m + d.n + 1);
             go += int64_t(K) * (d.m + d.n + 1);
         }
-        const int64_t nc = c1 - c0, na = nc * K;
         GBA_CUDA(ctx, ctx->en_pairs.ensure(size_t(nc) * sizeof(EnumPair)));
         GBA_CUDA(ctx, ctx->en_mat.ensure(size_t(mo) * 4 + 16));
         GBA_CUDA(ctx, ctx->en_forb.ensure(size_t(fo) + 16));
@@ -121,7 +146,11 @@ GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params,
         GBA_CUDA(ctx, ctx->en_out.ensure(size_t(na) * 6 * 4 + size_t(nc) * 2 * 4 + 64));
         GBA_CUDA(ctx, cudaMemcpyAsync(ctx->en_pairs.ptr, pairs.data() + c0, size_t(nc) * sizeof(EnumPair),
                                       cudaMemcpyHostToDevice, st));
-        int32_t *o = ctx->en_out.as<int32_t>();
+        if (band) {   // the band storage starts zeroed, as the reference's matrix does
+            GBA_CUDA(ctx, cudaMemsetAsync(ctx->en_mat.ptr, 0, size_t(mo) * 4, st));
+            GBA_CUDA(ctx, cudaMemsetAsync(ctx->en_forb.ptr, 0, size_t(fo), st));
+        }
+        o = ctx->en_out.as<int32_t>();
         EnumArgs a{};
         a.seq_h = ctx->seq_h.as<uint8_t>();
         a.seq_v = ctx->seq_v.as<uint8_t>();
@@ -149,18 +178,32 @@ GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params,
         a.max_count = K;
         GBA_CUDA(ctx, cudaMemsetAsync(a.seg_count, 0, size_t(na) * 4, st));
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-        k_waterman_eggert<<<unsigned((nc + 127) / 128), 128, 0, st>>>(a);
+        if (band)
+            k_waterman_eggert_banded<<<unsigned((nc + 127) / 128), 128, 0, st>>>(a, band[0], band[1]);
+        else
+            k_waterman_eggert<<<unsigned((nc + 127) / 128), 128, 0, st>>>(a);
         GBA_CUDA(ctx, cudaGetLastError());
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
         ++launches;
         // results of the chunk
-        std::vector<int32_t> outh(size_t(na) * 6 + size_t(nc) * 2);
         GBA_CUDA(ctx, cudaMemcpyAsync(outh.data(), o, outh.size() * 4, cudaMemcpyDeviceToHost, st));
         GBA_CUDA(ctx, cudaStreamSynchronize(st));
         {
             float ms = 0;
             GBA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
             dp_ms += ms;
+        }
+        bool rerun = false;
+        for (int64_t k = 0; k < nc; ++k)
+            if (outh[size_t(6 * na + nc + k)] == 2) {
+                EnumPair &d = pairs[c0 + k];
+                const int64_t bound = int64_t(K) * cells_of[c0 + k] + 16;
+                if (attempt > 0 || d.heap_cap >= bound)
+                    return fail(ctx, GBA_EUNSUPPORTED, "pair %lld: heap beyond its bound", (long long)(c0 + k));
+                d.heap_cap = bound;
+                rerun = true;
+            }
+        if (!rerun) break;
         }
         std::vector<int64_t> dense(size_t(na) + 1, 0), src(size_t(na), 0);
         for (int64_t i = 0; i < na; ++i) {
@@ -211,6 +254,23 @@ GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params,
     ctx->stats.kernel_launches = launches;
     ctx->stats.call_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return GBA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GBA_API int gba_local_enumerate(gba_context *ctx, const gba_enum_params *params, const gba_batch *batch,
+                                gba_enum_result *result)
+{
+    return enumerate_impl(ctx, params, nullptr, batch, result);
+}
+
+GBA_API int gba_local_enumerate_banded(gba_context *ctx, const gba_enum_params *params, int32_t lower_diag,
+                                       int32_t upper_diag, const gba_batch *batch, gba_enum_result *result)
+{
+    const int32_t band[2] = {lower_diag, upper_diag};
+    return enumerate_impl(ctx, params, band, batch, result);
 }
 
 }  // extern "C"

@@ -1,11 +1,13 @@
 """Waterman-Eggert suboptimal local alignments with the reference's call surface
-(align/local_alignment_enumeration_unbanded.h).
+(align/local_alignment_enumeration_unbanded.h, align/local_alignment_enumeration_banded.h).
 
 :func:`local_enumerate` runs the enumeration for a batch of pairs in one GPU call
 (``gba_local_enumerate``): per pair, up to ``max_count`` alignments, each with the enumerator's
 score (getScore), the gapped rows as the reference prints them, the clipped source positions and
 the alignment's columns as runs.  :class:`LocalAlignmentEnumerator` with :func:`nextLocalAlignment`
 is the reference's stateful form for one pair: each call gives the next alignment or False.
+With ``band=(lowerDiag, upperDiag)`` both run LocalAlignmentEnumerator<Score, Banded>
+(``gba_local_enumerate_banded``).
 Linear gaps only, as the reference's Waterman-Eggert is: every gap column costs the scheme's gap
 extension score.
 """
@@ -74,13 +76,14 @@ def _rows(segments, h_text, v_text):
             r0.append(h_text[hb:hb + ln]); r1.append("-" * ln)
         else:
             r0.append("-" * ln); r1.append(v_text[vb:vb + ln])
-    # each row's clipped region starts at its first residue
-    return "".join(r0).lstrip("-"), "".join(r1).lstrip("-")
+    # each row's clipped region runs from its first to its last residue
+    return "".join(r0).strip("-"), "".join(r1).strip("-")
 
 
 def local_enumerate(H, V, score, cutoff: int = 0, max_count: int = 25, alphabet: str = "dna5",
-                    context=None) -> list:
-    """One GPU call: up to max_count Waterman-Eggert alignments per pair (H[k], V[k])."""
+                    context=None, band=None) -> list:
+    """One GPU call: up to max_count Waterman-Eggert alignments per pair (H[k], V[k]); band =
+    (lowerDiag, upperDiag) for the banded enumerator."""
     ch = [np.ascontiguousarray(encode(s, alphabet), dtype=np.uint8) for s in H]
     cv = [np.ascontiguousarray(encode(s, alphabet), dtype=np.uint8) for s in V]
     n = len(ch)
@@ -108,7 +111,11 @@ def local_enumerate(H, V, score, cutoff: int = 0, max_count: int = 25, alphabet:
     r = N.GbaEnumResult(count.ctypes.data, status.ctypes.data, *[a.ctypes.data for a in arrs], segs.ctypes.data,
                         cap, off.ctypes.data)
     ctx = context or N.default_context()
-    ctx.check(N.lib().gba_local_enumerate(ctx.handle, C.byref(p), C.byref(b), C.byref(r)), "gba_local_enumerate")
+    if band is None:
+        ctx.check(N.lib().gba_local_enumerate(ctx.handle, C.byref(p), C.byref(b), C.byref(r)), "gba_local_enumerate")
+    else:
+        ctx.check(N.lib().gba_local_enumerate_banded(ctx.handle, C.byref(p), int(band[0]), int(band[1]), C.byref(b),
+                                                     C.byref(r)), "gba_local_enumerate_banded")
     del keep
     out = _Batch(ch, cv, alphabet, max_count, count, arrs, segs, off)
     return [PairEnumeration(out, k, int(status[k]) == N.GBA_ENUM_UNDEFINED_NEXT) for k in range(n)]
@@ -147,10 +154,16 @@ class _Texts:
 
 
 class LocalAlignmentEnumerator:
-    """LocalAlignmentEnumerator<Score, Unbanded>(score[, cutoff]) for one pair of sequences."""
+    """LocalAlignmentEnumerator<Score, Unbanded>(score[, cutoff]) for one pair of sequences, or
+    LocalAlignmentEnumerator<Score, Banded>(score, lowerDiag, upperDiag[, cutoff]) when both
+    diagonals are given."""
 
-    def __init__(self, score, cutoff: int = 0, alphabet: str = "dna5", context=None):
-        self.score_scheme, self.cutoff, self.alphabet, self.context = score, cutoff, alphabet, context
+    def __init__(self, score, *args, alphabet: str = "dna5", context=None):
+        if len(args) >= 2:
+            self.band, self.cutoff = (int(args[0]), int(args[1])), int(args[2]) if len(args) > 2 else 0
+        else:
+            self.band, self.cutoff = None, int(args[0]) if args else 0
+        self.score_scheme, self.alphabet, self.context = score, alphabet, context
         self._pair = None
         self._done = []
         self._next = 0
@@ -158,7 +171,8 @@ class LocalAlignmentEnumerator:
         self.current = None
 
     def _fill(self, h, v, want):
-        e = local_enumerate([h], [v], self.score_scheme, self.cutoff, want, self.alphabet, self.context)[0]
+        e = local_enumerate([h], [v], self.score_scheme, self.cutoff, want, self.alphabet, self.context,
+                            band=self.band)[0]
         self._done = e.alignments
         self._exhausted = len(e.alignments) < want
 
