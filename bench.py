@@ -65,7 +65,11 @@ EXTEND_WORKLOADS = {"extend_reads_250k"}
 WORKLOADS["waterman_eggert_10k"] = ("10000 DNA pairs of 100-200 bp (half related: 10% subs, 2% indels), "
                                     "LocalAlignmentEnumerator<Score<int,Simple>(2,-1,-2,-2), Unbanded>, cutoff 10, "
                                     "up to 10 suboptimal local alignments per pair (scores, rows, positions)")
-WE_WORKLOADS = {"waterman_eggert_10k"}
+WORKLOADS["waterman_eggert_banded_10k"] = ("the same 10000 DNA pairs, LocalAlignmentEnumerator<Score<int,Simple>"
+                                           "(2,-1,-2,-2), Banded> over diagonals -16..16, cutoff 10, up to 10 "
+                                           "suboptimal local alignments per pair")
+WE_WORKLOADS = {"waterman_eggert_10k", "waterman_eggert_banded_10k"}
+WE_BAND = {"waterman_eggert_banded_10k": (-16, 16)}
 WORKLOADS["banded_chain_20k"] = ("20000 genomic pairs of 1-3 kbp (5% subs, 1% indels) with LAGAN-style anchor chains (the "
                                  "exact matches of >= 20 bp on the true alignment, at most 64 per pair, 35 on average), "
                                  "bandedChainAlignment(align, chain, Score<int,Simple>(2,-3,-1,-5), AlignConfig<>(), 15): "
@@ -1236,17 +1240,29 @@ def we_pairs(n: int, seed: int):
 WE_SCORE, WE_CUTOFF, WE_COUNT = (2, -1, -2), 10, 10
 
 
-def we_cpu_time(H, V, kind, lib=None):
+def we_cpu_time(H, V, kind, lib=None, band=None):
     """Seconds for the enumeration of every pair: the oracle ("port") or the compiled reference
     ("reference", through lib), one pair after another, as the reference's enumerator runs."""
     from oracle import oracle as O
     t0 = time.perf_counter()
     for h, v in zip(H, V):
         if kind == "reference":
-            O.ref_local_enumerate(h, v, *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT, lib=lib)
+            O.ref_local_enumerate(h, v, *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT, lib=lib, band=band)
         else:
-            O.oracle_local_enumerate(h, v, *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT)
+            O.oracle_local_enumerate(h, v, *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT, band=band)
     return time.perf_counter() - t0
+
+
+def we_band_cells(m, n, band):
+    """Cells of the banded enumerator's band storage that lie in the matrix (1 <= column <= m)."""
+    lo, up = band
+    return sum(max(0, min(m, r + up) - max(1, r + lo) + 1) for r in range(1, n + 1))
+
+
+def we_metric(band):
+    if band:
+        return "pairs/s, banded Waterman-Eggert enumeration (LocalAlignmentEnumerator<Score, Banded>)"
+    return "pairs/s, Waterman-Eggert enumeration (LocalAlignmentEnumerator)"
 
 
 def run_we_bench(args, rank, world, local_rank, dist):
@@ -1258,11 +1274,15 @@ def run_we_bench(args, rank, world, local_rank, dist):
     ctx = N.Context(local_rank)
     n = args.pairs or 10_000
     H, V = we_pairs(n, 70 + rank)
-    cells = int(sum(len(h) * len(v) for h, v in zip(H, V)))
+    band = WE_BAND.get(args.workload)
+    if band is None:
+        cells = int(sum(len(h) * len(v) for h, v in zip(H, V)))
+    else:
+        cells = int(sum(we_band_cells(len(h), len(v), band) for h, v in zip(H, V)))
     score = sg.Score(WE_SCORE[0], WE_SCORE[1], WE_SCORE[2], WE_SCORE[2])
 
     def call():
-        return LE.local_enumerate(H, V, score, WE_CUTOFF, WE_COUNT, alphabet="dna5", context=ctx)
+        return LE.local_enumerate(H, V, score, WE_CUTOFF, WE_COUNT, alphabet="dna5", context=ctx, band=band)
 
     for _ in range(args.warmup):
         out = call()
@@ -1288,7 +1308,7 @@ def run_we_bench(args, rank, world, local_rank, dist):
     from oracle import oracle as O
     parity = True
     for k in range(min(n, 300)):
-        ref = O.oracle_local_enumerate(H[k], V[k], *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT)
+        ref = O.oracle_local_enumerate(H[k], V[k], *WE_SCORE, WE_CUTOFF, max_count=WE_COUNT, band=band)
         und = bool(ref) and ref[-1] is None
         ref = ref[:-1] if und else ref
         if out[k].undefined_next != und or [(a.score, a.row0, a.row1, a.h_begin, a.h_end, a.v_begin, a.v_end)
@@ -1301,7 +1321,8 @@ def run_we_bench(args, rank, world, local_rank, dist):
     # the initial fill alone: linear local, 6 ops per cell (two gap adds, diagonal add, two maxima,
     # the zero floor); the heap, the traces and the declumping come on top
     achieved = cells * OPS_PER_CELL["linear_local"] / (kernel_ms * 1e-3) / 1e12
-    line = {"metric": "pairs/s, Waterman-Eggert enumeration (LocalAlignmentEnumerator)", "value": value,
+    kname = "k_waterman_eggert_banded" if band else "k_waterman_eggert"
+    line = {"metric": we_metric(band), "value": value,
             "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "pairs": n,
@@ -1315,15 +1336,16 @@ def run_we_bench(args, rank, world, local_rank, dist):
             "gpu_launches": args.steps * int(st.kernel_launches),
             "roofline": {"bound": "latency", "achieved": achieved, "peak": peak.value, "unit": "Tops/s",
                          "frac": achieved / peak.value if peak.value else None, "traffic": None,
-                         "kernel": "k_waterman_eggert (one thread per pair: heap, forward traces and declumping "
-                                   "are sequential per pair) + k_enum_pack",
+                         "kernel": kname + " (one thread per pair: heap, traces and declumping are sequential "
+                                           "per pair) + k_enum_pack",
                          "ops_per_cell": OPS_PER_CELL["linear_local"], "dp_kernel_ms": kernel_ms,
-                         "note": "achieved counts the initial matrix fill only",
+                         "note": "achieved counts the initial matrix fill only" +
+                                 (" (the band's cells inside the matrix)" if band else ""),
                          "peak_source": "measured live by gba_measure_int_peak (32-bit add+max issue rate)"},
             "clocks": clocks, "parity_first_300_vs_oracle": parity}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         k = min(n, 1000)
-        t = we_cpu_time(H[:k], V[:k], "port")
+        t = we_cpu_time(H[:k], V[:k], "port", band=band)
         line["cpu_baseline"] = {"value": k / t, "unit": "pairs/s", "cores": 1, "kind": "port",
                                 "sample": f"the first {k} pairs, the oracle's enumeration one pair after another",
                                 "seconds": t}
@@ -1343,17 +1365,25 @@ def run_we_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": "the reference's headers are not on this host "
                                                               "(baseline/_ref/include)"}), flush=True)
         return
+    band = WE_BAND.get(args.workload)
     lib.ref_local_enumerate_batch.argtypes = [C.c_int32] * 4 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                                                 C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]
+    lib.ref_local_enumerate_banded_batch.argtypes = [C.c_int32] * 6 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                                       C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]
     sh, oh = O.concat(H)
     sv, ov = O.concat(V)
     count = np.zeros(n, np.int32)
     threads = os.cpu_count() or 1
 
     def step(k):
-        lib.ref_local_enumerate_batch(WE_SCORE[0], WE_SCORE[1], WE_SCORE[2], WE_CUTOFF, k, sh.ctypes.data,
-                                      oh.ctypes.data, sv.ctypes.data, ov.ctypes.data, WE_COUNT, count.ctypes.data,
-                                      threads)
+        if band:
+            lib.ref_local_enumerate_banded_batch(WE_SCORE[0], WE_SCORE[1], WE_SCORE[2], band[0], band[1], WE_CUTOFF,
+                                                 k, sh.ctypes.data, oh.ctypes.data, sv.ctypes.data, ov.ctypes.data,
+                                                 WE_COUNT, count.ctypes.data, threads)
+        else:
+            lib.ref_local_enumerate_batch(WE_SCORE[0], WE_SCORE[1], WE_SCORE[2], WE_CUTOFF, k, sh.ctypes.data,
+                                          oh.ctypes.data, sv.ctypes.data, ov.ctypes.data, WE_COUNT, count.ctypes.data,
+                                          threads)
 
     for _ in range(args.warmup):
         step(min(n, 200))
@@ -1363,15 +1393,15 @@ def run_we_reference(args):
         step(n)
         times.append(time.perf_counter() - t0)
     rate = n * len(times) / sum(times)
-    print(json.dumps({"metric": "pairs/s, Waterman-Eggert enumeration (LocalAlignmentEnumerator)", "value": rate,
+    print(json.dumps({"metric": we_metric(band), "value": rate,
                       "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
                       "vs_baseline": None, "dtype": "int32", "data": "synthetic", "impl": "reference",
                       "config": {"workload": args.workload, "pairs_per_step": n, "description": WORKLOADS[args.workload]},
                       "cpu_baseline": {"value": rate, "unit": "pairs/s", "cores": threads, "kind": "reference",
                                        "sample": f"the first {n} pairs of the workload per step through the compiled "
-                                                 f"reference's LocalAlignmentEnumerator, {threads} OpenMP threads "
-                                                 "over the pairs"},
+                                                 f"reference's LocalAlignmentEnumerator{'<.., Banded>' if band else ''}, "
+                                                 f"{threads} OpenMP threads over the pairs"},
                       "e2e": {"value": rate, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
           flush=True)
 

@@ -128,4 +128,28 @@ int ref_local_enumerate_batch(int32_t match, int32_t mismatch, int32_t gap, int3
     return 0;
 }
 
+// The same batch through LocalAlignmentEnumerator<Score, Banded>(sc, lower, upper, cutoff).
+int ref_local_enumerate_banded_batch(int32_t match, int32_t mismatch, int32_t gap, int32_t lower, int32_t upper,
+                                     int32_t cutoff, int64_t n_pairs, const uint8_t * seq_h, const int64_t * off_h,
+                                     const uint8_t * seq_v, const int64_t * off_v, int32_t max_count, int32_t * count,
+                                     int32_t threads)
+{
+    const int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<int32_t> scores(size_t(max_count > 0 ? max_count : 1)), pos(size_t(4 * (max_count > 0 ? max_count : 1)));
+        std::vector<char> rows;
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t k = 0; k < n_pairs; ++k)
+        {
+            const int64_t m = off_h[k + 1] - off_h[k], n = off_v[k + 1] - off_v[k];
+            rows.resize(size_t(max_count) * size_t(2 * (m + n + 2)) + 8);
+            count[k] = ref_local_enumerate_banded(0, 0, match, mismatch, gap, lower, upper, cutoff, seq_h + off_h[k], m,
+                                                  seq_v + off_v[k], n, max_count, scores.data(), pos.data(),
+                                                  rows.data(), int64_t(rows.size()));
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"
