@@ -607,8 +607,9 @@ typedef struct {
     /* BamAlignmentRecord.tags: each record's tags in BAM form (two name characters, a type
      * character, the value), back to back; NULL tags_off: no record has tags.  SAM writes them as
      * NAME:TYPE:VALUE separated by tabs (c, s, i, C, S, I as 'i'; Z and H up to their NUL; B arrays
-     * as the element type and ","-prefixed values); float values (f, B:f) and malformed tags are
-     * GBA_EUNSUPPORTED / GBA_EINVAL there.  BAM appends the bytes as they are. */
+     * as the element type and ","-prefixed values; float values (f, B:f) as printf "%g" of the
+     * value, as the reference's appendNumber(float) writes them); malformed tags are GBA_EINVAL
+     * there.  BAM appends the bytes as they are. */
     const char *tags;
     const int64_t *tags_off;                   /* num + 1, or NULL */
 } gba_sam_records;

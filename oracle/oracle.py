@@ -736,12 +736,23 @@ def ref_local_enumerate(h, v, match=2, mismatch=-1, gap=-2, cutoff=0, blosum62=F
 # SAM lines (bam_io/write_sam.h:126-217) of BamAlignmentRecord fields given as plain lists.
 # ---------------------------------------------------------------------------------------------
 
-_TAG_FMT = {"c": ("<b", 1), "C": ("<B", 1), "s": ("<h", 2), "S": ("<H", 2), "i": ("<i", 4), "I": ("<I", 4)}
+_TAG_FMT = {"c": ("<b", 1), "C": ("<B", 1), "s": ("<h", 2), "S": ("<H", 2), "i": ("<i", 4), "I": ("<I", 4),
+            "f": ("<f", 4)}
+
+
+def _tag_str(x, ty):
+    """A tag number as the reference appends it: integers in decimal, floats as C's "%g" of the
+    value (basic/basic_stream.h:1145-1155; a negative NaN prints as "-nan")."""
+    if ty != "f":
+        return str(x)
+    import math
+    if math.isnan(x):
+        return "-nan" if math.copysign(1.0, x) < 0 else "nan"
+    return "%g" % x
 
 
 def tags_bam_to_sam(t: bytes) -> str:
-    """appendTagsBamToSam (bam_io/bam_sam_conversion.h:250-360) of one record's BAM tag bytes (no
-    float values)."""
+    """appendTagsBamToSam (bam_io/bam_sam_conversion.h:250-360) of one record's BAM tag bytes."""
     import struct
     out, i = [], 0
     while i < len(t):
@@ -759,13 +770,13 @@ def tags_bam_to_sam(t: bytes) -> str:
             fmt, sz = _TAG_FMT[et]
             vals = [struct.unpack_from(fmt, t, i + q * sz)[0] for q in range(cnt)]
             i += cnt * sz
-            val = et + "".join("," + str(x) for x in vals)
+            val = et + "".join("," + _tag_str(x, et) for x in vals)
         elif ty == "A":
             val = chr(t[i])
             i += 1
         else:
             fmt, sz = _TAG_FMT[ty]
-            val = str(struct.unpack_from(fmt, t, i)[0])
+            val = _tag_str(struct.unpack_from(fmt, t, i)[0], ty)
             i += sz
         out.append(f"{name}:{shown}:{val}")
     return "\t".join(out)

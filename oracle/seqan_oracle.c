@@ -29,6 +29,7 @@
 
 #include <limits.h>
 #include <stdlib.h>
+#include <stdio.h>
 #include <string.h>
 #include <omp.h>
 
@@ -1199,8 +1200,8 @@ static int sam_num(char *p, int64_t v)
  * the two name characters, ':', the type ('c', 's', 'i', 'C', 'S', 'I' all written as 'i'), ':'
  * and the value -- Z and H strings up to their NUL, B arrays as the element type and ","-prefixed
  * values, numbers in decimal, A as the character; tags separated by tabs.  p == NULL only counts.
- * Returns -1 for bytes that are not well-formed tags and for float values (f, B:f), which this
- * restatement does not format. */
+ * Float values (f, B:f) as the reference's appendNumber(float) prints them: snprintf "%g" of the
+ * value (basic/basic_stream.h:1145-1155).  Returns -1 for bytes that are not well-formed tags. */
 static int64_t tag_size(char t)
 {
     switch (t) {
@@ -1223,6 +1224,19 @@ static int64_t tag_num(const char *q, char t)
     case 'i': return (int32_t)v;
     default: return v;   /* 'I' */
     }
+}
+
+static int64_t tag_float(char *p, const char *q)
+{
+    const unsigned char *u = (const unsigned char *)q;
+    const uint32_t v = (uint32_t)u[0] | ((uint32_t)u[1] << 8) | ((uint32_t)u[2] << 16) | ((uint32_t)u[3] << 24);
+    float f;
+    char buf[32];
+    int n;
+    memcpy(&f, &v, 4);
+    n = snprintf(buf, sizeof(buf), "%g", (double)f);
+    if (p) memcpy(p, buf, (size_t)n);
+    return n;
 }
 
 static int64_t sam_tags(char *p, const char *t, int64_t len)
@@ -1251,20 +1265,22 @@ static int64_t sam_tags(char *p, const char *t, int64_t len)
             if (i + 5 > len) return -1;
             et = t[i];
             sz = tag_size(et);
-            if (sz == 0 || et == 'f' || et == 'A') return -1;
+            if (sz == 0 || et == 'A') return -1;
             TPUT(et);
             cnt = (uint32_t)tag_num(t + i + 1, 'I');
             i += 5;
             if ((int64_t)cnt * sz > len - i) return -1;
             for (e = 0; e < cnt; ++e) {
                 TPUT(',');
-                w += sam_num(p ? p + w : NULL, tag_num(t + i, et));
+                if (et == 'f') w += tag_float(p ? p + w : NULL, t + i);
+                else w += sam_num(p ? p + w : NULL, tag_num(t + i, et));
                 i += sz;
             }
         } else {
             const int64_t sz = tag_size(ty);
-            if (sz == 0 || ty == 'f' || i + sz > len) return -1;
+            if (sz == 0 || i + sz > len) return -1;
             if (ty == 'A') TPUT(t[i]);
+            else if (ty == 'f') w += tag_float(p ? p + w : NULL, t + i);
             else w += sam_num(p ? p + w : NULL, tag_num(t + i, ty));
             i += sz;
         }

@@ -98,10 +98,10 @@ int enumerate_impl(gba_context *ctx, const gba_enum_params *params, const int32_
         d.v_off = v0;
         d.m = int32_t(m);
         d.n = int32_t(n);
-        // banded: the fill pushes each cell once, a declump at most each cell again; the first
-        // launch gives room for one declump's pushes, a pair that needs more is rerun with the
-        // bound of max_count pushes per cell
-        d.heap_cap = band ? 2 * cells + 16 : m * n;
+        // banded: the fill pushes each cell once, a declump at most each cell again, so
+        // max_count pushes per cell bound the heap; the first launch gives room for up to 16 per
+        // cell, and a pair that needs more (max_count > 16) is rerun with the bound
+        d.heap_cap = band ? int64_t(K < 16 ? K : 16) * cells + 16 : m * n;
         cells_of[k] = cells;
         need[k] = size_t(cells) * 5 + size_t(d.heap_cap) * 8 + size_t(2 * (m + n + 5)) * 4 +
                   size_t(K) * size_t(m + n + 1) * 16 + 64;
@@ -178,10 +178,12 @@ int enumerate_impl(gba_context *ctx, const gba_enum_params *params, const int32_
         a.max_count = K;
         GBA_CUDA(ctx, cudaMemsetAsync(a.seg_count, 0, size_t(na) * 4, st));
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+        // one warp per block: a thread's enumeration is a chain of dependent loads, so the pairs
+        // are spread over every SM (and its L1) rather than packed into few blocks
         if (band)
-            k_waterman_eggert_banded<<<unsigned((nc + 127) / 128), 128, 0, st>>>(a, band[0], band[1]);
+            k_waterman_eggert_banded<<<unsigned((nc + 31) / 32), 32, 0, st>>>(a, band[0], band[1]);
         else
-            k_waterman_eggert<<<unsigned((nc + 127) / 128), 128, 0, st>>>(a);
+            k_waterman_eggert<<<unsigned((nc + 31) / 32), 32, 0, st>>>(a);
         GBA_CUDA(ctx, cudaGetLastError());
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
         ++launches;

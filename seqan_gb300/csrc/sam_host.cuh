@@ -81,7 +81,128 @@ __host__ __device__ __forceinline__ int64_t tag_value(const char *q, char t)
     }
 }
 
-// 0 when t[0, len) are tags the SAM writer formats here; 1 malformed; 2 a float value.
+// A float tag value as C's printf "%g" prints the value (the reference's appendNumber(float),
+// basic/basic_stream.h:1145-1155): six significant digits, correctly rounded with ties to even,
+// %e style when the decimal exponent is below -4 or at least 6, trailing zeros removed; "inf",
+// "nan" with the sign.  The value M * 2^E is written exactly as D * 10^-k (D = M * 5^k for
+// E = -k < 0, D = M * 2^E otherwise) in 32-bit limbs, D's decimal digits are produced by
+// division by 10^9, and the rounding works on those digits.  w == nullptr only counts.
+__host__ __device__ inline int tag_float_text(uint32_t bits, char *w)
+{
+    int n = 0;
+    auto put = [&](char c) {
+        if (w) w[n] = c;
+        ++n;
+    };
+    const uint32_t ex = (bits >> 23) & 0xffu, fr = bits & 0x7fffffu;
+    if (bits >> 31) put('-');
+    if (ex == 255) {
+        const char *t = fr ? "nan" : "inf";
+        for (int i = 0; i < 3; ++i) put(t[i]);
+        return n;
+    }
+    const uint32_t M = ex ? (fr | 0x800000u) : fr;
+    const int E = ex ? int(ex) - 150 : -149;
+    if (M == 0) {
+        put('0');
+        return n;
+    }
+    uint32_t D[13];   // M * 5^149 < 2^370
+    int nl = 1, k = 0;
+    D[0] = M;
+    auto mul = [&](uint32_t f) {
+        uint64_t c = 0;
+        for (int i = 0; i < nl; ++i) {
+            const uint64_t t = uint64_t(D[i]) * f + c;
+            D[i] = uint32_t(t);
+            c = t >> 32;
+        }
+        if (c) D[nl++] = uint32_t(c);
+    };
+    if (E >= 0) {
+        for (int e = E; e > 0; e -= 16) mul(1u << (e < 16 ? e : 16));
+    } else {
+        k = -E;
+        for (int e = k; e > 0; e -= 13) {
+            uint32_t f = 1;
+            for (int i = 0; i < (e < 13 ? e : 13); ++i) f *= 5u;
+            mul(f);
+        }
+    }
+    // decimal digits of D, most significant first
+    char dig[120];
+    int nd = 0;
+    {
+        char rev[126];
+        int nr = 0;
+        while (nl > 0) {
+            uint64_t r = 0;
+            for (int i = nl - 1; i >= 0; --i) {
+                const uint64_t t = (r << 32) | D[i];
+                D[i] = uint32_t(t / 1000000000u);
+                r = t % 1000000000u;
+            }
+            while (nl > 0 && D[nl - 1] == 0) --nl;
+            for (int q = 0; q < 9; ++q) {
+                rev[nr++] = char('0' + r % 10);
+                r /= 10;
+            }
+        }
+        while (nr > 1 && rev[nr - 1] == '0') --nr;
+        for (int i = nr - 1; i >= 0; --i) dig[nd++] = rev[i];
+    }
+    int X = nd - k - 1;   // decimal exponent of the first digit
+    char s[6];
+    for (int i = 0; i < 6; ++i) s[i] = i < nd ? dig[i] : '0';
+    if (nd > 6) {
+        bool up;
+        if (dig[6] != '5') {
+            up = dig[6] > '5';
+        } else {
+            bool rest = false;
+            for (int i = 7; i < nd; ++i) rest |= dig[i] != '0';
+            up = rest || ((s[5] - '0') & 1);
+        }
+        if (up) {
+            int i = 5;
+            while (i >= 0 && s[i] == '9') s[i--] = '0';
+            if (i >= 0) {
+                ++s[i];
+            } else {
+                s[0] = '1';
+                ++X;
+            }
+        }
+    }
+    int last = 5;   // last significant digit kept after removing trailing zeros
+    while (last > 0 && s[last] == '0') --last;
+    if (X < -4 || X >= 6) {
+        put(s[0]);
+        if (last > 0) {
+            put('.');
+            for (int i = 1; i <= last; ++i) put(s[i]);
+        }
+        put('e');
+        put(X < 0 ? '-' : '+');
+        const int ax = X < 0 ? -X : X;
+        put(char('0' + ax / 10));
+        put(char('0' + ax % 10));
+    } else if (X >= 0) {
+        for (int i = 0; i <= X; ++i) put(s[i]);
+        if (last > X) {
+            put('.');
+            for (int i = X + 1; i <= last; ++i) put(s[i]);
+        }
+    } else {
+        put('0');
+        put('.');
+        for (int i = 0; i < -X - 1; ++i) put('0');
+        for (int i = 0; i <= last; ++i) put(s[i]);
+    }
+    return n;
+}
+
+// 0 when t[0, len) are tags the SAM writer formats here; 1 malformed.
 inline int tags_check(const char *t, int64_t len)
 {
     int64_t i = 0;
@@ -97,7 +218,6 @@ inline int tags_check(const char *t, int64_t len)
             if (i + 5 > len) return 1;
             const char et = t[i];
             const int sz = tag_size(et);
-            if (et == 'f') return 2;
             if (sz == 0 || et == 'A') return 1;
             const int64_t cnt = tag_value(t + i + 1, 'I');
             i += 5;
@@ -105,7 +225,6 @@ inline int tags_check(const char *t, int64_t len)
             i += cnt * sz;
         } else {
             const int sz = tag_size(ty);
-            if (ty == 'f') return 2;
             if (sz == 0 || i + sz > len) return 1;
             i += sz;
         }
@@ -145,12 +264,16 @@ __device__ int64_t sam_tags_text(const char *t, int64_t len, char *w)
             i += 5;
             for (int64_t e = 0; e < cnt; ++e) {
                 put(',');
-                num(tag_value(t + i, et));
+                if (et == 'f') n += tag_float_text(uint32_t(tag_value(t + i, 'I')), w ? w + n : nullptr);
+                else num(tag_value(t + i, et));
                 i += sz;
             }
         } else if (ty == 'A') {
             put(t[i]);
             i += 1;
+        } else if (ty == 'f') {
+            n += tag_float_text(uint32_t(tag_value(t + i, 'I')), w ? w + n : nullptr);
+            i += 4;
         } else {
             num(tag_value(t + i, ty));
             i += tag_size(ty);
@@ -479,7 +602,6 @@ GBA_API int gba_format_sam(gba_context *ctx, const gba_sam_records *r, char *out
             if (r->tags_off[k + 1] < r->tags_off[k]) return fail(ctx, GBA_EINVAL, "record %lld: bad tag offsets", (long long)k);
             const int c = r->tags ? tags_check(r->tags + r->tags_off[k], r->tags_off[k + 1] - r->tags_off[k]) : 0;
             if (c == 1) return fail(ctx, GBA_EINVAL, "record %lld: malformed tags", (long long)k);
-            if (c == 2) return fail(ctx, GBA_EUNSUPPORTED, "record %lld: float tag values are not written", (long long)k);
         }
     }
     SamArgs a{};

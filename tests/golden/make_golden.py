@@ -11,6 +11,9 @@ Outputs (all small, committed):
   seed_cases.json       seeds extended by the reference's extendSeed (MatchExtend, UnGappedXDrop,
                         GappedXDrop; seeds/seeds_extension.h) with the gapped extension scores.
   sam_cases.json        BamAlignmentRecord fields and the SAM text the reference's writer makes of them.
+  sam_tag_cases.json, sam_float_tag_cases.json  records with BAM tags (integer, character, string
+                        and array values; the second set with float values of every kind) and the
+                        SAM lines / BAM records the reference's writers make of them.
   packed_cases.json     host words of String<Dna|Dna5|AminoAcid, Packed<>> built by the reference
                         (the bits that hold no value, undefined there, masked to zero).
   extend_cases.json     ungapped seed alignments grown by the reference's extendAlignment
@@ -339,16 +342,36 @@ def random_tags(rng, floats=False):
             alphabet = b"0123456789ABCDEF" if kd == "H" else bytes(range(33, 127))
             out += name + kd.encode() + bytes(alphabet[int(x)] for x in rng.integers(0, len(alphabet), ln)) + b"\0"
         elif kd == "f":
-            out += name + b"f" + struct.pack("<f", float(rng.normal()))
+            out += name + b"f" + random_float_bytes(rng)
         else:
             et = "f" if kd == "Bf" else "cCsSiI"[int(rng.integers(0, 6))]
             cnt = int(rng.integers(0, 6))
             fmt = {"c": "<b", "C": "<B", "s": "<h", "S": "<H", "i": "<i", "I": "<I", "f": "<f"}[et]
             lim = {"c": 127, "C": 255, "s": 32767, "S": 65535, "i": 2 ** 31 - 1, "I": 2 ** 32 - 1, "f": 1}[et]
-            vals = [float(rng.normal()) if et == "f" else int(rng.integers(0 if et.isupper() else -lim, lim))
-                    for _ in range(cnt)]
-            out += name + b"B" + et.encode() + struct.pack("<I", cnt) + b"".join(struct.pack(fmt, x) for x in vals)
+            if et == "f":
+                body = b"".join(random_float_bytes(rng) for _ in range(cnt))
+            else:
+                body = b"".join(struct.pack(fmt, int(rng.integers(0 if et.isupper() else -lim, lim)))
+                                for _ in range(cnt))
+            out += name + b"B" + et.encode() + struct.pack("<I", cnt) + body
     return out
+
+
+def random_float_bytes(rng):
+    """A little-endian float32 for a tag: normal values, any bit pattern (denormals, infinities,
+    NaNs of either sign), halves and decimal powers whose %g rounding ties."""
+    import struct
+    r = int(rng.integers(0, 4))
+    if r == 0:
+        return struct.pack("<f", float(rng.normal()) * 10.0 ** int(rng.integers(-8, 9)))
+    if r == 1:
+        if rng.random() < 0.3:   # infinities, NaNs of both signs, -0, the smallest denormal, the largest float
+            return struct.pack("<I", [0x7f800000, 0xff800000, 0x7fc00000, 0xffc00000, 0x80000000, 1,
+                                      0x7f7fffff][int(rng.integers(0, 7))])
+        return struct.pack("<I", int(rng.integers(0, 2 ** 32)))
+    if r == 2:
+        return struct.pack("<f", int(rng.integers(-4_000_000, 4_000_000)) * 0.5)
+    return struct.pack("<f", min(float(10.0 ** int(rng.integers(-40, 38))) * int(rng.integers(1, 20)), 3.0e38))
 
 
 def write_tag_cases():
@@ -369,6 +392,20 @@ def write_tag_cases():
                    "tags": [base64.b64encode(t).decode() for t in rec.tags], "text": text,
                    "bam": base64.b64encode(data).decode()}, f, separators=(",", ":"))
     print(f"{len(rec.qname)} SAM/BAM records with tags written")
+    rng = np.random.Generator(np.random.PCG64(20261213))
+    rec = sam_records(rng, 300)
+    rec.tags = [random_tags(rng, floats=True) for _ in rec.qname]
+    text = O.ref_write_sam(rec)
+    data = O.ref_write_bam(rec)
+    with open(os.path.join(HERE, "sam_float_tag_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only tags", "seed": 20261213, "contigs": rec.contigs,
+                   "qname": rec.qname, "flag": rec.flag.tolist(), "ref_id": rec.ref_id.tolist(),
+                   "pos": rec.pos.tolist(), "mapq": rec.mapq.tolist(), "cigar": [list(map(int, c)) for c in rec.cigar],
+                   "next_ref_id": rec.next_ref_id.tolist(), "next_pos": rec.next_pos.tolist(),
+                   "tlen": rec.tlen.tolist(), "seq": [s.tolist() for s in rec.seq], "qual": rec.qual,
+                   "tags": [base64.b64encode(t).decode() for t in rec.tags], "text": text,
+                   "bam": base64.b64encode(data).decode()}, f, separators=(",", ":"))
+    print(f"{len(rec.qname)} SAM/BAM records with float tags written")
 
 
 def write_packed():
