@@ -12,6 +12,7 @@ raises ParseError / UnexpectedEnd.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -115,3 +116,126 @@ def readRecords(ids: list, seqs: list, *args, fmt: str = "fasta", alphabet: str 
     if quals is not None:
         quals.extend(rec.quals_list)
     return rec
+
+
+# --- SeqFileIn: format and compression guessing --------------------------------------------------
+# The reference's FormattedFile<Fastq, Input> opens a file through a VirtualStream that recognises
+# a compressed stream by its magic bytes (stream/stream_base.h:99-148: gzip 1f 8b 08, bzip2 "BZh";
+# BGZF is gzip members with an extra field), then picks the record format from the file name with
+# the compression extension removed (stream/formatted_file.h:700-730, guessFormatFromFilename) and
+# raises UnknownExtensionError when no format claims the extension; a pipe or an open stream is
+# recognised by the first character instead (guessFormat, MagicHeader: '>' FASTA, '@' FASTQ;
+# seq_io/fasta_fastq.h:79-132).  Decompression runs on the host (Python's zlib / bz2 modules, as the
+# reference's streams call zlib / libbz2); the records are then read as read_records reads them.
+
+FASTA_EXTENSIONS = (".fa", ".fasta", ".faa", ".ffn", ".fna", ".frn", ".fas")
+FASTQ_EXTENSIONS = (".fq", ".fastq")
+COMPRESSION_EXTENSIONS = {"gzip": (".gz",), "bgzf": (".bgzf", ".bam", ".vcf.gz", ".bed.gz", ".tbi"),
+                          "bzip2": (".bz2",)}
+
+
+class UnknownFileFormat(ValueError):
+    """No record format claims the file name's extension, or the text's first character."""
+
+
+def guess_compression(data: bytes) -> str | None:
+    """'bgzf', 'gzip', 'bzip2' or None from the stream's first bytes."""
+    if data[:3] == b"\x1f\x8b\x08":
+        # BGZF: FEXTRA set with the "BC" subfield first (SAM/BAM specification, section 4.1)
+        if len(data) >= 18 and data[3] & 4 and data[12:14] == b"BC":
+            return "bgzf"
+        return "gzip"
+    if data[:3] == b"BZh":
+        return "bzip2"
+    return None
+
+
+def guess_format_from_filename(name: str, compression: str | None = None) -> str | None:
+    """'fasta' / 'fastq' from a file name whose compression extension (of the detected
+    compression) is removed first; None when no format claims the extension."""
+    low = name.lower()
+    if compression is not None:
+        exts = COMPRESSION_EXTENSIONS["gzip"] + COMPRESSION_EXTENSIONS["bgzf"] if compression in ("gzip", "bgzf") \
+            else COMPRESSION_EXTENSIONS[compression]
+        for ext in sorted(exts, key=len, reverse=True):
+            if low.endswith(ext):
+                low = low[:-len(ext)]
+                break
+    if low.endswith(FASTA_EXTENSIONS):
+        return "fasta"
+    if low.endswith(FASTQ_EXTENSIONS):
+        return "fastq"
+    return None
+
+
+def guess_format(text: bytes) -> str | None:
+    """'fasta' / 'fastq' from the first character of the (uncompressed) text."""
+    if text[:1] == b">":
+        return "fasta"
+    if text[:1] == b"@":
+        return "fastq"
+    return None
+
+
+def decompress(data: bytes, compression: str | None) -> bytes:
+    if compression in ("gzip", "bgzf"):
+        import gzip
+        return gzip.decompress(data)   # every member, as BGZF files hold many
+    if compression == "bzip2":
+        import bz2
+        return bz2.decompress(data)
+    return data
+
+
+class SeqFileIn:
+    """SeqFileIn(fileName) / SeqFileIn(stream): a FASTA or FASTQ file, plain, gzip, BGZF or bzip2
+    compressed, read into the engine's record layout (FASTA on the device, FASTQ on the host)."""
+
+    def __init__(self, source, alphabet: str = "dna5", ctx: N.Context | None = None):
+        if isinstance(source, (str, os.PathLike)):
+            with open(source, "rb") as f:
+                raw = f.read()
+            self.compression = guess_compression(raw)
+            self.format = guess_format_from_filename(str(source), self.compression)
+            if self.format is None:
+                raise UnknownFileFormat(f"unknown file extension of {source!r}")
+            self.text = decompress(raw, self.compression)
+        else:
+            raw = source.read() if hasattr(source, "read") else bytes(source)
+            self.compression = guess_compression(raw)
+            self.text = decompress(raw, self.compression)
+            self.format = guess_format(self.text)
+            if self.format is None:
+                raise UnknownFileFormat("the stream starts with neither '>' nor '@'")
+        self.alphabet, self.ctx = alphabet, ctx
+        self._records = None
+        self._next = 0
+
+    def records(self) -> SeqRecords:
+        if self._records is None:
+            self._records = read_records(self.text, self.format, self.alphabet, self.ctx)
+        return self._records
+
+    def atEnd(self) -> bool:
+        return self._next >= len(self.records())
+
+    def readRecord(self):
+        """(id, codes, qual) of the next record (qual b"" for FASTA)."""
+        rec = self.records()
+        if self._next >= len(rec):
+            raise EOFError("no record left")
+        k = self._next
+        self._next += 1
+        return rec.id(k), rec.seq(k), rec.qual(k) if self.format == "fastq" else b""
+
+    def readRecords(self, ids: list, seqs: list, quals: list | None = None, max_records: int | None = None):
+        """Appends up to max_records (all by default) of the remaining records."""
+        rec = self.records()
+        end = len(rec) if max_records is None else min(len(rec), self._next + max_records)
+        for k in range(self._next, end):
+            ids.append(rec.id(k))
+            seqs.append(rec.seq(k))
+            if quals is not None:
+                quals.append(rec.qual(k) if self.format == "fastq" else b"")
+        self._next = end
+        return end
