@@ -178,12 +178,24 @@ int enumerate_impl(gba_context *ctx, const gba_enum_params *params, const int32_
         a.max_count = K;
         GBA_CUDA(ctx, cudaMemsetAsync(a.seg_count, 0, size_t(na) * 4, st));
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-        // one warp per block: a thread's enumeration is a chain of dependent loads, so the pairs
-        // are spread over every SM (and its L1) rather than packed into few blocks
-        if (band)
-            k_waterman_eggert_banded<<<unsigned((nc + 31) / 32), 32, 0, st>>>(a, band[0], band[1]);
-        else
-            k_waterman_eggert<<<unsigned((nc + 31) / 32), 32, 0, st>>>(a);
+        {
+            // Each pair is one thread's sequential enumeration whose heap and declump steps take
+            // data-dependent branches, so the lanes of a warp diverge and run one after another.
+            // A warp therefore takes few pairs -- the smallest power of two that still fits
+            // the batch into the resident warps (measured on 10,000 pairs of 100-200 bp: 2 pairs
+            // per warp 2.4x faster than 32, 4 per warp 2.0x) -- and blocks are one warp each.
+            // "Fits" allows two warps per resident warp slot.
+            const void *fn = band ? reinterpret_cast<const void *>(&k_waterman_eggert_banded)
+                                  : reinterpret_cast<const void *>(&k_waterman_eggert);
+            const int64_t resident = persistent_grid(ctx, fn) * (kBlock / 32);
+            a.lanes = 2;
+            while (a.lanes < 32 && 2 * int64_t(a.lanes) * resident < nc) a.lanes *= 2;
+            const int64_t warps = (nc + a.lanes - 1) / a.lanes;
+            if (band)
+                k_waterman_eggert_banded<<<unsigned(warps), 32, 0, st>>>(a, band[0], band[1]);
+            else
+                k_waterman_eggert<<<unsigned(warps), 32, 0, st>>>(a);
+        }
         GBA_CUDA(ctx, cudaGetLastError());
         GBA_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
         ++launches;

@@ -47,7 +47,18 @@ struct EnumArgs {
     const int32_t *matrix;
     int32_t alphabet;
     int32_t match, mismatch, gap, cutoff, max_count;
+    int32_t lanes;         // pairs per warp (lanes 0 .. lanes - 1 of each warp take one pair each)
 };
+
+// The pair of this thread, or -1: warp w takes pairs w * lanes .. w * lanes + lanes - 1.
+__device__ __forceinline__ int64_t enum_pair_of_thread(const EnumArgs &a)
+{
+    const int lane = int(threadIdx.x & 31u);
+    const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (lane >= a.lanes) return -1;
+    const int64_t p = warp * a.lanes + lane;
+    return p < a.num_pairs ? p : -1;
+}
 
 struct WeState {
     const EnumArgs *a;
@@ -292,8 +303,8 @@ __device__ __forceinline__ uint32_t we_type(int32_t sh, int32_t sv)
 
 __global__ void __launch_bounds__(128) k_waterman_eggert(EnumArgs a)
 {
-    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (p >= a.num_pairs) return;
+    const int64_t p = enum_pair_of_thread(a);
+    if (p < 0) return;
     const EnumPair d = a.pairs[p];
     WeState w;
     w.a = &a;
@@ -676,8 +687,8 @@ struct WbState {
 // needs more than heap_cap entries (the host reruns the pair with the exact bound).
 __global__ void __launch_bounds__(128) k_waterman_eggert_banded(EnumArgs a, int32_t lower, int32_t upper)
 {
-    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (p >= a.num_pairs) return;
+    const int64_t p = enum_pair_of_thread(a);
+    if (p < 0) return;
     const EnumPair d = a.pairs[p];
     WbState w;
     w.a = &a;
