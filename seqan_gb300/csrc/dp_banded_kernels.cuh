@@ -343,9 +343,12 @@ struct BandedPair {
                     // Upper: diagonal or horizontal.
                     if (AFFINE) {
                         const int eExt = hE + EXT, eOpn = hS + OPEN;
-                        e = max(eExt, eOpn);
-                        s = max(inter, e);
-                        tv = (eExt < eOpn ? 4u : 0u) | (inter < e ? 3u : 1u);
+                        // DPX max with its comparison as a predicate: pe = eExt >= eOpn (the
+                        // extension wins ties), pd = inter >= e (the diagonal wins ties)
+                        bool pe, pd;
+                        e = __vibmax_s32(eExt, eOpn, &pe);
+                        s = __vibmax_s32(inter, e, &pd);
+                        tv = (pe ? 0u : 4u) | (pd ? 1u : 3u);
                         vF = INF;
                     } else {
                         const int gh = hS + EXT;
@@ -357,19 +360,30 @@ struct BandedPair {
                     // All directions.
                     if (AFFINE) {
                         const int eExt = hE + EXT, eOpn = hS + OPEN;
-                        e = max(eExt, eOpn);
                         const int fExt = vF + EXT, fOpn = vS + OPEN;
-                        f = max(fExt, fOpn);
-                        s = __vimax3_s32(inter, e, f);
                         if (TRACE) {
-                            tv = (eExt < eOpn ? 4u : 0u) | (fExt < fOpn ? 8u : 0u);
-                            tv |= s == inter ? 1u : (f < e ? 3u : 2u);
+                            // pe / pf: the extension wins; pfe: f >= e (vertical over
+                            // horizontal); pd: inter >= max(e, f), i.e. s == inter
+                            bool pe, pf, pfe, pd;
+                            e = __vibmax_s32(eExt, eOpn, &pe);
+                            f = __vibmax_s32(fExt, fOpn, &pf);
+                            s = __vibmax_s32(inter, __vibmax_s32(f, e, &pfe), &pd);
+                            tv = (pe ? 0u : 4u) | (pf ? 0u : 8u) | (pd ? 1u : (pfe ? 2u : 3u));
+                        } else {
+                            e = max(eExt, eOpn);
+                            f = max(fExt, fOpn);
+                            s = __vimax3_s32(inter, e, f);
                         }
                         vF = f;
                     } else {
                         const int gv = vS + EXT, gh = hS + EXT;
-                        s = __vimax3_s32(inter, gv, gh);
-                        if (TRACE) tv = s == inter ? 1u : (gv < gh ? 3u : 2u);
+                        if (TRACE) {
+                            bool pvh, pd;
+                            s = __vibmax_s32(inter, __vibmax_s32(gv, gh, &pvh), &pd);
+                            tv = pd ? 1u : (pvh ? 2u : 3u);
+                        } else {
+                            s = __vimax3_s32(inter, gv, gh);
+                        }
                         e = hE;
                     }
                 }
@@ -395,13 +409,15 @@ struct BandedPair {
                 uint32_t tv;
                 if (AFFINE) {
                     const int fExt = vF + EXT, fOpn = vS + OPEN;
-                    f = max(fExt, fOpn);
-                    s = max(inter, f);
-                    tv = (fExt < fOpn ? 8u : 0u) | (inter < f ? 2u : 1u);
+                    bool pf, pd;
+                    f = __vibmax_s32(fExt, fOpn, &pf);
+                    s = __vibmax_s32(inter, f, &pd);
+                    tv = (pf ? 0u : 8u) | (pd ? 1u : 2u);
                 } else {
                     const int gv = vS + EXT;
-                    s = max(inter, gv);
-                    tv = inter < gv ? 2u : 1u;
+                    bool pd;
+                    s = __vibmax_s32(inter, gv, &pd);
+                    tv = pd ? 1u : 2u;
                 }
                 if (LOCAL && s <= 0) {
                     s = 0;
