@@ -998,7 +998,7 @@ def ref_read_records(text: bytes, fmt: str, alphabet: str = "dna5"):
     cap = 3 * len(text) + 64
     out = C.create_string_buffer(cap)
     nrec = C.c_int64()
-    r = lib.ref_read_records(C.c_int32(1 if fmt == "fastq" else 0), C.c_int32(SEQIO_ALPHABETS[alphabet]),
+    r = lib.ref_read_records(C.c_int32({"fasta": 0, "fastq": 1, "raw": 2}[fmt]), C.c_int32(SEQIO_ALPHABETS[alphabet]),
                              C.c_char_p(text), C.c_int64(len(text)), out, C.c_int64(cap), C.byref(nrec))
     if r == -1:
         raise SeqParseError("parse", None)

@@ -26,6 +26,7 @@ int64_t read_all(int32_t format, const char * text, int64_t n, char * out, int64
     try {
         while (!atEnd(iter)) {
             if (format == 1) readRecord(id, seq, qual, iter, Fastq());
+            else if (format == 2) readRecord(id, seq, qual, iter, Raw());
             else readRecord(id, seq, qual, iter, Fasta());
             put_u32(buf, uint32_t(length(id)));
             buf.append(toCString(id), length(id));

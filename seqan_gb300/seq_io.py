@@ -97,6 +97,42 @@ def read_records(text: bytes, fmt: str = "fasta", alphabet: str = "dna5", ctx: N
     return SeqRecords(text, ib[:k], ie[:k], so[:k + 1], qe[:k], codes[:r.residues], quals[:r.residues])
 
 
+def read_raw(text: bytes, alphabet: str = "dna5", ctx: N.Context | None = None) -> SeqRecords:
+    """Every line of ``text`` as one record with an empty id, as the reference's readRecord(Raw)
+    reads them (seq_io/fasta_fastq.h:235-261: the residues up to the line end with FASTA's ignore
+    / assert rule, then skipLine: "\r\n", "\r" and "\n" end a line).  The lines are framed as
+    FASTA records (">" + newline before each) and read by the device FASTA reader.  A '>' starts a
+    record anywhere in FASTA but is a residue that fails the assert in Raw, so it is handed to the
+    reader as '!', which no alphabet holds; error offsets refer to ``text``."""
+    import re
+    text = bytes(text)
+    starts, ends = [], []
+    pos = 0
+    for mt in re.finditer(rb"\r\n|\r|\n", text):
+        starts.append(pos)
+        ends.append(mt.start())
+        pos = mt.end()
+    if pos < len(text):
+        starts.append(pos)
+        ends.append(len(text))
+    parts, conv_starts = [], []
+    q = 0
+    for a, b in zip(starts, ends):
+        line = text[a:b].replace(b">", b"!")
+        parts.append(b">\n" + line + b"\n")
+        conv_starts.append(q + 2)
+        q += len(line) + 3
+    fasta = b"".join(parts)
+    try:
+        rec = read_records(fasta, "fasta", alphabet, ctx)
+    except SeqParseError as e:
+        i = max(0, int(np.searchsorted(np.asarray(conv_starts, np.int64), e.offset, side="right")) - 1)
+        off = starts[i] + (e.offset - conv_starts[i]) if starts else 0
+        raise SeqParseError(f"raw text not in the format at offset {off}", off) from None
+    return SeqRecords(text, np.zeros(len(rec), np.int64), np.zeros(len(rec), np.int64), rec.seq_off, rec.qual_end,
+                      rec.codes, rec.quals)
+
+
 def read_fasta(text: bytes, alphabet: str = "dna5", ctx: N.Context | None = None) -> SeqRecords:
     return read_records(text, "fasta", alphabet, ctx)
 
@@ -124,12 +160,14 @@ def readRecords(ids: list, seqs: list, *args, fmt: str = "fasta", alphabet: str 
 # BGZF is gzip members with an extra field), then picks the record format from the file name with
 # the compression extension removed (stream/formatted_file.h:700-730, guessFormatFromFilename) and
 # raises UnknownExtensionError when no format claims the extension; a pipe or an open stream is
-# recognised by the first character instead (guessFormat, MagicHeader: '>' FASTA, '@' FASTQ;
-# seq_io/fasta_fastq.h:79-132).  Decompression runs on the host (Python's zlib / bz2 modules, as the
+# recognised by its first bytes instead, the formats tried in SeqInFormats order (guessFormat,
+# MagicHeader: '@' FASTQ, '>' FASTA; Raw has no magic header and takes any other text;
+# seq_io/fasta_fastq.h:79-143, seq_io/sequence_file.h:86-97, stream/stream_base.h:196-230).  Decompression runs on the host (Python's zlib / bz2 modules, as the
 # reference's streams call zlib / libbz2); the records are then read as read_records reads them.
 
 FASTA_EXTENSIONS = (".fa", ".fasta", ".faa", ".ffn", ".fna", ".frn", ".fas")
 FASTQ_EXTENSIONS = (".fq", ".fastq")
+RAW_EXTENSIONS = (".raw",)
 COMPRESSION_EXTENSIONS = {"gzip": (".gz",), "bgzf": (".bgzf", ".bam", ".vcf.gz", ".bed.gz", ".tbi"),
                           "bzip2": (".bz2",)}
 
@@ -165,16 +203,22 @@ def guess_format_from_filename(name: str, compression: str | None = None) -> str
         return "fasta"
     if low.endswith(FASTQ_EXTENSIONS):
         return "fastq"
+    if low.endswith(RAW_EXTENSIONS):
+        return "raw"
     return None
 
 
-def guess_format(text: bytes) -> str | None:
-    """'fasta' / 'fastq' from the first character of the (uncompressed) text."""
-    if text[:1] == b">":
-        return "fasta"
+def guess_format(text: bytes) -> str:
+    """'fastq' / 'fasta' from the first character of the (uncompressed) text, else 'raw'.
+    EMBL ("ID ") and GenBank ("LOCUS ") texts, which the reference recognises before Raw
+    (seq_io/read_embl.h:73, read_genbank.h:82), are refused: their readers are not built."""
     if text[:1] == b"@":
         return "fastq"
-    return None
+    if text[:1] == b">":
+        return "fasta"
+    if text[:3] == b"ID " or text[:6] == b"LOCUS ":
+        raise UnknownFileFormat("EMBL / GenBank input is not supported")
+    return "raw"
 
 
 def decompress(data: bytes, compression: str | None) -> bytes:
@@ -188,8 +232,9 @@ def decompress(data: bytes, compression: str | None) -> bytes:
 
 
 class SeqFileIn:
-    """SeqFileIn(fileName) / SeqFileIn(stream): a FASTA or FASTQ file, plain, gzip, BGZF or bzip2
-    compressed, read into the engine's record layout (FASTA on the device, FASTQ on the host)."""
+    """SeqFileIn(fileName) / SeqFileIn(stream): a FASTA, FASTQ or Raw file, plain, gzip, BGZF or
+    bzip2 compressed, read into the engine's record layout (FASTA and Raw on the device, FASTQ on
+    the host)."""
 
     def __init__(self, source, alphabet: str = "dna5", ctx: N.Context | None = None):
         if isinstance(source, (str, os.PathLike)):
@@ -205,15 +250,16 @@ class SeqFileIn:
             self.compression = guess_compression(raw)
             self.text = decompress(raw, self.compression)
             self.format = guess_format(self.text)
-            if self.format is None:
-                raise UnknownFileFormat("the stream starts with neither '>' nor '@'")
         self.alphabet, self.ctx = alphabet, ctx
         self._records = None
         self._next = 0
 
     def records(self) -> SeqRecords:
         if self._records is None:
-            self._records = read_records(self.text, self.format, self.alphabet, self.ctx)
+            if self.format == "raw":
+                self._records = read_raw(self.text, self.alphabet, self.ctx)
+            else:
+                self._records = read_records(self.text, self.format, self.alphabet, self.ctx)
         return self._records
 
     def atEnd(self) -> bool:

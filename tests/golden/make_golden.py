@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the compiled reference.
 
 Run where the reference tree exists (it builds oracle/_ref/ from its headers):
-    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|waterman_eggert_banded|packed|sam|seqio|bam|cpp|dynamic|banded_chain|tags]
+    python tests/golden/make_golden.py [--only seeds|extend|extend_banded|waterman_eggert|waterman_eggert_banded|raw|packed|sam|seqio|bam|cpp|dynamic|banded_chain|tags]
 Outputs (all small, committed):
   reference_cases.json  seeded inputs with the reference's outputs: batch scores through
                         ExecutionPolicy<Parallel, Vectorial>, batch Gaps rows / clip positions /
@@ -24,6 +24,8 @@ Outputs (all small, committed):
                         LocalAlignmentEnumerator<Score, Unbanded> (scores, rows, positions).
   waterman_eggert_banded_cases.json  the same for LocalAlignmentEnumerator<Score, Banded> with
                         random diagonal bands.
+  seqio_raw_cases.json  Raw texts (one sequence per line; LF, CR LF and CR line ends, empty lines,
+                        blanks, invalid characters) read by the reference's readRecord(Raw).
   dynamic_cases.json    pairs aligned by the reference's single-pair DP with DynamicGaps cells
                         (score and raw TraceSegment_ list) for the shapes oracle/ref/units/dynamic_*.cpp
                         instantiate.
@@ -117,6 +119,9 @@ def main():
         return
     if only == "waterman_eggert_banded":
         write_waterman_eggert_banded(b62)
+        return
+    if only == "raw":
+        write_raw_cases()
         return
     if only == "packed":
         write_packed()
@@ -281,6 +286,7 @@ def main():
     write_extend_banded(b62)
     write_waterman_eggert(b62)
     write_waterman_eggert_banded(b62)
+    write_raw_cases()
     write_packed()
     write_sam_cases()
 
@@ -645,6 +651,47 @@ def write_waterman_eggert_banded(b62):
         json.dump({"generator": "tests/golden/make_golden.py --only waterman_eggert_banded", "seed": 20261212,
                    "cases": cases}, f, separators=(",", ":"))
     print(f"{len(cases)} banded Waterman-Eggert cases written")
+
+
+def write_raw_cases():
+    """Raw texts through the reference's `while (!atEnd(iter)) readRecord(id, seq, qual, iter, Raw())`
+    for the three alphabets: records (empty ids) or the ParseError."""
+    rng = np.random.Generator(np.random.PCG64(20261214))
+    letters = {"dna": b"ACGTacgt", "dna5": b"ACGTNacgtn", "aa": b"ACDEFGHIKLMNPQRSTVWYXacdefghik*"}
+    ends = [b"\n", b"\r\n", b"\r"]
+    cases = []
+    fixed = [b"", b"\n", b"ACGT", b"ACGT\n", b"ACGT\n\n", b"\n\nAC\n", b"AC\rGT\r\nTT\n", b"A C\tG T\n",
+             b">ACGT\n", b"AC>GT\n", b"AC\nG1T\n", b"acgtn\nNNNN", b"AC GT \r\n\r\nGG"]
+    for alph in ("dna5", "dna", "aa"):
+        for t in fixed:
+            cases.append((alph, t))
+        for _ in range(60):
+            lines = []
+            for _ in range(int(rng.integers(0, 8))):
+                ln = bytes(letters[alph][int(x)] for x in rng.integers(0, len(letters[alph]), int(rng.integers(0, 40))))
+                if rng.random() < 0.15:
+                    i = int(rng.integers(0, len(ln) + 1))
+                    ln = ln[:i] + bytes([b" \t"[int(rng.integers(0, 2))]]) + ln[i:]
+                if rng.random() < 0.05:
+                    i = int(rng.integers(0, len(ln) + 1))
+                    ln = ln[:i] + bytes([b"#>1@"[int(rng.integers(0, 4))]]) + ln[i:]
+                lines.append(ln + ends[int(rng.integers(0, 3))])
+            t = b"".join(lines)
+            if t and rng.random() < 0.3:
+                t = t.rstrip(b"\r\n")
+            cases.append((alph, t))
+    out = []
+    for alph, t in cases:
+        try:
+            recs = O.ref_read_records(t, "raw", alph)
+            out.append({"alphabet": alph, "text": t.decode("latin1"), "error": None,
+                        "records": [[r[0].decode("latin1"), r[1].tolist()] for r in recs]})
+        except O.SeqParseError:
+            out.append({"alphabet": alph, "text": t.decode("latin1"), "error": "parse", "records": None})
+    with open(os.path.join(HERE, "seqio_raw_cases.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --only raw", "seed": 20261214, "cases": out}, f,
+                  separators=(",", ":"))
+    print(f"{len(out)} Raw texts written ({sum(c['error'] is not None for c in out)} with a ParseError)")
 
 
 def chain_case(rng, max_len=200, max_seeds=8, max_seed_len=30):

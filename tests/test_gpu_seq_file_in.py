@@ -1,11 +1,14 @@
 """SeqFileIn on the GPU machine: gzip, BGZF and bzip2 FASTA files read through the device FASTA reader
-give the records of the plain text (format from the file name, compression from the magic bytes)."""
+give the records of the plain text (format from the file name, compression from the magic bytes);
+Raw texts (one sequence per line) give the records of the reference's readRecord(Raw)
+(tests/golden/seqio_raw_cases.json)."""
 import bz2
 import gzip
 
 import numpy as np
 import pytest
 
+from tests import golden_cases as G
 from tests.test_seq_file_in import bgzf
 
 pytestmark = pytest.mark.gpu
@@ -28,3 +31,21 @@ def test_fasta_files(engine, tmp_path, comp):
     want = S.read_fasta(text)
     assert ids == want.ids
     assert [s.tolist() for s in seqs] == [s.tolist() for s in want.seqs]
+
+
+def test_raw_texts_match_reference(engine, tmp_path):
+    from seqan_gb300 import seq_io as S
+    cases = G.load("seqio_raw_cases.json")["cases"]
+    for i, c in enumerate(cases):
+        text = c["text"].encode("latin1")
+        p = tmp_path / f"t{i}.raw"
+        p.write_bytes(gzip.compress(text) if i % 3 == 0 else text)
+        f = S.SeqFileIn(str(p), alphabet=c["alphabet"])
+        assert f.format == "raw"
+        if c["error"]:
+            with pytest.raises(S.SeqParseError):
+                f.records()
+            continue
+        ids, seqs = [], []
+        f.readRecords(ids, seqs)
+        assert [[x.decode("latin1"), s.tolist()] for x, s in zip(ids, seqs)] == c["records"], c

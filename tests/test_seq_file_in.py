@@ -40,7 +40,7 @@ def bgzf(data: bytes, block: int = 7) -> bytes:
     ("x.fna", None, "fasta"), ("x.frn", None, "fasta"), ("x.fas", None, "fasta"), ("READS.FQ", None, "fastq"),
     ("reads.fastq", None, "fastq"), ("reads.fq.gz", "gzip", "fastq"), ("reads.fa.gz", "gzip", "fasta"),
     ("reads.fa.bgzf", "bgzf", "fasta"), ("reads.fq.bz2", "bzip2", "fastq"), ("reads.txt", None, None),
-    ("reads.fq.gz", None, None), ("reads.sam", None, None)])
+    ("reads.fq.gz", None, None), ("reads.sam", None, None), ("reads.raw", None, "raw"), ("r.raw.gz", "gzip", "raw")])
 def test_format_from_file_name(name, comp, fmt):
     assert S.guess_format_from_filename(name, comp) == fmt
 
@@ -51,7 +51,11 @@ def test_compression_from_magic_bytes():
     assert S.guess_compression(bz2.compress(FASTQ)) == "bzip2"
     assert S.guess_compression(FASTQ) is None
     assert S.guess_format(FASTQ) == "fastq" and S.guess_format(b">x\nAC\n") == "fasta"
-    assert S.guess_format(b"ACGT") is None
+    # Raw has no magic header: any other text is Raw (EMBL and GenBank come first and are refused)
+    assert S.guess_format(b"ACGT") == "raw" and S.guess_format(b"") == "raw" and S.guess_format(b"IDLE") == "raw"
+    for t in (b"ID   X; SV 1\n", b"LOCUS       X\n"):
+        with pytest.raises(S.UnknownFileFormat):
+            S.guess_format(t)
 
 
 def _recs(f):
@@ -83,8 +87,7 @@ def test_unknown_extension_and_content(tmp_path):
     p.write_bytes(FASTQ)
     with pytest.raises(S.UnknownFileFormat):
         S.SeqFileIn(str(p))
-    with pytest.raises(S.UnknownFileFormat):
-        S.SeqFileIn(b"ACGT\n")
+    assert S.SeqFileIn(b"ACGT\n").format == "raw"
 
 
 def test_records_in_parts(tmp_path):
