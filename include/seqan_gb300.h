@@ -654,9 +654,21 @@ typedef struct {
  * NUL, CIGAR words, Iupac sequence two codes per byte, qualities minus '!' or 0xFF, the tag
  * bytes), formatted on the device; rec_off[num + 1] gets each record's byte offset.  Names of more than 254 characters,
  * more than 65535 CIGAR operations and more qualities than residues are GBA_EINVAL (the core's
- * fields cannot hold them; the reference asserts on the last).  BGZF compression is not done. */
+ * fields cannot hold them; the reference asserts on the last).  gba_bgzf_compress writes the blocks
+ * as a BGZF file. */
 GBA_API int gba_format_bam(gba_context *ctx, const gba_sam_records *records, char *out, int64_t capacity,
                            int64_t *rec_off);
+
+/* BGZF compression of a byte stream (the reference's BgzfFile stream under BamFileOut,
+ * stream/stream_compressor.h:60-130, 325-375): pages of 65,505 input bytes, each one gzip member
+ * with the BGZF header ("BC" extra field = member size - 1), raw deflate data, CRC-32 and input
+ * size, compressed on the device; with eof_marker the 28-byte empty member follows.  The member
+ * partition, headers, CRC-32s and sizes are the reference's; the deflate data is this engine's
+ * (greedy LZ77 with fixed Huffman codes, or a stored block), so each member inflates to the same
+ * page while the compressed bytes differ from zlib's.  *out_len gets the size; GBA_ECAPACITY when
+ * capacity is smaller. */
+GBA_API int gba_bgzf_compress(gba_context *ctx, const uint8_t *data, int64_t length, int32_t eof_marker, uint8_t *out,
+                              int64_t capacity, int64_t *out_len);
 
 GBA_API int gba_read_fasta(gba_context *ctx, const char *text, int64_t length, int32_t alphabet,
                            gba_seq_records *records);

@@ -49,7 +49,7 @@ EXPORTED = ["gba_create", "gba_destroy", "gba_status_string", "gba_last_error", 
             "gba_server_last_error", "gba_server_destroy", "gba_clock_seconds", "gba_server_submit_schedule",
             "gba_extend_seeds", "gba_extend_seeds_device", "gba_extend_alignments", "gba_align_packed",
             "gba_format_sam", "gba_read_fasta", "gba_read_fastq", "gba_format_bam",
-            "gba_align_fasta"]
+            "gba_align_fasta", "gba_bgzf_compress"]
 
 
 class GbaConfig(C.Structure):
@@ -298,6 +298,7 @@ def lib():
                                            C.POINTER(GbaPackedSet), C.c_int32, C.POINTER(GbaResult)]
             L.gba_format_sam.argtypes = [vp, C.POINTER(GbaSamRecords), vp, i64, vp]
             L.gba_format_bam.argtypes = [vp, C.POINTER(GbaSamRecords), vp, i64, vp]
+            L.gba_bgzf_compress.argtypes = [vp, vp, i64, C.c_int32, vp, i64, vp]
             L.gba_align_fasta.argtypes = [vp, C.POINTER(GbaParams), vp, i64, vp, i64, i32, i32, i64,
                                           C.POINTER(i64), C.POINTER(GbaResult)]
             L.gba_read_fasta.argtypes = [vp, vp, i64, i32, C.POINTER(GbaSeqRecords)]

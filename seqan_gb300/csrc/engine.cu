@@ -223,6 +223,7 @@ struct gba_context {
     DevBuf xa_tasks, xa_out, xa_trace, xa_segs, xa_segoff, xa_segcnt, xa_scratch, xa_next, xa_packoff, xa_packed;
     DevBuf en_pairs, en_mat, en_forb, en_heap, en_steps, en_slots, en_out, en_dense, en_offs, en_cnt;   // gba_local_enumerate
     DevBuf bc_seeds, bc_desc, bc_arena, bc_out, bc_dense, bc_offs;   // gba_banded_chain
+    DevBuf bz_in, bz_slots, bz_scratch, bz_meta, bz_out;             // gba_bgzf_compress
     // packed input: the codes are already in seq_h / seq_v (gba_align_packed unpacked them)
     bool device_codes = false;
     DevBuf pk_words, pk_off_h, pk_off_v;
@@ -2179,6 +2180,7 @@ GBA_API int gba_get_stats(gba_context *ctx, gba_stats *stats)
 #include "extend_host.cuh"
 #include "enum_host.cuh"
 #include "chain_host.cuh"
+#include "bgzf_host.cuh"
 #include "packed_host.cuh"
 #include "sam_host.cuh"
 #include "seqio_host.cuh"

@@ -102,6 +102,26 @@ def format_bam(rec: SamRecords, ctx=None) -> bytes:
     return bytes(out[:int(rec_off[-1])])
 
 
+def bgzf_compress(data: bytes, eof_marker: bool = True, ctx=None) -> bytes:
+    """``data`` as a BGZF file, compressed on the device (gba_bgzf_compress): the reference's member
+    partition (65,505 bytes per member), headers, CRC-32s and sizes, this engine's deflate data, and
+    the end-of-file member when eof_marker."""
+    ctx = ctx or N.default_context()
+    buf = np.frombuffer(bytes(data), np.uint8) if len(data) else np.zeros(1, np.uint8)
+    cap = len(data) + 64 * (len(data) // 65505 + 2) + 64
+    out = np.zeros(cap, np.uint8)
+    n = C.c_int64()
+    ctx.check(N.lib().gba_bgzf_compress(ctx.handle, buf.ctypes.data, len(data), 1 if eof_marker else 0, out.ctypes.data,
+                                        cap, C.byref(n)), "gba_bgzf_compress")
+    return bytes(out[:n.value])
+
+
+def write_bam_file(rec: SamRecords, header: bytes = b"", ctx=None) -> bytes:
+    """A BAM file's bytes: the given BAM header bytes (magic, text and reference list, as the
+    reference's writer lays them out) and the records' blocks, BGZF-compressed on the device."""
+    return bgzf_compress(bytes(header) + format_bam(rec, ctx), True, ctx)
+
+
 def format_sam(rec: SamRecords, ctx=None) -> str:
     ctx = ctx or N.default_context()
     n = len(rec.qname)
