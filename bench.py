@@ -88,7 +88,8 @@ WORKLOADS["dynamic_dna_tb_100k"] = ("the 100000 pairs of affine_dna_100k with Dy
                                     "flags per cell; align/dp_formula_dynamic.h), Score(2,-4,-1,-6) int16, global, score + "
                                     "end position + trace segments")
 WORKLOADS["bam_records_1m"] = ("the 1000000 records of sam_records_1m as uncompressed BAM blocks "
-                               "(write(target, record, context, Bam()), no tags, no BGZF)")
+                               "(write(target, record, context, Bam()), no tags); the line's bgzf key times the "
+                               "blocks' BGZF compression")
 BAM_WORKLOADS = {"bam_records_1m"}
 
 
@@ -104,6 +105,8 @@ def run_bam_bench(args, rank, world, local_rank, dist):
     a = O.sam_arrays(rec)
     pinned_bufs = {}
     for key, arr in a.items():
+        if arr is None:   # no tags: the records struct's tag fields stay NULL
+            continue
         p = C.c_void_p()
         ctx.check(L.gba_host_alloc(h, C.byref(p), max(arr.nbytes, 1)), "alloc")
         C.memmove(p, arr.ctypes.data, arr.nbytes)
@@ -139,7 +142,7 @@ def run_bam_bench(args, rank, world, local_rank, dist):
     value = n * world / (kernel_ms * 1e-3) / 1e6
     e2e = n * world * len(wall) / sum(wall) / 1e6
     hbm = measured_hbm_gbs()
-    in_bytes = sum(int(x.nbytes) for x in a.values())
+    in_bytes = sum(int(x.nbytes) for x in a.values() if x is not None)
     line = {"metric": "M BAM records/s, device formatting", "value": value, "unit": "M records/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
@@ -166,10 +169,60 @@ def run_bam_bench(args, rank, world, local_rank, dist):
                                 "sample": f"all {n} records, orc_write_bam (oracle/seqan_oracle.c, the reference's "
                                           f"BAM writer restated) with OpenMP over {threads} threads, best of 2",
                                 "seconds": best}
+    line["bgzf"] = bgzf_measure(ctx, data, args, threads)
     for p in list(pinned_bufs.values()) + [p_out]:
         L.gba_host_free(h, p)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def bgzf_measure(ctx, data: bytes, args, threads: int) -> dict:
+    """The BAM blocks as a BGZF file (gba_bgzf_compress, the BgzfFile stream under BamFileOut):
+    device kernel rate, the whole call from host buffers, the size ratio, whether every member
+    inflates to its page, and zlib level 1 (the reference's deflateInit2(Z_BEST_SPEED) per 65,505-byte
+    page) on the host threads as the CPU side."""
+    import gzip
+    import zlib
+    from concurrent.futures import ThreadPoolExecutor
+    from seqan_gb300 import _native as N
+    L = N.lib()
+    n = len(data)
+    src = np.frombuffer(data, np.uint8)
+    cap = n + 64 * (n // 65505 + 2) + 64
+    out = np.zeros(cap, np.uint8)
+    olen = C.c_int64()
+
+    def call():
+        ctx.check(L.gba_bgzf_compress(ctx.handle, src.ctypes.data, n, 1, out.ctypes.data, cap, C.byref(olen)), "bgzf")
+
+    for _ in range(max(args.warmup, 1)):
+        call()
+    wall, kern = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        call()
+        wall.append(time.perf_counter() - t0)
+        kern.append(ctx.stats().dp_kernel_ms)
+    z = bytes(out[:olen.value])
+    res = {"value": n / (sum(kern) / len(kern) * 1e-3) / 1e9, "unit": "GB/s of BAM bytes", "input_bytes": n,
+           "output_bytes": len(z), "ratio": len(z) / max(n, 1), "e2e_gbs": n * len(wall) / sum(wall) / 1e9,
+           "kernel": "k_bgzf_members (one warp per member) + k_bgzf_pack", "inflates_equal": gzip.decompress(z) == data,
+           "timing": "CUDA events around k_bgzf_members; e2e = the whole call from host buffers"}
+    if not args.no_cpu_baseline:
+        pages = [data[i:i + 65505] for i in range(0, n, 65505)]
+
+        def deflate(page):
+            c = zlib.compressobj(1, zlib.DEFLATED, -15, 8)
+            return c.compress(page) + c.flush()
+
+        with ThreadPoolExecutor(threads) as ex:
+            t0 = time.perf_counter()
+            zs = list(ex.map(deflate, pages))
+            dt = time.perf_counter() - t0
+        res["cpu_zlib_level1"] = {"value": n / dt / 1e9, "unit": "GB/s", "cores": threads,
+                                  "ratio": (sum(len(x) for x in zs) + 26 * len(pages) + 28) / max(n, 1),
+                                  "sample": "every page through zlib level 1 (Python's zlib, threads over pages)"}
+    return res
 
 
 def run_bam_reference(args):
@@ -420,6 +473,8 @@ def run_sam_bench(args, rank, world, local_rank, dist):
     a = O.sam_arrays(rec)
     pinned_bufs = {}
     for key, arr in a.items():
+        if arr is None:   # no tags: the records struct's tag fields stay NULL
+            continue
         p = C.c_void_p()
         ctx.check(L.gba_host_alloc(h, C.byref(p), max(arr.nbytes, 1)), "alloc")
         C.memmove(p, arr.ctypes.data, arr.nbytes)
@@ -458,7 +513,7 @@ def run_sam_bench(args, rank, world, local_rank, dist):
     value = n * world / (kernel_ms * 1e-3) / 1e6
     e2e = n * world * len(wall) / sum(wall) / 1e6
     hbm = measured_hbm_gbs()
-    in_bytes = sum(int(x.nbytes) for x in a.values())
+    in_bytes = sum(int(x.nbytes) for x in a.values() if x is not None)
     line = {"metric": "M SAM records/s, device formatting", "value": value, "unit": "M records/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
