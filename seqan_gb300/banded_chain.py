@@ -87,8 +87,38 @@ def banded_chain_codes(codes_h, codes_v, chains, score_anchor, score_gap=None, c
     ctx = context or N.default_context()
     ctx.check(N.lib().gba_banded_chain(ctx.handle, C.byref(p), C.byref(b), C.byref(sd), C.byref(r)),
               "gba_banded_chain")
-    seg_lists = [[tuple(x) for x in segs[off[k]:off[k + 1]].tolist()] for k in range(n)]
-    return score[:n], status[:n], ntr[:n], seg_lists
+    return score[:n], status[:n], ntr[:n], SegmentLists(segs, off, n)
+
+
+class SegmentLists:
+    """The pairs' TraceSegment_ runs of one call: item k is pair k's list of (h, v, length, type)
+    tuples, built from the call's output arrays when first read."""
+
+    def __init__(self, segs, off, n):
+        self._segs, self._off, self._n = segs, off, n
+        self._cache = {}
+
+    def __len__(self):
+        return self._n
+
+    def __getitem__(self, k):
+        if isinstance(k, slice):
+            return [self[i] for i in range(*k.indices(self._n))]
+        if k < 0:
+            k += self._n
+        if not 0 <= k < self._n:
+            raise IndexError(k)
+        got = self._cache.get(k)
+        if got is None:
+            got = [tuple(x) for x in self._segs[self._off[k]:self._off[k + 1]].tolist()]
+            self._cache[k] = got
+        return got
+
+    def __iter__(self):
+        return (self[k] for k in range(self._n))
+
+    def __eq__(self, other):
+        return list(self) == list(other)
 
 
 def bandedChainAlignment(seqsH, seqsV, chains, scoreAnchor, scoreGap=None, alignConfig: AlignConfig | None = None,
